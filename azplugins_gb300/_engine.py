@@ -1,0 +1,193 @@
+"""Python handle of the resident engine (``azp_md_*`` in the C ABI)."""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .bond import Bond
+from .methods import BrownianFlow, LangevinFlow
+from .pair import Pair
+
+
+def _stream():
+    import torch
+
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def split_forces(integ):
+    pairs = [f for f in integ.forces if isinstance(f, Pair)]
+    bonds = [f for f in integ.forces if isinstance(f, Bond)]
+    other = [f for f in integ.forces if not isinstance(f, (Pair, Bond))]
+    if other:
+        raise NotImplementedError(f"unsupported force objects: {other}")
+    if len(pairs) > 1 or len(bonds) > 1:
+        raise NotImplementedError("the engine advances at most one pair and one bond potential")
+    return (pairs[0] if pairs else None), (bonds[0] if bonds else None)
+
+
+class Engine:
+    """Owns one ``azp_md`` object."""
+
+    @staticmethod
+    def config_key(sim, integ):
+        pair, bond = split_forces(integ)
+        if len(integ.methods) != 1 or not isinstance(integ.methods[0], (LangevinFlow, BrownianFlow)):
+            raise NotImplementedError("exactly one LangevinFlow or BrownianFlow method is required")
+        m = integ.methods[0]
+        parts = [sim.precision, sim.seed, integ.dt, type(m).__name__, m.kT, m.noiseless, m.alpha,
+                 getattr(m, "max_displacement", 0.0), repr(m.flow_field), sorted(m.gamma.items()),
+                 m.gamma.default]
+        if pair is not None:
+            parts += [type(pair).__name__, pair.mode, sorted(pair.params.items()), sorted(pair.r_cut.items()),
+                      pair.r_cut.default, sorted(pair.r_on.items()), pair.r_on.default, pair.nlist.buffer,
+                      pair.nlist.exclusions]
+        if bond is not None:
+            parts += [type(bond).__name__, sorted((k, sorted(v.items())) for k, v in bond.params.items())]
+        return repr(parts)
+
+    def __init__(self, sim, integ, snap):
+        L = _lib.load()
+        _lib.require_gpu()
+        import torch  # noqa: F401  (initialises the CUDA context used by torch streams)
+
+        self._L = L
+        pair, bond = split_forces(integ)
+        m = integ.methods[0]
+        p = snap.particles
+        types = list(p.types)
+        nt = len(types)
+        c = _lib.MDConfig()
+        c.N = p.N
+        c.ntypes = nt
+        for d in range(3):
+            c.box.L[d] = snap.configuration.box[d]
+        c.precision = _lib.FP32 if sim.precision == "fp32" else _lib.FP64
+        self._keep = []
+
+        def arr(a, dt=np.float64):
+            a = np.ascontiguousarray(a, dtype=dt)
+            self._keep.append(a)
+            return a.ctypes.data
+
+        if pair is not None:
+            rec, rc, ro = pair._tables(types)
+            c.pair_kind = pair.kind
+            c.shift_mode = _lib.MODES[pair.mode]
+            c.pair_params = arr(rec.reshape(-1))
+            c.r_cut = arr(rc.reshape(-1))
+            c.r_on = arr(ro.reshape(-1))
+            c.r_buff = pair.nlist.buffer
+            c.exclude_bonds = int(pair.nlist.exclude_bonds)
+        else:
+            c.pair_kind = -1
+            c.r_buff = 0.4
+            c.exclude_bonds = 0
+        b = snap.bonds
+        if bond is not None and b.N > 0:
+            c.bond_kind = bond.kind
+            c.nbondtypes = len(b.types)
+            c.bond_params = arr(bond._table(b.types).reshape(-1))
+            c.nbonds = b.N
+            c.bonds = arr(np.asarray(b.group).reshape(-1), np.uint32)
+            c.bond_types = arr(b.typeid, np.uint32)
+        else:
+            c.bond_kind = -1
+        c.method = _lib.METHOD_BROWNIAN if isinstance(m, BrownianFlow) else _lib.METHOD_LANGEVIN
+        c.dt = integ.dt
+        c.kT = m.kT
+        c.seed = sim.seed
+        c.noiseless = int(m.noiseless)
+        c.gamma = arr(m._gamma_table(types))
+        c.use_lambda = int(m.alpha is not None)
+        c.lambda_ = m.alpha or 0.0
+        c.flow = m.flow_field._record()
+        c.max_displacement = getattr(m, "max_displacement", 0.0)
+        st = ctypes.c_int(0)
+        self._md = L.azp_md_create(ctypes.byref(c), ctypes.byref(st))
+        _lib.check(st.value, "azp_md_create")
+        self.N = p.N
+        self.has_accel = p.acceleration is not None
+        self.last_launches = 0
+
+    def push(self, snap, timestep):
+        p = snap.particles
+        N = p.N
+        pos = np.empty((N, 4))
+        pos[:, :3] = p.position
+        pos[:, 3] = p.typeid
+        vel = np.empty((N, 4))
+        vel[:, :3] = p.velocity
+        vel[:, 3] = p.mass
+        img = np.ascontiguousarray(p.image, dtype=np.int32)
+        diam = np.ascontiguousarray(p.diameter, dtype=np.float64)
+        acc = None if p.acceleration is None else np.ascontiguousarray(p.acceleration, dtype=np.float64)
+        s = _stream()
+        _lib.check(
+            self._L.azp_md_set_state(self._md, pos.ctypes.data, vel.ctypes.data,
+                                     None if acc is None else acc.ctypes.data, img.ctypes.data, diam.ctypes.data,
+                                     int(timestep), 0, s),
+            "azp_md_set_state")
+
+    def pull(self, snap):
+        p = snap.particles
+        N = p.N
+        pos = np.empty((N, 4))
+        vel = np.empty((N, 4))
+        acc = np.empty((N, 3))
+        img = np.empty((N, 3), dtype=np.int32)
+        ts = ctypes.c_uint64(0)
+        _lib.check(self._L.azp_md_get_state(self._md, pos.ctypes.data, vel.ctypes.data, acc.ctypes.data,
+                                            img.ctypes.data, ctypes.byref(ts), 0, _stream()), "azp_md_get_state")
+        p.position = pos[:, :3].copy()
+        p.velocity = vel[:, :3].copy()
+        p.acceleration = acc
+        p.image = img
+
+    def run(self, steps):
+        s = _stream()
+        _lib.check(self._L.azp_md_run(self._md, int(steps), s), "azp_md_run")
+        self.last_launches = int(self._L.azp_md_last_launches(self._md))
+        err = ctypes.c_uint32(0)
+        _lib.check(self._L.azp_md_error(self._md, ctypes.byref(err), s), "azp_md_error")
+        if err.value & _lib.EBIT_NLIST_OVERFLOW:
+            raise _lib.AzpError(-3, "azp_md_run")
+        if err.value & _lib.EBIT_BOND:
+            raise _lib.AzpError(-4, "azp_md_run")
+        if err.value & _lib.EBIT_NONFINITE:
+            raise _lib.AzpError(-7, "azp_md_run")
+
+    def run_async(self, steps):
+        """Enqueue ``steps`` timesteps without reading the error word back."""
+        _lib.check(self._L.azp_md_run(self._md, int(steps), _stream()), "azp_md_run")
+        self.last_launches = int(self._L.azp_md_last_launches(self._md))
+
+    def forces(self):
+        f = np.empty((self.N, 4))
+        w = np.empty((self.N, 6))
+        _lib.check(self._L.azp_md_forces(self._md, f.ctypes.data, w.ctypes.data, 0, _stream()), "azp_md_forces")
+        return f, w
+
+    def thermo(self):
+        out = np.zeros(9)
+        _lib.check(self._L.azp_md_thermo(self._md, out.ctypes.data, _stream()), "azp_md_thermo")
+        return {
+            "potential_energy": out[0],
+            "kinetic_energy": out[1],
+            "virial": out[2:8].copy(),
+            "nlist_builds": int(out[8]),
+        }
+
+    def close(self):
+        if getattr(self, "_md", None):
+            self._L.azp_md_destroy(self._md)
+            self._md = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

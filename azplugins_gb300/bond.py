@@ -1,0 +1,92 @@
+"""Bond potentials (mirror of ``hoomd.azplugins.bond``, ``src/bond.py``).
+
+``params["A-A"]`` keys follow the reference schemas (``src/bond.py:45-49`` for
+DoubleWell, ``:141-156`` for Quartic, whose ``delta`` defaults to 0 as in the
+reference); records are built by the native ports of the reference dict
+constructors.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+from .typeparam import TypeParameterDict
+
+
+class Bond:
+    """Base class of the bond potentials (HOOMD ``md.bond.Bond``)."""
+
+    _name = None
+    _keys = ()
+    _defaults = {}
+
+    def __init__(self):
+        self.params = TypeParameterDict(1, required=tuple(k for k in self._keys if k not in self._defaults),
+                                        defaults=self._defaults, name="params")
+        self._sim = None
+
+    @property
+    def kind(self) -> int:
+        return _lib.BOND_KINDS[self._name]
+
+    def _table(self, bond_types):
+        L = _lib.load()
+        rec = np.zeros((len(bond_types), 8))
+        for t, name in enumerate(bond_types):
+            if name not in self.params:
+                raise KeyError(f"{type(self).__name__}.params[{name!r}] is not set")
+            d = self.params[name]
+            vals = np.ascontiguousarray([d[k] for k in self._keys], dtype=np.float64)
+            out = np.zeros(8)
+            _lib.check(L.azp_bond_params_from_values(self.kind, vals.ctypes.data, out.ctypes.data), "params")
+            rec[t] = out
+        return rec
+
+    def record_to_dict(self, rec):
+        L = _lib.load()
+        rec = np.ascontiguousarray(rec, dtype=np.float64)
+        vals = np.zeros(len(self._keys))
+        _lib.check(L.azp_bond_params_to_values(self.kind, rec.ctypes.data, vals.ctypes.data), "asDict")
+        return dict(zip(self._keys, (float(v) for v in vals)))
+
+    def _compute(self):
+        if self._sim is None:
+            raise RuntimeError("attach the force to a Simulation (sim.run(0)) before reading results")
+        from . import _compute
+
+        return _compute.bond_forces(self._sim.state, self, self._sim.precision)
+
+    @property
+    def forces(self):
+        return self._compute()[0][:, :3].copy()
+
+    @property
+    def energies(self):
+        return self._compute()[0][:, 3].copy()
+
+    @property
+    def energy(self):
+        return float(self._compute()[0][:, 3].sum())
+
+    @property
+    def virials(self):
+        return self._compute()[1].copy()
+
+
+class DoubleWell(Bond):
+    """Double-well bond potential (``src/BondEvaluatorDoubleWell.h``)."""
+
+    _name = "DoubleWell"
+    _keys = ("r_0", "r_1", "U_1", "U_tilt")
+
+
+class Quartic(Bond):
+    """Quartic (breakable) bond potential with a WCA core (``src/BondEvaluatorQuartic.h``)."""
+
+    _name = "Quartic"
+    _keys = ("k", "r_0", "b_1", "b_2", "U_0", "sigma", "epsilon", "delta")
+    _defaults = {"delta": 0.0}
+
+
+__all__ = ["Bond", "DoubleWell", "Quartic"]

@@ -1,0 +1,62 @@
+// celllist.cuh -- cell binning and neighbour-list construction shared by the
+// standalone azp_nlist object and the resident engine.
+#pragma once
+
+#include "common.cuh"
+
+namespace azp
+{
+// Cells of width >= r_list_max along each axis; an axis with fewer than 3 cells
+// is scanned as a single cell (no duplicate images).
+struct CellGrid {
+    int dim[3];
+    int reach[3];    // 1 when the axis has >= 3 cells, else 0
+    double lo[3];    // -L/2
+    double scale[3]; // dim / L
+    uint32_t ncell;
+};
+
+CellGrid make_grid(const azp_box& box, double rlist_max);
+
+// Per type pair thresholds of the list decision (host-built, ntypes^2 entries).
+struct ListCut {
+    double rlistsq;  // exact FP64 test: rsq < rlistsq
+    float lo, hi;    // FP32 prefilter: rsq_f < lo -> listed, rsq_f >= hi -> not listed
+    float pad;
+};
+
+// Launch helpers (all stream-ordered, no allocation, no synchronisation).
+// fixed[N] <- 16-byte fixed-point shadow of pos (x, y, z fractions of L, type)
+void launch_to_fixed(const double4_32a* pos, uint4* fixed, uint32_t N, const azp_box& box, cudaStream_t s);
+
+// cell_of[i], slot[i] (arrival order inside the cell) and cell_count[c] += 1.
+// cell_count must be zeroed by the caller.
+void launch_cell_assign(const double4_32a* pos, uint32_t N, const CellGrid& g, uint32_t* cell_of, uint32_t* slot,
+                        uint32_t* cell_count, cudaStream_t s, const uint32_t* gate = nullptr);
+
+// members[cell_start[c] + rank] = i with the rank of i among the particles of
+// its cell in increasing index order (deterministic: a stable counting sort).
+void launch_cell_scatter(const uint32_t* cell_of, const uint32_t* slot, const uint32_t* cell_start,
+                         uint32_t* members, uint32_t N, uint32_t ncell, cudaStream_t s,
+                         const uint32_t* gate = nullptr);
+
+// Full neighbour list. members == NULL means the particles are already stored in
+// cell order (members[s] = s). keys: exclusion keys of particles (NULL: index);
+// ex_n[i] / ex_keys[k * N + i]: excluded keys of particle i. Rows are written
+// column-major nbrs[k * N + i]; counts[i] = the true count even past max_nn;
+// flags[0] = max count over particles (atomicMax), used to detect overflow.
+void launch_nlist_build(const double4_32a* pos, const uint4* fixed, uint32_t N, const azp_box& box, const CellGrid& g,
+                        const uint32_t* cell_start, const uint32_t* members, const uint32_t* cell_of,
+                        const ListCut* cuts, uint32_t ntypes, const uint32_t* ex_n, const uint32_t* ex_keys,
+                        uint32_t ex_width, const uint32_t* keys, uint32_t* counts, uint32_t* nbrs,
+                        uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s);
+
+// fixed-point shadow of pos into one or two arrays (gated)
+void launch_to_fixed2(const double4_32a* pos, uint4* a, uint4* b, uint32_t N, const azp_box& box, cudaStream_t s,
+                      const uint32_t* gate);
+
+// host: thresholds for r_cut[ntypes^2], r_buff and the box
+void make_list_cuts(const double* r_cut, uint32_t ntypes, double r_buff, const azp_box& box, ListCut* out,
+                    double* rlist_max);
+
+}  // namespace azp

@@ -1,0 +1,1041 @@
+// engine.cu -- the resident MD engine (azp_md): state in cell order in HBM, one
+// fused force-and-integrate launch per timestep, list rebuild + particle re-sort
+// on the device when any particle moved more than r_buff / 2 since the last
+// build (HOOMD's distance check), and CUDA-graph replay of the step sequence with
+// the rebuild as a conditional node armed by the step kernel itself.
+//
+// Host-visible state is always in tag order; inside, index order is the cell
+// order of the last rebuild and tag[] / rtag[] map between the two. The RNG is
+// keyed by tag and timestep, so results do not depend on the order.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "celllist.cuh"
+#include "engine.cuh"
+#include "engine_kernels.cuh"
+#include "scan.cuh"
+
+namespace azp
+{
+int launch_md_step(int pair_kind, int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s)
+{
+    switch (pair_kind) {
+    case -1: return launch_md_nopair(bond_kind, precision, integ, a, s);
+    case AZP_PAIR_PERTURBED_LJ: return launch_md_plj(bond_kind, precision, integ, a, s);
+    case AZP_PAIR_EXPANDED_YUKAWA: return launch_md_eyuk(bond_kind, precision, integ, a, s);
+    case AZP_PAIR_HERTZ: return launch_md_hertz(bond_kind, precision, integ, a, s);
+    case AZP_PAIR_COLLOID: return launch_md_colloid(bond_kind, precision, integ, a, s);
+    default: return AZP_ERR_INVALID;
+    }
+}
+
+// ---------------------------------------------------------------- rebuild kernels
+__global__ void k_zero_gated(uint32_t* __restrict__ p, uint32_t n, const uint32_t* __restrict__ gate)
+{
+    if (gate && *gate == 0u) return;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0u;
+}
+
+struct PermArgs {
+    const uint32_t* members;
+    double4_32a *pos, *t_pos;
+    double4_32a *vel, *t_vel;
+    double *accel, *t_accel;
+    int *image, *t_image;
+    uint32_t *tag, *t_tag, *rtag;
+    double *diam, *t_diam;
+    uint32_t *cell_of, *t_cell;
+    uint32_t N;
+};
+
+// temps[s] <- arrays[members[s]]
+__global__ void k_perm_gather(PermArgs a, const uint32_t* __restrict__ gate)
+{
+    if (gate && *gate == 0u) return;
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.N) return;
+    const uint32_t o = a.members[s];
+    a.t_pos[s] = a.pos[o];
+    a.t_vel[s] = a.vel[o];
+    a.t_accel[3 * s] = a.accel[3 * o];
+    a.t_accel[3 * s + 1] = a.accel[3 * o + 1];
+    a.t_accel[3 * s + 2] = a.accel[3 * o + 2];
+    a.t_image[3 * s] = a.image[3 * o];
+    a.t_image[3 * s + 1] = a.image[3 * o + 1];
+    a.t_image[3 * s + 2] = a.image[3 * o + 2];
+    a.t_tag[s] = a.tag[o];
+    if (a.diam) a.t_diam[s] = a.diam[o];
+    a.t_cell[s] = a.cell_of[o];
+}
+
+// arrays[s] <- temps[s]; rtag[tag[s]] = s
+__global__ void k_perm_back(PermArgs a, const uint32_t* __restrict__ gate)
+{
+    if (gate && *gate == 0u) return;
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.N) return;
+    a.pos[s] = a.t_pos[s];
+    a.vel[s] = a.t_vel[s];
+    a.accel[3 * s] = a.t_accel[3 * s];
+    a.accel[3 * s + 1] = a.t_accel[3 * s + 1];
+    a.accel[3 * s + 2] = a.t_accel[3 * s + 2];
+    a.image[3 * s] = a.t_image[3 * s];
+    a.image[3 * s + 1] = a.t_image[3 * s + 1];
+    a.image[3 * s + 2] = a.t_image[3 * s + 2];
+    const uint32_t t = a.t_tag[s];
+    a.tag[s] = t;
+    a.rtag[t] = s;
+    if (a.diam) a.diam[s] = a.t_diam[s];
+    a.cell_of[s] = a.t_cell[s];
+}
+
+// per-particle bond table and exclusions in the new index order, from the
+// tag-order master table [k * N + tag]
+__global__ void k_bond_table(const uint32_t* __restrict__ tag, const uint32_t* __restrict__ rtag,
+                             const uint32_t* __restrict__ n_tag, const uint32_t* __restrict__ partner_tag,
+                             const uint32_t* __restrict__ type_tag, uint32_t N, uint32_t* __restrict__ bt_n,
+                             uint2* __restrict__ bt, uint32_t* __restrict__ ex_n, uint32_t* __restrict__ ex_idx,
+                             int exclude, const uint32_t* __restrict__ gate)
+{
+    if (gate && *gate == 0u) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const uint32_t t = tag[i];
+    const uint32_t n = n_tag[t];
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t p = rtag[partner_tag[(size_t)k * N + t]];
+        bt[(size_t)k * N + i] = make_uint2(p, type_tag[(size_t)k * N + t]);
+        if (exclude) ex_idx[(size_t)k * N + i] = p;
+    }
+    bt_n[i] = n;
+    if (ex_n) ex_n[i] = exclude ? n : 0u;
+}
+
+__global__ void k_finish_rebuild(uint32_t* __restrict__ flags, const uint32_t* __restrict__ gate)
+{
+    if (gate && *gate == 0u) return;
+    flags[0] = 0u;
+    flags[2] += 1u;
+}
+
+// first graph node of a replay: arm the first conditional from the request flag
+__global__ void k_arm(const uint32_t* __restrict__ flags, cudaGraphConditionalHandle h)
+{
+    cudaGraphSetConditional(h, flags[0] ? 1u : 0u);
+}
+
+// Langevin step one in place at the start of a run (src/TwoStepLangevinFlow.h:128-153)
+__global__ void k_md_step1(double4_32a* __restrict__ pos, uint4* __restrict__ fix, const uint4* __restrict__ fix_build,
+                           double4_32a* __restrict__ vel, const double* __restrict__ accel, int* __restrict__ image,
+                           uint32_t N, double dt, double L0, double L1, double L2, double Li0, double Li1, double Li2,
+                           float s0, float s1, float s2, float thresh2, uint32_t* __restrict__ flags)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool want = false;
+    if (i < N) {
+        double4_32a p = pos[i];
+        double4_32a v = vel[i];
+        const double ax = accel[3 * i], ay = accel[3 * i + 1], az = accel[3 * i + 2];
+        const double h = 0.5 * dt;
+        p.x += (v.x + h * ax) * dt;
+        p.y += (v.y + h * ay) * dt;
+        p.z += (v.z + h * az) * dt;
+        int wx = 0, wy = 0, wz = 0;
+        wrap1(p.x, wx, L0, -0.5 * L0, 0.5 * L0);
+        wrap1(p.y, wy, L1, -0.5 * L1, 0.5 * L1);
+        wrap1(p.z, wz, L2, -0.5 * L2, 0.5 * L2);
+        if (wx | wy | wz) {
+            image[3 * i] += wx;
+            image[3 * i + 1] += wy;
+            image[3 * i + 2] += wz;
+        }
+        v.x += h * ax;
+        v.y += h * ay;
+        v.z += h * az;
+        pos[i] = p;
+        vel[i] = v;
+        uint4 f;
+        f.x = to_fixed(p.x, Li0);
+        f.y = to_fixed(p.y, Li1);
+        f.z = to_fixed(p.z, Li2);
+        f.w = type_of(p.w);
+        fix[i] = f;
+        const uint4 fb = fix_build[i];
+        const float dx = (float)(int32_t)(f.x - fb.x) * s0;
+        const float dy = (float)(int32_t)(f.y - fb.y) * s1;
+        const float dz = (float)(int32_t)(f.z - fb.z) * s2;
+        want = dx * dx + dy * dy + dz * dz > thresh2;
+    }
+    if (__any_sync(0xffffffffu, want) && (threadIdx.x & 31) == 0) atomicOr(&flags[0], 1u);
+}
+
+// accelerations a = F / m (HOOMD sets them this way before the first step)
+__global__ void k_accel_from_force(const double4_32a* __restrict__ f, const double4_32a* __restrict__ vel,
+                                   double* __restrict__ accel, uint32_t N)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const double4_32a F = f[i];
+    const double minv = 1.0 / vel[i].w;
+    accel[3 * i] = F.x * minv;
+    accel[3 * i + 1] = F.y * minv;
+    accel[3 * i + 2] = F.z * minv;
+}
+
+// thermo partial sums per block (deterministic two-pass reduction)
+constexpr int THERMO_BLOCK = 256;
+__global__ void k_thermo_partials(const double4_32a* __restrict__ f, const double* __restrict__ vir,
+                                  const double4_32a* __restrict__ vel, uint32_t N, double* __restrict__ part)
+{
+    __shared__ double s[THERMO_BLOCK][8];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (i < N) {
+        v[0] = f[i].w;
+        const double4_32a u = vel[i];
+        v[1] = 0.5 * u.w * (u.x * u.x + u.y * u.y + u.z * u.z);
+        for (int c = 0; c < 6; ++c) v[2 + c] = vir[(size_t)c * N + i];
+    }
+    for (int c = 0; c < 8; ++c) s[threadIdx.x][c] = v[c];
+    __syncthreads();
+    for (int st = THERMO_BLOCK / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st)
+            for (int c = 0; c < 8; ++c) s[threadIdx.x][c] += s[threadIdx.x + st][c];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int c = 0; c < 8; ++c) part[(size_t)blockIdx.x * 8 + c] = s[0][c];
+}
+
+__global__ void k_thermo_final(const double* __restrict__ part, uint32_t nb, double* __restrict__ out)
+{
+    const int c = threadIdx.x;
+    if (c >= 8) return;
+    double acc = 0.0;
+    for (uint32_t b = 0; b < nb; ++b) acc += part[(size_t)b * 8 + c];
+    out[c] = acc;
+}
+
+// index order -> tag order
+__global__ void k_to_tag_order4(const double4_32a* __restrict__ src, const uint32_t* __restrict__ tag, uint32_t N,
+                                double4_32a* __restrict__ dst)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) dst[tag[i]] = src[i];
+}
+
+__global__ void k_to_tag_order_n(const double* __restrict__ src, const uint32_t* __restrict__ tag, uint32_t N,
+                                 int ncomp, int soa, double* __restrict__ dst)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const uint32_t t = tag[i];
+    for (int c = 0; c < ncomp; ++c) dst[(size_t)t * ncomp + c] = soa ? src[(size_t)c * N + i] : src[(size_t)i * ncomp + c];
+}
+
+__global__ void k_to_tag_order_i3(const int* __restrict__ src, const uint32_t* __restrict__ tag, uint32_t N,
+                                  int* __restrict__ dst)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const uint32_t t = tag[i];
+    dst[3 * t] = src[3 * i];
+    dst[3 * t + 1] = src[3 * i + 1];
+    dst[3 * t + 2] = src[3 * i + 2];
+}
+
+// tag-order input (pos w = integer-valued type) -> device state, identity order
+__global__ void k_load_state(const double* __restrict__ pos_in, const double* __restrict__ vel_in,
+                             const double* __restrict__ accel_in, const int* __restrict__ image_in,
+                             const double* __restrict__ diam_in, uint32_t N, double4_32a* __restrict__ pos,
+                             double4_32a* __restrict__ vel, double* __restrict__ accel, int* __restrict__ image,
+                             double* __restrict__ diam, uint32_t* __restrict__ tag, uint32_t* __restrict__ rtag)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    pos[i] = make_double4_32a(pos_in[4 * i], pos_in[4 * i + 1], pos_in[4 * i + 2],
+                              type_as_double((uint32_t)pos_in[4 * i + 3]));
+    vel[i] = make_double4_32a(vel_in[4 * i], vel_in[4 * i + 1], vel_in[4 * i + 2], vel_in[4 * i + 3]);
+    for (int d = 0; d < 3; ++d) {
+        accel[3 * i + d] = accel_in ? accel_in[3 * i + d] : 0.0;
+        image[3 * i + d] = image_in ? image_in[3 * i + d] : 0;
+    }
+    if (diam) diam[i] = diam_in ? diam_in[i] : 1.0;
+    tag[i] = i;
+    rtag[i] = i;
+}
+
+// device state -> tag order output (pos w = type as an integer-valued double)
+__global__ void k_store_state(const double4_32a* __restrict__ pos, const double4_32a* __restrict__ vel,
+                              const double* __restrict__ accel, const int* __restrict__ image,
+                              const uint32_t* __restrict__ tag, uint32_t N, double* __restrict__ pos_out,
+                              double* __restrict__ vel_out, double* __restrict__ accel_out, int* __restrict__ image_out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const uint32_t t = tag[i];
+    const double4_32a p = pos[i];
+    if (pos_out) {
+        pos_out[4 * t] = p.x;
+        pos_out[4 * t + 1] = p.y;
+        pos_out[4 * t + 2] = p.z;
+        pos_out[4 * t + 3] = (double)type_of(p.w);
+    }
+    if (vel_out) {
+        const double4_32a v = vel[i];
+        vel_out[4 * t] = v.x;
+        vel_out[4 * t + 1] = v.y;
+        vel_out[4 * t + 2] = v.z;
+        vel_out[4 * t + 3] = v.w;
+    }
+    for (int d = 0; d < 3; ++d) {
+        if (accel_out) accel_out[3 * t + d] = accel[3 * i + d];
+        if (image_out) image_out[3 * t + d] = image[3 * i + d];
+    }
+}
+
+}  // namespace azp
+
+using namespace azp;
+
+struct azp_md {
+    uint32_t N = 0, ntypes = 0, nbt = 0;
+    int precision = AZP_FP64, pair_kind = -1, shift_mode = 0, bond_kind = -1, method = 0;
+    int exclude_bonds = 1, use_lambda = 0, noiseless = 0, tpp = 1;
+    double r_buff = 0.4, dt = 0.005, kT = 1.0, lambda = 0.0, max_disp = 0.0;
+    uint32_t seed = 0;
+    FlowD flow{};
+    azp_box box{};
+    std::vector<double> pair_params, r_cut, r_on, bond_params, gamma;
+    // device state
+    double4_32a* pos[2] = {nullptr, nullptr};
+    uint4* fix[2] = {nullptr, nullptr};
+    int cur = 0;
+    uint4* fix_build = nullptr;
+    double4_32a* vel = nullptr;
+    double* accel = nullptr;
+    int* image = nullptr;
+    uint32_t* tag = nullptr;
+    uint32_t* rtag = nullptr;
+    double* diam = nullptr;
+    // permutation temps
+    double4_32a* t_pos = nullptr;
+    double4_32a* t_vel = nullptr;
+    double* t_accel = nullptr;
+    int* t_image = nullptr;
+    uint32_t* t_tag = nullptr;
+    double* t_diam = nullptr;
+    uint32_t* t_cell = nullptr;
+    // cells
+    CellGrid grid{};
+    uint32_t *cell_of = nullptr, *slot = nullptr, *cell_count = nullptr, *cell_start = nullptr, *members = nullptr,
+             *scan_tmp = nullptr;
+    // list
+    uint32_t max_nn = 0;
+    uint32_t* counts = nullptr;
+    uint32_t* nbrs = nullptr;
+    ListCut* cuts = nullptr;
+    double rlist_max = 0.0;
+    // bonds
+    uint32_t bt_width = 0;
+    uint32_t *bt_n_tag = nullptr, *bt_partner_tag = nullptr, *bt_type_tag = nullptr;
+    uint32_t* bt_n = nullptr;
+    uint2* bt = nullptr;
+    uint32_t* ex_n = nullptr;
+    uint32_t* ex_idx = nullptr;
+    double* d_bond_params = nullptr;
+    double* d_pair_table = nullptr;
+    double* d_gamma = nullptr;
+    // control
+    uint32_t* flags = nullptr;  // [0] rebuild request [1] error bits [2] builds [3] max count [4] ticket
+    unsigned long long* d_ts = nullptr;
+    uint64_t timestep = 0;
+    // outputs
+    double4_32a* out_force = nullptr;
+    double* out_virial = nullptr;
+    double* partials = nullptr;
+    double* thermo = nullptr;
+    double4_32a* tmp4 = nullptr;  // tag-order staging [N]
+    double* tmpd = nullptr;       // tag-order staging [N * 6]
+    uint64_t launches = 0;
+    bool have_state = false;
+    // graphs
+    bool use_graphs = true;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // pair of mid steps starting at cur = 0 / 1
+    uint32_t graph_steps = 0;
+    cudaStream_t graph_stream = nullptr;
+};
+
+namespace
+{
+template<typename T> int dalloc(T** p, size_t n)
+{
+    *p = nullptr;
+    if (n == 0) n = 1;
+    const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * n);
+    return e == cudaSuccess ? AZP_OK : record_cuda_error(e, "cudaMalloc (engine)");
+}
+
+void free_graphs(azp_md* m)
+{
+    for (auto& g : m->gexec)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    m->graph_steps = 0;
+}
+
+void free_all(azp_md* m)
+{
+    free_graphs(m);
+    void* ptrs[] = {m->pos[0], m->pos[1], m->fix[0], m->fix[1], m->fix_build, m->vel, m->accel, m->image, m->tag,
+                    m->rtag, m->diam, m->t_pos, m->t_vel, m->t_accel, m->t_image, m->t_tag, m->t_diam, m->t_cell,
+                    m->cell_of, m->slot, m->cell_count, m->cell_start, m->members, m->scan_tmp, m->counts, m->nbrs,
+                    m->cuts, m->bt_n_tag, m->bt_partner_tag, m->bt_type_tag, m->bt_n, m->bt, m->ex_n, m->ex_idx,
+                    m->d_bond_params, m->d_pair_table, m->d_gamma, m->flags, m->d_ts, m->out_force, m->out_virial,
+                    m->partials, m->thermo, m->tmp4, m->tmpd};
+    for (void* p : ptrs) cudaFree(p);
+}
+
+uint32_t blocks_for(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
+
+MDArgs base_args(azp_md* m)
+{
+    MDArgs a{};
+    a.pos = m->pos[m->cur];
+    a.pos_next = m->pos[m->cur ^ 1];
+    a.fix = m->fix[m->cur];
+    a.fix_next = m->fix[m->cur ^ 1];
+    a.fix_build = m->fix_build;
+    a.vel = m->vel;
+    a.accel = m->accel;
+    a.image = m->image;
+    a.tag = m->tag;
+    a.diameter = m->diam;
+    a.N = m->N;
+    a.ntypes = m->ntypes;
+    for (int d = 0; d < 3; ++d) {
+        a.L[d] = m->box.L[d];
+        a.Linv[d] = 1.0 / m->box.L[d];
+        a.lo[d] = -0.5 * m->box.L[d];
+        a.hi[d] = 0.5 * m->box.L[d];
+        a.sfix[d] = (float)(m->box.L[d] * 2.3283064365386963e-10);
+    }
+    a.counts = m->counts;
+    a.nbrs = m->nbrs;
+    a.pair_table = m->d_pair_table;
+    a.bt_n = m->bt_n;
+    a.bt = m->bt;
+    a.bond_params = m->d_bond_params;
+    a.nbondtypes = m->nbt;
+    a.dt = m->dt;
+    a.kT = m->kT;
+    a.d_timestep = m->d_ts;
+    a.d_timestep_rw = m->d_ts;
+    a.seed = m->seed;
+    a.noiseless = m->noiseless;
+    a.gamma = m->d_gamma;
+    a.use_lambda = m->use_lambda;
+    a.lambda = m->lambda;
+    a.flow = m->flow;
+    a.max_disp = m->max_disp;
+    const double half = 0.5 * m->r_buff;
+    a.disp_thresh2 = (float)(half * half * (1.0 - 1e-5));
+    a.flags = m->flags;
+    a.out_force = m->out_force;
+    a.out_virial = m->out_virial;
+    a.set_cond = 0;
+    a.next = 0;
+    a.out = 0;
+    a.tpp = m->tpp;
+    return a;
+}
+
+// the list rebuild + re-sort, gated by flags[0] (gate) or unconditional (gate NULL)
+int enqueue_rebuild(azp_md* m, cudaStream_t s, const uint32_t* gate)
+{
+    const uint32_t N = m->N;
+    if (N == 0) return AZP_OK;
+    const uint32_t nb = blocks_for(N, 256);
+    k_zero_gated<<<std::min<uint32_t>(blocks_for(m->grid.ncell, 256), 1024), 256, 0, s>>>(m->cell_count, m->grid.ncell,
+                                                                                          gate);
+    launch_cell_assign(m->pos[m->cur], N, m->grid, m->cell_of, m->slot, m->cell_count, s, gate);
+    int st = exclusive_scan(m->cell_count, m->cell_start, m->grid.ncell, m->scan_tmp, s, gate);
+    if (st) return st;
+    launch_cell_scatter(m->cell_of, m->slot, m->cell_start, m->members, N, m->grid.ncell, s, gate);
+    PermArgs p;
+    p.members = m->members;
+    p.pos = m->pos[m->cur];
+    p.t_pos = m->t_pos;
+    p.vel = m->vel;
+    p.t_vel = m->t_vel;
+    p.accel = m->accel;
+    p.t_accel = m->t_accel;
+    p.image = m->image;
+    p.t_image = m->t_image;
+    p.tag = m->tag;
+    p.t_tag = m->t_tag;
+    p.rtag = m->rtag;
+    p.diam = m->diam;
+    p.t_diam = m->t_diam;
+    p.cell_of = m->cell_of;
+    p.t_cell = m->t_cell;
+    p.N = N;
+    k_perm_gather<<<nb, 256, 0, s>>>(p, gate);
+    k_perm_back<<<nb, 256, 0, s>>>(p, gate);
+    if (m->bond_kind >= 0)
+        k_bond_table<<<nb, 256, 0, s>>>(m->tag, m->rtag, m->bt_n_tag, m->bt_partner_tag, m->bt_type_tag, N, m->bt_n,
+                                        m->bt, m->ex_n, m->ex_idx, m->exclude_bonds, gate);
+    launch_to_fixed2(m->pos[m->cur], m->fix[m->cur], m->fix_build, N, m->box, s, gate);
+    if (m->pair_kind >= 0)
+        launch_nlist_build(m->pos[m->cur], m->fix[m->cur], N, m->box, m->grid, m->cell_start, nullptr, m->cell_of,
+                           m->cuts, m->ntypes, m->ex_n, m->ex_idx, m->bt_width, nullptr, m->counts, m->nbrs,
+                           m->max_nn, m->flags + 3, gate, s);
+    k_finish_rebuild<<<1, 1, 0, s>>>(m->flags, gate);
+    AZP_CHECK_LAUNCH("enqueue_rebuild");
+    m->launches += 11 + (m->bond_kind >= 0) + (m->pair_kind >= 0);
+    return AZP_OK;
+}
+
+int enqueue_step(azp_md* m, int integ, int next, int out, cudaStream_t s, int set_cond,
+                 cudaGraphConditionalHandle h)
+{
+    MDArgs a = base_args(m);
+    a.next = next;
+    a.out = out;
+    a.set_cond = set_cond;
+    a.next_cond = h;
+    const int st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, integ, a, s);
+    m->launches += 1;
+    return st;
+}
+
+int enqueue_step1(azp_md* m, cudaStream_t s)
+{
+    const double half = 0.5 * m->r_buff;
+    k_md_step1<<<blocks_for(m->N, 256), 256, 0, s>>>(
+        m->pos[m->cur], m->fix[m->cur], m->fix_build, m->vel, m->accel, m->image, m->N, m->dt, m->box.L[0],
+        m->box.L[1], m->box.L[2], 1.0 / m->box.L[0], 1.0 / m->box.L[1], 1.0 / m->box.L[2],
+        (float)(m->box.L[0] * 2.3283064365386963e-10), (float)(m->box.L[1] * 2.3283064365386963e-10),
+        (float)(m->box.L[2] * 2.3283064365386963e-10), (float)(half * half * (1.0 - 1e-5)), m->flags);
+    AZP_CHECK_LAUNCH("k_md_step1");
+    m->launches += 1;
+    return AZP_OK;
+}
+
+// Build the executable graph of two mid steps starting at buffer parity cur0:
+//   arm -> IF(rebuild) -> step(next) -> IF(rebuild) -> step(next)
+// Each step kernel arms the following conditional from its last block.
+int build_pair_graph(azp_md* m, int cur0, int integ, cudaGraphExec_t* out)
+{
+    cudaGraph_t g = nullptr;
+    AZP_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h[2];
+    for (int k = 0; k < 2; ++k) AZP_CUDA_TRY(cudaGraphConditionalHandleCreate(&h[k], g, 0, cudaGraphCondAssignDefault));
+    const int saved_cur = m->cur;
+    const uint64_t saved_launches = m->launches;
+    m->cur = cur0;
+    cudaStream_t s = m->graph_stream;
+    cudaGraphNode_t prev = nullptr;
+    int st = AZP_OK;
+    // arm node
+    {
+        AZP_CUDA_TRY(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        k_arm<<<1, 1, 0, s>>>(m->flags, h[0]);
+        cudaGraph_t gg = nullptr;
+        AZP_CUDA_TRY(cudaStreamEndCapture(s, &gg));
+        size_t n = 0;
+        AZP_CUDA_TRY(cudaGraphGetNodes(g, nullptr, &n));
+        std::vector<cudaGraphNode_t> nodes(n);
+        AZP_CUDA_TRY(cudaGraphGetNodes(g, nodes.data(), &n));
+        prev = nodes.back();
+    }
+    for (int k = 0; k < 2 && st == AZP_OK; ++k) {
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h[k];
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cnode;
+        AZP_CUDA_TRY(cudaGraphAddNode(&cnode, g, &prev, nullptr, 1, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        AZP_CUDA_TRY(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        st = enqueue_rebuild(m, s, nullptr);
+        cudaGraph_t bb = nullptr;
+        const cudaError_t e1 = cudaStreamEndCapture(s, &bb);
+        if (st) break;
+        if (e1 != cudaSuccess) {
+            st = record_cuda_error(e1, "capture rebuild body");
+            break;
+        }
+        // the step node, depending on the conditional
+        AZP_CUDA_TRY(cudaStreamBeginCaptureToGraph(s, g, &cnode, nullptr, 1, cudaStreamCaptureModeThreadLocal));
+        st = enqueue_step(m, integ, 1, 0, s, k == 0 ? 1 : 0, k == 0 ? h[1] : 0);
+        cudaGraph_t sg = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(s, &sg);
+        if (st) break;
+        if (e2 != cudaSuccess) {
+            st = record_cuda_error(e2, "capture step");
+            break;
+        }
+        // find the node just added: the one that depends on cnode
+        size_t nd = 0;
+        AZP_CUDA_TRY(cudaGraphNodeGetDependentNodes(cnode, nullptr, nullptr, &nd));
+        std::vector<cudaGraphNode_t> deps(nd);
+        AZP_CUDA_TRY(cudaGraphNodeGetDependentNodes(cnode, deps.data(), nullptr, &nd));
+        if (nd != 1) {
+            st = AZP_ERR_CUDA;
+            break;
+        }
+        prev = deps[0];
+        m->cur ^= 1;
+    }
+    m->cur = saved_cur;
+    m->launches = saved_launches;
+    if (st == AZP_OK) {
+        const cudaError_t e = cudaGraphInstantiate(out, g, 0);
+        if (e != cudaSuccess) st = record_cuda_error(e, "cudaGraphInstantiate");
+    }
+    cudaGraphDestroy(g);
+    return st;
+}
+
+int check_errors(azp_md* m, cudaStream_t s)
+{
+    uint32_t f[8];
+    AZP_CUDA_TRY(cudaMemcpyAsync(f, m->flags, sizeof(f), cudaMemcpyDeviceToHost, s));
+    AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    if (f[3] > m->max_nn) return AZP_ERR_NLIST_OVERFLOW;
+    if (f[1] & AZP_EBIT_BOND) return AZP_ERR_BOND;
+    if (f[1] & AZP_EBIT_NONFINITE) return AZP_ERR_NONFINITE;
+    return AZP_OK;
+}
+
+int size_list(azp_md* m, cudaStream_t s)
+{
+    // first build: measure the largest neighbour count and size the list
+    if (m->pair_kind < 0) return AZP_OK;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        AZP_CUDA_TRY(cudaMemsetAsync(m->flags + 3, 0, sizeof(uint32_t), s));
+        const uint32_t one = 1u;
+        AZP_CUDA_TRY(cudaMemcpyAsync(m->flags, &one, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        int st = enqueue_rebuild(m, s, nullptr);
+        if (st) return st;
+        uint32_t need = 0;
+        AZP_CUDA_TRY(cudaMemcpyAsync(&need, m->flags + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        AZP_CUDA_TRY(cudaStreamSynchronize(s));
+        if (need <= m->max_nn) return AZP_OK;
+        // headroom for density fluctuations between builds
+        cudaFree(m->nbrs);
+        m->nbrs = nullptr;
+        m->max_nn = (uint32_t)std::ceil(need * 1.3) + 8;
+        st = dalloc(&m->nbrs, (size_t)m->N * m->max_nn);
+        if (st) return st;
+        free_graphs(m);
+    }
+    return AZP_ERR_NLIST_OVERFLOW;
+}
+
+}  // namespace
+
+extern "C" {
+
+azp_md* azp_md_create(const azp_md_config* c, int* status)
+{
+    auto fail = [&](int st, azp_md* m) -> azp_md* {
+        if (status) *status = st;
+        if (m) {
+            free_all(m);
+            delete m;
+        }
+        return nullptr;
+    };
+    if (!c || c->ntypes == 0 || c->ntypes > MAX_PAIR_TYPES) return fail(AZP_ERR_INVALID, nullptr);
+    for (int d = 0; d < 3; ++d)
+        if (!(c->box.L[d] > 0.0)) return fail(AZP_ERR_INVALID, nullptr);
+    if (c->precision != AZP_FP64 && c->precision != AZP_FP32) return fail(AZP_ERR_INVALID, nullptr);
+    if (c->method != AZP_METHOD_LANGEVIN_FLOW && c->method != AZP_METHOD_BROWNIAN_FLOW)
+        return fail(AZP_ERR_INVALID, nullptr);
+    if (c->pair_kind >= AZP_PAIR_NUM_KINDS || c->bond_kind >= AZP_BOND_NUM_KINDS) return fail(AZP_ERR_INVALID, nullptr);
+    if (!(c->dt > 0.0)) return fail(AZP_ERR_INVALID, nullptr);
+    if (!c->use_lambda && !c->gamma) return fail(AZP_ERR_INVALID, nullptr);
+    azp_md* m = new (std::nothrow) azp_md();
+    if (!m) return fail(AZP_ERR_INVALID, nullptr);
+    m->N = c->N;
+    m->ntypes = c->ntypes;
+    m->box = c->box;
+    m->precision = c->precision;
+    m->pair_kind = c->pair_kind < 0 ? -1 : c->pair_kind;
+    m->shift_mode = c->shift_mode;
+    m->bond_kind = (c->bond_kind < 0 || c->nbonds == 0) ? -1 : c->bond_kind;
+    m->method = c->method;
+    m->exclude_bonds = c->exclude_bonds;
+    m->r_buff = c->r_buff;
+    m->dt = c->dt;
+    m->kT = c->kT;
+    m->seed = c->seed;
+    m->noiseless = c->noiseless;
+    m->use_lambda = c->use_lambda;
+    m->lambda = c->lambda;
+    m->flow = make_flow(c->flow);
+    m->max_disp = c->max_displacement;
+    const uint32_t nt2 = c->ntypes * c->ntypes;
+    if (m->pair_kind >= 0) {
+        if (!c->pair_params || !c->r_cut) return fail(AZP_ERR_INVALID, m);
+        m->pair_params.assign(c->pair_params, c->pair_params + (size_t)nt2 * AZP_PAIR_PARAM_DOUBLES);
+        m->r_cut.assign(c->r_cut, c->r_cut + nt2);
+        if (c->r_on) m->r_on.assign(c->r_on, c->r_on + nt2);
+        else m->r_on.assign(nt2, 0.0);
+        // same per-type-pair r_cut in both directions
+        for (uint32_t a = 0; a < c->ntypes; ++a)
+            for (uint32_t b = 0; b < c->ntypes; ++b)
+                if (m->r_cut[a * c->ntypes + b] != m->r_cut[b * c->ntypes + a]) return fail(AZP_ERR_INVALID, m);
+    }
+    if (!c->use_lambda) m->gamma.assign(c->gamma, c->gamma + c->ntypes);
+    else m->gamma.assign(c->ntypes, 0.0);
+    const char* env_tpp = std::getenv("AZP_TPP");
+    m->tpp = env_tpp ? std::atoi(env_tpp) : 1;
+    if (!(m->tpp == 1 || m->tpp == 2 || m->tpp == 4 || m->tpp == 8 || m->tpp == 16 || m->tpp == 32)) m->tpp = 1;
+    const char* env_graph = std::getenv("AZP_GRAPHS");
+    m->use_graphs = !(env_graph && env_graph[0] == '0');
+
+    const uint32_t N = c->N;
+    int st = AZP_OK;
+#define CTRY(call)                                                  \
+    do {                                                            \
+        const cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return fail(record_cuda_error(e_, #call), m); \
+    } while (0)
+#define ALLOC(p, n) \
+    do {            \
+        st = dalloc(&(p), (n)); \
+        if (st) return fail(st, m); \
+    } while (0)
+    ALLOC(m->pos[0], N);
+    ALLOC(m->pos[1], N);
+    ALLOC(m->fix[0], N);
+    ALLOC(m->fix[1], N);
+    ALLOC(m->fix_build, N);
+    ALLOC(m->vel, N);
+    ALLOC(m->accel, (size_t)3 * N);
+    ALLOC(m->image, (size_t)3 * N);
+    ALLOC(m->tag, N);
+    ALLOC(m->rtag, N);
+    if (c->use_lambda) {
+        ALLOC(m->diam, N);
+        ALLOC(m->t_diam, N);
+    }
+    ALLOC(m->t_pos, N);
+    ALLOC(m->t_vel, N);
+    ALLOC(m->t_accel, (size_t)3 * N);
+    ALLOC(m->t_image, (size_t)3 * N);
+    ALLOC(m->t_tag, N);
+    ALLOC(m->t_cell, N);
+    ALLOC(m->cell_of, N);
+    ALLOC(m->slot, N);
+    ALLOC(m->members, N);
+    ALLOC(m->counts, N);
+    ALLOC(m->flags, 8);
+    ALLOC(m->d_ts, 1);
+    ALLOC(m->out_force, N);
+    ALLOC(m->out_virial, (size_t)6 * N);
+    ALLOC(m->tmp4, N);
+    ALLOC(m->tmpd, (size_t)6 * N);
+    ALLOC(m->partials, (size_t)8 * (blocks_for(N, THERMO_BLOCK) + 1));
+    ALLOC(m->thermo, 8);
+    ALLOC(m->d_gamma, c->ntypes);
+    CTRY(cudaMemset(m->flags, 0, sizeof(uint32_t) * 8));
+    CTRY(cudaMemcpy(m->d_gamma, m->gamma.data(), sizeof(double) * c->ntypes, cudaMemcpyHostToDevice));
+    // pair table + list thresholds + cell grid
+    if (m->pair_kind >= 0) {
+        std::vector<double> table((size_t)nt2 * PAIR_TBL);
+        st = build_pair_table(m->pair_kind, m->pair_params.data(), m->r_cut.data(), m->r_on.data(), m->shift_mode,
+                              c->ntypes, table.data());
+        if (st) return fail(st, m);
+        ALLOC(m->d_pair_table, table.size());
+        CTRY(cudaMemcpy(m->d_pair_table, table.data(), sizeof(double) * table.size(), cudaMemcpyHostToDevice));
+        std::vector<ListCut> cuts(nt2);
+        make_list_cuts(m->r_cut.data(), c->ntypes, m->r_buff, m->box, cuts.data(), &m->rlist_max);
+        for (int d = 0; d < 3; ++d)
+            if (m->rlist_max > 0.0 && m->box.L[d] < 2.0 * m->rlist_max) return fail(AZP_ERR_BOX_TOO_SMALL, m);
+        ALLOC(m->cuts, nt2);
+        CTRY(cudaMemcpy(m->cuts, cuts.data(), sizeof(ListCut) * nt2, cudaMemcpyHostToDevice));
+        m->max_nn = 32;
+        ALLOC(m->nbrs, (size_t)N * m->max_nn);
+    }
+    m->grid = make_grid(m->box, m->rlist_max > 0.0 ? m->rlist_max : std::max(m->box.L[0], 1.0));
+    ALLOC(m->cell_count, m->grid.ncell);
+    ALLOC(m->cell_start, (size_t)m->grid.ncell + 1);
+    ALLOC(m->scan_tmp, scan_tmp_words(m->grid.ncell));
+    // bonds: tag-order master table
+    if (m->bond_kind >= 0) {
+        if (!c->bonds || !c->bond_types || !c->bond_params || c->nbondtypes == 0 ||
+            c->nbondtypes > MD_MAX_BOND_TYPES)
+            return fail(AZP_ERR_INVALID, m);
+        m->nbt = c->nbondtypes;
+        m->bond_params.assign(c->bond_params, c->bond_params + (size_t)c->nbondtypes * AZP_BOND_PARAM_DOUBLES);
+        std::vector<uint32_t> n(N, 0);
+        for (uint32_t b = 0; b < c->nbonds; ++b) {
+            const uint32_t x = c->bonds[2 * b], y = c->bonds[2 * b + 1];
+            if (x >= N || y >= N || x == y || c->bond_types[b] >= c->nbondtypes) return fail(AZP_ERR_INVALID, m);
+            n[x]++;
+            n[y]++;
+        }
+        uint32_t w = 0;
+        for (uint32_t i = 0; i < N; ++i) w = std::max(w, n[i]);
+        m->bt_width = w;
+        std::vector<uint32_t> partner((size_t)w * N, 0), btype((size_t)w * N, 0), fill(N, 0);
+        for (uint32_t b = 0; b < c->nbonds; ++b) {
+            const uint32_t x = c->bonds[2 * b], y = c->bonds[2 * b + 1], t = c->bond_types[b];
+            partner[(size_t)fill[x] * N + x] = y;
+            btype[(size_t)fill[x] * N + x] = t;
+            fill[x]++;
+            partner[(size_t)fill[y] * N + y] = x;
+            btype[(size_t)fill[y] * N + y] = t;
+            fill[y]++;
+        }
+        ALLOC(m->bt_n_tag, N);
+        ALLOC(m->bt_partner_tag, (size_t)w * N);
+        ALLOC(m->bt_type_tag, (size_t)w * N);
+        ALLOC(m->bt_n, N);
+        ALLOC(m->bt, (size_t)w * N);
+        ALLOC(m->d_bond_params, m->bond_params.size());
+        if (m->exclude_bonds) {
+            ALLOC(m->ex_n, N);
+            ALLOC(m->ex_idx, (size_t)w * N);
+        }
+        CTRY(cudaMemcpy(m->bt_n_tag, n.data(), sizeof(uint32_t) * N, cudaMemcpyHostToDevice));
+        CTRY(cudaMemcpy(m->bt_partner_tag, partner.data(), sizeof(uint32_t) * partner.size(),
+                                cudaMemcpyHostToDevice));
+        CTRY(cudaMemcpy(m->bt_type_tag, btype.data(), sizeof(uint32_t) * btype.size(), cudaMemcpyHostToDevice));
+        CTRY(cudaMemcpy(m->d_bond_params, m->bond_params.data(), sizeof(double) * m->bond_params.size(),
+                                cudaMemcpyHostToDevice));
+    }
+    CTRY(cudaStreamCreateWithFlags(&m->graph_stream, cudaStreamNonBlocking));
+#undef ALLOC
+#undef CTRY
+    if (status) *status = AZP_OK;
+    return m;
+}
+
+void azp_md_destroy(azp_md* m)
+{
+    if (!m) return;
+    free_all(m);
+    if (m->graph_stream) cudaStreamDestroy(m->graph_stream);
+    delete m;
+}
+
+int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const double* accel, const int32_t* image,
+                     const double* diameter, uint64_t timestep, int on_device, void* stream)
+{
+    if (!m || !pos || !vel) return AZP_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    const uint32_t N = m->N;
+    if (N == 0) return AZP_OK;
+    const double *dp = pos, *dv = vel, *da = accel, *dd = diameter;
+    const int* di = image;
+    std::vector<void*> tmp;
+    if (!on_device) {
+        auto up = [&](const void* h, size_t bytes) -> void* {
+            if (!h) return nullptr;
+            void* d = nullptr;
+            if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
+            cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s);
+            tmp.push_back(d);
+            return d;
+        };
+        dp = (const double*)up(pos, sizeof(double) * 4 * N);
+        dv = (const double*)up(vel, sizeof(double) * 4 * N);
+        da = (const double*)up(accel, sizeof(double) * 3 * N);
+        di = (const int*)up(image, sizeof(int) * 3 * N);
+        dd = (const double*)up(diameter, sizeof(double) * N);
+        if (!dp || !dv) {
+            for (void* p : tmp) cudaFree(p);
+            return AZP_ERR_CUDA;
+        }
+    }
+    m->cur = 0;
+    k_load_state<<<blocks_for(N, 256), 256, 0, s>>>(dp, dv, da, di, dd, N, m->pos[0], m->vel, m->accel, m->image,
+                                                     m->diam, m->tag, m->rtag);
+    AZP_CHECK_LAUNCH("k_load_state");
+    m->timestep = timestep;
+    const unsigned long long ts = timestep;
+    AZP_CUDA_TRY(cudaMemcpyAsync(m->d_ts, &ts, sizeof(ts), cudaMemcpyHostToDevice, s));
+    AZP_CUDA_TRY(cudaMemsetAsync(m->flags, 0, sizeof(uint32_t) * 8, s));
+    int st = size_list(m, s);  // unconditional first rebuild (sorts the particles)
+    if (st == AZP_OK && m->pair_kind < 0) {
+        const uint32_t one = 1u;
+        AZP_CUDA_TRY(cudaMemcpyAsync(m->flags, &one, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        st = enqueue_rebuild(m, s, nullptr);
+    }
+    AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    for (void* p : tmp) cudaFree(p);
+    if (st) return st;
+    if (!accel && m->method == AZP_METHOD_LANGEVIN_FLOW) {
+        // HOOMD starts a run from a = F / m when no acceleration is known
+        MDArgs a = base_args(m);
+        a.out = 1;
+        st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
+        if (st) return st;
+        k_accel_from_force<<<blocks_for(N, 256), 256, 0, s>>>(m->out_force, m->vel, m->accel, N);
+        AZP_CHECK_LAUNCH("k_accel_from_force");
+    }
+    m->have_state = true;
+    return check_errors(m, s);
+}
+
+int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t* image, uint64_t* timestep,
+                     int on_device, void* stream)
+{
+    if (!m || !m->have_state) return AZP_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    const uint32_t N = m->N;
+    if (timestep) {
+        unsigned long long ts = 0;
+        AZP_CUDA_TRY(cudaMemcpyAsync(&ts, m->d_ts, sizeof(ts), cudaMemcpyDeviceToHost, s));
+        AZP_CUDA_TRY(cudaStreamSynchronize(s));
+        *timestep = ts;
+    }
+    if (N == 0) return AZP_OK;
+    if (on_device) {
+        k_store_state<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[m->cur], m->vel, m->accel, m->image, m->tag, N, pos,
+                                                          vel, accel, image);
+        AZP_CHECK_LAUNCH("k_store_state");
+        return AZP_OK;
+    }
+    double *dp = nullptr, *dv = nullptr, *da = nullptr;
+    int* di = nullptr;
+    if (pos) AZP_CUDA_TRY(cudaMalloc(&dp, sizeof(double) * 4 * N));
+    if (vel) AZP_CUDA_TRY(cudaMalloc(&dv, sizeof(double) * 4 * N));
+    if (accel) AZP_CUDA_TRY(cudaMalloc(&da, sizeof(double) * 3 * N));
+    if (image) AZP_CUDA_TRY(cudaMalloc(&di, sizeof(int) * 3 * N));
+    k_store_state<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[m->cur], m->vel, m->accel, m->image, m->tag, N, dp, dv,
+                                                      da, di);
+    AZP_CHECK_LAUNCH("k_store_state");
+    if (pos) AZP_CUDA_TRY(cudaMemcpyAsync(pos, dp, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, s));
+    if (vel) AZP_CUDA_TRY(cudaMemcpyAsync(vel, dv, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, s));
+    if (accel) AZP_CUDA_TRY(cudaMemcpyAsync(accel, da, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
+    if (image) AZP_CUDA_TRY(cudaMemcpyAsync(image, di, sizeof(int) * 3 * N, cudaMemcpyDeviceToHost, s));
+    AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    cudaFree(dp);
+    cudaFree(dv);
+    cudaFree(da);
+    cudaFree(di);
+    return AZP_OK;
+}
+
+int azp_md_run(azp_md* m, uint64_t steps, void* stream)
+{
+    if (!m || !m->have_state) return AZP_ERR_INVALID;
+    m->launches = 0;
+    if (steps == 0 || m->N == 0) return AZP_OK;
+    cudaStream_t s = as_stream(stream);
+    const int integ = m->method == AZP_METHOD_BROWNIAN_FLOW ? MD_INTEG_BROWNIAN : MD_INTEG_LANGEVIN;
+    int st = AZP_OK;
+    // Langevin: step one opens the run, the last step closes it without one
+    uint64_t mid = integ == MD_INTEG_LANGEVIN ? steps - 1 : steps;
+    if (integ == MD_INTEG_LANGEVIN) {
+        st = enqueue_step1(m, s);
+        if (st) return st;
+    }
+    if (m->use_graphs && mid >= 2) {
+        for (int p = 0; p < 2; ++p)
+            if (!m->gexec[p]) {
+                st = build_pair_graph(m, p, integ, &m->gexec[p]);
+                if (st) return st;
+            }
+        while (mid >= 2) {
+            AZP_CUDA_TRY(cudaGraphLaunch(m->gexec[m->cur], s));
+            m->launches += 3;  // arm + two step kernels (+ rebuild bodies when armed)
+            mid -= 2;
+        }
+    }
+    while (mid > 0) {
+        st = enqueue_rebuild(m, s, m->flags);
+        if (st) return st;
+        st = enqueue_step(m, integ, 1, 0, s, 0, 0);
+        if (st) return st;
+        m->cur ^= 1;
+        --mid;
+    }
+    if (integ == MD_INTEG_LANGEVIN) {
+        st = enqueue_rebuild(m, s, m->flags);
+        if (st) return st;
+        st = enqueue_step(m, integ, 0, 1, s, 0, 0);
+        if (st) return st;
+    }
+    m->timestep += steps;
+    return AZP_OK;
+}
+
+int azp_md_forces(azp_md* m, double* force, double* virial, int on_device, void* stream)
+{
+    if (!m || !m->have_state) return AZP_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    const uint32_t N = m->N;
+    if (N == 0) return AZP_OK;
+    int st = enqueue_rebuild(m, s, m->flags);
+    if (st) return st;
+    MDArgs a = base_args(m);
+    a.out = 1;
+    st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
+    if (st) return st;
+    k_to_tag_order4<<<blocks_for(N, 256), 256, 0, s>>>(m->out_force, m->tag, N, m->tmp4);
+    k_to_tag_order_n<<<blocks_for(N, 256), 256, 0, s>>>(m->out_virial, m->tag, N, 6, 1, m->tmpd);
+    AZP_CHECK_LAUNCH("azp_md_forces");
+    const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (force) AZP_CUDA_TRY(cudaMemcpyAsync(force, m->tmp4, sizeof(double) * 4 * N, k, s));
+    if (virial) AZP_CUDA_TRY(cudaMemcpyAsync(virial, m->tmpd, sizeof(double) * 6 * N, k, s));
+    if (!on_device) AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    return check_errors(m, s);
+}
+
+int azp_md_thermo(azp_md* m, double* out, void* stream)
+{
+    if (!m || !m->have_state || !out) return AZP_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    const uint32_t N = m->N;
+    for (int c = 0; c < 9; ++c) out[c] = 0.0;
+    if (N == 0) return AZP_OK;
+    int st = enqueue_rebuild(m, s, m->flags);
+    if (st) return st;
+    MDArgs a = base_args(m);
+    a.out = 1;
+    st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
+    if (st) return st;
+    const uint32_t nb = blocks_for(N, THERMO_BLOCK);
+    k_thermo_partials<<<nb, THERMO_BLOCK, 0, s>>>(m->out_force, m->out_virial, m->vel, N, m->partials);
+    k_thermo_final<<<1, 32, 0, s>>>(m->partials, nb, m->thermo);
+    AZP_CHECK_LAUNCH("azp_md_thermo");
+    double h[8];
+    uint32_t f[8];
+    AZP_CUDA_TRY(cudaMemcpyAsync(h, m->thermo, sizeof(h), cudaMemcpyDeviceToHost, s));
+    AZP_CUDA_TRY(cudaMemcpyAsync(f, m->flags, sizeof(f), cudaMemcpyDeviceToHost, s));
+    AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int c = 0; c < 8; ++c) out[c] = h[c];
+    out[8] = (double)f[2];
+    return check_errors(m, s);
+}
+
+int azp_md_error(azp_md* m, uint32_t* err_word, void* stream)
+{
+    if (!m || !err_word) return AZP_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    uint32_t f[8];
+    AZP_CUDA_TRY(cudaMemcpyAsync(f, m->flags, sizeof(f), cudaMemcpyDeviceToHost, s));
+    AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    uint32_t e = f[1];
+    if (f[3] > m->max_nn) e |= AZP_EBIT_NLIST_OVERFLOW;
+    *err_word = e;
+    return AZP_OK;
+}
+
+uint64_t azp_md_last_launches(const azp_md* m) { return m ? m->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+// engine.cuh -- device side of the resident MD engine (azp_md).
+#pragma once
+
+#include "common.cuh"
+#include "integrate.cuh"
+
+namespace azp
+{
+// MODE bits of the fused step kernel
+
+struct MDArgs {
+    const double4_32a* pos;     // current positions
+    double4_32a* pos_next;      // written when integrating
+    const uint4* fix;           // fixed-point shadow of pos
+    uint4* fix_next;
+    const uint4* fix_build;     // shadow at the last list build
+    double4_32a* vel;
+    double* accel;              // [N][3]
+    int* image;                 // [N][3]
+    const uint32_t* tag;
+    const double* diameter;
+    uint32_t N, ntypes;
+    double L[3], Linv[3], lo[3], hi[3];
+    float sfix[3];
+    // pair
+    const uint32_t* counts;
+    const uint32_t* nbrs;
+    const double* pair_table;   // [ntypes^2][12]
+    // bonds (index order)
+    const uint32_t* bt_n;
+    const uint2* bt;
+    const double* bond_params;
+    uint32_t nbondtypes;
+    // integrator
+    double dt, kT;
+    const unsigned long long* d_timestep;
+    uint32_t seed;
+    int noiseless;
+    const double* gamma;
+    int use_lambda;
+    double lambda;
+    FlowD flow;
+    double max_disp;
+    float disp_thresh2;         // (r_buff / 2)^2, slightly reduced
+    uint32_t* flags;            // [0] rebuild request, [1] error bits, [2] builds, [4] ticket
+    unsigned long long* d_timestep_rw;
+    // outputs (M_OUT / M_FORCES)
+    double4_32a* out_force;     // fx, fy, fz, energy
+    double* out_virial;         // [6][N]
+    // graph conditional of the next rebuild (set_cond == 0: none)
+    cudaGraphConditionalHandle next_cond;
+    int set_cond;
+    int next;                   // Langevin: also do step one of the next timestep
+    int out;                    // write out_force / out_virial
+    int tpp;                    // threads per particle (1, 2, 4, 8, 16, 32)
+};
+
+constexpr int MD_INTEG_LANGEVIN = 0;
+constexpr int MD_INTEG_BROWNIAN = 1;
+constexpr int MD_FORCES_ONLY = 2;
+
+// one launcher per pair evaluator (engine_<pair>.cu); pair_kind -1 = no pair force
+int launch_md_step(int pair_kind, int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s);
+
+}  // namespace azp

@@ -1,0 +1,391 @@
+// engine_kernels.cuh -- the fused force-and-integrate step of the resident engine.
+//
+// One launch per timestep: pair forces over the column-major list + bond forces
+// from the per-particle table (TPP threads per particle, warp-shuffle reduction),
+// then, by the group's first lane, Langevin step two at timestep t followed by
+// step one of timestep t + 1 (or the Brownian move at t), writing the next
+// position buffer and its fixed-point shadow, and the list-rebuild request.
+// Arithmetic of each phase follows the standalone kernels (pair.cu, bond.cu,
+// integrate.cu) and through them the reference lines cited there.
+#pragma once
+
+#include "engine.cuh"
+#include "evaluators.cuh"
+#include "pair.cuh"
+
+namespace azp
+{
+constexpr int MD_BLOCK = 256;
+constexpr uint32_t MD_MAX_BOND_TYPES = 32;
+
+struct NoPair {
+    static constexpr int SHIFT_SLOT = 7;
+    template<typename R> AZP_HD static bool enabled(const R*) { return false; }
+    template<typename R> AZP_HD static void eval(const R*, R, R& f, R& e) { f = e = R(0); }
+};
+struct NoBond {
+    template<typename R> AZP_HD static bool eval(const R*, R, R& f, R& e)
+    {
+        f = e = R(0);
+        return true;
+    }
+};
+
+// accumulator: compensated force / energy in FP32, plain in FP64
+template<typename R> struct Acc;
+template<> struct Acc<double> {
+    double fx = 0, fy = 0, fz = 0, u = 0, w[6] = {0, 0, 0, 0, 0, 0};
+    AZP_D void add(double dx, double dy, double dz, double fdr, double e, bool vir)
+    {
+        fx += dx * fdr;
+        fy += dy * fdr;
+        fz += dz * fdr;
+        u += 0.5 * e;
+        if (vir) {
+            const double h = 0.5 * fdr;
+            w[0] += h * dx * dx;
+            w[1] += h * dx * dy;
+            w[2] += h * dx * dz;
+            w[3] += h * dy * dy;
+            w[4] += h * dy * dz;
+            w[5] += h * dz * dz;
+        }
+    }
+    AZP_D void reduce(int tpp, bool vir)
+    {
+        for (int m = tpp >> 1; m > 0; m >>= 1) {
+            fx += __shfl_xor_sync(0xffffffffu, fx, m);
+            fy += __shfl_xor_sync(0xffffffffu, fy, m);
+            fz += __shfl_xor_sync(0xffffffffu, fz, m);
+            u += __shfl_xor_sync(0xffffffffu, u, m);
+            if (vir)
+                for (int c = 0; c < 6; ++c) w[c] += __shfl_xor_sync(0xffffffffu, w[c], m);
+        }
+    }
+    AZP_D double Fx() const { return fx; }
+    AZP_D double Fy() const { return fy; }
+    AZP_D double Fz() const { return fz; }
+    AZP_D double U() const { return u; }
+};
+template<> struct Acc<float> {
+    Comp fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f}, u{0.f, 0.f};
+    float w[6] = {0, 0, 0, 0, 0, 0};
+    AZP_D void add(float dx, float dy, float dz, float fdr, float e, bool vir)
+    {
+        fx.add(dx * fdr);
+        fy.add(dy * fdr);
+        fz.add(dz * fdr);
+        u.add(0.5f * e);
+        if (vir) {
+            const float h = 0.5f * fdr;
+            w[0] += h * dx * dx;
+            w[1] += h * dx * dy;
+            w[2] += h * dx * dz;
+            w[3] += h * dy * dy;
+            w[4] += h * dy * dz;
+            w[5] += h * dz * dz;
+        }
+    }
+    AZP_D static void comb(Comp& c, int m)
+    {
+        const float s2 = __shfl_xor_sync(0xffffffffu, c.s, m);
+        const float c2 = __shfl_xor_sync(0xffffffffu, c.c, m);
+        c.add(s2);
+        c.c += c2;
+    }
+    AZP_D void reduce(int tpp, bool vir)
+    {
+        for (int m = tpp >> 1; m > 0; m >>= 1) {
+            comb(fx, m);
+            comb(fy, m);
+            comb(fz, m);
+            comb(u, m);
+            if (vir)
+                for (int c = 0; c < 6; ++c) w[c] += __shfl_xor_sync(0xffffffffu, w[c], m);
+        }
+    }
+    // sum and carry converted separately: the FP64 result keeps the compensation
+    AZP_D double Fx() const { return (double)fx.s + (double)fx.c; }
+    AZP_D double Fy() const { return (double)fy.s + (double)fy.c; }
+    AZP_D double Fz() const { return (double)fz.s + (double)fz.c; }
+    AZP_D double U() const { return (double)u.s + (double)u.c; }
+};
+
+template<typename R> AZP_D size_t md_smem_bytes(uint32_t ntypes, uint32_t nbt)
+{
+    const size_t nt2 = (size_t)ntypes * ntypes;
+    return nt2 * sizeof(double) + ntypes * sizeof(double) + nt2 * PAIR_TBL * sizeof(R) +
+           (size_t)nbt * AZP_BOND_PARAM_DOUBLES * sizeof(R);
+}
+
+template<class PE, class BE, typename R, int INTEG>
+__global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const uint32_t nt2 = a.ntypes * a.ntypes;
+    double* s_rc2 = reinterpret_cast<double*>(smem_raw);
+    double* s_gamma = s_rc2 + nt2;
+    R* s_rec = reinterpret_cast<R*>(s_gamma + a.ntypes);
+    R* s_bond = s_rec + nt2 * PAIR_TBL;
+    if (!std::is_same<PE, NoPair>::value)
+        for (uint32_t t = threadIdx.x; t < nt2 * PAIR_TBL; t += blockDim.x) {
+            s_rec[t] = (R)a.pair_table[t];
+            if (t % PAIR_TBL == PAIR_REC) s_rc2[t / PAIR_TBL] = a.pair_table[t];
+        }
+    if (!std::is_same<BE, NoBond>::value)
+        for (uint32_t t = threadIdx.x; t < a.nbondtypes * AZP_BOND_PARAM_DOUBLES; t += blockDim.x)
+            s_bond[t] = (R)a.bond_params[t];
+    if (INTEG != MD_FORCES_ONLY && !a.use_lambda)
+        for (uint32_t t = threadIdx.x; t < a.ntypes; t += blockDim.x) s_gamma[t] = a.gamma[t];
+    __syncthreads();
+
+    const int tpp = a.tpp;
+    const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = gid / tpp;
+    const uint32_t sub = gid % tpp;
+    const bool active = i < a.N;
+    const bool vir = a.out != 0;
+    Acc<R> acc;
+    if (active) {
+        // ---------------------------------------------------------------- pair
+        if constexpr (!std::is_same<PE, NoPair>::value) {
+            const uint32_t n = a.counts[i];
+            if constexpr (std::is_same<R, double>::value) {
+                const double4_32a pi = a.pos[i];
+                const uint32_t ti = type_of(pi.w);
+                for (uint32_t k = sub; k < n; k += tpp) {
+                    const uint32_t j = a.nbrs[(size_t)k * a.N + i];
+                    const double4_32a pj = a.pos[j];
+                    const double dx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
+                    const double dy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
+                    const double dz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
+                    const double rsq = rsq_exact(dx, dy, dz);
+                    const uint32_t tp = ti * a.ntypes + type_of(pj.w);
+                    const R* rec = s_rec + (size_t)tp * PAIR_TBL;
+                    const R* cut = rec + PAIR_REC;
+                    if (!(rsq < cut[0]) || !PE::enabled(rec)) continue;
+                    R fdr, e;
+                    PE::eval(rec, rsq, fdr, e);
+                    e -= rec[PE::SHIFT_SLOT];
+                    xplor(cut, rsq, fdr, e);
+                    acc.add(dx, dy, dz, fdr, e, vir);
+                }
+            } else {
+                const uint4 fi = a.fix[i];
+                const uint32_t ti = fi.w;
+                for (uint32_t k = sub; k < n; k += tpp) {
+                    const uint32_t j = a.nbrs[(size_t)k * a.N + i];
+                    const uint4 fj = a.fix[j];
+                    const float dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
+                    const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
+                    const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
+                    const float rsq = dx * dx + dy * dy + dz * dz;
+                    const uint32_t tp = ti * a.ntypes + fj.w;
+                    const R* rec = s_rec + (size_t)tp * PAIR_TBL;
+                    const R* cut = rec + PAIR_REC;
+                    const float rc2 = cut[0];
+                    if (rsq >= rc2 * 1.000004f || !PE::enabled(rec)) continue;
+                    if (rsq >= rc2 * 0.999996f) {
+                        const double4_32a pi = a.pos[i];
+                        const double4_32a pj = a.pos[j];
+                        const double vx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
+                        const double vy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
+                        const double vz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
+                        if (!(rsq_exact(vx, vy, vz) < s_rc2[tp])) continue;
+                    }
+                    R fdr, e;
+                    PE::eval(rec, rsq, fdr, e);
+                    e -= rec[PE::SHIFT_SLOT];
+                    xplor(cut, rsq, fdr, e);
+                    acc.add(dx, dy, dz, fdr, e, vir);
+                }
+            }
+        }
+        // ---------------------------------------------------------------- bonds
+        if constexpr (!std::is_same<BE, NoBond>::value) {
+            const uint32_t nb = a.bt_n[i];
+            for (uint32_t k = sub; k < nb; k += tpp) {
+                const uint2 e2 = a.bt[(size_t)k * a.N + i];
+                R dx, dy, dz, rsq;
+                if constexpr (std::is_same<R, double>::value) {
+                    const double4_32a pi = a.pos[i];
+                    const double4_32a pj = a.pos[e2.x];
+                    dx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
+                    dy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
+                    dz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
+                    rsq = rsq_exact(dx, dy, dz);
+                } else {
+                    const uint4 fi = a.fix[i];
+                    const uint4 fj = a.fix[e2.x];
+                    dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
+                    dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
+                    dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
+                    rsq = dx * dx + dy * dy + dz * dz;
+                }
+                R fdr, en;
+                if (!BE::eval(s_bond + e2.y * AZP_BOND_PARAM_DOUBLES, rsq, fdr, en)) {
+                    atomicOr(&a.flags[1], AZP_EBIT_BOND);
+                    continue;
+                }
+                acc.add(dx, dy, dz, fdr, en, vir);
+            }
+        }
+    }
+    if (tpp > 1) acc.reduce(tpp, vir);
+
+    bool want_rebuild = false;
+    if (active && sub == 0) {
+        const double Fx = acc.Fx(), Fy = acc.Fy(), Fz = acc.Fz();
+        if (a.out) {
+            a.out_force[i] = make_double4_32a(Fx, Fy, Fz, acc.U());
+            for (int c = 0; c < 6; ++c) a.out_virial[(size_t)c * a.N + i] = (double)acc.w[c];
+        }
+        if constexpr (INTEG != MD_FORCES_ONLY) {
+            const unsigned long long ts = *a.d_timestep;
+            double4_32a p = a.pos[i];
+            const double gam = a.use_lambda ? a.lambda * a.diameter[i] : s_gamma[type_of(p.w)];
+            double ux, uy, uz;
+            flow_at(a.flow, p.y, ux, uy, uz);
+            const double c = a.noiseless ? 0.0 : sqrt(6.0 * gam * a.kT / a.dt);
+            const uint32_t tg = a.tag[i];
+            double r0, r1, r2;
+            bool moved = false;
+            if constexpr (INTEG == MD_INTEG_LANGEVIN) {
+                uniform3(AZP_RNG_LANGEVIN_FLOW, ts, a.seed, tg, -c, c - (-c), r0, r1, r2);
+                double4_32a v = a.vel[i];
+                const double minv = 1.0 / v.w;
+                const double ax = (Fx + (r0 - gam * (v.x - ux))) * minv;
+                const double ay = (Fy + (r1 - gam * (v.y - uy))) * minv;
+                const double az = (Fz + (r2 - gam * (v.z - uz))) * minv;
+                const double h = 0.5 * a.dt;
+                v.x += h * ax;
+                v.y += h * ay;
+                v.z += h * az;
+                if (a.next) {
+                    // step one of the next timestep with the acceleration just computed
+                    p.x += (v.x + h * ax) * a.dt;
+                    p.y += (v.y + h * ay) * a.dt;
+                    p.z += (v.z + h * az) * a.dt;
+                    v.x += h * ax;
+                    v.y += h * ay;
+                    v.z += h * az;
+                    moved = true;
+                } else {
+                    a.accel[3 * i] = ax;
+                    a.accel[3 * i + 1] = ay;
+                    a.accel[3 * i + 2] = az;
+                }
+                a.vel[i] = v;
+            } else {
+                uniform3(AZP_RNG_BROWNIAN_FLOW, ts, a.seed, tg, -c, c - (-c), r0, r1, r2);
+                double dx = (ux + (Fx + r0) / gam) * a.dt;
+                double dy = (uy + (Fy + r1) / gam) * a.dt;
+                double dz = (uz + (Fz + r2) / gam) * a.dt;
+                if (a.max_disp > 0.0) {
+                    dx = fmin(fmax(dx, -a.max_disp), a.max_disp);
+                    dy = fmin(fmax(dy, -a.max_disp), a.max_disp);
+                    dz = fmin(fmax(dz, -a.max_disp), a.max_disp);
+                }
+                p.x += dx;
+                p.y += dy;
+                p.z += dz;
+                moved = true;
+            }
+            if (moved) {
+                int wx = 0, wy = 0, wz = 0;
+                wrap1(p.x, wx, a.L[0], a.lo[0], a.hi[0]);
+                wrap1(p.y, wy, a.L[1], a.lo[1], a.hi[1]);
+                wrap1(p.z, wz, a.L[2], a.lo[2], a.hi[2]);
+                if (wx | wy | wz) {
+                    a.image[3 * i] += wx;
+                    a.image[3 * i + 1] += wy;
+                    a.image[3 * i + 2] += wz;
+                }
+                a.pos_next[i] = p;
+                uint4 f;
+                f.x = to_fixed(p.x, a.Linv[0]);
+                f.y = to_fixed(p.y, a.Linv[1]);
+                f.z = to_fixed(p.z, a.Linv[2]);
+                f.w = type_of(p.w);
+                a.fix_next[i] = f;
+                const uint4 fb = a.fix_build[i];
+                const float ddx = (float)(int32_t)(f.x - fb.x) * a.sfix[0];
+                const float ddy = (float)(int32_t)(f.y - fb.y) * a.sfix[1];
+                const float ddz = (float)(int32_t)(f.z - fb.z) * a.sfix[2];
+                want_rebuild = ddx * ddx + ddy * ddy + ddz * ddz > a.disp_thresh2;
+                if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(&a.flags[1], AZP_EBIT_NONFINITE);
+            }
+        }
+    }
+    if constexpr (INTEG != MD_FORCES_ONLY) {
+        if (__any_sync(0xffffffffu, want_rebuild) && (threadIdx.x & 31) == 0) atomicOr(&a.flags[0], 1u);
+        // the last block to finish advances the timestep and arms the next rebuild
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            const uint32_t t = atomicAdd(&a.flags[4], 1u);
+            if (t == gridDim.x - 1) {
+                __threadfence();
+                const uint32_t req = atomicAdd(&a.flags[0], 0u);
+                if (a.set_cond) cudaGraphSetConditional(a.next_cond, req ? 1u : 0u);
+                a.flags[4] = 0u;
+                *a.d_timestep_rw = *a.d_timestep_rw + 1ull;
+            }
+        }
+    }
+}
+
+template<class PE, class BE, typename R, int INTEG>
+int launch_md_t(const MDArgs& a, cudaStream_t s)
+{
+    const size_t threads = (size_t)a.N * a.tpp;
+    const uint32_t blocks = (uint32_t)((threads + MD_BLOCK - 1) / MD_BLOCK);
+    if (blocks == 0) return AZP_OK;
+    const size_t nt2 = (size_t)a.ntypes * a.ntypes;
+    const size_t smem = nt2 * sizeof(double) + a.ntypes * sizeof(double) + nt2 * PAIR_TBL * sizeof(R) +
+                        (size_t)a.nbondtypes * AZP_BOND_PARAM_DOUBLES * sizeof(R);
+    auto k = k_md_step<PE, BE, R, INTEG>;
+    if (smem > 48 * 1024) AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<blocks, MD_BLOCK, smem, s>>>(a);
+    AZP_CHECK_LAUNCH("k_md_step");
+    return AZP_OK;
+}
+
+template<class PE, class BE, typename R>
+int launch_md_integ(int integ, const MDArgs& a, cudaStream_t s)
+{
+    switch (integ) {
+    case MD_INTEG_LANGEVIN: return launch_md_t<PE, BE, R, MD_INTEG_LANGEVIN>(a, s);
+    case MD_INTEG_BROWNIAN: return launch_md_t<PE, BE, R, MD_INTEG_BROWNIAN>(a, s);
+    case MD_FORCES_ONLY: return launch_md_t<PE, BE, R, MD_FORCES_ONLY>(a, s);
+    default: return AZP_ERR_INVALID;
+    }
+}
+
+template<class PE>
+int launch_md_pe(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s)
+{
+    if (precision == AZP_FP32) {
+        switch (bond_kind) {
+        case -1: return launch_md_integ<PE, NoBond, float>(integ, a, s);
+        case AZP_BOND_QUARTIC: return launch_md_integ<PE, QuarticBond, float>(integ, a, s);
+        case AZP_BOND_DOUBLE_WELL: return launch_md_integ<PE, DoubleWellBond, float>(integ, a, s);
+        default: return AZP_ERR_INVALID;
+        }
+    }
+    switch (bond_kind) {
+    case -1: return launch_md_integ<PE, NoBond, double>(integ, a, s);
+    case AZP_BOND_QUARTIC: return launch_md_integ<PE, QuarticBond, double>(integ, a, s);
+    case AZP_BOND_DOUBLE_WELL: return launch_md_integ<PE, DoubleWellBond, double>(integ, a, s);
+    default: return AZP_ERR_INVALID;
+    }
+}
+
+// per-evaluator entry points, one per translation unit
+int launch_md_nopair(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s);
+int launch_md_plj(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s);
+int launch_md_eyuk(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s);
+int launch_md_hertz(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s);
+int launch_md_colloid(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s);
+
+}  // namespace azp

@@ -1,0 +1,11 @@
+// engine_plj.cu -- fused step kernels of the resident engine for pair evaluator
+// PerturbedLJ (one translation unit per evaluator so the instantiations compile in parallel).
+#include "engine_kernels.cuh"
+
+namespace azp
+{
+int launch_md_plj(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s)
+{
+    return launch_md_pe<PerturbedLJ>(bond_kind, precision, integ, a, s);
+}
+}  // namespace azp

@@ -1,0 +1,275 @@
+// evaluators.cuh -- azplugins pair and bond potentials as device functors,
+// templated on the arithmetic type (float for AZP_FP32, double for AZP_FP64).
+//
+// Each pair potential works on an 8-value "kernel record" derived on the host
+// from the reference's param_type fields (prepare_*), so per-pair work holds no
+// parameter arithmetic. The formulas are those of the reference evaluators:
+//   PerturbedLennardJones  src/PairEvaluatorPerturbedLennardJones.h:117-155
+//   ExpandedYukawa         src/PairEvaluatorExpandedYukawa.h:92-115
+//   Hertz                  src/PairEvaluatorHertz.h:93-110
+//   Colloid                src/PairEvaluatorColloid.h:101-269
+//   Quartic bond           src/BondEvaluatorQuartic.h:129-200
+//   DoubleWell bond        src/BondEvaluatorDoubleWell.h:96-113
+#pragma once
+
+#include "common.cuh"
+#include <math.h>
+#include <type_traits>
+
+namespace azp
+{
+constexpr int PAIR_REC = 8;   // values per pair kernel record
+constexpr int CUT_REC = 4;    // rcutsq, ronsq, 1/(rcutsq-ronsq)^3, xplor flag
+
+template<typename R> AZP_HD R rcp(R x) { return R(1) / x; }
+
+// ================================================================ pair potentials
+// Interface: enabled(rec) -- the reference's "lj1 != 0" / "epsilon != 0" test;
+// eval(rec, rsq, fdr, e) -- force/r and energy at rsq < rcutsq, unshifted.
+// The energy shift at r_cut is rec[SHIFT_SLOT], subtracted by the caller.
+
+struct PerturbedLJ {
+    // rec: lj1, lj2, lambda, rwcasq, wca_shift, 12 lj1, 6 lj2, (shift)
+    static constexpr int SHIFT_SLOT = 7;
+    AZP_HD static void prepare(const double* p, double* rec)
+    {
+        const double s6 = p[0], e4 = p[1], lam = p[2];
+        rec[0] = e4 * s6 * s6;
+        rec[1] = e4 * s6;
+        rec[2] = lam;
+        rec[3] = p[3];
+        rec[4] = e4 * (1.0 - lam) / 4.0;
+        rec[5] = 12.0 * rec[0];
+        rec[6] = 6.0 * rec[1];
+        rec[7] = 0.0;
+    }
+    template<typename R> AZP_HD static bool enabled(const R* rec) { return rec[0] != R(0); }
+    template<typename R> AZP_HD static void eval(const R* rec, R rsq, R& fdr, R& e)
+    {
+        const R r2inv = rcp(rsq);
+        const R r6inv = r2inv * r2inv * r2inv;
+        R f = r2inv * r6inv * (rec[5] * r6inv - rec[6]);
+        R u = r6inv * (rec[0] * r6inv - rec[1]);
+        if (rsq < rec[3]) {
+            u += rec[4];
+        } else {
+            f *= rec[2];
+            u *= rec[2];
+        }
+        fdr = f;
+        e = u;
+    }
+};
+
+struct ExpandedYukawa {
+    // rec: epsilon, kappa, delta, (shift)
+    static constexpr int SHIFT_SLOT = 3;
+    AZP_HD static void prepare(const double* p, double* rec)
+    {
+        rec[0] = p[0];
+        rec[1] = p[1];
+        rec[2] = p[2];
+        for (int k = 3; k < PAIR_REC; ++k) rec[k] = 0.0;
+    }
+    template<typename R> AZP_HD static bool enabled(const R* rec) { return rec[0] != R(0); }
+    template<typename R> AZP_HD static void eval(const R* rec, R rsq, R& fdr, R& e)
+    {
+        const R r = sqrt(rsq);
+        const R s = r - rec[2];
+        const R sinv = rcp(s);
+        const R u = rec[0] * exp(-rec[1] * s) * sinv;
+        fdr = u * (rec[1] + sinv) / r;
+        e = u;
+    }
+};
+
+struct Hertz {
+    // rec: epsilon, r_cut, (shift, never set: the reference has no shift branch)
+    static constexpr int SHIFT_SLOT = 7;
+    AZP_HD static void prepare(const double* p, double* rec)
+    {
+        rec[0] = p[0];
+        for (int k = 1; k < PAIR_REC; ++k) rec[k] = 0.0;
+    }
+    template<typename R> AZP_HD static bool enabled(const R* rec) { return rec[0] != R(0); }
+    template<typename R> AZP_HD static void eval(const R* rec, R rsq, R& fdr, R& e)
+    {
+        const R r = sqrt(rsq);
+        const R rc = rec[1];
+        const R x = R(1) - r / rc;
+        const R ex32 = rec[0] * x * sqrt(x);
+        fdr = R(2.5) * ex32 / (r * rc);
+        e = ex32 * x;
+    }
+};
+
+struct Colloid {
+    // rec: A, a_1, a_2, sigma^3, sigma^6, form (0 SS, 1 CS, 2 CC), max(a_1,a_2), (shift)
+    static constexpr int SHIFT_SLOT = 7;
+    AZP_HD static void prepare(const double* p, double* rec)
+    {
+        rec[0] = p[0];
+        rec[1] = p[1];
+        rec[2] = p[2];
+        rec[3] = p[3];
+        rec[4] = p[3] * p[3];
+        rec[5] = (p[1] == 0.0 && p[2] == 0.0) ? 0.0 : ((p[1] != 0.0 && p[2] != 0.0) ? 2.0 : 1.0);
+        rec[6] = p[1] > p[2] ? p[1] : p[2];
+        rec[7] = 0.0;
+    }
+    template<typename R> AZP_HD static bool enabled(const R* rec) { return rec[0] != R(0); }
+
+    template<typename R> AZP_HD static R inv7(R x)
+    {
+        const R xi = rcp(x);
+        R g = xi * xi;
+        g = g * g * g;
+        return g * xi;
+    }
+
+    template<typename R> AZP_HD static void eval(const R* rec, R rsq, R& fdr, R& e)
+    {
+        const R A = rec[0], s3 = rec[3], s6 = rec[4];
+        const int form = (int)rec[5];
+        if (form == 0) {
+            // integrated over no sphere: LJ with prefactor A/36
+            const R r2inv = rcp(rsq);
+            const R r6inv = r2inv * r2inv * r2inv;
+            const R c = A * s6 / R(36);
+            fdr = R(6) * c * r2inv * r6inv * (R(2) * s6 * r6inv - R(1));
+            e = c * r6inv * (s6 * r6inv - R(1));
+        } else if (form == 1) {
+            // point -- sphere of radius a
+            const R a = rec[6];
+            const R a2 = a * a;
+            const R d = a2 - rsq;
+            const R d3 = d * d * d;
+            const R d6 = d3 * d3;
+            const R r4 = rsq * rsq;
+            const R pre = s3 * A * a * a2 / d3;
+            const R poly = R(2) * (a2 + rsq) * (a2 * (R(5) * a2 + R(22) * rsq) + R(5) * r4);
+            fdr = R(4.0 / 15.0) * pre * (poly * s6 / d6 - R(5)) / d;
+            const R poly_e = a2 * (a2 * (a2 / R(3) + R(3) * rsq) + R(4.2) * r4) + rsq * r4;
+            e = R(2.0 / 9.0) * pre * (R(1) - poly_e * s6 / d6);
+        } else {
+            // sphere -- sphere (Everaers & Ejtehadi, PRE 67, 041710)
+            const R ai = rec[1], aj = rec[2];
+            const R r = sqrt(rsq);
+            const R prod = ai * aj, sum = ai + aj, dif = ai - aj;
+            const R sp = sum + r, sm = sum - r, dp = dif + r, dm = dif - r;
+            const R q7 = rcp(sp * sm);
+            const R q8 = rcp(dp * dm);
+            R g0 = inv7(sp), g1 = inv7(sm), g2 = inv7(dp), g3 = inv7(dm);
+            const R h0 = ((sp + R(5) * sum) * sp + R(30) * prod) * g0;
+            const R h1 = ((sm + R(5) * sum) * sm + R(30) * prod) * g1;
+            const R h2 = ((dp + R(5) * dif) * dp - R(30) * prod) * g2;
+            const R h3 = ((dm + R(5) * dif) * dm - R(30) * prod) * g3;
+            const R pre = A * s6 / r / R(37800);
+            R u = pre * (h0 - h1 - h2 + h3);
+            g0 *= R(42) * prod / sp + R(6) * sum + sp;
+            g1 *= R(42) * prod / sm + R(6) * sum + sm;
+            g2 *= R(-42) * prod / dp + R(6) * dif + dp;
+            g3 *= R(-42) * prod / dm + R(6) * dif + dm;
+            const R dur = u / r + R(5) * pre * (g0 + g1 - g2 - g3);
+            const R dua = -A / R(3) * r * ((R(2) * prod * q7 + R(1)) * q7 + (R(2) * prod * q8 - R(1)) * q8);
+            fdr = (dur + dua) / r;
+            u += A / R(6) * (R(2) * prod * (q7 + q8) - log(q8 / q7));
+            e = u;
+        }
+    }
+};
+
+// Host: fill the kernel record and cut record of one type pair.
+// p: the reference param_type (4 doubles); mode: azp_shift_mode.
+template<class Eval>
+AZP_HD void prepare_pair(const double* p, double rcut, double ron, int mode, double* rec, double* cut)
+{
+    Eval::prepare(p, rec);
+    const double rcutsq = rcut * rcut;
+    const double ronsq = ron * ron;
+    if (std::is_same<Eval, Hertz>::value) rec[1] = rcut;
+    cut[0] = rcutsq;
+    cut[1] = ronsq;
+    cut[2] = (mode == AZP_MODE_XPLOR && ronsq < rcutsq) ? 1.0 / ((rcutsq - ronsq) * (rcutsq - ronsq) * (rcutsq - ronsq)) : 0.0;
+    cut[3] = (mode == AZP_MODE_XPLOR && ronsq < rcutsq) ? 1.0 : 0.0;
+    const bool shift = (mode == AZP_MODE_SHIFT) || (mode == AZP_MODE_XPLOR && ronsq > rcutsq);
+    if (shift && rcut > 0.0 && Eval::enabled(rec) && !std::is_same<Eval, Hertz>::value) {
+        double f = 0.0, e = 0.0;
+        Eval::eval(rec, rcutsq, f, e);
+        rec[Eval::SHIFT_SLOT] = e;
+    }
+    if (!(rcut > 0.0)) cut[0] = 0.0;  // r_cut 0: the type pair is never evaluated
+}
+
+// XPLOR smoothing of (fdr, e) for ronsq <= rsq < rcutsq (HOOMD pair.Pair mode
+// "xplor"): S = (rc2 - r2)^2 (rc2 + 2 r2 - 3 ro2) / (rc2 - ro2)^3.
+template<typename R> AZP_HD void xplor(const R* cut, R rsq, R& fdr, R& e)
+{
+    if (cut[3] != R(0) && rsq >= cut[1]) {
+        const R a = rsq - cut[0];
+        const R s = a * a * (cut[0] + R(2) * rsq - R(3) * cut[1]) * cut[2];
+        const R dsdr_r = R(12) * (rsq - cut[1]) * a * cut[2];
+        fdr = s * fdr - dsdr_r * e;
+        e = e * s;
+    }
+}
+
+// ================================================================ bond potentials
+// rec = the reference param_type (8 doubles). eval returns false when the
+// evaluator refuses (the reference's "invalid parameters" returns).
+struct QuarticBond {
+    template<typename R> AZP_HD static bool eval(const R* p, R rsq, R& fdr, R& e)
+    {
+        const R k = p[0], r0 = p[1], b1 = p[2], b2 = p[3], U0 = p[4];
+        const R lj1 = p[6] * p[5] * p[5];
+        const R lj2 = p[6] * p[5];
+        const R del = p[7];
+        fdr = R(0);
+        e = R(0);
+        if (r0 == R(0)) return false;
+        R rr = R(1);
+        if (del == R(0)) {
+            const R r2inv = rcp(rsq);
+            const R r6inv = r2inv * r2inv * r2inv;
+            if (lj1 != R(0) && r6inv > (lj2 / lj1) / R(2)) {
+                fdr += r2inv * r6inv * (R(12) * lj1 * r6inv - R(6) * lj2);
+                e += r6inv * (lj1 * r6inv - lj2) + lj2 * lj2 / R(4) / lj1;
+            }
+            if (rsq < r0 * r0) rr = sqrt(rsq) - r0;
+        } else {
+            const R rs = sqrt(rsq) - del;
+            const R r2inv = R(1) / rs / rs;
+            const R r6inv = r2inv * r2inv * r2inv;
+            if (lj1 != R(0) && r6inv > (lj2 / lj1) / R(2)) {
+                fdr += r6inv * (R(12) * lj1 * r6inv - R(6) * lj2) / rs / (rs + del);
+                e += r6inv * (lj1 * r6inv - lj2) + p[6] / R(4);
+            }
+            if (rs < r0) rr = rs - r0;
+        }
+        if (rr < R(0)) {
+            fdr += -k * rr * (R(4) * rr * rr - R(3) * (b1 + b2) * rr + R(2) * b1 * b2) / (rr + r0 + del);
+            e += k * (rr - b1) * (rr - b2) * rr * rr + U0;
+        } else {
+            e += U0;
+        }
+        return true;
+    }
+};
+
+struct DoubleWellBond {
+    template<typename R> AZP_HD static bool eval(const R* p, R rsq, R& fdr, R& e)
+    {
+        const R r1 = p[0], rd = p[1], U1 = p[2], Ut = p[3];
+        fdr = R(0);
+        e = R(0);
+        if (rd == R(0)) return false;
+        const R r = sqrt(rsq);
+        const R x = (r1 - r) / rd;
+        const R y = R(1) - x * x;
+        e = U1 * y * y + Ut * (R(1) - x - y * y);
+        fdr = (R(4) * x * y * (Ut - U1) - Ut) / (rd * r);
+        return true;
+    }
+};
+
+}  // namespace azp

@@ -1,0 +1,500 @@
+// nlist.cu -- cell list and full neighbour list on the device, and the
+// standalone azp_nlist object of the C ABI (replaces HOOMD's
+// NeighborListGPUBinned + CellListGPU behind hoomd.md.nlist.Cell).
+//
+// Membership contract (oracle/azp_oracle.cpp, orc_nlist_*): j != i is listed for
+// i when r_cut(ti, tj) > 0, |min_image(x_i - x_j)|^2 < (r_cut + r_buff)^2 in FP64
+// with every product and sum rounded separately, and j is not excluded.
+// The FP64 test runs only for candidates whose FP32 fixed-point distance falls in
+// a narrow band around r_list; everything else is decided in FP32 with a margin
+// larger than its worst-case error, so the sets are bit-exact.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "celllist.cuh"
+#include "nlist_impl.cuh"
+#include "scan.cuh"
+
+namespace azp
+{
+// ---------------------------------------------------------------- host helpers
+CellGrid make_grid(const azp_box& box, double rlist_max)
+{
+    CellGrid g;
+    g.ncell = 1;
+    for (int d = 0; d < 3; ++d) {
+        int n = rlist_max > 0.0 ? (int)std::floor(box.L[d] / rlist_max) : 1;
+        if (n < 3) n = 1;
+        // keep the grid modest: at most 2^20 cells per axis product is plenty
+        if (n > 1024) n = 1024;
+        g.dim[d] = n;
+        g.reach[d] = n >= 3 ? 1 : 0;
+        g.lo[d] = -0.5 * box.L[d];
+        g.scale[d] = (double)n / box.L[d];
+        g.ncell *= (uint32_t)n;
+    }
+    return g;
+}
+
+void make_list_cuts(const double* r_cut, uint32_t ntypes, double r_buff, const azp_box& box, ListCut* out,
+                    double* rlist_max)
+{
+    double rmax = 0.0, rmin = 1e300;
+    for (uint32_t t = 0; t < ntypes * ntypes; ++t) {
+        if (r_cut[t] > 0.0) {
+            const double rl = r_cut[t] + r_buff;
+            rmax = std::max(rmax, rl);
+            rmin = std::min(rmin, rl);
+        }
+    }
+    const double Lmax = std::max(box.L[0], std::max(box.L[1], box.L[2]));
+    // worst-case relative error of the FP32 fixed-point rsq: float rounding of
+    // three components and their squares (< 1e-6) plus the fixed-point rounding
+    // of both positions (L 2^-33 each) against the smallest list radius.
+    double delta = 4e-6;
+    if (rmax > 0.0) delta = std::max(delta, 16.0 * Lmax * 2.3283064365386963e-10 / rmin);
+    for (uint32_t t = 0; t < ntypes * ntypes; ++t) {
+        ListCut c;
+        if (r_cut[t] > 0.0) {
+            const double rl = r_cut[t] + r_buff;
+            c.rlistsq = rl * rl;
+            c.lo = std::nextafter((float)(c.rlistsq * (1.0 - delta)), 0.0f);
+            c.hi = std::nextafter((float)(c.rlistsq * (1.0 + delta)), 1e30f);
+        } else {
+            c.rlistsq = 0.0;
+            c.lo = -1.0f;
+            c.hi = -1.0f;  // rsq_f >= hi always: never listed
+        }
+        c.pad = 0.0f;
+        out[t] = c;
+    }
+    *rlist_max = rmax;
+}
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_to_fixed(const double4_32a* __restrict__ pos, uint4* __restrict__ fixed, uint32_t N, double lx,
+                           double ly, double lz)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const double4_32a p = pos[i];
+    uint4 f;
+    f.x = to_fixed(p.x, lx);
+    f.y = to_fixed(p.y, ly);
+    f.z = to_fixed(p.z, lz);
+    f.w = type_of(p.w);
+    fixed[i] = f;
+}
+
+__device__ __forceinline__ int cell_coord(double x, double lo, double scale, int dim)
+{
+    int c = (int)floor((x - lo) * scale);
+    if (c < 0) c += dim;
+    if (c >= dim) c -= dim;
+    return min(max(c, 0), dim - 1);
+}
+
+__global__ void k_cell_assign(const double4_32a* __restrict__ pos, uint32_t N, CellGrid g, uint32_t* __restrict__ cell_of,
+                              uint32_t* __restrict__ slot, uint32_t* __restrict__ cell_count,
+                              const uint32_t* __restrict__ gate)
+{
+    if (gate && *gate == 0u) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const double4_32a p = pos[i];
+    const int cx = cell_coord(p.x, g.lo[0], g.scale[0], g.dim[0]);
+    const int cy = cell_coord(p.y, g.lo[1], g.scale[1], g.dim[1]);
+    const int cz = cell_coord(p.z, g.lo[2], g.scale[2], g.dim[2]);
+    const uint32_t c = ((uint32_t)cz * g.dim[1] + cy) * g.dim[0] + cx;
+    cell_of[i] = c;
+    slot[i] = atomicAdd(&cell_count[c], 1u);
+}
+
+__global__ void k_cell_scatter(const uint32_t* __restrict__ cell_of, const uint32_t* __restrict__ slot,
+                               const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ members, uint32_t N,
+                               const uint32_t* __restrict__ gate)
+{
+    if (gate && *gate == 0u) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    members[cell_start[cell_of[i]] + slot[i]] = i;
+}
+
+// insertion sort of each cell's members by index: deterministic order
+__global__ void k_cell_sort(const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ members, uint32_t ncell,
+                            const uint32_t* __restrict__ gate)
+{
+    if (gate && *gate == 0u) return;
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const uint32_t b = cell_start[c], e = cell_start[c + 1];
+    for (uint32_t a = b + 1; a < e; ++a) {
+        const uint32_t v = members[a];
+        uint32_t k = a;
+        while (k > b && members[k - 1] > v) {
+            members[k] = members[k - 1];
+            --k;
+        }
+        members[k] = v;
+    }
+}
+
+struct BoxArgs {
+    double L[3], Linv[3];
+    float sfix[3];  // L * 2^-32 (fixed-point unit)
+};
+
+inline BoxArgs box_args(const azp_box& b)
+{
+    BoxArgs a;
+    for (int d = 0; d < 3; ++d) {
+        a.L[d] = b.L[d];
+        a.Linv[d] = 1.0 / b.L[d];
+        a.sfix[d] = (float)(b.L[d] * 2.3283064365386963e-10);
+    }
+    return a;
+}
+
+constexpr int NLIST_BLOCK = 128;
+constexpr uint32_t MAX_LIST_TYPES = 16;  // ntypes^2 <= 256 thresholds in shared memory
+
+__global__ void __launch_bounds__(NLIST_BLOCK)
+    k_nlist_build(const double4_32a* __restrict__ pos, const uint4* __restrict__ fixed, uint32_t N, BoxArgs bx,
+                  CellGrid g, const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ members,
+                  const uint32_t* __restrict__ cell_of, const ListCut* __restrict__ cuts, uint32_t ntypes,
+                  const uint32_t* __restrict__ ex_n, const uint32_t* __restrict__ ex_keys, uint32_t ex_width,
+                  const uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, uint32_t* __restrict__ nbrs,
+                  uint32_t max_nn, uint32_t* __restrict__ flags, const uint32_t* __restrict__ gate)
+{
+    if (gate && *gate == 0u) return;
+    __shared__ ListCut s_cut[MAX_LIST_TYPES * MAX_LIST_TYPES];
+    const uint32_t nt2 = ntypes * ntypes;
+    for (uint32_t t = threadIdx.x; t < nt2; t += blockDim.x) s_cut[t] = cuts[t];
+    __syncthreads();
+
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const uint4 fi = fixed[i];
+    const uint32_t c = cell_of[i];
+    const int cx = (int)(c % g.dim[0]);
+    const int cy = (int)((c / g.dim[0]) % g.dim[1]);
+    const int cz = (int)(c / ((uint32_t)g.dim[0] * g.dim[1]));
+    const uint32_t row = fi.w * ntypes;
+    const uint32_t nex = ex_n ? ex_n[i] : 0u;
+    double4_32a pi;
+    bool have_pi = false;
+    uint32_t n = 0;
+    for (int oz = -g.reach[2]; oz <= g.reach[2]; ++oz) {
+        int nz = cz + oz;
+        nz += (nz < 0) ? g.dim[2] : 0;
+        nz -= (nz >= g.dim[2]) ? g.dim[2] : 0;
+        for (int oy = -g.reach[1]; oy <= g.reach[1]; ++oy) {
+            int ny = cy + oy;
+            ny += (ny < 0) ? g.dim[1] : 0;
+            ny -= (ny >= g.dim[1]) ? g.dim[1] : 0;
+            for (int ox = -g.reach[0]; ox <= g.reach[0]; ++ox) {
+                int nx = cx + ox;
+                nx += (nx < 0) ? g.dim[0] : 0;
+                nx -= (nx >= g.dim[0]) ? g.dim[0] : 0;
+                const uint32_t nc = ((uint32_t)nz * g.dim[1] + ny) * g.dim[0] + nx;
+                const uint32_t sb = cell_start[nc], se = cell_start[nc + 1];
+                for (uint32_t s = sb; s < se; ++s) {
+                    const uint32_t j = members ? members[s] : s;
+                    if (j == i) continue;
+                    const uint4 fj = fixed[j];
+                    const ListCut cut = s_cut[row + fj.w];
+                    const float dx = (float)(int32_t)(fi.x - fj.x) * bx.sfix[0];
+                    const float dy = (float)(int32_t)(fi.y - fj.y) * bx.sfix[1];
+                    const float dz = (float)(int32_t)(fi.z - fj.z) * bx.sfix[2];
+                    const float rs = dx * dx + dy * dy + dz * dz;
+                    if (rs >= cut.hi) continue;
+                    if (!(rs < cut.lo)) {
+                        // ambiguous band: the oracle's exact FP64 decision
+                        if (!have_pi) {
+                            pi = pos[i];
+                            have_pi = true;
+                        }
+                        const double4_32a pj = pos[j];
+                        const double vx = min_image1(pi.x - pj.x, bx.L[0], bx.Linv[0]);
+                        const double vy = min_image1(pi.y - pj.y, bx.L[1], bx.Linv[1]);
+                        const double vz = min_image1(pi.z - pj.z, bx.L[2], bx.Linv[2]);
+                        if (!(rsq_exact(vx, vy, vz) < cut.rlistsq)) continue;
+                    }
+                    if (nex) {
+                        const uint32_t kj = keys ? keys[j] : j;
+                        bool ex = false;
+                        for (uint32_t e = 0; e < nex; ++e) ex |= (ex_keys[e * N + i] == kj);
+                        if (ex) continue;
+                    }
+                    if (n < max_nn) nbrs[(size_t)n * N + i] = j;
+                    ++n;
+                }
+            }
+        }
+    }
+    counts[i] = n;
+    if (n > max_nn) atomicMax(&flags[0], n);
+    (void)ex_width;
+}
+
+// ---------------------------------------------------------------- launch helpers
+void launch_to_fixed(const double4_32a* pos, uint4* fixed, uint32_t N, const azp_box& box, cudaStream_t s)
+{
+    if (N == 0) return;
+    k_to_fixed<<<(N + 255) / 256, 256, 0, s>>>(pos, fixed, N, 1.0 / box.L[0], 1.0 / box.L[1], 1.0 / box.L[2]);
+}
+
+void launch_cell_assign(const double4_32a* pos, uint32_t N, const CellGrid& g, uint32_t* cell_of, uint32_t* slot,
+                        uint32_t* cell_count, cudaStream_t s, const uint32_t* gate)
+{
+    if (N == 0) return;
+    k_cell_assign<<<(N + 255) / 256, 256, 0, s>>>(pos, N, g, cell_of, slot, cell_count, gate);
+}
+
+void launch_cell_scatter(const uint32_t* cell_of, const uint32_t* slot, const uint32_t* cell_start,
+                         uint32_t* members, uint32_t N, uint32_t ncell, cudaStream_t s, const uint32_t* gate)
+{
+    if (N == 0) return;
+    k_cell_scatter<<<(N + 255) / 256, 256, 0, s>>>(cell_of, slot, cell_start, members, N, gate);
+    k_cell_sort<<<(ncell + 255) / 256, 256, 0, s>>>(cell_start, members, ncell, gate);
+}
+
+__global__ void k_to_fixed2(const double4_32a* __restrict__ pos, uint4* __restrict__ fa, uint4* __restrict__ fb,
+                            uint32_t N, double lx, double ly, double lz, const uint32_t* __restrict__ gate)
+{
+    if (gate && *gate == 0u) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const double4_32a p = pos[i];
+    uint4 f;
+    f.x = to_fixed(p.x, lx);
+    f.y = to_fixed(p.y, ly);
+    f.z = to_fixed(p.z, lz);
+    f.w = type_of(p.w);
+    fa[i] = f;
+    if (fb) fb[i] = f;
+}
+
+void launch_to_fixed2(const double4_32a* pos, uint4* a, uint4* b, uint32_t N, const azp_box& box, cudaStream_t s,
+                      const uint32_t* gate)
+{
+    if (N == 0) return;
+    k_to_fixed2<<<(N + 255) / 256, 256, 0, s>>>(pos, a, b, N, 1.0 / box.L[0], 1.0 / box.L[1], 1.0 / box.L[2], gate);
+}
+
+void launch_nlist_build(const double4_32a* pos, const uint4* fixed, uint32_t N, const azp_box& box, const CellGrid& g,
+                        const uint32_t* cell_start, const uint32_t* members, const uint32_t* cell_of,
+                        const ListCut* cuts, uint32_t ntypes, const uint32_t* ex_n, const uint32_t* ex_keys,
+                        uint32_t ex_width, const uint32_t* keys, uint32_t* counts, uint32_t* nbrs,
+                        uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s)
+{
+    if (N == 0) return;
+    k_nlist_build<<<(N + NLIST_BLOCK - 1) / NLIST_BLOCK, NLIST_BLOCK, 0, s>>>(
+        pos, fixed, N, box_args(box), g, cell_start, members, cell_of, cuts, ntypes, ex_n, ex_keys, ex_width, keys,
+        counts, nbrs, max_nn, flags, gate);
+}
+
+}  // namespace azp
+
+// ==================================================================== C ABI object
+namespace
+{
+void free_nl(azp_nlist* nl)
+{
+    cudaFree(nl->counts);
+    cudaFree(nl->nbrs);
+    cudaFree(nl->cuts);
+    cudaFree(nl->fixed);
+    cudaFree(nl->cell_of);
+    cudaFree(nl->slot);
+    cudaFree(nl->members);
+    cudaFree(nl->cell_count);
+    cudaFree(nl->cell_start);
+    cudaFree(nl->scan_tmp);
+    cudaFree(nl->flags);
+    cudaFree(nl->ex_n);
+    cudaFree(nl->ex_keys);
+    cudaFree(nl->table);
+    cudaFree(nl->cutbuf);
+}
+
+int ensure_cells(azp_nlist* nl, uint32_t ncell)
+{
+    if (ncell <= nl->ncell_cap) return AZP_OK;
+    cudaFree(nl->cell_count);
+    cudaFree(nl->cell_start);
+    cudaFree(nl->scan_tmp);
+    nl->cell_count = nl->cell_start = nl->scan_tmp = nullptr;
+    AZP_CUDA_TRY(cudaMalloc(&nl->cell_count, sizeof(uint32_t) * ncell));
+    AZP_CUDA_TRY(cudaMalloc(&nl->cell_start, sizeof(uint32_t) * (ncell + 1)));
+    AZP_CUDA_TRY(cudaMalloc(&nl->scan_tmp, sizeof(uint32_t) * azp::scan_tmp_words(ncell)));
+    nl->ncell_cap = ncell;
+    return AZP_OK;
+}
+}  // namespace
+
+extern "C" {
+
+azp_nlist* azp_nlist_create(uint32_t N, uint32_t ntypes, uint32_t max_neighbors, int* status)
+{
+    int st = AZP_OK;
+    azp_nlist* nl = new (std::nothrow) azp_nlist();
+    if (!nl || ntypes == 0 || ntypes > azp::MAX_LIST_TYPES) {
+        if (status) *status = AZP_ERR_INVALID;
+        delete nl;
+        return nullptr;
+    }
+    nl->N = N;
+    nl->ntypes = ntypes;
+    nl->max_nn = max_neighbors ? max_neighbors : 64;
+    const size_t n1 = N ? N : 1;
+    auto fail = [&](cudaError_t e, const char* w) {
+        st = azp::record_cuda_error(e, w);
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&nl->counts, sizeof(uint32_t) * n1)) != cudaSuccess) fail(e, "nlist counts");
+    if (!st && (e = cudaMalloc(&nl->nbrs, sizeof(uint32_t) * n1 * nl->max_nn)) != cudaSuccess) fail(e, "nlist nbrs");
+    if (!st && (e = cudaMalloc(&nl->cuts, sizeof(azp::ListCut) * ntypes * ntypes)) != cudaSuccess) fail(e, "cuts");
+    if (!st && (e = cudaMalloc(&nl->fixed, sizeof(uint4) * n1)) != cudaSuccess) fail(e, "fixed");
+    if (!st && (e = cudaMalloc(&nl->cell_of, sizeof(uint32_t) * n1)) != cudaSuccess) fail(e, "cell_of");
+    if (!st && (e = cudaMalloc(&nl->slot, sizeof(uint32_t) * n1)) != cudaSuccess) fail(e, "slot");
+    if (!st && (e = cudaMalloc(&nl->members, sizeof(uint32_t) * n1)) != cudaSuccess) fail(e, "members");
+    if (!st && (e = cudaMalloc(&nl->flags, sizeof(uint32_t) * 4)) != cudaSuccess) fail(e, "flags");
+    if (!st && (e = cudaMalloc(&nl->table, sizeof(double) * ntypes * ntypes * 12)) != cudaSuccess) fail(e, "table");
+    if (!st && (e = cudaMalloc(&nl->cutbuf, sizeof(double) * ntypes * ntypes * 2)) != cudaSuccess) fail(e, "cutbuf");
+    if (st) {
+        free_nl(nl);
+        delete nl;
+        if (status) *status = st;
+        return nullptr;
+    }
+    if (status) *status = AZP_OK;
+    return nl;
+}
+
+void azp_nlist_destroy(azp_nlist* nl)
+{
+    if (!nl) return;
+    free_nl(nl);
+    delete nl;
+}
+
+int azp_nlist_set_cutoffs(azp_nlist* nl, const double* r_cut, double r_buff)
+{
+    if (!nl || !r_cut || r_buff < 0.0) return AZP_ERR_INVALID;
+    const uint32_t nt2 = nl->ntypes * nl->ntypes;
+    for (uint32_t a = 0; a < nl->ntypes; ++a)
+        for (uint32_t b = 0; b < nl->ntypes; ++b)
+            if (r_cut[a * nl->ntypes + b] != r_cut[b * nl->ntypes + a]) return AZP_ERR_INVALID;
+    nl->r_cut.assign(r_cut, r_cut + nt2);
+    nl->r_buff = r_buff;
+    nl->have_cuts = true;
+    return AZP_OK;
+}
+
+int azp_nlist_set_exclusions(azp_nlist* nl, const uint32_t* start, const uint32_t* partners)
+{
+    if (!nl) return AZP_ERR_INVALID;
+    cudaFree(nl->ex_n);
+    cudaFree(nl->ex_keys);
+    nl->ex_n = nl->ex_keys = nullptr;
+    nl->ex_width = 0;
+    if (!start) return AZP_OK;
+    const uint32_t N = nl->N;
+    uint32_t w = 0;
+    for (uint32_t i = 0; i < N; ++i) w = std::max(w, start[i + 1] - start[i]);
+    if (w == 0) return AZP_OK;
+    std::vector<uint32_t> n(N), keys((size_t)w * N, 0xffffffffu);
+    for (uint32_t i = 0; i < N; ++i) {
+        n[i] = start[i + 1] - start[i];
+        for (uint32_t k = 0; k < n[i]; ++k) keys[(size_t)k * N + i] = partners[start[i] + k];
+    }
+    AZP_CUDA_TRY(cudaMalloc(&nl->ex_n, sizeof(uint32_t) * N));
+    AZP_CUDA_TRY(cudaMalloc(&nl->ex_keys, sizeof(uint32_t) * keys.size()));
+    AZP_CUDA_TRY(cudaMemcpy(nl->ex_n, n.data(), sizeof(uint32_t) * N, cudaMemcpyHostToDevice));
+    AZP_CUDA_TRY(cudaMemcpy(nl->ex_keys, keys.data(), sizeof(uint32_t) * keys.size(), cudaMemcpyHostToDevice));
+    nl->ex_width = w;
+    return AZP_OK;
+}
+
+int azp_nlist_build(azp_nlist* nl, const azp_system* sys, void* stream)
+{
+    if (!nl || !sys || !nl->have_cuts || sys->N != nl->N || sys->ntypes != nl->ntypes) return AZP_ERR_INVALID;
+    cudaStream_t s = azp::as_stream(stream);
+    const uint32_t N = nl->N;
+    std::vector<azp::ListCut> cuts(nl->ntypes * nl->ntypes);
+    double rmax = 0.0;
+    azp::make_list_cuts(nl->r_cut.data(), nl->ntypes, nl->r_buff, sys->box, cuts.data(), &rmax);
+    for (int d = 0; d < 3; ++d)
+        if (rmax > 0.0 && sys->box.L[d] < 2.0 * rmax) return AZP_ERR_BOX_TOO_SMALL;
+    const azp::CellGrid g = azp::make_grid(sys->box, rmax);
+    int st = ensure_cells(nl, g.ncell);
+    if (st) return st;
+    AZP_CUDA_TRY(cudaMemcpyAsync(nl->cuts, cuts.data(), sizeof(azp::ListCut) * cuts.size(), cudaMemcpyHostToDevice, s));
+    if (N == 0) {
+        nl->n_builds++;
+        return AZP_OK;
+    }
+    const double4_32a* pos = reinterpret_cast<const double4_32a*>(sys->pos);
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        AZP_CUDA_TRY(cudaMemsetAsync(nl->cell_count, 0, sizeof(uint32_t) * g.ncell, s));
+        AZP_CUDA_TRY(cudaMemsetAsync(nl->flags, 0, sizeof(uint32_t) * 4, s));
+        azp::launch_to_fixed(pos, nl->fixed, N, sys->box, s);
+        azp::launch_cell_assign(pos, N, g, nl->cell_of, nl->slot, nl->cell_count, s);
+        st = azp::exclusive_scan(nl->cell_count, nl->cell_start, g.ncell, nl->scan_tmp, s);
+        if (st) return st;
+        azp::launch_cell_scatter(nl->cell_of, nl->slot, nl->cell_start, nl->members, N, g.ncell, s);
+        azp::launch_nlist_build(pos, nl->fixed, N, sys->box, g, nl->cell_start, nl->members, nl->cell_of, nl->cuts,
+                                nl->ntypes, nl->ex_n, nl->ex_keys, nl->ex_width, nullptr, nl->counts, nl->nbrs,
+                                nl->max_nn, nl->flags, nullptr, s);
+        AZP_CHECK_LAUNCH("azp_nlist_build");
+        uint32_t need = 0;
+        AZP_CUDA_TRY(cudaMemcpyAsync(&need, nl->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        AZP_CUDA_TRY(cudaStreamSynchronize(s));
+        if (need <= nl->max_nn) {
+            nl->n_builds++;
+            return AZP_OK;
+        }
+        // grow (HOOMD re-allocates and rebuilds on overflow as well)
+        cudaFree(nl->nbrs);
+        nl->nbrs = nullptr;
+        nl->max_nn = need + 8;
+        AZP_CUDA_TRY(cudaMalloc(&nl->nbrs, sizeof(uint32_t) * (size_t)N * nl->max_nn));
+    }
+    return AZP_ERR_NLIST_OVERFLOW;
+}
+
+int azp_nlist_view(const azp_nlist* nl, const uint32_t** counts, const uint32_t** neighbors, uint32_t* max_neighbors,
+                   uint32_t* n_builds)
+{
+    if (!nl) return AZP_ERR_INVALID;
+    if (counts) *counts = nl->counts;
+    if (neighbors) *neighbors = nl->nbrs;
+    if (max_neighbors) *max_neighbors = nl->max_nn;
+    if (n_builds) *n_builds = nl->n_builds;
+    return AZP_OK;
+}
+
+}  // extern "C"
+
+extern "C" int azp_nlist_set_tpp(azp_nlist* nl, int tpp)
+{
+    if (!nl || !(tpp == 1 || tpp == 2 || tpp == 4 || tpp == 8 || tpp == 16 || tpp == 32)) return AZP_ERR_INVALID;
+    nl->tpp = tpp;
+    return AZP_OK;
+}
+
+extern "C" int azp_nlist_download(const azp_nlist* nl, uint32_t* counts, uint32_t* neighbors, void* stream)
+{
+    if (!nl || !counts || !neighbors) return AZP_ERR_INVALID;
+    cudaStream_t s = azp::as_stream(stream);
+    if (nl->N == 0) return AZP_OK;
+    AZP_CUDA_TRY(cudaMemcpyAsync(counts, nl->counts, sizeof(uint32_t) * nl->N, cudaMemcpyDeviceToHost, s));
+    AZP_CUDA_TRY(cudaMemcpyAsync(neighbors, nl->nbrs, sizeof(uint32_t) * (size_t)nl->N * nl->max_nn,
+                                 cudaMemcpyDeviceToHost, s));
+    AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    return AZP_OK;
+}

@@ -1,0 +1,65 @@
+"""Integration methods in a flow field.
+
+The reference keeps Langevin and Brownian dynamics in a flow field as legacy,
+unbuilt C++ classes (``src/TwoStepLangevinFlow.h:30-273``,
+``src/TwoStepBrownianFlow.h:30-206``; constructor arguments group, kT, flow
+field, seed, use_lambda / lambda, noiseless) whose Python front end was removed
+(``CHANGELOG.rst:300-303`` records the v0 ``flow.langevin`` / ``flow.brownian``).
+These classes give that integrator a HOOMD-v4-style front end:
+
+* ``gamma[type]`` per-type drag (``default_gamma``), or ``alpha`` for
+  gamma = alpha * diameter (the reference's use_lambda / lambda);
+* ``kT`` is a constant (a HOOMD Variant is not supported);
+* the RNG seed is the Simulation's seed.
+"""
+
+from __future__ import annotations
+
+from .flow import FlowField
+from .typeparam import TypeParameterDict
+
+
+class _FlowMethod:
+    def __init__(self, filter, kT, flow_field, default_gamma=1.0, alpha=None, noiseless=False):
+        if filter not in (None, "all"):
+            raise ValueError("only the whole system (filter='all') is supported")
+        if not isinstance(flow_field, FlowField):
+            raise TypeError("flow_field must be an azplugins_gb300.flow.FlowField")
+        self.filter = "all"
+        self.kT = float(kT)
+        self.flow_field = flow_field
+        self.noiseless = bool(noiseless)
+        self.alpha = None if alpha is None else float(alpha)
+        self.gamma = TypeParameterDict(1, scalar=True, name="gamma")
+        self.gamma.set_default(default_gamma)
+
+    def _gamma_table(self, types):
+        return [self.gamma[t] for t in types]
+
+
+class LangevinFlow(_FlowMethod):
+    """Langevin dynamics relative to a flow field u(r) (velocity Verlet, uniform noise).
+
+    a = (F + R - gamma (v - u(r))) / m with R uniform in [-c, c]^3,
+    c = sqrt(6 gamma kT / dt) (``src/TwoStepLangevinFlow.h:194-245``).
+    """
+
+    method_id = 0
+
+
+class BrownianFlow(_FlowMethod):
+    """Overdamped Brownian dynamics in a flow field:
+    x += (u(x) + (F + R) / gamma) dt (``src/TwoStepBrownianFlow.h:136-178``).
+
+    ``max_displacement`` (default 0 = off) caps each displacement component; it
+    exists for overlap relaxation of generated configurations.
+    """
+
+    method_id = 1
+
+    def __init__(self, filter, kT, flow_field, default_gamma=1.0, alpha=None, noiseless=False, max_displacement=0.0):
+        super().__init__(filter, kT, flow_field, default_gamma, alpha, noiseless)
+        self.max_displacement = float(max_displacement)
+
+
+__all__ = ["LangevinFlow", "BrownianFlow"]

@@ -1,0 +1,305 @@
+/*
+ * azplugins_gb300.h -- C ABI of the GB300-native short-range force-and-integrate
+ * path (cell list + neighbour list, azplugins pair and bond evaluators, Langevin /
+ * Brownian dynamics in a flow field). Plain pointers, sizes and PODs only; every
+ * device entry takes an explicit cudaStream_t (passed as void*), never allocates
+ * inside a stream-ordered call, and returns an int status (0 = ok).
+ *
+ * Reference interfaces replaced (paths inside the azplugins tree):
+ *   parameter structs   src/PairEvaluatorPerturbedLennardJones.h:25-66,
+ *                       src/PairEvaluatorExpandedYukawa.h:23-53,
+ *                       src/PairEvaluatorHertz.h:23-47,
+ *                       src/PairEvaluatorColloid.h:23-57,
+ *                       src/BondEvaluatorQuartic.h:28-82,
+ *                       src/BondEvaluatorDoubleWell.h:28-61
+ *   pair force driver   gpu_compute_pair_forces<Eval>, instantiated in
+ *                       src/PotentialPairGPUKernel.cu.inc:25-28
+ *   bond force driver   gpu_compute_bond_forces<Eval,2>, instantiated in
+ *                       src/PotentialBondGPUKernel.cu.inc:25-29
+ *   Langevin flow       gpu::langevin_flow_step1 / langevin_flow_step2<Flow>,
+ *                       src/TwoStepLangevinFlowGPU.cuh:25-55
+ *   Brownian flow       gpu::brownian_flow<Flow>, src/TwoStepBrownianFlowGPU.cuh:26-44
+ *   flow fields         src/ConstantFlow.h:30-65, src/ParabolicFlow.h:51-98
+ *   RNG stream ids      src/RNGIdentifiers.h:20-27
+ */
+#ifndef AZPLUGINS_GB300_H_
+#define AZPLUGINS_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AZP_ABI_VERSION 1
+
+/* every entry point is exported; everything else in the library is hidden */
+#if defined(__GNUC__)
+#define AZP_API __attribute__((visibility("default")))
+#else
+#define AZP_API
+#endif
+
+/* ------------------------------------------------------------------ status */
+enum azp_status {
+    AZP_OK = 0,
+    AZP_ERR_INVALID = -1,         /* bad argument */
+    AZP_ERR_CUDA = -2,            /* a CUDA runtime call failed */
+    AZP_ERR_NLIST_OVERFLOW = -3,  /* a particle has more neighbours than the list holds */
+    AZP_ERR_BOND = -4,            /* a bond evaluator refused (r_0 == 0, r_1 == r_0) */
+    AZP_ERR_BOX_TOO_SMALL = -5,   /* L < 2 (r_cut + r_buff) along a periodic axis */
+    AZP_ERR_TIMEOUT = -6,         /* a bounded device wait gave up */
+    AZP_ERR_NONFINITE = -7,       /* a non-finite position was produced */
+    AZP_ERR_UNSUPPORTED = -8,     /* combination not built */
+    AZP_ERR_CELL_OVERFLOW = -9,   /* internal cell list capacity exceeded */
+    AZP_ERR_NO_DEVICE = -10       /* no CUDA device visible */
+};
+
+/* device error word bits (azp_md_error / azp_err_word) */
+#define AZP_EBIT_NLIST_OVERFLOW 0x1u
+#define AZP_EBIT_BOND 0x2u
+#define AZP_EBIT_NONFINITE 0x4u
+#define AZP_EBIT_TIMEOUT 0x8u
+#define AZP_EBIT_CELL_OVERFLOW 0x10u
+
+/* ------------------------------------------------------------------ kinds */
+enum azp_pair_kind {
+    AZP_PAIR_PERTURBED_LJ = 0,     /* PairEvaluatorPerturbedLennardJones */
+    AZP_PAIR_EXPANDED_YUKAWA = 1,  /* PairEvaluatorExpandedYukawa */
+    AZP_PAIR_HERTZ = 2,            /* PairEvaluatorHertz */
+    AZP_PAIR_COLLOID = 3,          /* PairEvaluatorColloid */
+    AZP_PAIR_NUM_KINDS = 4
+};
+enum azp_bond_kind {
+    AZP_BOND_QUARTIC = 0,          /* BondEvaluatorQuartic */
+    AZP_BOND_DOUBLE_WELL = 1,      /* BondEvaluatorDoubleWell */
+    AZP_BOND_NUM_KINDS = 2
+};
+/* HOOMD pair.Pair modes accepted by azplugins (src/pair.py:415) */
+enum azp_shift_mode { AZP_MODE_NONE = 0, AZP_MODE_SHIFT = 1, AZP_MODE_XPLOR = 2 };
+/* arithmetic of the pair / bond evaluation. FP32: FP32 arithmetic on exact
+ * fixed-point displacements, compensated force / energy sums, FP64 cutoff
+ * decision; state and integration stay FP64. */
+enum azp_precision { AZP_FP64 = 0, AZP_FP32 = 1 };
+enum azp_flow_kind { AZP_FLOW_CONSTANT = 0, AZP_FLOW_PARABOLIC = 1 };
+enum azp_method { AZP_METHOD_LANGEVIN_FLOW = 0, AZP_METHOD_BROWNIAN_FLOW = 1 };
+
+/* RNG stream identifiers, same values as src/RNGIdentifiers.h:20-27 */
+#define AZP_RNG_DPD_GENERAL_WEIGHT 200u
+#define AZP_RNG_BROWNIAN_FLOW 201u
+#define AZP_RNG_LANGEVIN_FLOW 202u
+
+/* ------------------------------------------------------------------ parameter structs
+ * Field names and order of the reference param_type structs. Every pair record
+ * is padded to 4 doubles (32 bytes, the reference's aligned(32)), every bond
+ * record to 8 doubles; tables are indexed [type_i * ntypes + type_j] (pairs,
+ * symmetric) or [bond_type] (bonds). */
+typedef struct { double sigma_6, epsilon_x_4, attraction_scale_factor, rwcasq; } azp_params_perturbed_lj;
+typedef struct { double epsilon, kappa, delta, pad_; } azp_params_expanded_yukawa;
+typedef struct { double epsilon, pad_[3]; } azp_params_hertz;
+typedef struct { double A, a_1, a_2, sigma_3; } azp_params_colloid;
+typedef struct { double k, r_0, b_1, b_2, U_0, sigma_6, epsilon_x_4, delta; } azp_params_quartic;
+typedef struct { double r_1, r_diff, U_1, U_tilt, pad_[4]; } azp_params_double_well;
+
+#define AZP_PAIR_PARAM_DOUBLES 4
+#define AZP_BOND_PARAM_DOUBLES 8
+
+/* Dict constructor / asDict of each param_type, host-only, no device work.
+ * values[] holds the Python parameter dict in this key order:
+ *   PerturbedLennardJones: epsilon, sigma, attraction_scale_factor
+ *   ExpandedYukawa:        epsilon, kappa, delta
+ *   Hertz:                 epsilon
+ *   Colloid:               A, a_1, a_2, sigma
+ *   Quartic:               k, r_0, b_1, b_2, U_0, sigma, epsilon, delta
+ *   DoubleWell:            r_0, r_1, U_1, U_tilt
+ * Replaces e.g. PairParametersPerturbedLennardJones(pybind11::dict) and asDict()
+ * (src/PairEvaluatorPerturbedLennardJones.h:33-54). */
+AZP_API int azp_pair_params_from_values(int kind, const double* values, double* record);
+AZP_API int azp_pair_params_to_values(int kind, const double* record, double* values);
+AZP_API int azp_bond_params_from_values(int kind, const double* values, double* record);
+AZP_API int azp_bond_params_to_values(int kind, const double* record, double* values);
+AZP_API int azp_pair_num_values(int kind);
+AZP_API int azp_bond_num_values(int kind);
+
+/* ------------------------------------------------------------------ system */
+/* Orthorhombic periodic box centred on the origin: [-L/2, L/2) per axis. */
+typedef struct { double L[3]; } azp_box;
+
+/* Flow field passed by value (the reference passes the functor by value,
+ * src/TwoStepLangevinFlowGPU.h:180). CONSTANT: u = (p0, p1, p2).
+ * PARABOLIC: p0 = mean_velocity, p1 = separation; u_x = 1.5 p0 (1 - (y / (p1/2))^2). */
+typedef struct { int32_t kind; int32_t pad_; double p[3]; } azp_flow;
+
+/* Particle arrays, all DEVICE pointers, index order (not tag order):
+ *   pos   [N][4] doubles: x, y, z, w; the low 32 bits of w's bit pattern hold the
+ *         type (HOOMD's __int_as_scalar convention)
+ *   vel   [N][4] doubles: vx, vy, vz, mass
+ *   accel [N][3] doubles
+ *   image [N][3] int32
+ *   tag   [N] uint32 (RNG counter)
+ *   diameter [N] doubles (only read when gamma comes from lambda * diameter) */
+typedef struct {
+    uint32_t N;
+    uint32_t ntypes;
+    double* pos;
+    double* vel;
+    double* accel;
+    int32_t* image;
+    const uint32_t* tag;
+    const double* diameter;
+    azp_box box;
+} azp_system;
+
+/* Force output. precision FP64: force [N][4] doubles (fx, fy, fz, energy),
+ * virial [6][virial_pitch] doubles (xx, xy, xz, yy, yz, zz), may be NULL.
+ * precision FP32: the same layouts in floats. Written, not accumulated, by the
+ * pair driver; accumulated by the bond driver. */
+typedef struct {
+    void* force;
+    void* virial;
+    uint32_t virial_pitch;
+    int32_t precision;
+} azp_forces;
+
+/* ------------------------------------------------------------------ device / library */
+AZP_API int azp_abi_version(void);
+/* number of visible CUDA devices (0 when none); never faults */
+AZP_API int azp_device_count(void);
+/* last CUDA error string of this thread's last failing call */
+AZP_API const char* azp_last_error(void);
+
+/* ------------------------------------------------------------------ neighbour list
+ * Cell list binned at width >= max(r_cut + r_buff), full list (j listed for i and
+ * i for j), pairs with r_cut == 0 never listed, exclusions removed. Membership is
+ * decided in FP64 with the oracle's exact rounding (|dx|^2 < r_list^2), so the
+ * sets are bit-exact. Layout: column-major neighbours[k * N + i], counts[i].
+ * Replaces HOOMD's NeighborListGPUBinned behind hoomd.md.nlist.Cell(buffer=...). */
+typedef struct azp_nlist azp_nlist;
+AZP_API azp_nlist* azp_nlist_create(uint32_t N, uint32_t ntypes, uint32_t max_neighbors, int* status);
+AZP_API void azp_nlist_destroy(azp_nlist* nl);
+/* r_cut[ntypes*ntypes] (symmetric), host pointer */
+AZP_API int azp_nlist_set_cutoffs(azp_nlist* nl, const double* r_cut, double r_buff);
+/* exclusions as host CSR in index order: start[N+1], partners[] (both directions) */
+AZP_API int azp_nlist_set_exclusions(azp_nlist* nl, const uint32_t* start, const uint32_t* partners);
+/* unconditional rebuild at the current positions (synchronises the stream to
+ * check overflow; grows and rebuilds on overflow) */
+AZP_API int azp_nlist_build(azp_nlist* nl, const azp_system* sys, void* stream);
+/* device views of the list, valid until the next build */
+AZP_API int azp_nlist_view(const azp_nlist* nl, const uint32_t** counts, const uint32_t** neighbors,
+                   uint32_t* max_neighbors, uint32_t* n_builds);
+/* copy the list to HOST memory: counts[N], neighbors[max_neighbors * N]
+ * (column-major); synchronises the stream */
+AZP_API int azp_nlist_download(const azp_nlist* nl, uint32_t* counts, uint32_t* neighbors, void* stream);
+
+/* ------------------------------------------------------------------ force drivers
+ * Pair forces over the list (replaces gpu_compute_pair_forces<Eval>).
+ * params: device table [ntypes*ntypes] of 4-double param_type records;
+ * r_cut / r_on: device tables [ntypes*ntypes] (r_on may be NULL).
+ * Overwrites out->force (and virial). Uses nl as its workspace (type-pair table,
+ * FP32 fixed-point shadow): stream-ordered, no allocation, no synchronisation. */
+AZP_API int azp_pair_forces(const azp_system* sys, azp_nlist* nl, int kind, const double* params,
+                    const double* r_cut, const double* r_on, int shift_mode, const azp_forces* out,
+                    void* stream);
+/* threads per particle of azp_pair_forces: 1, 2, 4, 8, 16 or 32 */
+AZP_API int azp_nlist_set_tpp(azp_nlist* nl, int tpp);
+
+/* Bond forces from a per-particle bond table (replaces
+ * gpu_compute_bond_forces<Eval,2>): for particle i its bonds are
+ * table[k * N + i] = (partner index, bond type) for k < n_bonds[i].
+ * params: device table [nbondtypes] of 8-double records. ACCUMULATES into out.
+ * FP32 precision evaluates in FP32 on the FP64 minimum-image displacement.
+ * err: device uint32 error word (AZP_EBIT_BOND set when an evaluator refuses). */
+AZP_API int azp_bond_forces(const azp_system* sys, const uint32_t* n_bonds, const uint32_t* table,
+                    uint32_t table_height, int kind, const double* params, uint32_t nbondtypes,
+                    const azp_forces* out, uint32_t* err, void* stream);
+
+/* ------------------------------------------------------------------ integrator drivers
+ * Particle subsets: group[n_group] index list, or NULL for all N particles.
+ * gamma: device table [ntypes] (ignored when use_lambda != 0: gamma = lambda * diameter).
+ * net_force: device [N][4] in the precision named by net_precision (FP64 doubles or FP32 floats). */
+AZP_API int azp_langevin_step1(const azp_system* sys, const uint32_t* group, uint32_t n_group, double dt,
+                       void* stream);
+AZP_API int azp_langevin_step2(const azp_system* sys, const uint32_t* group, uint32_t n_group,
+                       const void* net_force, int net_precision, const double* gamma, int use_lambda,
+                       double lambda, azp_flow flow, double dt, double kT, uint64_t timestep,
+                       uint32_t seed, int noiseless, void* stream);
+AZP_API int azp_brownian_step(const azp_system* sys, const uint32_t* group, uint32_t n_group,
+                      const void* net_force, int net_precision, const double* gamma, int use_lambda,
+                      double lambda, azp_flow flow, double dt, double kT, uint64_t timestep,
+                      uint32_t seed, int noiseless, double max_displacement, void* stream);
+
+/* ------------------------------------------------------------------ RNG (test hook)
+ * Three uniform doubles in (lo, hi) for (stream id, timestep, seed, tag), the same
+ * numbers the integrators draw; computed on the device into out[3*n] for tags[n]. */
+AZP_API int azp_uniform3(uint32_t rng_id, uint64_t timestep, uint32_t seed, const uint32_t* tags, uint32_t n,
+                 double lo, double hi, double* out, void* stream);
+
+/* ------------------------------------------------------------------ engine
+ * Resident MD engine: particles kept in cell order in HBM, one fused
+ * force + integrate kernel per step, conditional list rebuild and particle
+ * re-sort on the device, steps replayed from captured CUDA graphs. Host-visible
+ * state is always in tag order. */
+typedef struct azp_md azp_md;
+
+typedef struct {
+    uint32_t N;
+    uint32_t ntypes;
+    azp_box box;
+    int32_t precision;          /* azp_precision of the force evaluation */
+    /* pair */
+    int32_t pair_kind;          /* -1: no pair force */
+    int32_t shift_mode;
+    const double* pair_params;  /* host [ntypes*ntypes][4] param_type records */
+    const double* r_cut;        /* host [ntypes*ntypes] */
+    const double* r_on;         /* host [ntypes*ntypes] or NULL */
+    double r_buff;
+    /* bonds */
+    int32_t bond_kind;          /* -1: no bond force */
+    uint32_t nbondtypes;
+    const double* bond_params;  /* host [nbondtypes][8] */
+    uint32_t nbonds;
+    const uint32_t* bonds;      /* host [nbonds][2] tags */
+    const uint32_t* bond_types; /* host [nbonds] */
+    int32_t exclude_bonds;      /* remove bonded pairs from the pair list */
+    /* method */
+    int32_t method;             /* azp_method */
+    double dt;
+    double kT;
+    uint32_t seed;
+    int32_t noiseless;
+    const double* gamma;        /* host [ntypes] */
+    int32_t use_lambda;
+    double lambda;
+    azp_flow flow;
+    double max_displacement;    /* Brownian only; 0 = uncapped */
+} azp_md_config;
+
+AZP_API azp_md* azp_md_create(const azp_md_config* cfg, int* status);
+AZP_API void azp_md_destroy(azp_md* md);
+/* Load state in TAG order from host (on_device == 0) or device pointers:
+ * pos [N][4] (w = type as an integer-valued double), vel [N][4] (w = mass),
+ * accel [N][3], image [N][3], diameter [N] or NULL. */
+AZP_API int azp_md_set_state(azp_md* md, const double* pos, const double* vel, const double* accel,
+                     const int32_t* image, const double* diameter, uint64_t timestep, int on_device,
+                     void* stream);
+AZP_API int azp_md_get_state(azp_md* md, double* pos, double* vel, double* accel, int32_t* image,
+                     uint64_t* timestep, int on_device, void* stream);
+/* Advance `steps` timesteps (HOOMD order: step one, forces, step two). */
+AZP_API int azp_md_run(azp_md* md, uint64_t steps, void* stream);
+/* Net force [N][4] (fx, fy, fz, energy) and virial [N][6] at the current
+ * positions, in tag order, FP64 (host or device pointers). */
+AZP_API int azp_md_forces(azp_md* md, double* force, double* virial, int on_device, void* stream);
+/* Global sums in FP64: out[0] potential energy, out[1] kinetic energy,
+ * out[2..7] virial xx, xy, xz, yy, yz, zz, out[8] list builds so far (host out). */
+AZP_API int azp_md_thermo(azp_md* md, double* out, void* stream);
+/* The accumulated device error word (AZP_EBIT_*), 0 when clean. */
+AZP_API int azp_md_error(azp_md* md, uint32_t* err_word, void* stream);
+/* number of kernel launches issued by the last azp_md_run */
+AZP_API uint64_t azp_md_last_launches(const azp_md* md);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AZPLUGINS_GB300_H_ */

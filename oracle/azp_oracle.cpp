@@ -1,0 +1,836 @@
+// azp_oracle.cpp -- CPU restatement of the azplugins short-range
+// force-and-integrate path, in FP64. TEST INFRASTRUCTURE ONLY: the tests, the
+// smoke check and the bench's CPU-baseline leg load it as the checker; the
+// product (azplugins_gb300) never links, imports or calls it.
+//
+// What is restated, and from where (paths relative to the azplugins tree):
+//   * pair evaluators   src/PairEvaluatorPerturbedLennardJones.h:117-155,
+//                       src/PairEvaluatorExpandedYukawa.h:92-115,
+//                       src/PairEvaluatorHertz.h:93-110,
+//                       src/PairEvaluatorColloid.h:101-269
+//   * pair parameters   the dict constructors of the same headers (:25-66 etc.)
+//   * bond evaluators   src/BondEvaluatorQuartic.h:129-200,
+//                       src/BondEvaluatorDoubleWell.h:96-113
+//   * flow fields       src/ConstantFlow.h:48-51, src/ParabolicFlow.h:69-93
+//   * Langevin flow     src/TwoStepLangevinFlow.h:128-153 (step one),
+//                       :194-245 (step two)
+//   * Brownian flow     src/TwoStepBrownianFlow.h:136-178 (type bits kept)
+//   * RNG stream ids    src/RNGIdentifiers.h:20-27
+//   * pair loop         HOOMD PotentialPair (not in the tree); observable
+//                       contract src/pytest/test_pair.py:351-363 (half energy per
+//                       particle, equal and opposite forces), virial order
+//                       src/ImagePotentialBondGPU.cuh:228-234
+//   * bond loop         src/ImagePotentialBond.h:142-194 with minimum image
+//   * neighbour list    HOOMD NeighborListBinned (not in the tree): all j != i
+//                       with |dx|^2 < (r_cut_ij + r_buff)^2, r_cut_ij > 0,
+//                       minus exclusions; rebuilt when a particle moved more
+//                       than r_buff/2 since the last build.
+//   * Philox4x32-10     Salmon, Moraes, Dror, Shaw, SC'11 (published algorithm)
+//
+// Compiled with -ffp-contract=off so that x86 and Arm builds round alike.
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace
+{
+// ---------------------------------------------------------------- evaluators
+enum PairKind { PAIR_PLJ = 0, PAIR_EYUK = 1, PAIR_HERTZ = 2, PAIR_COLLOID = 3, PAIR_DPD = 4 };
+enum BondKind { BOND_QUARTIC = 0, BOND_DOUBLEWELL = 1 };
+enum ShiftMode { MODE_NONE = 0, MODE_SHIFT = 1, MODE_XPLOR = 2 };
+
+// Perturbed LJ: p = {sigma^6, 4 eps, lambda, 2^(1/3) sigma^2}
+inline double plj_energy_raw(double r6inv, double lj1, double lj2) { return r6inv * (lj1 * r6inv - lj2); }
+
+bool eval_plj(const double* p, double rsq, double rcutsq, bool shift, double& fdr, double& e)
+{
+    const double lj1 = p[1] * p[0] * p[0];
+    const double lj2 = p[1] * p[0];
+    const double lam = p[2];
+    const double rwcasq = p[3];
+    if (!(rsq < rcutsq) || lj1 == 0.0) return false;
+    const double wca_shift = p[1] * (1.0 - lam) / 4.0;
+    const double r2inv = 1.0 / rsq;
+    const double r6inv = r2inv * r2inv * r2inv;
+    double f = r2inv * r6inv * (12.0 * lj1 * r6inv - 6.0 * lj2);
+    double u = plj_energy_raw(r6inv, lj1, lj2);
+    if (rsq < rwcasq) {
+        u += wca_shift;
+    } else {
+        f *= lam;
+        u *= lam;
+    }
+    if (shift) {
+        const double rc2inv = 1.0 / rcutsq;
+        const double rc6inv = rc2inv * rc2inv * rc2inv;
+        double uc = plj_energy_raw(rc6inv, lj1, lj2);
+        if (rcutsq < rwcasq) uc += wca_shift; else uc *= lam;
+        u -= uc;
+    }
+    fdr = f;
+    e = u;
+    return true;
+}
+
+// Expanded Yukawa: p = {eps, kappa, delta}
+bool eval_eyuk(const double* p, double rsq, double rcutsq, bool shift, double& fdr, double& e)
+{
+    const double eps = p[0], kap = p[1], del = p[2];
+    if (!(rsq < rcutsq) || eps == 0.0) return false;
+    const double r = std::sqrt(rsq);
+    const double s = r - del;
+    const double sinv = 1.0 / s;
+    double u = eps * std::exp(-kap * s) * sinv;
+    fdr = u * (kap + sinv) / r;
+    if (shift) {
+        const double sc = std::sqrt(rcutsq) - del;
+        u -= eps * std::exp(-kap * sc) / sc;
+    }
+    e = u;
+    return true;
+}
+
+// Hertz: p = {eps}; never shifted (goes to zero at r_cut)
+bool eval_hertz(const double* p, double rsq, double rcutsq, bool, double& fdr, double& e)
+{
+    const double eps = p[0];
+    if (!(rsq < rcutsq) || eps == 0.0) return false;
+    const double r = std::sqrt(rsq);
+    const double rc = std::sqrt(rcutsq);
+    const double x = 1.0 - r / rc;
+    const double ex32 = eps * x * std::sqrt(x);
+    fdr = 2.5 * ex32 / (r * rc);
+    e = ex32 * x;
+    return true;
+}
+
+// Colloid (Everaers-Ejtehadi integrated LJ): p = {A, a_1, a_2, sigma^3}
+double colloid_ss(double A, double s6, double rsq, double* fdr)
+{
+    const double r2inv = 1.0 / rsq;
+    const double r6inv = r2inv * r2inv * r2inv;
+    const double c = A * s6 / 36.0;
+    if (fdr) *fdr = 6.0 * c * r2inv * r6inv * (2.0 * s6 * r6inv - 1.0);
+    return c * r6inv * (s6 * r6inv - 1.0);
+}
+
+double colloid_cs(double A, double s3, double s6, double a, double rsq, double* fdr)
+{
+    const double a2 = a * a;
+    const double d = a2 - rsq;           // a^2 - r^2
+    const double d3 = d * d * d;
+    const double d6 = d3 * d3;
+    const double r4 = rsq * rsq;
+    const double pre = s3 * A * a * a2 / d3;
+    if (fdr) {
+        const double poly = 2.0 * (a2 + rsq) * (a2 * (5.0 * a2 + 22.0 * rsq) + 5.0 * r4);
+        *fdr = (4.0 / 15.0) * pre * (poly * s6 / d6 - 5.0) / d;
+    }
+    const double poly_e = a2 * (a2 * (a2 / 3.0 + 3.0 * rsq) + 4.2 * r4) + rsq * r4;
+    return (2.0 / 9.0) * pre * (1.0 - poly_e * s6 / d6);
+}
+
+inline double inv7(double x)
+{
+    const double xi = 1.0 / x;
+    double g = xi * xi;
+    g = g * g * g;
+    return g * xi;
+}
+
+double colloid_cc(double A, double s6, double ai, double aj, double rsq, double* fdr)
+{
+    const double r = std::sqrt(rsq);
+    const double prod = ai * aj;
+    const double sum = ai + aj;
+    const double dif = ai - aj;
+    const double sp = sum + r, sm = sum - r, dp = dif + r, dm = dif - r;
+    const double q7 = 1.0 / (sp * sm);
+    const double q8 = 1.0 / (dp * dm);
+    double g0 = inv7(sp), g1 = inv7(sm), g2 = inv7(dp), g3 = inv7(dm);
+    const double h0 = ((sp + 5.0 * sum) * sp + 30.0 * prod) * g0;
+    const double h1 = ((sm + 5.0 * sum) * sm + 30.0 * prod) * g1;
+    const double h2 = ((dp + 5.0 * dif) * dp - 30.0 * prod) * g2;
+    const double h3 = ((dm + 5.0 * dif) * dm - 30.0 * prod) * g3;
+    const double pre = A * s6 / r / 37800.0;
+    double u = pre * (h0 - h1 - h2 + h3);
+    if (fdr) {
+        g0 *= 42.0 * prod / sp + 6.0 * sum + sp;
+        g1 *= 42.0 * prod / sm + 6.0 * sum + sm;
+        g2 *= -42.0 * prod / dp + 6.0 * dif + dp;
+        g3 *= -42.0 * prod / dm + 6.0 * dif + dm;
+        const double dur = u / r + 5.0 * pre * (g0 + g1 - g2 - g3);
+        const double dua = -A / 3.0 * r * ((2.0 * prod * q7 + 1.0) * q7 + (2.0 * prod * q8 - 1.0) * q8);
+        *fdr = (dur + dua) / r;
+    }
+    u += A / 6.0 * (2.0 * prod * (q7 + q8) - std::log(q8 / q7));
+    return u;
+}
+
+bool eval_colloid(const double* p, double rsq, double rcutsq, bool shift, double& fdr, double& e)
+{
+    const double A = p[0], a1 = p[1], a2 = p[2], s3 = p[3];
+    if (!(rsq < rcutsq) || A == 0.0) return false;
+    const double s6 = s3 * s3;
+    double u;
+    if (a1 == 0.0 && a2 == 0.0) {
+        u = colloid_ss(A, s6, rsq, &fdr);
+        if (shift) u -= colloid_ss(A, s6, rcutsq, nullptr);
+    } else if (a1 != 0.0 && a2 != 0.0) {
+        u = colloid_cc(A, s6, a1, a2, rsq, &fdr);
+        if (shift) u -= colloid_cc(A, s6, a1, a2, rcutsq, nullptr);
+    } else {
+        const double a = a1 > a2 ? a1 : a2;
+        u = colloid_cs(A, s3, s6, a, rsq, &fdr);
+        if (shift) u -= colloid_cs(A, s3, s6, a, rcutsq, nullptr);
+    }
+    e = u;
+    return true;
+}
+
+// DPD general weight, conservative part only: p = {A, gamma, s}
+bool eval_dpd_cons(const double* p, double rsq, double rcutsq, bool, double& fdr, double& e)
+{
+    if (!(rsq < rcutsq)) return false;
+    const double A = p[0];
+    const double rinv = 1.0 / std::sqrt(rsq);
+    const double r = 1.0 / rinv;
+    const double rcinv = 1.0 / std::sqrt(rcutsq);
+    const double rc = 1.0 / rcinv;
+    fdr = A * (rinv - rcinv);
+    e = A * (rc - r) - 0.5 * A * rcinv * (rcutsq - rsq);
+    return true;
+}
+
+bool eval_pair(int kind, const double* p, double rsq, double rcutsq, bool shift, double& f, double& e)
+{
+    switch (kind) {
+    case PAIR_PLJ: return eval_plj(p, rsq, rcutsq, shift, f, e);
+    case PAIR_EYUK: return eval_eyuk(p, rsq, rcutsq, shift, f, e);
+    case PAIR_HERTZ: return eval_hertz(p, rsq, rcutsq, shift, f, e);
+    case PAIR_COLLOID: return eval_colloid(p, rsq, rcutsq, shift, f, e);
+    case PAIR_DPD: return eval_dpd_cons(p, rsq, rcutsq, shift, f, e);
+    default: return false;
+    }
+}
+
+// Quartic bond: p = {k, r_0, b_1, b_2, U_0, sigma^6, 4 eps, delta}
+bool eval_quartic(const double* p, double rsq, double& fdr, double& e)
+{
+    const double k = p[0], r0 = p[1], b1 = p[2], b2 = p[3], U0 = p[4];
+    const double lj1 = p[6] * p[5] * p[5];
+    const double lj2 = p[6] * p[5];
+    const double del = p[7];
+    fdr = 0.0;
+    e = 0.0;
+    if (r0 == 0.0) return false;
+    double rr = 1.0;  // (reduced distance) - r_0, positive means "beyond r_0"
+    if (del == 0.0) {
+        const double r2inv = 1.0 / rsq;
+        const double r6inv = r2inv * r2inv * r2inv;
+        if (lj1 != 0.0 && r6inv > (lj2 / lj1) / 2.0) {
+            fdr += r2inv * r6inv * (12.0 * lj1 * r6inv - 6.0 * lj2);
+            e += r6inv * (lj1 * r6inv - lj2) + lj2 * lj2 / 4.0 / lj1;
+        }
+        if (rsq < r0 * r0) rr = std::sqrt(rsq) - r0;
+    } else {
+        const double rs = std::sqrt(rsq) - del;
+        const double r2inv = 1.0 / rs / rs;
+        const double r6inv = r2inv * r2inv * r2inv;
+        if (lj1 != 0.0 && r6inv > (lj2 / lj1) / 2.0) {
+            fdr += r6inv * (12.0 * lj1 * r6inv - 6.0 * lj2) / rs / (rs + del);
+            e += r6inv * (lj1 * r6inv - lj2) + p[6] / 4.0;
+        }
+        if (rs < r0) rr = rs - r0;
+    }
+    if (rr < 0.0) {
+        fdr += -k * rr * (4.0 * rr * rr - 3.0 * (b1 + b2) * rr + 2.0 * b1 * b2) / (rr + r0 + del);
+        e += k * (rr - b1) * (rr - b2) * rr * rr + U0;
+    } else {
+        e += U0;
+    }
+    return true;
+}
+
+// Double well bond: p = {r_1, r_1 - r_0, U_1, U_tilt}
+bool eval_doublewell(const double* p, double rsq, double& fdr, double& e)
+{
+    const double r1 = p[0], rd = p[1], U1 = p[2], Ut = p[3];
+    fdr = 0.0;
+    e = 0.0;
+    if (rd == 0.0) return false;
+    const double r = std::sqrt(rsq);
+    const double x = (r1 - r) / rd;
+    const double y = 1.0 - x * x;
+    e = U1 * y * y + Ut * (1.0 - x - y * y);
+    fdr = (4.0 * x * y * (Ut - U1) - Ut) / (rd * r);
+    return true;
+}
+
+bool eval_bond(int kind, const double* p, double rsq, double& f, double& e)
+{
+    switch (kind) {
+    case BOND_QUARTIC: return eval_quartic(p, rsq, f, e);
+    case BOND_DOUBLEWELL: return eval_doublewell(p, rsq, f, e);
+    default: return false;
+    }
+}
+
+// ---------------------------------------------------------------- Philox4x32-10
+inline void mulhilo(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo)
+{
+    const uint64_t p = (uint64_t)a * (uint64_t)b;
+    hi = (uint32_t)(p >> 32);
+    lo = (uint32_t)p;
+}
+
+void philox(const uint32_t in[4], const uint32_t key_in[2], uint32_t out[4])
+{
+    uint32_t c0 = in[0], c1 = in[1], c2 = in[2], c3 = in[3];
+    uint32_t k0 = key_in[0], k1 = key_in[1];
+    for (int round = 0; round < 10; ++round) {
+        uint32_t hi0, lo0, hi1, lo1;
+        mulhilo(0xD2511F53u, c0, hi0, lo0);
+        mulhilo(0xCD9E8D57u, c2, hi1, lo1);
+        const uint32_t n0 = hi1 ^ c1 ^ k0;
+        const uint32_t n1 = lo1;
+        const uint32_t n2 = hi0 ^ c3 ^ k1;
+        const uint32_t n3 = lo0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// Stream layout of this build (mirrors HOOMD's Seed(id, timestep, seed) +
+// Counter(tag) structure; HOOMD's exact packing is not available to pin):
+//   key = { id<<24 | (seed & 0xffff)<<8 | (timestep>>32 & 0xff), timestep & 0xffffffff }
+//   ctr = { call index, tag, 0, 0 }
+// Each Philox call yields two 64-bit words (w0<<32|w1, w2<<32|w3); a uniform
+// double in (0,1) is ((u64 >> 11) + 0.5) * 2^-53. Three draws use two calls.
+inline void stream_key(uint8_t id, uint64_t timestep, uint32_t seed, uint32_t key[2])
+{
+    key[0] = ((uint32_t)id << 24) | ((seed & 0xffffu) << 8) | (uint32_t)((timestep >> 32) & 0xffu);
+    key[1] = (uint32_t)(timestep & 0xffffffffu);
+}
+
+inline double u64_to_open01(uint64_t u) { return ((double)(u >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+
+void uniform3(uint8_t id, uint64_t timestep, uint32_t seed, uint32_t tag, double lo, double hi, double r[3])
+{
+    uint32_t key[2];
+    stream_key(id, timestep, seed, key);
+    uint32_t c0[4] = {0u, tag, 0u, 0u}, c1[4] = {1u, tag, 0u, 0u};
+    uint32_t o0[4], o1[4];
+    philox(c0, key, o0);
+    philox(c1, key, o1);
+    const uint64_t u0 = ((uint64_t)o0[0] << 32) | o0[1];
+    const uint64_t u1 = ((uint64_t)o0[2] << 32) | o0[3];
+    const uint64_t u2 = ((uint64_t)o1[0] << 32) | o1[1];
+    const double w = hi - lo;
+    r[0] = lo + w * u64_to_open01(u0);
+    r[1] = lo + w * u64_to_open01(u1);
+    r[2] = lo + w * u64_to_open01(u2);
+}
+
+// ---------------------------------------------------------------- box
+struct Box {
+    double L[3], Linv[3], lo[3], hi[3];
+};
+
+inline Box make_box(const double* L)
+{
+    Box b;
+    for (int d = 0; d < 3; ++d) {
+        b.L[d] = L[d];
+        b.Linv[d] = 1.0 / L[d];
+        b.lo[d] = -0.5 * L[d];
+        b.hi[d] = 0.5 * L[d];
+    }
+    return b;
+}
+
+inline void min_image(const Box& b, double* v)
+{
+    for (int d = 0; d < 3; ++d) v[d] -= b.L[d] * std::rint(v[d] * b.Linv[d]);
+}
+
+inline void wrap(const Box& b, double* x, int* img)
+{
+    for (int d = 0; d < 3; ++d) {
+        if (x[d] >= b.hi[d]) { x[d] -= b.L[d]; img[d] += 1; }
+        else if (x[d] < b.lo[d]) { x[d] += b.L[d]; img[d] -= 1; }
+    }
+}
+
+inline double rsq_of(const double* v) { return v[0] * v[0] + v[1] * v[1] + v[2] * v[2]; }
+
+// ---------------------------------------------------------------- neighbour list
+struct Excl {
+    const int32_t* start;  // [N+1] CSR of excluded partner indices
+    const int32_t* idx;
+};
+
+inline bool excluded(const Excl& ex, int i, int j)
+{
+    if (!ex.start) return false;
+    for (int k = ex.start[i]; k < ex.start[i + 1]; ++k)
+        if (ex.idx[k] == j) return true;
+    return false;
+}
+
+inline bool listed(const Box& b, const double* pos, const int32_t* type, int ntypes,
+                   const double* rlistsq, int i, int j)
+{
+    double v[3] = {pos[4 * i] - pos[4 * j], pos[4 * i + 1] - pos[4 * j + 1], pos[4 * i + 2] - pos[4 * j + 2]};
+    min_image(b, v);
+    const double rs = rsq_of(v);
+    return rs < rlistsq[type[i] * ntypes + type[j]];
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- version / identity
+int orc_version() { return 3; }
+
+// ---- threads used by every parallel phase (1 = the scalar oracle)
+int orc_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+// ---- parameter construction (the dict constructors), in param_type field order
+// PLJ in: {epsilon, sigma, attraction_scale_factor} -> {sigma_6, epsilon_x_4, lambda, rwcasq}
+// EYUK in: {epsilon, kappa, delta} -> same
+// HERTZ in: {epsilon} -> same
+// COLLOID in: {A, a_1, a_2, sigma} -> {A, a_1, a_2, sigma_3}
+// DPD in: {A, gamma, s} -> same
+int orc_pair_params(int kind, const double* in, double* out)
+{
+    switch (kind) {
+    case PAIR_PLJ: {
+        const double s2 = in[1] * in[1];
+        out[0] = s2 * (s2 * s2);
+        out[1] = 4.0 * in[0];
+        out[2] = in[2];
+        out[3] = std::pow(2.0, 1.0 / 3.0) * s2;
+        return 0;
+    }
+    case PAIR_EYUK: out[0] = in[0]; out[1] = in[1]; out[2] = in[2]; return 0;
+    case PAIR_HERTZ: out[0] = in[0]; return 0;
+    case PAIR_COLLOID: out[0] = in[0]; out[1] = in[1]; out[2] = in[2]; out[3] = in[3] * in[3] * in[3]; return 0;
+    case PAIR_DPD: out[0] = in[0]; out[1] = in[1]; out[2] = in[2]; return 0;
+    default: return -1;
+    }
+}
+
+// Quartic in: {k, r_0, b_1, b_2, U_0, sigma, epsilon, delta}
+// DoubleWell in: {r_0, r_1, U_1, U_tilt} -> {r_1, r_1 - r_0, U_1, U_tilt}
+int orc_bond_params(int kind, const double* in, double* out)
+{
+    switch (kind) {
+    case BOND_QUARTIC: {
+        const double s2 = in[5] * in[5];
+        out[0] = in[0]; out[1] = in[1]; out[2] = in[2]; out[3] = in[3]; out[4] = in[4];
+        out[5] = s2 * (s2 * s2);
+        out[6] = 4.0 * in[6];
+        out[7] = in[7];
+        return 0;
+    }
+    case BOND_DOUBLEWELL:
+        out[0] = in[1]; out[1] = in[1] - in[0]; out[2] = in[2]; out[3] = in[3];
+        return 0;
+    default: return -1;
+    }
+}
+
+int orc_pair_eval(int kind, const double* p, double rsq, double rcutsq, int shift, double* f, double* e)
+{
+    double ff = 0.0, ee = 0.0;
+    const bool ok = eval_pair(kind, p, rsq, rcutsq, shift != 0, ff, ee);
+    *f = ok ? ff : 0.0;
+    *e = ok ? ee : 0.0;
+    return ok ? 1 : 0;
+}
+
+int orc_bond_eval(int kind, const double* p, double rsq, double* f, double* e)
+{
+    double ff = 0.0, ee = 0.0;
+    const bool ok = eval_bond(kind, p, rsq, ff, ee);
+    *f = ff;
+    *e = ee;
+    return ok ? 1 : 0;
+}
+
+// flow: kind 0 = ConstantFlow {Ux,Uy,Uz}; kind 1 = ParabolicFlow {mean_velocity, separation}
+void orc_flow(int kind, const double* fp, const double* r, double* u)
+{
+    if (kind == 0) {
+        u[0] = fp[0]; u[1] = fp[1]; u[2] = fp[2];
+    } else {
+        const double umax = 1.5 * fp[0];
+        const double half = 0.5 * fp[1];
+        const double yr = r[1] / half;
+        u[0] = umax * (1.0 - yr * yr);
+        u[1] = 0.0;
+        u[2] = 0.0;
+    }
+}
+
+void orc_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out) { philox(ctr, key, out); }
+
+void orc_uniform3(int id, uint64_t timestep, uint32_t seed, uint32_t tag, double lo, double hi, double* r)
+{
+    uniform3((uint8_t)id, timestep, seed, tag, lo, hi, r);
+}
+
+// ---- neighbour list (CSR output: start[N+1], idx[], each row ascending)
+// Brute force O(N^2). rlistsq[ti*ntypes+tj] = (r_cut + r_buff)^2, or 0 to skip.
+// Returns the number of entries written, or -(needed) if cap is too small.
+long orc_nlist_brute(int N, const double* pos, const int32_t* type, int ntypes, const double* L,
+                     const double* rlistsq, const int32_t* ex_start, const int32_t* ex_idx,
+                     int32_t* start, int32_t* idx, long cap)
+{
+    const Box b = make_box(L);
+    const Excl ex{ex_start, ex_idx};
+    long n = 0;
+    for (int i = 0; i < N; ++i) {
+        start[i] = (int32_t)std::min<long>(n, cap);
+        for (int j = 0; j < N; ++j) {
+            if (j == i) continue;
+            if (!listed(b, pos, type, ntypes, rlistsq, i, j)) continue;
+            if (excluded(ex, i, j)) continue;
+            if (n < cap) idx[n] = j;
+            ++n;
+        }
+    }
+    start[N] = (int32_t)std::min<long>(n, cap);
+    return n <= cap ? n : -n;
+}
+
+// Cell-list build, same contract as orc_nlist_brute (cells of width >= r_list_max).
+// Parallel over particles: count pass, prefix sum, write pass; rows ascending.
+long orc_nlist_cell(int N, const double* pos, const int32_t* type, int ntypes, const double* L,
+                    const double* rlistsq, const int32_t* ex_start, const int32_t* ex_idx,
+                    int32_t* start, int32_t* idx, long cap)
+{
+    const Box b = make_box(L);
+    const Excl ex{ex_start, ex_idx};
+    double rmax = 0.0;
+    for (int t = 0; t < ntypes * ntypes; ++t) rmax = std::max(rmax, std::sqrt(rlistsq[t]));
+    int dim[3];
+    for (int d = 0; d < 3; ++d) {
+        dim[d] = rmax > 0.0 ? (int)std::floor(L[d] / rmax) : 1;
+        if (dim[d] < 3) dim[d] = 1;  // too few cells: scan everything along d
+    }
+    const int ncell = dim[0] * dim[1] * dim[2];
+    std::vector<int> cell_of(N), head(ncell + 1, 0), order(N);
+    for (int i = 0; i < N; ++i) {
+        int c[3];
+        for (int d = 0; d < 3; ++d) {
+            const double f = (pos[4 * i + d] - b.lo[d]) * b.Linv[d];
+            int ci = (int)std::floor(f * dim[d]);
+            ci = ((ci % dim[d]) + dim[d]) % dim[d];
+            c[d] = ci;
+        }
+        cell_of[i] = (c[2] * dim[1] + c[1]) * dim[0] + c[0];
+        head[cell_of[i] + 1]++;
+    }
+    for (int c = 0; c < ncell; ++c) head[c + 1] += head[c];
+    {
+        std::vector<int> fill(head.begin(), head.end() - 1);
+        for (int i = 0; i < N; ++i) order[fill[cell_of[i]]++] = i;
+    }
+    const int rx = dim[0] >= 3 ? 1 : 0, ry = dim[1] >= 3 ? 1 : 0, rz = dim[2] >= 3 ? 1 : 0;
+    auto gather_row = [&](int i, std::vector<int>& row) {
+        row.clear();
+        const int c = cell_of[i];
+        const int cx = c % dim[0], cy = (c / dim[0]) % dim[1], cz = c / (dim[0] * dim[1]);
+        for (int oz = -rz; oz <= rz; ++oz)
+            for (int oy = -ry; oy <= ry; ++oy)
+                for (int ox = -rx; ox <= rx; ++ox) {
+                    const int nx = (cx + ox + dim[0]) % dim[0];
+                    const int ny = (cy + oy + dim[1]) % dim[1];
+                    const int nz = (cz + oz + dim[2]) % dim[2];
+                    const int nc = (nz * dim[1] + ny) * dim[0] + nx;
+                    for (int s = head[nc]; s < head[nc + 1]; ++s) {
+                        const int j = order[s];
+                        if (j == i) continue;
+                        if (!listed(b, pos, type, ntypes, rlistsq, i, j)) continue;
+                        if (excluded(ex, i, j)) continue;
+                        row.push_back(j);
+                    }
+                }
+        std::sort(row.begin(), row.end());
+        row.erase(std::unique(row.begin(), row.end()), row.end());
+    };
+    std::vector<long> cnt(N + 1, 0);
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+    {
+        std::vector<int> row;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 512)
+#endif
+        for (int i = 0; i < N; ++i) {
+            gather_row(i, row);
+            cnt[i + 1] = (long)row.size();
+        }
+    }
+    for (int i = 0; i < N; ++i) cnt[i + 1] += cnt[i];
+    if (cnt[N] > cap) return -cnt[N];
+    for (int i = 0; i <= N; ++i) start[i] = (int32_t)cnt[i];
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+    {
+        std::vector<int> row;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 512)
+#endif
+        for (int i = 0; i < N; ++i) {
+            gather_row(i, row);
+            std::copy(row.begin(), row.end(), idx + cnt[i]);
+        }
+    }
+    return cnt[N];
+}
+
+// ---- pair forces over a CSR full list.
+// params[(ti*ntypes+tj)*pstride ...], rcutsq / ronsq per type pair.
+// Outputs are OVERWRITTEN: force[N*3], energy[N], virial[N*6] (xx,xy,xz,yy,yz,zz).
+void orc_pair_forces(int N, const double* pos, const int32_t* type, int ntypes, const double* L,
+                     const int32_t* start, const int32_t* idx, int kind, const double* params, int pstride,
+                     const double* rcutsq, const double* ronsq, int mode, double* force, double* energy,
+                     double* virial)
+{
+    const Box b = make_box(L);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+    for (int i = 0; i < N; ++i) {
+        double F[3] = {0, 0, 0}, U = 0.0, W[6] = {0, 0, 0, 0, 0, 0};
+        const int ti = type[i];
+        for (int k = start[i]; k < start[i + 1]; ++k) {
+            const int j = idx[k];
+            double v[3] = {pos[4 * i] - pos[4 * j], pos[4 * i + 1] - pos[4 * j + 1], pos[4 * i + 2] - pos[4 * j + 2]};
+            min_image(b, v);
+            const double rs = rsq_of(v);
+            const int tp = ti * ntypes + type[j];
+            const double rc2 = rcutsq[tp];
+            const double ro2 = ronsq ? ronsq[tp] : 0.0;
+            bool shift = (mode == MODE_SHIFT);
+            if (mode == MODE_XPLOR && ro2 > rc2) shift = true;
+            double fdr = 0.0, e = 0.0;
+            if (!eval_pair(kind, params + (size_t)tp * pstride, rs, rc2, shift, fdr, e)) continue;
+            if (mode == MODE_XPLOR && rs >= ro2 && rs < rc2) {
+                // XPLOR smoothing S(r) between r_on and r_cut
+                const double den = (rc2 - ro2) * (rc2 - ro2) * (rc2 - ro2);
+                const double a = rs - rc2;
+                const double s = a * a * (rc2 + 2.0 * rs - 3.0 * ro2) / den;
+                const double dsdr_r = 12.0 * (rs - ro2) * a / den;
+                fdr = s * fdr - dsdr_r * e;
+                e = e * s;
+            }
+            F[0] += v[0] * fdr;
+            F[1] += v[1] * fdr;
+            F[2] += v[2] * fdr;
+            U += 0.5 * e;
+            const double h = 0.5 * fdr;
+            W[0] += h * v[0] * v[0];
+            W[1] += h * v[0] * v[1];
+            W[2] += h * v[0] * v[2];
+            W[3] += h * v[1] * v[1];
+            W[4] += h * v[1] * v[2];
+            W[5] += h * v[2] * v[2];
+        }
+        for (int d = 0; d < 3; ++d) force[3 * i + d] = F[d];
+        energy[i] = U;
+        if (virial)
+            for (int c = 0; c < 6; ++c) virial[6 * i + c] = W[c];
+    }
+}
+
+// ---- bond forces. bonds[2*b] = {a, b} particle indices; btype[b]; params[t*8...].
+// ACCUMULATES into force/energy/virial. Returns 0, or 1 + index of the first
+// bond whose evaluator refused (r_0 == 0 / r_1 == r_0), like the device flag.
+long orc_bond_forces(int N, const double* pos, const double* L, long nbonds, const int32_t* bonds,
+                     const int32_t* btype, int kind, const double* params, int pstride, double* force,
+                     double* energy, double* virial)
+{
+    (void)N;
+    const Box b = make_box(L);
+    for (long k = 0; k < nbonds; ++k) {
+        const int ia = bonds[2 * k], ib = bonds[2 * k + 1];
+        double v[3] = {pos[4 * ib] - pos[4 * ia], pos[4 * ib + 1] - pos[4 * ia + 1], pos[4 * ib + 2] - pos[4 * ia + 2]};
+        min_image(b, v);
+        const double rs = rsq_of(v);
+        double fdr = 0.0, e = 0.0;
+        if (!eval_bond(kind, params + (size_t)btype[k] * pstride, rs, fdr, e)) return 1 + k;
+        e *= 0.5;
+        const double h = 0.5 * fdr;
+        const double w[6] = {h * v[0] * v[0], h * v[0] * v[1], h * v[0] * v[2], h * v[1] * v[1], h * v[1] * v[2], h * v[2] * v[2]};
+        for (int d = 0; d < 3; ++d) {
+            force[3 * ib + d] += fdr * v[d];
+            force[3 * ia + d] -= fdr * v[d];
+        }
+        energy[ia] += e;
+        energy[ib] += e;
+        if (virial)
+            for (int c = 0; c < 6; ++c) {
+                virial[6 * ia + c] += w[c];
+                virial[6 * ib + c] += w[c];
+            }
+    }
+    return 0;
+}
+
+// ---- bond forces from a per-particle table (each bond listed on both ends):
+// bt_start[N+1], bt_partner[], bt_type[]. For particle i and partner j,
+// dx = x_i - x_j (minimum image) and F_i += dx * f/r, U_i += U/2, W_i += dx dx f/(2r).
+// ACCUMULATES. Parallel over particles. Returns 0, or 1 + the first failing particle.
+long orc_bond_forces_pp(int N, const double* pos, const double* L, const int32_t* bt_start,
+                        const int32_t* bt_partner, const int32_t* bt_type, int kind, const double* params,
+                        int pstride, double* force, double* energy, double* virial)
+{
+    const Box b = make_box(L);
+    long fail = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(max : fail)
+#endif
+    for (int i = 0; i < N; ++i) {
+        for (int k = bt_start[i]; k < bt_start[i + 1]; ++k) {
+            const int j = bt_partner[k];
+            double v[3] = {pos[4 * i] - pos[4 * j], pos[4 * i + 1] - pos[4 * j + 1], pos[4 * i + 2] - pos[4 * j + 2]};
+            min_image(b, v);
+            const double rs = rsq_of(v);
+            double fdr = 0.0, e = 0.0;
+            if (!eval_bond(kind, params + (size_t)bt_type[k] * pstride, rs, fdr, e)) {
+                fail = std::max<long>(fail, 1 + i);
+                continue;
+            }
+            for (int d = 0; d < 3; ++d) force[3 * i + d] += fdr * v[d];
+            energy[i] += 0.5 * e;
+            if (virial) {
+                const double h = 0.5 * fdr;
+                virial[6 * i + 0] += h * v[0] * v[0];
+                virial[6 * i + 1] += h * v[0] * v[1];
+                virial[6 * i + 2] += h * v[0] * v[2];
+                virial[6 * i + 3] += h * v[1] * v[1];
+                virial[6 * i + 4] += h * v[1] * v[2];
+                virial[6 * i + 5] += h * v[2] * v[2];
+            }
+        }
+    }
+    return fail;
+}
+
+// ---- integrators. pos[N*4] (w ignored), vel[N*4] (w = mass), accel[N*3], image[N*3].
+void orc_langevin_step1(int N, double* pos, int32_t* image, double* vel, const double* accel, const double* L,
+                        double dt)
+{
+    const Box b = make_box(L);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i = 0; i < N; ++i) {
+        double x[3], v[3];
+        for (int d = 0; d < 3; ++d) {
+            x[d] = pos[4 * i + d];
+            v[d] = vel[4 * i + d];
+        }
+        for (int d = 0; d < 3; ++d) x[d] += (v[d] + 0.5 * dt * accel[3 * i + d]) * dt;
+        wrap(b, x, image + 3 * i);
+        for (int d = 0; d < 3; ++d) v[d] += 0.5 * dt * accel[3 * i + d];
+        for (int d = 0; d < 3; ++d) {
+            pos[4 * i + d] = x[d];
+            vel[4 * i + d] = v[d];
+        }
+    }
+}
+
+// gamma: per-type table (use_lambda == 0) or lambda * diameter[i].
+void orc_langevin_step2(int N, const double* pos, const int32_t* type, double* vel, double* accel,
+                        const double* net_force, const uint32_t* tag, const double* diameter,
+                        const double* gamma, int use_lambda, double lambda, int flow_kind, const double* flow_p,
+                        double kT, double dt, uint64_t timestep, uint32_t seed, int noiseless)
+{
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i = 0; i < N; ++i) {
+        const double g = use_lambda ? lambda * diameter[i] : gamma[type[i]];
+        double u[3];
+        orc_flow(flow_kind, flow_p, pos + 4 * i, u);
+        double c = std::sqrt(6.0 * g * kT / dt);
+        if (noiseless) c = 0.0;
+        double R[3];
+        uniform3(202, timestep, seed, tag[i], -c, c, R);
+        const double m = vel[4 * i + 3];
+        const double minv = 1.0 / m;
+        for (int d = 0; d < 3; ++d) {
+            const double bd = R[d] - g * (vel[4 * i + d] - u[d]);
+            const double a = (net_force[3 * i + d] + bd) * minv;
+            vel[4 * i + d] += 0.5 * dt * a;
+            accel[3 * i + d] = a;
+        }
+    }
+}
+
+void orc_brownian(int N, double* pos, int32_t* image, const int32_t* type, const double* net_force,
+                  const uint32_t* tag, const double* diameter, const double* gamma, int use_lambda, double lambda,
+                  int flow_kind, const double* flow_p, const double* L, double kT, double dt, uint64_t timestep,
+                  uint32_t seed, int noiseless)
+{
+    const Box b = make_box(L);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i = 0; i < N; ++i) {
+        const double g = use_lambda ? lambda * diameter[i] : gamma[type[i]];
+        double x[3] = {pos[4 * i], pos[4 * i + 1], pos[4 * i + 2]};
+        double u[3];
+        orc_flow(flow_kind, flow_p, x, u);
+        double c = std::sqrt(6.0 * g * kT / dt);
+        if (noiseless) c = 0.0;
+        double R[3];
+        uniform3(201, timestep, seed, tag[i], -c, c, R);
+        for (int d = 0; d < 3; ++d) x[d] += (u[d] + (net_force[3 * i + d] + R[d]) / g) * dt;
+        wrap(b, x, image + 3 * i);
+        for (int d = 0; d < 3; ++d) pos[4 * i + d] = x[d];
+    }
+}
+
+// ---- maximum squared displacement since the last list build
+double orc_max_disp2(int N, const double* pos, const double* pos_build, const double* L)
+{
+    const Box b = make_box(L);
+    double m = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(max : m)
+#endif
+    for (int i = 0; i < N; ++i) {
+        double v[3] = {pos[4 * i] - pos_build[4 * i], pos[4 * i + 1] - pos_build[4 * i + 1], pos[4 * i + 2] - pos_build[4 * i + 2]};
+        min_image(b, v);
+        m = std::max(m, rsq_of(v));
+    }
+    return m;
+}
+
+}  // extern "C"

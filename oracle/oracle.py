@@ -1,0 +1,396 @@
+"""ctypes front end of the CPU oracle (``azp_oracle.cpp``).
+
+TEST INFRASTRUCTURE ONLY. The tests, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` use it as the checker; the product package
+``azplugins_gb300`` never imports it.
+
+The oracle restates, in FP64, the azplugins short-range force-and-integrate
+path (evaluators from ``src/PairEvaluator*.h`` / ``src/BondEvaluator*.h``,
+flow fields ``src/ConstantFlow.h`` / ``src/ParabolicFlow.h``, the legacy flow
+integrators ``src/TwoStepLangevinFlow.h:128-245`` and
+``src/TwoStepBrownianFlow.h:136-178``) plus HOOMD's pair / bond / neighbour
+list loops, which are not in the azplugins tree. Every function of the C file
+cites the reference line it follows.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "libazp_oracle.so")
+
+PAIR_KINDS = {
+    "PerturbedLennardJones": 0,
+    "ExpandedYukawa": 1,
+    "Hertz": 2,
+    "Colloid": 3,
+    "DPDGeneralWeight": 4,
+}
+BOND_KINDS = {"Quartic": 0, "DoubleWell": 1}
+
+# dict keys in the order the C parameter builders read them
+PAIR_KEYS = {
+    "PerturbedLennardJones": ("epsilon", "sigma", "attraction_scale_factor"),
+    "ExpandedYukawa": ("epsilon", "kappa", "delta"),
+    "Hertz": ("epsilon",),
+    "Colloid": ("A", "a_1", "a_2", "sigma"),
+    "DPDGeneralWeight": ("A", "gamma", "s"),
+}
+BOND_KEYS = {
+    "Quartic": ("k", "r_0", "b_1", "b_2", "U_0", "sigma", "epsilon", "delta"),
+    "DoubleWell": ("r_0", "r_1", "U_1", "U_tilt"),
+}
+PAIR_STRIDE = 4
+BOND_STRIDE = 8
+MODES = {"none": 0, "shift": 1, "xplor": 2}
+
+_lib = None
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+
+
+def build():
+    """Compile the oracle library with its recipe (g++, a second or two)."""
+    subprocess.run(["bash", os.path.join(_HERE, "build_oracle.sh")], check=True)
+
+
+def lib():
+    """Load (building on first use) the oracle shared library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        build()
+    L = ctypes.CDLL(_LIB_PATH)
+    c_int, c_long, c_double, c_u32, c_u64 = (
+        ctypes.c_int,
+        ctypes.c_long,
+        ctypes.c_double,
+        ctypes.c_uint32,
+        ctypes.c_uint64,
+    )
+    vp = ctypes.c_void_p
+    L.orc_version.restype = c_int
+    L.orc_set_threads.argtypes = [c_int]
+    L.orc_set_threads.restype = c_int
+    L.orc_pair_params.argtypes = [c_int, _dp, _dp]
+    L.orc_bond_params.argtypes = [c_int, _dp, _dp]
+    L.orc_pair_eval.argtypes = [c_int, _dp, c_double, c_double, c_int, ctypes.POINTER(c_double), ctypes.POINTER(c_double)]
+    L.orc_bond_eval.argtypes = [c_int, _dp, c_double, ctypes.POINTER(c_double), ctypes.POINTER(c_double)]
+    L.orc_flow.argtypes = [c_int, _dp, _dp, _dp]
+    L.orc_philox4x32_10.argtypes = [_up, _up, _up]
+    L.orc_uniform3.argtypes = [c_int, c_u64, c_u32, c_u32, c_double, c_double, _dp]
+    for fn in (L.orc_nlist_brute, L.orc_nlist_cell):
+        fn.argtypes = [c_int, _dp, _ip, c_int, _dp, _dp, vp, vp, _ip, _ip, c_long]
+        fn.restype = c_long
+    L.orc_pair_forces.argtypes = [c_int, _dp, _ip, c_int, _dp, _ip, _ip, c_int, _dp, c_int, _dp, vp, c_int, _dp, _dp, vp]
+    L.orc_bond_forces.argtypes = [c_int, _dp, _dp, c_long, _ip, _ip, c_int, _dp, c_int, _dp, _dp, vp]
+    L.orc_bond_forces.restype = c_long
+    L.orc_bond_forces_pp.argtypes = [c_int, _dp, _dp, _ip, _ip, _ip, c_int, _dp, c_int, _dp, _dp, vp]
+    L.orc_bond_forces_pp.restype = c_long
+    L.orc_langevin_step1.argtypes = [c_int, _dp, _ip, _dp, _dp, _dp, c_double]
+    L.orc_langevin_step2.argtypes = [c_int, _dp, _ip, _dp, _dp, _dp, _up, vp, _dp, c_int, c_double, c_int, _dp, c_double, c_double, c_u64, c_u32, c_int]
+    L.orc_brownian.argtypes = [c_int, _dp, _ip, _ip, _dp, _up, vp, _dp, c_int, c_double, c_int, _dp, _dp, c_double, c_double, c_u64, c_u32, c_int]
+    L.orc_max_disp2.argtypes = [c_int, _dp, _dp, _dp]
+    L.orc_max_disp2.restype = c_double
+    _lib = L
+    return L
+
+
+def set_threads(n: int) -> int:
+    """Threads for every parallel phase; returns the count in effect."""
+    return lib().orc_set_threads(int(n))
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+# ------------------------------------------------------------------ evaluators
+def pair_params(name: str, d: dict) -> np.ndarray:
+    """The reference param_type fields built from a parameter dict (padded to 4)."""
+    vals = np.array([float(d[k]) for k in PAIR_KEYS[name]], dtype=np.float64)
+    out = np.zeros(PAIR_STRIDE, dtype=np.float64)
+    lib().orc_pair_params(PAIR_KINDS[name], np.ascontiguousarray(vals), out)
+    return out
+
+
+def bond_params(name: str, d: dict) -> np.ndarray:
+    vals = np.array([float(d[k]) for k in BOND_KEYS[name]], dtype=np.float64)
+    out = np.zeros(BOND_STRIDE, dtype=np.float64)
+    lib().orc_bond_params(BOND_KINDS[name], np.ascontiguousarray(vals), out)
+    return out
+
+
+def pair_eval(name: str, p: np.ndarray, rsq: float, rcutsq: float, shift: bool):
+    f, e = ctypes.c_double(), ctypes.c_double()
+    ok = lib().orc_pair_eval(PAIR_KINDS[name], np.ascontiguousarray(p, dtype=np.float64), rsq, rcutsq, int(shift), ctypes.byref(f), ctypes.byref(e))
+    return bool(ok), f.value, e.value
+
+
+def bond_eval(name: str, p: np.ndarray, rsq: float):
+    f, e = ctypes.c_double(), ctypes.c_double()
+    ok = lib().orc_bond_eval(BOND_KINDS[name], np.ascontiguousarray(p, dtype=np.float64), rsq, ctypes.byref(f), ctypes.byref(e))
+    return bool(ok), f.value, e.value
+
+
+def flow(kind: int, fp, r):
+    out = np.zeros(3)
+    lib().orc_flow(kind, np.ascontiguousarray(fp, dtype=np.float64), np.ascontiguousarray(r, dtype=np.float64), out)
+    return out
+
+
+def philox(ctr, key):
+    out = np.zeros(4, dtype=np.uint32)
+    lib().orc_philox4x32_10(np.ascontiguousarray(ctr, dtype=np.uint32), np.ascontiguousarray(key, dtype=np.uint32), out)
+    return out
+
+
+def uniform3(rng_id: int, timestep: int, seed: int, tag: int, lo: float, hi: float):
+    out = np.zeros(3)
+    lib().orc_uniform3(rng_id, timestep, seed, tag, lo, hi, out)
+    return out
+
+
+# ------------------------------------------------------------------ neighbour list
+def _excl_csr(N, exclusions):
+    """exclusions: iterable of (i, j) pairs -> CSR arrays (both directions)."""
+    if exclusions is None or len(exclusions) == 0:
+        return None, None
+    ex = np.asarray(exclusions, dtype=np.int64).reshape(-1, 2)
+    a = np.concatenate([ex[:, 0], ex[:, 1]])
+    b = np.concatenate([ex[:, 1], ex[:, 0]])
+    order = np.lexsort((b, a))
+    a, b = a[order], b[order]
+    start = np.zeros(N + 1, dtype=np.int32)
+    np.add.at(start, a + 1, 1)
+    start = np.cumsum(start).astype(np.int32)
+    return start, np.ascontiguousarray(b, dtype=np.int32)
+
+
+def nlist(pos4, types, ntypes, L, rlistsq, exclusions=None, method="cell"):
+    """Full neighbour list as CSR (start[N+1], idx) with ascending rows."""
+    N = pos4.shape[0]
+    pos4 = np.ascontiguousarray(pos4, dtype=np.float64)
+    types = np.ascontiguousarray(types, dtype=np.int32)
+    L = np.ascontiguousarray(L, dtype=np.float64)
+    rlistsq = np.ascontiguousarray(rlistsq, dtype=np.float64).reshape(-1)
+    es, ei = _excl_csr(N, exclusions)
+    fn = lib().orc_nlist_brute if method == "brute" else lib().orc_nlist_cell
+    cap = max(64 * N, 1024)
+    while True:
+        start = np.zeros(N + 1, dtype=np.int32)
+        idx = np.zeros(cap, dtype=np.int32)
+        n = fn(N, pos4, types, ntypes, L, rlistsq, _ptr(es), _ptr(ei), start, idx, cap)
+        if n >= 0:
+            return start, idx[:n].copy()
+        cap = -n + 16
+
+
+# ------------------------------------------------------------------ forces
+def pair_forces(pos4, types, ntypes, L, start, idx, name, params, rcutsq, ronsq=None, mode="none"):
+    """Pair force, per-particle energy (half per pair) and virial (xx,xy,xz,yy,yz,zz)."""
+    N = pos4.shape[0]
+    F = np.zeros((N, 3))
+    U = np.zeros(N)
+    W = np.zeros((N, 6))
+    ron = None if ronsq is None else np.ascontiguousarray(ronsq, dtype=np.float64).reshape(-1)
+    lib().orc_pair_forces(
+        N,
+        np.ascontiguousarray(pos4, dtype=np.float64),
+        np.ascontiguousarray(types, dtype=np.int32),
+        ntypes,
+        np.ascontiguousarray(L, dtype=np.float64),
+        np.ascontiguousarray(start, dtype=np.int32),
+        np.ascontiguousarray(idx, dtype=np.int32),
+        PAIR_KINDS[name],
+        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        PAIR_STRIDE,
+        np.ascontiguousarray(rcutsq, dtype=np.float64).reshape(-1),
+        _ptr(ron),
+        MODES[mode],
+        F,
+        U,
+        _ptr(W),
+    )
+    return F, U, W
+
+
+def bond_forces(pos4, L, bonds, btypes, name, params, F=None, U=None, W=None):
+    """Bond forces (accumulated into F/U/W if given). Raises on a refused bond."""
+    N = pos4.shape[0]
+    F = np.zeros((N, 3)) if F is None else F
+    U = np.zeros(N) if U is None else U
+    W = np.zeros((N, 6)) if W is None else W
+    bonds = np.ascontiguousarray(bonds, dtype=np.int32).reshape(-1, 2)
+    rc = lib().orc_bond_forces(
+        N,
+        np.ascontiguousarray(pos4, dtype=np.float64),
+        np.ascontiguousarray(L, dtype=np.float64),
+        bonds.shape[0],
+        bonds,
+        np.ascontiguousarray(btypes, dtype=np.int32),
+        BOND_KINDS[name],
+        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        BOND_STRIDE,
+        F,
+        U,
+        _ptr(W),
+    )
+    if rc:
+        raise RuntimeError(f"bond.{name}: bond out of bounds (bond {rc - 1})")
+    return F, U, W
+
+
+def bond_table(N, bonds, btypes):
+    """Per-particle bond table (each bond on both ends): start[N+1], partner, type."""
+    bonds = np.asarray(bonds, dtype=np.int64).reshape(-1, 2)
+    bt = np.asarray(btypes, dtype=np.int64)
+    a = np.concatenate([bonds[:, 0], bonds[:, 1]])
+    b = np.concatenate([bonds[:, 1], bonds[:, 0]])
+    t = np.concatenate([bt, bt])
+    order = np.argsort(a, kind="stable")
+    start = np.zeros(N + 1, dtype=np.int64)
+    np.add.at(start, a + 1, 1)
+    start = np.cumsum(start)
+    return start.astype(np.int32), b[order].astype(np.int32), t[order].astype(np.int32)
+
+
+def bond_forces_pp(pos4, L, table, name, params, F, U, W=None):
+    start, partner, btype = table
+    rc = lib().orc_bond_forces_pp(
+        pos4.shape[0],
+        pos4,
+        np.ascontiguousarray(L, dtype=np.float64),
+        start,
+        partner,
+        btype,
+        BOND_KINDS[name],
+        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        BOND_STRIDE,
+        F,
+        U,
+        _ptr(W),
+    )
+    if rc:
+        raise RuntimeError(f"bond.{name}: bond out of bounds (particle {rc - 1})")
+
+
+# ------------------------------------------------------------------ integrators
+FLOW_CONSTANT, FLOW_PARABOLIC = 0, 1
+
+
+def langevin_step1(pos4, image, vel4, accel, L, dt):
+    lib().orc_langevin_step1(pos4.shape[0], pos4, image, vel4, accel, np.ascontiguousarray(L, dtype=np.float64), dt)
+
+
+def langevin_step2(pos4, types, vel4, accel, net_force, tags, gamma, flow_kind, flow_p, kT, dt, timestep, seed,
+                   noiseless=False, diameter=None, use_lambda=False, lam=0.0):
+    lib().orc_langevin_step2(
+        pos4.shape[0], pos4, types, vel4, accel, np.ascontiguousarray(net_force, dtype=np.float64), tags,
+        _ptr(diameter), np.ascontiguousarray(gamma, dtype=np.float64), int(use_lambda), lam, flow_kind,
+        np.ascontiguousarray(flow_p, dtype=np.float64), kT, dt, timestep, seed, int(noiseless))
+
+
+def brownian(pos4, image, types, net_force, tags, gamma, flow_kind, flow_p, L, kT, dt, timestep, seed,
+             noiseless=False, diameter=None, use_lambda=False, lam=0.0):
+    lib().orc_brownian(
+        pos4.shape[0], pos4, image, types, np.ascontiguousarray(net_force, dtype=np.float64), tags, _ptr(diameter),
+        np.ascontiguousarray(gamma, dtype=np.float64), int(use_lambda), lam, flow_kind,
+        np.ascontiguousarray(flow_p, dtype=np.float64), np.ascontiguousarray(L, dtype=np.float64), kT, dt, timestep,
+        seed, int(noiseless))
+
+
+def max_disp2(pos4, pos_build, L):
+    return lib().orc_max_disp2(pos4.shape[0], pos4, pos_build, np.ascontiguousarray(L, dtype=np.float64))
+
+
+class OracleMD:
+    """HOOMD-order MD loop on the oracle: step one, list check, forces, step two.
+
+    ``system`` is a dict of numpy arrays in tag order (see tests/systems.py):
+    pos4 (N,4: x,y,z,type), vel4 (N,4: v, mass), accel (N,3), image (N,3),
+    types (N,), tags (N,), L (3,), bonds (B,2), btypes (B,).
+    """
+
+    def __init__(self, system, pair=None, bond=None, method="langevin", gamma=(1.0,), flow_kind=0,
+                 flow_p=(0.0, 0.0, 0.0), kT=1.0, dt=0.005, seed=0, r_buff=0.4, noiseless=False, exclude_bonds=True):
+        self.s = {k: (np.ascontiguousarray(v).copy() if isinstance(v, np.ndarray) else v) for k, v in system.items()}
+        s = self.s
+        self.N = s["pos4"].shape[0]
+        self.pair = pair  # dict(name, params[ntypes,ntypes,4], rcut[ntypes,ntypes], ron, mode)
+        self.bond = bond  # dict(name, params[nbt,8])
+        self.method = method
+        self.gamma = np.asarray(gamma, dtype=np.float64)
+        self.flow_kind = flow_kind
+        self.flow_p = np.asarray(flow_p, dtype=np.float64)
+        self.kT, self.dt, self.seed = kT, dt, seed
+        self.r_buff = r_buff
+        self.noiseless = noiseless
+        self.timestep = int(s.get("timestep", 0))
+        self.ntypes = int(s.get("ntypes", int(s["types"].max()) + 1))
+        self.exclusions = s["bonds"] if (exclude_bonds and s.get("bonds") is not None and len(s["bonds"])) else None
+        self.table = oracle_table = None
+        if bond is not None and s.get("bonds") is not None and len(s["bonds"]):
+            self.table = bond_table(self.N, s["bonds"], s["btypes"])
+        self.pos_build = None
+        self.nlist_csr = None
+        self.builds = 0
+        del oracle_table
+
+    def _rlistsq(self):
+        rc = np.asarray(self.pair["rcut"], dtype=np.float64)
+        rl = np.where(rc > 0, rc + self.r_buff, 0.0)
+        return rl * rl
+
+    def _check_build(self):
+        s = self.s
+        if self.pos_build is not None:
+            if max_disp2(s["pos4"], self.pos_build, s["L"]) <= (0.5 * self.r_buff) ** 2:
+                return
+        self.nlist_csr = nlist(s["pos4"], s["types"], self.ntypes, s["L"], self._rlistsq(), self.exclusions)
+        self.pos_build = s["pos4"].copy()
+        self.builds += 1
+
+    def forces(self):
+        s = self.s
+        N = self.N
+        F = np.zeros((N, 3))
+        U = np.zeros(N)
+        W = np.zeros((N, 6))
+        if self.pair is not None:
+            self._check_build()
+            rc = np.asarray(self.pair["rcut"], dtype=np.float64)
+            ron = self.pair.get("ron")
+            ronsq = None if ron is None else np.asarray(ron, dtype=np.float64) ** 2
+            F, U, W = pair_forces(s["pos4"], s["types"], self.ntypes, s["L"], *self.nlist_csr, self.pair["name"],
+                                  self.pair["params"], rc * rc, ronsq, self.pair.get("mode", "none"))
+        if self.bond is not None and self.table is not None:
+            bond_forces_pp(s["pos4"], s["L"], self.table, self.bond["name"], self.bond["params"], F, U, W)
+        return F, U, W
+
+    def step(self):
+        s = self.s
+        t = self.timestep
+        if self.method == "langevin":
+            langevin_step1(s["pos4"], s["image"], s["vel4"], s["accel"], s["L"], self.dt)
+            F, U, W = self.forces()
+            langevin_step2(s["pos4"], s["types"], s["vel4"], s["accel"], F, s["tags"], self.gamma, self.flow_kind,
+                           self.flow_p, self.kT, self.dt, t, self.seed, self.noiseless)
+        else:
+            F, U, W = self.forces()
+            brownian(s["pos4"], s["image"], s["types"], F, s["tags"], self.gamma, self.flow_kind, self.flow_p,
+                     s["L"], self.kT, self.dt, t, self.seed, self.noiseless)
+        self.timestep = t + 1
+        self.last = (F, U, W)
+
+    def run(self, steps):
+        for _ in range(int(steps)):
+            self.step()

@@ -1,0 +1,56 @@
+"""Extract the known-answer cases of the reference's own tests into kats.json.
+
+Reads ``src/pytest/test_pair.py`` and ``src/pytest/test_bond.py`` of the
+azplugins tree AS TEXT (``ast``; the files import hoomd, which is not needed):
+every ``PotentialTestCase(...)`` call becomes one record with its line number.
+
+Usage: python tests/golden/make_kats.py [/path/to/azplugins]
+"""
+
+from __future__ import annotations
+
+import ast
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _value(node):
+    # dict(k=v, ...) calls are literals too
+    if isinstance(node, ast.Call) and getattr(node.func, "id", None) == "dict":
+        return {kw.arg: ast.literal_eval(kw.value) for kw in node.keywords}
+    return ast.literal_eval(node)
+
+
+def cases(path, fields):
+    tree = ast.parse(open(path).read())
+    out = []
+    for node in ast.walk(tree):
+        if isinstance(node, ast.Call) and getattr(node.func, "id", None) == "PotentialTestCase":
+            pot = node.args[0]
+            name = pot.attr  # hoomd.azplugins.pair.<Name>
+            vals = [_value(a) for a in node.args[1:]]
+            rec = {"potential": name, "line": node.lineno}
+            rec.update(dict(zip(fields, vals)))
+            out.append(rec)
+    return out
+
+
+def main():
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    pair = cases(os.path.join(root, "src", "pytest", "test_pair.py"),
+                 ["params", "r_cut", "shift", "distance", "energy", "force"])
+    bond = cases(os.path.join(root, "src", "pytest", "test_bond.py"), ["params", "distance", "energy", "force"])
+    for r in pair:
+        r["source"] = f"src/pytest/test_pair.py:{r['line']}"
+    for r in bond:
+        r["source"] = f"src/pytest/test_bond.py:{r['line']}"
+    with open(os.path.join(HERE, "kats.json"), "w") as f:
+        json.dump({"pair": pair, "bond": bond}, f, indent=1)
+    print(f"{len(pair)} pair and {len(bond)} bond cases")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,158 @@
+"""The resident engine (sim.run) against the oracle's HOOMD-order MD loop:
+trajectories over 100 steps, run splitting, graph / no-graph equivalence,
+thermodynamic sums, FP32-force mode, and Brownian dynamics."""
+
+import os
+
+import numpy as np
+import pytest
+
+import azplugins_gb300 as az
+from helpers import box_of, force_error, oracle_system, pos4_of, random_fluid, rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _pos_err(a, b, L):
+    d = a - b
+    d -= L * np.rint(d / L)
+    return float(np.abs(d).max())
+
+
+def _lj_setup(snap, precision="fp64", method="langevin", flow=None, seed=5, kT=1.0, dt=0.005, gamma=1.0,
+              lam=0.5, rcut=3.0, mode="none"):
+    sim = az.Simulation(seed=seed, precision=precision)
+    sim.create_state_from_snapshot(snap)
+    nl = az.nlist.Cell(buffer=0.4)
+    lj = az.pair.PerturbedLennardJones(nlist=nl, default_r_cut=rcut, mode=mode)
+    lj.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=lam)
+    flow = flow or az.flow.ConstantFlow((0.0, 0.0, 0.0))
+    cls = az.methods.LangevinFlow if method == "langevin" else az.methods.BrownianFlow
+    m = cls("all", kT=kT, flow_field=flow, default_gamma=gamma)
+    sim.operations.integrator = az.md.Integrator(dt=dt, methods=[m], forces=[lj])
+    return sim, lj
+
+
+def _oracle_lj(orc, snap, seed=5, kT=1.0, dt=0.005, lam=0.5, rcut=3.0, method="langevin", flow_kind=0,
+               flow_p=(0, 0, 0), mode="none", bond=None):
+    rec = orc.pair_params("PerturbedLennardJones", dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=lam))
+    return orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
+                        pair=dict(name="PerturbedLennardJones", params=rec.reshape(1, 1, 4),
+                                  rcut=np.array([[rcut]]), mode=mode),
+                        bond=bond, method=method, gamma=[1.0], kT=kT, dt=dt, seed=seed, flow_kind=flow_kind,
+                        flow_p=flow_p)
+
+
+def test_lj_fluid_100_steps_fp64(orc):
+    from azplugins_gb300 import workloads
+
+    snap = workloads.lj_fluid(n_side=8, density=0.8, seed=21)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    sim, lj = _lj_setup(snap)
+    sim.run(100)
+    md = _oracle_lj(orc, snap)
+    md.run(100)
+    out = sim.state.get_snapshot().particles
+    L = box_of(snap)
+    assert _pos_err(out.position, md.s["pos4"][:, :3], L) < 1e-9
+    assert np.abs(out.velocity - md.s["vel4"][:, :3]).max() < 1e-8
+    assert np.array_equal(out.image, md.s["image"])
+    th = sim.thermo()
+    F, U, W = md.forces()
+    assert rel(th["potential_energy"], U.sum()) < 1e-10
+    assert th["nlist_builds"] >= 2
+
+
+def test_run_splitting_and_graphs_are_bitwise_identical():
+    from azplugins_gb300 import workloads
+
+    snap = workloads.lj_fluid(n_side=10, density=0.8, seed=22)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    results = []
+    for graphs, chunks in [("1", [60]), ("1", [7, 13, 40]), ("0", [60])]:
+        os.environ["AZP_GRAPHS"] = graphs
+        try:
+            sim, lj = _lj_setup(snap)
+            for c in chunks:
+                sim.run(c)
+            results.append(sim.state.get_snapshot().particles)
+        finally:
+            os.environ.pop("AZP_GRAPHS", None)
+    for r in results[1:]:
+        assert np.array_equal(r.position, results[0].position)
+        assert np.array_equal(r.velocity, results[0].velocity)
+        assert np.array_equal(r.image, results[0].image)
+
+
+def test_forces_at_state_match_oracle(orc):
+    snap = random_fluid(1200, 0.8, seed=23)
+    sim, lj = _lj_setup(snap)
+    sim.run(1)
+    s = sim.state.get_snapshot()
+    f, w = sim._engine.forces()
+    md = _oracle_lj(orc, s)
+    F, U, W = md.forces()
+    assert force_error(f, F) < 1e-12
+    assert rel(f[:, 3].sum(), U.sum()) < 1e-12
+
+
+def test_fp32_forces_fp64_integration(orc):
+    from azplugins_gb300 import workloads
+
+    snap = workloads.lj_fluid(n_side=8, density=0.8, seed=24)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    sim, lj = _lj_setup(snap, precision="fp32")
+    sim.run(1)
+    s = sim.state.get_snapshot()
+    f, w = sim._engine.forces()
+    F, U, W = _oracle_lj(orc, s).forces()
+    assert force_error(f, F) < 1e-5
+    sim.run(99)
+    md = _oracle_lj(orc, snap)
+    md.run(100)
+    # FP32 forces: trajectories stay close over 100 steps (0.5 tau)
+    assert _pos_err(sim.state.get_snapshot().particles.position, md.s["pos4"][:, :3], box_of(snap)) < 1e-3
+
+
+def test_bead_spring_parabolic_flow(orc):
+    from azplugins_gb300 import workloads
+
+    snap = workloads.bead_spring_melt(30, 20, density=0.6, seed=25)
+    # relax random-walk overlaps with capped Brownian steps first
+    sim = az.Simulation(seed=9)
+    sim.create_state_from_snapshot(snap)
+    wca = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), default_r_cut=2 ** (1 / 6))
+    wca.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.0)
+    qb = az.bond.Quartic()
+    qb.params["A-A"] = dict(k=1434.3, r_0=1.5, b_1=-0.7589, b_2=0.0, U_0=67.2234, sigma=1.0, epsilon=1.0)
+    relax = az.methods.BrownianFlow("all", kT=1.0, flow_field=az.flow.ConstantFlow((0, 0, 0)), max_displacement=0.02)
+    sim.operations.integrator = az.md.Integrator(dt=0.001, methods=[relax], forces=[wca, qb])
+    sim.run(200)
+    relaxed = sim.state.get_snapshot()
+    relaxed.particles.acceleration = np.zeros((relaxed.particles.N, 3))
+    L = box_of(relaxed)
+    flow = az.flow.ParabolicFlow(mean_velocity=2.0 / 3.0, separation=L[1])
+    sim2 = az.Simulation(seed=10)
+    sim2.create_state_from_snapshot(relaxed)
+    m = az.methods.LangevinFlow("all", kT=1.0, flow_field=flow, default_gamma=1.0)
+    sim2.operations.integrator = az.md.Integrator(dt=0.005, methods=[m], forces=[wca, qb])
+    sim2.run(100)
+    rec = orc.bond_params("Quartic", qb.params["A-A"])
+    md = _oracle_lj(orc, relaxed, seed=10, lam=0.0, rcut=2 ** (1 / 6), flow_kind=1,
+                    flow_p=(2.0 / 3.0, L[1], 0.0), bond=dict(name="Quartic", params=rec.reshape(1, 8)))
+    md.run(100)
+    out = sim2.state.get_snapshot().particles
+    assert _pos_err(out.position, md.s["pos4"][:, :3], L) < 1e-8
+    assert np.abs(out.velocity - md.s["vel4"][:, :3]).max() < 1e-7
+
+
+def test_brownian_colloid_like(orc):
+    snap = random_fluid(800, 0.5, seed=26)
+    sim, lj = _lj_setup(snap, method="brownian", flow=az.flow.ConstantFlow((0.1, 0.0, 0.0)), dt=0.001,
+                        lam=1.0, rcut=2.5)
+    sim.run(50)
+    md = _oracle_lj(orc, snap, method="brownian", dt=0.001, lam=1.0, rcut=2.5, flow_kind=0, flow_p=(0.1, 0, 0))
+    md.run(50)
+    out = sim.state.get_snapshot().particles
+    assert _pos_err(out.position, md.s["pos4"][:, :3], box_of(snap)) < 1e-10
+    assert np.array_equal(out.image, md.s["image"])
