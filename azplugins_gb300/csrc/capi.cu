@@ -194,6 +194,7 @@ int azp_pair_forces(const azp_system* sys, azp_nlist* nl, int kind, const double
     fill_box(sys->box, a.L, a.Linv, a.sfix);
     a.counts = nl->counts;
     a.nbrs = nl->nbrs;
+    a.max_nn = nl->max_nn;
     a.table = nl->table;
     a.force = out->force;
     a.virial = out->virial;

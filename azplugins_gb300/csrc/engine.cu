@@ -428,6 +428,7 @@ MDArgs base_args(azp_md* m)
     }
     a.counts = m->counts;
     a.nbrs = m->nbrs;
+    a.max_nn = m->max_nn;
     a.pair_table = m->d_pair_table;
     a.bt_n = m->bt_n;
     a.bt = m->bt;

@@ -25,6 +25,7 @@ struct MDArgs {
     // pair
     const uint32_t* counts;
     const uint32_t* nbrs;
+    uint32_t max_nn;            // rows allocated: reads stop there even if a count overflowed
     const double* pair_table;   // [ntypes^2][12]
     // bonds (index order)
     const uint32_t* bt_n;

@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
     if (active) {
         // ---------------------------------------------------------------- pair
         if constexpr (!std::is_same<PE, NoPair>::value) {
-            const uint32_t n = a.counts[i];
+            const uint32_t n = min(a.counts[i], a.max_nn);
             if constexpr (std::is_same<R, double>::value) {
                 const double4_32a pi = a.pos[i];
                 const uint32_t ti = type_of(pi.w);

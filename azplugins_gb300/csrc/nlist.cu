@@ -25,11 +25,14 @@ CellGrid make_grid(const azp_box& box, double rlist_max)
 {
     CellGrid g;
     g.ncell = 1;
+    // cell width >= r_list; widened if the grid would exceed 2^24 cells
+    double w = rlist_max;
+    if (w > 0.0) {
+        while ((box.L[0] / w) * (box.L[1] / w) * (box.L[2] / w) > 16777216.0) w *= 1.25;
+    }
     for (int d = 0; d < 3; ++d) {
-        int n = rlist_max > 0.0 ? (int)std::floor(box.L[d] / rlist_max) : 1;
+        int n = w > 0.0 ? (int)std::floor(box.L[d] / w) : 1;
         if (n < 3) n = 1;
-        // keep the grid modest: at most 2^20 cells per axis product is plenty
-        if (n > 1024) n = 1024;
         g.dim[d] = n;
         g.reach[d] = n >= 3 ? 1 : 0;
         g.lo[d] = -0.5 * box.L[d];

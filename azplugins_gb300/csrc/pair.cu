@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(PAIR_BLOCK) k_pair(PairArgs a)
     const bool active = i < a.N;
     PairAccum<Eval, R> acc;
     if (active) {
-        const uint32_t n = a.counts[i];
+        const uint32_t n = min(a.counts[i], a.max_nn);
         if constexpr (std::is_same<R, double>::value) {
             const double4_32a pi = a.pos[i];
             const uint32_t ti = type_of(pi.w);

@@ -26,6 +26,7 @@ struct PairArgs {
     float sfix[3];
     const uint32_t* counts;
     const uint32_t* nbrs;
+    uint32_t max_nn;       // rows allocated: reads stop there even if a count overflowed
     const double* table;   // [ntypes^2][PAIR_TBL]
     void* force;           // double4_32a / float4 [N]
     void* virial;          // [6][pitch] or null
