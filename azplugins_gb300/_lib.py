@@ -156,6 +156,7 @@ _SIGNATURES = [
     ("azp_md_thermo", _i, [_vp, _vp, _vp]),
     ("azp_md_error", _i, [_vp, ctypes.POINTER(_u32), _vp]),
     ("azp_md_last_launches", _u64, [_vp]),
+    ("azp_md_time_step_kernel", _i, [_vp, _i, ctypes.POINTER(ctypes.c_float), _vp]),
 ]
 
 

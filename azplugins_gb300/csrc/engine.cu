@@ -1039,4 +1039,29 @@ int azp_md_error(azp_md* m, uint32_t* err_word, void* stream)
 
 uint64_t azp_md_last_launches(const azp_md* m) { return m ? m->launches : 0; }
 
+int azp_md_time_step_kernel(azp_md* m, int reps, float* ms, void* stream)
+{
+    if (!m || !m->have_state || reps <= 0 || !ms) return AZP_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    const int integ = m->method == AZP_METHOD_BROWNIAN_FLOW ? MD_INTEG_BROWNIAN : MD_INTEG_LANGEVIN;
+    cudaEvent_t e0, e1;
+    AZP_CUDA_TRY(cudaEventCreate(&e0));
+    AZP_CUDA_TRY(cudaEventCreate(&e1));
+    int st = enqueue_step(m, integ, 1, 0, s, 0, 0);  // warm
+    m->cur ^= 1;
+    AZP_CUDA_TRY(cudaEventRecord(e0, s));
+    for (int r = 0; r < reps && st == AZP_OK; ++r) {
+        st = enqueue_step(m, integ, 1, 0, s, 0, 0);
+        m->cur ^= 1;
+    }
+    AZP_CUDA_TRY(cudaEventRecord(e1, s));
+    AZP_CUDA_TRY(cudaEventSynchronize(e1));
+    float t = 0.0f;
+    AZP_CUDA_TRY(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / (float)reps;
+    return st;
+}
+
 }  // extern "C"

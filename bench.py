@@ -1,0 +1,441 @@
+"""Benchmark of the short-range force-and-integrate path on one GB300.
+
+Workload (the headline metric's configuration): a bead-spring melt of 10,486
+linear chains x 100 beads (N = 1,048,600) at number density 0.85, seeded random
+walks with bond length 0.97 relaxed by 200 displacement-capped Brownian steps;
+PerturbedLennardJones with lambda = 0, r_cut = 2^(1/6) (WCA), buffer 0.4, bonded
+pairs excluded; Quartic bonds k = 1434.3, b_1 = -0.7589, b_2 = 0, r_0 = 1.5,
+U_0 = 67.2234, sigma = epsilon = 1; LangevinFlow with ParabolicFlow
+(mean_velocity = 2/3, separation = L: centreline speed 1.0 along x, gradient
+along y as in the reference functor), gamma = 1, kT = 1, dt = 0.005. FP32 pair
+and bond arithmetic (compensated sums) with FP64 integration.
+
+A "step" is one MD timestep (forces + Langevin step two + step one of the next
+timestep, list rebuilds amortised as they happen). ``value`` is timesteps/s
+with the state resident in HBM; ``e2e`` is the same metric through the public
+C ABI with a full host snapshot round trip every step (pinned host buffers:
+positions, velocities, accelerations, images in; the same out, plus the
+thermodynamic sums). The working set (about 0.6 GB) is larger than L2.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+For N > 1 (torchrun, one rank per GPU) every rank advances an independent
+replica (replicas only: the single-system path has no exchange-free sharding).
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "timesteps/s & HBM GB/s vs peak at N=1M; batched & adjoint vs plain at 1e-5 err"
+N_CHAINS, CHAIN_LEN, DENSITY = 10486, 100, 0.85
+QUARTIC = dict(k=1434.3, r_0=1.5, b_1=-0.7589, b_2=0.0, U_0=67.2234, sigma=1.0, epsilon=1.0, delta=0.0)
+DT, KT, GAMMA, R_BUFF = 0.005, 1.0, 1.0, 0.4
+RCUT = 2.0 ** (1.0 / 6.0)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=200)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--chains", type=int, default=N_CHAINS)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_melt(n_chains, seed):
+    from azplugins_gb300 import workloads
+
+    return workloads.bead_spring_melt(n_chains, CHAIN_LEN, DENSITY, 0.97, KT, seed=seed)
+
+
+def forces_and_method(az, flow, precision_unused=None):
+    wca = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=R_BUFF), default_r_cut=RCUT)
+    wca.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.0)
+    qb = az.bond.Quartic()
+    qb.params["A-A"] = QUARTIC
+    return wca, qb
+
+
+def relaxed_melt(az, n_chains, seed):
+    """Random-walk melt with overlaps removed by 200 capped Brownian steps (FP64)."""
+    snap = make_melt(n_chains, seed)
+    sim = az.Simulation(seed=seed, precision="fp64")
+    sim.create_state_from_snapshot(snap)
+    wca, qb = forces_and_method(az, None)
+    relax = az.methods.BrownianFlow("all", kT=KT, flow_field=az.flow.ConstantFlow((0.0, 0.0, 0.0)),
+                                    max_displacement=0.03)
+    sim.operations.integrator = az.md.Integrator(dt=0.002, methods=[relax], forces=[wca, qb])
+    sim.run(200)
+    out = sim.state.get_snapshot()
+    sim.close()
+    p = out.particles
+    rng = np.random.Generator(np.random.PCG64(seed + 1))
+    v = rng.normal(0.0, np.sqrt(KT), size=(p.N, 3))
+    p.velocity = v - v.mean(axis=0)
+    p.acceleration = np.zeros((p.N, 3))
+    # broken bonds (stretched past r_0 by the relaxation), reported
+    g = np.asarray(out.bonds.group)
+    L = np.array(out.configuration.box[:3])
+    d = p.position[g[:, 0]] - p.position[g[:, 1]]
+    d -= L * np.rint(d / L)
+    broken = int((np.sqrt((d * d).sum(axis=1)) >= QUARTIC["r_0"]).sum())
+    return out, broken
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(HERE, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_bytes(n_nbr_mean, n_bond_mean):
+    """Bytes per particle of one fused step launch (FP32 forces, FP64 state):
+    reads fixed_i 16, count 4, list 4 n, bond count 4 + table 8 n_b, pos 32,
+    vel 32, tag 4, build shadow 16; writes pos_next 32, vel 32, fixed_next 16."""
+    return 16 + 4 + 4 * n_nbr_mean + 4 + 8 * n_bond_mean + 32 + 32 + 4 + 16 + 32 + 32 + 16
+
+
+def measured_peak():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(snap, gpu_builds_per_step, seconds=15.0):
+    """The oracle port (OpenMP, all host cores) on a bounded sample of the same
+    workload: full N, a few steps after one untimed step; the list-build cost is
+    timed separately and amortised at the GPU run's rebuild rate."""
+    from oracle import oracle as orc
+    from tests.helpers import oracle_system  # noqa: E402
+
+    cores = orc.set_threads(os.cpu_count() or 1)
+    rec = orc.pair_params("PerturbedLennardJones", dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.0))
+    brec = orc.bond_params("Quartic", QUARTIC)
+    L = np.array(snap.configuration.box[:3])
+    md = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
+                      pair=dict(name="PerturbedLennardJones", params=rec.reshape(1, 1, 4), rcut=np.array([[RCUT]])),
+                      bond=dict(name="Quartic", params=brec.reshape(1, 8)), gamma=[GAMMA], kT=KT, dt=DT, seed=7,
+                      flow_kind=1, flow_p=(2.0 / 3.0, L[1], 0.0), r_buff=R_BUFF)
+    t0 = time.perf_counter()
+    md.step()  # includes the first list build
+    first = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    md.nlist_csr = orc.nlist(md.s["pos4"], md.s["types"], 1, L, np.array([[(RCUT + R_BUFF) ** 2]]), md.exclusions)
+    build = time.perf_counter() - t0
+    md.pos_build = md.s["pos4"].copy()
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds or steps < 2:
+        md.step()
+        steps += 1
+    per_step = (time.perf_counter() - t0) / steps
+    per_step_amortised = per_step + build * gpu_builds_per_step
+    return {"value": 1.0 / per_step_amortised, "unit": "timesteps/s", "cores": cores, "kind": "port",
+            "sample": f"N={snap.particles.N} full system, {steps} timed steps after one untimed step "
+                      f"({first:.2f} s incl. list build); list build {build:.3f} s amortised at "
+                      f"{gpu_builds_per_step:.4f} builds/step; oracle/azp_oracle.cpp, OpenMP {cores} threads"}
+
+
+def run_reference(args):
+    """The reference arm: the CPU oracle port of the path on all host cores."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import azplugins_gb300 as az  # noqa: F401  (snapshot types only, no GPU work)
+    from oracle import oracle as orc
+    from tests.helpers import oracle_system
+
+    snap = make_melt(args.chains, seed=1)
+    cores = orc.set_threads(os.cpu_count() or 1)
+    L = np.array(snap.configuration.box[:3])
+    rec = orc.pair_params("PerturbedLennardJones", dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.0))
+    brec = orc.bond_params("Quartic", QUARTIC)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    # the oracle relaxes its own copy on the host: the same 200 capped Brownian steps
+    relax = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
+                         pair=dict(name="PerturbedLennardJones", params=rec.reshape(1, 1, 4),
+                                   rcut=np.array([[RCUT]])),
+                         bond=dict(name="Quartic", params=brec.reshape(1, 8)), method="brownian", gamma=[GAMMA],
+                         kT=KT, dt=0.002, seed=1, r_buff=R_BUFF, max_disp=0.03)
+    relax.run(200)
+    snap.particles.position = relax.s["pos4"][:, :3].copy()
+    snap.particles.image = relax.s["image"].copy()
+    md = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
+                      pair=dict(name="PerturbedLennardJones", params=rec.reshape(1, 1, 4), rcut=np.array([[RCUT]])),
+                      bond=dict(name="Quartic", params=brec.reshape(1, 8)), gamma=[GAMMA], kT=KT, dt=DT, seed=7,
+                      flow_kind=1, flow_p=(2.0 / 3.0, L[1], 0.0), r_buff=R_BUFF)
+    for _ in range(args.warmup):
+        md.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        md.step()
+    t = time.perf_counter() - t0
+    v = args.steps / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "timesteps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random-walk melt)",
+        "config": {"workload": f"bead-spring melt N={snap.particles.N} PLJ(WCA)+Quartic LangevinFlow(Parabolic)",
+                   "N": snap.particles.N, "chains": args.chains, "chain_length": CHAIN_LEN},
+        "cpu_baseline": {"value": v, "unit": "timesteps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full-N steps after {args.warmup} warm-up steps, "
+                                   "melt relaxed by 200 capped Brownian steps on the host"},
+        "e2e": {"value": v, "unit": "timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import azplugins_gb300 as az
+    from azplugins_gb300 import _lib
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    _lib.load()
+    snap, broken = relaxed_melt(az, args.chains, seed=1 + rank)
+    N = snap.particles.N
+    L = snap.configuration.box[:3]
+    flow = az.flow.ParabolicFlow(mean_velocity=2.0 / 3.0, separation=L[1])
+    wca, qb = forces_and_method(az, flow)
+    sim = az.Simulation(seed=7 + rank, precision=args.precision)
+    sim.create_state_from_snapshot(snap)
+    m = az.methods.LangevinFlow("all", kT=KT, flow_field=flow, default_gamma=GAMMA)
+    sim.operations.integrator = az.md.Integrator(dt=DT, methods=[m], forces=[wca, qb])
+    sim.run(args.warmup)
+    eng = sim._engine
+    builds0 = sim.thermo()["nlist_builds"]
+    stream = torch.cuda.current_stream()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        start.record(stream)
+        eng.run_async(args.steps)
+        end.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = start.elapsed_time(end)
+    launches = eng.last_launches
+    eng.run(0)
+    th = sim.thermo()
+    builds = th["nlist_builds"] - builds0
+    sim._timestep += args.steps
+    sim.state._host_valid = False
+    t_max, value = reduce_over_ranks(ms, args.steps, world, "cuda")
+
+    state_after = sim.state.get_snapshot()
+    n_nbr, n_bond = neighbour_stats(state_after)
+    # end to end through the public C ABI with pinned host buffers
+    e2e = e2e_measure(eng, state_after, args.e2e_steps)
+    # dominant kernel alone (last: it advances the state without list checks)
+    kernel_ms = time_step_kernel(eng, reps=200)
+    bytes_per_launch = algorithmic_bytes(n_nbr, n_bond) * N
+    peak, peak_kind = measured_peak()
+    achieved = bytes_per_launch / (kernel_ms * 1e-3) / 1e9
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "timesteps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
+            "data": "synthetic (seeded random-walk melt, capped-Brownian relaxed)",
+            "config": {"workload": f"bead-spring melt N={N} PLJ(WCA)+Quartic LangevinFlow(Parabolic)",
+                       "N": N, "chains": args.chains, "chain_length": CHAIN_LEN, "density": DENSITY,
+                       "forces": args.precision, "integration": "f64", "dt": DT, "r_buff": R_BUFF,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "working set > L2 (no flush needed)", "broken_bonds_after_relax": broken},
+            "gpu_launches": int(launches),
+            "nlist_builds_per_step": builds / args.steps,
+            "pair_interactions_per_s": None,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "kernel": "k_md_step (fused forces + Langevin step)",
+                         "kernel_ms": kernel_ms, "bytes_per_launch": bytes_per_launch,
+                         "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "mean_neighbours": n_nbr,
+                         "mean_bonds": n_bond},
+            "clocks": clk.summary(),
+            "e2e": e2e,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(state_after, builds / args.steps)
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def reduce_over_ranks(ms, steps, world, device="cpu"):
+    """Slowest rank's time and the whole-job rate (replicas: every rank advanced
+    `steps` timesteps of its own system)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * steps / (ms * 1e-3)
+
+
+def neighbour_stats(s):
+    from azplugins_gb300 import _compute
+
+    N = s.particles.N
+    ex = _compute.exclusions_csr(N, s.bonds.group)
+    pos = _compute.device_positions(s)
+    sysd = _compute.make_system(s, pos)
+    nl = _compute.NeighborList(N, 1, np.array([[RCUT]]), R_BUFF, ex)
+    nl.build(sysd)
+    st, _ = nl.to_csr()
+    nl.close()
+    return float(st[-1]) / N, 2.0 * s.bonds.N / N
+
+
+def time_step_kernel(eng, reps):
+    import torch
+
+    from azplugins_gb300 import _lib
+
+    L = _lib.load()
+    stream = torch.cuda.current_stream()
+    s = ctypes.c_void_p(stream.cuda_stream)
+    ms = ctypes.c_float(0.0)
+    _lib.check(L.azp_md_time_step_kernel(eng._md, reps, ctypes.byref(ms), s), "azp_md_time_step_kernel")
+    return ms.value
+
+
+def e2e_measure(eng, s, steps):
+    """Per step: pinned host snapshot -> device, one timestep, device -> pinned host, thermo sums."""
+    import torch
+
+    from azplugins_gb300 import _lib
+
+    L = _lib.load()
+    p = s.particles
+    N = p.N
+    pos = torch.empty((N, 4), dtype=torch.float64).pin_memory()
+    vel = torch.empty((N, 4), dtype=torch.float64).pin_memory()
+    acc = torch.empty((N, 3), dtype=torch.float64).pin_memory()
+    img = torch.empty((N, 3), dtype=torch.int32).pin_memory()
+    pos[:, :3] = torch.from_numpy(p.position)
+    pos[:, 3] = torch.from_numpy(p.typeid.astype(np.float64))
+    vel[:, :3] = torch.from_numpy(p.velocity)
+    vel[:, 3] = torch.from_numpy(p.mass)
+    acc[:] = torch.from_numpy(p.acceleration)
+    img[:] = torch.from_numpy(p.image)
+    thermo = np.zeros(9)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ts = ctypes.c_uint64(0)
+
+    def one(t):
+        _lib.check(L.azp_md_set_state(eng._md, pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), img.data_ptr(), None,
+                                      t, 0, stream), "set_state")
+        _lib.check(L.azp_md_run(eng._md, 1, stream), "run")
+        _lib.check(L.azp_md_get_state(eng._md, pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), img.data_ptr(),
+                                      ctypes.byref(ts), 0, stream), "get_state")
+        _lib.check(L.azp_md_thermo(eng._md, thermo.ctypes.data, stream), "thermo")
+
+    for t in range(3):
+        one(t)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for t in range(steps):
+        one(3 + t)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    h2d = N * (32 + 32 + 24 + 12)
+    return {"value": steps / dt, "unit": "timesteps/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": h2d + 72, "api": "azp_md_set_state / azp_md_run(1) / azp_md_get_state / azp_md_thermo",
+            "steps": steps}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

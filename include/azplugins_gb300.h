@@ -297,6 +297,10 @@ AZP_API int azp_md_thermo(azp_md* md, double* out, void* stream);
 AZP_API int azp_md_error(azp_md* md, uint32_t* err_word, void* stream);
 /* number of kernel launches issued by the last azp_md_run */
 AZP_API uint64_t azp_md_last_launches(const azp_md* md);
+/* Measurement hook: launch the fused step kernel alone `reps` times (no list
+ * checks or rebuilds; the state advances and is only fit for timing afterwards)
+ * between two CUDA events on `stream`; *ms = mean milliseconds per launch. */
+AZP_API int azp_md_time_step_kernel(azp_md* md, int reps, float* ms, void* stream);
 
 #ifdef __cplusplus
 }

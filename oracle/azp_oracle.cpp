@@ -796,7 +796,7 @@ void orc_langevin_step2(int N, const double* pos, const int32_t* type, double* v
 void orc_brownian(int N, double* pos, int32_t* image, const int32_t* type, const double* net_force,
                   const uint32_t* tag, const double* diameter, const double* gamma, int use_lambda, double lambda,
                   int flow_kind, const double* flow_p, const double* L, double kT, double dt, uint64_t timestep,
-                  uint32_t seed, int noiseless)
+                  uint32_t seed, int noiseless, double max_disp)
 {
     const Box b = make_box(L);
 #ifdef _OPENMP
@@ -811,7 +811,11 @@ void orc_brownian(int N, double* pos, int32_t* image, const int32_t* type, const
         if (noiseless) c = 0.0;
         double R[3];
         uniform3(201, timestep, seed, tag[i], -c, c, R);
-        for (int d = 0; d < 3; ++d) x[d] += (u[d] + (net_force[3 * i + d] + R[d]) / g) * dt;
+        for (int d = 0; d < 3; ++d) {
+            double dd = (u[d] + (net_force[3 * i + d] + R[d]) / g) * dt;
+            if (max_disp > 0.0) dd = std::fmin(std::fmax(dd, -max_disp), max_disp);
+            x[d] += dd;
+        }
         wrap(b, x, image + 3 * i);
         for (int d = 0; d < 3; ++d) pos[4 * i + d] = x[d];
     }

@@ -97,7 +97,7 @@ def lib():
     L.orc_bond_forces_pp.restype = c_long
     L.orc_langevin_step1.argtypes = [c_int, _dp, _ip, _dp, _dp, _dp, c_double]
     L.orc_langevin_step2.argtypes = [c_int, _dp, _ip, _dp, _dp, _dp, _up, vp, _dp, c_int, c_double, c_int, _dp, c_double, c_double, c_u64, c_u32, c_int]
-    L.orc_brownian.argtypes = [c_int, _dp, _ip, _ip, _dp, _up, vp, _dp, c_int, c_double, c_int, _dp, _dp, c_double, c_double, c_u64, c_u32, c_int]
+    L.orc_brownian.argtypes = [c_int, _dp, _ip, _ip, _dp, _up, vp, _dp, c_int, c_double, c_int, _dp, _dp, c_double, c_double, c_u64, c_u32, c_int, c_double]
     L.orc_max_disp2.argtypes = [c_int, _dp, _dp, _dp]
     L.orc_max_disp2.restype = c_double
     _lib = L
@@ -300,12 +300,12 @@ def langevin_step2(pos4, types, vel4, accel, net_force, tags, gamma, flow_kind, 
 
 
 def brownian(pos4, image, types, net_force, tags, gamma, flow_kind, flow_p, L, kT, dt, timestep, seed,
-             noiseless=False, diameter=None, use_lambda=False, lam=0.0):
+             noiseless=False, diameter=None, use_lambda=False, lam=0.0, max_disp=0.0):
     lib().orc_brownian(
         pos4.shape[0], pos4, image, types, np.ascontiguousarray(net_force, dtype=np.float64), tags, _ptr(diameter),
         np.ascontiguousarray(gamma, dtype=np.float64), int(use_lambda), lam, flow_kind,
         np.ascontiguousarray(flow_p, dtype=np.float64), np.ascontiguousarray(L, dtype=np.float64), kT, dt, timestep,
-        seed, int(noiseless))
+        seed, int(noiseless), float(max_disp))
 
 
 def max_disp2(pos4, pos_build, L):
@@ -321,7 +321,8 @@ class OracleMD:
     """
 
     def __init__(self, system, pair=None, bond=None, method="langevin", gamma=(1.0,), flow_kind=0,
-                 flow_p=(0.0, 0.0, 0.0), kT=1.0, dt=0.005, seed=0, r_buff=0.4, noiseless=False, exclude_bonds=True):
+                 flow_p=(0.0, 0.0, 0.0), kT=1.0, dt=0.005, seed=0, r_buff=0.4, noiseless=False, exclude_bonds=True,
+                 max_disp=0.0):
         self.s = {k: (np.ascontiguousarray(v).copy() if isinstance(v, np.ndarray) else v) for k, v in system.items()}
         s = self.s
         self.N = s["pos4"].shape[0]
@@ -334,16 +335,16 @@ class OracleMD:
         self.kT, self.dt, self.seed = kT, dt, seed
         self.r_buff = r_buff
         self.noiseless = noiseless
+        self.max_disp = max_disp
         self.timestep = int(s.get("timestep", 0))
         self.ntypes = int(s.get("ntypes", int(s["types"].max()) + 1))
         self.exclusions = s["bonds"] if (exclude_bonds and s.get("bonds") is not None and len(s["bonds"])) else None
-        self.table = oracle_table = None
+        self.table = None
         if bond is not None and s.get("bonds") is not None and len(s["bonds"]):
             self.table = bond_table(self.N, s["bonds"], s["btypes"])
         self.pos_build = None
         self.nlist_csr = None
         self.builds = 0
-        del oracle_table
 
     def _rlistsq(self):
         rc = np.asarray(self.pair["rcut"], dtype=np.float64)
@@ -387,7 +388,7 @@ class OracleMD:
         else:
             F, U, W = self.forces()
             brownian(s["pos4"], s["image"], s["types"], F, s["tags"], self.gamma, self.flow_kind, self.flow_p,
-                     s["L"], self.kT, self.dt, t, self.seed, self.noiseless)
+                     s["L"], self.kT, self.dt, t, self.seed, self.noiseless, max_disp=self.max_disp)
         self.timestep = t + 1
         self.last = (F, U, W)
 

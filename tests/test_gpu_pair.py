@@ -41,9 +41,12 @@ def test_pair_kat(case, precision):
     _attach(sim, pot)
     assert pot.params[("A", "A")] == case["params"]
     e, f = case["energy"], case["force"]
-    dec = 4 if precision == "fp64" else 3
-    np.testing.assert_array_almost_equal(pot.energies, [0.5 * e, 0.5 * e], decimal=dec)
-    np.testing.assert_array_almost_equal(pot.forces, [[-f, 0, 0], [f, 0, 0]], decimal=dec)
+    np.testing.assert_array_almost_equal(pot.energies, [0.5 * e, 0.5 * e], decimal=4)
+    if precision == "fp64":
+        np.testing.assert_array_almost_equal(pot.forces, [[-f, 0, 0], [f, 0, 0]], decimal=4)
+    if precision == "fp32":
+        # FP32 budget: 1e-5 relative to the force magnitude (forces reach ~1200 here)
+        np.testing.assert_allclose(pot.forces, [[-f, 0, 0], [f, 0, 0]], rtol=1e-5, atol=1e-4)
 
 
 def _oracle_forces(orc, snap, name, params, rcut, ron=None, mode="none", r_buff=0.4, exclusions=None):
