@@ -39,7 +39,7 @@ class Engine:
             raise NotImplementedError("exactly one LangevinFlow or BrownianFlow method is required")
         m = integ.methods[0]
         parts = [sim.precision, sim.seed, integ.dt, type(m).__name__, m.kT, m.noiseless, m.alpha,
-                 getattr(m, "max_displacement", 0.0), repr(m.flow_field), sorted(m.gamma.items()),
+                 getattr(m, "max_displacement", 0.0), getattr(m, "force_cap", 0.0), repr(m.flow_field), sorted(m.gamma.items()),
                  m.gamma.default]
         if pair is not None:
             parts += [type(pair).__name__, pair.mode, sorted(pair.params.items()), sorted(pair.r_cut.items()),
@@ -106,6 +106,7 @@ class Engine:
         c.lambda_ = m.alpha or 0.0
         c.flow = m.flow_field._record()
         c.max_displacement = getattr(m, "max_displacement", 0.0)
+        c.pair_force_cap = getattr(m, "force_cap", 0.0)
         st = ctypes.c_int(0)
         self._md = L.azp_md_create(ctypes.byref(c), ctypes.byref(st))
         _lib.check(st.value, "azp_md_create")

@@ -111,6 +111,7 @@ class MDConfig(ctypes.Structure):
         ("lambda_", ctypes.c_double),
         ("flow", Flow),
         ("max_displacement", ctypes.c_double),
+        ("pair_force_cap", ctypes.c_double),
     ]
 
 

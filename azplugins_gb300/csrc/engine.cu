@@ -306,7 +306,7 @@ struct azp_md {
     uint32_t N = 0, ntypes = 0, nbt = 0;
     int precision = AZP_FP64, pair_kind = -1, shift_mode = 0, bond_kind = -1, method = 0;
     int exclude_bonds = 1, use_lambda = 0, noiseless = 0, tpp = 1;
-    double r_buff = 0.4, dt = 0.005, kT = 1.0, lambda = 0.0, max_disp = 0.0;
+    double r_buff = 0.4, dt = 0.005, kT = 1.0, lambda = 0.0, max_disp = 0.0, fcap = 0.0;
     uint32_t seed = 0;
     FlowD flow{};
     azp_box box{};
@@ -350,6 +350,7 @@ struct azp_md {
     double* d_bond_params = nullptr;
     double* d_pair_table = nullptr;
     double* d_gamma = nullptr;
+    double* d_noise = nullptr;
     // control
     uint32_t* flags = nullptr;  // [0] rebuild request [1] error bits [2] builds [3] max count [4] ticket
     unsigned long long* d_ts = nullptr;
@@ -397,7 +398,7 @@ void free_all(azp_md* m)
                     m->rtag, m->diam, m->t_pos, m->t_vel, m->t_accel, m->t_image, m->t_tag, m->t_diam, m->t_cell,
                     m->cell_of, m->slot, m->cell_count, m->cell_start, m->members, m->scan_tmp, m->counts, m->nbrs,
                     m->cuts, m->bt_n_tag, m->bt_partner_tag, m->bt_type_tag, m->bt_n, m->bt, m->ex_n, m->ex_idx,
-                    m->d_bond_params, m->d_pair_table, m->d_gamma, m->flags, m->d_ts, m->out_force, m->out_virial,
+                    m->d_bond_params, m->d_pair_table, m->d_gamma, m->d_noise, m->flags, m->d_ts, m->out_force, m->out_virial,
                     m->partials, m->thermo, m->tmp4, m->tmpd};
     for (void* p : ptrs) cudaFree(p);
 }
@@ -425,6 +426,7 @@ MDArgs base_args(azp_md* m)
         a.lo[d] = -0.5 * m->box.L[d];
         a.hi[d] = 0.5 * m->box.L[d];
         a.sfix[d] = (float)(m->box.L[d] * 2.3283064365386963e-10);
+        a.fscale[d] = a.Linv[d] * 4294967296.0;
     }
     a.counts = m->counts;
     a.nbrs = m->nbrs;
@@ -441,10 +443,12 @@ MDArgs base_args(azp_md* m)
     a.seed = m->seed;
     a.noiseless = m->noiseless;
     a.gamma = m->d_gamma;
+    a.noise = m->d_noise;
     a.use_lambda = m->use_lambda;
     a.lambda = m->lambda;
     a.flow = m->flow;
     a.max_disp = m->max_disp;
+    a.fcap = m->fcap;
     const double half = 0.5 * m->r_buff;
     a.disp_thresh2 = (float)(half * half * (1.0 - 1e-5));
     a.flags = m->flags;
@@ -685,6 +689,7 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     m->lambda = c->lambda;
     m->flow = make_flow(c->flow);
     m->max_disp = c->max_displacement;
+    m->fcap = c->pair_force_cap > 0.0 ? c->pair_force_cap : 0.0;
     const uint32_t nt2 = c->ntypes * c->ntypes;
     if (m->pair_kind >= 0) {
         if (!c->pair_params || !c->r_cut) return fail(AZP_ERR_INVALID, m);
@@ -750,8 +755,17 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     ALLOC(m->partials, (size_t)8 * (blocks_for(N, THERMO_BLOCK) + 1));
     ALLOC(m->thermo, 8);
     ALLOC(m->d_gamma, c->ntypes);
+    ALLOC(m->d_noise, c->ntypes);
     CTRY(cudaMemset(m->flags, 0, sizeof(uint32_t) * 8));
     CTRY(cudaMemcpy(m->d_gamma, m->gamma.data(), sizeof(double) * c->ntypes, cudaMemcpyHostToDevice));
+    {
+        // noise amplitude per type, with the operations of the reference's
+        // per-particle expression (src/TwoStepLangevinFlow.h:213-215)
+        std::vector<double> noise(c->ntypes, 0.0);
+        if (!c->noiseless)
+            for (uint32_t t = 0; t < c->ntypes; ++t) noise[t] = std::sqrt(6.0 * m->gamma[t] * c->kT / c->dt);
+        CTRY(cudaMemcpy(m->d_noise, noise.data(), sizeof(double) * c->ntypes, cudaMemcpyHostToDevice));
+    }
     // pair table + list thresholds + cell grid
     if (m->pair_kind >= 0) {
         std::vector<double> table((size_t)nt2 * PAIR_TBL);

@@ -21,6 +21,7 @@ struct MDArgs {
     const double* diameter;
     uint32_t N, ntypes;
     double L[3], Linv[3], lo[3], hi[3];
+    double fscale[3];           // 2^32 / L
     float sfix[3];
     // pair
     const uint32_t* counts;
@@ -38,10 +39,12 @@ struct MDArgs {
     uint32_t seed;
     int noiseless;
     const double* gamma;
+    const double* noise;        // per type sqrt(6 gamma kT / dt), 0 when noiseless
     int use_lambda;
     double lambda;
     FlowD flow;
     double max_disp;
+    double fcap;                // > 0: per-pair force magnitude cap
     float disp_thresh2;         // (r_buff / 2)^2, slightly reduced
     uint32_t* flags;            // [0] rebuild request, [1] error bits, [2] builds, [4] ticket
     unsigned long long* d_timestep_rw;

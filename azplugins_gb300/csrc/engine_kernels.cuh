@@ -111,11 +111,45 @@ template<> struct Acc<float> {
     AZP_D double U() const { return (double)u.s + (double)u.c; }
 };
 
-template<typename R> AZP_D size_t md_smem_bytes(uint32_t ntypes, uint32_t nbt)
+// |fixed - fixed at the last build|^2 > threshold, in FP32 on exact integer differences
+AZP_D bool displaced(const uint4& f, const uint4& fb, const float* sfix, float thresh2)
 {
-    const size_t nt2 = (size_t)ntypes * ntypes;
-    return nt2 * sizeof(double) + ntypes * sizeof(double) + nt2 * PAIR_TBL * sizeof(R) +
-           (size_t)nbt * AZP_BOND_PARAM_DOUBLES * sizeof(R);
+    const float dx = (float)(int32_t)(f.x - fb.x) * sfix[0];
+    const float dy = (float)(int32_t)(f.y - fb.y) * sfix[1];
+    const float dz = (float)(int32_t)(f.z - fb.z) * sfix[2];
+    return dx * dx + dy * dy + dz * dz > thresh2;
+}
+
+// Wrap one coordinate into [lo, hi) and return its 32-bit fixed-point value.
+// The fixed value x * (2^32 / L) decides without FP64 compares whether the
+// particle can be near a face; only then is the exact FP64 wrap test done.
+AZP_D uint32_t wrap_fixed(double& x, int* img, double fscale, double L, double lo, double hi)
+{
+    long long q = __double2ll_rn(x * fscale);
+    if (q >= 2146435072ll || q < -2146435072ll) {  // within 2^20 units of a face
+        int w = 0;
+        wrap1(x, w, L, lo, hi);
+        if (w) {
+            *img += w;
+            q = __double2ll_rn(x * fscale);
+        }
+    }
+    return (uint32_t)(int32_t)q;
+}
+
+// flow field in FP32 (same functor values to FP32 rounding)
+AZP_D void flow_at_f(const FlowD& f, float y, float& ux, float& uy, float& uz)
+{
+    if (f.kind == AZP_FLOW_PARABOLIC) {
+        const float yr = y * (float)(1.0 / f.b);
+        ux = (float)f.a * (1.0f - yr * yr);
+        uy = 0.0f;
+        uz = 0.0f;
+    } else {
+        ux = (float)f.a;
+        uy = (float)f.b;
+        uz = (float)f.c;
+    }
 }
 
 template<class PE, class BE, typename R, int INTEG>
@@ -125,7 +159,8 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
     const uint32_t nt2 = a.ntypes * a.ntypes;
     double* s_rc2 = reinterpret_cast<double*>(smem_raw);
     double* s_gamma = s_rc2 + nt2;
-    R* s_rec = reinterpret_cast<R*>(s_gamma + a.ntypes);
+    double* s_noise = s_gamma + a.ntypes;
+    R* s_rec = reinterpret_cast<R*>(s_noise + a.ntypes);
     R* s_bond = s_rec + nt2 * PAIR_TBL;
     if (!std::is_same<PE, NoPair>::value)
         for (uint32_t t = threadIdx.x; t < nt2 * PAIR_TBL; t += blockDim.x) {
@@ -136,7 +171,10 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
         for (uint32_t t = threadIdx.x; t < a.nbondtypes * AZP_BOND_PARAM_DOUBLES; t += blockDim.x)
             s_bond[t] = (R)a.bond_params[t];
     if (INTEG != MD_FORCES_ONLY && !a.use_lambda)
-        for (uint32_t t = threadIdx.x; t < a.ntypes; t += blockDim.x) s_gamma[t] = a.gamma[t];
+        for (uint32_t t = threadIdx.x; t < a.ntypes; t += blockDim.x) {
+            s_gamma[t] = a.gamma[t];
+            s_noise[t] = a.noise[t];
+        }
     __syncthreads();
 
     const int tpp = a.tpp;
@@ -168,6 +206,8 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
                     PE::eval(rec, rsq, fdr, e);
                     e -= rec[PE::SHIFT_SLOT];
                     xplor(cut, rsq, fdr, e);
+                    if (a.fcap > 0.0 && (double)fdr * fdr * rsq > a.fcap * a.fcap)
+                        fdr = (R)copysign(a.fcap / sqrt((double)rsq), (double)fdr);
                     acc.add(dx, dy, dz, fdr, e, vir);
                 }
             } else {
@@ -197,6 +237,8 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
                     PE::eval(rec, rsq, fdr, e);
                     e -= rec[PE::SHIFT_SLOT];
                     xplor(cut, rsq, fdr, e);
+                    if (a.fcap > 0.0 && (double)fdr * fdr * rsq > a.fcap * a.fcap)
+                        fdr = (R)copysign(a.fcap / sqrt((double)rsq), (double)fdr);
                     acc.add(dx, dy, dz, fdr, e, vir);
                 }
             }
@@ -243,77 +285,152 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
         if constexpr (INTEG != MD_FORCES_ONLY) {
             const unsigned long long ts = *a.d_timestep;
             double4_32a p = a.pos[i];
-            const double gam = a.use_lambda ? a.lambda * a.diameter[i] : s_gamma[type_of(p.w)];
-            double ux, uy, uz;
-            flow_at(a.flow, p.y, ux, uy, uz);
-            const double c = a.noiseless ? 0.0 : sqrt(6.0 * gam * a.kT / a.dt);
+            const uint32_t ti = type_of(p.w);
             const uint32_t tg = a.tag[i];
-            double r0, r1, r2;
             bool moved = false;
-            if constexpr (INTEG == MD_INTEG_LANGEVIN) {
-                uniform3(AZP_RNG_LANGEVIN_FLOW, ts, a.seed, tg, -c, c - (-c), r0, r1, r2);
-                double4_32a v = a.vel[i];
-                const double minv = 1.0 / v.w;
-                const double ax = (Fx + (r0 - gam * (v.x - ux))) * minv;
-                const double ay = (Fy + (r1 - gam * (v.y - uy))) * minv;
-                const double az = (Fz + (r2 - gam * (v.z - uz))) * minv;
-                const double h = 0.5 * a.dt;
-                v.x += h * ax;
-                v.y += h * ay;
-                v.z += h * az;
-                if (a.next) {
-                    // step one of the next timestep with the acceleration just computed
-                    p.x += (v.x + h * ax) * a.dt;
-                    p.y += (v.y + h * ay) * a.dt;
-                    p.z += (v.z + h * az) * a.dt;
+            if constexpr (std::is_same<R, double>::value) {
+                // FP64 path: the reference arithmetic throughout; the per-type noise
+                // amplitude sqrt(6 gamma kT / dt) comes from a host table built with
+                // the same double operations, so the draws stay bit-exact
+                const double gam = a.use_lambda ? a.lambda * a.diameter[i] : s_gamma[ti];
+                const double c = a.noiseless ? 0.0 : (a.use_lambda ? sqrt(6.0 * gam * a.kT / a.dt) : s_noise[ti]);
+                double ux, uy, uz;
+                flow_at(a.flow, p.y, ux, uy, uz);
+                double r0, r1, r2;
+                if constexpr (INTEG == MD_INTEG_LANGEVIN) {
+                    uniform3(AZP_RNG_LANGEVIN_FLOW, ts, a.seed, tg, -c, c - (-c), r0, r1, r2);
+                    double4_32a v = a.vel[i];
+                    const double minv = 1.0 / v.w;
+                    const double ax = (Fx + (r0 - gam * (v.x - ux))) * minv;
+                    const double ay = (Fy + (r1 - gam * (v.y - uy))) * minv;
+                    const double az = (Fz + (r2 - gam * (v.z - uz))) * minv;
+                    const double h = 0.5 * a.dt;
                     v.x += h * ax;
                     v.y += h * ay;
                     v.z += h * az;
-                    moved = true;
+                    if (a.next) {
+                        // step one of the next timestep with the acceleration just computed
+                        p.x += (v.x + h * ax) * a.dt;
+                        p.y += (v.y + h * ay) * a.dt;
+                        p.z += (v.z + h * az) * a.dt;
+                        v.x += h * ax;
+                        v.y += h * ay;
+                        v.z += h * az;
+                        moved = true;
+                    } else {
+                        a.accel[3 * i] = ax;
+                        a.accel[3 * i + 1] = ay;
+                        a.accel[3 * i + 2] = az;
+                    }
+                    a.vel[i] = v;
                 } else {
-                    a.accel[3 * i] = ax;
-                    a.accel[3 * i + 1] = ay;
-                    a.accel[3 * i + 2] = az;
+                    uniform3(AZP_RNG_BROWNIAN_FLOW, ts, a.seed, tg, -c, c - (-c), r0, r1, r2);
+                    double dx = (ux + (Fx + r0) / gam) * a.dt;
+                    double dy = (uy + (Fy + r1) / gam) * a.dt;
+                    double dz = (uz + (Fz + r2) / gam) * a.dt;
+                    if (a.max_disp > 0.0) {
+                        dx = fmin(fmax(dx, -a.max_disp), a.max_disp);
+                        dy = fmin(fmax(dy, -a.max_disp), a.max_disp);
+                        dz = fmin(fmax(dz, -a.max_disp), a.max_disp);
+                    }
+                    p.x += dx;
+                    p.y += dy;
+                    p.z += dz;
+                    moved = true;
                 }
-                a.vel[i] = v;
+                if (moved) {
+                    int wx = 0, wy = 0, wz = 0;
+                    wrap1(p.x, wx, a.L[0], a.lo[0], a.hi[0]);
+                    wrap1(p.y, wy, a.L[1], a.lo[1], a.hi[1]);
+                    wrap1(p.z, wz, a.L[2], a.lo[2], a.hi[2]);
+                    if (wx | wy | wz) {
+                        a.image[3 * i] += wx;
+                        a.image[3 * i + 1] += wy;
+                        a.image[3 * i + 2] += wz;
+                    }
+                    a.pos_next[i] = p;
+                    uint4 f;
+                    f.x = to_fixed(p.x, a.Linv[0]);
+                    f.y = to_fixed(p.y, a.Linv[1]);
+                    f.z = to_fixed(p.z, a.Linv[2]);
+                    f.w = ti;
+                    a.fix_next[i] = f;
+                    want_rebuild = displaced(f, a.fix_build[i], a.sfix, a.disp_thresh2);
+                    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(&a.flags[1], AZP_EBIT_NONFINITE);
+                }
             } else {
-                uniform3(AZP_RNG_BROWNIAN_FLOW, ts, a.seed, tg, -c, c - (-c), r0, r1, r2);
-                double dx = (ux + (Fx + r0) / gam) * a.dt;
-                double dy = (uy + (Fy + r1) / gam) * a.dt;
-                double dz = (uz + (Fz + r2) / gam) * a.dt;
-                if (a.max_disp > 0.0) {
-                    dx = fmin(fmax(dx, -a.max_disp), a.max_disp);
-                    dy = fmin(fmax(dy, -a.max_disp), a.max_disp);
-                    dz = fmin(fmax(dz, -a.max_disp), a.max_disp);
+                // FP32-force path. GB300 issues FP64 at a small fraction of its FP32
+                // rate, so the increments (drag, noise, kicks, displacements) are
+                // formed in FP32 -- as accurate as the FP32 forces they come from --
+                // and only the accumulations v += dv, x += dx are FP64.
+                const float fx = acc.fx.s + acc.fx.c, fy = acc.fy.s + acc.fy.c, fz = acc.fz.s + acc.fz.c;
+                const float gam = a.use_lambda ? (float)(a.lambda * a.diameter[i]) : (float)s_gamma[ti];
+                const float c = a.noiseless ? 0.0f
+                                            : (a.use_lambda ? sqrtf(6.0f * gam * (float)a.kT / (float)a.dt)
+                                                            : (float)s_noise[ti]);
+                float ux, uy, uz;
+                flow_at_f(a.flow, (float)p.y, ux, uy, uz);
+                const float dt = (float)a.dt;
+                float r0, r1, r2;
+                double ddx, ddy, ddz;
+                if constexpr (INTEG == MD_INTEG_LANGEVIN) {
+                    uniform3f(AZP_RNG_LANGEVIN_FLOW, ts, a.seed, tg, -c, 2.0f * c, r0, r1, r2);
+                    double4_32a v = a.vel[i];
+                    const float minv = __frcp_rn((float)v.w);
+                    const float ax = (fx + (r0 - gam * ((float)v.x - ux))) * minv;
+                    const float ay = (fy + (r1 - gam * ((float)v.y - uy))) * minv;
+                    const float az = (fz + (r2 - gam * ((float)v.z - uz))) * minv;
+                    if (a.next) {
+                        // v(t+dt/2) = v + dt a: the half kick of step two and of step one
+                        const float kx = dt * ax, ky = dt * ay, kz = dt * az;
+                        ddx = (double)(((float)v.x + kx) * dt);
+                        ddy = (double)(((float)v.y + ky) * dt);
+                        ddz = (double)(((float)v.z + kz) * dt);
+                        v.x += (double)kx;
+                        v.y += (double)ky;
+                        v.z += (double)kz;
+                        moved = true;
+                    } else {
+                        const float h = 0.5f * dt;
+                        v.x += (double)(h * ax);
+                        v.y += (double)(h * ay);
+                        v.z += (double)(h * az);
+                        a.accel[3 * i] = ax;
+                        a.accel[3 * i + 1] = ay;
+                        a.accel[3 * i + 2] = az;
+                    }
+                    a.vel[i] = v;
+                } else {
+                    uniform3f(AZP_RNG_BROWNIAN_FLOW, ts, a.seed, tg, -c, 2.0f * c, r0, r1, r2);
+                    const float gi = 1.0f / gam;
+                    float dx = (ux + (fx + r0) * gi) * dt;
+                    float dy = (uy + (fy + r1) * gi) * dt;
+                    float dz = (uz + (fz + r2) * gi) * dt;
+                    if (a.max_disp > 0.0) {
+                        const float m = (float)a.max_disp;
+                        dx = fminf(fmaxf(dx, -m), m);
+                        dy = fminf(fmaxf(dy, -m), m);
+                        dz = fminf(fmaxf(dz, -m), m);
+                    }
+                    ddx = dx;
+                    ddy = dy;
+                    ddz = dz;
+                    moved = true;
                 }
-                p.x += dx;
-                p.y += dy;
-                p.z += dz;
-                moved = true;
-            }
-            if (moved) {
-                int wx = 0, wy = 0, wz = 0;
-                wrap1(p.x, wx, a.L[0], a.lo[0], a.hi[0]);
-                wrap1(p.y, wy, a.L[1], a.lo[1], a.hi[1]);
-                wrap1(p.z, wz, a.L[2], a.lo[2], a.hi[2]);
-                if (wx | wy | wz) {
-                    a.image[3 * i] += wx;
-                    a.image[3 * i + 1] += wy;
-                    a.image[3 * i + 2] += wz;
+                if (moved) {
+                    p.x += ddx;
+                    p.y += ddy;
+                    p.z += ddz;
+                    uint4 f;
+                    f.x = wrap_fixed(p.x, a.image + 3 * i, a.fscale[0], a.L[0], a.lo[0], a.hi[0]);
+                    f.y = wrap_fixed(p.y, a.image + 3 * i + 1, a.fscale[1], a.L[1], a.lo[1], a.hi[1]);
+                    f.z = wrap_fixed(p.z, a.image + 3 * i + 2, a.fscale[2], a.L[2], a.lo[2], a.hi[2]);
+                    f.w = ti;
+                    a.pos_next[i] = p;
+                    a.fix_next[i] = f;
+                    want_rebuild = displaced(f, a.fix_build[i], a.sfix, a.disp_thresh2);
+                    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(&a.flags[1], AZP_EBIT_NONFINITE);
                 }
-                a.pos_next[i] = p;
-                uint4 f;
-                f.x = to_fixed(p.x, a.Linv[0]);
-                f.y = to_fixed(p.y, a.Linv[1]);
-                f.z = to_fixed(p.z, a.Linv[2]);
-                f.w = type_of(p.w);
-                a.fix_next[i] = f;
-                const uint4 fb = a.fix_build[i];
-                const float ddx = (float)(int32_t)(f.x - fb.x) * a.sfix[0];
-                const float ddy = (float)(int32_t)(f.y - fb.y) * a.sfix[1];
-                const float ddz = (float)(int32_t)(f.z - fb.z) * a.sfix[2];
-                want_rebuild = ddx * ddx + ddy * ddy + ddz * ddz > a.disp_thresh2;
-                if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(&a.flags[1], AZP_EBIT_NONFINITE);
             }
         }
     }
@@ -342,7 +459,7 @@ int launch_md_t(const MDArgs& a, cudaStream_t s)
     const uint32_t blocks = (uint32_t)((threads + MD_BLOCK - 1) / MD_BLOCK);
     if (blocks == 0) return AZP_OK;
     const size_t nt2 = (size_t)a.ntypes * a.ntypes;
-    const size_t smem = nt2 * sizeof(double) + a.ntypes * sizeof(double) + nt2 * PAIR_TBL * sizeof(R) +
+    const size_t smem = nt2 * sizeof(double) + 2 * a.ntypes * sizeof(double) + nt2 * PAIR_TBL * sizeof(R) +
                         (size_t)a.nbondtypes * AZP_BOND_PARAM_DOUBLES * sizeof(R);
     auto k = k_md_step<PE, BE, R, INTEG>;
     if (smem > 48 * 1024) AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -21,7 +21,17 @@ namespace azp
 constexpr int PAIR_REC = 8;   // values per pair kernel record
 constexpr int CUT_REC = 4;    // rcutsq, ronsq, 1/(rcutsq-ronsq)^3, xplor flag
 
-template<typename R> AZP_HD R rcp(R x) { return R(1) / x; }
+// correctly rounded reciprocal; the FP32 form maps to the hardware-assisted
+// rounded reciprocal instead of a full division
+AZP_HD double rcp(double x) { return 1.0 / x; }
+AZP_HD float rcp(float x)
+{
+#ifdef __CUDA_ARCH__
+    return __frcp_rn(x);
+#else
+    return 1.0f / x;
+#endif
+}
 
 // ================================================================ pair potentials
 // Interface: enabled(rec) -- the reference's "lj1 != 0" / "epsilon != 0" test;

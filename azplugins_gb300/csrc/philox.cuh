@@ -90,4 +90,20 @@ AZP_HD void uniform3(uint32_t id, uint64_t timestep, uint32_t seed, uint32_t tag
 #endif
 }
 
+// The same three draws at 24-bit resolution for the FP32-force integrator: the
+// top 24 bits of each 64-bit word above, as a float in (0, 1).
+AZP_HD float open01f(uint32_t hi) { return ((float)(hi >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+
+AZP_HD void uniform3f(uint32_t id, uint64_t timestep, uint32_t seed, uint32_t tag, float lo, float width, float& r0,
+                      float& r1, float& r2)
+{
+    uint32_t k0, k1;
+    stream_key(id, timestep, seed, k0, k1);
+    const Philox4 a = philox4x32_10(0u, tag, 0u, 0u, k0, k1);
+    const Philox4 b = philox4x32_10(1u, tag, 0u, 0u, k0, k1);
+    r0 = lo + width * open01f(a.v[0]);
+    r1 = lo + width * open01f(a.v[2]);
+    r2 = lo + width * open01f(b.v[0]);
+}
+
 }  // namespace azp

@@ -51,15 +51,18 @@ class BrownianFlow(_FlowMethod):
     """Overdamped Brownian dynamics in a flow field:
     x += (u(x) + (F + R) / gamma) dt (``src/TwoStepBrownianFlow.h:136-178``).
 
-    ``max_displacement`` (default 0 = off) caps each displacement component; it
-    exists for overlap relaxation of generated configurations.
+    ``max_displacement`` (default 0 = off) caps each displacement component and
+    ``force_cap`` (default 0 = off) caps the magnitude of every pair force; both
+    exist for the overlap relaxation of generated configurations.
     """
 
     method_id = 1
 
-    def __init__(self, filter, kT, flow_field, default_gamma=1.0, alpha=None, noiseless=False, max_displacement=0.0):
+    def __init__(self, filter, kT, flow_field, default_gamma=1.0, alpha=None, noiseless=False, max_displacement=0.0,
+                 force_cap=0.0):
         super().__init__(filter, kT, flow_field, default_gamma, alpha, noiseless)
         self.max_displacement = float(max_displacement)
+        self.force_cap = float(force_cap)
 
 
 __all__ = ["LangevinFlow", "BrownianFlow"]

@@ -273,6 +273,7 @@ typedef struct {
     double lambda;
     azp_flow flow;
     double max_displacement;    /* Brownian only; 0 = uncapped */
+    double pair_force_cap;      /* > 0: |pair force| capped per pair (overlap relaxation); 0 = off */
 } azp_md_config;
 
 AZP_API azp_md* azp_md_create(const azp_md_config* cfg, int* status);

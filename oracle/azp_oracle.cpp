@@ -618,7 +618,7 @@ long orc_nlist_cell(int N, const double* pos, const int32_t* type, int ntypes, c
 void orc_pair_forces(int N, const double* pos, const int32_t* type, int ntypes, const double* L,
                      const int32_t* start, const int32_t* idx, int kind, const double* params, int pstride,
                      const double* rcutsq, const double* ronsq, int mode, double* force, double* energy,
-                     double* virial)
+                     double* virial, double fcap)
 {
     const Box b = make_box(L);
 #ifdef _OPENMP
@@ -648,6 +648,8 @@ void orc_pair_forces(int N, const double* pos, const int32_t* type, int ntypes, 
                 fdr = s * fdr - dsdr_r * e;
                 e = e * s;
             }
+            // optional per-pair force cap (overlap relaxation of generated systems)
+            if (fcap > 0.0 && fdr * fdr * rs > fcap * fcap) fdr = std::copysign(fcap / std::sqrt(rs), fdr);
             F[0] += v[0] * fdr;
             F[1] += v[1] * fdr;
             F[2] += v[2] * fdr;

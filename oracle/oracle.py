@@ -90,7 +90,7 @@ def lib():
     for fn in (L.orc_nlist_brute, L.orc_nlist_cell):
         fn.argtypes = [c_int, _dp, _ip, c_int, _dp, _dp, vp, vp, _ip, _ip, c_long]
         fn.restype = c_long
-    L.orc_pair_forces.argtypes = [c_int, _dp, _ip, c_int, _dp, _ip, _ip, c_int, _dp, c_int, _dp, vp, c_int, _dp, _dp, vp]
+    L.orc_pair_forces.argtypes = [c_int, _dp, _ip, c_int, _dp, _ip, _ip, c_int, _dp, c_int, _dp, vp, c_int, _dp, _dp, vp, c_double]
     L.orc_bond_forces.argtypes = [c_int, _dp, _dp, c_long, _ip, _ip, c_int, _dp, c_int, _dp, _dp, vp]
     L.orc_bond_forces.restype = c_long
     L.orc_bond_forces_pp.argtypes = [c_int, _dp, _dp, _ip, _ip, _ip, c_int, _dp, c_int, _dp, _dp, vp]
@@ -195,7 +195,7 @@ def nlist(pos4, types, ntypes, L, rlistsq, exclusions=None, method="cell"):
 
 
 # ------------------------------------------------------------------ forces
-def pair_forces(pos4, types, ntypes, L, start, idx, name, params, rcutsq, ronsq=None, mode="none"):
+def pair_forces(pos4, types, ntypes, L, start, idx, name, params, rcutsq, ronsq=None, mode="none", fcap=0.0):
     """Pair force, per-particle energy (half per pair) and virial (xx,xy,xz,yy,yz,zz)."""
     N = pos4.shape[0]
     F = np.zeros((N, 3))
@@ -219,6 +219,7 @@ def pair_forces(pos4, types, ntypes, L, start, idx, name, params, rcutsq, ronsq=
         F,
         U,
         _ptr(W),
+        float(fcap),
     )
     return F, U, W
 
@@ -322,7 +323,7 @@ class OracleMD:
 
     def __init__(self, system, pair=None, bond=None, method="langevin", gamma=(1.0,), flow_kind=0,
                  flow_p=(0.0, 0.0, 0.0), kT=1.0, dt=0.005, seed=0, r_buff=0.4, noiseless=False, exclude_bonds=True,
-                 max_disp=0.0):
+                 max_disp=0.0, force_cap=0.0):
         self.s = {k: (np.ascontiguousarray(v).copy() if isinstance(v, np.ndarray) else v) for k, v in system.items()}
         s = self.s
         self.N = s["pos4"].shape[0]
@@ -336,6 +337,7 @@ class OracleMD:
         self.r_buff = r_buff
         self.noiseless = noiseless
         self.max_disp = max_disp
+        self.force_cap = force_cap
         self.timestep = int(s.get("timestep", 0))
         self.ntypes = int(s.get("ntypes", int(s["types"].max()) + 1))
         self.exclusions = s["bonds"] if (exclude_bonds and s.get("bonds") is not None and len(s["bonds"])) else None
@@ -372,7 +374,7 @@ class OracleMD:
             ron = self.pair.get("ron")
             ronsq = None if ron is None else np.asarray(ron, dtype=np.float64) ** 2
             F, U, W = pair_forces(s["pos4"], s["types"], self.ntypes, s["L"], *self.nlist_csr, self.pair["name"],
-                                  self.pair["params"], rc * rc, ronsq, self.pair.get("mode", "none"))
+                                  self.pair["params"], rc * rc, ronsq, self.pair.get("mode", "none"), self.force_cap)
         if self.bond is not None and self.table is not None:
             bond_forces_pp(s["pos4"], s["L"], self.table, self.bond["name"], self.bond["params"], F, U, W)
         return F, U, W
