@@ -115,6 +115,27 @@ class MDConfig(ctypes.Structure):
     ]
 
 
+class BatchConfig(ctypes.Structure):
+    _fields_ = [
+        ("nsys", ctypes.c_uint32),
+        ("N", ctypes.c_void_p),
+        ("L", ctypes.c_void_p),
+        ("precision", ctypes.c_int32),
+        ("pair_kind", ctypes.c_int32),
+        ("shift_mode", ctypes.c_int32),
+        ("pair_params", ctypes.c_void_p),
+        ("r_cut", ctypes.c_void_p),
+        ("r_buff", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("kT", ctypes.c_double),
+        ("gamma", ctypes.c_double),
+        ("seeds", ctypes.c_void_p),
+        ("noiseless", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("flow", Flow),
+    ]
+
+
 _lib = None
 
 _vp = ctypes.c_void_p
@@ -144,6 +165,8 @@ _SIGNATURES = [
     ("azp_nlist_download", _i, [_vp, _vp, _vp, _vp]),
     ("azp_pair_forces", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _vp, _i, ctypes.POINTER(Forces), _vp]),
     ("azp_bond_forces", _i, [ctypes.POINTER(System), _vp, _vp, _u32, _i, _vp, _u32, ctypes.POINTER(Forces), _vp, _vp]),
+    ("azp_pair_adjoint", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
+    ("azp_bond_adjoint", _i, [ctypes.POINTER(System), _vp, _vp, _i, _vp, _u32, _vp, _vp, _vp, _vp, _vp]),
     ("azp_langevin_step1", _i, [ctypes.POINTER(System), _vp, _u32, _d, _vp]),
     ("azp_langevin_step2", _i, [ctypes.POINTER(System), _vp, _u32, _vp, _i, _vp, _i, _d, Flow, _d, _d, _u64, _u32, _i, _vp]),
     ("azp_brownian_step", _i, [ctypes.POINTER(System), _vp, _u32, _vp, _i, _vp, _i, _d, Flow, _d, _d, _u64, _u32, _i, _d, _vp]),
@@ -158,6 +181,14 @@ _SIGNATURES = [
     ("azp_md_error", _i, [_vp, ctypes.POINTER(_u32), _vp]),
     ("azp_md_last_launches", _u64, [_vp]),
     ("azp_md_time_step_kernel", _i, [_vp, _i, ctypes.POINTER(ctypes.c_float), _vp]),
+    ("azp_batch_create", _vp, [ctypes.POINTER(BatchConfig), ctypes.POINTER(_i)]),
+    ("azp_batch_destroy", None, [_vp]),
+    ("azp_batch_set_state", _i, [_vp, _vp, _vp, _vp, _vp, _u64, _vp]),
+    ("azp_batch_get_state", _i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    ("azp_batch_run", _i, [_vp, _u64, _vp]),
+    ("azp_batch_error", _i, [_vp, ctypes.POINTER(_u32), ctypes.POINTER(_u32), _vp]),
+    ("azp_batch_set_tpp", _i, [_vp, _i]),
+    ("azp_batch_last_launches", _u64, [_vp]),
 ]
 
 

@@ -137,20 +137,6 @@ AZP_D uint32_t wrap_fixed(double& x, int* img, double fscale, double L, double l
     return (uint32_t)(int32_t)q;
 }
 
-// flow field in FP32 (same functor values to FP32 rounding)
-AZP_D void flow_at_f(const FlowD& f, float y, float& ux, float& uy, float& uz)
-{
-    if (f.kind == AZP_FLOW_PARABOLIC) {
-        const float yr = y * (float)(1.0 / f.b);
-        ux = (float)f.a * (1.0f - yr * yr);
-        uy = 0.0f;
-        uz = 0.0f;
-    } else {
-        ux = (float)f.a;
-        uy = (float)f.b;
-        uz = (float)f.c;
-    }
-}
 
 template<class PE, class BE, typename R, int INTEG>
 __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)

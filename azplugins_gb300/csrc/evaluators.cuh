@@ -41,17 +41,17 @@ AZP_HD float rcp(float x)
 struct PerturbedLJ {
     // rec: lj1, lj2, lambda, rwcasq, wca_shift, 12 lj1, 6 lj2, (shift)
     static constexpr int SHIFT_SLOT = 7;
-    AZP_HD static void prepare(const double* p, double* rec)
+    template<typename R> AZP_HD static void prepare(const R* p, R* rec)
     {
-        const double s6 = p[0], e4 = p[1], lam = p[2];
+        const R s6 = p[0], e4 = p[1], lam = p[2];
         rec[0] = e4 * s6 * s6;
         rec[1] = e4 * s6;
         rec[2] = lam;
         rec[3] = p[3];
-        rec[4] = e4 * (1.0 - lam) / 4.0;
-        rec[5] = 12.0 * rec[0];
-        rec[6] = 6.0 * rec[1];
-        rec[7] = 0.0;
+        rec[4] = e4 * (R(1) - lam) / R(4);
+        rec[5] = R(12) * rec[0];
+        rec[6] = R(6) * rec[1];
+        rec[7] = R(0);
     }
     template<typename R> AZP_HD static bool enabled(const R* rec) { return rec[0] != R(0); }
     template<typename R> AZP_HD static void eval(const R* rec, R rsq, R& fdr, R& e)
@@ -74,12 +74,12 @@ struct PerturbedLJ {
 struct ExpandedYukawa {
     // rec: epsilon, kappa, delta, (shift)
     static constexpr int SHIFT_SLOT = 3;
-    AZP_HD static void prepare(const double* p, double* rec)
+    template<typename R> AZP_HD static void prepare(const R* p, R* rec)
     {
         rec[0] = p[0];
         rec[1] = p[1];
         rec[2] = p[2];
-        for (int k = 3; k < PAIR_REC; ++k) rec[k] = 0.0;
+        for (int k = 3; k < PAIR_REC; ++k) rec[k] = R(0);
     }
     template<typename R> AZP_HD static bool enabled(const R* rec) { return rec[0] != R(0); }
     template<typename R> AZP_HD static void eval(const R* rec, R rsq, R& fdr, R& e)
@@ -96,10 +96,10 @@ struct ExpandedYukawa {
 struct Hertz {
     // rec: epsilon, r_cut, (shift, never set: the reference has no shift branch)
     static constexpr int SHIFT_SLOT = 7;
-    AZP_HD static void prepare(const double* p, double* rec)
+    template<typename R> AZP_HD static void prepare(const R* p, R* rec)
     {
         rec[0] = p[0];
-        for (int k = 1; k < PAIR_REC; ++k) rec[k] = 0.0;
+        for (int k = 1; k < PAIR_REC; ++k) rec[k] = R(0);
     }
     template<typename R> AZP_HD static bool enabled(const R* rec) { return rec[0] != R(0); }
     template<typename R> AZP_HD static void eval(const R* rec, R rsq, R& fdr, R& e)
@@ -116,16 +116,16 @@ struct Hertz {
 struct Colloid {
     // rec: A, a_1, a_2, sigma^3, sigma^6, form (0 SS, 1 CS, 2 CC), max(a_1,a_2), (shift)
     static constexpr int SHIFT_SLOT = 7;
-    AZP_HD static void prepare(const double* p, double* rec)
+    template<typename R> AZP_HD static void prepare(const R* p, R* rec)
     {
         rec[0] = p[0];
         rec[1] = p[1];
         rec[2] = p[2];
         rec[3] = p[3];
         rec[4] = p[3] * p[3];
-        rec[5] = (p[1] == 0.0 && p[2] == 0.0) ? 0.0 : ((p[1] != 0.0 && p[2] != 0.0) ? 2.0 : 1.0);
+        rec[5] = (p[1] == R(0) && p[2] == R(0)) ? R(0) : ((p[1] != R(0) && p[2] != R(0)) ? R(2) : R(1));
         rec[6] = p[1] > p[2] ? p[1] : p[2];
-        rec[7] = 0.0;
+        rec[7] = R(0);
     }
     template<typename R> AZP_HD static bool enabled(const R* rec) { return rec[0] != R(0); }
 
@@ -191,24 +191,31 @@ struct Colloid {
 
 // Host: fill the kernel record and cut record of one type pair.
 // p: the reference param_type (4 doubles); mode: azp_shift_mode.
-template<class Eval>
-AZP_HD void prepare_pair(const double* p, double rcut, double ron, int mode, double* rec, double* cut)
+template<class Eval, typename R>
+AZP_HD void prepare_pair_t(const R* p, double rcut, double ron, int mode, R* rec, R* cut)
 {
     Eval::prepare(p, rec);
     const double rcutsq = rcut * rcut;
     const double ronsq = ron * ron;
-    if (std::is_same<Eval, Hertz>::value) rec[1] = rcut;
-    cut[0] = rcutsq;
-    cut[1] = ronsq;
-    cut[2] = (mode == AZP_MODE_XPLOR && ronsq < rcutsq) ? 1.0 / ((rcutsq - ronsq) * (rcutsq - ronsq) * (rcutsq - ronsq)) : 0.0;
-    cut[3] = (mode == AZP_MODE_XPLOR && ronsq < rcutsq) ? 1.0 : 0.0;
+    if (std::is_same<Eval, Hertz>::value) rec[1] = R(rcut);
+    cut[0] = R(rcutsq);
+    cut[1] = R(ronsq);
+    cut[2] = R((mode == AZP_MODE_XPLOR && ronsq < rcutsq) ? 1.0 / ((rcutsq - ronsq) * (rcutsq - ronsq) * (rcutsq - ronsq))
+                                                          : 0.0);
+    cut[3] = R((mode == AZP_MODE_XPLOR && ronsq < rcutsq) ? 1.0 : 0.0);
     const bool shift = (mode == AZP_MODE_SHIFT) || (mode == AZP_MODE_XPLOR && ronsq > rcutsq);
     if (shift && rcut > 0.0 && Eval::enabled(rec) && !std::is_same<Eval, Hertz>::value) {
-        double f = 0.0, e = 0.0;
-        Eval::eval(rec, rcutsq, f, e);
+        R f = R(0), e = R(0);
+        Eval::eval(rec, R(rcutsq), f, e);
         rec[Eval::SHIFT_SLOT] = e;
     }
-    if (!(rcut > 0.0)) cut[0] = 0.0;  // r_cut 0: the type pair is never evaluated
+    if (!(rcut > 0.0)) cut[0] = R(0);  // r_cut 0: the type pair is never evaluated
+}
+
+template<class Eval>
+AZP_HD void prepare_pair(const double* p, double rcut, double ron, int mode, double* rec, double* cut)
+{
+    prepare_pair_t<Eval, double>(p, rcut, ron, mode, rec, cut);
 }
 
 // XPLOR smoothing of (fdr, e) for ronsq <= rsq < rcutsq (HOOMD pair.Pair mode

@@ -51,6 +51,21 @@ AZP_D void flow_at(const FlowD& f, double y, double& ux, double& uy, double& uz)
     }
 }
 
+// flow field in FP32 (same functor values to FP32 rounding)
+AZP_D void flow_at_f(const FlowD& f, float y, float& ux, float& uy, float& uz)
+{
+    if (f.kind == AZP_FLOW_PARABOLIC) {
+        const float yr = y * (float)(1.0 / f.b);
+        ux = (float)f.a * (1.0f - yr * yr);
+        uy = 0.0f;
+        uz = 0.0f;
+    } else {
+        ux = (float)f.a;
+        uy = (float)f.b;
+        uz = (float)f.c;
+    }
+}
+
 AZP_D void wrap1(double& x, int& img, double L, double lo, double hi)
 {
     if (x >= hi) {

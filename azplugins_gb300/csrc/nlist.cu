@@ -322,6 +322,7 @@ void free_nl(azp_nlist* nl)
     cudaFree(nl->ex_keys);
     cudaFree(nl->table);
     cudaFree(nl->cutbuf);
+    cudaFree(nl->adj_table);
 }
 
 int ensure_cells(azp_nlist* nl, uint32_t ncell)
@@ -368,6 +369,8 @@ azp_nlist* azp_nlist_create(uint32_t N, uint32_t ntypes, uint32_t max_neighbors,
     if (!st && (e = cudaMalloc(&nl->flags, sizeof(uint32_t) * 4)) != cudaSuccess) fail(e, "flags");
     if (!st && (e = cudaMalloc(&nl->table, sizeof(double) * ntypes * ntypes * 12)) != cudaSuccess) fail(e, "table");
     if (!st && (e = cudaMalloc(&nl->cutbuf, sizeof(double) * ntypes * ntypes * 2)) != cudaSuccess) fail(e, "cutbuf");
+    if (!st && (e = cudaMalloc(&nl->adj_table, sizeof(double) * 6 * 12 * ntypes * ntypes)) != cudaSuccess)
+        fail(e, "adj_table");
     if (st) {
         free_nl(nl);
         delete nl;

@@ -30,5 +30,7 @@ struct azp_nlist {
     // pair-driver workspace: derived type-pair table and r_cut / r_on staging
     double* table = nullptr;   // [ntypes^2][12]
     double* cutbuf = nullptr;  // [2][ntypes^2]
+    // adjoint workspace: dual-number type-pair records [ntypes^2][12] x (1 + 5) doubles
+    double* adj_table = nullptr;
 };
 

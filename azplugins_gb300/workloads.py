@@ -87,3 +87,139 @@ def bead_spring_melt(n_chains, chain_length=100, density=0.85, bond_length=0.97,
     s.bonds.group = group
     s.bonds.typeid = np.zeros(len(group), dtype=np.int32)
     return s
+
+
+def _jittered_lattice(rng, N, L, jitter_frac=0.1):
+    """N points on a jittered simple-cubic lattice filling a cube of side L."""
+    n = int(np.ceil(N ** (1.0 / 3.0)))
+    a = L / n
+    g = (np.arange(n) + 0.5) * a - 0.5 * L
+    x, y, z = np.meshgrid(g, g, g, indexing="ij")
+    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+    pts = pts[rng.permutation(len(pts))[:N]]
+    pts += rng.uniform(-jitter_frac * a, jitter_frac * a, size=pts.shape)
+    box = np.array([L, L, L])
+    pts, img = _wrap(pts, box)
+    return pts
+
+
+def yukawa_replicas(n_replicas=256, seed=4, n_min=500, n_max=20000, rho=(0.3, 0.8), kappa=(0.5, 3.0),
+                    delta=(0.0, 1.0), r_buff=0.4, kT=1.0):
+    """Independent ExpandedYukawa systems of uneven size: N log-uniform in
+    [n_min, n_max], density uniform in rho, kappa and delta uniform, r_cut =
+    delta + 5 / kappa. A draw whose box is smaller than 2 (r_cut + r_buff) is
+    redrawn (kappa, delta) from the same stream; the number of redraws is returned.
+
+    Returns (snapshots, params) with params[r] = dict(epsilon, kappa, delta, r_cut)."""
+    rng = _rng(seed)
+    snaps, params = [], []
+    redraws = 0
+    for _ in range(n_replicas):
+        N = int(round(np.exp(rng.uniform(np.log(n_min), np.log(n_max)))))
+        density = rng.uniform(*rho)
+        L = (N / density) ** (1.0 / 3.0)
+        while True:
+            k = rng.uniform(*kappa)
+            d = rng.uniform(*delta)
+            rc = d + 5.0 / k
+            if L >= 2.0 * (rc + r_buff):
+                break
+            redraws += 1
+        s = Snapshot(N)
+        s.particles.types = ["A"]
+        s.particles.position = _jittered_lattice(rng, N, L, 0.05)
+        s.particles.velocity = maxwell_boltzmann(rng, N, kT)
+        s.particles.acceleration = np.zeros((N, 3))
+        s.configuration.box = [L, L, L, 0.0, 0.0, 0.0]
+        snaps.append(s)
+        params.append(dict(epsilon=1.0, kappa=k, delta=d, r_cut=rc))
+    return snaps, params, redraws
+
+
+def colloid_mixture(N=262144, colloid_fraction=0.04, colloid_diameter=5.0, solvent_diameter=1.0, phi=0.3, seed=3,
+                    kT=1.0):
+    """Binary colloid (type C) / solvent (type S) mixture at total volume fraction
+    phi, placed without overlaps: colloids by random sequential addition at
+    centre distance >= colloid_diameter, solvent on a jittered grid of spacing
+    1.1 solvent diameters outside the colloids' exclusion shells."""
+    rng = _rng(seed)
+    nc = int(round(colloid_fraction * N))
+    ns = N - nc
+    ac, as_ = 0.5 * colloid_diameter, 0.5 * solvent_diameter
+    vol = (4.0 / 3.0) * np.pi * (nc * ac ** 3 + ns * as_ ** 3)
+    L = (vol / phi) ** (1.0 / 3.0)
+    box = np.array([L, L, L])
+    # colloids: random sequential addition on a cell hash
+    cell = colloid_diameter
+    nb = max(1, int(L // cell))
+    w = L / nb
+    grid = {}
+    cols = []
+    while len(cols) < nc:
+        cand = rng.uniform(-0.5 * L, 0.5 * L, size=(4096, 3))
+        for x in cand:
+            c = tuple(((x + 0.5 * L) // w).astype(int) % nb)
+            ok = True
+            for ox in (-1, 0, 1):
+                for oy in (-1, 0, 1):
+                    for oz in (-1, 0, 1):
+                        for j in grid.get(((c[0] + ox) % nb, (c[1] + oy) % nb, (c[2] + oz) % nb), ()):
+                            dd = x - cols[j]
+                            dd -= L * np.rint(dd / L)
+                            if dd @ dd < colloid_diameter ** 2:
+                                ok = False
+                                break
+                        if not ok:
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                grid.setdefault(c, []).append(len(cols))
+                cols.append(x)
+                if len(cols) == nc:
+                    break
+    cols = np.array(cols).reshape(-1, 3)
+    # solvent: jittered grid points outside the colloid shells
+    sp = 1.1 * solvent_diameter
+    n = int(L // sp)
+    g = (np.arange(n) + 0.5) * (L / n) - 0.5 * L
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    keep = np.ones((n, n, n), dtype=bool)
+    excl = ac + solvent_diameter
+    h = L / n
+    reach = int(np.ceil(excl / h)) + 1
+    off = np.arange(-reach, reach + 1)
+    for c in cols:
+        # grid cells around the colloid only
+        ic = np.floor((c + 0.5 * L) / h - 0.5).astype(int)
+        ix = (ic[0] + off) % n
+        iy = (ic[1] + off) % n
+        iz = (ic[2] + off) % n
+        dx = g[ix] - c[0]
+        dy = g[iy] - c[1]
+        dz = g[iz] - c[2]
+        dx -= L * np.rint(dx / L)
+        dy -= L * np.rint(dy / L)
+        dz -= L * np.rint(dz / L)
+        inside = (dx[:, None, None] ** 2 + dy[None, :, None] ** 2 + dz[None, None, :] ** 2) < excl * excl
+        sub = keep[np.ix_(ix, iy, iz)]
+        keep[np.ix_(ix, iy, iz)] = sub & ~inside
+    pts = pts[keep.ravel()]
+    if len(pts) < ns:
+        raise ValueError("not enough room for the solvent at this volume fraction")
+    pts = pts[rng.permutation(len(pts))[:ns]]
+    pts += rng.uniform(-0.04, 0.04, size=pts.shape) * (L / n)
+    pos, img = _wrap(np.concatenate([pts, cols]), box)
+    s = Snapshot(N)
+    p = s.particles
+    p.types = ["S", "C"]
+    p.position = pos
+    p.image = img
+    p.typeid = np.array([0] * ns + [1] * nc, dtype=np.int32)
+    p.diameter = np.where(p.typeid == 1, colloid_diameter, solvent_diameter).astype(np.float64)
+    p.velocity = maxwell_boltzmann(rng, N, kT)
+    s.configuration.box = [L, L, L, 0.0, 0.0, 0.0]
+    return s

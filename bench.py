@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--suite", default="melt", choices=["melt", "batched", "adjoint", "precision", "lj"],
+                    help="melt: the headline line; the others measure the remaining workloads")
     return ap.parse_args()
 
 
@@ -440,8 +442,12 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif args.suite == "melt":
         run_ours(args)
+    else:
+        import bench_suites
+
+        bench_suites.run(args)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,288 @@
+"""Measurements of the workloads beside the headline melt (``bench.py --suite ...``).
+
+Each suite prints one JSON line:
+
+* ``lj``: the PerturbedLennardJones fluid (N = 4096 on a jittered 16^3 lattice,
+  density 0.8, epsilon = sigma = 1, lambda = 0.5, r_cut = 3, buffer 0.4;
+  LangevinFlow, ConstantFlow 0, gamma = 1, dt = 0.005, 1000 steps; forces,
+  energy and virial every 100 steps) on the GPU next to the CPU oracle.
+* ``batched``: 256 ExpandedYukawa replicas (N log-uniform in [500, 20000],
+  density U(0.3, 0.8), kappa U(0.5, 3), delta U(0, 1), r_cut = delta + 5 / kappa,
+  LangevinFlow kT = 1, dt = 0.002) in one fused launch per step (graph-replayed,
+  autotuned threads per particle) against the same replicas advanced one after
+  the other through per-replica engines with plain stream launches.
+* ``adjoint``: gradients on the PerturbedLJ fluid (N = 65,536, density 0.8,
+  learnable epsilon, sigma, lambda; loss on forces and energy against targets at
+  (1.1, 0.98, 0.4)): adjoint / forward cost, agreement with FP64 central finite
+  differences (h = 1e-6), for one force call and through K Langevin steps with
+  checkpoints every 10.
+* ``precision``: the colloid-solvent mixture (N = 262,144, 4 % colloids of
+  diameter 5, phi = 0.3, Hamaker A_SS = 144, A_CS = 100, A_CC = 40, r_cut 3 / 6 / 10;
+  BrownianFlow, ConstantFlow U = 0.1 x, dt = 0.001) -- FP32-compensated against FP64
+  forces, energy and virial along an FP64 Brownian trajectory.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import time
+
+import numpy as np
+
+
+def _cuda_ms(fn, reps=1):
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+# ---------------------------------------------------------------- LJ fluid
+def suite_lj(args):
+    import azplugins_gb300 as az
+    from azplugins_gb300 import workloads
+    from oracle import oracle as orc
+    from tests.helpers import force_error, oracle_system
+
+    snap = workloads.lj_fluid(16, 0.8, 0.05, 1.0, seed=1)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    steps = 1000
+    out = {}
+    for prec in ("fp64", "fp32"):
+        sim = az.Simulation(seed=1, precision=prec)
+        sim.create_state_from_snapshot(snap)
+        lj = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), default_r_cut=3.0)
+        lj.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.5)
+        m = az.methods.LangevinFlow("all", kT=1.0, flow_field=az.flow.ConstantFlow((0, 0, 0)), default_gamma=1.0)
+        sim.operations.integrator = az.md.Integrator(dt=0.005, methods=[m], forces=[lj])
+        sim.run(10)
+        t0 = time.perf_counter()
+        logs = []
+        for _ in range(steps // 100):
+            sim.run(100)
+            logs.append(sim.thermo())
+        dt = time.perf_counter() - t0
+        out[prec] = {"timesteps_per_s": steps / dt, "final_pe": logs[-1]["potential_energy"],
+                     "list_builds": logs[-1]["nlist_builds"]}
+        if prec == "fp32":
+            s = sim.state.get_snapshot()
+            f32, _ = sim._engine.forces()
+        sim.close()
+    # FP32 force error against the FP64 oracle at the final FP32 state
+    rec = orc.pair_params("PerturbedLennardJones", dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.5))
+    md = orc.OracleMD(oracle_system(s, s.particles.acceleration),
+                      pair=dict(name="PerturbedLennardJones", params=rec.reshape(1, 1, 4), rcut=np.array([[3.0]])),
+                      gamma=[1.0], kT=1.0, dt=0.005, seed=1)
+    F, U, W = md.forces()
+    cores = orc.set_threads(os.cpu_count() or 1)
+    md2 = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
+                       pair=dict(name="PerturbedLennardJones", params=rec.reshape(1, 1, 4), rcut=np.array([[3.0]])),
+                       gamma=[1.0], kT=1.0, dt=0.005, seed=1)
+    t0 = time.perf_counter()
+    md2.run(200)
+    cpu = 200 / (time.perf_counter() - t0)
+    line = {"suite": "lj", "workload": "PerturbedLJ fluid N=4096 rho=0.8 lambda=0.5 r_cut=3 LangevinFlow 1000 steps",
+            "gpu": out, "fp32_force_error_vs_fp64_oracle": force_error(f32, F),
+            "fp32_energy_rel_error": abs(f32[:, 3].sum() - U.sum()) / abs(U.sum()),
+            "cpu_oracle": {"timesteps_per_s": cpu, "cores": cores, "sample": "200 steps, OpenMP"}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- batched replicas
+def suite_batched(args):
+    import torch
+
+    import azplugins_gb300 as az
+    from azplugins_gb300 import workloads
+    from azplugins_gb300.batch import ReplicaBatch
+
+    snaps, params, redraws = workloads.yukawa_replicas(256, seed=4)
+    seeds = list(range(1000, 1256))
+    yk = [dict(epsilon=p["epsilon"], kappa=p["kappa"], delta=p["delta"]) for p in params]
+    rc = [p["r_cut"] for p in params]
+    b = ReplicaBatch(snaps, az.pair.ExpandedYukawa, yk, rc, seeds, dt=0.002, precision="fp32")
+    tune = b.autotune(candidates=(1, 2, 4, 8), steps=20)
+    b.run(50)  # warm-up
+    steps = args.steps if args.steps != 2000 else 500
+    ms = _cuda_ms(lambda: b.run(steps, check=False))
+    b.run(0)
+    batched = 256 * steps / (ms * 1e-3)
+    launches = b.last_launches
+    b.close()
+    # the same replicas one after the other, plain stream launches
+    os.environ["AZP_GRAPHS"] = "0"
+    sims = []
+    try:
+        for s, p, sd in zip(snaps, params, seeds):
+            sim = az.Simulation(seed=sd, precision="fp32")
+            sim.create_state_from_snapshot(s)
+            pot = az.pair.ExpandedYukawa(nlist=az.nlist.Cell(buffer=0.4), default_r_cut=p["r_cut"])
+            pot.params[("A", "A")] = dict(epsilon=p["epsilon"], kappa=p["kappa"], delta=p["delta"])
+            m = az.methods.LangevinFlow("all", kT=1.0, flow_field=az.flow.ConstantFlow((0, 0, 0)))
+            sim.operations.integrator = az.md.Integrator(dt=0.002, methods=[m], forces=[pot])
+            sim.run(2)
+            sims.append(sim)
+    finally:
+        os.environ.pop("AZP_GRAPHS", None)
+    sep_steps = 20
+
+    def sweep():
+        for _ in range(sep_steps):
+            for sim in sims:
+                sim._engine.run_async(1)
+
+    ms_sep = _cuda_ms(sweep)
+    separate = 256 * sep_steps / (ms_sep * 1e-3)
+    for sim in sims:
+        sim.close()
+    line = {"suite": "batched", "workload": "256 ExpandedYukawa replicas, N log-uniform [500, 20000], LangevinFlow",
+            "total_particles": int(sum(s.particles.N for s in snaps)), "redraws_for_min_image": redraws,
+            "batched_replica_steps_per_s": batched, "separate_replica_steps_per_s": separate,
+            "speedup": batched / separate, "autotune_ms_per_step": {str(k): v for k, v in tune.items()},
+            "tpp": int(min(tune, key=tune.get)), "batched_launches_in_timed_region": launches,
+            "steps_batched": steps, "steps_separate": sep_steps, "forces": "fp32", "integration": "f64"}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- adjoint
+def suite_adjoint(args):
+    import torch
+
+    import azplugins_gb300 as az
+    from azplugins_gb300 import autodiff
+    from tests.helpers import random_fluid
+
+    snap = random_fluid(65536, 0.8, seed=5, min_dist=0.9)
+    pot = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), mode="shift")
+    ctx = autodiff.Context(pot, snap.particles.types, snap.particles.typeid, snap.configuration.box, 3.0)
+    x = torch.tensor(snap.particles.position, dtype=torch.float64, device="cuda", requires_grad=True)
+    vals = torch.tensor([1.0, 1.0, 0.5], dtype=torch.float64, device="cuda", requires_grad=True)
+    valst = torch.tensor([1.1, 0.98, 0.4], dtype=torch.float64, device="cuda")
+    with torch.no_grad():
+        Ft, Ut = autodiff.pair_forces(x, valst, ctx)
+        Ut = Ut.sum()
+
+    def loss_fn(F, U):
+        return ((F - Ft) ** 2).sum(dim=1).mean() + (U.sum() - Ut) ** 2
+
+    # cost: forward kernel alone vs adjoint kernel alone (same list)
+    F, U = autodiff.pair_forces(x, vals, ctx)
+    loss = loss_fn(F, U)
+    gF, gU = torch.autograd.grad(loss, (F, U), retain_graph=True)
+    fwd = _cuda_ms(lambda: autodiff.pair_forces(x.detach(), vals.detach(), ctx), reps=20)
+    bwd = _cuda_ms(lambda: torch.autograd.grad((F, U), (x, vals), (gF, gU), retain_graph=True), reps=20)
+    gx, gv = torch.autograd.grad(loss, (x, vals))
+    h = 1e-6
+    fd_err = []
+    for k in range(3):
+        with torch.no_grad():
+            vp, vm = vals.detach().clone(), vals.detach().clone()
+            vp[k] += h
+            vm[k] -= h
+            fd = (loss_fn(*autodiff.pair_forces(x.detach(), vp, ctx)) - loss_fn(*autodiff.pair_forces(x.detach(), vm, ctx))) / (2 * h)
+        fd_err.append(abs(float(gv[k]) - float(fd)) / abs(float(fd)))
+    # through K Langevin steps with checkpoints every 10
+    K = 100
+    x0 = x.detach()
+    v0 = torch.tensor(snap.particles.velocity, dtype=torch.float64, device="cuda")
+
+    def roll(v):
+        xx, vv, FF, UU = autodiff.langevin_rollout(x0, v0, v, ctx, K, 0.005, seed=9, checkpoint_every=10)
+        return loss_fn(FF, UU)
+
+    t0 = time.perf_counter()
+    lossK = roll(vals)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    (gK,) = torch.autograd.grad(lossK, (vals,))
+    torch.cuda.synchronize()
+    t_bwd = time.perf_counter() - t0
+    roll_err = []
+    for k in range(3):
+        with torch.no_grad():
+            vp, vm = vals.detach().clone(), vals.detach().clone()
+            vp[k] += h
+            vm[k] -= h
+            fd = (roll(vp) - roll(vm)) / (2 * h)
+        roll_err.append(abs(float(gK[k]) - float(fd)) / abs(float(fd)))
+    line = {"suite": "adjoint", "workload": "PerturbedLJ fluid N=65536 rho=0.8 r_cut=3 shift; learn (eps, sigma, lambda)",
+            "forward_ms": fwd, "adjoint_ms": bwd, "adjoint_over_forward": bwd / fwd,
+            "single_call_fd_rel_error": fd_err, "rollout_steps": K, "checkpoint_every": 10,
+            "rollout_forward_s": t_fwd, "rollout_backward_s": t_bwd, "rollout_fd_rel_error": roll_err,
+            "fd_step": h, "precision": "f64"}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- precision study
+def suite_precision(args):
+    import torch
+
+    import azplugins_gb300 as az
+    from azplugins_gb300 import _compute, workloads
+    from tests.helpers import force_error
+
+    snap = workloads.colloid_mixture(262144, seed=3)
+    N = snap.particles.N
+
+    def colloid(mode="shift"):
+        c = az.pair.Colloid(nlist=az.nlist.Cell(buffer=0.4), mode=mode)
+        c.params[("S", "S")] = dict(A=144.0, a_1=0.0, a_2=0.0, sigma=1.0)
+        c.params[("S", "C")] = dict(A=100.0, a_1=0.0, a_2=2.5, sigma=1.0)
+        c.params[("C", "C")] = dict(A=40.0, a_1=2.5, a_2=2.5, sigma=1.0)
+        c.r_cut[("S", "S")] = 3.0
+        c.r_cut[("S", "C")] = 6.0
+        c.r_cut[("C", "C")] = 10.0
+        return c
+
+    sim = az.Simulation(seed=3, precision="fp64")
+    sim.create_state_from_snapshot(snap)
+    pot = colloid()
+    m = az.methods.BrownianFlow("all", kT=1.0, flow_field=az.flow.ConstantFlow((0.1, 0.0, 0.0)), default_gamma=1.0)
+    sim.operations.integrator = az.md.Integrator(dt=0.001, methods=[m], forces=[pot])
+    total = 5000 if args.steps == 2000 else args.steps
+    every = max(total // 10, 1)
+    rows = []
+    done = 0
+    t_run = 0.0
+    while True:
+        s = sim.state.get_snapshot()
+        st = az.Simulation(precision="fp64")
+        st.create_state_from_snapshot(s)
+        f64, w64 = _compute.pair_forces(st.state, pot, "fp64")
+        f32, w32 = _compute.pair_forces(st.state, pot, "fp32")
+        typ = s.particles.typeid
+        rows.append({"step": done, "force_error": force_error(f32, f64),
+                     "force_error_solvent": force_error(f32[typ == 0], f64[typ == 0]),
+                     "force_error_colloid": force_error(f32[typ == 1], f64[typ == 1]),
+                     "energy_rel_error": abs(f32[:, 3].sum() - f64[:, 3].sum()) / abs(f64[:, 3].sum()),
+                     "virial_rel_error": float(np.abs(w32.sum(axis=0) - w64.sum(axis=0)).max() /
+                                               np.abs(w64.sum(axis=0)).max())})
+        if done >= total:
+            break
+        t0 = time.perf_counter()
+        sim.run(every)
+        t_run += time.perf_counter() - t0
+        done += every
+    line = {"suite": "precision", "workload": f"colloid mixture N={N}, 4% colloids (d=5), phi=0.3, BrownianFlow "
+                                              f"U=0.1x dt=0.001, {total} steps (FP64 trajectory)",
+            "samples": rows, "max_force_error": max(r["force_error"] for r in rows),
+            "max_energy_rel_error": max(r["energy_rel_error"] for r in rows),
+            "max_virial_rel_error": max(r["virial_rel_error"] for r in rows),
+            "fp64_brownian_timesteps_per_s": total / t_run if t_run else None}
+    print(json.dumps(line), flush=True)
+
+
+def run(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    {"lj": suite_lj, "batched": suite_batched, "adjoint": suite_adjoint, "precision": suite_precision}[args.suite](args)

@@ -214,6 +214,21 @@ AZP_API int azp_bond_forces(const azp_system* sys, const uint32_t* n_bonds, cons
                     uint32_t table_height, int kind, const double* params, uint32_t nbondtypes,
                     const azp_forces* out, uint32_t* err, void* stream);
 
+/* ------------------------------------------------------------------ adjoint (gradients)
+ * Vector-Jacobian products of the force drivers, FP64. grad [N][4] holds dL/dF_i
+ * (x, y, z) and dL/dU_i (w) for the per-particle forces and energies the forward
+ * driver writes. Outputs: grad_pos [N][3] = dL/dx_i, and (optional) grad_params,
+ * each particle's share of dL/d(param_type record fields) -- [N][4] for pairs,
+ * [N][8] for bonds -- whose sum over particles is the parameter gradient (for
+ * one type pair / bond type). Pair modes none and shift. No counterpart in the
+ * reference (azplugins has no gradients); they differentiate the drivers above. */
+AZP_API int azp_pair_adjoint(const azp_system* sys, azp_nlist* nl, int kind, const double* params,
+                             const double* r_cut, int shift_mode, const double* grad, double* grad_pos,
+                             double* grad_params, void* stream);
+AZP_API int azp_bond_adjoint(const azp_system* sys, const uint32_t* n_bonds, const uint32_t* table, int kind,
+                             const double* params, uint32_t nbondtypes, const double* grad, double* grad_pos,
+                             double* grad_params, uint32_t* err, void* stream);
+
 /* ------------------------------------------------------------------ integrator drivers
  * Particle subsets: group[n_group] index list, or NULL for all N particles.
  * gamma: device table [ntypes] (ignored when use_lambda != 0: gamma = lambda * diameter).
@@ -302,6 +317,44 @@ AZP_API uint64_t azp_md_last_launches(const azp_md* md);
  * checks or rebuilds; the state advances and is only fit for timing afterwards)
  * between two CUDA events on `stream`; *ms = mean milliseconds per launch. */
 AZP_API int azp_md_time_step_kernel(azp_md* md, int reps, float* ms, void* stream);
+
+/* ------------------------------------------------------------------ batched replicas
+ * Many independent systems (own box, pair parameters, seed; one particle type
+ * each) advanced together: one fused force + Langevin launch per timestep for
+ * all of them, replayed from a CUDA graph, list rebuilds as a graph conditional.
+ * Host arrays are packed replica after replica (replica r at offset
+ * sum_{q<r} N_q, in tag order within the replica). No counterpart in the
+ * reference, which advances one system per HOOMD simulation. */
+typedef struct azp_batch azp_batch;
+typedef struct {
+    uint32_t nsys;
+    const uint32_t* N;          /* host [nsys] */
+    const double* L;            /* host [nsys][3] */
+    int32_t precision;
+    int32_t pair_kind;
+    int32_t shift_mode;
+    const double* pair_params;  /* host [nsys][4] param_type records */
+    const double* r_cut;        /* host [nsys] */
+    double r_buff;
+    double dt, kT, gamma;
+    const uint32_t* seeds;      /* host [nsys] */
+    int32_t noiseless;
+    int32_t pad_;
+    azp_flow flow;
+} azp_batch_config;
+AZP_API azp_batch* azp_batch_create(const azp_batch_config* cfg, int* status);
+AZP_API void azp_batch_destroy(azp_batch* b);
+/* pos [sumN][4] (w ignored), vel [sumN][4] (w = mass), accel [sumN][3] or NULL,
+ * image [sumN][3] or NULL; host pointers */
+AZP_API int azp_batch_set_state(azp_batch* b, const double* pos, const double* vel, const double* accel,
+                                const int32_t* image, uint64_t timestep, void* stream);
+AZP_API int azp_batch_get_state(azp_batch* b, double* pos, double* vel, double* accel, int32_t* image,
+                                void* stream);
+AZP_API int azp_batch_run(azp_batch* b, uint64_t steps, void* stream);
+AZP_API int azp_batch_error(azp_batch* b, uint32_t* err_word, uint32_t* n_builds, void* stream);
+/* threads per particle of the fused step (the autotuner's knob) */
+AZP_API int azp_batch_set_tpp(azp_batch* b, int tpp);
+AZP_API uint64_t azp_batch_last_launches(const azp_batch* b);
 
 #ifdef __cplusplus
 }
