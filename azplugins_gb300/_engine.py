@@ -149,8 +149,9 @@ class Engine:
         p.image = img
 
     def run(self, steps):
+        """Advance with the overflow-safe entry (grows the list and replays)."""
         s = _stream()
-        _lib.check(self._L.azp_md_run(self._md, int(steps), s), "azp_md_run")
+        _lib.check(self._L.azp_md_run_checked(self._md, int(steps), s), "azp_md_run_checked")
         self.last_launches = int(self._L.azp_md_last_launches(self._md))
         err = ctypes.c_uint32(0)
         _lib.check(self._L.azp_md_error(self._md, ctypes.byref(err), s), "azp_md_error")
@@ -160,6 +161,11 @@ class Engine:
             raise _lib.AzpError(-4, "azp_md_run")
         if err.value & _lib.EBIT_NONFINITE:
             raise _lib.AzpError(-7, "azp_md_run")
+
+    def error_word(self):
+        err = ctypes.c_uint32(0)
+        _lib.check(self._L.azp_md_error(self._md, ctypes.byref(err), _stream()), "azp_md_error")
+        return err.value
 
     def run_async(self, steps):
         """Enqueue ``steps`` timesteps without reading the error word back."""

@@ -176,6 +176,7 @@ _SIGNATURES = [
     ("azp_md_set_state", _i, [_vp, _vp, _vp, _vp, _vp, _vp, _u64, _i, _vp]),
     ("azp_md_get_state", _i, [_vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64), _i, _vp]),
     ("azp_md_run", _i, [_vp, _u64, _vp]),
+    ("azp_md_run_checked", _i, [_vp, _u64, _vp]),
     ("azp_md_forces", _i, [_vp, _vp, _vp, _i, _vp]),
     ("azp_md_thermo", _i, [_vp, _vp, _vp]),
     ("azp_md_error", _i, [_vp, ctypes.POINTER(_u32), _vp]),

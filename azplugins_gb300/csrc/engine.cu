@@ -364,6 +364,12 @@ struct azp_md {
     double* tmpd = nullptr;       // tag-order staging [N * 6]
     uint64_t launches = 0;
     bool have_state = false;
+    // entry snapshot of azp_md_run_checked (tag order, allocated on first use)
+    double* snap_pos = nullptr;
+    double* snap_vel = nullptr;
+    double* snap_acc = nullptr;
+    int* snap_img = nullptr;
+    double* snap_diam = nullptr;
     // graphs
     bool use_graphs = true;
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // pair of mid steps starting at cur = 0 / 1
@@ -399,7 +405,8 @@ void free_all(azp_md* m)
                     m->cell_of, m->slot, m->cell_count, m->cell_start, m->members, m->scan_tmp, m->counts, m->nbrs,
                     m->cuts, m->bt_n_tag, m->bt_partner_tag, m->bt_type_tag, m->bt_n, m->bt, m->ex_n, m->ex_idx,
                     m->d_bond_params, m->d_pair_table, m->d_gamma, m->d_noise, m->flags, m->d_ts, m->out_force, m->out_virial,
-                    m->partials, m->thermo, m->tmp4, m->tmpd};
+                    m->partials, m->thermo, m->tmp4, m->tmpd, m->snap_pos, m->snap_vel, m->snap_acc,
+                    m->snap_img, m->snap_diam};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -638,7 +645,7 @@ int size_list(azp_md* m, cudaStream_t s)
         // headroom for density fluctuations between builds
         cudaFree(m->nbrs);
         m->nbrs = nullptr;
-        m->max_nn = (uint32_t)std::ceil(need * 1.3) + 8;
+        m->max_nn = (uint32_t)std::ceil(need * 1.5) + 16;
         st = dalloc(&m->nbrs, (size_t)m->N * m->max_nn);
         if (st) return st;
         free_graphs(m);
@@ -1052,6 +1059,49 @@ int azp_md_error(azp_md* m, uint32_t* err_word, void* stream)
 }
 
 uint64_t azp_md_last_launches(const azp_md* m) { return m ? m->launches : 0; }
+
+int azp_md_run_checked(azp_md* m, uint64_t steps, void* stream)
+{
+    if (!m || !m->have_state) return AZP_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    const uint32_t N = m->N;
+    if (steps == 0 || N == 0) return azp_md_run(m, steps, stream);
+    if (!m->snap_pos) {
+        int st = dalloc(&m->snap_pos, (size_t)4 * N);
+        if (!st) st = dalloc(&m->snap_vel, (size_t)4 * N);
+        if (!st) st = dalloc(&m->snap_acc, (size_t)3 * N);
+        if (!st) st = dalloc(&m->snap_img, (size_t)3 * N);
+        if (!st && m->diam) st = dalloc(&m->snap_diam, N);
+        if (st) return st;
+    }
+    unsigned long long ts0 = 0;
+    AZP_CUDA_TRY(cudaMemcpyAsync(&ts0, m->d_ts, sizeof(ts0), cudaMemcpyDeviceToHost, s));
+    k_store_state<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[m->cur], m->vel, m->accel, m->image, m->tag, N,
+                                                      m->snap_pos, m->snap_vel, m->snap_acc, m->snap_img);
+    if (m->diam) k_to_tag_order_n<<<blocks_for(N, 256), 256, 0, s>>>(m->diam, m->tag, N, 1, 0, m->snap_diam);
+    AZP_CHECK_LAUNCH("k_store_state (snapshot)");
+    AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        int st = azp_md_run(m, steps, stream);
+        if (st) return st;
+        uint32_t f[8];
+        AZP_CUDA_TRY(cudaMemcpyAsync(f, m->flags, sizeof(f), cudaMemcpyDeviceToHost, s));
+        AZP_CUDA_TRY(cudaStreamSynchronize(s));
+        if (f[3] <= m->max_nn) return check_errors(m, s);
+        // grow to the largest count seen and replay from the entry state
+        cudaFree(m->nbrs);
+        m->nbrs = nullptr;
+        m->max_nn = (uint32_t)std::ceil(f[3] * 1.5) + 16;
+        st = dalloc(&m->nbrs, (size_t)N * m->max_nn);
+        if (st) return st;
+        free_graphs(m);
+        AZP_CUDA_TRY(cudaMemsetAsync(m->flags + 1, 0, sizeof(uint32_t) * 3, s));
+        st = azp_md_set_state(m, m->snap_pos, m->snap_vel, m->snap_acc, m->snap_img, m->snap_diam, ts0, 1, stream);
+        if (st) return st;
+        m->launches = 0;
+    }
+    return AZP_ERR_NLIST_OVERFLOW;
+}
 
 int azp_md_time_step_kernel(azp_md* m, int reps, float* ms, void* stream)
 {

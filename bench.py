@@ -62,6 +62,11 @@ def parse():
     return ap.parse_args()
 
 
+def log(msg):
+    """Stage marker on stderr (flushed), so a slow stage can be located."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -276,7 +281,9 @@ def run_ours(args):
         torch.cuda.set_device(0)
     dev = torch.cuda.current_device()
     _lib.load()
+    log("relaxing the melt")
     snap, broken = relaxed_melt(az, args.chains, seed=1 + rank)
+    log(f"relaxed: {broken} stretched bonds")
     N = snap.particles.N
     L = snap.configuration.box[:3]
     flow = az.flow.ParabolicFlow(mean_velocity=2.0 / 3.0, separation=L[1])
@@ -286,6 +293,7 @@ def run_ours(args):
     m = az.methods.LangevinFlow("all", kT=KT, flow_field=flow, default_gamma=GAMMA)
     sim.operations.integrator = az.md.Integrator(dt=DT, methods=[m], forces=[wca, qb])
     sim.run(args.warmup)
+    log("warm-up done")
     eng = sim._engine
     builds0 = sim.thermo()["nlist_builds"]
     stream = torch.cuda.current_stream()
@@ -304,19 +312,25 @@ def run_ours(args):
         torch.distributed.barrier()
     ms = start.elapsed_time(end)
     launches = eng.last_launches
-    eng.run(0)
+    err = eng.error_word()
+    if err:
+        raise RuntimeError(f"timed region raised device error word 0x{err:x}: measurement invalid")
     th = sim.thermo()
     builds = th["nlist_builds"] - builds0
     sim._timestep += args.steps
     sim.state._host_valid = False
     t_max, value = reduce_over_ranks(ms, args.steps, world, "cuda")
 
+    log(f"timed region done: {ms:.1f} ms")
     state_after = sim.state.get_snapshot()
     n_nbr, n_bond = neighbour_stats(state_after)
+    log("neighbour statistics done")
     # end to end through the public C ABI with pinned host buffers
     e2e = e2e_measure(eng, state_after, args.e2e_steps)
+    log("e2e done")
     # dominant kernel alone (last: it advances the state without list checks)
     kernel_ms = time_step_kernel(eng, reps=200)
+    log("kernel timing done")
     bytes_per_launch = algorithmic_bytes(n_nbr, n_bond) * N
     peak, peak_kind = measured_peak()
     achieved = bytes_per_launch / (kernel_ms * 1e-3) / 1e9
@@ -346,6 +360,7 @@ def run_ours(args):
             "e2e": e2e,
         }
         if not args.no_cpu_baseline:
+            log("cpu baseline")
             line["cpu_baseline"] = cpu_baseline(state_after, builds / args.steps)
         print(json.dumps(line), flush=True)
     sim.close()

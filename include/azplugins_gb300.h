@@ -301,8 +301,14 @@ AZP_API int azp_md_set_state(azp_md* md, const double* pos, const double* vel, c
                      void* stream);
 AZP_API int azp_md_get_state(azp_md* md, double* pos, double* vel, double* accel, int32_t* image,
                      uint64_t* timestep, int on_device, void* stream);
-/* Advance `steps` timesteps (HOOMD order: step one, forces, step two). */
+/* Advance `steps` timesteps (HOOMD order: step one, forces, step two).
+ * Enqueues only: errors (list overflow, refused bond, non-finite position) are
+ * read with azp_md_error. */
 AZP_API int azp_md_run(azp_md* md, uint64_t steps, void* stream);
+/* azp_md_run, then synchronise and check: on a list overflow the state saved at
+ * entry is restored, the list grown to the largest count seen, and the steps run
+ * again (HOOMD likewise grows its list and recomputes). */
+AZP_API int azp_md_run_checked(azp_md* md, uint64_t steps, void* stream);
 /* Net force [N][4] (fx, fy, fz, energy) and virial [N][6] at the current
  * positions, in tag order, FP64 (host or device pointers). */
 AZP_API int azp_md_forces(azp_md* md, double* force, double* virial, int on_device, void* stream);
