@@ -165,7 +165,7 @@ _SIGNATURES = [
     ("azp_nlist_download", _i, [_vp, _vp, _vp, _vp]),
     ("azp_pair_forces", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _vp, _i, ctypes.POINTER(Forces), _vp]),
     ("azp_bond_forces", _i, [ctypes.POINTER(System), _vp, _vp, _u32, _i, _vp, _u32, ctypes.POINTER(Forces), _vp, _vp]),
-    ("azp_pair_adjoint", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
+    ("azp_pair_adjoint", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
     ("azp_bond_adjoint", _i, [ctypes.POINTER(System), _vp, _vp, _i, _vp, _u32, _vp, _vp, _vp, _vp, _vp]),
     ("azp_langevin_step1", _i, [ctypes.POINTER(System), _vp, _u32, _d, _vp]),
     ("azp_langevin_step2", _i, [ctypes.POINTER(System), _vp, _u32, _vp, _i, _vp, _i, _d, Flow, _d, _d, _u64, _u32, _i, _vp]),

@@ -74,13 +74,14 @@ class Context:
     """Static inputs of a differentiable force: types, box, list parameters."""
 
     def __init__(self, pair, types, typeid, box, r_cut, r_buff=0.4, exclusions=None, bond=None, bond_group=None,
-                 bond_typeid=None, bond_types=None):
+                 bond_typeid=None, bond_types=None, r_on=0.0):
         torch = _torch()
         self.pair = pair
         self.types = list(types)
         self.typeid = torch.as_tensor(np.asarray(typeid, dtype=np.int64)).cuda()
         self.box = [float(x) for x in box[:3]]
         self.r_cut = float(r_cut)
+        self.r_on = float(r_on)
         self.r_buff = float(r_buff)
         self.N = int(len(typeid))
         self.exclusions = exclusions
@@ -137,7 +138,8 @@ def _pair_tables(ctx, values):
     nt = len(ctx.types)
     params = torch.from_numpy(np.tile(rec, nt * nt)).cuda()
     rc = torch.full((nt * nt,), ctx.r_cut, dtype=torch.float64, device="cuda")
-    return params, rc
+    ro = torch.full((nt * nt,), ctx.r_on, dtype=torch.float64, device="cuda")
+    return params, rc, ro
 
 
 def _make_pair_fn():
@@ -150,14 +152,14 @@ def _make_pair_fn():
             nl = ctx.neighbor_list(x)
             pos4 = ctx.pos4(x)
             sysd = ctx.system(pos4)
-            params, rc = _pair_tables(ctx, values)
+            params, rc, ro = _pair_tables(ctx, values)
             force = torch.zeros((ctx.N, 4), dtype=torch.float64, device="cuda")
             out = _lib.Forces()
             out.force, out.virial, out.virial_pitch, out.precision = force.data_ptr(), None, ctx.N, _lib.FP64
             _lib.check(L.azp_pair_forces(ctypes.byref(sysd), nl.handle, ctx.pair.kind, params.data_ptr(), rc.data_ptr(),
-                                         None, _lib.MODES[ctx.pair.mode], ctypes.byref(out), _stream()),
+                                         ro.data_ptr(), _lib.MODES[ctx.pair.mode], ctypes.byref(out), _stream()),
                        "azp_pair_forces")
-            fctx.save_for_backward(pos4, params, rc, values)
+            fctx.save_for_backward(pos4, params, rc, ro, values)
             fctx.ctx = ctx
             fctx.nl = nl
             return force[:, :3].clone(), force[:, 3].clone()
@@ -165,7 +167,7 @@ def _make_pair_fn():
         @staticmethod
         def backward(fctx, gF, gU):
             L = _lib.load()
-            pos4, params, rc, values = fctx.saved_tensors
+            pos4, params, rc, ro, values = fctx.saved_tensors
             ctx = fctx.ctx
             grad = torch.zeros((ctx.N, 4), dtype=torch.float64, device="cuda")
             if gF is not None:
@@ -176,8 +178,8 @@ def _make_pair_fn():
             grec = torch.empty((ctx.N, 4), dtype=torch.float64, device="cuda")
             sysd = ctx.system(pos4)
             _lib.check(L.azp_pair_adjoint(ctypes.byref(sysd), fctx.nl.handle, ctx.pair.kind, params.data_ptr(),
-                                          rc.data_ptr(), _lib.MODES[ctx.pair.mode], grad.data_ptr(), gpos.data_ptr(),
-                                          grec.data_ptr(), _stream()), "azp_pair_adjoint")
+                                          rc.data_ptr(), ro.data_ptr(), _lib.MODES[ctx.pair.mode], grad.data_ptr(),
+                                          gpos.data_ptr(), grec.data_ptr(), _stream()), "azp_pair_adjoint")
             J = torch.from_numpy(record_jacobian(ctx.pair._name, values.detach().cpu().numpy())).cuda()
             gvals = J.T @ grec.sum(dim=0)
             return gpos, gvals.to(values.dtype), None

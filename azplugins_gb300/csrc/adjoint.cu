@@ -28,8 +28,8 @@ constexpr int ADJ_BLOCK = 128;
 
 // dual records of every type pair: rec[PAIR_REC] then cut[CUT_REC], seeded on p
 template<class Eval>
-__global__ void k_pair_adj_table(const double* __restrict__ params, const double* __restrict__ r_cut, int mode,
-                                 uint32_t ntypes, D5* __restrict__ out)
+__global__ void k_pair_adj_table(const double* __restrict__ params, const double* __restrict__ r_cut,
+                                 const double* __restrict__ r_on, int mode, uint32_t ntypes, D5* __restrict__ out)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntypes * ntypes) return;
@@ -39,7 +39,7 @@ __global__ void k_pair_adj_table(const double* __restrict__ params, const double
         p[m].d[1 + m] = 1.0;
     }
     D5* rec = out + (size_t)t * PAIR_TBL;
-    prepare_pair_t<Eval, D5>(p, r_cut[t], 0.0, mode, rec, rec + PAIR_REC);
+    prepare_pair_t<Eval, D5>(p, r_cut[t], r_on ? r_on[t] : 0.0, mode, rec, rec + PAIR_REC);
 }
 
 struct AdjArgs {
@@ -54,6 +54,7 @@ struct AdjArgs {
     double* grad_pos;         // [N][3]
     double* grad_params;      // [N][4]
     int tpp;
+    int xplor;                // smoothing active: every evaluator takes the dual path
 };
 
 // phi, phi' = dphi/ds, dphi/dp[m], de/dp[m] of one pair
@@ -116,6 +117,7 @@ template<class Eval> AZP_D PairDerivs dual_derivs(const D5* rec, double s)
     D5 f, e;
     Eval::eval(rec, x, f, e);
     e -= rec[Eval::SHIFT_SLOT];
+    xplor(rec + PAIR_REC, x, f, e);  // no-op unless the type pair is smoothed
     r.phi = f.v;
     r.dphi_ds = f.d[0];
     for (int m = 0; m < 4; ++m) {
@@ -151,10 +153,14 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_pair_adjoint(AdjArgs a)
             const D5* cut = rec + PAIR_REC;
             if (!(s < cut[0].v) || !Eval::enabled(rec)) continue;
             PairDerivs q;
-            if constexpr (std::is_same<Eval, PerturbedLJ>::value)
-                q = plj_derivs(rec, s);
-            else
+            if constexpr (std::is_same<Eval, PerturbedLJ>::value) {
+                if (a.xplor)
+                    q = dual_derivs<Eval>(rec, s);
+                else
+                    q = plj_derivs(rec, s);
+            } else {
                 q = dual_derivs<Eval>(rec, s);
+            }
             const double4_32a Gj = a.grad[j];
             const double Gx = Gi.x - Gj.x, Gy = Gi.y - Gj.y, Gz = Gi.z - Gj.z;
             const double g = 0.5 * (Gi.w + Gj.w);
@@ -242,12 +248,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_bond_adjoint(BondAdjArgs a)
 }
 
 template<class Eval>
-int launch_adj(const azp_system* sys, azp_nlist* nl, const double* params, const double* r_cut, int mode,
-               const double* grad, double* grad_pos, double* grad_params, cudaStream_t s)
+int launch_adj(const azp_system* sys, azp_nlist* nl, const double* params, const double* r_cut, const double* r_on,
+               int mode, const double* grad, double* grad_pos, double* grad_params, cudaStream_t s)
 {
     const uint32_t nt2 = sys->ntypes * sys->ntypes;
     D5* table = reinterpret_cast<D5*>(nl->adj_table);
-    k_pair_adj_table<Eval><<<(nt2 + 63) / 64, 64, 0, s>>>(params, r_cut, mode, sys->ntypes, table);
+    k_pair_adj_table<Eval><<<(nt2 + 63) / 64, 64, 0, s>>>(params, r_cut, r_on, mode, sys->ntypes, table);
     AdjArgs a;
     a.pos = reinterpret_cast<const double4_32a*>(sys->pos);
     a.grad = reinterpret_cast<const double4_32a*>(grad);
@@ -264,6 +270,7 @@ int launch_adj(const azp_system* sys, azp_nlist* nl, const double* params, const
     a.grad_pos = grad_pos;
     a.grad_params = grad_params;
     a.tpp = nl->tpp;
+    a.xplor = mode == AZP_MODE_XPLOR;
     const size_t threads = (size_t)sys->N * a.tpp;
     k_pair_adjoint<Eval><<<(uint32_t)((threads + ADJ_BLOCK - 1) / ADJ_BLOCK), ADJ_BLOCK, 0, s>>>(a);
     AZP_CHECK_LAUNCH("k_pair_adjoint");
@@ -275,23 +282,24 @@ int launch_adj(const azp_system* sys, azp_nlist* nl, const double* params, const
 extern "C" {
 
 int azp_pair_adjoint(const azp_system* sys, azp_nlist* nl, int kind, const double* params, const double* r_cut,
-                     int shift_mode, const double* grad, double* grad_pos, double* grad_params, void* stream)
+                     const double* r_on, int shift_mode, const double* grad, double* grad_pos, double* grad_params,
+                     void* stream)
 {
     if (!sys || !nl || !params || !r_cut || !grad || !grad_pos) return AZP_ERR_INVALID;
     if (sys->N != nl->N || sys->ntypes != nl->ntypes || sys->ntypes == 0 || sys->ntypes > azp::MAX_PAIR_TYPES)
         return AZP_ERR_INVALID;
-    if (shift_mode != AZP_MODE_NONE && shift_mode != AZP_MODE_SHIFT) return AZP_ERR_UNSUPPORTED;
+    if (shift_mode < AZP_MODE_NONE || shift_mode > AZP_MODE_XPLOR) return AZP_ERR_INVALID;
     if (sys->N == 0) return AZP_OK;
     cudaStream_t s = azp::as_stream(stream);
     switch (kind) {
     case AZP_PAIR_PERTURBED_LJ:
-        return azp::launch_adj<azp::PerturbedLJ>(sys, nl, params, r_cut, shift_mode, grad, grad_pos, grad_params, s);
+        return azp::launch_adj<azp::PerturbedLJ>(sys, nl, params, r_cut, r_on, shift_mode, grad, grad_pos, grad_params, s);
     case AZP_PAIR_EXPANDED_YUKAWA:
-        return azp::launch_adj<azp::ExpandedYukawa>(sys, nl, params, r_cut, shift_mode, grad, grad_pos, grad_params, s);
+        return azp::launch_adj<azp::ExpandedYukawa>(sys, nl, params, r_cut, r_on, shift_mode, grad, grad_pos, grad_params, s);
     case AZP_PAIR_HERTZ:
-        return azp::launch_adj<azp::Hertz>(sys, nl, params, r_cut, shift_mode, grad, grad_pos, grad_params, s);
+        return azp::launch_adj<azp::Hertz>(sys, nl, params, r_cut, r_on, shift_mode, grad, grad_pos, grad_params, s);
     case AZP_PAIR_COLLOID:
-        return azp::launch_adj<azp::Colloid>(sys, nl, params, r_cut, shift_mode, grad, grad_pos, grad_params, s);
+        return azp::launch_adj<azp::Colloid>(sys, nl, params, r_cut, r_on, shift_mode, grad, grad_pos, grad_params, s);
     default: return AZP_ERR_INVALID;
     }
 }

@@ -58,7 +58,7 @@ AZP_D void comp_shfl_add(Comp& c, int m)
 // ---------------------------------------------------------------- rebuild kernels
 __global__ void k_b_zero(uint32_t* __restrict__ p, uint32_t n, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0u;
 }
 
@@ -75,7 +75,7 @@ __global__ void k_b_assign(const double4_32a* __restrict__ pos, const uint16_t* 
                            uint32_t* __restrict__ slot, uint32_t* __restrict__ cell_count,
                            const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const SysInfo& si = info[sys[i]];
@@ -92,7 +92,7 @@ __global__ void k_b_scatter(const uint32_t* __restrict__ cell_of, const uint32_t
                             const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ members, uint32_t N,
                             const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     members[cell_start[cell_of[i]] + slot[i]] = i;
@@ -101,10 +101,13 @@ __global__ void k_b_scatter(const uint32_t* __restrict__ cell_of, const uint32_t
 __global__ void k_b_cell_sort(const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ members, uint32_t ncell,
                               const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
     const uint32_t b = cell_start[c], e = cell_start[c + 1];
+    // a cell this crowded only occurs in a broken configuration: keep the
+    // arrival order rather than spend O(n^2) on it
+    if (e - b > kMaxSortedCell) return;
     for (uint32_t a = b + 1; a < e; ++a) {
         const uint32_t v = members[a];
         uint32_t k = a;
@@ -129,7 +132,7 @@ struct BPerm {
 
 __global__ void k_b_gather(BPerm a, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.N) return;
     const uint32_t o = a.members[s];
@@ -146,7 +149,7 @@ __global__ void k_b_gather(BPerm a, const uint32_t* __restrict__ gate)
 
 __global__ void k_b_back(BPerm a, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.N) return;
     a.pos[s] = a.t_pos[s];
@@ -164,7 +167,7 @@ __global__ void k_b_fixed(const double4_32a* __restrict__ pos, const uint16_t* _
                           const SysInfo* __restrict__ info, uint4* __restrict__ fa, uint4* __restrict__ fb,
                           const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const SysInfo& si = info[sys[i]];
@@ -184,7 +187,7 @@ __global__ void __launch_bounds__(128)
               const uint32_t* __restrict__ cell_of, uint32_t* __restrict__ counts, uint32_t* __restrict__ nbrs,
               uint32_t max_nn, uint32_t* __restrict__ maxcount, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const SysInfo& si = info[sys[i]];
@@ -236,14 +239,14 @@ __global__ void __launch_bounds__(128)
 
 __global__ void k_b_finish(uint32_t* __restrict__ flags, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     flags[0] = 0u;
     flags[2] += 1u;
 }
 
 __global__ void k_b_arm(const uint32_t* __restrict__ flags, cudaGraphConditionalHandle h)
 {
-    cudaGraphSetConditional(h, flags[0] ? 1u : 0u);
+    cudaGraphSetConditional(h, (flags[0] && !flags[1]) ? 1u : 0u);
 }
 
 // ---------------------------------------------------------------- fused step
@@ -441,7 +444,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_b_step(BStep a)
         const uint32_t t = atomicAdd(&a.flags[4], 1u);
         if (t == gridDim.x - 1) {
             __threadfence();
-            const uint32_t req = atomicAdd(&a.flags[0], 0u);
+            const uint32_t req = atomicAdd(&a.flags[0], 0u) && !atomicAdd(&a.flags[1], 0u);
             if (a.set_cond) cudaGraphSetConditional(a.next_cond, req ? 1u : 0u);
             a.flags[4] = 0u;
             *a.d_ts_rw = *a.d_ts_rw + 1ull;

@@ -6,6 +6,9 @@
 
 namespace azp
 {
+// cells holding more particles than this are not sorted by index
+constexpr uint32_t kMaxSortedCell = 512;
+
 // Cells of width >= r_list_max along each axis; an axis with fewer than 3 cells
 // is scanned as a single cell (no duplicate images).
 struct CellGrid {

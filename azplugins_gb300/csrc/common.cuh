@@ -29,6 +29,12 @@ int record_cuda_error(cudaError_t e, const char* what);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Rebuild kernels take a pointer to the engine's flag words: [0] the rebuild
+// request, [1] the error bits. They do nothing unless a rebuild was requested
+// and no error has been raised (a system that produced non-finite positions is
+// not re-binned: the run ends with the error instead). NULL: always run.
+AZP_D bool gated_off(const uint32_t* gate) { return gate && (gate[0] == 0u || gate[1] != 0u); }
+
 // ---------------------------------------------------------------- type bits
 // The type lives in the low 32 bits of pos.w's bit pattern (HOOMD __int_as_scalar).
 AZP_HD uint32_t type_of(double w)

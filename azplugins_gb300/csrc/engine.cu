@@ -36,7 +36,7 @@ int launch_md_step(int pair_kind, int bond_kind, int precision, int integ, const
 // ---------------------------------------------------------------- rebuild kernels
 __global__ void k_zero_gated(uint32_t* __restrict__ p, uint32_t n, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0u;
 }
 
@@ -55,7 +55,7 @@ struct PermArgs {
 // temps[s] <- arrays[members[s]]
 __global__ void k_perm_gather(PermArgs a, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.N) return;
     const uint32_t o = a.members[s];
@@ -75,7 +75,7 @@ __global__ void k_perm_gather(PermArgs a, const uint32_t* __restrict__ gate)
 // arrays[s] <- temps[s]; rtag[tag[s]] = s
 __global__ void k_perm_back(PermArgs a, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.N) return;
     a.pos[s] = a.t_pos[s];
@@ -101,7 +101,7 @@ __global__ void k_bond_table(const uint32_t* __restrict__ tag, const uint32_t* _
                              uint2* __restrict__ bt, uint32_t* __restrict__ ex_n, uint32_t* __restrict__ ex_idx,
                              int exclude, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const uint32_t t = tag[i];
@@ -117,7 +117,7 @@ __global__ void k_bond_table(const uint32_t* __restrict__ tag, const uint32_t* _
 
 __global__ void k_finish_rebuild(uint32_t* __restrict__ flags, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     flags[0] = 0u;
     flags[2] += 1u;
 }
@@ -125,7 +125,7 @@ __global__ void k_finish_rebuild(uint32_t* __restrict__ flags, const uint32_t* _
 // first graph node of a replay: arm the first conditional from the request flag
 __global__ void k_arm(const uint32_t* __restrict__ flags, cudaGraphConditionalHandle h)
 {
-    cudaGraphSetConditional(h, flags[0] ? 1u : 0u);
+    cudaGraphSetConditional(h, (flags[0] && !flags[1]) ? 1u : 0u);
 }
 
 // Langevin step one in place at the start of a run (src/TwoStepLangevinFlow.h:128-153)

@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
             const uint32_t t = atomicAdd(&a.flags[4], 1u);
             if (t == gridDim.x - 1) {
                 __threadfence();
-                const uint32_t req = atomicAdd(&a.flags[0], 0u);
+                const uint32_t req = atomicAdd(&a.flags[0], 0u) && !atomicAdd(&a.flags[1], 0u);
                 if (a.set_cond) cudaGraphSetConditional(a.next_cond, req ? 1u : 0u);
                 a.flags[4] = 0u;
                 *a.d_timestep_rw = *a.d_timestep_rw + 1ull;

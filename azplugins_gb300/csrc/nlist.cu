@@ -104,7 +104,7 @@ __global__ void k_cell_assign(const double4_32a* __restrict__ pos, uint32_t N, C
                               uint32_t* __restrict__ slot, uint32_t* __restrict__ cell_count,
                               const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const double4_32a p = pos[i];
@@ -120,7 +120,7 @@ __global__ void k_cell_scatter(const uint32_t* __restrict__ cell_of, const uint3
                                const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ members, uint32_t N,
                                const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     members[cell_start[cell_of[i]] + slot[i]] = i;
@@ -130,10 +130,13 @@ __global__ void k_cell_scatter(const uint32_t* __restrict__ cell_of, const uint3
 __global__ void k_cell_sort(const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ members, uint32_t ncell,
                             const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
     const uint32_t b = cell_start[c], e = cell_start[c + 1];
+    // a cell this crowded only occurs in a broken configuration: keep the
+    // arrival order rather than spend O(n^2) on it
+    if (e - b > kMaxSortedCell) return;
     for (uint32_t a = b + 1; a < e; ++a) {
         const uint32_t v = members[a];
         uint32_t k = a;
@@ -172,7 +175,7 @@ __global__ void __launch_bounds__(NLIST_BLOCK)
                   const uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, uint32_t* __restrict__ nbrs,
                   uint32_t max_nn, uint32_t* __restrict__ flags, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     __shared__ ListCut s_cut[MAX_LIST_TYPES * MAX_LIST_TYPES];
     const uint32_t nt2 = ntypes * ntypes;
     for (uint32_t t = threadIdx.x; t < nt2; t += blockDim.x) s_cut[t] = cuts[t];
@@ -268,7 +271,7 @@ void launch_cell_scatter(const uint32_t* cell_of, const uint32_t* slot, const ui
 __global__ void k_to_fixed2(const double4_32a* __restrict__ pos, uint4* __restrict__ fa, uint4* __restrict__ fb,
                             uint32_t N, double lx, double ly, double lz, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const double4_32a p = pos[i];

@@ -31,7 +31,7 @@ __device__ __forceinline__ uint32_t block_inclusive_scan(uint32_t v, uint32_t* s
 __global__ void k_scan_blocks(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                               uint32_t* __restrict__ sums, uint32_t n, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     __shared__ uint32_t s_warp[32];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t v = i < n ? in[i] : 0u;
@@ -42,7 +42,7 @@ __global__ void k_scan_blocks(const uint32_t* __restrict__ in, uint32_t* __restr
 
 __global__ void k_scan_sums(uint32_t* __restrict__ sums, uint32_t nb, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     __shared__ uint32_t s_warp[32];
     __shared__ uint32_t s_carry;
     if (threadIdx.x == 0) s_carry = 0u;
@@ -62,7 +62,7 @@ __global__ void k_scan_sums(uint32_t* __restrict__ sums, uint32_t nb, const uint
 __global__ void k_scan_finish(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                               const uint32_t* __restrict__ sums, uint32_t n, const uint32_t* __restrict__ gate)
 {
-    if (gate && *gate == 0u) return;
+    if (gated_off(gate)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         const uint32_t v = in[i];

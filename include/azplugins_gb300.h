@@ -220,11 +220,11 @@ AZP_API int azp_bond_forces(const azp_system* sys, const uint32_t* n_bonds, cons
  * driver writes. Outputs: grad_pos [N][3] = dL/dx_i, and (optional) grad_params,
  * each particle's share of dL/d(param_type record fields) -- [N][4] for pairs,
  * [N][8] for bonds -- whose sum over particles is the parameter gradient (for
- * one type pair / bond type). Pair modes none and shift. No counterpart in the
- * reference (azplugins has no gradients); they differentiate the drivers above. */
+ * one type pair / bond type). All pair modes (r_on may be NULL). No counterpart
+ * in the reference (azplugins has no gradients); they differentiate the drivers above. */
 AZP_API int azp_pair_adjoint(const azp_system* sys, azp_nlist* nl, int kind, const double* params,
-                             const double* r_cut, int shift_mode, const double* grad, double* grad_pos,
-                             double* grad_params, void* stream);
+                             const double* r_cut, const double* r_on, int shift_mode, const double* grad,
+                             double* grad_pos, double* grad_params, void* stream);
 AZP_API int azp_bond_adjoint(const azp_system* sys, const uint32_t* n_bonds, const uint32_t* table, int kind,
                              const double* params, uint32_t nbondtypes, const double* grad, double* grad_pos,
                              double* grad_params, uint32_t* err, void* stream);

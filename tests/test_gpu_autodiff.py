@@ -198,14 +198,41 @@ def test_quartic_bond_k_gradient():
     assert abs(float(gv[0]) - float(fd)) <= 1e-6 * abs(float(fd))
 
 
+def test_xplor_single_call_gradient():
+    torch = _torch()
+    import azplugins_gb300 as az
+    from azplugins_gb300 import autodiff
+
+    snap = _fluid(3000, 0.8, seed=47)
+    pot = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), mode="xplor")
+    ctx = autodiff.Context(pot, snap.particles.types, snap.particles.typeid, snap.configuration.box, 3.0, r_on=2.5)
+    x = torch.tensor(snap.particles.position, dtype=torch.float64, device="cuda", requires_grad=True)
+    v = torch.tensor([1.0, 1.0, 0.5], dtype=torch.float64, device="cuda", requires_grad=True)
+    F, U = autodiff.pair_forces(x, v, ctx)
+    loss = (F ** 2).sum() + U.sum()
+    (gv,) = torch.autograd.grad(loss, (v,))
+    h = 1e-6
+    for k in range(3):
+        with torch.no_grad():
+            vp, vm = v.detach().clone(), v.detach().clone()
+            vp[k] += h
+            vm[k] -= h
+            Fp, Up = autodiff.pair_forces(x, vp, ctx)
+            Fm, Um = autodiff.pair_forces(x, vm, ctx)
+            fd = (((Fp ** 2).sum() + Up.sum()) - ((Fm ** 2).sum() + Um.sum())) / (2 * h)
+        assert abs(float(gv[k]) - float(fd)) <= 1e-6 * abs(float(fd)), k
+
+
 def test_rollout_gradient_matches_finite_differences():
+    # forces smoothed to zero at r_cut (xplor): the loss is C1 along trajectories,
+    # so central differences through the dynamics are meaningful
     torch = _torch()
     import azplugins_gb300 as az
     from azplugins_gb300 import autodiff, workloads
 
     snap = workloads.lj_fluid(n_side=8, density=0.8, seed=46)
-    pot = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), mode="shift")
-    ctx = _ctx(snap, pot, 3.0)
+    pot = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), mode="xplor")
+    ctx = autodiff.Context(pot, snap.particles.types, snap.particles.typeid, snap.configuration.box, 3.0, r_on=2.5)
     x0 = torch.tensor(snap.particles.position, dtype=torch.float64, device="cuda")
     v0 = torch.tensor(snap.particles.velocity, dtype=torch.float64, device="cuda")
     vals = torch.tensor([1.0, 1.0, 0.5], dtype=torch.float64, device="cuda", requires_grad=True)
@@ -223,4 +250,64 @@ def test_rollout_gradient_matches_finite_differences():
             vp[k] += h
             vm[k] -= h
             fd = (loss_of(vp) - loss_of(vm)) / (2 * h)
-        assert abs(float(gv[k]) - float(fd)) <= 1e-5 * abs(float(fd)), (k, float(gv[k]), float(fd))
+        assert abs(float(gv[k]) - float(fd)) <= 1e-6 * abs(float(fd)), (k, float(gv[k]), float(fd))
+
+
+def test_rollout_gradient_matches_dense_autograd():
+    # PerturbedLJ with its force jump at r_cut: the exact gradient of the same
+    # discrete dynamics, taken by torch autograd through a dense FP64 all-pairs
+    # implementation, is the reference (finite differences see the cutoff jumps)
+    torch = _torch()
+    import azplugins_gb300 as az
+    from azplugins_gb300 import autodiff, workloads
+
+    snap = workloads.lj_fluid(n_side=8, density=0.8, seed=48)
+    pot = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), mode="shift")
+    ctx = _ctx(snap, pot, 2.5)
+    L = torch.tensor(snap.configuration.box[:3], dtype=torch.float64, device="cuda")
+    x0 = torch.tensor(snap.particles.position, dtype=torch.float64, device="cuda")
+    v0 = torch.tensor(snap.particles.velocity, dtype=torch.float64, device="cuda")
+    K, dt, seed = 10, 0.005, 9
+    vals = torch.tensor([1.0, 1.0, 0.5], dtype=torch.float64, device="cuda", requires_grad=True)
+    x, v, F, U = autodiff.langevin_rollout(x0, v0, vals, ctx, K, dt, seed=seed, checkpoint_every=5)
+    loss = (F ** 2).sum(dim=1).mean() + (U.sum() / x.shape[0]) ** 2
+    (gv,) = torch.autograd.grad(loss, (vals,))
+    # dense
+    p = vals.detach().clone().requires_grad_(True)
+    c = float(np.sqrt(6.0 * 1.0 * 1.0 / dt))
+
+    def dense_forces(xx):
+        d = xx[:, None, :] - xx[None, :, :]
+        d = d - L * torch.round(d / L)
+        N = xx.shape[0]
+        eye = torch.eye(N, dtype=torch.bool, device="cuda")
+        s = (d * d).sum(-1) + eye.double()
+        mask = (s < 2.5 * 2.5) & ~eye
+        eps, sig, lam = p[0], p[1], p[2]
+
+        def e_of(s):
+            r6 = (sig * sig / s) ** 3
+            elj = 4 * eps * (r6 * r6 - r6)
+            return torch.where(s < 2 ** (1 / 3) * sig * sig, elj + eps * (1 - lam), lam * elj)
+
+        r6 = (sig * sig / s) ** 3
+        fdr = 24 * eps * (2 * r6 * r6 - r6) / s
+        fdr = torch.where(s < 2 ** (1 / 3) * sig * sig, fdr, lam * fdr)
+        fdr = torch.where(mask, fdr, torch.zeros_like(fdr))
+        e = torch.where(mask, e_of(s) - e_of(torch.tensor(6.25, dtype=torch.float64, device="cuda")),
+                        torch.zeros_like(s))
+        return (fdr[:, :, None] * d).sum(1), 0.5 * e.sum(1)
+
+    xx, vv = x0, v0
+    FF, UU = dense_forces(xx)
+    a = FF
+    for t in range(K):
+        xx = xx + (vv + 0.5 * dt * a) * dt
+        vv = vv + 0.5 * dt * a
+        FF, UU = dense_forces(xx)
+        a = FF + (autodiff.langevin_noise(xx.shape[0], t, seed, c) - vv)
+        vv = vv + 0.5 * dt * a
+    assert torch.allclose(xx, x, rtol=0, atol=1e-9)
+    loss_d = (FF ** 2).sum(dim=1).mean() + (UU.sum() / xx.shape[0]) ** 2
+    (gd,) = torch.autograd.grad(loss_d, (p,))
+    assert bool(((gv - gd).abs() <= 1e-6 * gd.abs() + 1e-10).all()), (gv, gd)
