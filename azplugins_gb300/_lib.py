@@ -27,6 +27,7 @@ STATUS = {
     -8: "unsupported combination",
     -9: "cell list overflow",
     -10: "no CUDA device",
+    -11: "size above the entry point's fixed limit",
 }
 
 # header enums
@@ -46,7 +47,7 @@ class AzpError(RuntimeError):
         self.status = status
         msg = STATUS.get(status, f"status {status}")
         detail = ""
-        if status == -2 and _lib is not None:
+        if status in (-2, -11) and _lib is not None:
             detail = _lib.azp_last_error().decode(errors="replace")
         super().__init__(f"{what}: {msg}" + (f" ({detail})" if detail else ""))
 
@@ -164,6 +165,8 @@ _SIGNATURES = [
     ("azp_nlist_set_tpp", _i, [_vp, _i]),
     ("azp_nlist_download", _i, [_vp, _vp, _vp, _vp]),
     ("azp_pair_forces", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _vp, _i, ctypes.POINTER(Forces), _vp]),
+    ("azp_pair_forces_static", _i, [ctypes.POINTER(System), _vp, _vp, _u32, _i, _vp, _vp, _vp, _i,
+                                    ctypes.POINTER(Forces), _vp]),
     ("azp_bond_forces", _i, [ctypes.POINTER(System), _vp, _vp, _u32, _i, _vp, _u32, ctypes.POINTER(Forces), _vp, _vp]),
     ("azp_pair_adjoint", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
     ("azp_bond_adjoint", _i, [ctypes.POINTER(System), _vp, _vp, _i, _vp, _u32, _vp, _vp, _vp, _vp, _vp]),

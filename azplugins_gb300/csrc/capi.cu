@@ -23,6 +23,12 @@ int record_cuda_error(cudaError_t e, const char* what)
     return AZP_ERR_CUDA;
 }
 
+int record_error(int status, const char* msg)
+{
+    g_last_error = msg;
+    return status;
+}
+
 }  // namespace azp
 
 namespace

@@ -14,6 +14,8 @@ namespace azp
 // ---------------------------------------------------------------- error handling
 // Records the last failing CUDA call for azp_last_error(); returns AZP_ERR_CUDA.
 int record_cuda_error(cudaError_t e, const char* what);
+// Records a message for azp_last_error(); returns status.
+int record_error(int status, const char* msg);
 
 #define AZP_CUDA_TRY(call)                                        \
     do {                                                          \

@@ -53,7 +53,8 @@ enum azp_status {
     AZP_ERR_NONFINITE = -7,       /* a non-finite position was produced */
     AZP_ERR_UNSUPPORTED = -8,     /* combination not built */
     AZP_ERR_CELL_OVERFLOW = -9,   /* internal cell list capacity exceeded */
-    AZP_ERR_NO_DEVICE = -10       /* no CUDA device visible */
+    AZP_ERR_NO_DEVICE = -10,      /* no CUDA device visible */
+    AZP_ERR_TOO_LARGE = -11       /* size above a fixed limit of the entry point */
 };
 
 /* device error word bits (azp_md_error / azp_err_word) */
@@ -203,6 +204,28 @@ AZP_API int azp_pair_forces(const azp_system* sys, azp_nlist* nl, int kind, cons
                     void* stream);
 /* threads per particle of azp_pair_forces: 1, 2, 4, 8, 16 or 32 */
 AZP_API int azp_nlist_set_tpp(azp_nlist* nl, int tpp);
+
+/* Pair forces without any allocation. No counterpart in the reference: it is
+ * azp_pair_forces for callers that cannot allocate device memory (a host code
+ * that reserves its whole device budget at start-up and lets plugins use only
+ * buffers it owns, or a caller that cannot accept cudaMalloc's implicit device
+ * synchronisation), so it cannot hold an azp_nlist workspace. The list comes in
+ * as plain device arrays: counts[N] and neighbors[k * N + i] for
+ * k < max_neighbors (the layout azp_nlist_view returns); everything else is as
+ * for azp_pair_forces, with 4 threads per particle, so the results are the same.
+ * Its scratch (type-pair table, FP32 position shadow) is one static device array
+ * of this library, about 4.1 MB, held on every GPU that loads the library until
+ * the process exits. Limits: N <= AZP_STATIC_MAX_N (else AZP_ERR_TOO_LARGE with a
+ * message in azp_last_error) and ntypes <= 16.
+ * The first call on a device looks the array's address up for that device (with
+ * that device current); make that first call before any stream capture.
+ * Calls share the array: two calls whose kernels overlap on the GPU (different
+ * streams, or different host threads, on one device) race on it. Every call
+ * rewrites what it reads, so nothing carries over from the previous call. */
+#define AZP_STATIC_MAX_N 262144u
+AZP_API int azp_pair_forces_static(const azp_system* sys, const uint32_t* counts, const uint32_t* neighbors,
+                                   uint32_t max_neighbors, int kind, const double* params, const double* r_cut,
+                                   const double* r_on, int shift_mode, const azp_forces* out, void* stream);
 
 /* Bond forces from a per-particle bond table (replaces
  * gpu_compute_bond_forces<Eval,2>): for particle i its bonds are
