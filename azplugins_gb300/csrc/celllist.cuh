@@ -52,7 +52,14 @@ void launch_nlist_build(const double4_32a* pos, const uint4* fixed, uint32_t N, 
                         const uint32_t* cell_start, const uint32_t* members, const uint32_t* cell_of,
                         const ListCut* cuts, uint32_t ntypes, const uint32_t* ex_n, const uint32_t* ex_keys,
                         uint32_t ex_width, const uint32_t* keys, uint32_t* counts, uint32_t* nbrs,
-                        uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s);
+                        uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s,
+                        const uint4* lo = nullptr);
+// lo != NULL: positions are the 64-bit fixed words (fixed = high, lo = low) of the
+// FP32-force engine, and the exact FP64 test runs on their FP64 conversion
+
+// cell_of / slot / cell_count from the high words of 64-bit fixed positions
+void launch_cell_assign_fx(const uint4* fixed, uint32_t N, const CellGrid& g, uint32_t* cell_of, uint32_t* slot,
+                           uint32_t* cell_count, cudaStream_t s, const uint32_t* gate);
 
 // fixed-point shadow of pos into one or two arrays (gated)
 void launch_to_fixed2(const double4_32a* pos, uint4* a, uint4* b, uint32_t N, const azp_box& box, cudaStream_t s,

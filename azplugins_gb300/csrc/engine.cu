@@ -42,7 +42,11 @@ __global__ void k_zero_gated(uint32_t* __restrict__ p, uint32_t n, const uint32_
 
 struct PermArgs {
     const uint32_t* members;
-    double4_32a *pos, *t_pos;
+    double4_32a *pos, *t_pos;   // pos NULL in FP32-force mode (the fixed words move instead)
+    uint4 *fix, *t_fix;         // FP32-force mode: high and low fixed words, masses
+    uint4 *lo, *t_lo;
+    double *mass, *t_mass;
+    uint4* fix_build;           // FP32-force mode: receives the new high words too
     double4_32a *vel, *t_vel;
     double *accel, *t_accel;
     int *image, *t_image;
@@ -59,7 +63,12 @@ __global__ void k_perm_gather(PermArgs a, const uint32_t* __restrict__ gate)
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.N) return;
     const uint32_t o = a.members[s];
-    a.t_pos[s] = a.pos[o];
+    if (a.pos) a.t_pos[s] = a.pos[o];
+    if (a.fix) {
+        a.t_fix[s] = a.fix[o];
+        a.t_lo[s] = a.lo[o];
+        a.t_mass[s] = a.mass[o];
+    }
     a.t_vel[s] = a.vel[o];
     a.t_accel[3 * s] = a.accel[3 * o];
     a.t_accel[3 * s + 1] = a.accel[3 * o + 1];
@@ -78,7 +87,14 @@ __global__ void k_perm_back(PermArgs a, const uint32_t* __restrict__ gate)
     if (gated_off(gate)) return;
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.N) return;
-    a.pos[s] = a.t_pos[s];
+    if (a.pos) a.pos[s] = a.t_pos[s];
+    if (a.fix) {
+        const uint4 f = a.t_fix[s];
+        a.fix[s] = f;
+        a.fix_build[s] = f;
+        a.lo[s] = a.t_lo[s];
+        a.mass[s] = a.t_mass[s];
+    }
     a.vel[s] = a.t_vel[s];
     a.accel[3 * s] = a.t_accel[3 * s];
     a.accel[3 * s + 1] = a.t_accel[3 * s + 1];
@@ -173,14 +189,110 @@ __global__ void k_md_step1(double4_32a* __restrict__ pos, uint4* __restrict__ fi
     if (__any_sync(0xffffffffu, want) && (threadIdx.x & 31) == 0) atomicOr(&flags[0], 1u);
 }
 
+// FP32-force mode: Langevin step one in place at the start of a run, on the
+// 64-bit fixed positions and float-float velocities (fixed64.cuh)
+__global__ void k_md_step1_fx(uint4* __restrict__ fix, uint4* __restrict__ lo, const uint4* __restrict__ fix_build,
+                              VelFF* __restrict__ vel, const double* __restrict__ accel, int* __restrict__ image,
+                              uint32_t N, float dt, float3 s64h, float3 s64l, float3 sfix, float thresh2,
+                              uint32_t* __restrict__ flags)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool want = false;
+    if (i < N) {
+        uint4 f = fix[i];
+        uint4 l = lo[i];
+        VelFF v = vel[i];
+        const float h = 0.5f * dt;
+        const float kx = h * (float)accel[3 * i], ky = h * (float)accel[3 * i + 1], kz = h * (float)accel[3 * i + 2];
+        bool bad = false;
+        const int wx = fx_advance(f.x, l.x, (v.h.x + kx) * dt, s64h.x, s64l.x, bad);
+        const int wy = fx_advance(f.y, l.y, (v.h.y + ky) * dt, s64h.y, s64l.y, bad);
+        const int wz = fx_advance(f.z, l.z, (v.h.z + kz) * dt, s64h.z, s64l.z, bad);
+        if (wx | wy | wz) {
+            image[3 * i] += wx;
+            image[3 * i + 1] += wy;
+            image[3 * i + 2] += wz;
+        }
+        ff_add(v.h.x, v.l.x, kx);
+        ff_add(v.h.y, v.l.y, ky);
+        ff_add(v.h.z, v.l.z, kz);
+        fix[i] = f;
+        lo[i] = l;
+        vel[i] = v;
+        const uint4 fb = fix_build[i];
+        const float dx = (float)(int32_t)(f.x - fb.x) * sfix.x;
+        const float dy = (float)(int32_t)(f.y - fb.y) * sfix.y;
+        const float dz = (float)(int32_t)(f.z - fb.z) * sfix.z;
+        want = dx * dx + dy * dy + dz * dz > thresh2;
+        if (bad) atomicOr(&flags[1], AZP_EBIT_NONFINITE);
+    }
+    if (__any_sync(0xffffffffu, want) && (threadIdx.x & 31) == 0) atomicOr(&flags[0], 1u);
+}
+
+// FP32-force mode: FP64 state (k_load_state's layout) -> fixed words, float-float
+// velocities (vel buffer, in place) and masses
+__global__ void k_state_to_fx(const double4_32a* __restrict__ pos, double4_32a* __restrict__ vel,
+                              uint4* __restrict__ fix, uint4* __restrict__ lo, double* __restrict__ mass, uint32_t N,
+                              double Li0, double Li1, double Li2)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const double4_32a p = pos[i];
+    uint4 h, l;
+    fx_split(fx_from_double(p.x, Li0), h.x, l.x);
+    fx_split(fx_from_double(p.y, Li1), h.y, l.y);
+    fx_split(fx_from_double(p.z, Li2), h.z, l.z);
+    h.w = type_of(p.w);
+    l.w = 0u;
+    fix[i] = h;
+    lo[i] = l;
+    const double4_32a v = vel[i];
+    VelFF f;
+    f.h = make_float4((float)v.x, (float)v.y, (float)v.z, (float)(1.0 / v.w));
+    f.l = make_float4((float)(v.x - (double)f.h.x), (float)(v.y - (double)f.h.y), (float)(v.z - (double)f.h.z), 0.0f);
+    mass[i] = v.w;
+    *reinterpret_cast<VelFF*>(vel + i) = f;
+}
+
+// FP32-force mode: device state -> tag order output (the k_store_state layout)
+__global__ void k_store_state_fx(const uint4* __restrict__ fix, const uint4* __restrict__ lo,
+                                 const VelFF* __restrict__ vel, const double* __restrict__ mass,
+                                 const double* __restrict__ accel, const int* __restrict__ image,
+                                 const uint32_t* __restrict__ tag, uint32_t N, double l0, double l1, double l2,
+                                 double* __restrict__ pos_out, double* __restrict__ vel_out,
+                                 double* __restrict__ accel_out, int* __restrict__ image_out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const uint32_t t = tag[i];
+    if (pos_out) {
+        const uint4 h = fix[i], l = lo[i];
+        pos_out[4 * t] = fx_to_double(fx_join(h.x, l.x), l0);
+        pos_out[4 * t + 1] = fx_to_double(fx_join(h.y, l.y), l1);
+        pos_out[4 * t + 2] = fx_to_double(fx_join(h.z, l.z), l2);
+        pos_out[4 * t + 3] = (double)h.w;
+    }
+    if (vel_out) {
+        const VelFF v = vel[i];
+        vel_out[4 * t] = (double)v.h.x + (double)v.l.x;
+        vel_out[4 * t + 1] = (double)v.h.y + (double)v.l.y;
+        vel_out[4 * t + 2] = (double)v.h.z + (double)v.l.z;
+        vel_out[4 * t + 3] = mass[i];
+    }
+    for (int d = 0; d < 3; ++d) {
+        if (accel_out) accel_out[3 * t + d] = accel[3 * i + d];
+        if (image_out) image_out[3 * t + d] = image[3 * i + d];
+    }
+}
+
 // accelerations a = F / m (HOOMD sets them this way before the first step)
 __global__ void k_accel_from_force(const double4_32a* __restrict__ f, const double4_32a* __restrict__ vel,
-                                   double* __restrict__ accel, uint32_t N)
+                                   const double* __restrict__ mass, double* __restrict__ accel, uint32_t N)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const double4_32a F = f[i];
-    const double minv = 1.0 / vel[i].w;
+    const double minv = 1.0 / (mass ? mass[i] : vel[i].w);
     accel[3 * i] = F.x * minv;
     accel[3 * i + 1] = F.y * minv;
     accel[3 * i + 2] = F.z * minv;
@@ -189,15 +301,24 @@ __global__ void k_accel_from_force(const double4_32a* __restrict__ f, const doub
 // thermo partial sums per block (deterministic two-pass reduction)
 constexpr int THERMO_BLOCK = 256;
 __global__ void k_thermo_partials(const double4_32a* __restrict__ f, const double* __restrict__ vir,
-                                  const double4_32a* __restrict__ vel, uint32_t N, double* __restrict__ part)
+                                  const double4_32a* __restrict__ vel, const double* __restrict__ mass, uint32_t N,
+                                  double* __restrict__ part)
 {
     __shared__ double s[THERMO_BLOCK][8];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (i < N) {
         v[0] = f[i].w;
-        const double4_32a u = vel[i];
-        v[1] = 0.5 * u.w * (u.x * u.x + u.y * u.y + u.z * u.z);
+        if (mass) {
+            // FP32-force mode: float-float velocities
+            const VelFF u = reinterpret_cast<const VelFF*>(vel)[i];
+            const double x = (double)u.h.x + (double)u.l.x, y = (double)u.h.y + (double)u.l.y,
+                         z = (double)u.h.z + (double)u.l.z;
+            v[1] = 0.5 * mass[i] * (x * x + y * y + z * z);
+        } else {
+            const double4_32a u = vel[i];
+            v[1] = 0.5 * u.w * (u.x * u.x + u.y * u.y + u.z * u.z);
+        }
         for (int c = 0; c < 6; ++c) v[2 + c] = vir[(size_t)c * N + i];
     }
     for (int c = 0; c < 8; ++c) s[threadIdx.x][c] = v[c];
@@ -314,6 +435,9 @@ struct azp_md {
     // device state
     double4_32a* pos[2] = {nullptr, nullptr};
     uint4* fix[2] = {nullptr, nullptr};
+    uint4* lo[2] = {nullptr, nullptr};  // FP32-force mode: low fixed words
+    double* mass = nullptr;             // FP32-force mode: masses (vel holds VelFF records)
+    double* t_mass = nullptr;
     int cur = 0;
     uint4* fix_build = nullptr;
     double4_32a* vel = nullptr;
@@ -400,7 +524,7 @@ void free_graphs(azp_md* m)
 void free_all(azp_md* m)
 {
     free_graphs(m);
-    void* ptrs[] = {m->pos[0], m->pos[1], m->fix[0], m->fix[1], m->fix_build, m->vel, m->accel, m->image, m->tag,
+    void* ptrs[] = {m->pos[0], m->pos[1], m->fix[0], m->fix[1], m->lo[0], m->lo[1], m->mass, m->t_mass, m->fix_build, m->vel, m->accel, m->image, m->tag,
                     m->rtag, m->diam, m->t_pos, m->t_vel, m->t_accel, m->t_image, m->t_tag, m->t_diam, m->t_cell,
                     m->cell_of, m->slot, m->cell_count, m->cell_start, m->members, m->scan_tmp, m->counts, m->nbrs,
                     m->cuts, m->bt_n_tag, m->bt_partner_tag, m->bt_type_tag, m->bt_n, m->bt, m->ex_n, m->ex_idx,
@@ -465,6 +589,32 @@ MDArgs base_args(azp_md* m)
     a.next = 0;
     a.out = 0;
     a.tpp = m->tpp;
+    a.tpp_shift = 0;
+    while ((1 << a.tpp_shift) < m->tpp) ++a.tpp_shift;
+    a.flo = m->lo[m->cur];
+    a.flo_next = m->lo[m->cur ^ 1];
+    a.velf = reinterpret_cast<VelFF*>(m->vel);
+    for (int d = 0; d < 3; ++d) {
+        const double s64 = 4294967296.0 / m->box.L[d];
+        a.s64h[d] = (float)s64;
+        a.s64l[d] = (float)(s64 - (double)a.s64h[d]);
+        a.l64[d] = m->box.L[d] * 5.421010862427522e-20;
+    }
+    a.dtf = (float)m->dt;
+    a.kTf = (float)m->kT;
+    a.lambdaf = (float)m->lambda;
+    a.fcapf = (float)m->fcap;
+    a.max_dispf = (float)m->max_disp;
+    a.flowf.kind = m->flow.kind;
+    if (m->flow.kind == AZP_FLOW_PARABOLIC) {
+        a.flowf.a = (float)m->flow.a;
+        a.flowf.b = (float)(1.0 / m->flow.b);
+        a.flowf.c = 0.0f;
+    } else {
+        a.flowf.a = (float)m->flow.a;
+        a.flowf.b = (float)m->flow.b;
+        a.flowf.c = (float)m->flow.c;
+    }
     return a;
 }
 
@@ -476,14 +626,25 @@ int enqueue_rebuild(azp_md* m, cudaStream_t s, const uint32_t* gate)
     const uint32_t nb = blocks_for(N, 256);
     k_zero_gated<<<std::min<uint32_t>(blocks_for(m->grid.ncell, 256), 1024), 256, 0, s>>>(m->cell_count, m->grid.ncell,
                                                                                           gate);
-    launch_cell_assign(m->pos[m->cur], N, m->grid, m->cell_of, m->slot, m->cell_count, s, gate);
+    const bool fx = m->precision == AZP_FP32;
+    if (fx) launch_cell_assign_fx(m->fix[m->cur], N, m->grid, m->cell_of, m->slot, m->cell_count, s, gate);
+    else launch_cell_assign(m->pos[m->cur], N, m->grid, m->cell_of, m->slot, m->cell_count, s, gate);
     int st = exclusive_scan(m->cell_count, m->cell_start, m->grid.ncell, m->scan_tmp, s, gate);
     if (st) return st;
     launch_cell_scatter(m->cell_of, m->slot, m->cell_start, m->members, N, m->grid.ncell, s, gate);
     PermArgs p;
     p.members = m->members;
-    p.pos = m->pos[m->cur];
+    p.pos = fx ? nullptr : m->pos[m->cur];
     p.t_pos = m->t_pos;
+    // FP32-force mode: the next-step buffers serve as temporaries (the step after
+    // the rebuild overwrites them)
+    p.fix = fx ? m->fix[m->cur] : nullptr;
+    p.t_fix = fx ? m->fix[m->cur ^ 1] : nullptr;
+    p.lo = fx ? m->lo[m->cur] : nullptr;
+    p.t_lo = fx ? m->lo[m->cur ^ 1] : nullptr;
+    p.mass = m->mass;
+    p.t_mass = m->t_mass;
+    p.fix_build = m->fix_build;
     p.vel = m->vel;
     p.t_vel = m->t_vel;
     p.accel = m->accel;
@@ -503,14 +664,14 @@ int enqueue_rebuild(azp_md* m, cudaStream_t s, const uint32_t* gate)
     if (m->bond_kind >= 0)
         k_bond_table<<<nb, 256, 0, s>>>(m->tag, m->rtag, m->bt_n_tag, m->bt_partner_tag, m->bt_type_tag, N, m->bt_n,
                                         m->bt, m->ex_n, m->ex_idx, m->exclude_bonds, gate);
-    launch_to_fixed2(m->pos[m->cur], m->fix[m->cur], m->fix_build, N, m->box, s, gate);
+    if (!fx) launch_to_fixed2(m->pos[m->cur], m->fix[m->cur], m->fix_build, N, m->box, s, gate);
     if (m->pair_kind >= 0)
-        launch_nlist_build(m->pos[m->cur], m->fix[m->cur], N, m->box, m->grid, m->cell_start, nullptr, m->cell_of,
-                           m->cuts, m->ntypes, m->ex_n, m->ex_idx, m->bt_width, nullptr, m->counts, m->nbrs,
-                           m->max_nn, m->flags + 3, gate, s);
+        launch_nlist_build(fx ? nullptr : m->pos[m->cur], m->fix[m->cur], N, m->box, m->grid, m->cell_start, nullptr,
+                           m->cell_of, m->cuts, m->ntypes, m->ex_n, m->ex_idx, m->bt_width, nullptr, m->counts, m->nbrs,
+                           m->max_nn, m->flags + 3, gate, s, fx ? m->lo[m->cur] : nullptr);
     k_finish_rebuild<<<1, 1, 0, s>>>(m->flags, gate);
     AZP_CHECK_LAUNCH("enqueue_rebuild");
-    m->launches += 11 + (m->bond_kind >= 0) + (m->pair_kind >= 0);
+    m->launches += 11 + (m->bond_kind >= 0) + (m->pair_kind >= 0) - (fx ? 1 : 0);
     return AZP_OK;
 }
 
@@ -530,6 +691,16 @@ int enqueue_step(azp_md* m, int integ, int next, int out, cudaStream_t s, int se
 int enqueue_step1(azp_md* m, cudaStream_t s)
 {
     const double half = 0.5 * m->r_buff;
+    if (m->precision == AZP_FP32) {
+        const MDArgs a = base_args(m);
+        k_md_step1_fx<<<blocks_for(m->N, 256), 256, 0, s>>>(
+            m->fix[m->cur], m->lo[m->cur], m->fix_build, a.velf, m->accel, m->image, m->N, a.dtf,
+            make_float3(a.s64h[0], a.s64h[1], a.s64h[2]), make_float3(a.s64l[0], a.s64l[1], a.s64l[2]),
+            make_float3(a.sfix[0], a.sfix[1], a.sfix[2]), a.disp_thresh2, m->flags);
+        AZP_CHECK_LAUNCH("k_md_step1_fx");
+        m->launches += 1;
+        return AZP_OK;
+    }
     k_md_step1<<<blocks_for(m->N, 256), 256, 0, s>>>(
         m->pos[m->cur], m->fix[m->cur], m->fix_build, m->vel, m->accel, m->image, m->N, m->dt, m->box.L[0],
         m->box.L[1], m->box.L[2], 1.0 / m->box.L[0], 1.0 / m->box.L[1], 1.0 / m->box.L[2],
@@ -626,6 +797,20 @@ int check_errors(azp_md* m, cudaStream_t s)
     if (f[1] & AZP_EBIT_BOND) return AZP_ERR_BOND;
     if (f[1] & AZP_EBIT_NONFINITE) return AZP_ERR_NONFINITE;
     return AZP_OK;
+}
+
+// device state -> tag-order FP64 arrays (either precision's state layout)
+void enqueue_store_state(azp_md* m, double* pos, double* vel, double* accel, int* image, cudaStream_t s)
+{
+    const uint32_t N = m->N;
+    if (m->precision == AZP_FP32)
+        k_store_state_fx<<<blocks_for(N, 256), 256, 0, s>>>(
+            m->fix[m->cur], m->lo[m->cur], reinterpret_cast<const VelFF*>(m->vel), m->mass, m->accel, m->image, m->tag,
+            N, m->box.L[0] * 5.421010862427522e-20, m->box.L[1] * 5.421010862427522e-20,
+            m->box.L[2] * 5.421010862427522e-20, pos, vel, accel, image);
+    else
+        k_store_state<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[m->cur], m->vel, m->accel, m->image, m->tag, N, pos,
+                                                          vel, accel, image);
 }
 
 int size_list(azp_md* m, cudaStream_t s)
@@ -734,6 +919,12 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     ALLOC(m->fix[0], N);
     ALLOC(m->fix[1], N);
     ALLOC(m->fix_build, N);
+    if (c->precision == AZP_FP32) {
+        ALLOC(m->lo[0], N);
+        ALLOC(m->lo[1], N);
+        ALLOC(m->mass, N);
+        ALLOC(m->t_mass, N);
+    }
     ALLOC(m->vel, N);
     ALLOC(m->accel, (size_t)3 * N);
     ALLOC(m->image, (size_t)3 * N);
@@ -886,6 +1077,11 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
     k_load_state<<<blocks_for(N, 256), 256, 0, s>>>(dp, dv, da, di, dd, N, m->pos[0], m->vel, m->accel, m->image,
                                                      m->diam, m->tag, m->rtag);
     AZP_CHECK_LAUNCH("k_load_state");
+    if (m->precision == AZP_FP32) {
+        k_state_to_fx<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[0], m->vel, m->fix[0], m->lo[0], m->mass, N,
+                                                          1.0 / m->box.L[0], 1.0 / m->box.L[1], 1.0 / m->box.L[2]);
+        AZP_CHECK_LAUNCH("k_state_to_fx");
+    }
     m->timestep = timestep;
     const unsigned long long ts = timestep;
     AZP_CUDA_TRY(cudaMemcpyAsync(m->d_ts, &ts, sizeof(ts), cudaMemcpyHostToDevice, s));
@@ -905,7 +1101,7 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         a.out = 1;
         st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
         if (st) return st;
-        k_accel_from_force<<<blocks_for(N, 256), 256, 0, s>>>(m->out_force, m->vel, m->accel, N);
+        k_accel_from_force<<<blocks_for(N, 256), 256, 0, s>>>(m->out_force, m->vel, m->mass, m->accel, N);
         AZP_CHECK_LAUNCH("k_accel_from_force");
     }
     m->have_state = true;
@@ -926,8 +1122,7 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
     }
     if (N == 0) return AZP_OK;
     if (on_device) {
-        k_store_state<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[m->cur], m->vel, m->accel, m->image, m->tag, N, pos,
-                                                          vel, accel, image);
+        enqueue_store_state(m, pos, vel, accel, image, s);
         AZP_CHECK_LAUNCH("k_store_state");
         return AZP_OK;
     }
@@ -937,8 +1132,7 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
     if (vel) AZP_CUDA_TRY(cudaMalloc(&dv, sizeof(double) * 4 * N));
     if (accel) AZP_CUDA_TRY(cudaMalloc(&da, sizeof(double) * 3 * N));
     if (image) AZP_CUDA_TRY(cudaMalloc(&di, sizeof(int) * 3 * N));
-    k_store_state<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[m->cur], m->vel, m->accel, m->image, m->tag, N, dp, dv,
-                                                      da, di);
+    enqueue_store_state(m, dp, dv, da, di, s);
     AZP_CHECK_LAUNCH("k_store_state");
     if (pos) AZP_CUDA_TRY(cudaMemcpyAsync(pos, dp, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, s));
     if (vel) AZP_CUDA_TRY(cudaMemcpyAsync(vel, dv, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, s));
@@ -1032,7 +1226,7 @@ int azp_md_thermo(azp_md* m, double* out, void* stream)
     st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
     if (st) return st;
     const uint32_t nb = blocks_for(N, THERMO_BLOCK);
-    k_thermo_partials<<<nb, THERMO_BLOCK, 0, s>>>(m->out_force, m->out_virial, m->vel, N, m->partials);
+    k_thermo_partials<<<nb, THERMO_BLOCK, 0, s>>>(m->out_force, m->out_virial, m->vel, m->mass, N, m->partials);
     k_thermo_final<<<1, 32, 0, s>>>(m->partials, nb, m->thermo);
     AZP_CHECK_LAUNCH("azp_md_thermo");
     double h[8];
@@ -1076,8 +1270,7 @@ int azp_md_run_checked(azp_md* m, uint64_t steps, void* stream)
     }
     unsigned long long ts0 = 0;
     AZP_CUDA_TRY(cudaMemcpyAsync(&ts0, m->d_ts, sizeof(ts0), cudaMemcpyDeviceToHost, s));
-    k_store_state<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[m->cur], m->vel, m->accel, m->image, m->tag, N,
-                                                      m->snap_pos, m->snap_vel, m->snap_acc, m->snap_img);
+    enqueue_store_state(m, m->snap_pos, m->snap_vel, m->snap_acc, m->snap_img, s);
     if (m->diam) k_to_tag_order_n<<<blocks_for(N, 256), 256, 0, s>>>(m->diam, m->tag, N, 1, 0, m->snap_diam);
     AZP_CHECK_LAUNCH("k_store_state (snapshot)");
     AZP_CUDA_TRY(cudaStreamSynchronize(s));

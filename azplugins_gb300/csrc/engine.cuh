@@ -2,6 +2,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "fixed64.cuh"
 #include "integrate.cuh"
 
 namespace azp
@@ -57,6 +58,15 @@ struct MDArgs {
     int next;                   // Langevin: also do step one of the next timestep
     int out;                    // write out_force / out_virial
     int tpp;                    // threads per particle (1, 2, 4, 8, 16, 32)
+    int tpp_shift;              // log2(tpp)
+    // FP32-force state (fixed64.cuh): fix holds the high words, these the rest
+    const uint4* flo;           // low words of the 64-bit fixed positions (x, y, z)
+    uint4* flo_next;
+    VelFF* velf;                // float-float velocities and 1/m (in the vel buffer)
+    float s64h[3], s64l[3];     // 2^32 / L as a float pair
+    double l64[3];              // L * 2^-64 (exact cutoff decisions near r_cut)
+    float dtf, kTf, lambdaf, fcapf, max_dispf;
+    FlowF flowf;
 };
 
 constexpr int MD_INTEG_LANGEVIN = 0;

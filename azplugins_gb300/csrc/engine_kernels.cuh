@@ -120,27 +120,12 @@ AZP_D bool displaced(const uint4& f, const uint4& fb, const float* sfix, float t
     return dx * dx + dy * dy + dz * dz > thresh2;
 }
 
-// Wrap one coordinate into [lo, hi) and return its 32-bit fixed-point value.
-// The fixed value x * (2^32 / L) decides without FP64 compares whether the
-// particle can be near a face; only then is the exact FP64 wrap test done.
-AZP_D uint32_t wrap_fixed(double& x, int* img, double fscale, double L, double lo, double hi)
-{
-    long long q = __double2ll_rn(x * fscale);
-    if (q >= 2146435072ll || q < -2146435072ll) {  // within 2^20 units of a face
-        int w = 0;
-        wrap1(x, w, L, lo, hi);
-        if (w) {
-            *img += w;
-            q = __double2ll_rn(x * fscale);
-        }
-    }
-    return (uint32_t)(int32_t)q;
-}
-
-
+// FP64 step: FP64 positions, forces and integration, the oracle's rounding for
+// every decision.
 template<class PE, class BE, typename R, int INTEG>
 __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
 {
+    static_assert(std::is_same<R, double>::value, "k_md_step is the FP64 step; FP32 forces use k_md_step_fx");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t nt2 = a.ntypes * a.ntypes;
     double* s_rc2 = reinterpret_cast<double*>(smem_raw);
@@ -174,7 +159,7 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
         // ---------------------------------------------------------------- pair
         if constexpr (!std::is_same<PE, NoPair>::value) {
             const uint32_t n = min(a.counts[i], a.max_nn);
-            if constexpr (std::is_same<R, double>::value) {
+            {
                 const double4_32a pi = a.pos[i];
                 const uint32_t ti = type_of(pi.w);
                 for (uint32_t k = sub; k < n; k += tpp) {
@@ -196,37 +181,6 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
                         fdr = (R)copysign(a.fcap / sqrt((double)rsq), (double)fdr);
                     acc.add(dx, dy, dz, fdr, e, vir);
                 }
-            } else {
-                const uint4 fi = a.fix[i];
-                const uint32_t ti = fi.w;
-                for (uint32_t k = sub; k < n; k += tpp) {
-                    const uint32_t j = a.nbrs[(size_t)k * a.N + i];
-                    const uint4 fj = a.fix[j];
-                    const float dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
-                    const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
-                    const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
-                    const float rsq = dx * dx + dy * dy + dz * dz;
-                    const uint32_t tp = ti * a.ntypes + fj.w;
-                    const R* rec = s_rec + (size_t)tp * PAIR_TBL;
-                    const R* cut = rec + PAIR_REC;
-                    const float rc2 = cut[0];
-                    if (rsq >= rc2 * 1.000004f || !PE::enabled(rec)) continue;
-                    if (rsq >= rc2 * 0.999996f) {
-                        const double4_32a pi = a.pos[i];
-                        const double4_32a pj = a.pos[j];
-                        const double vx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
-                        const double vy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
-                        const double vz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
-                        if (!(rsq_exact(vx, vy, vz) < s_rc2[tp])) continue;
-                    }
-                    R fdr, e;
-                    PE::eval(rec, rsq, fdr, e);
-                    e -= rec[PE::SHIFT_SLOT];
-                    xplor(cut, rsq, fdr, e);
-                    if (a.fcap > 0.0 && (double)fdr * fdr * rsq > a.fcap * a.fcap)
-                        fdr = (R)copysign(a.fcap / sqrt((double)rsq), (double)fdr);
-                    acc.add(dx, dy, dz, fdr, e, vir);
-                }
             }
         }
         // ---------------------------------------------------------------- bonds
@@ -234,23 +188,13 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
             const uint32_t nb = a.bt_n[i];
             for (uint32_t k = sub; k < nb; k += tpp) {
                 const uint2 e2 = a.bt[(size_t)k * a.N + i];
-                R dx, dy, dz, rsq;
-                if constexpr (std::is_same<R, double>::value) {
-                    const double4_32a pi = a.pos[i];
-                    const double4_32a pj = a.pos[e2.x];
-                    dx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
-                    dy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
-                    dz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
-                    rsq = rsq_exact(dx, dy, dz);
-                } else {
-                    const uint4 fi = a.fix[i];
-                    const uint4 fj = a.fix[e2.x];
-                    dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
-                    dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
-                    dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
-                    rsq = dx * dx + dy * dy + dz * dz;
-                }
-                R fdr, en;
+                const double4_32a pi = a.pos[i];
+                const double4_32a pj = a.pos[e2.x];
+                const double dx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
+                const double dy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
+                const double dz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
+                const double rsq = rsq_exact(dx, dy, dz);
+                double fdr, en;
                 if (!BE::eval(s_bond + e2.y * AZP_BOND_PARAM_DOUBLES, rsq, fdr, en)) {
                     atomicOr(&a.flags[1], AZP_EBIT_BOND);
                     continue;
@@ -274,7 +218,7 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
             const uint32_t ti = type_of(p.w);
             const uint32_t tg = a.tag[i];
             bool moved = false;
-            if constexpr (std::is_same<R, double>::value) {
+            {
                 // FP64 path: the reference arithmetic throughout; the per-type noise
                 // amplitude sqrt(6 gamma kT / dt) comes from a host table built with
                 // the same double operations, so the draws stay bit-exact
@@ -344,79 +288,6 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
                     want_rebuild = displaced(f, a.fix_build[i], a.sfix, a.disp_thresh2);
                     if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(&a.flags[1], AZP_EBIT_NONFINITE);
                 }
-            } else {
-                // FP32-force path. GB300 issues FP64 at a small fraction of its FP32
-                // rate, so the increments (drag, noise, kicks, displacements) are
-                // formed in FP32 -- as accurate as the FP32 forces they come from --
-                // and only the accumulations v += dv, x += dx are FP64.
-                const float fx = acc.fx.s + acc.fx.c, fy = acc.fy.s + acc.fy.c, fz = acc.fz.s + acc.fz.c;
-                const float gam = a.use_lambda ? (float)(a.lambda * a.diameter[i]) : (float)s_gamma[ti];
-                const float c = a.noiseless ? 0.0f
-                                            : (a.use_lambda ? sqrtf(6.0f * gam * (float)a.kT / (float)a.dt)
-                                                            : (float)s_noise[ti]);
-                float ux, uy, uz;
-                flow_at_f(a.flow, (float)p.y, ux, uy, uz);
-                const float dt = (float)a.dt;
-                float r0, r1, r2;
-                double ddx, ddy, ddz;
-                if constexpr (INTEG == MD_INTEG_LANGEVIN) {
-                    uniform3f(AZP_RNG_LANGEVIN_FLOW, ts, a.seed, tg, -c, 2.0f * c, r0, r1, r2);
-                    double4_32a v = a.vel[i];
-                    const float minv = __frcp_rn((float)v.w);
-                    const float ax = (fx + (r0 - gam * ((float)v.x - ux))) * minv;
-                    const float ay = (fy + (r1 - gam * ((float)v.y - uy))) * minv;
-                    const float az = (fz + (r2 - gam * ((float)v.z - uz))) * minv;
-                    if (a.next) {
-                        // v(t+dt/2) = v + dt a: the half kick of step two and of step one
-                        const float kx = dt * ax, ky = dt * ay, kz = dt * az;
-                        ddx = (double)(((float)v.x + kx) * dt);
-                        ddy = (double)(((float)v.y + ky) * dt);
-                        ddz = (double)(((float)v.z + kz) * dt);
-                        v.x += (double)kx;
-                        v.y += (double)ky;
-                        v.z += (double)kz;
-                        moved = true;
-                    } else {
-                        const float h = 0.5f * dt;
-                        v.x += (double)(h * ax);
-                        v.y += (double)(h * ay);
-                        v.z += (double)(h * az);
-                        a.accel[3 * i] = ax;
-                        a.accel[3 * i + 1] = ay;
-                        a.accel[3 * i + 2] = az;
-                    }
-                    a.vel[i] = v;
-                } else {
-                    uniform3f(AZP_RNG_BROWNIAN_FLOW, ts, a.seed, tg, -c, 2.0f * c, r0, r1, r2);
-                    const float gi = 1.0f / gam;
-                    float dx = (ux + (fx + r0) * gi) * dt;
-                    float dy = (uy + (fy + r1) * gi) * dt;
-                    float dz = (uz + (fz + r2) * gi) * dt;
-                    if (a.max_disp > 0.0) {
-                        const float m = (float)a.max_disp;
-                        dx = fminf(fmaxf(dx, -m), m);
-                        dy = fminf(fmaxf(dy, -m), m);
-                        dz = fminf(fmaxf(dz, -m), m);
-                    }
-                    ddx = dx;
-                    ddy = dy;
-                    ddz = dz;
-                    moved = true;
-                }
-                if (moved) {
-                    p.x += ddx;
-                    p.y += ddy;
-                    p.z += ddz;
-                    uint4 f;
-                    f.x = wrap_fixed(p.x, a.image + 3 * i, a.fscale[0], a.L[0], a.lo[0], a.hi[0]);
-                    f.y = wrap_fixed(p.y, a.image + 3 * i + 1, a.fscale[1], a.L[1], a.lo[1], a.hi[1]);
-                    f.z = wrap_fixed(p.z, a.image + 3 * i + 2, a.fscale[2], a.L[2], a.lo[2], a.hi[2]);
-                    f.w = ti;
-                    a.pos_next[i] = p;
-                    a.fix_next[i] = f;
-                    want_rebuild = displaced(f, a.fix_build[i], a.sfix, a.disp_thresh2);
-                    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(&a.flags[1], AZP_EBIT_NONFINITE);
-                }
             }
         }
     }
@@ -438,6 +309,239 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
     }
 }
 
+// ---------------------------------------------------------------- FP32-force step
+// State: 64-bit fixed positions (fix = high words, lo = low words) and
+// float-float velocities (fixed64.cuh). Pair and bond arithmetic in FP32 on the
+// exact integer displacement of the high words, compensated force / energy sums;
+// the r_cut decision is the oracle's FP64 one within 4e-6 of r_cut^2, on the
+// full 64-bit positions. Integration with FP32 increments accumulated exactly
+// (positions) or in float-float (velocities): no FP64 instruction per particle.
+
+// |x_i - x_j|^2 < rc2 exactly as the FP64 oracle decides it, on the 64-bit positions
+AZP_D bool inside_exact(const MDArgs& a, uint32_t i, uint32_t j, double rc2)
+{
+    const uint4 hi = a.fix[i], hj = a.fix[j];
+    const uint4 li = a.flo[i], lj = a.flo[j];
+    const double vx = min_image1(fx_to_double(fx_join(hi.x, li.x), a.l64[0]) - fx_to_double(fx_join(hj.x, lj.x), a.l64[0]),
+                                 a.L[0], a.Linv[0]);
+    const double vy = min_image1(fx_to_double(fx_join(hi.y, li.y), a.l64[1]) - fx_to_double(fx_join(hj.y, lj.y), a.l64[1]),
+                                 a.L[1], a.Linv[1]);
+    const double vz = min_image1(fx_to_double(fx_join(hi.z, li.z), a.l64[2]) - fx_to_double(fx_join(hj.z, lj.z), a.l64[2]),
+                                 a.L[2], a.Linv[2]);
+    return rsq_exact(vx, vy, vz) < rc2;
+}
+
+template<class PE>
+AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j,
+                        const float* s_rec, const double* s_rc2, Acc<float>& acc, bool vir)
+{
+    const float dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
+    const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
+    const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
+    const float rsq = dx * dx + dy * dy + dz * dz;
+    const uint32_t tp = fi.w * a.ntypes + fj.w;
+    const float* rec = s_rec + (size_t)tp * PAIR_TBL;
+    const float* cut = rec + PAIR_REC;
+    const float rc2 = cut[0];
+    if (rsq >= rc2 * 1.000004f || !PE::enabled(rec)) return;
+    if (rsq >= rc2 * 0.999996f && !inside_exact(a, i, j, s_rc2[tp])) return;
+    float fdr, e;
+    PE::eval(rec, rsq, fdr, e);
+    e -= rec[PE::SHIFT_SLOT];
+    xplor(cut, rsq, fdr, e);
+    if (a.fcapf > 0.0f && fdr * fdr * rsq > a.fcapf * a.fcapf) fdr = copysignf(a.fcapf * rsqrtf(rsq), fdr);
+    acc.add(dx, dy, dz, fdr, e, vir);
+}
+
+template<class BE>
+AZP_D void bond_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t btype, const float* s_bond,
+                        Acc<float>& acc, bool vir)
+{
+    const float dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
+    const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
+    const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
+    const float rsq = dx * dx + dy * dy + dz * dz;
+    float fdr, en;
+    if (!BE::eval(s_bond + btype * AZP_BOND_PARAM_DOUBLES, rsq, fdr, en)) {
+        atomicOr(&a.flags[1], AZP_EBIT_BOND);
+        return;
+    }
+    acc.add(dx, dy, dz, fdr, en, vir);
+}
+
+// the last block to finish advances the timestep and arms the next rebuild
+AZP_D void finish_step(const MDArgs& a, bool want_rebuild)
+{
+    if (__any_sync(0xffffffffu, want_rebuild) && (threadIdx.x & 31) == 0) atomicOr(&a.flags[0], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const uint32_t t = atomicAdd(&a.flags[4], 1u);
+        if (t == gridDim.x - 1) {
+            __threadfence();
+            const uint32_t req = atomicAdd(&a.flags[0], 0u) && !atomicAdd(&a.flags[1], 0u);
+            if (a.set_cond) cudaGraphSetConditional(a.next_cond, req ? 1u : 0u);
+            a.flags[4] = 0u;
+            *a.d_timestep_rw = *a.d_timestep_rw + 1ull;
+        }
+    }
+}
+
+// neighbours gathered per batch: the list indices of a batch are loaded first,
+// then their positions, so each thread keeps this many gathers in flight
+constexpr int FX_BATCH = 4;
+
+template<class PE, class BE, int INTEG>
+__global__ void __launch_bounds__(MD_BLOCK, 4) k_md_step_fx(MDArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const uint32_t nt2 = a.ntypes * a.ntypes;
+    double* s_rc2 = reinterpret_cast<double*>(smem_raw);
+    float* s_rec = reinterpret_cast<float*>(s_rc2 + nt2);
+    float* s_bond = s_rec + nt2 * PAIR_TBL;
+    float* s_gamma = s_bond + a.nbondtypes * AZP_BOND_PARAM_DOUBLES;
+    float* s_noise = s_gamma + a.ntypes;
+    if (!std::is_same<PE, NoPair>::value)
+        for (uint32_t t = threadIdx.x; t < nt2 * PAIR_TBL; t += blockDim.x) {
+            s_rec[t] = (float)a.pair_table[t];
+            if (t % PAIR_TBL == PAIR_REC) s_rc2[t / PAIR_TBL] = a.pair_table[t];
+        }
+    if (!std::is_same<BE, NoBond>::value)
+        for (uint32_t t = threadIdx.x; t < a.nbondtypes * AZP_BOND_PARAM_DOUBLES; t += blockDim.x)
+            s_bond[t] = (float)a.bond_params[t];
+    if (INTEG != MD_FORCES_ONLY && !a.use_lambda)
+        for (uint32_t t = threadIdx.x; t < a.ntypes; t += blockDim.x) {
+            s_gamma[t] = (float)a.gamma[t];
+            s_noise[t] = (float)a.noise[t];
+        }
+    __syncthreads();
+
+    const uint32_t tpp = (uint32_t)a.tpp;
+    const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = gid >> a.tpp_shift;
+    const uint32_t sub = gid & (tpp - 1u);
+    const bool active = i < a.N;
+    const bool vir = a.out != 0;
+    Acc<float> acc;
+    uint4 fi = make_uint4(0u, 0u, 0u, 0u);
+    if (active) {
+        fi = __ldg(a.fix + i);
+        // ---------------------------------------------------------------- pair
+        if constexpr (!std::is_same<PE, NoPair>::value) {
+            const uint32_t n = min(__ldg(a.counts + i), a.max_nn);
+            const uint32_t* col = a.nbrs + i;
+            for (uint32_t k0 = sub; k0 < n; k0 += FX_BATCH * tpp) {
+                uint32_t jj[FX_BATCH];
+                uint4 fj[FX_BATCH];
+#pragma unroll
+                for (int u = 0; u < FX_BATCH; ++u) {
+                    const uint32_t k = k0 + u * tpp;
+                    jj[u] = k < n ? __ldg(col + (size_t)k * a.N) : i;
+                }
+#pragma unroll
+                for (int u = 0; u < FX_BATCH; ++u) fj[u] = __ldg(a.fix + jj[u]);
+#pragma unroll
+                for (int u = 0; u < FX_BATCH; ++u)
+                    if (k0 + u * tpp < n) pair_term_fx<PE>(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir);
+            }
+        }
+        // ---------------------------------------------------------------- bonds
+        if constexpr (!std::is_same<BE, NoBond>::value) {
+            const uint32_t nb = __ldg(a.bt_n + i);
+            for (uint32_t k0 = sub; k0 < nb; k0 += 2u * tpp) {
+                const uint32_t k1 = k0 + tpp;
+                const uint2 e0 = __ldg(a.bt + (size_t)k0 * a.N + i);
+                const uint2 e1 = k1 < nb ? __ldg(a.bt + (size_t)k1 * a.N + i) : make_uint2(i, 0u);
+                const uint4 f0 = __ldg(a.fix + e0.x);
+                const uint4 f1 = __ldg(a.fix + e1.x);
+                bond_term_fx<BE>(a, fi, f0, e0.y, s_bond, acc, vir);
+                if (k1 < nb) bond_term_fx<BE>(a, fi, f1, e1.y, s_bond, acc, vir);
+            }
+        }
+    }
+    if (tpp > 1) acc.reduce((int)tpp, vir);
+
+    bool want_rebuild = false;
+    if (active && sub == 0) {
+        if (a.out) {
+            a.out_force[i] = make_double4_32a(acc.Fx(), acc.Fy(), acc.Fz(), acc.U());
+            for (int c = 0; c < 6; ++c) a.out_virial[(size_t)c * a.N + i] = (double)acc.w[c];
+        }
+        if constexpr (INTEG != MD_FORCES_ONLY) {
+            const unsigned long long ts = *a.d_timestep;
+            const uint32_t ti = fi.w;
+            const uint32_t tg = __ldg(a.tag + i);
+            const float fx = acc.fx.s + acc.fx.c, fy = acc.fy.s + acc.fy.c, fz = acc.fz.s + acc.fz.c;
+            const float gam = a.use_lambda ? a.lambdaf * (float)a.diameter[i] : s_gamma[ti];
+            const float c = a.noiseless ? 0.0f : (a.use_lambda ? sqrtf(6.0f * gam * a.kTf / a.dtf) : s_noise[ti]);
+            float ux, uy, uz;
+            flow_at_ff(a.flowf, (float)(int32_t)fi.y * a.sfix[1], ux, uy, uz);
+            const float dt = a.dtf;
+            float r0, r1, r2, ddx = 0.0f, ddy = 0.0f, ddz = 0.0f;
+            bool moved = false;
+            if constexpr (INTEG == MD_INTEG_LANGEVIN) {
+                uniform3f(AZP_RNG_LANGEVIN_FLOW, ts, a.seed, tg, -c, 2.0f * c, r0, r1, r2);
+                VelFF v = a.velf[i];
+                const float minv = v.h.w;
+                const float ax = (fx + (r0 - gam * (v.h.x - ux))) * minv;
+                const float ay = (fy + (r1 - gam * (v.h.y - uy))) * minv;
+                const float az = (fz + (r2 - gam * (v.h.z - uz))) * minv;
+                if (a.next) {
+                    // v(t + dt/2) = v(t - dt/2) + dt a: the half kick of step two and of
+                    // step one; then x += v(t + dt/2) dt
+                    const float kx = dt * ax, ky = dt * ay, kz = dt * az;
+                    ddx = (v.h.x + kx) * dt;
+                    ddy = (v.h.y + ky) * dt;
+                    ddz = (v.h.z + kz) * dt;
+                    ff_add(v.h.x, v.l.x, kx);
+                    ff_add(v.h.y, v.l.y, ky);
+                    ff_add(v.h.z, v.l.z, kz);
+                    moved = true;
+                } else {
+                    const float h = 0.5f * dt;
+                    ff_add(v.h.x, v.l.x, h * ax);
+                    ff_add(v.h.y, v.l.y, h * ay);
+                    ff_add(v.h.z, v.l.z, h * az);
+                    a.accel[3 * i] = ax;
+                    a.accel[3 * i + 1] = ay;
+                    a.accel[3 * i + 2] = az;
+                }
+                a.velf[i] = v;
+            } else {
+                uniform3f(AZP_RNG_BROWNIAN_FLOW, ts, a.seed, tg, -c, 2.0f * c, r0, r1, r2);
+                const float gi = 1.0f / gam;
+                ddx = (ux + (fx + r0) * gi) * dt;
+                ddy = (uy + (fy + r1) * gi) * dt;
+                ddz = (uz + (fz + r2) * gi) * dt;
+                if (a.max_dispf > 0.0f) {
+                    const float m = a.max_dispf;
+                    ddx = fminf(fmaxf(ddx, -m), m);
+                    ddy = fminf(fmaxf(ddy, -m), m);
+                    ddz = fminf(fmaxf(ddz, -m), m);
+                }
+                moved = true;
+            }
+            if (moved) {
+                uint4 lo = a.flo[i];
+                bool bad = false;
+                const int wx = fx_advance(fi.x, lo.x, ddx, a.s64h[0], a.s64l[0], bad);
+                const int wy = fx_advance(fi.y, lo.y, ddy, a.s64h[1], a.s64l[1], bad);
+                const int wz = fx_advance(fi.z, lo.z, ddz, a.s64h[2], a.s64l[2], bad);
+                if (wx | wy | wz) {
+                    a.image[3 * i] += wx;
+                    a.image[3 * i + 1] += wy;
+                    a.image[3 * i + 2] += wz;
+                }
+                a.fix_next[i] = fi;
+                a.flo_next[i] = lo;
+                want_rebuild = displaced(fi, a.fix_build[i], a.sfix, a.disp_thresh2);
+                if (bad) atomicOr(&a.flags[1], AZP_EBIT_NONFINITE);
+            }
+        }
+    }
+    if constexpr (INTEG != MD_FORCES_ONLY) finish_step(a, want_rebuild);
+}
+
 template<class PE, class BE, typename R, int INTEG>
 int launch_md_t(const MDArgs& a, cudaStream_t s)
 {
@@ -445,12 +549,21 @@ int launch_md_t(const MDArgs& a, cudaStream_t s)
     const uint32_t blocks = (uint32_t)((threads + MD_BLOCK - 1) / MD_BLOCK);
     if (blocks == 0) return AZP_OK;
     const size_t nt2 = (size_t)a.ntypes * a.ntypes;
-    const size_t smem = nt2 * sizeof(double) + 2 * a.ntypes * sizeof(double) + nt2 * PAIR_TBL * sizeof(R) +
-                        (size_t)a.nbondtypes * AZP_BOND_PARAM_DOUBLES * sizeof(R);
-    auto k = k_md_step<PE, BE, R, INTEG>;
-    if (smem > 48 * 1024) AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<blocks, MD_BLOCK, smem, s>>>(a);
-    AZP_CHECK_LAUNCH("k_md_step");
+    if constexpr (std::is_same<R, float>::value) {
+        const size_t smem = nt2 * sizeof(double) + nt2 * PAIR_TBL * sizeof(float) +
+                            (size_t)a.nbondtypes * AZP_BOND_PARAM_DOUBLES * sizeof(float) + 2 * a.ntypes * sizeof(float);
+        auto k = k_md_step_fx<PE, BE, INTEG>;
+        if (smem > 48 * 1024) AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<blocks, MD_BLOCK, smem, s>>>(a);
+        AZP_CHECK_LAUNCH("k_md_step_fx");
+    } else {
+        const size_t smem = nt2 * sizeof(double) + 2 * a.ntypes * sizeof(double) + nt2 * PAIR_TBL * sizeof(R) +
+                            (size_t)a.nbondtypes * AZP_BOND_PARAM_DOUBLES * sizeof(R);
+        auto k = k_md_step<PE, BE, R, INTEG>;
+        if (smem > 48 * 1024) AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<blocks, MD_BLOCK, smem, s>>>(a);
+        AZP_CHECK_LAUNCH("k_md_step");
+    }
     return AZP_OK;
 }
 

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "celllist.cuh"
+#include "fixed64.cuh"
 #include "nlist_impl.cuh"
 #include "scan.cuh"
 
@@ -150,6 +151,7 @@ __global__ void k_cell_sort(const uint32_t* __restrict__ cell_start, uint32_t* _
 
 struct BoxArgs {
     double L[3], Linv[3];
+    double l64[3];  // L * 2^-64 (64-bit fixed-point unit)
     float sfix[3];  // L * 2^-32 (fixed-point unit)
 };
 
@@ -159,9 +161,37 @@ inline BoxArgs box_args(const azp_box& b)
     for (int d = 0; d < 3; ++d) {
         a.L[d] = b.L[d];
         a.Linv[d] = 1.0 / b.L[d];
+        a.l64[d] = b.L[d] * 5.421010862427522e-20;
         a.sfix[d] = (float)(b.L[d] * 2.3283064365386963e-10);
     }
     return a;
+}
+
+// FP64 position of particle i from its 64-bit fixed-point words (fixed64.cuh)
+__device__ __forceinline__ double4_32a fx_position(const uint4* __restrict__ hi, const uint4* __restrict__ lo,
+                                                   uint32_t i, const BoxArgs& bx)
+{
+    const uint4 h = hi[i], l = lo[i];
+    return make_double4_32a(fx_to_double(fx_join(h.x, l.x), bx.l64[0]), fx_to_double(fx_join(h.y, l.y), bx.l64[1]),
+                            fx_to_double(fx_join(h.z, l.z), bx.l64[2]), 0.0);
+}
+
+// cell of each particle from the high words of its 64-bit fixed position:
+// [-2^31, 2^31) maps linearly onto [0, dim) in integer arithmetic
+__global__ void k_cell_assign_fx(const uint4* __restrict__ fixed, uint32_t N, CellGrid g,
+                                 uint32_t* __restrict__ cell_of, uint32_t* __restrict__ slot,
+                                 uint32_t* __restrict__ cell_count, const uint32_t* __restrict__ gate)
+{
+    if (gated_off(gate)) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const uint4 f = fixed[i];
+    const uint32_t cx = (uint32_t)(((uint64_t)(f.x ^ 0x80000000u) * (uint32_t)g.dim[0]) >> 32);
+    const uint32_t cy = (uint32_t)(((uint64_t)(f.y ^ 0x80000000u) * (uint32_t)g.dim[1]) >> 32);
+    const uint32_t cz = (uint32_t)(((uint64_t)(f.z ^ 0x80000000u) * (uint32_t)g.dim[2]) >> 32);
+    const uint32_t c = (cz * (uint32_t)g.dim[1] + cy) * (uint32_t)g.dim[0] + cx;
+    cell_of[i] = c;
+    slot[i] = atomicAdd(&cell_count[c], 1u);
 }
 
 constexpr int NLIST_BLOCK = 128;
@@ -173,7 +203,8 @@ __global__ void __launch_bounds__(NLIST_BLOCK)
                   const uint32_t* __restrict__ cell_of, const ListCut* __restrict__ cuts, uint32_t ntypes,
                   const uint32_t* __restrict__ ex_n, const uint32_t* __restrict__ ex_keys, uint32_t ex_width,
                   const uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, uint32_t* __restrict__ nbrs,
-                  uint32_t max_nn, uint32_t* __restrict__ flags, const uint32_t* __restrict__ gate)
+                  uint32_t max_nn, uint32_t* __restrict__ flags, const uint32_t* __restrict__ gate,
+                  const uint4* __restrict__ lo)
 {
     if (gated_off(gate)) return;
     __shared__ ListCut s_cut[MAX_LIST_TYPES * MAX_LIST_TYPES];
@@ -220,10 +251,10 @@ __global__ void __launch_bounds__(NLIST_BLOCK)
                     if (!(rs < cut.lo)) {
                         // ambiguous band: the oracle's exact FP64 decision
                         if (!have_pi) {
-                            pi = pos[i];
+                            pi = lo ? fx_position(fixed, lo, i, bx) : pos[i];
                             have_pi = true;
                         }
-                        const double4_32a pj = pos[j];
+                        const double4_32a pj = lo ? fx_position(fixed, lo, j, bx) : pos[j];
                         const double vx = min_image1(pi.x - pj.x, bx.L[0], bx.Linv[0]);
                         const double vy = min_image1(pi.y - pj.y, bx.L[1], bx.Linv[1]);
                         const double vz = min_image1(pi.z - pj.z, bx.L[2], bx.Linv[2]);
@@ -295,12 +326,19 @@ void launch_nlist_build(const double4_32a* pos, const uint4* fixed, uint32_t N, 
                         const uint32_t* cell_start, const uint32_t* members, const uint32_t* cell_of,
                         const ListCut* cuts, uint32_t ntypes, const uint32_t* ex_n, const uint32_t* ex_keys,
                         uint32_t ex_width, const uint32_t* keys, uint32_t* counts, uint32_t* nbrs,
-                        uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s)
+                        uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s, const uint4* lo)
 {
     if (N == 0) return;
     k_nlist_build<<<(N + NLIST_BLOCK - 1) / NLIST_BLOCK, NLIST_BLOCK, 0, s>>>(
         pos, fixed, N, box_args(box), g, cell_start, members, cell_of, cuts, ntypes, ex_n, ex_keys, ex_width, keys,
-        counts, nbrs, max_nn, flags, gate);
+        counts, nbrs, max_nn, flags, gate, lo);
+}
+
+void launch_cell_assign_fx(const uint4* fixed, uint32_t N, const CellGrid& g, uint32_t* cell_of, uint32_t* slot,
+                           uint32_t* cell_count, cudaStream_t s, const uint32_t* gate)
+{
+    if (N == 0) return;
+    k_cell_assign_fx<<<(N + 255) / 256, 256, 0, s>>>(fixed, N, g, cell_of, slot, cell_count, gate);
 }
 
 }  // namespace azp

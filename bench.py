@@ -195,10 +195,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def algorithmic_bytes(n_nbr_mean, n_bond_mean):
-    """Bytes per particle of one fused step launch (FP32 forces, FP64 state):
-    reads fixed_i 16, count 4, list 4 n, bond count 4 + table 8 n_b, pos 32,
+def algorithmic_bytes(n_nbr_mean, n_bond_mean, precision="fp32"):
+    """Bytes per particle of one fused step launch.
+
+    FP32 forces (64-bit fixed positions, float-pair velocities): reads high
+    words 16, low words 16, count 4, list 4 n, bond count 4 + table 8 n_b,
+    velocity record 32, tag 4, build shadow 16; writes high words 16, low words
+    16, velocity record 32.
+    FP64: reads fixed_i 16, count 4, list 4 n, bond count 4 + table 8 n_b, pos 32,
     vel 32, tag 4, build shadow 16; writes pos_next 32, vel 32, fixed_next 16."""
+    if precision == "fp32":
+        return 16 + 16 + 4 + 4 * n_nbr_mean + 4 + 8 * n_bond_mean + 32 + 4 + 16 + 16 + 16 + 32
     return 16 + 4 + 4 * n_nbr_mean + 4 + 8 * n_bond_mean + 32 + 32 + 4 + 16 + 32 + 32 + 16
 
 
@@ -361,7 +368,7 @@ def run_ours(args):
     # dominant kernel alone (last: it advances the state without list checks)
     kernel_ms = time_step_kernel(eng, reps=200)
     log("kernel timing done")
-    bytes_per_launch = algorithmic_bytes(n_nbr, n_bond) * N
+    bytes_per_launch = algorithmic_bytes(n_nbr, n_bond, args.precision) * N
     peak, peak_kind = measured_peak()
     achieved = bytes_per_launch / (kernel_ms * 1e-3) / 1e9
 
@@ -382,7 +389,7 @@ def run_ours(args):
             "nlist_builds_per_step": builds / args.steps,
             "pair_interactions_per_s": None,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": "k_md_step (fused forces + Langevin step)",
+                         "traffic": None, "kernel": ("k_md_step_fx" if args.precision == "fp32" else "k_md_step") + " (fused forces + Langevin step)",
                          "kernel_ms": kernel_ms, "bytes_per_launch": bytes_per_launch,
                          "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "mean_neighbours": n_nbr,
                          "mean_bonds": n_bond},

@@ -172,3 +172,148 @@ def test_brownian_colloid_like(orc):
     out = sim.state.get_snapshot().particles
     assert _pos_err(out.position, md.s["pos4"][:, :3], box_of(snap)) < 1e-10
     assert np.array_equal(out.image, md.s["image"])
+
+
+# ---------------------------------------------------------------- FP32-force engine state
+# FP32-force mode keeps positions as 64-bit fixed point and velocities as float
+# pairs (csrc/fixed64.cuh). These tests pin that state: round trips, graph
+# equivalence, wrapping and images, and trajectories against the FP64 oracle.
+
+
+def _unwrapped(p, L):
+    return p.position + p.image * L
+
+
+def _relaxed_melt(n_chains=30, length=20, density=0.6, seed=25):
+    from azplugins_gb300 import workloads
+
+    snap = workloads.bead_spring_melt(n_chains, length, density=density, seed=seed)
+    sim = az.Simulation(seed=9)
+    sim.create_state_from_snapshot(snap)
+    wca = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), default_r_cut=2 ** (1 / 6))
+    wca.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.0)
+    qb = az.bond.Quartic()
+    qb.params["A-A"] = dict(k=1434.3, r_0=1.5, b_1=-0.7589, b_2=0.0, U_0=67.2234, sigma=1.0, epsilon=1.0)
+    relax = az.methods.BrownianFlow("all", kT=1.0, flow_field=az.flow.ConstantFlow((0, 0, 0)), max_displacement=0.02)
+    sim.operations.integrator = az.md.Integrator(dt=0.001, methods=[relax], forces=[wca, qb])
+    sim.run(200)
+    relaxed = sim.state.get_snapshot()
+    relaxed.particles.acceleration = np.zeros((relaxed.particles.N, 3))
+    return relaxed, wca, qb
+
+
+def test_fp32_state_round_trip():
+    snap = random_fluid(3000, 0.8, seed=31)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    snap.particles.image = np.random.default_rng(3).integers(-3, 4, size=(snap.particles.N, 3)).astype(np.int32)
+    sim, lj = _lj_setup(snap, precision="fp32")
+    from azplugins_gb300 import _engine, _lib
+
+    eng = _engine.Engine(sim, sim._attach(), sim.state._arrays())
+    eng.push(sim.state._arrays(), 0)
+    N = snap.particles.N
+    pos, vel = np.empty((N, 4)), np.empty((N, 4))
+    img = np.empty((N, 3), dtype=np.int32)
+    _lib.check(eng._L.azp_md_get_state(eng._md, pos.ctypes.data, vel.ctypes.data, None, img.ctypes.data, None, 0,
+                                       None), "azp_md_get_state")
+    L = box_of(snap)
+    # 64-bit fixed point holds every FP64 position to within an ulp of the box
+    assert np.abs(pos[:, :3] - snap.particles.position).max() <= 4 * np.spacing(L.max() / 2)
+    # float pairs hold velocities to 2^-48 relative
+    v0 = snap.particles.velocity
+    assert np.abs(vel[:, :3] - v0).max() <= 2.0 ** -46 * np.abs(v0).max()
+    assert np.array_equal(vel[:, 3], snap.particles.mass)
+    assert np.array_equal(pos[:, 3], snap.particles.typeid.astype(float))
+    assert np.array_equal(img, snap.particles.image)
+    eng.close()
+
+
+def test_fp32_graph_replay_is_bitwise_identical_to_stream_launches():
+    from azplugins_gb300 import workloads
+
+    snap = workloads.lj_fluid(n_side=10, density=0.8, seed=32)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    res = []
+    for graphs in ("1", "0"):
+        os.environ["AZP_GRAPHS"] = graphs
+        try:
+            sim, lj = _lj_setup(snap, precision="fp32")
+            sim.run(60)
+            sim.run(9)
+            res.append(sim.state.get_snapshot().particles)
+        finally:
+            os.environ.pop("AZP_GRAPHS", None)
+    a, b = res
+    assert np.array_equal(a.position, b.position)
+    assert np.array_equal(a.velocity, b.velocity)
+    assert np.array_equal(a.image, b.image)
+
+
+def test_fp32_run_splitting():
+    from azplugins_gb300 import workloads
+
+    snap = workloads.lj_fluid(n_side=10, density=0.8, seed=33)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    outs = []
+    for chunks in ([60], [7, 13, 40]):
+        sim, lj = _lj_setup(snap, precision="fp32")
+        for c in chunks:
+            sim.run(c)
+        outs.append(sim.state.get_snapshot().particles)
+    a, b = outs
+    L = box_of(snap)
+    # a run boundary replaces one fused half-kick pair by two FP32 half kicks
+    assert np.abs(_unwrapped(a, L) - _unwrapped(b, L)).max() < 1e-5
+
+
+def test_fp32_melt_parabolic_flow_vs_oracle(orc):
+    relaxed, wca, qb = _relaxed_melt()
+    L = box_of(relaxed)
+    flow = az.flow.ParabolicFlow(mean_velocity=2.0 / 3.0, separation=L[1])
+    sim = az.Simulation(seed=10, precision="fp32")
+    sim.create_state_from_snapshot(relaxed)
+    m = az.methods.LangevinFlow("all", kT=1.0, flow_field=flow, default_gamma=1.0)
+    sim.operations.integrator = az.md.Integrator(dt=0.005, methods=[m], forces=[wca, qb])
+    sim.run(100)
+    rec = orc.bond_params("Quartic", qb.params["A-A"])
+    md = _oracle_lj(orc, relaxed, seed=10, lam=0.0, rcut=2 ** (1 / 6), flow_kind=1,
+                    flow_p=(2.0 / 3.0, L[1], 0.0), bond=dict(name="Quartic", params=rec.reshape(1, 8)))
+    md.run(100)
+    out = sim.state.get_snapshot().particles
+    ref_unwrapped = md.s["pos4"][:, :3] + md.s["image"] * L
+    # FP32 forces: 100 steps (0.5 tau) of a stiff bead-spring melt stay within 1e-3
+    assert np.abs(_unwrapped(out, L) - ref_unwrapped).max() < 1e-3
+    assert np.abs(out.velocity - md.s["vel4"][:, :3]).max() < 2e-2
+    # wrapped positions lie in the box; images agree with the unwrapped trajectory
+    assert (np.abs(out.position) <= L / 2).all()
+
+
+def test_fp32_brownian_vs_oracle(orc):
+    snap = random_fluid(800, 0.3, seed=34, min_dist=1.05)
+    sim, lj = _lj_setup(snap, precision="fp32", method="brownian", flow=az.flow.ConstantFlow((0.1, 0.0, 0.0)),
+                        dt=2e-4, lam=1.0, rcut=2.5)
+    sim.run(50)
+    md = _oracle_lj(orc, snap, method="brownian", dt=2e-4, lam=1.0, rcut=2.5, flow_kind=0, flow_p=(0.1, 0, 0))
+    md.run(50)
+    out = sim.state.get_snapshot().particles
+    L = box_of(snap)
+    assert np.abs(_unwrapped(out, L) - (md.s["pos4"][:, :3] + md.s["image"] * L)).max() < 1e-6
+
+
+def test_fp32_images_cross_every_face():
+    # a constant drift carries every particle across the +x face and, with a
+    # negative y drift, across the -y face: images count the crossings exactly
+    snap = random_fluid(500, 0.2, seed=35, min_dist=1.2)
+    L = box_of(snap)
+    n = 400
+    dt = 1e-3
+    drift = (L[0] / (n * dt) * 1.3, -L[1] / (n * dt) * 0.6, 0.0)
+    sim, lj = _lj_setup(snap, precision="fp32", method="brownian", flow=az.flow.ConstantFlow(drift), dt=dt,
+                        lam=0.0, rcut=2 ** (1 / 6), kT=0.0)
+    sim.run(n)
+    out = sim.state.get_snapshot().particles
+    moved = _unwrapped(out, L) - snap.particles.position
+    # WCA pushes only at contact (none at this density and spacing); the drift dominates
+    assert np.allclose(moved[:, 0], drift[0] * n * dt, rtol=0, atol=0.05)
+    assert np.allclose(moved[:, 1], drift[1] * n * dt, rtol=0, atol=0.05)
+    assert (out.image[:, 0] >= 1).all() and (out.image[:, 1] <= 0).all()
