@@ -29,6 +29,12 @@ struct NoBond {
         f = e = R(0);
         return true;
     }
+    AZP_HD static void prepare_f(const double*, float*) {}
+    AZP_D static bool eval_f(const float*, float, float& f, float& e)
+    {
+        f = e = 0.0f;
+        return true;
+    }
 };
 
 // accumulator: compensated force / energy in FP32, plain in FP64
@@ -105,6 +111,58 @@ template<> struct Acc<float> {
         }
     }
     // sum and carry converted separately: the FP64 result keeps the compensation
+    AZP_D double Fx() const { return (double)fx.s + (double)fx.c; }
+    AZP_D double Fy() const { return (double)fy.s + (double)fy.c; }
+    AZP_D double Fz() const { return (double)fz.s + (double)fz.c; }
+    AZP_D double U() const { return (double)u.s + (double)u.c; }
+};
+
+// Accumulator of the FP32-force step. The terms of one gather batch (at most
+// FX_BATCH pairs, or the bonds) are summed in plain FP32, and each batch sum
+// enters the per-particle force with two-sum compensation, so the rounding error
+// does not grow with the neighbour count. Energy and virial are accumulated only
+// when the step writes them (the integrator needs forces alone).
+struct AccFx {
+    Comp fx{0.f, 0.f}, fy{0.f, 0.f}, fz{0.f, 0.f}, u{0.f, 0.f};
+    float w[6] = {0, 0, 0, 0, 0, 0};
+    float bx = 0.f, by = 0.f, bz = 0.f, bu = 0.f;
+    AZP_D void add(float dx, float dy, float dz, float fdr, float e, bool out)
+    {
+        bx += dx * fdr;
+        by += dy * fdr;
+        bz += dz * fdr;
+        if (out) {
+            bu += 0.5f * e;
+            const float h = 0.5f * fdr;
+            w[0] += h * dx * dx;
+            w[1] += h * dx * dy;
+            w[2] += h * dx * dz;
+            w[3] += h * dy * dy;
+            w[4] += h * dy * dz;
+            w[5] += h * dz * dz;
+        }
+    }
+    // close a batch: its sums enter the compensated totals
+    AZP_D void commit(bool out)
+    {
+        fx.add(bx);
+        fy.add(by);
+        fz.add(bz);
+        if (out) u.add(bu);
+        bx = by = bz = bu = 0.f;
+    }
+    AZP_D void reduce(int tpp, bool out)
+    {
+        for (int m = tpp >> 1; m > 0; m >>= 1) {
+            Acc<float>::comb(fx, m);
+            Acc<float>::comb(fy, m);
+            Acc<float>::comb(fz, m);
+            if (out) {
+                Acc<float>::comb(u, m);
+                for (int c = 0; c < 6; ++c) w[c] += __shfl_xor_sync(0xffffffffu, w[c], m);
+            }
+        }
+    }
     AZP_D double Fx() const { return (double)fx.s + (double)fx.c; }
     AZP_D double Fy() const { return (double)fy.s + (double)fy.c; }
     AZP_D double Fz() const { return (double)fz.s + (double)fz.c; }
@@ -333,7 +391,7 @@ AZP_D bool inside_exact(const MDArgs& a, uint32_t i, uint32_t j, double rc2)
 
 template<class PE>
 AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j,
-                        const float* s_rec, const double* s_rc2, Acc<float>& acc, bool vir)
+                        const float* s_rec, const double* s_rc2, AccFx& acc, bool vir)
 {
     const float dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
     const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
@@ -355,14 +413,14 @@ AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint3
 
 template<class BE>
 AZP_D void bond_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t btype, const float* s_bond,
-                        Acc<float>& acc, bool vir)
+                        AccFx& acc, bool vir)
 {
     const float dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
     const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
     const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
     const float rsq = dx * dx + dy * dy + dz * dz;
     float fdr, en;
-    if (!BE::eval(s_bond + btype * AZP_BOND_PARAM_DOUBLES, rsq, fdr, en)) {
+    if (!BE::eval_f(s_bond + btype * BOND_F, rsq, fdr, en)) {
         atomicOr(&a.flags[1], AZP_EBIT_BOND);
         return;
     }
@@ -389,17 +447,24 @@ AZP_D void finish_step(const MDArgs& a, bool want_rebuild)
 
 // neighbours gathered per batch: the list indices of a batch are loaded first,
 // then their positions, so each thread keeps this many gathers in flight
-constexpr int FX_BATCH = 4;
+#ifndef AZP_FX_BATCH
+#define AZP_FX_BATCH 4
+#endif
+constexpr int FX_BATCH = AZP_FX_BATCH;
+// resident blocks per SM the FP32-force step is compiled for (register cap)
+#ifndef AZP_FX_MIN_BLOCKS
+#define AZP_FX_MIN_BLOCKS 4
+#endif
 
-template<class PE, class BE, int INTEG>
-__global__ void __launch_bounds__(MD_BLOCK, 4) k_md_step_fx(MDArgs a)
+template<class PE, class BE, int INTEG, bool OUT>
+__global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t nt2 = a.ntypes * a.ntypes;
     double* s_rc2 = reinterpret_cast<double*>(smem_raw);
     float* s_rec = reinterpret_cast<float*>(s_rc2 + nt2);
     float* s_bond = s_rec + nt2 * PAIR_TBL;
-    float* s_gamma = s_bond + a.nbondtypes * AZP_BOND_PARAM_DOUBLES;
+    float* s_gamma = s_bond + a.nbondtypes * BOND_F;
     float* s_noise = s_gamma + a.ntypes;
     if (!std::is_same<PE, NoPair>::value)
         for (uint32_t t = threadIdx.x; t < nt2 * PAIR_TBL; t += blockDim.x) {
@@ -407,8 +472,8 @@ __global__ void __launch_bounds__(MD_BLOCK, 4) k_md_step_fx(MDArgs a)
             if (t % PAIR_TBL == PAIR_REC) s_rc2[t / PAIR_TBL] = a.pair_table[t];
         }
     if (!std::is_same<BE, NoBond>::value)
-        for (uint32_t t = threadIdx.x; t < a.nbondtypes * AZP_BOND_PARAM_DOUBLES; t += blockDim.x)
-            s_bond[t] = (float)a.bond_params[t];
+        for (uint32_t t = threadIdx.x; t < a.nbondtypes; t += blockDim.x)
+            BE::prepare_f(a.bond_params + (size_t)t * AZP_BOND_PARAM_DOUBLES, s_bond + (size_t)t * BOND_F);
     if (INTEG != MD_FORCES_ONLY && !a.use_lambda)
         for (uint32_t t = threadIdx.x; t < a.ntypes; t += blockDim.x) {
             s_gamma[t] = (float)a.gamma[t];
@@ -421,8 +486,8 @@ __global__ void __launch_bounds__(MD_BLOCK, 4) k_md_step_fx(MDArgs a)
     const uint32_t i = gid >> a.tpp_shift;
     const uint32_t sub = gid & (tpp - 1u);
     const bool active = i < a.N;
-    const bool vir = a.out != 0;
-    Acc<float> acc;
+    constexpr bool vir = OUT;
+    AccFx acc;
     uint4 fi = make_uint4(0u, 0u, 0u, 0u);
     if (active) {
         fi = __ldg(a.fix + i);
@@ -443,6 +508,7 @@ __global__ void __launch_bounds__(MD_BLOCK, 4) k_md_step_fx(MDArgs a)
 #pragma unroll
                 for (int u = 0; u < FX_BATCH; ++u)
                     if (k0 + u * tpp < n) pair_term_fx<PE>(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir);
+                acc.commit(vir);
             }
         }
         // ---------------------------------------------------------------- bonds
@@ -456,6 +522,7 @@ __global__ void __launch_bounds__(MD_BLOCK, 4) k_md_step_fx(MDArgs a)
                 const uint4 f1 = __ldg(a.fix + e1.x);
                 bond_term_fx<BE>(a, fi, f0, e0.y, s_bond, acc, vir);
                 if (k1 < nb) bond_term_fx<BE>(a, fi, f1, e1.y, s_bond, acc, vir);
+                acc.commit(vir);
             }
         }
     }
@@ -463,7 +530,7 @@ __global__ void __launch_bounds__(MD_BLOCK, 4) k_md_step_fx(MDArgs a)
 
     bool want_rebuild = false;
     if (active && sub == 0) {
-        if (a.out) {
+        if constexpr (OUT) {
             a.out_force[i] = make_double4_32a(acc.Fx(), acc.Fy(), acc.Fz(), acc.U());
             for (int c = 0; c < 6; ++c) a.out_virial[(size_t)c * a.N + i] = (double)acc.w[c];
         }
@@ -551,8 +618,8 @@ int launch_md_t(const MDArgs& a, cudaStream_t s)
     const size_t nt2 = (size_t)a.ntypes * a.ntypes;
     if constexpr (std::is_same<R, float>::value) {
         const size_t smem = nt2 * sizeof(double) + nt2 * PAIR_TBL * sizeof(float) +
-                            (size_t)a.nbondtypes * AZP_BOND_PARAM_DOUBLES * sizeof(float) + 2 * a.ntypes * sizeof(float);
-        auto k = k_md_step_fx<PE, BE, INTEG>;
+                            (size_t)a.nbondtypes * BOND_F * sizeof(float) + 2 * a.ntypes * sizeof(float);
+        auto k = a.out ? k_md_step_fx<PE, BE, INTEG, true> : k_md_step_fx<PE, BE, INTEG, false>;
         if (smem > 48 * 1024) AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<blocks, MD_BLOCK, smem, s>>>(a);
         AZP_CHECK_LAUNCH("k_md_step_fx");

@@ -21,13 +21,13 @@ namespace azp
 constexpr int PAIR_REC = 8;   // values per pair kernel record
 constexpr int CUT_REC = 4;    // rcutsq, ronsq, 1/(rcutsq-ronsq)^3, xplor flag
 
-// correctly rounded reciprocal; the FP32 form maps to the hardware-assisted
-// rounded reciprocal instead of a full division
+// reciprocal: FP64 correctly rounded; FP32 the hardware approximation (within
+// about 1 ulp, far inside the FP32 force budget of 1e-5 relative)
 AZP_HD double rcp(double x) { return 1.0 / x; }
 AZP_HD float rcp(float x)
 {
 #ifdef __CUDA_ARCH__
-    return __frcp_rn(x);
+    return __fdividef(1.0f, x);
 #else
     return 1.0f / x;
 #endif
@@ -234,6 +234,11 @@ template<typename R> AZP_HD void xplor(const R* cut, R rsq, R& fdr, R& e)
 // ================================================================ bond potentials
 // rec = the reference param_type (8 doubles). eval returns false when the
 // evaluator refuses (the reference's "invalid parameters" returns).
+// The FP32-force engine step uses FP32 records of BOND_F floats per bond type
+// instead, with the per-type constants of eval precomputed (prepare_f), so its
+// eval_f holds no parameter division.
+constexpr int BOND_F = 12;
+
 struct QuarticBond {
     template<typename R> AZP_HD static bool eval(const R* p, R rsq, R& fdr, R& e)
     {
@@ -271,6 +276,53 @@ struct QuarticBond {
         }
         return true;
     }
+    // q: k, r_0, b_1, b_2, U_0, lj1, lj2, delta, WCA r^-6 threshold, WCA energy
+    // shift, 3 (b_1 + b_2), 2 b_1 b_2
+    AZP_HD static void prepare_f(const double* p, float* q)
+    {
+        const double lj1 = p[6] * p[5] * p[5], lj2 = p[6] * p[5];
+        for (int k = 0; k < 5; ++k) q[k] = (float)p[k];
+        q[5] = (float)lj1;
+        q[6] = (float)lj2;
+        q[7] = (float)p[7];
+        q[8] = lj1 != 0.0 ? (float)((lj2 / lj1) / 2.0) : 0.0f;
+        q[9] = p[7] == 0.0 ? (lj1 != 0.0 ? (float)(lj2 * lj2 / 4.0 / lj1) : 0.0f) : (float)(p[6] / 4.0);
+        q[10] = (float)(3.0 * (p[2] + p[3]));
+        q[11] = (float)(2.0 * p[2] * p[3]);
+    }
+    AZP_D static bool eval_f(const float* q, float rsq, float& fdr, float& e)
+    {
+        const float k = q[0], r0 = q[1], b1 = q[2], b2 = q[3], lj1 = q[5], lj2 = q[6], del = q[7];
+        fdr = 0.0f;
+        e = 0.0f;
+        if (r0 == 0.0f) return false;
+        float rr = 1.0f;
+        if (del == 0.0f) {
+            const float r2inv = rcp(rsq);
+            const float r6inv = r2inv * r2inv * r2inv;
+            if (lj1 != 0.0f && r6inv > q[8]) {
+                fdr += r2inv * r6inv * (12.0f * lj1 * r6inv - 6.0f * lj2);
+                e += r6inv * (lj1 * r6inv - lj2) + q[9];
+            }
+            if (rsq < r0 * r0) rr = sqrtf(rsq) - r0;
+        } else {
+            const float rs = sqrtf(rsq) - del;
+            const float r2inv = rcp(rs * rs);
+            const float r6inv = r2inv * r2inv * r2inv;
+            if (lj1 != 0.0f && r6inv > q[8]) {
+                fdr += __fdividef(r6inv * (12.0f * lj1 * r6inv - 6.0f * lj2), rs * (rs + del));
+                e += r6inv * (lj1 * r6inv - lj2) + q[9];
+            }
+            if (rs < r0) rr = rs - r0;
+        }
+        if (rr < 0.0f) {
+            fdr += __fdividef(-k * rr * (4.0f * rr * rr - q[10] * rr + q[11]), rr + r0 + del);
+            e += k * (rr - b1) * (rr - b2) * rr * rr + q[4];
+        } else {
+            e += q[4];
+        }
+        return true;
+    }
 };
 
 struct DoubleWellBond {
@@ -287,6 +339,11 @@ struct DoubleWellBond {
         fdr = (R(4) * x * y * (Ut - U1) - Ut) / (rd * r);
         return true;
     }
+    AZP_HD static void prepare_f(const double* p, float* q)
+    {
+        for (int k = 0; k < BOND_F; ++k) q[k] = k < AZP_BOND_PARAM_DOUBLES ? (float)p[k] : 0.0f;
+    }
+    AZP_D static bool eval_f(const float* q, float rsq, float& fdr, float& e) { return eval(q, rsq, fdr, e); }
 };
 
 }  // namespace azp
