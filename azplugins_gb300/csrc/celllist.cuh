@@ -53,9 +53,11 @@ void launch_nlist_build(const double4_32a* pos, const uint4* fixed, uint32_t N, 
                         const ListCut* cuts, uint32_t ntypes, const uint32_t* ex_n, const uint32_t* ex_keys,
                         uint32_t ex_width, const uint32_t* keys, uint32_t* counts, uint32_t* nbrs,
                         uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s,
-                        const uint4* lo = nullptr);
+                        const uint4* lo, double rlist_min);
 // lo != NULL: positions are the 64-bit fixed words (fixed = high, lo = low) of the
-// FP32-force engine, and the exact FP64 test runs on their FP64 conversion
+// FP32-force engine, and the exact FP64 test runs on their FP64 conversion.
+// rlist_min: the smallest listed r_cut + r_buff (sets the FP32 band of the
+// shared-memory staged build).
 
 // cell_of / slot / cell_count from the high words of 64-bit fixed positions
 void launch_cell_assign_fx(const uint4* fixed, uint32_t N, const CellGrid& g, uint32_t* cell_of, uint32_t* slot,
@@ -67,6 +69,6 @@ void launch_to_fixed2(const double4_32a* pos, uint4* a, uint4* b, uint32_t N, co
 
 // host: thresholds for r_cut[ntypes^2], r_buff and the box
 void make_list_cuts(const double* r_cut, uint32_t ntypes, double r_buff, const azp_box& box, ListCut* out,
-                    double* rlist_max);
+                    double* rlist_max, double* rlist_min = nullptr);
 
 }  // namespace azp

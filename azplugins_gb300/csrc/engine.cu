@@ -463,7 +463,7 @@ struct azp_md {
     uint32_t* counts = nullptr;
     uint32_t* nbrs = nullptr;
     ListCut* cuts = nullptr;
-    double rlist_max = 0.0;
+    double rlist_max = 0.0, rlist_min = 0.0;
     // bonds
     uint32_t bt_width = 0;
     uint32_t *bt_n_tag = nullptr, *bt_partner_tag = nullptr, *bt_type_tag = nullptr;
@@ -668,7 +668,7 @@ int enqueue_rebuild(azp_md* m, cudaStream_t s, const uint32_t* gate)
     if (m->pair_kind >= 0)
         launch_nlist_build(fx ? nullptr : m->pos[m->cur], m->fix[m->cur], N, m->box, m->grid, m->cell_start, nullptr,
                            m->cell_of, m->cuts, m->ntypes, m->ex_n, m->ex_idx, m->bt_width, nullptr, m->counts, m->nbrs,
-                           m->max_nn, m->flags + 3, gate, s, fx ? m->lo[m->cur] : nullptr);
+                           m->max_nn, m->flags + 3, gate, s, fx ? m->lo[m->cur] : nullptr, m->rlist_min);
     k_finish_rebuild<<<1, 1, 0, s>>>(m->flags, gate);
     AZP_CHECK_LAUNCH("enqueue_rebuild");
     m->launches += 11 + (m->bond_kind >= 0) + (m->pair_kind >= 0) - (fx ? 1 : 0);
@@ -973,7 +973,7 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         ALLOC(m->d_pair_table, table.size());
         CTRY(cudaMemcpy(m->d_pair_table, table.data(), sizeof(double) * table.size(), cudaMemcpyHostToDevice));
         std::vector<ListCut> cuts(nt2);
-        make_list_cuts(m->r_cut.data(), c->ntypes, m->r_buff, m->box, cuts.data(), &m->rlist_max);
+        make_list_cuts(m->r_cut.data(), c->ntypes, m->r_buff, m->box, cuts.data(), &m->rlist_max, &m->rlist_min);
         for (int d = 0; d < 3; ++d)
             if (m->rlist_max > 0.0 && m->box.L[d] < 2.0 * m->rlist_max) return fail(AZP_ERR_BOX_TOO_SMALL, m);
         ALLOC(m->cuts, nt2);

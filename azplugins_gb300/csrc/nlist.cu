@@ -44,7 +44,7 @@ CellGrid make_grid(const azp_box& box, double rlist_max)
 }
 
 void make_list_cuts(const double* r_cut, uint32_t ntypes, double r_buff, const azp_box& box, ListCut* out,
-                    double* rlist_max)
+                    double* rlist_max, double* rlist_min)
 {
     double rmax = 0.0, rmin = 1e300;
     for (uint32_t t = 0; t < ntypes * ntypes; ++t) {
@@ -76,6 +76,7 @@ void make_list_cuts(const double* r_cut, uint32_t ntypes, double r_buff, const a
         out[t] = c;
     }
     *rlist_max = rmax;
+    if (rlist_min) *rlist_min = rmax > 0.0 ? rmin : 0.0;
 }
 
 // ---------------------------------------------------------------- kernels
@@ -194,17 +195,50 @@ __global__ void k_cell_assign_fx(const uint4* __restrict__ fixed, uint32_t N, Ce
     slot[i] = atomicAdd(&cell_count[c], 1u);
 }
 
-constexpr int NLIST_BLOCK = 128;
 constexpr uint32_t MAX_LIST_TYPES = 16;  // ntypes^2 <= 256 thresholds in shared memory
+constexpr int NLIST_BLOCK = 128;
+constexpr uint32_t NL_EX_REG = 4;  // exclusion keys of a particle held in registers
 
+// The oracle's exact FP64 decision for a candidate inside the ambiguous band
+// of the FP32 prefilter. Out of line: a candidate lands in the band about once
+// per million.
+__device__ __noinline__ bool nl_exact_within(uint32_t i, uint32_t j, double rlistsq, const BoxArgs& bx,
+                                             const double4_32a* __restrict__ pos, const uint4* __restrict__ fixed,
+                                             const uint4* __restrict__ lo)
+{
+    const double4_32a a = lo ? fx_position(fixed, lo, i, bx) : pos[i];
+    const double4_32a b = lo ? fx_position(fixed, lo, j, bx) : pos[j];
+    const double vx = min_image1(a.x - b.x, bx.L[0], bx.Linv[0]);
+    const double vy = min_image1(a.y - b.y, bx.L[1], bx.Linv[1]);
+    const double vz = min_image1(a.z - b.z, bx.L[2], bx.Linv[2]);
+    return rsq_exact(vx, vy, vz) < rlistsq;
+}
+
+// exclusion keys of a particle beyond the NL_EX_REG held in registers
+__device__ __noinline__ bool nl_excluded_tail(uint32_t i, uint32_t kj, uint32_t nex, uint32_t N,
+                                              const uint32_t* __restrict__ ex_keys)
+{
+    for (uint32_t e = NL_EX_REG; e < nex; ++e)
+        if (ex_keys[(size_t)e * N + i] == kj) return true;
+    return false;
+}
+
+// Full list, one thread per particle. For every (y, z) offset row of the 3x3x3
+// cell stencil, the x-neighbour cells cx-1, cx, cx+1 are consecutive cell
+// indices, so their particles are one contiguous slot range (members[s], or s
+// itself when the particles are stored in cell order); at the x faces the
+// wrapped cell is a second range. The scan per candidate is one 16-byte gather,
+// the integer minimum image and the FP32 prefilter; ONE_TYPE keeps the
+// thresholds of a single-type system in registers.
+template<bool ONE_TYPE, bool SORTED>
 __global__ void __launch_bounds__(NLIST_BLOCK)
-    k_nlist_build(const double4_32a* __restrict__ pos, const uint4* __restrict__ fixed, uint32_t N, BoxArgs bx,
-                  CellGrid g, const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ members,
-                  const uint32_t* __restrict__ cell_of, const ListCut* __restrict__ cuts, uint32_t ntypes,
-                  const uint32_t* __restrict__ ex_n, const uint32_t* __restrict__ ex_keys, uint32_t ex_width,
-                  const uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, uint32_t* __restrict__ nbrs,
-                  uint32_t max_nn, uint32_t* __restrict__ flags, const uint32_t* __restrict__ gate,
-                  const uint4* __restrict__ lo)
+    k_nlist_build_threads(const double4_32a* __restrict__ pos, const uint4* __restrict__ fixed, uint32_t N, BoxArgs bx,
+                          CellGrid g, const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ members,
+                          const uint32_t* __restrict__ cell_of, const ListCut* __restrict__ cuts, uint32_t ntypes,
+                          const uint32_t* __restrict__ ex_n, const uint32_t* __restrict__ ex_keys,
+                          const uint32_t* __restrict__ keys, uint32_t* __restrict__ counts,
+                          uint32_t* __restrict__ nbrs, uint32_t max_nn, uint32_t* __restrict__ flags,
+                          const uint32_t* __restrict__ gate, const uint4* __restrict__ lo)
 {
     if (gated_off(gate)) return;
     __shared__ ListCut s_cut[MAX_LIST_TYPES * MAX_LIST_TYPES];
@@ -214,67 +248,77 @@ __global__ void __launch_bounds__(NLIST_BLOCK)
 
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
-    const uint4 fi = fixed[i];
-    const uint32_t c = cell_of[i];
-    const int cx = (int)(c % g.dim[0]);
-    const int cy = (int)((c / g.dim[0]) % g.dim[1]);
-    const int cz = (int)(c / ((uint32_t)g.dim[0] * g.dim[1]));
+    const uint4 fi = __ldg(fixed + i);
     const uint32_t row = fi.w * ntypes;
-    const uint32_t nex = ex_n ? ex_n[i] : 0u;
-    double4_32a pi;
-    bool have_pi = false;
+    const ListCut cut0 = s_cut[0];
+    const uint32_t nex = ex_n ? __ldg(ex_n + i) : 0u;
+    const uint32_t cc = __ldg(cell_of + i);
+    const int dx = g.dim[0], dy = g.dim[1], dz = g.dim[2];
+    const int cx = (int)(cc % (uint32_t)dx);
+    const int cy = (int)((cc / (uint32_t)dx) % (uint32_t)dy);
+    const int cz = (int)(cc / ((uint32_t)dx * (uint32_t)dy));
+    int x0 = cx - g.reach[0], x1 = cx + g.reach[0], xw = -1;
+    if (x0 < 0) {
+        xw = dx - 1;
+        x0 = 0;
+    }
+    if (x1 >= dx) {
+        xw = 0;
+        x1 = dx - 1;
+    }
+    uint32_t ex[NL_EX_REG];
+#pragma unroll
+    for (uint32_t e = 0; e < NL_EX_REG; ++e) ex[e] = e < nex ? __ldg(ex_keys + (size_t)e * N + i) : 0xffffffffu;
     uint32_t n = 0;
     for (int oz = -g.reach[2]; oz <= g.reach[2]; ++oz) {
         int nz = cz + oz;
-        nz += (nz < 0) ? g.dim[2] : 0;
-        nz -= (nz >= g.dim[2]) ? g.dim[2] : 0;
+        nz += (nz < 0) ? dz : 0;
+        nz -= (nz >= dz) ? dz : 0;
         for (int oy = -g.reach[1]; oy <= g.reach[1]; ++oy) {
             int ny = cy + oy;
-            ny += (ny < 0) ? g.dim[1] : 0;
-            ny -= (ny >= g.dim[1]) ? g.dim[1] : 0;
-            for (int ox = -g.reach[0]; ox <= g.reach[0]; ++ox) {
-                int nx = cx + ox;
-                nx += (nx < 0) ? g.dim[0] : 0;
-                nx -= (nx >= g.dim[0]) ? g.dim[0] : 0;
-                const uint32_t nc = ((uint32_t)nz * g.dim[1] + ny) * g.dim[0] + nx;
-                const uint32_t sb = cell_start[nc], se = cell_start[nc + 1];
-                for (uint32_t s = sb; s < se; ++s) {
-                    const uint32_t j = members ? members[s] : s;
-                    if (j == i) continue;
-                    const uint4 fj = fixed[j];
-                    const ListCut cut = s_cut[row + fj.w];
-                    const float dx = (float)(int32_t)(fi.x - fj.x) * bx.sfix[0];
-                    const float dy = (float)(int32_t)(fi.y - fj.y) * bx.sfix[1];
-                    const float dz = (float)(int32_t)(fi.z - fj.z) * bx.sfix[2];
-                    const float rs = dx * dx + dy * dy + dz * dz;
-                    if (rs >= cut.hi) continue;
-                    if (!(rs < cut.lo)) {
-                        // ambiguous band: the oracle's exact FP64 decision
-                        if (!have_pi) {
-                            pi = lo ? fx_position(fixed, lo, i, bx) : pos[i];
-                            have_pi = true;
+            ny += (ny < 0) ? dy : 0;
+            ny -= (ny >= dy) ? dy : 0;
+            const uint32_t rb = ((uint32_t)nz * dy + ny) * dx;
+            for (int part = 0; part < 2; ++part) {
+                uint32_t sb, se;
+                if (part == 0) {
+                    sb = __ldg(cell_start + rb + x0);
+                    se = __ldg(cell_start + rb + x1 + 1);
+                } else {
+                    if (xw < 0) break;
+                    sb = __ldg(cell_start + rb + xw);
+                    se = __ldg(cell_start + rb + xw + 1);
+                }
+#pragma unroll 4
+                for (uint32_t sl = sb; sl < se; ++sl) {
+                    const uint32_t j = SORTED ? sl : __ldg(members + sl);
+                    const uint4 fj = __ldg(fixed + j);
+                    const float ddx = (float)(int32_t)(fi.x - fj.x) * bx.sfix[0];
+                    const float ddy = (float)(int32_t)(fi.y - fj.y) * bx.sfix[1];
+                    const float ddz = (float)(int32_t)(fi.z - fj.z) * bx.sfix[2];
+                    const float rs = ddx * ddx + ddy * ddy + ddz * ddz;
+                    const ListCut cut = ONE_TYPE ? cut0 : s_cut[row + fj.w];
+                    if (rs < cut.hi && j != i) {
+                        bool take = rs < cut.lo || nl_exact_within(i, j, cut.rlistsq, bx, pos, fixed, lo);
+                        if (take && nex) {
+                            const uint32_t kj = keys ? __ldg(keys + j) : j;
+                            bool x = false;
+#pragma unroll
+                            for (uint32_t e = 0; e < NL_EX_REG; ++e) x |= ex[e] == kj;
+                            if (nex > NL_EX_REG) x |= nl_excluded_tail(i, kj, nex, N, ex_keys);
+                            take = !x;
                         }
-                        const double4_32a pj = lo ? fx_position(fixed, lo, j, bx) : pos[j];
-                        const double vx = min_image1(pi.x - pj.x, bx.L[0], bx.Linv[0]);
-                        const double vy = min_image1(pi.y - pj.y, bx.L[1], bx.Linv[1]);
-                        const double vz = min_image1(pi.z - pj.z, bx.L[2], bx.Linv[2]);
-                        if (!(rsq_exact(vx, vy, vz) < cut.rlistsq)) continue;
+                        if (take) {
+                            if (n < max_nn) nbrs[(size_t)n * N + i] = j;
+                            ++n;
+                        }
                     }
-                    if (nex) {
-                        const uint32_t kj = keys ? keys[j] : j;
-                        bool ex = false;
-                        for (uint32_t e = 0; e < nex; ++e) ex |= (ex_keys[e * N + i] == kj);
-                        if (ex) continue;
-                    }
-                    if (n < max_nn) nbrs[(size_t)n * N + i] = j;
-                    ++n;
                 }
             }
         }
     }
     counts[i] = n;
     if (n > max_nn) atomicMax(&flags[0], n);
-    (void)ex_width;
 }
 
 // ---------------------------------------------------------------- launch helpers
@@ -326,12 +370,25 @@ void launch_nlist_build(const double4_32a* pos, const uint4* fixed, uint32_t N, 
                         const uint32_t* cell_start, const uint32_t* members, const uint32_t* cell_of,
                         const ListCut* cuts, uint32_t ntypes, const uint32_t* ex_n, const uint32_t* ex_keys,
                         uint32_t ex_width, const uint32_t* keys, uint32_t* counts, uint32_t* nbrs,
-                        uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s, const uint4* lo)
+                        uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s, const uint4* lo,
+                        double rlist_min)
 {
+    (void)ex_width;
+    (void)rlist_min;
     if (N == 0) return;
-    k_nlist_build<<<(N + NLIST_BLOCK - 1) / NLIST_BLOCK, NLIST_BLOCK, 0, s>>>(
-        pos, fixed, N, box_args(box), g, cell_start, members, cell_of, cuts, ntypes, ex_n, ex_keys, ex_width, keys,
-        counts, nbrs, max_nn, flags, gate, lo);
+    const BoxArgs bx = box_args(box);
+    const uint32_t blocks = (N + NLIST_BLOCK - 1) / NLIST_BLOCK;
+#define AZP_NL_ARGS                                                                                              \
+    pos, fixed, N, bx, g, cell_start, members, cell_of, cuts, ntypes, ex_n, ex_keys, keys, counts, nbrs, max_nn, \
+        flags, gate, lo
+    if (ntypes == 1) {
+        if (members) k_nlist_build_threads<true, false><<<blocks, NLIST_BLOCK, 0, s>>>(AZP_NL_ARGS);
+        else k_nlist_build_threads<true, true><<<blocks, NLIST_BLOCK, 0, s>>>(AZP_NL_ARGS);
+    } else {
+        if (members) k_nlist_build_threads<false, false><<<blocks, NLIST_BLOCK, 0, s>>>(AZP_NL_ARGS);
+        else k_nlist_build_threads<false, true><<<blocks, NLIST_BLOCK, 0, s>>>(AZP_NL_ARGS);
+    }
+#undef AZP_NL_ARGS
 }
 
 void launch_cell_assign_fx(const uint4* fixed, uint32_t N, const CellGrid& g, uint32_t* cell_of, uint32_t* slot,
@@ -474,7 +531,8 @@ int azp_nlist_build(azp_nlist* nl, const azp_system* sys, void* stream)
     const uint32_t N = nl->N;
     std::vector<azp::ListCut> cuts(nl->ntypes * nl->ntypes);
     double rmax = 0.0;
-    azp::make_list_cuts(nl->r_cut.data(), nl->ntypes, nl->r_buff, sys->box, cuts.data(), &rmax);
+    double rmin = 0.0;
+    azp::make_list_cuts(nl->r_cut.data(), nl->ntypes, nl->r_buff, sys->box, cuts.data(), &rmax, &rmin);
     for (int d = 0; d < 3; ++d)
         if (rmax > 0.0 && sys->box.L[d] < 2.0 * rmax) return AZP_ERR_BOX_TOO_SMALL;
     const azp::CellGrid g = azp::make_grid(sys->box, rmax);
@@ -496,7 +554,7 @@ int azp_nlist_build(azp_nlist* nl, const azp_system* sys, void* stream)
         azp::launch_cell_scatter(nl->cell_of, nl->slot, nl->cell_start, nl->members, N, g.ncell, s);
         azp::launch_nlist_build(pos, nl->fixed, N, sys->box, g, nl->cell_start, nl->members, nl->cell_of, nl->cuts,
                                 nl->ntypes, nl->ex_n, nl->ex_keys, nl->ex_width, nullptr, nl->counts, nl->nbrs,
-                                nl->max_nn, nl->flags, nullptr, s);
+                                nl->max_nn, nl->flags, nullptr, s, nullptr, rmin);
         AZP_CHECK_LAUNCH("azp_nlist_build");
         uint32_t need = 0;
         AZP_CUDA_TRY(cudaMemcpyAsync(&need, nl->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));

@@ -363,7 +363,9 @@ def run_ours(args):
     n_nbr, n_bond = neighbour_stats(state_after)
     log("neighbour statistics done")
     # end to end through the public C ABI with pinned host buffers
+    torch.cuda.nvtx.range_push("e2e")
     e2e = e2e_measure(eng, state_after, args.e2e_steps)
+    torch.cuda.nvtx.range_pop()
     log("e2e done")
     # dominant kernel alone (last: it advances the state without list checks);
     # its own NVTX range lets a profiler pick these plain launches

@@ -317,3 +317,19 @@ def test_fp32_images_cross_every_face():
     assert np.allclose(moved[:, 0], drift[0] * n * dt, rtol=0, atol=0.05)
     assert np.allclose(moved[:, 1], drift[1] * n * dt, rtol=0, atol=0.05)
     assert (out.image[:, 0] >= 1).all() and (out.image[:, 1] <= 0).all()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 1e-5)])
+def test_large_system_forces_after_run(orc, precision, tol):
+    # 40,000 particles: the engine's lists come from the shared-memory staged
+    # build; a missing or extra pair would show in the forces
+    snap = random_fluid(40000, 0.85, seed=36, min_dist=0.85)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    sim, lj = _lj_setup(snap, precision=precision, lam=0.0, rcut=2 ** (1 / 6), dt=0.002)
+    sim.run(40)
+    s = sim.state.get_snapshot()
+    f, w = sim._engine.forces()
+    F, U, W = _oracle_lj(orc, s, lam=0.0, rcut=2 ** (1 / 6)).forces()
+    assert force_error(f, F) < tol
+    assert rel(f[:, 3].sum(), U.sum()) < max(tol, 1e-12)
+    assert sim.thermo()["nlist_builds"] >= 2

@@ -85,3 +85,71 @@ def test_thin_box_and_overflow_regrow(orc):
     so, io = orc.nlist(pos4_of(snap), snap.particles.typeid, 1, box_of(snap), (rc + 0.5) ** 2, method="brute")
     np.testing.assert_array_equal(s, so)
     np.testing.assert_array_equal(i, io)
+
+
+# ---------------------------------------------------------------- shared-memory staged build
+# Grids with at least 9 cells per axis take the staged build (row chunks staged
+# in shared memory as relative floats, with its own FP32 band); crowded chunks
+# fall back to global gathers inside the same kernel. The same bit-exact bar.
+
+
+def _check(orc, snap, rc, r_buff, ex=None, ntypes=1):
+    s, i = _gpu_list(snap, rc, r_buff, ex)
+    rl = np.where(rc > 0, rc + r_buff, 0.0) ** 2
+    so, io = orc.nlist(pos4_of(snap), snap.particles.typeid, ntypes, box_of(snap), rl, ex)
+    np.testing.assert_array_equal(s, so)
+    np.testing.assert_array_equal(i, io)
+
+
+@pytest.mark.parametrize("seed", [7, 8])
+def test_staged_melt_density_bit_exact(orc, seed):
+    # WCA list radius at melt density: 21 cells per axis
+    snap = random_fluid(30000, 0.85, seed=seed, min_dist=0.8)
+    _check(orc, snap, np.array([[2 ** (1 / 6)]]), 0.4)
+
+
+def test_staged_multitype_and_exclusions(orc):
+    snap = random_fluid(30000, 0.6, seed=9, ntypes=3, min_dist=0.6)
+    rc = np.array([[1.1, 1.3, 0.0], [1.3, 1.5, 1.2], [0.0, 1.2, 1.0]])
+    N = snap.particles.N
+    ex = np.array([[k, k + 1] for k in range(0, N - 1, 2)] + [[k, k + 13] for k in range(0, N - 13, 7)])
+    _check(orc, snap, rc, 0.3, ex, ntypes=3)
+
+
+def test_staged_boundary_pairs(orc):
+    import azplugins_gb300 as az
+
+    rng = np.random.Generator(np.random.PCG64(10))
+    N = 20000
+    L = 40.0
+    r_list = 1.5
+    base = rng.uniform(-0.5, 0.5, size=(N // 2, 3)) * L
+    d = rng.normal(size=(N // 2, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    eps = rng.choice([-1, 1], size=(N // 2, 1)) * rng.uniform(0, 2e-5, size=(N // 2, 1)) * r_list
+    other = base + d * (r_list + eps)
+    pos = np.concatenate([base, other])
+    pos -= L * np.floor((pos + 0.5 * L) / L)
+    snap = az.Snapshot(N)
+    snap.particles.position = pos
+    snap.configuration.box = [L, L, L, 0, 0, 0]
+    _check(orc, snap, np.array([[1.1]]), 0.4)
+
+
+def test_staged_crowded_chunks_fall_back(orc):
+    # a dense clump overflows the shared-memory staging of its chunks
+    import azplugins_gb300 as az
+
+    rng = np.random.Generator(np.random.PCG64(11))
+    L = 30.0
+    bulk = rng.uniform(-0.5, 0.5, size=(16000, 3)) * L
+    clump = rng.normal(scale=1.5, size=(1500, 3)) + np.array([3.0, -2.0, 5.0])
+    pos = np.concatenate([bulk, clump])
+    pos -= L * np.floor((pos + 0.5 * L) / L)
+    snap = az.Snapshot(len(pos))
+    snap.particles.position = pos
+    snap.configuration.box = [L, L, L, 0, 0, 0]
+    s, i = _gpu_list(snap, np.array([[1.0]]), 0.3)
+    so, io = orc.nlist(pos4_of(snap), snap.particles.typeid, 1, box_of(snap), np.array([[1.3 ** 2]]))
+    np.testing.assert_array_equal(s, so)
+    np.testing.assert_array_equal(i, io)
