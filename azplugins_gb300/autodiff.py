@@ -70,6 +70,34 @@ def record_jacobian(name, values):
     raise KeyError(name)
 
 
+def record_jacobian_t(name, values):
+    """record_jacobian on the device: the same matrix built with torch from the
+    values tensor (no host round trip inside a backward pass)."""
+    torch = _torch()
+    v = values.detach().to(torch.float64)
+    dev = v.device
+    if name == "PerturbedLennardJones":
+        J = torch.zeros((4, 3), dtype=torch.float64, device=dev)
+        J[0, 1] = 6.0 * v[1] ** 5
+        J[1, 0] = 4.0
+        J[2, 2] = 1.0
+        J[3, 1] = 2.0 * _POW_2_13 * v[1]
+        return J
+    if name == "Colloid":
+        J = torch.eye(4, dtype=torch.float64, device=dev)
+        J[3, 3] = 3.0 * v[3] * v[3]
+        return J
+    if name == "Quartic":
+        J = torch.zeros((8, 8), dtype=torch.float64, device=dev)
+        for m in (0, 1, 2, 3, 4, 7):
+            J[m, m] = 1.0
+        J[5, 5] = 6.0 * v[5] ** 5
+        J[6, 6] = 4.0
+        return J
+    # constant Jacobians
+    return torch.from_numpy(record_jacobian(name, [0.0] * len(v))).to(dev)
+
+
 class Context:
     """Static inputs of a differentiable force: types, box, list parameters."""
 
@@ -180,7 +208,7 @@ def _make_pair_fn():
             _lib.check(L.azp_pair_adjoint(ctypes.byref(sysd), fctx.nl.handle, ctx.pair.kind, params.data_ptr(),
                                           rc.data_ptr(), ro.data_ptr(), _lib.MODES[ctx.pair.mode], grad.data_ptr(),
                                           gpos.data_ptr(), grec.data_ptr(), _stream()), "azp_pair_adjoint")
-            J = torch.from_numpy(record_jacobian(ctx.pair._name, values.detach().cpu().numpy())).cuda()
+            J = record_jacobian_t(ctx.pair._name, values)
             gvals = J.T @ grec.sum(dim=0)
             return gpos, gvals.to(values.dtype), None
 
@@ -238,7 +266,7 @@ def _make_bond_fn():
             _lib.check(L.azp_bond_adjoint(ctypes.byref(sysd), ctx.bond_n.data_ptr(), ctx.bond_table.data_ptr(),
                                           ctx.bond.kind, params.data_ptr(), len(ctx.bond_types), grad.data_ptr(),
                                           gpos.data_ptr(), grec.data_ptr(), None, _stream()), "azp_bond_adjoint")
-            J = torch.from_numpy(record_jacobian(ctx.bond._name, values.detach().cpu().numpy())).cuda()
+            J = record_jacobian_t(ctx.bond._name, values)
             gvals = J.T @ grec.sum(dim=0)
             return gpos, gvals.to(values.dtype), None
 

@@ -127,7 +127,10 @@ template<class Eval> AZP_D PairDerivs dual_derivs(const D5* rec, double s)
     return r;
 }
 
-template<class Eval>
+// WRITTEN: the hand-written PerturbedLennardJones derivatives (no smoothing);
+// otherwise the dual-number path. Separate instantiations keep the dual
+// records' registers out of the hand-written kernel.
+template<class Eval, bool WRITTEN>
 __global__ void __launch_bounds__(ADJ_BLOCK) k_pair_adjoint(AdjArgs a)
 {
     const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -153,14 +156,10 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_pair_adjoint(AdjArgs a)
             const D5* cut = rec + PAIR_REC;
             if (!(s < cut[0].v) || !Eval::enabled(rec)) continue;
             PairDerivs q;
-            if constexpr (std::is_same<Eval, PerturbedLJ>::value) {
-                if (a.xplor)
-                    q = dual_derivs<Eval>(rec, s);
-                else
-                    q = plj_derivs(rec, s);
-            } else {
+            if constexpr (WRITTEN)
+                q = plj_derivs(rec, s);
+            else
                 q = dual_derivs<Eval>(rec, s);
-            }
             const double4_32a Gj = a.grad[j];
             const double Gx = Gi.x - Gj.x, Gy = Gi.y - Gj.y, Gz = Gi.z - Gj.z;
             const double g = 0.5 * (Gi.w + Gj.w);
@@ -272,7 +271,11 @@ int launch_adj(const azp_system* sys, azp_nlist* nl, const double* params, const
     a.tpp = nl->tpp;
     a.xplor = mode == AZP_MODE_XPLOR;
     const size_t threads = (size_t)sys->N * a.tpp;
-    k_pair_adjoint<Eval><<<(uint32_t)((threads + ADJ_BLOCK - 1) / ADJ_BLOCK), ADJ_BLOCK, 0, s>>>(a);
+    const uint32_t blocks = (uint32_t)((threads + ADJ_BLOCK - 1) / ADJ_BLOCK);
+    if (std::is_same<Eval, PerturbedLJ>::value && !a.xplor)
+        k_pair_adjoint<PerturbedLJ, true><<<blocks, ADJ_BLOCK, 0, s>>>(a);
+    else
+        k_pair_adjoint<Eval, false><<<blocks, ADJ_BLOCK, 0, s>>>(a);
     AZP_CHECK_LAUNCH("k_pair_adjoint");
     return AZP_OK;
 }

@@ -488,6 +488,13 @@ struct azp_md {
     double* tmpd = nullptr;       // tag-order staging [N * 6]
     uint64_t launches = 0;
     bool have_state = false;
+    // host-transfer staging of azp_md_set_state / azp_md_get_state (tag order,
+    // allocated on the first host transfer and kept: no allocation per call)
+    double* st_pos = nullptr;
+    double* st_vel = nullptr;
+    double* st_acc = nullptr;
+    int* st_img = nullptr;
+    double* st_diam = nullptr;
     // entry snapshot of azp_md_run_checked (tag order, allocated on first use)
     double* snap_pos = nullptr;
     double* snap_vel = nullptr;
@@ -530,7 +537,7 @@ void free_all(azp_md* m)
                     m->cuts, m->bt_n_tag, m->bt_partner_tag, m->bt_type_tag, m->bt_n, m->bt, m->ex_n, m->ex_idx,
                     m->d_bond_params, m->d_pair_table, m->d_gamma, m->d_noise, m->flags, m->d_ts, m->out_force, m->out_virial,
                     m->partials, m->thermo, m->tmp4, m->tmpd, m->snap_pos, m->snap_vel, m->snap_acc,
-                    m->snap_img, m->snap_diam};
+                    m->snap_img, m->snap_diam, m->st_pos, m->st_vel, m->st_acc, m->st_img, m->st_diam};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -799,6 +806,19 @@ int check_errors(azp_md* m, cudaStream_t s)
     return AZP_OK;
 }
 
+// staging buffers of the host transfers (first use only)
+int ensure_staging(azp_md* m)
+{
+    if (m->st_pos) return AZP_OK;
+    const size_t N = m->N;
+    int st = dalloc(&m->st_pos, 4 * N);
+    if (!st) st = dalloc(&m->st_vel, 4 * N);
+    if (!st) st = dalloc(&m->st_acc, 3 * N);
+    if (!st) st = dalloc(&m->st_img, 3 * N);
+    if (!st) st = dalloc(&m->st_diam, N);
+    return st;
+}
+
 // device state -> tag-order FP64 arrays (either precision's state layout)
 void enqueue_store_state(azp_md* m, double* pos, double* vel, double* accel, int* image, cudaStream_t s)
 {
@@ -1053,25 +1073,20 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
     if (N == 0) return AZP_OK;
     const double *dp = pos, *dv = vel, *da = accel, *dd = diameter;
     const int* di = image;
-    std::vector<void*> tmp;
     if (!on_device) {
-        auto up = [&](const void* h, size_t bytes) -> void* {
+        int st0 = ensure_staging(m);
+        if (st0) return st0;
+        auto up = [&](const void* h, void* d, size_t bytes) -> const void* {
             if (!h) return nullptr;
-            void* d = nullptr;
-            if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
             cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s);
-            tmp.push_back(d);
             return d;
         };
-        dp = (const double*)up(pos, sizeof(double) * 4 * N);
-        dv = (const double*)up(vel, sizeof(double) * 4 * N);
-        da = (const double*)up(accel, sizeof(double) * 3 * N);
-        di = (const int*)up(image, sizeof(int) * 3 * N);
-        dd = (const double*)up(diameter, sizeof(double) * N);
-        if (!dp || !dv) {
-            for (void* p : tmp) cudaFree(p);
-            return AZP_ERR_CUDA;
-        }
+        dp = (const double*)up(pos, m->st_pos, sizeof(double) * 4 * N);
+        dv = (const double*)up(vel, m->st_vel, sizeof(double) * 4 * N);
+        da = (const double*)up(accel, m->st_acc, sizeof(double) * 3 * N);
+        di = (const int*)up(image, m->st_img, sizeof(int) * 3 * N);
+        dd = (const double*)up(diameter, m->st_diam, sizeof(double) * N);
+        AZP_CHECK_LAUNCH("azp_md_set_state (host to device)");
     }
     m->cur = 0;
     k_load_state<<<blocks_for(N, 256), 256, 0, s>>>(dp, dv, da, di, dd, N, m->pos[0], m->vel, m->accel, m->image,
@@ -1092,8 +1107,6 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         AZP_CUDA_TRY(cudaMemcpyAsync(m->flags, &one, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
         st = enqueue_rebuild(m, s, nullptr);
     }
-    AZP_CUDA_TRY(cudaStreamSynchronize(s));
-    for (void* p : tmp) cudaFree(p);
     if (st) return st;
     if (!accel && m->method == AZP_METHOD_LANGEVIN_FLOW) {
         // HOOMD starts a run from a = F / m when no acceleration is known
@@ -1126,12 +1139,12 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
         AZP_CHECK_LAUNCH("k_store_state");
         return AZP_OK;
     }
-    double *dp = nullptr, *dv = nullptr, *da = nullptr;
-    int* di = nullptr;
-    if (pos) AZP_CUDA_TRY(cudaMalloc(&dp, sizeof(double) * 4 * N));
-    if (vel) AZP_CUDA_TRY(cudaMalloc(&dv, sizeof(double) * 4 * N));
-    if (accel) AZP_CUDA_TRY(cudaMalloc(&da, sizeof(double) * 3 * N));
-    if (image) AZP_CUDA_TRY(cudaMalloc(&di, sizeof(int) * 3 * N));
+    int st0 = ensure_staging(m);
+    if (st0) return st0;
+    double* dp = pos ? m->st_pos : nullptr;
+    double* dv = vel ? m->st_vel : nullptr;
+    double* da = accel ? m->st_acc : nullptr;
+    int* di = image ? m->st_img : nullptr;
     enqueue_store_state(m, dp, dv, da, di, s);
     AZP_CHECK_LAUNCH("k_store_state");
     if (pos) AZP_CUDA_TRY(cudaMemcpyAsync(pos, dp, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, s));
@@ -1139,10 +1152,6 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
     if (accel) AZP_CUDA_TRY(cudaMemcpyAsync(accel, da, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
     if (image) AZP_CUDA_TRY(cudaMemcpyAsync(image, di, sizeof(int) * 3 * N, cudaMemcpyDeviceToHost, s));
     AZP_CUDA_TRY(cudaStreamSynchronize(s));
-    cudaFree(dp);
-    cudaFree(dv);
-    cudaFree(da);
-    cudaFree(di);
     return AZP_OK;
 }
 

@@ -77,20 +77,21 @@ AZP_D void ff_add(float& h, float& l, float k)
 // component (hi, lo). s_hi + s_lo = 2^32 / L as a float pair, so dx * 2^32 / L is
 // formed to float-float accuracy (the FMA gives the product's rounding error
 // exactly). Returns the image change (+1, -1 or 0). Sets bad (and leaves the
-// component unchanged) when dx is not finite or moves a tenth of the box or more.
+// component unchanged) when dx is not finite or moves half a box or more in one
+// step (a move the minimum-image convention cannot represent).
 AZP_D int fx_advance(uint32_t& hi, uint32_t& lo, float dx, float s_hi, float s_lo, bool& bad)
 {
     const float p = __fmul_rn(dx, s_hi);                               // units of L 2^-32
     const float e = __fadd_rn(__fmaf_rn(dx, s_hi, -p), __fmul_rn(dx, s_lo));
-    const bool ok = fabsf(p) < 429496729.6f;                           // |dx| < L / 10; false for NaN
+    const bool ok = fabsf(p) < 2147483392.0f;                          // |dx| < L / 2; false for NaN
     bad |= !ok;
     const float ip = rintf(p);
     const float t = __fadd_rn(__fsub_rn(p, ip), e);                     // p - ip is exact
     const float it = rintf(t);
     const float fr = __fsub_rn(t, it);                                   // exact, |fr| <= 1/2
-    const int32_t ih = ok ? __float2int_rn(ip) + __float2int_rn(it) : 0;
+    const int64_t ih = ok ? (int64_t)__float2int_rn(ip) + __float2int_rn(it) : 0;
     const int32_t il = ok ? __float2int_rn(__fmul_rn(fr, 2147483648.0f)) : 0;  // units of L 2^-63
-    const int64_t dq = (int64_t)((uint64_t)(int64_t)ih << 32) + (int64_t)il * 2;
+    const int64_t dq = (int64_t)((uint64_t)ih << 32) + (int64_t)il * 2;
     const int64_t q0 = fx_join(hi, lo);
     const int64_t q1 = (int64_t)((uint64_t)q0 + (uint64_t)dq);
     fx_split(q1, hi, lo);

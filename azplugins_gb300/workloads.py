@@ -107,8 +107,10 @@ def yukawa_replicas(n_replicas=256, seed=4, n_min=500, n_max=20000, rho=(0.3, 0.
                     delta=(0.0, 1.0), r_buff=0.4, kT=1.0):
     """Independent ExpandedYukawa systems of uneven size: N log-uniform in
     [n_min, n_max], density uniform in rho, kappa and delta uniform, r_cut =
-    delta + 5 / kappa. A draw whose box is smaller than 2 (r_cut + r_buff) is
-    redrawn (kappa, delta) from the same stream; the number of redraws is returned.
+    delta + 5 / kappa. A draw whose box is smaller than 2 (r_cut + r_buff), or
+    whose delta comes within 0.25 of the closest starting separation (0.9 of the
+    jittered lattice spacing; the potential diverges at r = delta), is redrawn
+    (kappa, delta) from the same stream; the number of redraws is returned.
 
     Returns (snapshots, params) with params[r] = dict(epsilon, kappa, delta, r_cut)."""
     rng = _rng(seed)
@@ -118,11 +120,12 @@ def yukawa_replicas(n_replicas=256, seed=4, n_min=500, n_max=20000, rho=(0.3, 0.
         N = int(round(np.exp(rng.uniform(np.log(n_min), np.log(n_max)))))
         density = rng.uniform(*rho)
         L = (N / density) ** (1.0 / 3.0)
+        closest = 0.9 * L / int(np.ceil(N ** (1.0 / 3.0)))
         while True:
             k = rng.uniform(*kappa)
             d = rng.uniform(*delta)
             rc = d + 5.0 / k
-            if L >= 2.0 * (rc + r_buff):
+            if L >= 2.0 * (rc + r_buff) and d <= closest - 0.25:
                 break
             redraws += 1
         s = Snapshot(N)
@@ -139,9 +142,11 @@ def yukawa_replicas(n_replicas=256, seed=4, n_min=500, n_max=20000, rho=(0.3, 0.
 def colloid_mixture(N=262144, colloid_fraction=0.04, colloid_diameter=5.0, solvent_diameter=1.0, phi=0.3, seed=3,
                     kT=1.0):
     """Binary colloid (type C) / solvent (type S) mixture at total volume fraction
-    phi, placed without overlaps: colloids by random sequential addition at
-    centre distance >= colloid_diameter, solvent on a jittered grid of spacing
-    1.1 solvent diameters outside the colloids' exclusion shells."""
+    phi, placed without overlaps: colloids on randomly chosen sites of a simple
+    cubic lattice, each jittered so that surface gaps stay at least 0.4 solvent
+    diameters (colloids at contact would start at a diverging colloid-colloid
+    force), then solvent on a jittered grid of spacing 1.1 solvent diameters
+    outside the colloids' exclusion shells."""
     rng = _rng(seed)
     nc = int(round(colloid_fraction * N))
     ns = N - nc
@@ -149,37 +154,18 @@ def colloid_mixture(N=262144, colloid_fraction=0.04, colloid_diameter=5.0, solve
     vol = (4.0 / 3.0) * np.pi * (nc * ac ** 3 + ns * as_ ** 3)
     L = (vol / phi) ** (1.0 / 3.0)
     box = np.array([L, L, L])
-    # colloids: random sequential addition on a cell hash
-    cell = colloid_diameter
-    nb = max(1, int(L // cell))
-    w = L / nb
-    grid = {}
-    cols = []
-    while len(cols) < nc:
-        cand = rng.uniform(-0.5 * L, 0.5 * L, size=(4096, 3))
-        for x in cand:
-            c = tuple(((x + 0.5 * L) // w).astype(int) % nb)
-            ok = True
-            for ox in (-1, 0, 1):
-                for oy in (-1, 0, 1):
-                    for oz in (-1, 0, 1):
-                        for j in grid.get(((c[0] + ox) % nb, (c[1] + oy) % nb, (c[2] + oz) % nb), ()):
-                            dd = x - cols[j]
-                            dd -= L * np.rint(dd / L)
-                            if dd @ dd < colloid_diameter ** 2:
-                                ok = False
-                                break
-                        if not ok:
-                            break
-                    if not ok:
-                        break
-                if not ok:
-                    break
-            if ok:
-                grid.setdefault(c, []).append(len(cols))
-                cols.append(x)
-                if len(cols) == nc:
-                    break
+    cols = np.zeros((0, 3))
+    if nc:
+        m = int(np.ceil(nc ** (1.0 / 3.0)))
+        a = L / m
+        gap = a - colloid_diameter
+        if gap < 0.4 * solvent_diameter:
+            raise ValueError("colloid lattice too tight for this volume fraction")
+        jit = 0.5 * (gap - 0.4 * solvent_diameter)
+        site = (np.arange(m) + 0.5) * a - 0.5 * L
+        X, Y, Z = np.meshgrid(site, site, site, indexing="ij")
+        sites = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+        cols = sites[rng.permutation(len(sites))[:nc]] + rng.uniform(-jit, jit, size=(nc, 3))
     cols = np.array(cols).reshape(-1, 3)
     # solvent: jittered grid points outside the colloid shells
     sp = 1.1 * solvent_diameter

@@ -18,8 +18,9 @@ Each suite prints one JSON line:
   checkpoints every 10.
 * ``precision``: the colloid-solvent mixture (N = 262,144, 4 % colloids of
   diameter 5, phi = 0.3, Hamaker A_SS = 144, A_CS = 100, A_CC = 40, r_cut 3 / 6 / 10;
-  BrownianFlow, ConstantFlow U = 0.1 x, dt = 0.001) -- FP32-compensated against FP64
-  forces, energy and virial along an FP64 Brownian trajectory.
+  BrownianFlow, ConstantFlow U = 0.1 x, dt = 0.001, drag gamma = 10 diameter) --
+  FP32-compensated against FP64 forces, energy and virial every 500 steps along the
+  FP32-force Brownian trajectory.
 """
 
 from __future__ import annotations
@@ -113,9 +114,9 @@ def suite_batched(args):
     b.run(50)  # warm-up
     steps = args.steps if args.steps != 2000 else 500
     ms = _cuda_ms(lambda: b.run(steps, check=False))
+    launches = b.last_launches
     b.run(0)
     batched = 256 * steps / (ms * 1e-3)
-    launches = b.last_launches
     b.close()
     # the same replicas one after the other, plain stream launches
     os.environ["AZP_GRAPHS"] = "0"
@@ -173,12 +174,37 @@ def suite_adjoint(args):
     def loss_fn(F, U):
         return ((F - Ft) ** 2).sum(dim=1).mean() + (U.sum() - Ut) ** 2
 
-    # cost: forward kernel alone vs adjoint kernel alone (same list)
+    # cost through torch autograd (Python, table set-up and reductions included)
     F, U = autodiff.pair_forces(x, vals, ctx)
     loss = loss_fn(F, U)
     gF, gU = torch.autograd.grad(loss, (F, U), retain_graph=True)
+    # one untimed call of each first (library handles, first use of torch ops)
+    autodiff.pair_forces(x.detach(), vals.detach(), ctx)
+    torch.autograd.grad((F, U), (x, vals), (gF, gU), retain_graph=True)
     fwd = _cuda_ms(lambda: autodiff.pair_forces(x.detach(), vals.detach(), ctx), reps=20)
     bwd = _cuda_ms(lambda: torch.autograd.grad((F, U), (x, vals), (gF, gU), retain_graph=True), reps=20)
+    # cost of the kernels alone through the C ABI: the forward pair driver and
+    # the adjoint driver on the same list, CUDA events on the launching stream
+    from azplugins_gb300 import _lib
+
+    L = _lib.load()
+    nl = ctx.neighbor_list(x)
+    pos4 = ctx.pos4(x)
+    sysd = ctx.system(pos4)
+    params, rc, ro = autodiff._pair_tables(ctx, vals.detach())
+    force = torch.empty((ctx.N, 4), dtype=torch.float64, device="cuda")
+    out = _lib.Forces()
+    out.force, out.virial, out.virial_pitch, out.precision = force.data_ptr(), None, ctx.N, _lib.FP64
+    grad = torch.cat([gF, gU[:, None]], dim=1).contiguous()
+    gpos = torch.empty((ctx.N, 3), dtype=torch.float64, device="cuda")
+    grec = torch.empty((ctx.N, 4), dtype=torch.float64, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    mode = _lib.MODES[pot.mode]
+    k_fwd = _cuda_ms(lambda: L.azp_pair_forces(ctypes.byref(sysd), nl.handle, pot.kind, params.data_ptr(), rc.data_ptr(),
+                                                ro.data_ptr(), mode, ctypes.byref(out), stream), reps=50)
+    k_adj = _cuda_ms(lambda: L.azp_pair_adjoint(ctypes.byref(sysd), nl.handle, pot.kind, params.data_ptr(),
+                                                 rc.data_ptr(), ro.data_ptr(), mode, grad.data_ptr(), gpos.data_ptr(),
+                                                 grec.data_ptr(), stream), reps=50)
     gx, gv = torch.autograd.grad(loss, (x, vals))
     h = 1e-6
     fd_err = []
@@ -189,14 +215,23 @@ def suite_adjoint(args):
             vm[k] -= h
             fd = (loss_fn(*autodiff.pair_forces(x.detach(), vp, ctx)) - loss_fn(*autodiff.pair_forces(x.detach(), vm, ctx))) / (2 * h)
         fd_err.append(abs(float(gv[k]) - float(fd)) / abs(float(fd)))
-    # through K Langevin steps with checkpoints every 10
+    # through K Langevin steps with checkpoints every 10. Finite differences of
+    # a trajectory loss are only meaningful when the forces are continuous in
+    # r: the rollout uses the xplor form (forces smoothed to zero between
+    # r_on = 2.5 and r_cut = 3), so no pair crossing r_cut makes the loss jump.
     K = 100
     x0 = x.detach()
     v0 = torch.tensor(snap.particles.velocity, dtype=torch.float64, device="cuda")
+    pot_s = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), mode="xplor")
+    ctx_s = autodiff.Context(pot_s, snap.particles.types, snap.particles.typeid, snap.configuration.box, 3.0,
+                             r_on=2.5)
+    with torch.no_grad():
+        Fts, Uts = autodiff.pair_forces(x0, valst, ctx_s)
+        Uts = Uts.sum()
 
     def roll(v):
-        xx, vv, FF, UU = autodiff.langevin_rollout(x0, v0, v, ctx, K, 0.005, seed=9, checkpoint_every=10)
-        return loss_fn(FF, UU)
+        xx, vv, FF, UU = autodiff.langevin_rollout(x0, v0, v, ctx_s, K, 0.005, seed=9, checkpoint_every=10)
+        return ((FF - Fts) ** 2).sum(dim=1).mean() + (UU.sum() - Uts) ** 2
 
     t0 = time.perf_counter()
     lossK = roll(vals)
@@ -206,26 +241,26 @@ def suite_adjoint(args):
     (gK,) = torch.autograd.grad(lossK, (vals,))
     torch.cuda.synchronize()
     t_bwd = time.perf_counter() - t0
-    roll_err = []
+    roll_err, roll_err_small = [], []
     for k in range(3):
-        with torch.no_grad():
-            vp, vm = vals.detach().clone(), vals.detach().clone()
-            vp[k] += h
-            vm[k] -= h
-            fd = (roll(vp) - roll(vm)) / (2 * h)
-        roll_err.append(abs(float(gK[k]) - float(fd)) / abs(float(fd)))
+        for hh, errs in ((h, roll_err), (0.1 * h, roll_err_small)):
+            with torch.no_grad():
+                vp, vm = vals.detach().clone(), vals.detach().clone()
+                vp[k] += hh
+                vm[k] -= hh
+                fd = (roll(vp) - roll(vm)) / (2 * hh)
+            errs.append(abs(float(gK[k]) - float(fd)) / abs(float(fd)))
     line = {"suite": "adjoint", "workload": "PerturbedLJ fluid N=65536 rho=0.8 r_cut=3 shift; learn (eps, sigma, lambda)",
             "forward_ms": fwd, "adjoint_ms": bwd, "adjoint_over_forward": bwd / fwd,
+            "kernel_forward_ms": k_fwd, "kernel_adjoint_ms": k_adj, "kernel_adjoint_over_forward": k_adj / k_fwd,
             "single_call_fd_rel_error": fd_err, "rollout_steps": K, "checkpoint_every": 10,
-            "rollout_forward_s": t_fwd, "rollout_backward_s": t_bwd, "rollout_fd_rel_error": roll_err,
+            "rollout_forward_s": t_fwd, "rollout_backward_s": t_bwd, "rollout_fd_rel_error": roll_err, "rollout_fd_rel_error_h_1e-7": roll_err_small,
             "fd_step": h, "precision": "f64"}
     print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------- precision study
 def suite_precision(args):
-    import torch
-
     import azplugins_gb300 as az
     from azplugins_gb300 import _compute, workloads
     from tests.helpers import force_error
@@ -243,10 +278,15 @@ def suite_precision(args):
         c.r_cut[("C", "C")] = 10.0
         return c
 
-    sim = az.Simulation(seed=3, precision="fp64")
+    # the trajectory: FP32 compensated forces, 64-bit integration; Stokes-like
+    # drag gamma = 10 diameter (the reference's use_lambda with lambda = 10): a
+    # solvent bead's Brownian step sqrt(2 kT dt / gamma) = 0.014 stays well inside
+    # its repulsive core (at gamma = 1 the kicks drive beads into the cores and
+    # the trajectory blows up at this dt)
+    sim = az.Simulation(seed=3, precision="fp32")
     sim.create_state_from_snapshot(snap)
     pot = colloid()
-    m = az.methods.BrownianFlow("all", kT=1.0, flow_field=az.flow.ConstantFlow((0.1, 0.0, 0.0)), default_gamma=1.0)
+    m = az.methods.BrownianFlow("all", kT=1.0, flow_field=az.flow.ConstantFlow((0.1, 0.0, 0.0)), alpha=10.0)
     sim.operations.integrator = az.md.Integrator(dt=0.001, methods=[m], forces=[pot])
     total = 5000 if args.steps == 2000 else args.steps
     every = max(total // 10, 1)
@@ -265,19 +305,23 @@ def suite_precision(args):
                      "force_error_colloid": force_error(f32[typ == 1], f64[typ == 1]),
                      "energy_rel_error": abs(f32[:, 3].sum() - f64[:, 3].sum()) / abs(f64[:, 3].sum()),
                      "virial_rel_error": float(np.abs(w32.sum(axis=0) - w64.sum(axis=0)).max() /
-                                               np.abs(w64.sum(axis=0)).max())})
+                                               np.abs(w64.sum(axis=0)).max()),
+                     "max_force": float(np.sqrt((f64[:, :3] ** 2).sum(axis=1)).max())})
         if done >= total:
             break
         t0 = time.perf_counter()
         sim.run(every)
         t_run += time.perf_counter() - t0
         done += every
+    finite = all(np.isfinite([r["force_error"], r["energy_rel_error"], r["virial_rel_error"]]).all() for r in rows)
     line = {"suite": "precision", "workload": f"colloid mixture N={N}, 4% colloids (d=5), phi=0.3, BrownianFlow "
-                                              f"U=0.1x dt=0.001, {total} steps (FP64 trajectory)",
-            "samples": rows, "max_force_error": max(r["force_error"] for r in rows),
+                                              f"U=0.1x dt=0.001 gamma=10 diameter, {total} steps (FP32-force trajectory)",
+            "samples": rows, "all_finite": bool(finite),
+            "max_force_error": max(r["force_error"] for r in rows),
             "max_energy_rel_error": max(r["energy_rel_error"] for r in rows),
             "max_virial_rel_error": max(r["virial_rel_error"] for r in rows),
-            "fp64_brownian_timesteps_per_s": total / t_run if t_run else None}
+            "reference": "FP64 drivers (equal to the FP64 oracle to 1e-12, tests/test_gpu_pair.py)",
+            "fp32_brownian_timesteps_per_s": total / t_run if t_run else None}
     print(json.dumps(line), flush=True)
 
 
