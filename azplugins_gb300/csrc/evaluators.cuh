@@ -141,6 +141,21 @@ struct Colloid {
     {
         const R A = rec[0], s3 = rec[3], s6 = rec[4];
         const int form = (int)rec[5];
+        if constexpr (std::is_same<R, float>::value) {
+            // The point-sphere and sphere-sphere forms subtract nearly equal terms
+            // (poly s6 / d6 - 5; h0 - h1 - h2 + h3 and log(q8 / q7)), so their FP32
+            // evaluation loses most of its digits near the potential's minimum:
+            // the FP32 path evaluates them in FP64 and rounds the result once.
+            if (form != 0) {
+                double rd[PAIR_REC];
+                for (int k = 0; k < PAIR_REC; ++k) rd[k] = (double)rec[k];
+                double f, u;
+                eval<double>(rd, (double)rsq, f, u);
+                fdr = (float)f;
+                e = (float)u;
+                return;
+            }
+        }
         if (form == 0) {
             // integrated over no sphere: LJ with prefactor A/36
             const R r2inv = rcp(rsq);

@@ -362,6 +362,8 @@ def run_ours(args):
     state_after = sim.state.get_snapshot()
     n_nbr, n_bond = neighbour_stats(state_after)
     log("neighbour statistics done")
+    accuracy = force_accuracy(az, eng, state_after, args.precision)
+    log("force accuracy done")
     # end to end through the public C ABI with pinned host buffers
     torch.cuda.nvtx.range_push("e2e")
     e2e = e2e_measure(eng, state_after, args.e2e_steps)
@@ -399,6 +401,7 @@ def run_ours(args):
                          "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "mean_neighbours": n_nbr,
                          "mean_bonds": n_bond},
             "clocks": clk.summary(),
+            "accuracy": accuracy,
             "e2e": e2e,
         }
         if not args.no_cpu_baseline:
@@ -435,6 +438,27 @@ def neighbour_stats(s):
     st, _ = nl.to_csr()
     nl.close()
     return float(st[-1]) / N, 2.0 * s.bonds.N / N
+
+
+def force_accuracy(az, eng, snap, precision):
+    """The engine's forces (pair + bond, its own precision and list) at the state
+    after the timed run against the FP64 drop-in drivers at the same positions
+    (tests/test_gpu_pair.py holds those to 1e-12 of the FP64 oracle):
+    max_i |dF_i| / max(|F_i|, F_rms) and the relative error of the total energy."""
+    from azplugins_gb300 import _compute
+    from tests.helpers import force_error
+
+    f_eng, _ = eng.forces()
+    ref = az.Simulation(precision="fp64")
+    ref.create_state_from_snapshot(snap)
+    wca, qb = forces_and_method(az, None)
+    fp, _ = _compute.pair_forces(ref.state, wca, "fp64")
+    fb, _ = _compute.bond_forces(ref.state, qb, "fp64")
+    f64 = fp + fb
+    return {"forces": precision, "reference": "FP64 drivers at the same state",
+            "force_error": force_error(f_eng, f64),
+            "energy_rel_error": abs(f_eng[:, 3].sum() - f64[:, 3].sum()) / abs(f64[:, 3].sum()),
+            "norm": "max_i |dF_i| / max(|F_i|, F_rms)"}
 
 
 def time_step_kernel(eng, reps):
