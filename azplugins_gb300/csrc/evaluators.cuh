@@ -21,13 +21,15 @@ namespace azp
 constexpr int PAIR_REC = 8;   // values per pair kernel record
 constexpr int CUT_REC = 4;    // rcutsq, ronsq, 1/(rcutsq-ronsq)^3, xplor flag
 
-// reciprocal: FP64 correctly rounded; FP32 the hardware approximation (within
-// about 1 ulp, far inside the FP32 force budget of 1e-5 relative)
+// correctly rounded reciprocal; the FP32 form maps to the hardware-assisted
+// rounded reciprocal instead of a full division (an approximate reciprocal's
+// extra ulp, raised to the 12th power by the LJ core, costs too much of the
+// FP32 force budget at overlapped pairs)
 AZP_HD double rcp(double x) { return 1.0 / x; }
 AZP_HD float rcp(float x)
 {
 #ifdef __CUDA_ARCH__
-    return __fdividef(1.0f, x);
+    return __frcp_rn(x);
 #else
     return 1.0f / x;
 #endif
@@ -141,21 +143,6 @@ struct Colloid {
     {
         const R A = rec[0], s3 = rec[3], s6 = rec[4];
         const int form = (int)rec[5];
-        if constexpr (std::is_same<R, float>::value) {
-            // The point-sphere and sphere-sphere forms subtract nearly equal terms
-            // (poly s6 / d6 - 5; h0 - h1 - h2 + h3 and log(q8 / q7)), so their FP32
-            // evaluation loses most of its digits near the potential's minimum:
-            // the FP32 path evaluates them in FP64 and rounds the result once.
-            if (form != 0) {
-                double rd[PAIR_REC];
-                for (int k = 0; k < PAIR_REC; ++k) rd[k] = (double)rec[k];
-                double f, u;
-                eval<double>(rd, (double)rsq, f, u);
-                fdr = (float)f;
-                e = (float)u;
-                return;
-            }
-        }
         if (form == 0) {
             // integrated over no sphere: LJ with prefactor A/36
             const R r2inv = rcp(rsq);
@@ -325,13 +312,13 @@ struct QuarticBond {
             const float r2inv = rcp(rs * rs);
             const float r6inv = r2inv * r2inv * r2inv;
             if (lj1 != 0.0f && r6inv > q[8]) {
-                fdr += __fdividef(r6inv * (12.0f * lj1 * r6inv - 6.0f * lj2), rs * (rs + del));
+                fdr += r6inv * (12.0f * lj1 * r6inv - 6.0f * lj2) / (rs * (rs + del));
                 e += r6inv * (lj1 * r6inv - lj2) + q[9];
             }
             if (rs < r0) rr = rs - r0;
         }
         if (rr < 0.0f) {
-            fdr += __fdividef(-k * rr * (4.0f * rr * rr - q[10] * rr + q[11]), rr + r0 + del);
+            fdr += -k * rr * (4.0f * rr * rr - q[10] * rr + q[11]) / (rr + r0 + del);
             e += k * (rr - b1) * (rr - b2) * rr * rr + q[4];
         } else {
             e += q[4];
