@@ -209,6 +209,13 @@ def algorithmic_bytes(n_nbr_mean, n_bond_mean, precision="fp32"):
     return 16 + 4 + 4 * n_nbr_mean + 4 + 8 * n_bond_mean + 32 + 32 + 4 + 16 + 32 + 32 + 16
 
 
+# DRAM traffic of one FP32-force fused step per particle, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on the melt at
+# N = 700,000, whose step traffic and resident set exceed L2
+# (profiles/k_md_step_fx_melt700k.md); scaled to a launch by N
+TRAFFIC_BYTES_PER_PARTICLE_FP32 = 196.9
+
+
 def measured_peak():
     path = os.path.join(HERE, "MEASURED_PEAKS.json")
     try:
@@ -396,7 +403,9 @@ def run_ours(args):
             "nlist_builds_per_step": builds / args.steps,
             "pair_interactions_per_s": None,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": ("k_md_step_fx" if args.precision == "fp32" else "k_md_step") + " (fused forces + Langevin step)",
+                         "traffic": (TRAFFIC_BYTES_PER_PARTICLE_FP32 * N if args.precision == "fp32" else None),
+                         "traffic_source": "ncu capture at N=700,000 scaled by N (profiles/k_md_step_fx_melt700k.md)",
+                         "kernel": ("k_md_step_fx" if args.precision == "fp32" else "k_md_step") + " (fused forces + Langevin step)",
                          "kernel_ms": kernel_ms, "bytes_per_launch": bytes_per_launch,
                          "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "mean_neighbours": n_nbr,
                          "mean_bonds": n_bond},
