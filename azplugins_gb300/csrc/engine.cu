@@ -390,6 +390,44 @@ __global__ void k_load_state(const double* __restrict__ pos_in, const double* __
     rtag[i] = i;
 }
 
+// tag-order input -> device state in the engine's current index order (particle
+// i takes the input row of its tag); tag / rtag are kept
+__global__ void k_load_state_ordered(const double* __restrict__ pos_in, const double* __restrict__ vel_in,
+                                     const double* __restrict__ accel_in, const int* __restrict__ image_in,
+                                     const double* __restrict__ diam_in, const uint32_t* __restrict__ tag, uint32_t N,
+                                     double4_32a* __restrict__ pos, double4_32a* __restrict__ vel,
+                                     double* __restrict__ accel, int* __restrict__ image, double* __restrict__ diam)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const uint32_t t = tag[i];
+    pos[i] = make_double4_32a(pos_in[4 * t], pos_in[4 * t + 1], pos_in[4 * t + 2],
+                              type_as_double((uint32_t)pos_in[4 * t + 3]));
+    vel[i] = make_double4_32a(vel_in[4 * t], vel_in[4 * t + 1], vel_in[4 * t + 2], vel_in[4 * t + 3]);
+    for (int d = 0; d < 3; ++d) {
+        accel[3 * i + d] = accel_in ? accel_in[3 * t + d] : 0.0;
+        image[3 * i + d] = image_in ? image_in[3 * t + d] : 0;
+    }
+    if (diam) diam[i] = diam_in ? diam_in[t] : 1.0;
+}
+
+// rebuild request when a particle of the loaded state lies more than r_buff / 2
+// from its position at the last list build (the step kernels' criterion)
+__global__ void k_request_if_displaced(const uint4* __restrict__ fix, const uint4* __restrict__ fix_build, uint32_t N,
+                                       float s0, float s1, float s2, float thresh2, uint32_t* __restrict__ flags)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool want = false;
+    if (i < N) {
+        const uint4 f = fix[i], fb = fix_build[i];
+        const float dx = (float)(int32_t)(f.x - fb.x) * s0;
+        const float dy = (float)(int32_t)(f.y - fb.y) * s1;
+        const float dz = (float)(int32_t)(f.z - fb.z) * s2;
+        want = dx * dx + dy * dy + dz * dz > thresh2;
+    }
+    if (__any_sync(0xffffffffu, want) && (threadIdx.x & 31) == 0) atomicOr(&flags[0], 1u);
+}
+
 // device state -> tag order output (pos w = type as an integer-valued double)
 __global__ void k_store_state(const double4_32a* __restrict__ pos, const double4_32a* __restrict__ vel,
                               const double* __restrict__ accel, const int* __restrict__ image,
@@ -1089,25 +1127,57 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         AZP_CHECK_LAUNCH("azp_md_set_state (host to device)");
     }
     m->cur = 0;
-    k_load_state<<<blocks_for(N, 256), 256, 0, s>>>(dp, dv, da, di, dd, N, m->pos[0], m->vel, m->accel, m->image,
-                                                     m->diam, m->tag, m->rtag);
-    AZP_CHECK_LAUNCH("k_load_state");
-    if (m->precision == AZP_FP32) {
-        k_state_to_fx<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[0], m->vel, m->fix[0], m->lo[0], m->mass, N,
-                                                          1.0 / m->box.L[0], 1.0 / m->box.L[1], 1.0 / m->box.L[2]);
-        AZP_CHECK_LAUNCH("k_state_to_fx");
-    }
     m->timestep = timestep;
     const unsigned long long ts = timestep;
     AZP_CUDA_TRY(cudaMemcpyAsync(m->d_ts, &ts, sizeof(ts), cudaMemcpyHostToDevice, s));
     AZP_CUDA_TRY(cudaMemsetAsync(m->flags, 0, sizeof(uint32_t) * 8, s));
-    int st = size_list(m, s);  // unconditional first rebuild (sorts the particles)
-    if (st == AZP_OK && m->pair_kind < 0) {
-        const uint32_t one = 1u;
-        AZP_CUDA_TRY(cudaMemcpyAsync(m->flags, &one, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-        st = enqueue_rebuild(m, s, nullptr);
+    int st = AZP_OK;
+    bool placed = false;
+    if (m->have_state) {
+        // Keep the current particle order and list: load the new state in index
+        // order and rebuild only if some particle lies more than r_buff / 2 from
+        // its position at the last build (a state read back from this engine and
+        // set again moves nothing). A denser new state that overflows the list
+        // takes the full path below.
+        k_load_state_ordered<<<blocks_for(N, 256), 256, 0, s>>>(dp, dv, da, di, dd, m->tag, N, m->pos[0], m->vel,
+                                                                 m->accel, m->image, m->diam);
+        AZP_CHECK_LAUNCH("k_load_state_ordered");
+        if (m->precision == AZP_FP32) {
+            k_state_to_fx<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[0], m->vel, m->fix[0], m->lo[0], m->mass, N,
+                                                              1.0 / m->box.L[0], 1.0 / m->box.L[1], 1.0 / m->box.L[2]);
+            AZP_CHECK_LAUNCH("k_state_to_fx");
+        } else {
+            launch_to_fixed(m->pos[0], m->fix[0], N, m->box, s);
+        }
+        const MDArgs a = base_args(m);
+        k_request_if_displaced<<<blocks_for(N, 256), 256, 0, s>>>(m->fix[0], m->fix_build, N, a.sfix[0], a.sfix[1],
+                                                                   a.sfix[2], a.disp_thresh2, m->flags);
+        AZP_CHECK_LAUNCH("k_request_if_displaced");
+        st = enqueue_rebuild(m, s, m->flags);
+        if (st) return st;
+        uint32_t f3 = 0;
+        AZP_CUDA_TRY(cudaMemcpyAsync(&f3, m->flags + 3, sizeof(f3), cudaMemcpyDeviceToHost, s));
+        AZP_CUDA_TRY(cudaStreamSynchronize(s));
+        placed = f3 <= m->max_nn;
+        if (!placed) AZP_CUDA_TRY(cudaMemsetAsync(m->flags, 0, sizeof(uint32_t) * 8, s));
     }
-    if (st) return st;
+    if (!placed) {
+        k_load_state<<<blocks_for(N, 256), 256, 0, s>>>(dp, dv, da, di, dd, N, m->pos[0], m->vel, m->accel, m->image,
+                                                         m->diam, m->tag, m->rtag);
+        AZP_CHECK_LAUNCH("k_load_state");
+        if (m->precision == AZP_FP32) {
+            k_state_to_fx<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[0], m->vel, m->fix[0], m->lo[0], m->mass, N,
+                                                              1.0 / m->box.L[0], 1.0 / m->box.L[1], 1.0 / m->box.L[2]);
+            AZP_CHECK_LAUNCH("k_state_to_fx");
+        }
+        st = size_list(m, s);  // unconditional rebuild (sorts the particles)
+        if (st == AZP_OK && m->pair_kind < 0) {
+            const uint32_t one = 1u;
+            AZP_CUDA_TRY(cudaMemcpyAsync(m->flags, &one, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+            st = enqueue_rebuild(m, s, nullptr);
+        }
+        if (st) return st;
+    }
     if (!accel && m->method == AZP_METHOD_LANGEVIN_FLOW) {
         // HOOMD starts a run from a = F / m when no acceleration is known
         MDArgs a = base_args(m);
@@ -1298,6 +1368,9 @@ int azp_md_run_checked(azp_md* m, uint64_t steps, void* stream)
         if (st) return st;
         free_graphs(m);
         AZP_CUDA_TRY(cudaMemsetAsync(m->flags + 1, 0, sizeof(uint32_t) * 3, s));
+        // the regrown list holds nothing yet: replay through the full set-up path
+        // (sort and build), not the order-keeping one
+        m->have_state = false;
         st = azp_md_set_state(m, m->snap_pos, m->snap_vel, m->snap_acc, m->snap_img, m->snap_diam, ts0, 1, stream);
         if (st) return st;
         m->launches = 0;

@@ -333,3 +333,69 @@ def test_large_system_forces_after_run(orc, precision, tol):
     assert force_error(f, F) < tol
     assert rel(f[:, 3].sum(), U.sum()) < max(tol, 1e-12)
     assert sim.thermo()["nlist_builds"] >= 2
+
+
+# ---------------------------------------------------------------- state set on a running engine
+# azp_md_set_state on an engine that holds a state keeps its particle order and
+# list, rebuilding only if a particle lies more than r_buff / 2 from its position
+# at the last build; a denser state that overflows the list takes the full path.
+
+
+def _engine_roundtrip(sim):
+    s = sim.state.get_snapshot()
+    sim.state.set_snapshot(s)
+
+
+def test_state_round_trip_continues_bitwise_fp64():
+    from azplugins_gb300 import workloads
+
+    snap = workloads.lj_fluid(n_side=10, density=0.8, seed=37)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    runs = []
+    for roundtrip in (False, True):
+        sim, lj = _lj_setup(snap)
+        sim.run(30)
+        if roundtrip:
+            _engine_roundtrip(sim)
+        sim.run(30)
+        runs.append(sim.state.get_snapshot().particles)
+    a, b = runs
+    assert np.array_equal(a.position, b.position)
+    assert np.array_equal(a.velocity, b.velocity)
+    assert np.array_equal(a.image, b.image)
+
+
+def test_state_set_far_from_last_build_rebuilds(orc):
+    snap = random_fluid(3000, 0.8, seed=38)
+    sim, lj = _lj_setup(snap, rcut=2.5)
+    sim.run(5)
+    other = random_fluid(3000, 0.8, seed=39)  # same N and box, unrelated positions
+    other.particles.acceleration = np.zeros((3000, 3))
+    sim.state.set_snapshot(other)
+    sim.run(1)
+    s = sim.state.get_snapshot()
+    f, w = sim._engine.forces()
+    F, U, W = _oracle_lj(orc, s, rcut=2.5).forces()
+    assert force_error(f, F) < 1e-12
+
+
+def test_state_set_denser_overflows_to_full_path(orc):
+    import azplugins_gb300 as az
+
+    snap = random_fluid(4000, 0.3, seed=40, min_dist=1.0)
+    sim, lj = _lj_setup(snap, rcut=2.5, dt=1e-5)
+    sim.run(3)
+    # the same particles squeezed into a third of the box: three times the
+    # density, more neighbours than the list was sized for
+    dense = sim.state.get_snapshot()
+    p = dense.particles
+    L = box_of(dense)
+    p.position = p.position.copy()
+    p.position[:, 0] = p.position[:, 0] / 3.0 - L[0] / 3.0
+    p.image = np.zeros_like(p.image)
+    sim.state.set_snapshot(dense)
+    sim.run(1)
+    s = sim.state.get_snapshot()
+    f, w = sim._engine.forces()
+    F, U, W = _oracle_lj(orc, s, rcut=2.5).forces()
+    assert force_error(f, F) < 1e-12
