@@ -470,6 +470,7 @@ struct azp_md {
     FlowD flow{};
     azp_box box{};
     std::vector<double> pair_params, r_cut, r_on, bond_params, gamma;
+    std::vector<double> pair_table_host, noise_host;  // the device tables, kept for the step arguments
     // device state
     double4_32a* pos[2] = {nullptr, nullptr};
     uint4* fix[2] = {nullptr, nullptr};
@@ -650,6 +651,17 @@ MDArgs base_args(azp_md* m)
     a.lambdaf = (float)m->lambda;
     a.fcapf = (float)m->fcap;
     a.max_dispf = (float)m->max_disp;
+    // single-type systems: type pair 0, bond type 0 and type 0 as kernel arguments
+    a.one_type = (m->ntypes == 1 && m->nbt <= 1 && !m->use_lambda) ? 1 : 0;
+    for (int k = 0; k < MD_PAIR_TBL; ++k)
+        a.rec0[k] = m->pair_table_host.empty() ? 0.0f : (float)m->pair_table_host[k];
+    a.rc2_0 = m->pair_table_host.empty() ? 0.0 : m->pair_table_host[PAIR_REC];
+    for (int k = 0; k < MD_BOND_F; ++k) a.bond0[k] = 0.0f;
+    if (m->bond_kind == AZP_BOND_QUARTIC && !m->bond_params.empty()) QuarticBond::prepare_f(m->bond_params.data(), a.bond0);
+    if (m->bond_kind == AZP_BOND_DOUBLE_WELL && !m->bond_params.empty())
+        DoubleWellBond::prepare_f(m->bond_params.data(), a.bond0);
+    a.gamma0 = m->gamma.empty() ? 0.0f : (float)m->gamma[0];
+    a.noise0 = m->noise_host.empty() ? 0.0f : (float)m->noise_host[0];
     a.flowf.kind = m->flow.kind;
     if (m->flow.kind == AZP_FLOW_PARABOLIC) {
         a.flowf.a = (float)m->flow.a;
@@ -1021,6 +1033,7 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         if (!c->noiseless)
             for (uint32_t t = 0; t < c->ntypes; ++t) noise[t] = std::sqrt(6.0 * m->gamma[t] * c->kT / c->dt);
         CTRY(cudaMemcpy(m->d_noise, noise.data(), sizeof(double) * c->ntypes, cudaMemcpyHostToDevice));
+        m->noise_host = noise;
     }
     // pair table + list thresholds + cell grid
     if (m->pair_kind >= 0) {
@@ -1030,6 +1043,7 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         if (st) return fail(st, m);
         ALLOC(m->d_pair_table, table.size());
         CTRY(cudaMemcpy(m->d_pair_table, table.data(), sizeof(double) * table.size(), cudaMemcpyHostToDevice));
+        m->pair_table_host = table;
         std::vector<ListCut> cuts(nt2);
         make_list_cuts(m->r_cut.data(), c->ntypes, m->r_buff, m->box, cuts.data(), &m->rlist_max, &m->rlist_min);
         for (int d = 0; d < 3; ++d)

@@ -7,7 +7,10 @@
 
 namespace azp
 {
-// MODE bits of the fused step kernel
+// sizes of the FP32 records carried in MDArgs (PAIR_TBL and BOND_F of
+// evaluators.cuh / pair.cuh; checked there)
+constexpr int MD_PAIR_TBL = 12;
+constexpr int MD_BOND_F = 12;
 
 struct MDArgs {
     const double4_32a* pos;     // current positions
@@ -67,6 +70,14 @@ struct MDArgs {
     double l64[3];              // L * 2^-64 (exact cutoff decisions near r_cut)
     float dtf, kTf, lambdaf, fcapf, max_dispf;
     FlowF flowf;
+    // single-type systems (one particle type, at most one bond type): the FP32
+    // records of type pair 0 and bond type 0, r_cut^2 and the drag / noise of
+    // type 0 as kernel arguments, read from the constant bank in the step
+    int one_type;
+    float rec0[MD_PAIR_TBL];
+    float bond0[MD_BOND_F];
+    double rc2_0;
+    float gamma0, noise0;
 };
 
 constexpr int MD_INTEG_LANGEVIN = 0;

@@ -15,6 +15,7 @@
 
 namespace azp
 {
+static_assert(MD_PAIR_TBL == PAIR_TBL && MD_BOND_F == BOND_F, "record sizes of MDArgs");
 constexpr int MD_BLOCK = 256;
 constexpr uint32_t MD_MAX_BOND_TYPES = 32;
 
@@ -456,7 +457,9 @@ constexpr int FX_BATCH = AZP_FX_BATCH;
 #define AZP_FX_MIN_BLOCKS 4
 #endif
 
-template<class PE, class BE, int INTEG, bool OUT>
+// ONE: single-type system, records from the kernel arguments (no shared-memory
+// tables, no block barrier before the work)
+template<class PE, class BE, int INTEG, bool OUT, bool ONE>
 __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -466,20 +469,28 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
     float* s_bond = s_rec + nt2 * PAIR_TBL;
     float* s_gamma = s_bond + a.nbondtypes * BOND_F;
     float* s_noise = s_gamma + a.ntypes;
-    if (!std::is_same<PE, NoPair>::value)
-        for (uint32_t t = threadIdx.x; t < nt2 * PAIR_TBL; t += blockDim.x) {
-            s_rec[t] = (float)a.pair_table[t];
-            if (t % PAIR_TBL == PAIR_REC) s_rc2[t / PAIR_TBL] = a.pair_table[t];
-        }
-    if (!std::is_same<BE, NoBond>::value)
-        for (uint32_t t = threadIdx.x; t < a.nbondtypes; t += blockDim.x)
-            BE::prepare_f(a.bond_params + (size_t)t * AZP_BOND_PARAM_DOUBLES, s_bond + (size_t)t * BOND_F);
-    if (INTEG != MD_FORCES_ONLY && !a.use_lambda)
-        for (uint32_t t = threadIdx.x; t < a.ntypes; t += blockDim.x) {
-            s_gamma[t] = (float)a.gamma[t];
-            s_noise[t] = (float)a.noise[t];
-        }
-    __syncthreads();
+    if constexpr (ONE) {
+        s_rc2 = &a.rc2_0;
+        s_rec = a.rec0;
+        s_bond = a.bond0;
+        s_gamma = &a.gamma0;
+        s_noise = &a.noise0;
+    } else {
+        if (!std::is_same<PE, NoPair>::value)
+            for (uint32_t t = threadIdx.x; t < nt2 * PAIR_TBL; t += blockDim.x) {
+                s_rec[t] = (float)a.pair_table[t];
+                if (t % PAIR_TBL == PAIR_REC) s_rc2[t / PAIR_TBL] = a.pair_table[t];
+            }
+        if (!std::is_same<BE, NoBond>::value)
+            for (uint32_t t = threadIdx.x; t < a.nbondtypes; t += blockDim.x)
+                BE::prepare_f(a.bond_params + (size_t)t * AZP_BOND_PARAM_DOUBLES, s_bond + (size_t)t * BOND_F);
+        if (INTEG != MD_FORCES_ONLY && !a.use_lambda)
+            for (uint32_t t = threadIdx.x; t < a.ntypes; t += blockDim.x) {
+                s_gamma[t] = (float)a.gamma[t];
+                s_noise[t] = (float)a.noise[t];
+            }
+        __syncthreads();
+    }
 
     const uint32_t tpp = (uint32_t)a.tpp;
     const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -619,7 +630,9 @@ int launch_md_t(const MDArgs& a, cudaStream_t s)
     if constexpr (std::is_same<R, float>::value) {
         const size_t smem = nt2 * sizeof(double) + nt2 * PAIR_TBL * sizeof(float) +
                             (size_t)a.nbondtypes * BOND_F * sizeof(float) + 2 * a.ntypes * sizeof(float);
-        auto k = a.out ? k_md_step_fx<PE, BE, INTEG, true> : k_md_step_fx<PE, BE, INTEG, false>;
+        auto k = a.out ? (a.one_type ? k_md_step_fx<PE, BE, INTEG, true, true> : k_md_step_fx<PE, BE, INTEG, true, false>)
+                       : (a.one_type ? k_md_step_fx<PE, BE, INTEG, false, true>
+                                     : k_md_step_fx<PE, BE, INTEG, false, false>);
         if (smem > 48 * 1024) AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<blocks, MD_BLOCK, smem, s>>>(a);
         AZP_CHECK_LAUNCH("k_md_step_fx");
