@@ -298,26 +298,38 @@ __global__ void __launch_bounds__(NLIST_BLOCK)
                     const float ddz = (float)(int32_t)(fi.z - fj.z) * bx.sfix[2];
                     const float rs = ddx * ddx + ddy * ddy + ddz * ddz;
                     const ListCut cut = ONE_TYPE ? cut0 : s_cut[row + fj.w];
-                    if (rs < cut.hi && j != i) {
-                        bool take = rs < cut.lo || nl_exact_within(i, j, cut.rlistsq, bx, pos, fixed, lo);
-                        if (take && nex) {
-                            const uint32_t kj = keys ? __ldg(keys + j) : j;
-                            bool x = false;
-#pragma unroll
-                            for (uint32_t e = 0; e < NL_EX_REG; ++e) x |= ex[e] == kj;
-                            if (nex > NL_EX_REG) x |= nl_excluded_tail(i, kj, nex, N, ex_keys);
-                            take = !x;
-                        }
-                        if (take) {
-                            if (n < max_nn) nbrs[(size_t)n * N + i] = j;
-                            ++n;
-                        }
+                    // within r_list: appended (i itself and its excluded partners too;
+                    // the pass below takes them out)
+                    if (rs < cut.hi && (rs < cut.lo || nl_exact_within(i, j, cut.rlistsq, bx, pos, fixed, lo))) {
+                        if (n < max_nn) nbrs[(size_t)n * N + i] = j;
+                        ++n;
                     }
                 }
             }
         }
     }
-    counts[i] = n;
+    // Compact the row in place: drop i itself and the excluded partners, keeping
+    // the order. The warp-wide scan above stays a load, a test and an append; the
+    // exclusion compares run once per listed entry here instead of on every
+    // candidate iteration. Overflow is judged on the raw count, which bounds the
+    // true one, so a row that lost entries to the capacity is always reported.
+    const uint32_t stored = min(n, max_nn);
+    uint32_t m = 0;
+    for (uint32_t k = 0; k < stored; ++k) {
+        const uint32_t j = nbrs[(size_t)k * N + i];
+        bool drop = j == i;
+        if (nex && !drop) {
+            const uint32_t kj = keys ? __ldg(keys + j) : j;
+#pragma unroll
+            for (uint32_t e = 0; e < NL_EX_REG; ++e) drop |= ex[e] == kj;
+            if (nex > NL_EX_REG) drop |= nl_excluded_tail(i, kj, nex, N, ex_keys);
+        }
+        if (!drop) {
+            if (m != k) nbrs[(size_t)m * N + i] = j;
+            ++m;
+        }
+    }
+    counts[i] = n > max_nn ? n : m;
     if (n > max_nn) atomicMax(&flags[0], n);
 }
 
