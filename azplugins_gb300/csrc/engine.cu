@@ -258,13 +258,14 @@ __global__ void k_state_to_fx(const double4_32a* __restrict__ pos, double4_32a* 
 __global__ void k_store_state_fx(const uint4* __restrict__ fix, const uint4* __restrict__ lo,
                                  const VelFF* __restrict__ vel, const double* __restrict__ mass,
                                  const double* __restrict__ accel, const int* __restrict__ image,
-                                 const uint32_t* __restrict__ tag, uint32_t N, double l0, double l1, double l2,
+                                 const uint32_t* __restrict__ rtag, uint32_t N, double l0, double l1, double l2,
                                  double* __restrict__ pos_out, double* __restrict__ vel_out,
                                  double* __restrict__ accel_out, int* __restrict__ image_out)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const uint32_t t = tag[i];
+    // one thread per tag: the outputs are written in order
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    const uint32_t i = rtag[t];
     if (pos_out) {
         const uint4 h = fix[i], l = lo[i];
         pos_out[4 * t] = fx_to_double(fx_join(h.x, l.x), l0);
@@ -394,13 +395,14 @@ __global__ void k_load_state(const double* __restrict__ pos_in, const double* __
 // i takes the input row of its tag); tag / rtag are kept
 __global__ void k_load_state_ordered(const double* __restrict__ pos_in, const double* __restrict__ vel_in,
                                      const double* __restrict__ accel_in, const int* __restrict__ image_in,
-                                     const double* __restrict__ diam_in, const uint32_t* __restrict__ tag, uint32_t N,
-                                     double4_32a* __restrict__ pos, double4_32a* __restrict__ vel,
+                                     const double* __restrict__ diam_in, const uint32_t* __restrict__ rtag,
+                                     uint32_t N, double4_32a* __restrict__ pos, double4_32a* __restrict__ vel,
                                      double* __restrict__ accel, int* __restrict__ image, double* __restrict__ diam)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const uint32_t t = tag[i];
+    // one thread per tag: the inputs are read in order
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    const uint32_t i = rtag[t];
     pos[i] = make_double4_32a(pos_in[4 * t], pos_in[4 * t + 1], pos_in[4 * t + 2],
                               type_as_double((uint32_t)pos_in[4 * t + 3]));
     vel[i] = make_double4_32a(vel_in[4 * t], vel_in[4 * t + 1], vel_in[4 * t + 2], vel_in[4 * t + 3]);
@@ -431,12 +433,13 @@ __global__ void k_request_if_displaced(const uint4* __restrict__ fix, const uint
 // device state -> tag order output (pos w = type as an integer-valued double)
 __global__ void k_store_state(const double4_32a* __restrict__ pos, const double4_32a* __restrict__ vel,
                               const double* __restrict__ accel, const int* __restrict__ image,
-                              const uint32_t* __restrict__ tag, uint32_t N, double* __restrict__ pos_out,
+                              const uint32_t* __restrict__ rtag, uint32_t N, double* __restrict__ pos_out,
                               double* __restrict__ vel_out, double* __restrict__ accel_out, int* __restrict__ image_out)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const uint32_t t = tag[i];
+    // one thread per tag: the outputs are written in order
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    const uint32_t i = rtag[t];
     const double4_32a p = pos[i];
     if (pos_out) {
         pos_out[4 * t] = p.x;
@@ -527,6 +530,9 @@ struct azp_md {
     double* tmpd = nullptr;       // tag-order staging [N * 6]
     uint64_t launches = 0;
     bool have_state = false;
+    // out_force / out_virial hold the forces of the current state (written by a
+    // forces-only launch or by the closing step of a Langevin run)
+    bool forces_valid = false;
     // host-transfer staging of azp_md_set_state / azp_md_get_state (tag order,
     // allocated on the first host transfer and kept: no allocation per call)
     double* st_pos = nullptr;
@@ -875,13 +881,14 @@ void enqueue_store_state(azp_md* m, double* pos, double* vel, double* accel, int
     const uint32_t N = m->N;
     if (m->precision == AZP_FP32)
         k_store_state_fx<<<blocks_for(N, 256), 256, 0, s>>>(
-            m->fix[m->cur], m->lo[m->cur], reinterpret_cast<const VelFF*>(m->vel), m->mass, m->accel, m->image, m->tag,
+            m->fix[m->cur], m->lo[m->cur], reinterpret_cast<const VelFF*>(m->vel), m->mass, m->accel, m->image, m->rtag,
             N, m->box.L[0] * 5.421010862427522e-20, m->box.L[1] * 5.421010862427522e-20,
             m->box.L[2] * 5.421010862427522e-20, pos, vel, accel, image);
     else
-        k_store_state<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[m->cur], m->vel, m->accel, m->image, m->tag, N, pos,
+        k_store_state<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[m->cur], m->vel, m->accel, m->image, m->rtag, N, pos,
                                                           vel, accel, image);
 }
+
 
 int size_list(azp_md* m, cudaStream_t s)
 {
@@ -1141,6 +1148,7 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         AZP_CHECK_LAUNCH("azp_md_set_state (host to device)");
     }
     m->cur = 0;
+    m->forces_valid = false;
     m->timestep = timestep;
     const unsigned long long ts = timestep;
     AZP_CUDA_TRY(cudaMemcpyAsync(m->d_ts, &ts, sizeof(ts), cudaMemcpyHostToDevice, s));
@@ -1153,7 +1161,7 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         // its position at the last build (a state read back from this engine and
         // set again moves nothing). A denser new state that overflows the list
         // takes the full path below.
-        k_load_state_ordered<<<blocks_for(N, 256), 256, 0, s>>>(dp, dv, da, di, dd, m->tag, N, m->pos[0], m->vel,
+        k_load_state_ordered<<<blocks_for(N, 256), 256, 0, s>>>(dp, dv, da, di, dd, m->rtag, N, m->pos[0], m->vel,
                                                                  m->accel, m->image, m->diam);
         AZP_CHECK_LAUNCH("k_load_state_ordered");
         if (m->precision == AZP_FP32) {
@@ -1200,6 +1208,7 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         if (st) return st;
         k_accel_from_force<<<blocks_for(N, 256), 256, 0, s>>>(m->out_force, m->vel, m->mass, m->accel, N);
         AZP_CHECK_LAUNCH("k_accel_from_force");
+        m->forces_valid = true;
     }
     m->have_state = true;
     return check_errors(m, s);
@@ -1244,6 +1253,7 @@ int azp_md_run(azp_md* m, uint64_t steps, void* stream)
     if (!m || !m->have_state) return AZP_ERR_INVALID;
     m->launches = 0;
     if (steps == 0 || m->N == 0) return AZP_OK;
+    m->forces_valid = false;
     cudaStream_t s = as_stream(stream);
     const int integ = m->method == AZP_METHOD_BROWNIAN_FLOW ? MD_INTEG_BROWNIAN : MD_INTEG_LANGEVIN;
     int st = AZP_OK;
@@ -1278,6 +1288,7 @@ int azp_md_run(azp_md* m, uint64_t steps, void* stream)
         if (st) return st;
         st = enqueue_step(m, integ, 0, 1, s, 0, 0);
         if (st) return st;
+        m->forces_valid = true;  // the closing step wrote the forces of the final state
     }
     m->timestep += steps;
     return AZP_OK;
@@ -1295,6 +1306,7 @@ int azp_md_forces(azp_md* m, double* force, double* virial, int on_device, void*
     a.out = 1;
     st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
     if (st) return st;
+    m->forces_valid = true;
     k_to_tag_order4<<<blocks_for(N, 256), 256, 0, s>>>(m->out_force, m->tag, N, m->tmp4);
     k_to_tag_order_n<<<blocks_for(N, 256), 256, 0, s>>>(m->out_virial, m->tag, N, 6, 1, m->tmpd);
     AZP_CHECK_LAUNCH("azp_md_forces");
@@ -1312,12 +1324,15 @@ int azp_md_thermo(azp_md* m, double* out, void* stream)
     const uint32_t N = m->N;
     for (int c = 0; c < 9; ++c) out[c] = 0.0;
     if (N == 0) return AZP_OK;
-    int st = enqueue_rebuild(m, s, m->flags);
-    if (st) return st;
-    MDArgs a = base_args(m);
-    a.out = 1;
-    st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
-    if (st) return st;
+    if (!m->forces_valid) {
+        int st = enqueue_rebuild(m, s, m->flags);
+        if (st) return st;
+        MDArgs a = base_args(m);
+        a.out = 1;
+        st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
+        if (st) return st;
+        m->forces_valid = true;
+    }
     const uint32_t nb = blocks_for(N, THERMO_BLOCK);
     k_thermo_partials<<<nb, THERMO_BLOCK, 0, s>>>(m->out_force, m->out_virial, m->vel, m->mass, N, m->partials);
     k_thermo_final<<<1, 32, 0, s>>>(m->partials, nb, m->thermo);
@@ -1397,6 +1412,7 @@ int azp_md_time_step_kernel(azp_md* m, int reps, float* ms, void* stream)
     if (!m || !m->have_state || reps <= 0 || !ms) return AZP_ERR_INVALID;
     cudaStream_t s = as_stream(stream);
     const int integ = m->method == AZP_METHOD_BROWNIAN_FLOW ? MD_INTEG_BROWNIAN : MD_INTEG_LANGEVIN;
+    m->forces_valid = false;
     cudaEvent_t e0, e1;
     AZP_CUDA_TRY(cudaEventCreate(&e0));
     AZP_CUDA_TRY(cudaEventCreate(&e1));

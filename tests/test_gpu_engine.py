@@ -399,3 +399,45 @@ def test_state_set_denser_overflows_to_full_path(orc):
     f, w = sim._engine.forces()
     F, U, W = _oracle_lj(orc, s, rcut=2.5).forces()
     assert force_error(f, F) < 1e-12
+
+
+def test_pinned_and_pageable_state_transfers_agree():
+    # page-locked and pageable host arrays give the same state transfers
+    import ctypes
+
+    import torch
+
+    from azplugins_gb300 import _lib, workloads
+
+    snap = workloads.lj_fluid(n_side=10, density=0.8, seed=41)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    sim, lj = _lj_setup(snap, precision="fp32")
+    sim.run(25)
+    eng = sim._engine
+    N = snap.particles.N
+    L = eng._L
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def get(pinned):
+        mk = (lambda shape, dt: torch.empty(shape, dtype=dt).pin_memory()) if pinned else \
+            (lambda shape, dt: torch.empty(shape, dtype=dt))
+        pos, vel, acc, img = mk((N, 4), torch.float64), mk((N, 4), torch.float64), mk((N, 3), torch.float64), \
+            mk((N, 3), torch.int32)
+        _lib.check(L.azp_md_get_state(eng._md, pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), img.data_ptr(), None, 0,
+                                      stream), "azp_md_get_state")
+        return pos, vel, acc, img
+
+    a = get(True)
+    b = get(False)
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+    # set the state back through pinned arrays, run, read: equal to the pageable round trip
+    outs = []
+    for pinned in (True, False):
+        src = a if pinned else tuple(t.clone() for t in b)
+        _lib.check(L.azp_md_set_state(eng._md, src[0].data_ptr(), src[1].data_ptr(), src[2].data_ptr(),
+                                      src[3].data_ptr(), None, 25, 0, stream), "azp_md_set_state")
+        _lib.check(L.azp_md_run(eng._md, 7, stream), "azp_md_run")
+        outs.append(get(False))
+    for x, y in zip(*outs):
+        assert torch.equal(x, y)
