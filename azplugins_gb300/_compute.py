@@ -154,6 +154,50 @@ def pair_forces(state, pair, precision="fp64", tpp=4):
     return f, w
 
 
+def dpd_forces(state, pair, precision, dt, timestep, seed, tpp=4):
+    """(force4 [N,4], virial [N,6]) of a DPDGeneralWeight potential at the state:
+    conservative + dissipative + random forces, conservative energy and virial."""
+    torch = _torch()
+    _lib.require_gpu()
+    L = _lib.load()
+    snap = state._arrays()
+    p = snap.particles
+    N = p.N
+    types = list(p.types)
+    nt = len(types)
+    rec, rc, ro = pair._tables(types)
+    excl = None
+    if pair.nlist.exclude_bonds and snap.bonds.N:
+        excl = exclusions_csr(N, snap.bonds.group)
+    pos = device_positions(snap)
+    vel = torch.zeros((max(N, 1), 4), dtype=torch.float64, device="cuda")
+    tags = torch.arange(max(N, 1), dtype=torch.int32, device="cuda")
+    if N:
+        vel[:N, :3] = torch.from_numpy(np.ascontiguousarray(p.velocity, dtype=np.float64)).cuda()
+        vel[:N, 3] = torch.from_numpy(np.ascontiguousarray(p.mass, dtype=np.float64)).cuda()
+    sysd = make_system(snap, pos, vel=vel.data_ptr(), tag=tags.data_ptr())
+    nl = NeighborList(N, nt, rc, pair.nlist.buffer, excl, tpp=tpp)
+    nl.build(sysd)
+    prec = _lib.FP32 if precision == "fp32" else _lib.FP64
+    dt_ = torch.float32 if prec == _lib.FP32 else torch.float64
+    params_d = torch.from_numpy(rec.reshape(-1).copy()).cuda()
+    rc_d = torch.from_numpy(rc.reshape(-1).copy()).cuda()
+    force = torch.zeros((max(N, 1), 4), dtype=dt_, device="cuda")
+    vir = torch.zeros((6, max(N, 1)), dtype=dt_, device="cuda")
+    out = _lib.Forces()
+    out.force = force.data_ptr()
+    out.virial = vir.data_ptr()
+    out.virial_pitch = max(N, 1)
+    out.precision = prec
+    _lib.check(L.azp_dpd_forces(ctypes.byref(sysd), nl.handle, params_d.data_ptr(), rc_d.data_ptr(), float(pair.kT),
+                                float(dt), int(timestep), int(seed), ctypes.byref(out), _stream()), "azp_dpd_forces")
+    torch.cuda.synchronize()
+    f = force[:N].double().cpu().numpy()
+    w = vir[:, :N].double().cpu().numpy().T.copy()
+    nl.close()
+    return f, w
+
+
 def bond_table(N, group, typeid):
     """Per-particle table: n_bonds[N], table [height][N][2] (partner, type)."""
     group = np.asarray(group, dtype=np.int64).reshape(-1, 2)

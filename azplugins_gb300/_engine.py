@@ -26,6 +26,9 @@ def split_forces(integ):
         raise NotImplementedError(f"unsupported force objects: {other}")
     if len(pairs) > 1 or len(bonds) > 1:
         raise NotImplementedError("the engine advances at most one pair and one bond potential")
+    if pairs and pairs[0]._name == "DPDGeneralWeight":
+        raise NotImplementedError("DPDGeneralWeight runs through the drop-in driver (azp_dpd_forces); "
+                                  "the resident engine does not take it")
     return (pairs[0] if pairs else None), (bonds[0] if bonds else None)
 
 

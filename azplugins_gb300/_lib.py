@@ -31,7 +31,7 @@ STATUS = {
 }
 
 # header enums
-PAIR_KINDS = {"PerturbedLennardJones": 0, "ExpandedYukawa": 1, "Hertz": 2, "Colloid": 3}
+PAIR_KINDS = {"PerturbedLennardJones": 0, "ExpandedYukawa": 1, "Hertz": 2, "Colloid": 3, "DPDGeneralWeight": 4}
 BOND_KINDS = {"Quartic": 0, "DoubleWell": 1}
 MODES = {"none": 0, "shift": 1, "xplor": 2}
 FP64, FP32 = 0, 1
@@ -167,6 +167,7 @@ _SIGNATURES = [
     ("azp_pair_forces", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _vp, _i, ctypes.POINTER(Forces), _vp]),
     ("azp_pair_forces_static", _i, [ctypes.POINTER(System), _vp, _vp, _u32, _i, _vp, _vp, _vp, _i,
                                     ctypes.POINTER(Forces), _vp]),
+    ("azp_dpd_forces", _i, [ctypes.POINTER(System), _vp, _vp, _vp, _d, _d, _u64, _u32, ctypes.POINTER(Forces), _vp]),
     ("azp_bond_forces", _i, [ctypes.POINTER(System), _vp, _vp, _u32, _i, _vp, _u32, ctypes.POINTER(Forces), _vp, _vp]),
     ("azp_pair_adjoint", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
     ("azp_bond_adjoint", _i, [ctypes.POINTER(System), _vp, _vp, _i, _vp, _u32, _vp, _vp, _vp, _vp, _vp]),

@@ -40,6 +40,7 @@ int n_pair_values(int kind)
     case AZP_PAIR_EXPANDED_YUKAWA: return 3;
     case AZP_PAIR_HERTZ: return 1;
     case AZP_PAIR_COLLOID: return 4;
+    case AZP_PAIR_DPD_GENERAL_WEIGHT: return 3;
     default: return -1;
     }
 }
@@ -109,6 +110,8 @@ int azp_pair_params_from_values(int kind, const double* v, double* rec)
     case AZP_PAIR_EXPANDED_YUKAWA: rec[0] = v[0]; rec[1] = v[1]; rec[2] = v[2]; return AZP_OK;
     case AZP_PAIR_HERTZ: rec[0] = v[0]; return AZP_OK;
     case AZP_PAIR_COLLOID: rec[0] = v[0]; rec[1] = v[1]; rec[2] = v[2]; rec[3] = v[3] * v[3] * v[3]; return AZP_OK;
+    // PairParametersDPDGeneralWeight(pybind11::dict), src/DPDPairEvaluatorGeneralWeight.h:37-42
+    case AZP_PAIR_DPD_GENERAL_WEIGHT: rec[0] = v[0]; rec[1] = v[1]; rec[2] = v[2]; return AZP_OK;
     default: return AZP_ERR_INVALID;
     }
 }
@@ -126,6 +129,7 @@ int azp_pair_params_to_values(int kind, const double* rec, double* v)
     case AZP_PAIR_EXPANDED_YUKAWA: v[0] = rec[0]; v[1] = rec[1]; v[2] = rec[2]; return AZP_OK;
     case AZP_PAIR_HERTZ: v[0] = rec[0]; return AZP_OK;
     case AZP_PAIR_COLLOID: v[0] = rec[0]; v[1] = rec[1]; v[2] = rec[2]; v[3] = std::cbrt(rec[3]); return AZP_OK;
+    case AZP_PAIR_DPD_GENERAL_WEIGHT: v[0] = rec[0]; v[1] = rec[1]; v[2] = rec[2]; return AZP_OK;
     default: return AZP_ERR_INVALID;
     }
 }

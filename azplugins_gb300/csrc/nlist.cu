@@ -433,6 +433,8 @@ void free_nl(azp_nlist* nl)
     cudaFree(nl->table);
     cudaFree(nl->cutbuf);
     cudaFree(nl->adj_table);
+    cudaFree(nl->vel_f);
+    cudaFree(nl->dpd_table);
 }
 
 int ensure_cells(azp_nlist* nl, uint32_t ncell)
@@ -481,6 +483,9 @@ azp_nlist* azp_nlist_create(uint32_t N, uint32_t ntypes, uint32_t max_neighbors,
     if (!st && (e = cudaMalloc(&nl->cutbuf, sizeof(double) * ntypes * ntypes * 2)) != cudaSuccess) fail(e, "cutbuf");
     if (!st && (e = cudaMalloc(&nl->adj_table, sizeof(double) * 6 * 12 * ntypes * ntypes)) != cudaSuccess)
         fail(e, "adj_table");
+    if (!st && (e = cudaMalloc(&nl->vel_f, sizeof(float4) * n1)) != cudaSuccess) fail(e, "vel_f");
+    if (!st && (e = cudaMalloc(&nl->dpd_table, sizeof(double) * 8 * ntypes * ntypes)) != cudaSuccess)
+        fail(e, "dpd_table");
     if (st) {
         free_nl(nl);
         delete nl;

@@ -32,5 +32,8 @@ struct azp_nlist {
     double* cutbuf = nullptr;  // [2][ntypes^2]
     // adjoint workspace: dual-number type-pair records [ntypes^2][12] x (1 + 5) doubles
     double* adj_table = nullptr;
+    // DPD driver workspace: FP32 velocity shadow [N] and per-type-pair constants
+    float4* vel_f = nullptr;
+    double* dpd_table = nullptr;  // [ntypes^2][8]
 };
 

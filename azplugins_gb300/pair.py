@@ -104,6 +104,36 @@ class Colloid(Pair):
     _keys = ("A", "a_1", "a_2", "sigma")
 
 
+class DPDGeneralWeight(Pair):
+    """DPD with a general weight function (``src/DPDPairEvaluatorGeneralWeight.h``,
+    ``src/pair.py:121-239``): conservative A (1 - r / r_cut), dissipative
+    -gamma w(r) (v_ij . r_hat) r_hat and random sqrt(gamma w(r)) theta r_hat forces
+    with w = (1 - r / r_cut)^s. ``params`` keys: ``A``, ``gamma``, ``s``; mode
+    ``"none"`` only; ``kT`` the thermostat temperature (a constant here).
+
+    The forces depend on the velocities, the timestep and the Simulation's seed:
+    ``forces`` / ``energies`` / ``virials`` are evaluated by the drop-in driver
+    (``azp_dpd_forces``) at the current state, timestep and integrator ``dt``.
+    The resident engine (``Simulation.run``) does not take this potential."""
+
+    _name = "DPDGeneralWeight"
+    _keys = ("A", "gamma", "s")
+    _accepted_modes = ("none",)
+
+    def __init__(self, nlist, kT, default_r_cut=None):
+        super().__init__(nlist=nlist, default_r_cut=default_r_cut, default_r_on=0.0, mode="none")
+        self.kT = float(kT)
+
+    def _compute(self):
+        if self._sim is None:
+            raise RuntimeError("attach the force to a Simulation (sim.run(0)) before reading results")
+        from . import _compute
+
+        integ = self._sim.operations.integrator
+        return _compute.dpd_forces(self._sim.state, self, self._sim.precision, integ.dt, self._sim.timestep,
+                                   self._sim.seed)
+
+
 class ExpandedYukawa(Pair):
     """Expanded Yukawa pair potential (``src/PairEvaluatorExpandedYukawa.h``)."""
 
@@ -125,4 +155,4 @@ class PerturbedLennardJones(Pair):
     _keys = ("epsilon", "sigma", "attraction_scale_factor")
 
 
-__all__ = ["Pair", "Colloid", "ExpandedYukawa", "Hertz", "PerturbedLennardJones"]
+__all__ = ["Pair", "Colloid", "DPDGeneralWeight", "ExpandedYukawa", "Hertz", "PerturbedLennardJones"]

@@ -70,7 +70,8 @@ enum azp_pair_kind {
     AZP_PAIR_EXPANDED_YUKAWA = 1,  /* PairEvaluatorExpandedYukawa */
     AZP_PAIR_HERTZ = 2,            /* PairEvaluatorHertz */
     AZP_PAIR_COLLOID = 3,          /* PairEvaluatorColloid */
-    AZP_PAIR_NUM_KINDS = 4
+    AZP_PAIR_NUM_KINDS = 4,        /* kinds of azp_pair_forces and the engine */
+    AZP_PAIR_DPD_GENERAL_WEIGHT = 4 /* DPDPairEvaluatorGeneralWeight: azp_dpd_forces only */
 };
 enum azp_bond_kind {
     AZP_BOND_QUARTIC = 0,          /* BondEvaluatorQuartic */
@@ -100,6 +101,7 @@ typedef struct { double sigma_6, epsilon_x_4, attraction_scale_factor, rwcasq; }
 typedef struct { double epsilon, kappa, delta, pad_; } azp_params_expanded_yukawa;
 typedef struct { double epsilon, pad_[3]; } azp_params_hertz;
 typedef struct { double A, a_1, a_2, sigma_3; } azp_params_colloid;
+typedef struct { double A, gamma, s, pad_; } azp_params_dpd_general_weight;
 typedef struct { double k, r_0, b_1, b_2, U_0, sigma_6, epsilon_x_4, delta; } azp_params_quartic;
 typedef struct { double r_1, r_diff, U_1, U_tilt, pad_[4]; } azp_params_double_well;
 
@@ -112,6 +114,7 @@ typedef struct { double r_1, r_diff, U_1, U_tilt, pad_[4]; } azp_params_double_w
  *   ExpandedYukawa:        epsilon, kappa, delta
  *   Hertz:                 epsilon
  *   Colloid:               A, a_1, a_2, sigma
+ *   DPDGeneralWeight:      A, gamma, s
  *   Quartic:               k, r_0, b_1, b_2, U_0, sigma, epsilon, delta
  *   DoubleWell:            r_0, r_1, U_1, U_tilt
  * Replaces e.g. PairParametersPerturbedLennardJones(pybind11::dict) and asDict()
@@ -226,6 +229,19 @@ AZP_API int azp_nlist_set_tpp(azp_nlist* nl, int tpp);
 AZP_API int azp_pair_forces_static(const azp_system* sys, const uint32_t* counts, const uint32_t* neighbors,
                                    uint32_t max_neighbors, int kind, const double* params, const double* r_cut,
                                    const double* r_on, int shift_mode, const azp_forces* out, void* stream);
+
+/* DPD with a general weight function (replaces HOOMD's gpu_compute_dpd_forces for
+ * src/DPDPairEvaluatorGeneralWeight.h:165-255, instantiated in
+ * src/PotentialPairDPDThermoGPUKernel.cu.inc:21-24): conservative, dissipative and
+ * random pair forces over the list. params: device [ntypes^2] records (A, gamma, s,
+ * -); r_cut: device [ntypes^2]; reads sys->pos, sys->vel (v, mass) and sys->tag.
+ * The random draw of a pair comes from the stream (AZP_RNG_DPD_GENERAL_WEIGHT,
+ * timestep, seed) at the ordered tag pair, so both particles see the same number.
+ * Writes force and energy (conservative, half per particle) and the conservative
+ * virial. Uses nl as its workspace; no allocation, no synchronisation. */
+AZP_API int azp_dpd_forces(const azp_system* sys, azp_nlist* nl, const double* params, const double* r_cut,
+                           double kT, double dt, uint64_t timestep, uint32_t seed, const azp_forces* out,
+                           void* stream);
 
 /* Bond forces from a per-particle bond table (replaces
  * gpu_compute_bond_forces<Eval,2>): for particle i its bonds are

@@ -282,6 +282,9 @@ bool eval_bond(int kind, const double* p, double rsq, double& f, double& e)
     }
 }
 
+// RNG stream ids, src/RNGIdentifiers.h:20-27
+constexpr uint8_t RNG_DPD = 200, RNG_BROWNIAN = 201, RNG_LANGEVIN = 202;
+
 // ---------------------------------------------------------------- Philox4x32-10
 inline void mulhilo(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo)
 {
@@ -669,6 +672,79 @@ void orc_pair_forces(int N, const double* pos, const int32_t* type, int ntypes, 
     }
 }
 
+// ---- DPD with general weight, full thermostat (src/DPDPairEvaluatorGeneralWeight.h:165-255):
+// conservative A (1/r - 1/r_cut), dissipative -gamma w(r) (dx . dv) / r^2 with
+// w = (1 - r/r_cut)^s, random sqrt(6 kT gamma / dt) sqrt(w) alpha / r with alpha
+// uniform in (-1, 1) drawn once per pair from the stream
+// (RNG id 200, timestep, seed) at counter {0, min(tag_i, tag_j), max(...), 0}
+// (the reference's Seed(id, timestep, seed) + Counter(i, j) at :227-233). Energy
+// and virial: conservative part only (:203-204, :249-250). params [ntypes^2][4]:
+// A, gamma, s, -; vel [N][4] (v, mass).
+double dpd_alpha(uint64_t timestep, uint32_t seed, uint32_t ti, uint32_t tj)
+{
+    uint32_t key[2];
+    stream_key(RNG_DPD, timestep, seed, key);
+    const uint32_t oi = ti < tj ? ti : tj, oj = ti < tj ? tj : ti;
+    uint32_t c[4] = {0u, oi, oj, 0u}, o[4];
+    philox(c, key, o);
+    const uint64_t u = ((uint64_t)o[0] << 32) | o[1];
+    return -1.0 + 2.0 * u64_to_open01(u);
+}
+
+void orc_dpd_forces(int N, const double* pos, const double* vel, const int32_t* type, const uint32_t* tag,
+                    int ntypes, const double* L, const int32_t* start, const int32_t* idx, const double* params,
+                    const double* rcutsq, double kT, double dt, uint64_t timestep, uint32_t seed, double* force,
+                    double* energy, double* virial)
+{
+    const Box b = make_box(L);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+    for (int i = 0; i < N; ++i) {
+        double F[3] = {0, 0, 0}, U = 0.0, W[6] = {0, 0, 0, 0, 0, 0};
+        const int ti = type[i];
+        for (int k = start[i]; k < start[i + 1]; ++k) {
+            const int j = idx[k];
+            double v[3] = {pos[4 * i] - pos[4 * j], pos[4 * i + 1] - pos[4 * j + 1], pos[4 * i + 2] - pos[4 * j + 2]};
+            min_image(b, v);
+            const double rs = rsq_of(v);
+            const int tp = ti * ntypes + type[j];
+            const double rc2 = rcutsq[tp];
+            if (!(rs < rc2)) continue;
+            const double* p = params + (size_t)tp * 4;
+            const double A = p[0], gamma = p[1], s = p[2];
+            const double rinv = 1.0 / std::sqrt(rs);
+            const double r = 1.0 / rinv;
+            const double rcinv = 1.0 / std::sqrt(rc2);
+            const double rc = 1.0 / rcinv;
+            const double dot = v[0] * (vel[4 * i] - vel[4 * j]) + v[1] * (vel[4 * i + 1] - vel[4 * j + 1]) +
+                               v[2] * (vel[4 * i + 2] - vel[4 * j + 2]);
+            const double fc = A * (rinv - rcinv);
+            // r < r_cut, but 1 - r / r_cut can round below 0 right at the cutoff, where the
+            // reference's pow would return NaN: clamped to 0
+            const double wR = std::pow(std::fmax(1.0 - r * rcinv, 0.0), 0.5 * s) * rinv;
+            const double alpha = dpd_alpha(timestep, seed, tag[i], tag[j]);
+            const double fdr = fc - gamma * wR * wR * dot + std::sqrt(6.0 * kT * gamma / dt) * wR * alpha;
+            const double e = A * (rc - r) - 0.5 * A * rcinv * (rc2 - rs);
+            F[0] += v[0] * fdr;
+            F[1] += v[1] * fdr;
+            F[2] += v[2] * fdr;
+            U += 0.5 * e;
+            const double h = 0.5 * fc;
+            W[0] += h * v[0] * v[0];
+            W[1] += h * v[0] * v[1];
+            W[2] += h * v[0] * v[2];
+            W[3] += h * v[1] * v[1];
+            W[4] += h * v[1] * v[2];
+            W[5] += h * v[2] * v[2];
+        }
+        for (int d = 0; d < 3; ++d) force[3 * i + d] = F[d];
+        energy[i] = U;
+        if (virial)
+            for (int c = 0; c < 6; ++c) virial[6 * i + c] = W[c];
+    }
+}
+
 // ---- bond forces. bonds[2*b] = {a, b} particle indices; btype[b]; params[t*8...].
 // ACCUMULATES into force/energy/virial. Returns 0, or 1 + index of the first
 // bond whose evaluator refused (r_0 == 0 / r_1 == r_0), like the device flag.
@@ -783,7 +859,7 @@ void orc_langevin_step2(int N, const double* pos, const int32_t* type, double* v
         double c = std::sqrt(6.0 * g * kT / dt);
         if (noiseless) c = 0.0;
         double R[3];
-        uniform3(202, timestep, seed, tag[i], -c, c, R);
+        uniform3(RNG_LANGEVIN, timestep, seed, tag[i], -c, c, R);
         const double m = vel[4 * i + 3];
         const double minv = 1.0 / m;
         for (int d = 0; d < 3; ++d) {
@@ -812,7 +888,7 @@ void orc_brownian(int N, double* pos, int32_t* image, const int32_t* type, const
         double c = std::sqrt(6.0 * g * kT / dt);
         if (noiseless) c = 0.0;
         double R[3];
-        uniform3(201, timestep, seed, tag[i], -c, c, R);
+        uniform3(RNG_BROWNIAN, timestep, seed, tag[i], -c, c, R);
         for (int d = 0; d < 3; ++d) {
             double dd = (u[d] + (net_force[3 * i + d] + R[d]) / g) * dt;
             if (max_disp > 0.0) dd = std::fmin(std::fmax(dd, -max_disp), max_disp);

@@ -91,6 +91,8 @@ def lib():
         fn.argtypes = [c_int, _dp, _ip, c_int, _dp, _dp, vp, vp, _ip, _ip, c_long]
         fn.restype = c_long
     L.orc_pair_forces.argtypes = [c_int, _dp, _ip, c_int, _dp, _ip, _ip, c_int, _dp, c_int, _dp, vp, c_int, _dp, _dp, vp, c_double]
+    L.orc_dpd_forces.argtypes = [c_int, _dp, _dp, _ip, _up, c_int, _dp, _ip, _ip, _dp, _dp, c_double, c_double, c_u64,
+                                 c_u32, _dp, _dp, vp]
     L.orc_bond_forces.argtypes = [c_int, _dp, _dp, c_long, _ip, _ip, c_int, _dp, c_int, _dp, _dp, vp]
     L.orc_bond_forces.restype = c_long
     L.orc_bond_forces_pp.argtypes = [c_int, _dp, _dp, _ip, _ip, _ip, c_int, _dp, c_int, _dp, _dp, vp]
@@ -220,6 +222,37 @@ def pair_forces(pos4, types, ntypes, L, start, idx, name, params, rcutsq, ronsq=
         U,
         _ptr(W),
         float(fcap),
+    )
+    return F, U, W
+
+
+def dpd_forces(pos4, vel4, types, tags, ntypes, L, start, idx, params, rcutsq, kT, dt, timestep, seed):
+    """DPDGeneralWeight thermostat forces (conservative + dissipative + random),
+    per-particle energy (conservative, half per pair) and conservative virial.
+    params [ntypes, ntypes, 4] records (A, gamma, s, -)."""
+    N = pos4.shape[0]
+    F = np.zeros((N, 3))
+    U = np.zeros(N)
+    W = np.zeros((N, 6))
+    lib().orc_dpd_forces(
+        N,
+        np.ascontiguousarray(pos4, dtype=np.float64),
+        np.ascontiguousarray(vel4, dtype=np.float64),
+        np.ascontiguousarray(types, dtype=np.int32),
+        np.ascontiguousarray(tags, dtype=np.uint32),
+        ntypes,
+        np.ascontiguousarray(L, dtype=np.float64),
+        np.ascontiguousarray(start, dtype=np.int32),
+        np.ascontiguousarray(idx, dtype=np.int32),
+        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        np.ascontiguousarray(rcutsq, dtype=np.float64).reshape(-1),
+        float(kT),
+        float(dt),
+        int(timestep),
+        int(seed),
+        F,
+        U,
+        _ptr(W),
     )
     return F, U, W
 

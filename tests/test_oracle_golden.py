@@ -166,3 +166,36 @@ def test_xplor_smoothing_continuity(orc):
         vals.append((F[1, 0], U.sum()))
     assert abs(vals[0][0] - vals[1][0]) < 1e-5 and abs(vals[0][1] - vals[1][1]) < 1e-6
     assert abs(vals[2][0]) < 1e-6 and abs(vals[2][1]) < 1e-9
+
+
+@pytest.mark.parametrize("case", [c for c in KATS["pair"] if c["potential"] == "DPDGeneralWeight"],
+                         ids=lambda c: f"DPD-thermostat@{c['line']}")
+def test_dpd_thermostat_oracle_kat(orc, case):
+    # the full thermostat restatement at kT = 0 with particles at rest reduces to the KAT
+    d = case["distance"]
+    pos4 = np.array([[-0.5 * d, 0, 0, 0], [0.5 * d, 0, 0, 0]], dtype=np.float64)
+    vel4 = np.array([[0, 0, 0, 1.0], [0, 0, 0, 1.0]])
+    rec = orc.pair_params("DPDGeneralWeight", case["params"]).reshape(1, 1, 4)
+    L = np.array([10.0, 10.0, 10.0])
+    F, U, W = orc.dpd_forces(pos4, vel4, [0, 0], [0, 1], 1, L, np.array([0, 1, 2]), np.array([1, 0]), rec,
+                             np.array([[case["r_cut"] ** 2]]), 0.0, 0.001, 7, 3)
+    np.testing.assert_allclose(F[:, 0], [-case["force"], case["force"]], atol=1e-12)
+    np.testing.assert_allclose(U, [0.5 * case["energy"]] * 2, atol=1e-12)
+
+
+def test_dpd_thermostat_oracle_pair_draw_is_shared(orc):
+    # i and j draw the same number (ordered tag counter): the pair forces cancel
+    rng = np.random.Generator(np.random.PCG64(2))
+    N, L = 300, 6.0
+    pos4 = np.concatenate([rng.uniform(-3, 3, size=(N, 3)), np.zeros((N, 1))], axis=1)
+    vel4 = np.concatenate([rng.normal(size=(N, 3)), np.ones((N, 1))], axis=1)
+    rec = orc.pair_params("DPDGeneralWeight", dict(A=25.0, gamma=4.5, s=0.5)).reshape(1, 1, 4)
+    Lv = np.array([L, L, L])
+    st, idx = orc.nlist(pos4, np.zeros(N, dtype=np.int32), 1, Lv, np.array([[1.0]]))
+    F, U, W = orc.dpd_forces(pos4, vel4, np.zeros(N, dtype=np.int32), np.arange(N, dtype=np.uint32), 1, Lv, st, idx,
+                             rec, np.array([[1.0]]), 1.5, 0.01, 11, 4)
+    assert np.abs(F.sum(axis=0)).max() < 1e-10 * np.abs(F).sum()
+    # the random term is on: a different timestep gives different forces
+    F2, _, _ = orc.dpd_forces(pos4, vel4, np.zeros(N, dtype=np.int32), np.arange(N, dtype=np.uint32), 1, Lv, st, idx,
+                              rec, np.array([[1.0]]), 1.5, 0.01, 12, 4)
+    assert not np.allclose(F, F2)
