@@ -250,3 +250,36 @@ def bond_forces(state, bond, precision="fp64"):
     f = force[:N].double().cpu().numpy()
     w = vir[:, :N].double().cpu().numpy().T.copy()
     return f, w
+
+
+def barrier_forces(state, barrier, precision, timestep):
+    """(force4 [N,4], virial [N,6]) of a harmonic barrier at the state: the
+    barrier's force and energy per particle; the virial is zero, as the
+    reference leaves it (src/HarmonicBarrier.h:177-179)."""
+    torch = _torch()
+    _lib.require_gpu()
+    L = _lib.load()
+    snap = state._arrays()
+    p = snap.particles
+    N = p.N
+    types = list(p.types)
+    location = barrier._location_at(timestep, snap.configuration.box[:3])
+    pos = device_positions(snap)
+    sysd = make_system(snap, pos)
+    prec = _lib.FP32 if precision == "fp32" else _lib.FP64
+    dt_ = torch.float32 if prec == _lib.FP32 else torch.float64
+    params_d = torch.from_numpy(barrier._table(types).reshape(-1).copy()).cuda()
+    force = torch.zeros((max(N, 1), 4), dtype=dt_, device="cuda")
+    vir = torch.full((6, max(N, 1)), float("nan"), dtype=dt_, device="cuda")
+    out = _lib.Forces()
+    out.force = force.data_ptr()
+    out.virial = vir.data_ptr()
+    out.virial_pitch = max(N, 1)
+    out.precision = prec
+    _lib.check(L.azp_harmonic_barrier_forces(ctypes.byref(sysd), barrier.geometry, float(location),
+                                             params_d.data_ptr(), ctypes.byref(out), _stream()),
+               "azp_harmonic_barrier_forces")
+    torch.cuda.synchronize()
+    f = force[:N].double().cpu().numpy()
+    w = vir[:, :N].double().cpu().numpy().T.copy()
+    return f, w

@@ -8,8 +8,13 @@ import numpy as np
 
 from . import _lib
 from .bond import Bond
+from .external import HarmonicBarrier
 from .methods import BrownianFlow, LangevinFlow
 from .pair import Pair
+from .variant import Constant
+
+# rows of the engine's barrier-location table (AZP_MD_BARRIER_ROWS)
+BARRIER_ROWS = 65536
 
 
 def _stream():
@@ -19,17 +24,19 @@ def _stream():
 
 
 def split_forces(integ):
+    """(pair, bond, barrier) of the integrator's forces, each None when absent."""
     pairs = [f for f in integ.forces if isinstance(f, Pair)]
     bonds = [f for f in integ.forces if isinstance(f, Bond)]
-    other = [f for f in integ.forces if not isinstance(f, (Pair, Bond))]
+    barriers = [f for f in integ.forces if isinstance(f, HarmonicBarrier)]
+    other = [f for f in integ.forces if not isinstance(f, (Pair, Bond, HarmonicBarrier))]
     if other:
         raise NotImplementedError(f"unsupported force objects: {other}")
-    if len(pairs) > 1 or len(bonds) > 1:
-        raise NotImplementedError("the engine advances at most one pair and one bond potential")
+    if len(pairs) > 1 or len(bonds) > 1 or len(barriers) > 1:
+        raise NotImplementedError("the engine advances at most one pair, one bond and one barrier potential")
     if pairs and pairs[0]._name == "DPDGeneralWeight":
         raise NotImplementedError("DPDGeneralWeight runs through the drop-in driver (azp_dpd_forces); "
                                   "the resident engine does not take it")
-    return (pairs[0] if pairs else None), (bonds[0] if bonds else None)
+    return (pairs[0] if pairs else None), (bonds[0] if bonds else None), (barriers[0] if barriers else None)
 
 
 class Engine:
@@ -37,7 +44,7 @@ class Engine:
 
     @staticmethod
     def config_key(sim, integ):
-        pair, bond = split_forces(integ)
+        pair, bond, barrier = split_forces(integ)
         if len(integ.methods) != 1 or not isinstance(integ.methods[0], (LangevinFlow, BrownianFlow)):
             raise NotImplementedError("exactly one LangevinFlow or BrownianFlow method is required")
         m = integ.methods[0]
@@ -50,6 +57,9 @@ class Engine:
                       pair.nlist.exclusions]
         if bond is not None:
             parts += [type(bond).__name__, sorted((k, sorted(v.items())) for k, v in bond.params.items())]
+        if barrier is not None:
+            # the location is not part of the key: it is tabulated run by run
+            parts += [type(barrier).__name__, sorted((k, sorted(v.items())) for k, v in barrier.params.items())]
         return repr(parts)
 
     def __init__(self, sim, integ, snap):
@@ -58,7 +68,7 @@ class Engine:
         import torch  # noqa: F401  (initialises the CUDA context used by torch streams)
 
         self._L = L
-        pair, bond = split_forces(integ)
+        pair, bond, barrier = split_forces(integ)
         m = integ.methods[0]
         p = snap.particles
         types = list(p.types)
@@ -110,12 +120,22 @@ class Engine:
         c.flow = m.flow_field._record()
         c.max_displacement = getattr(m, "max_displacement", 0.0)
         c.pair_force_cap = getattr(m, "force_cap", 0.0)
+        self._barrier = barrier
+        self._box = tuple(snap.configuration.box[:3])
+        self._brownian = isinstance(m, BrownianFlow)
+        if barrier is not None:
+            c.barrier_geometry = barrier.geometry
+            c.barrier_params = arr(barrier._table(types).reshape(-1))
+        else:
+            c.barrier_geometry = 0
+            c.barrier_params = None
         st = ctypes.c_int(0)
         self._md = L.azp_md_create(ctypes.byref(c), ctypes.byref(st))
         _lib.check(st.value, "azp_md_create")
         self.N = p.N
         self.has_accel = p.acceleration is not None
         self.last_launches = 0
+        self.timestep = 0
 
     def push(self, snap, timestep):
         p = snap.particles
@@ -135,6 +155,7 @@ class Engine:
                                      None if acc is None else acc.ctypes.data, img.ctypes.data, diam.ctypes.data,
                                      int(timestep), 0, s),
             "azp_md_set_state")
+        self.timestep = int(timestep)
 
     def pull(self, snap):
         p = snap.particles
@@ -151,10 +172,52 @@ class Engine:
         p.acceleration = acc
         p.image = img
 
+    def _set_barrier(self, t0, steps):
+        """Tabulate the barrier's locations for the timesteps whose forces a run of
+        ``steps`` from ``t0`` evaluates (t0 .. t0 + steps), checked against the box
+        as HarmonicBarrier::makeEvaluator checks them (src/HarmonicBarrier.h:121-130)."""
+        loc = self._barrier.location
+        if isinstance(loc, Constant):
+            vals = np.array([loc.value])
+        elif hasattr(loc, "values"):
+            vals = np.asarray(loc.values(t0, steps + 1), dtype=np.float64)
+        else:
+            vals = np.array([float(loc(t)) for t in range(t0, t0 + steps + 1)], dtype=np.float64)
+        for v in np.unique(vals):
+            if not self._barrier._valid(float(v), self._box):
+                raise RuntimeError("Barrier position is invalid")
+        vals = np.ascontiguousarray(vals)
+        _lib.check(self._L.azp_md_set_barrier_locations(self._md, int(t0), len(vals), vals.ctypes.data, _stream()),
+                   "azp_md_set_barrier_locations")
+
+    def _chunks(self, steps):
+        """Runs of at most BARRIER_ROWS - 1 steps when a moving barrier is tabulated."""
+        steps = int(steps)
+        if self._barrier is None:
+            yield steps
+            return
+        if isinstance(self._barrier.location, Constant):
+            self._set_barrier(self.timestep, steps)
+            yield steps
+            return
+        while steps > 0:
+            n = min(steps, BARRIER_ROWS - 1)
+            self._set_barrier(self.timestep, n)
+            yield n
+            steps -= n
+
+    def prepare_forces(self):
+        """Before a forces-only evaluation (azp_md_forces / azp_md_thermo): the
+        barrier location of the current timestep."""
+        if self._barrier is not None:
+            self._set_barrier(self.timestep, 0)
+
     def run(self, steps):
         """Advance with the overflow-safe entry (grows the list and replays)."""
         s = _stream()
-        _lib.check(self._L.azp_md_run_checked(self._md, int(steps), s), "azp_md_run_checked")
+        for n in self._chunks(steps):
+            _lib.check(self._L.azp_md_run_checked(self._md, n, s), "azp_md_run_checked")
+            self.timestep += n
         self.last_launches = int(self._L.azp_md_last_launches(self._md))
         err = ctypes.c_uint32(0)
         _lib.check(self._L.azp_md_error(self._md, ctypes.byref(err), s), "azp_md_error")
@@ -172,10 +235,13 @@ class Engine:
 
     def run_async(self, steps):
         """Enqueue ``steps`` timesteps without reading the error word back."""
-        _lib.check(self._L.azp_md_run(self._md, int(steps), _stream()), "azp_md_run")
+        for n in self._chunks(steps):
+            _lib.check(self._L.azp_md_run(self._md, n, _stream()), "azp_md_run")
+            self.timestep += n
         self.last_launches = int(self._L.azp_md_last_launches(self._md))
 
     def forces(self):
+        self.prepare_forces()
         f = np.empty((self.N, 4))
         w = np.empty((self.N, 6))
         _lib.check(self._L.azp_md_forces(self._md, f.ctypes.data, w.ctypes.data, 0, _stream()), "azp_md_forces")
@@ -183,6 +249,8 @@ class Engine:
 
     def thermo(self):
         out = np.zeros(9)
+        # a barrier's forces are re-evaluated at the location of the current timestep
+        self.prepare_forces()
         _lib.check(self._L.azp_md_thermo(self._md, out.ctypes.data, _stream()), "azp_md_thermo")
         return {
             "potential_energy": out[0],

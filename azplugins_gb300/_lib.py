@@ -37,6 +37,7 @@ MODES = {"none": 0, "shift": 1, "xplor": 2}
 FP64, FP32 = 0, 1
 FLOW_CONSTANT, FLOW_PARABOLIC = 0, 1
 METHOD_LANGEVIN, METHOD_BROWNIAN = 0, 1
+BARRIER_GEOMETRIES = {"planar": 0, "spherical": 1}
 EBIT_NLIST_OVERFLOW, EBIT_BOND, EBIT_NONFINITE, EBIT_TIMEOUT = 0x1, 0x2, 0x4, 0x8
 
 
@@ -113,6 +114,8 @@ class MDConfig(ctypes.Structure):
         ("flow", Flow),
         ("max_displacement", ctypes.c_double),
         ("pair_force_cap", ctypes.c_double),
+        ("barrier_geometry", ctypes.c_int32),
+        ("barrier_params", ctypes.c_void_p),
     ]
 
 
@@ -168,6 +171,7 @@ _SIGNATURES = [
     ("azp_pair_forces_static", _i, [ctypes.POINTER(System), _vp, _vp, _u32, _i, _vp, _vp, _vp, _i,
                                     ctypes.POINTER(Forces), _vp]),
     ("azp_dpd_forces", _i, [ctypes.POINTER(System), _vp, _vp, _vp, _d, _d, _u64, _u32, ctypes.POINTER(Forces), _vp]),
+    ("azp_harmonic_barrier_forces", _i, [ctypes.POINTER(System), _i, _d, _vp, ctypes.POINTER(Forces), _vp]),
     ("azp_bond_forces", _i, [ctypes.POINTER(System), _vp, _vp, _u32, _i, _vp, _u32, ctypes.POINTER(Forces), _vp, _vp]),
     ("azp_pair_adjoint", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
     ("azp_bond_adjoint", _i, [ctypes.POINTER(System), _vp, _vp, _i, _vp, _u32, _vp, _vp, _vp, _vp, _vp]),
@@ -179,6 +183,7 @@ _SIGNATURES = [
     ("azp_md_destroy", None, [_vp]),
     ("azp_md_set_state", _i, [_vp, _vp, _vp, _vp, _vp, _vp, _u64, _i, _vp]),
     ("azp_md_get_state", _i, [_vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64), _i, _vp]),
+    ("azp_md_set_barrier_locations", _i, [_vp, _u64, _u32, _vp, _vp]),
     ("azp_md_run", _i, [_vp, _u64, _vp]),
     ("azp_md_run_checked", _i, [_vp, _u64, _vp]),
     ("azp_md_forces", _i, [_vp, _vp, _vp, _i, _vp]),

@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "celllist.cuh"
@@ -517,6 +518,13 @@ struct azp_md {
     double* d_pair_table = nullptr;
     double* d_gamma = nullptr;
     double* d_noise = nullptr;
+    // harmonic barrier (bar_geom -1: none): per-type (k, offset), the device table
+    // of per-(timestep, type) records and its header (first timestep, rows)
+    int bar_geom = -1;
+    std::vector<double> bar_params;
+    double* d_bar_tab = nullptr;  // 16-byte records, as double pairs
+    unsigned long long* d_bar_hdr = nullptr;
+    bool bar_set = false;
     // control
     uint32_t* flags = nullptr;  // [0] rebuild request [1] error bits [2] builds [3] max count [4] ticket
     unsigned long long* d_ts = nullptr;
@@ -582,7 +590,8 @@ void free_all(azp_md* m)
                     m->cuts, m->bt_n_tag, m->bt_partner_tag, m->bt_type_tag, m->bt_n, m->bt, m->ex_n, m->ex_idx,
                     m->d_bond_params, m->d_pair_table, m->d_gamma, m->d_noise, m->flags, m->d_ts, m->out_force, m->out_virial,
                     m->partials, m->thermo, m->tmp4, m->tmpd, m->snap_pos, m->snap_vel, m->snap_acc,
-                    m->snap_img, m->snap_diam, m->st_pos, m->st_vel, m->st_acc, m->st_img, m->st_diam};
+                    m->snap_img, m->snap_diam, m->st_pos, m->st_vel, m->st_acc, m->st_img, m->st_diam,
+                    m->d_bar_tab, m->d_bar_hdr};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -668,6 +677,9 @@ MDArgs base_args(azp_md* m)
         DoubleWellBond::prepare_f(m->bond_params.data(), a.bond0);
     a.gamma0 = m->gamma.empty() ? 0.0f : (float)m->gamma[0];
     a.noise0 = m->noise_host.empty() ? 0.0f : (float)m->noise_host[0];
+    a.bar_geom = m->bar_geom;
+    a.bar_tab = m->d_bar_tab;
+    a.bar_hdr = m->d_bar_hdr;
     a.flowf.kind = m->flow.kind;
     if (m->flow.kind == AZP_FLOW_PARABOLIC) {
         a.flowf.a = (float)m->flow.a;
@@ -1108,6 +1120,16 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         CTRY(cudaMemcpy(m->d_bond_params, m->bond_params.data(), sizeof(double) * m->bond_params.size(),
                                 cudaMemcpyHostToDevice));
     }
+    // harmonic barrier: the table of a run's locations is filled by
+    // azp_md_set_barrier_locations before the first run
+    if (c->barrier_params) {
+        if (c->barrier_geometry != AZP_BARRIER_PLANAR && c->barrier_geometry != AZP_BARRIER_SPHERICAL)
+            return fail(AZP_ERR_INVALID, m);
+        m->bar_geom = c->barrier_geometry;
+        m->bar_params.assign(c->barrier_params, c->barrier_params + 2 * (size_t)c->ntypes);
+        ALLOC(m->d_bar_tab, (size_t)2 * AZP_MD_BARRIER_ROWS * c->ntypes);
+        ALLOC(m->d_bar_hdr, 2);
+    }
     CTRY(cudaStreamCreateWithFlags(&m->graph_stream, cudaStreamNonBlocking));
 #undef ALLOC
 #undef CTRY
@@ -1248,9 +1270,48 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
     return AZP_OK;
 }
 
+int azp_md_set_barrier_locations(azp_md* m, uint64_t t_first, uint32_t n, const double* location, void* stream)
+{
+    if (!m || m->bar_geom < 0 || n == 0 || !location) return AZP_ERR_INVALID;
+    if (n > AZP_MD_BARRIER_ROWS) {
+        const std::string msg = "azp_md_set_barrier_locations: " + std::to_string(n) + " rows exceed the table of " +
+                                std::to_string(AZP_MD_BARRIER_ROWS) + " (set the locations run by run)";
+        return record_error(AZP_ERR_TOO_LARGE, msg.c_str());
+    }
+    for (uint32_t r = 0; r < n; ++r)
+        if (!barrier_location_valid(m->bar_geom, location[r], m->box))
+            return record_error(AZP_ERR_INVALID, "Barrier position is invalid");
+    const uint32_t nt = m->ntypes;
+    // records of c = location + offset (the driver's addition), FP64 (c, k) or FP32
+    std::vector<double> tab((size_t)2 * n * nt);
+    for (uint32_t r = 0; r < n; ++r)
+        for (uint32_t t = 0; t < nt; ++t) {
+            const double k = m->bar_params[2 * t], c = location[r] + m->bar_params[2 * t + 1];
+            double* rec = &tab[2 * ((size_t)r * nt + t)];
+            if (m->precision == AZP_FP32) {
+                const BarrierRecF f = barrier_rec_f(m->bar_geom, c, k, m->box.L[1]);
+                std::memcpy(rec, &f, sizeof(f));
+            } else {
+                rec[0] = c;
+                rec[1] = k;
+            }
+        }
+    const unsigned long long hdr[2] = {(unsigned long long)t_first, (unsigned long long)n};
+    cudaStream_t s = as_stream(stream);
+    // pageable sources: both copies are staged before the calls return
+    AZP_CUDA_TRY(cudaMemcpyAsync(m->d_bar_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, s));
+    AZP_CUDA_TRY(cudaMemcpyAsync(m->d_bar_hdr, hdr, sizeof(hdr), cudaMemcpyHostToDevice, s));
+    AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    m->bar_set = true;
+    m->forces_valid = false;
+    return AZP_OK;
+}
+
 int azp_md_run(azp_md* m, uint64_t steps, void* stream)
 {
     if (!m || !m->have_state) return AZP_ERR_INVALID;
+    if (m->bar_geom >= 0 && !m->bar_set)
+        return record_error(AZP_ERR_INVALID, "azp_md_run: the barrier locations are not set");
     m->launches = 0;
     if (steps == 0 || m->N == 0) return AZP_OK;
     m->forces_valid = false;
@@ -1297,6 +1358,8 @@ int azp_md_run(azp_md* m, uint64_t steps, void* stream)
 int azp_md_forces(azp_md* m, double* force, double* virial, int on_device, void* stream)
 {
     if (!m || !m->have_state) return AZP_ERR_INVALID;
+    if (m->bar_geom >= 0 && !m->bar_set)
+        return record_error(AZP_ERR_INVALID, "azp_md_forces: the barrier locations are not set");
     cudaStream_t s = as_stream(stream);
     const uint32_t N = m->N;
     if (N == 0) return AZP_OK;
@@ -1325,6 +1388,8 @@ int azp_md_thermo(azp_md* m, double* out, void* stream)
     for (int c = 0; c < 9; ++c) out[c] = 0.0;
     if (N == 0) return AZP_OK;
     if (!m->forces_valid) {
+        if (m->bar_geom >= 0 && !m->bar_set)
+            return record_error(AZP_ERR_INVALID, "azp_md_thermo: the barrier locations are not set");
         int st = enqueue_rebuild(m, s, m->flags);
         if (st) return st;
         MDArgs a = base_args(m);

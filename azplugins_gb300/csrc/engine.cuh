@@ -78,6 +78,14 @@ struct MDArgs {
     float bond0[MD_BOND_F];
     double rc2_0;
     float gamma0, noise0;
+    // harmonic barrier added to the net force (bar_geom -1: none). bar_tab holds
+    // one record per (row, type): FP64 steps double2 (c = location + offset, k),
+    // FP32 steps BarrierRecF; row r belongs to timestep bar_hdr[0] + r (clamped to
+    // the bar_hdr[1] rows). A Langevin step at timestep t evaluates the forces of
+    // the positions of t + 1, a Brownian step and a forces-only launch those of t.
+    int bar_geom;
+    const void* bar_tab;
+    const unsigned long long* bar_hdr;
 };
 
 constexpr int MD_INTEG_LANGEVIN = 0;

@@ -9,6 +9,7 @@
 // integrate.cu) and through them the reference lines cited there.
 #pragma once
 
+#include "barrier.cuh"
 #include "engine.cuh"
 #include "evaluators.cuh"
 #include "pair.cuh"
@@ -170,6 +171,42 @@ struct AccFx {
     AZP_D double U() const { return (double)u.s + (double)u.c; }
 };
 
+// ---------------------------------------------------------------- harmonic barrier
+// record offset of (timestep ts, type ti) in the barrier table (rows clamped)
+AZP_D size_t barrier_slot(const MDArgs& a, unsigned long long ts, uint32_t ti)
+{
+    const unsigned long long t0 = a.bar_hdr[0], rows = a.bar_hdr[1];
+    const unsigned long long r = ts <= t0 ? 0ull : min(ts - t0, rows - 1ull);
+    return (size_t)r * a.ntypes + ti;
+}
+
+// FP64: the barrier force and energy of particle i (position p) at timestep ts
+AZP_D void barrier_fp64(const MDArgs& a, const double4_32a& p, unsigned long long ts, double* f, double& e)
+{
+    const double2 ck = __ldg(reinterpret_cast<const double2*>(a.bar_tab) + barrier_slot(a, ts, type_of(p.w)));
+    const double x[3] = {p.x, p.y, p.z};
+    if (a.bar_geom == AZP_BARRIER_PLANAR)
+        planar_barrier(x, ck.x, ck.y, f, e);
+    else
+        spherical_barrier(x, ck.x, ck.y, f, e);
+}
+
+// FP32: the same on the fixed-point shadow fi (hi words, type in w)
+AZP_D void barrier_fx(const MDArgs& a, const uint4& fi, unsigned long long ts, float* f, float& e)
+{
+    const BarrierRecF* tab = reinterpret_cast<const BarrierRecF*>(a.bar_tab);
+    const size_t k = barrier_slot(a, ts, fi.w);
+    BarrierRecF r;
+    const int4 raw = __ldg(reinterpret_cast<const int4*>(tab + k));
+    r.q = (long long)(((unsigned long long)(uint32_t)raw.y << 32) | (uint32_t)raw.x);
+    r.c = __int_as_float(raw.z);
+    r.k = __int_as_float(raw.w);
+    if (a.bar_geom == AZP_BARRIER_PLANAR)
+        planar_barrier_fx(fi, r, a.sfix[1], f, e);
+    else
+        spherical_barrier_fx(fi, r, a.sfix, f, e);
+}
+
 // |fixed - fixed at the last build|^2 > threshold, in FP32 on exact integer differences
 AZP_D bool displaced(const uint4& f, const uint4& fb, const float* sfix, float thresh2)
 {
@@ -266,9 +303,18 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
 
     bool want_rebuild = false;
     if (active && sub == 0) {
-        const double Fx = acc.Fx(), Fy = acc.Fy(), Fz = acc.Fz();
+        double Fx = acc.Fx(), Fy = acc.Fy(), Fz = acc.Fz();
+        double Ub = 0.0;
+        if (a.bar_geom >= 0) {
+            // the barrier's force joins the net force (src/HarmonicBarrier.h:149-180)
+            double fb[3] = {0.0, 0.0, 0.0};
+            barrier_fp64(a, a.pos[i], *a.d_timestep + (INTEG == MD_INTEG_LANGEVIN ? 1ull : 0ull), fb, Ub);
+            Fx += fb[0];
+            Fy += fb[1];
+            Fz += fb[2];
+        }
         if (a.out) {
-            a.out_force[i] = make_double4_32a(Fx, Fy, Fz, acc.U());
+            a.out_force[i] = make_double4_32a(Fx, Fy, Fz, acc.U() + Ub);
             for (int c = 0; c < 6; ++c) a.out_virial[(size_t)c * a.N + i] = (double)acc.w[c];
         }
         if constexpr (INTEG != MD_FORCES_ONLY) {
@@ -541,15 +587,20 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
 
     bool want_rebuild = false;
     if (active && sub == 0) {
+        float fb[3] = {0.0f, 0.0f, 0.0f}, ub = 0.0f;
+        if (a.bar_geom >= 0)
+            // the barrier's force joins the net force (src/HarmonicBarrier.h:149-180)
+            barrier_fx(a, fi, *a.d_timestep + (INTEG == MD_INTEG_LANGEVIN ? 1ull : 0ull), fb, ub);
         if constexpr (OUT) {
-            a.out_force[i] = make_double4_32a(acc.Fx(), acc.Fy(), acc.Fz(), acc.U());
+            a.out_force[i] = make_double4_32a(acc.Fx() + fb[0], acc.Fy() + fb[1], acc.Fz() + fb[2], acc.U() + ub);
             for (int c = 0; c < 6; ++c) a.out_virial[(size_t)c * a.N + i] = (double)acc.w[c];
         }
         if constexpr (INTEG != MD_FORCES_ONLY) {
             const unsigned long long ts = *a.d_timestep;
             const uint32_t ti = fi.w;
             const uint32_t tg = __ldg(a.tag + i);
-            const float fx = acc.fx.s + acc.fx.c, fy = acc.fy.s + acc.fy.c, fz = acc.fz.s + acc.fz.c;
+            const float fx = acc.fx.s + (acc.fx.c + fb[0]), fy = acc.fy.s + (acc.fy.c + fb[1]),
+                        fz = acc.fz.s + (acc.fz.c + fb[2]);
             const float gam = a.use_lambda ? a.lambdaf * (float)a.diameter[i] : s_gamma[ti];
             const float c = a.noiseless ? 0.0f : (a.use_lambda ? sqrtf(6.0f * gam * a.kTf / a.dtf) : s_noise[ti]);
             float ux, uy, uz;

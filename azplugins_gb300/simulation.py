@@ -131,6 +131,13 @@ class State:
 class _Operations:
     def __init__(self):
         self.integrator = None
+        self.computes = []
+
+    def add(self, op):
+        """Add a force as a compute (HOOMD ``Operations.add``): it is not
+        integrated, its ``forces`` / ``energies`` / ``virials`` are read."""
+        if op not in self.computes:
+            self.computes.append(op)
 
 
 class Integrator:
@@ -188,7 +195,7 @@ class Simulation:
         integ = self.operations.integrator
         if integ is None:
             raise RuntimeError("set sim.operations.integrator first")
-        for f in integ.forces:
+        for f in list(integ.forces) + list(self.operations.computes):
             f._sim = self
         return integ
 

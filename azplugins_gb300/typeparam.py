@@ -12,6 +12,32 @@ from __future__ import annotations
 import copy
 
 
+class _Entry(dict):
+    """The dict ``params[key]`` returns: a copy whose ``update`` / item assignment
+    write back into the owner (``barrier.params["A"].update(k=..., offset=...)``
+    as in src/pytest/test_external.py:65). Keys still missing stay missing until
+    they are set; the tables that use the entry report them."""
+
+    def __init__(self, owner, key, values):
+        super().__init__(values)
+        self._owner = owner
+        self._key = key
+
+    def _store(self):
+        self._owner._data[self._key] = dict(self)
+
+    def update(self, *args, **kw):
+        new = dict(*args, **kw)
+        self._owner._check_keys(new)
+        super().update({k: float(v) for k, v in new.items()})
+        self._store()
+
+    def __setitem__(self, k, v):
+        self._owner._check_keys({k: v})
+        super().__setitem__(k, float(v))
+        self._store()
+
+
 class TypeParameterDict:
     """Dict of parameter dicts (or scalars) with required keys and defaults."""
 
@@ -40,15 +66,18 @@ class TypeParameterDict:
         return [self._norm(key)]
 
     # ------------------------------------------------------------------ values
+    def _check_keys(self, value):
+        allowed = set(self._required) | set(self._defaults)
+        extra = set(value) - allowed
+        if extra:
+            raise KeyError(f"{self._name}: unknown keys {sorted(extra)}; expected {sorted(allowed)}")
+
     def _validate(self, value):
         if self._scalar:
             return float(value)
         if not isinstance(value, dict):
             raise TypeError(f"{self._name} values are dicts, got {type(value).__name__}")
-        allowed = set(self._required) | set(self._defaults)
-        extra = set(value) - allowed
-        if extra:
-            raise KeyError(f"{self._name}: unknown keys {sorted(extra)}; expected {sorted(allowed)}")
+        self._check_keys(value)
         out = dict(self._defaults)
         out.update({k: float(v) for k, v in value.items()})
         missing = [k for k in self._required if k not in out]
@@ -63,10 +92,19 @@ class TypeParameterDict:
 
     def __getitem__(self, key):
         k = self._norm(key)
+        if self._scalar:
+            if k in self._data:
+                return self._data[k]
+            if self._default_value is not None:
+                return self._default_value
+            raise KeyError(f"{self._name}[{key!r}] is not set")
         if k in self._data:
-            return copy.copy(self._data[k])
+            return _Entry(self, k, self._data[k])
         if self._default_value is not None:
-            return copy.copy(self._default_value)
+            return _Entry(self, k, self._default_value)
+        if self._len == 1:
+            # unset type: an entry holding the defaults, filled in by update()
+            return _Entry(self, k, self._defaults)
         raise KeyError(f"{self._name}[{key!r}] is not set")
 
     def __contains__(self, key):

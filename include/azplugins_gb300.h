@@ -21,6 +21,7 @@
  *   Brownian flow       gpu::brownian_flow<Flow>, src/TwoStepBrownianFlowGPU.cuh:26-44
  *   flow fields         src/ConstantFlow.h:30-65, src/ParabolicFlow.h:51-98
  *   RNG stream ids      src/RNGIdentifiers.h:20-27
+ *   harmonic barriers   HarmonicBarrierGPU<Evaluator>, src/HarmonicBarrierGPU.cuh:50-83
  */
 #ifndef AZPLUGINS_GB300_H_
 #define AZPLUGINS_GB300_H_
@@ -243,6 +244,24 @@ AZP_API int azp_dpd_forces(const azp_system* sys, azp_nlist* nl, const double* p
                            double kT, double dt, uint64_t timestep, uint32_t seed, const azp_forces* out,
                            void* stream);
 
+/* Moving harmonic barriers (replaces HarmonicBarrierGPU<Evaluator>::computeForces
+ * and kernel::compute_harmonic_barrier, src/HarmonicBarrierGPU.cuh:50-83, with
+ * src/PlanarBarrierEvaluator.h:36-56 and src/SphericalBarrierEvaluator.h:36-61).
+ * geometry AZP_BARRIER_PLANAR: U = k/2 (y - H - offset)^2 above y = H + offset,
+ * pushing -y; AZP_BARRIER_SPHERICAL: U = k/2 (r - R - offset)^2 beyond
+ * r = R + offset, pushing inward. location: H or R, the value of the barrier's
+ * variant at the timestep (HarmonicBarrier::makeEvaluator evaluates it, :121-130).
+ * params: device [ntypes][2] doubles (k, offset). Each position is wrapped into
+ * the box first (:168-170). OVERWRITES out->force (fx, fy, fz, energy) and zeroes
+ * out->virial (may be NULL): the reference does not compute the virial (:177-179).
+ * A location that fails the evaluator's valid(box) -- planar: -Ly/2 <= H < Ly/2;
+ * spherical: R >= 0 and 2R <= each edge -- returns AZP_ERR_INVALID with
+ * "Barrier position is invalid" in azp_last_error, before any device work.
+ * Arithmetic FP64 in both output precisions. */
+enum azp_barrier_geometry { AZP_BARRIER_PLANAR = 0, AZP_BARRIER_SPHERICAL = 1 };
+AZP_API int azp_harmonic_barrier_forces(const azp_system* sys, int geometry, double location, const double* params,
+                                        const azp_forces* out, void* stream);
+
 /* Bond forces from a per-particle bond table (replaces
  * gpu_compute_bond_forces<Eval,2>): for particle i its bonds are
  * table[k * N + i] = (partner index, bond type) for k < n_bonds[i].
@@ -328,10 +347,26 @@ typedef struct {
     azp_flow flow;
     double max_displacement;    /* Brownian only; 0 = uncapped */
     double pair_force_cap;      /* > 0: |pair force| capped per pair (overlap relaxation); 0 = off */
+    /* harmonic barrier added to the net force inside the fused step (the
+     * reference's HarmonicBarrier in the integrator's forces, src/HarmonicBarrier.h) */
+    int32_t barrier_geometry;   /* azp_barrier_geometry (read when barrier_params is set) */
+    const double* barrier_params; /* host [ntypes][2] (k, offset); NULL: no barrier */
 } azp_md_config;
 
 AZP_API azp_md* azp_md_create(const azp_md_config* cfg, int* status);
 AZP_API void azp_md_destroy(azp_md* md);
+/* Locations of the engine's harmonic barrier (its variant's values, host array):
+ * location[r] belongs to timestep t_first + r, r < n <= AZP_MD_BARRIER_ROWS. The
+ * forces of the positions at timestep t use the location of t: a Langevin step at
+ * t evaluates t + 1 (HOOMD computes the net force of t + 1 between the two
+ * halves), a Brownian step t; timesteps outside the rows take the nearest row, so
+ * a constant barrier needs one row. Every location is checked as by
+ * azp_harmonic_barrier_forces (AZP_ERR_INVALID, "Barrier position is invalid").
+ * Must be called before the first run of an engine with a barrier; synchronises
+ * the stream. */
+#define AZP_MD_BARRIER_ROWS 65536u
+AZP_API int azp_md_set_barrier_locations(azp_md* md, uint64_t t_first, uint32_t n, const double* location,
+                                         void* stream);
 /* Load state in TAG order from host (on_device == 0) or device pointers:
  * pos [N][4] (w = type as an integer-valued double), vel [N][4] (w = mass),
  * accel [N][3], image [N][3], diameter [N] or NULL. */

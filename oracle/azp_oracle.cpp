@@ -25,6 +25,9 @@
 //                       with |dx|^2 < (r_cut_ij + r_buff)^2, r_cut_ij > 0,
 //                       minus exclusions; rebuilt when a particle moved more
 //                       than r_buff/2 since the last build.
+//   * harmonic barrier  src/HarmonicBarrier.h:149-180,
+//                       src/PlanarBarrierEvaluator.h:36-56,
+//                       src/SphericalBarrierEvaluator.h:36-61
 //   * Philox4x32-10     Salmon, Moraes, Dror, Shaw, SC'11 (published algorithm)
 //
 // Compiled with -ffp-contract=off so that x86 and Arm builds round alike.
@@ -897,6 +900,53 @@ void orc_brownian(int N, double* pos, int32_t* image, const int32_t* type, const
         wrap(b, x, image + 3 * i);
         for (int d = 0; d < 3; ++d) pos[4 * i + d] = x[d];
     }
+}
+
+// ---- harmonic barriers (src/HarmonicBarrier.h:149-180: wrap each position into
+// the box, then the evaluator with the type's (k, offset); the virial is not
+// computed). geometry 0: src/PlanarBarrierEvaluator.h:36-47 (push -y above
+// y = H + offset); 1: src/SphericalBarrierEvaluator.h:36-51 (push inward beyond
+// r = R + offset). params[2 * type] = {k, offset}. Writes force[3N], energy[N].
+// Returns 0, or -1 when the location fails the evaluator's valid(box)
+// (PlanarBarrierEvaluator.h:50-56, SphericalBarrierEvaluator.h:54-61).
+int orc_barrier_valid(int geometry, double location, const double* L)
+{
+    if (geometry == 0) return (location >= -0.5 * L[1] && location < 0.5 * L[1]) ? 0 : -1;
+    const double two_R = 2.0 * location;
+    // nearest plane distances of an orthorhombic box are its edge lengths
+    return (location >= 0.0 && L[0] >= two_R && L[1] >= two_R && L[2] >= two_R) ? 0 : -1;
+}
+
+int orc_harmonic_barrier(int N, const double* pos, const int32_t* type, const double* L, int geometry,
+                         double location, const double* params, double* force, double* energy)
+{
+    if (orc_barrier_valid(geometry, location, L)) return -1;
+    const Box b = make_box(L);
+    for (int i = 0; i < N; ++i) {
+        double x[3] = {pos[4 * i], pos[4 * i + 1], pos[4 * i + 2]};
+        int img[3] = {0, 0, 0};
+        wrap(b, x, img);
+        const double k = params[2 * type[i]], offset = params[2 * type[i] + 1];
+        double f[3] = {0.0, 0.0, 0.0}, e = 0.0;
+        if (geometry == 0) {
+            const double dy = x[1] - (location + offset);
+            if (dy > 0.0) {
+                f[1] = -k * dy;
+                e = -0.5 * f[1] * dy;
+            }
+        } else {
+            const double r = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+            const double dr = r - (location + offset);
+            if (dr > 0.0) {
+                const double k_dr = k * dr;
+                for (int d = 0; d < 3; ++d) f[d] = -(k_dr / r) * x[d];
+                e = 0.5 * k_dr * dr;
+            }
+        }
+        for (int d = 0; d < 3; ++d) force[3 * i + d] = f[d];
+        energy[i] = e;
+    }
+    return 0;
 }
 
 // ---- maximum squared displacement since the last list build

@@ -66,7 +66,8 @@ def lib():
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(_LIB_PATH):
+    src = os.path.join(_HERE, "azp_oracle.cpp")
+    if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
         build()
     L = ctypes.CDLL(_LIB_PATH)
     c_int, c_long, c_double, c_u32, c_u64 = (
@@ -102,6 +103,8 @@ def lib():
     L.orc_brownian.argtypes = [c_int, _dp, _ip, _ip, _dp, _up, vp, _dp, c_int, c_double, c_int, _dp, _dp, c_double, c_double, c_u64, c_u32, c_int, c_double]
     L.orc_max_disp2.argtypes = [c_int, _dp, _dp, _dp]
     L.orc_max_disp2.restype = c_double
+    L.orc_barrier_valid.argtypes = [c_int, c_double, _dp]
+    L.orc_harmonic_barrier.argtypes = [c_int, _dp, _ip, _dp, c_int, c_double, _dp, _dp, _dp]
     _lib = L
     return L
 
@@ -257,6 +260,32 @@ def dpd_forces(pos4, vel4, types, tags, ntypes, L, start, idx, params, rcutsq, k
     return F, U, W
 
 
+BARRIER_GEOMETRIES = {"planar": 0, "spherical": 1}
+
+
+def harmonic_barrier(pos4, types, L, geometry, location, params):
+    """Harmonic barrier force [N,3] and energy [N] (src/HarmonicBarrier.h:149-180);
+    geometry "planar" or "spherical", params [ntypes, 2] = (k, offset). Raises
+    ValueError("Barrier position is invalid") like the reference's makeEvaluator."""
+    N = pos4.shape[0]
+    F = np.zeros((N, 3))
+    U = np.zeros(N)
+    st = lib().orc_harmonic_barrier(
+        N,
+        np.ascontiguousarray(pos4, dtype=np.float64),
+        np.ascontiguousarray(types, dtype=np.int32),
+        np.ascontiguousarray(L, dtype=np.float64),
+        BARRIER_GEOMETRIES[geometry],
+        float(location),
+        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        F,
+        U,
+    )
+    if st:
+        raise ValueError("Barrier position is invalid")
+    return F, U
+
+
 def bond_forces(pos4, L, bonds, btypes, name, params, F=None, U=None, W=None):
     """Bond forces (accumulated into F/U/W if given). Raises on a refused bond."""
     N = pos4.shape[0]
@@ -356,7 +385,7 @@ class OracleMD:
 
     def __init__(self, system, pair=None, bond=None, method="langevin", gamma=(1.0,), flow_kind=0,
                  flow_p=(0.0, 0.0, 0.0), kT=1.0, dt=0.005, seed=0, r_buff=0.4, noiseless=False, exclude_bonds=True,
-                 max_disp=0.0, force_cap=0.0):
+                 max_disp=0.0, force_cap=0.0, barrier=None):
         self.s = {k: (np.ascontiguousarray(v).copy() if isinstance(v, np.ndarray) else v) for k, v in system.items()}
         s = self.s
         self.N = s["pos4"].shape[0]
@@ -371,6 +400,8 @@ class OracleMD:
         self.noiseless = noiseless
         self.max_disp = max_disp
         self.force_cap = force_cap
+        # dict(geometry, location: float or callable(timestep), params [ntypes, 2])
+        self.barrier = barrier
         self.timestep = int(s.get("timestep", 0))
         self.ntypes = int(s.get("ntypes", int(s["types"].max()) + 1))
         self.exclusions = s["bonds"] if (exclude_bonds and s.get("bonds") is not None and len(s["bonds"])) else None
@@ -395,7 +426,9 @@ class OracleMD:
         self.pos_build = s["pos4"].copy()
         self.builds += 1
 
-    def forces(self):
+    def forces(self, timestep=None):
+        """Net force, energy and virial at the current positions; ``timestep`` is the
+        one the positions belong to (the barrier location's argument)."""
         s = self.s
         N = self.N
         F = np.zeros((N, 3))
@@ -410,6 +443,13 @@ class OracleMD:
                                   self.pair["params"], rc * rc, ronsq, self.pair.get("mode", "none"), self.force_cap)
         if self.bond is not None and self.table is not None:
             bond_forces_pp(s["pos4"], s["L"], self.table, self.bond["name"], self.bond["params"], F, U, W)
+        if self.barrier is not None:
+            loc = self.barrier["location"]
+            t = self.timestep if timestep is None else timestep
+            Fb, Ub = harmonic_barrier(s["pos4"], s["types"], s["L"], self.barrier["geometry"],
+                                      loc(t) if callable(loc) else loc, self.barrier["params"])
+            F = F + Fb
+            U = U + Ub
         return F, U, W
 
     def step(self):
@@ -417,11 +457,11 @@ class OracleMD:
         t = self.timestep
         if self.method == "langevin":
             langevin_step1(s["pos4"], s["image"], s["vel4"], s["accel"], s["L"], self.dt)
-            F, U, W = self.forces()
+            F, U, W = self.forces(t + 1)
             langevin_step2(s["pos4"], s["types"], s["vel4"], s["accel"], F, s["tags"], self.gamma, self.flow_kind,
                            self.flow_p, self.kT, self.dt, t, self.seed, self.noiseless)
         else:
-            F, U, W = self.forces()
+            F, U, W = self.forces(t)
             brownian(s["pos4"], s["image"], s["types"], F, s["tags"], self.gamma, self.flow_kind, self.flow_p,
                      s["L"], self.kT, self.dt, t, self.seed, self.noiseless, max_disp=self.max_disp)
         self.timestep = t + 1
