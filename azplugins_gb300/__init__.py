@@ -8,7 +8,7 @@ hand-written CUDA kernels through the C ABI declared in
 ``include/azplugins_gb300.h``; there is no CPU path.
 """
 
-from . import bond, external, flow, methods, nlist, pair, variant
+from . import bond, compute, external, filter, flow, methods, nlist, pair, variant, wall
 from .simulation import Integrator, Simulation, Snapshot, State
 
 __version__ = "0.1.0"
@@ -20,4 +20,4 @@ class md:  # noqa: N801
     nlist = nlist
 
 
-__all__ = ["bond", "external", "flow", "variant", "methods", "nlist", "pair", "md", "Integrator", "Simulation", "Snapshot", "State"]
+__all__ = ["bond", "compute", "external", "filter", "flow", "variant", "wall", "methods", "nlist", "pair", "md", "Integrator", "Simulation", "Snapshot", "State"]

@@ -283,3 +283,78 @@ def barrier_forces(state, barrier, precision, timestep):
     f = force[:N].double().cpu().numpy()
     w = vir[:, :N].double().cpu().numpy().T.copy()
     return f, w
+
+
+def wall_forces(state, pot, precision):
+    """(force4 [N,4], virial [N,6]) of a wall potential at the state."""
+    torch = _torch()
+    _lib.require_gpu()
+    L = _lib.load()
+    snap = state._arrays()
+    p = snap.particles
+    N = p.N
+    types = list(p.types)
+    rec, rc, rx = pot._tables(types)
+    walls, keep = pot._walls_struct()
+    pos = device_positions(snap)
+    sysd = make_system(snap, pos)
+    prec = _lib.FP32 if precision == "fp32" else _lib.FP64
+    dt_ = torch.float32 if prec == _lib.FP32 else torch.float64
+    dev = [torch.from_numpy(np.ascontiguousarray(a).reshape(-1).copy()).cuda() for a in (rec, rc, rx)]
+    force = torch.zeros((max(N, 1), 4), dtype=dt_, device="cuda")
+    vir = torch.zeros((6, max(N, 1)), dtype=dt_, device="cuda")
+    out = _lib.Forces()
+    out.force = force.data_ptr()
+    out.virial = vir.data_ptr()
+    out.virial_pitch = max(N, 1)
+    out.precision = prec
+    _lib.check(L.azp_wall_forces(ctypes.byref(sysd), pot.kind, ctypes.byref(walls), dev[0].data_ptr(),
+                                 dev[1].data_ptr(), dev[2].data_ptr(), ctypes.byref(out), _stream()),
+               "azp_wall_forces")
+    torch.cuda.synchronize()
+    del keep
+    f = force[:N].double().cpu().numpy()
+    w = vir[:, :N].double().cpu().numpy().T.copy()
+    return f, w
+
+
+def velocity_field(snap, kind, num_bins, lower, upper, members):
+    """(mass [nb], momentum [nb, 3], velocity [nb, 3]) through ``azp_vfield_*``;
+    members: uint32 index array, or None for every particle."""
+    torch = _torch()
+    _lib.require_gpu()
+    L = _lib.load()
+    p = snap.particles
+    N = p.N
+    nb = np.ascontiguousarray(num_bins, dtype=np.uint32)
+    lo = np.ascontiguousarray(lower, dtype=np.float64)
+    hi = np.ascontiguousarray(upper, dtype=np.float64)
+    st = ctypes.c_int(0)
+    vf = L.azp_vfield_create(int(kind), nb.ctypes.data, lo.ctypes.data, hi.ctypes.data, ctypes.byref(st))
+    _lib.check(st.value, "azp_vfield_create")
+    try:
+        total = int(L.azp_vfield_num_bins(vf))
+        pos = device_positions(snap)
+        vel = torch.zeros((max(N, 1), 4), dtype=torch.float64, device="cuda")
+        if N:
+            vel[:N, :3] = torch.from_numpy(np.ascontiguousarray(p.velocity, dtype=np.float64)).cuda()
+            vel[:N, 3] = torch.from_numpy(np.ascontiguousarray(p.mass, dtype=np.float64)).cuda()
+        sysd = make_system(snap, pos, vel=vel.data_ptr())
+        group = None
+        n_group = 0
+        if members is not None:
+            group = torch.from_numpy(np.ascontiguousarray(members, dtype=np.int32).reshape(-1)).cuda()
+            n_group = int(group.numel())
+            group = torch.cat([group, torch.zeros(1, dtype=torch.int32, device="cuda")])  # never empty
+        out = torch.zeros((total, 7), dtype=torch.float64, device="cuda")
+        mass, mom, velo = out[:, 0].contiguous(), out[:, 1:4].contiguous(), out[:, 4:7].contiguous()
+        _lib.check(L.azp_vfield_compute(vf, ctypes.byref(sysd), None if group is None else group.data_ptr(), n_group,
+                                        mass.data_ptr(), mom.data_ptr(), velo.data_ptr(), _stream()),
+                   "azp_vfield_compute")
+        err = ctypes.c_uint32(0)
+        _lib.check(L.azp_vfield_error(vf, ctypes.byref(err), _stream()), "azp_vfield_error")
+        if err.value & _lib.EBIT_RANGE:
+            raise _lib.AzpError(-11, "azp_vfield_compute (a momentum above the fixed-point range)")
+        return mass.cpu().numpy(), mom.cpu().numpy(), velo.cpu().numpy()
+    finally:
+        L.azp_vfield_destroy(vf)

@@ -12,6 +12,7 @@ from .external import HarmonicBarrier
 from .methods import BrownianFlow, LangevinFlow
 from .pair import Pair
 from .variant import Constant
+from .wall import WallPotential
 
 # rows of the engine's barrier-location table (AZP_MD_BARRIER_ROWS)
 BARRIER_ROWS = 65536
@@ -24,19 +25,19 @@ def _stream():
 
 
 def split_forces(integ):
-    """(pair, bond, barrier) of the integrator's forces, each None when absent."""
-    pairs = [f for f in integ.forces if isinstance(f, Pair)]
-    bonds = [f for f in integ.forces if isinstance(f, Bond)]
-    barriers = [f for f in integ.forces if isinstance(f, HarmonicBarrier)]
-    other = [f for f in integ.forces if not isinstance(f, (Pair, Bond, HarmonicBarrier))]
+    """(pair, bond, barrier, wall) of the integrator's forces, each None when absent."""
+    kinds = (Pair, Bond, HarmonicBarrier, WallPotential)
+    found = [[f for f in integ.forces if isinstance(f, k)] for k in kinds]
+    other = [f for f in integ.forces if not isinstance(f, kinds)]
     if other:
         raise NotImplementedError(f"unsupported force objects: {other}")
-    if len(pairs) > 1 or len(bonds) > 1 or len(barriers) > 1:
-        raise NotImplementedError("the engine advances at most one pair, one bond and one barrier potential")
+    if any(len(x) > 1 for x in found):
+        raise NotImplementedError("the engine advances at most one pair, one bond, one barrier and one wall potential")
+    pairs = found[0]
     if pairs and pairs[0]._name == "DPDGeneralWeight":
         raise NotImplementedError("DPDGeneralWeight runs through the drop-in driver (azp_dpd_forces); "
                                   "the resident engine does not take it")
-    return (pairs[0] if pairs else None), (bonds[0] if bonds else None), (barriers[0] if barriers else None)
+    return tuple(x[0] if x else None for x in found)
 
 
 class Engine:
@@ -44,7 +45,7 @@ class Engine:
 
     @staticmethod
     def config_key(sim, integ):
-        pair, bond, barrier = split_forces(integ)
+        pair, bond, barrier, wall = split_forces(integ)
         if len(integ.methods) != 1 or not isinstance(integ.methods[0], (LangevinFlow, BrownianFlow)):
             raise NotImplementedError("exactly one LangevinFlow or BrownianFlow method is required")
         m = integ.methods[0]
@@ -60,6 +61,8 @@ class Engine:
         if barrier is not None:
             # the location is not part of the key: it is tabulated run by run
             parts += [type(barrier).__name__, sorted((k, sorted(v.items())) for k, v in barrier.params.items())]
+        if wall is not None:
+            parts += [type(wall).__name__, repr(wall.walls), sorted((k, sorted(v.items())) for k, v in wall.params.items())]
         return repr(parts)
 
     def __init__(self, sim, integ, snap):
@@ -68,7 +71,7 @@ class Engine:
         import torch  # noqa: F401  (initialises the CUDA context used by torch streams)
 
         self._L = L
-        pair, bond, barrier = split_forces(integ)
+        pair, bond, barrier, wall = split_forces(integ)
         m = integ.methods[0]
         p = snap.particles
         types = list(p.types)
@@ -129,6 +132,18 @@ class Engine:
         else:
             c.barrier_geometry = 0
             c.barrier_params = None
+        if wall is not None:
+            rec_w, rc_w, rx_w = wall._tables(types)
+            walls, keep = wall._walls_struct()
+            self._keep += [walls, keep]
+            c.wall_kind = wall.kind
+            c.walls = ctypes.addressof(walls)
+            c.wall_params = arr(rec_w.reshape(-1))
+            c.wall_r_cut = arr(rc_w)
+            c.wall_r_extrap = arr(rx_w)
+        else:
+            c.wall_kind = 0
+            c.walls = None
         st = ctypes.c_int(0)
         self._md = L.azp_md_create(ctypes.byref(c), ctypes.byref(st))
         _lib.check(st.value, "azp_md_create")

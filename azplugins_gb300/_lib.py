@@ -38,7 +38,10 @@ FP64, FP32 = 0, 1
 FLOW_CONSTANT, FLOW_PARABOLIC = 0, 1
 METHOD_LANGEVIN, METHOD_BROWNIAN = 0, 1
 BARRIER_GEOMETRIES = {"planar": 0, "spherical": 1}
+WALL_KINDS = {"LJ93": 0, "Colloid": 1}
 EBIT_NLIST_OVERFLOW, EBIT_BOND, EBIT_NONFINITE, EBIT_TIMEOUT = 0x1, 0x2, 0x4, 0x8
+EBIT_RANGE = 0x20
+BINNING_KINDS = {"cartesian": 0, "cylindrical": 1}
 
 
 class AzpError(RuntimeError):
@@ -84,6 +87,27 @@ class Forces(ctypes.Structure):
     ]
 
 
+class WallSphere(ctypes.Structure):
+    _fields_ = [("r", ctypes.c_double), ("origin", ctypes.c_double * 3), ("inside", ctypes.c_int32),
+                ("open", ctypes.c_int32)]
+
+
+class WallCylinder(ctypes.Structure):
+    _fields_ = [("r", ctypes.c_double), ("origin", ctypes.c_double * 3), ("axis", ctypes.c_double * 3),
+                ("inside", ctypes.c_int32), ("open", ctypes.c_int32)]
+
+
+class WallPlane(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_double * 3), ("normal", ctypes.c_double * 3), ("open", ctypes.c_int32),
+                ("pad_", ctypes.c_int32)]
+
+
+class Walls(ctypes.Structure):
+    _fields_ = [("n_spheres", ctypes.c_uint32), ("n_cylinders", ctypes.c_uint32), ("n_planes", ctypes.c_uint32),
+                ("pad_", ctypes.c_uint32), ("spheres", ctypes.c_void_p), ("cylinders", ctypes.c_void_p),
+                ("planes", ctypes.c_void_p)]
+
+
 class MDConfig(ctypes.Structure):
     _fields_ = [
         ("N", ctypes.c_uint32),
@@ -116,6 +140,11 @@ class MDConfig(ctypes.Structure):
         ("pair_force_cap", ctypes.c_double),
         ("barrier_geometry", ctypes.c_int32),
         ("barrier_params", ctypes.c_void_p),
+        ("wall_kind", ctypes.c_int32),
+        ("walls", ctypes.c_void_p),
+        ("wall_params", ctypes.c_void_p),
+        ("wall_r_cut", ctypes.c_void_p),
+        ("wall_r_extrap", ctypes.c_void_p),
     ]
 
 
@@ -172,6 +201,15 @@ _SIGNATURES = [
                                     ctypes.POINTER(Forces), _vp]),
     ("azp_dpd_forces", _i, [ctypes.POINTER(System), _vp, _vp, _vp, _d, _d, _u64, _u32, ctypes.POINTER(Forces), _vp]),
     ("azp_harmonic_barrier_forces", _i, [ctypes.POINTER(System), _i, _d, _vp, ctypes.POINTER(Forces), _vp]),
+    ("azp_wall_params_from_values", _i, [_i, _vp, _vp]),
+    ("azp_wall_params_to_values", _i, [_i, _vp, _vp]),
+    ("azp_wall_forces", _i, [ctypes.POINTER(System), _i, ctypes.POINTER(Walls), _vp, _vp, _vp, ctypes.POINTER(Forces),
+                             _vp]),
+    ("azp_vfield_create", _vp, [_i, _vp, _vp, _vp, ctypes.POINTER(_i)]),
+    ("azp_vfield_destroy", None, [_vp]),
+    ("azp_vfield_num_bins", _u32, [_vp]),
+    ("azp_vfield_compute", _i, [_vp, ctypes.POINTER(System), _vp, _u32, _vp, _vp, _vp, _vp]),
+    ("azp_vfield_error", _i, [_vp, ctypes.POINTER(_u32), _vp]),
     ("azp_bond_forces", _i, [ctypes.POINTER(System), _vp, _vp, _u32, _i, _vp, _u32, ctypes.POINTER(Forces), _vp, _vp]),
     ("azp_pair_adjoint", _i, [ctypes.POINTER(System), _vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
     ("azp_bond_adjoint", _i, [ctypes.POINTER(System), _vp, _vp, _i, _vp, _u32, _vp, _vp, _vp, _vp, _vp]),

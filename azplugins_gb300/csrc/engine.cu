@@ -525,6 +525,11 @@ struct azp_md {
     double* d_bar_tab = nullptr;  // 16-byte records, as double pairs
     unsigned long long* d_bar_hdr = nullptr;
     bool bar_set = false;
+    // wall potential (wall_kind -1: none): the walls and the per-type table
+    int wall_kind = -1;
+    WallField* d_walls = nullptr;
+    double* d_wall_tab = nullptr;
+    float wall_tol = 0.0f;
     // control
     uint32_t* flags = nullptr;  // [0] rebuild request [1] error bits [2] builds [3] max count [4] ticket
     unsigned long long* d_ts = nullptr;
@@ -591,7 +596,7 @@ void free_all(azp_md* m)
                     m->d_bond_params, m->d_pair_table, m->d_gamma, m->d_noise, m->flags, m->d_ts, m->out_force, m->out_virial,
                     m->partials, m->thermo, m->tmp4, m->tmpd, m->snap_pos, m->snap_vel, m->snap_acc,
                     m->snap_img, m->snap_diam, m->st_pos, m->st_vel, m->st_acc, m->st_img, m->st_diam,
-                    m->d_bar_tab, m->d_bar_hdr};
+                    m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -680,6 +685,10 @@ MDArgs base_args(azp_md* m)
     a.bar_geom = m->bar_geom;
     a.bar_tab = m->d_bar_tab;
     a.bar_hdr = m->d_bar_hdr;
+    a.wall_kind = m->wall_kind;
+    a.walls = m->d_walls;
+    a.wall_tab = m->d_wall_tab;
+    a.wall_tol = m->wall_tol;
     a.flowf.kind = m->flow.kind;
     if (m->flow.kind == AZP_FLOW_PARABOLIC) {
         a.flowf.a = (float)m->flow.a;
@@ -1129,6 +1138,32 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         m->bar_params.assign(c->barrier_params, c->barrier_params + 2 * (size_t)c->ntypes);
         ALLOC(m->d_bar_tab, (size_t)2 * AZP_MD_BARRIER_ROWS * c->ntypes);
         ALLOC(m->d_bar_hdr, 2);
+    }
+    // wall potential: the wall field and per-type rows (record, r_cut^2,
+    // r_extrap, screening reach) in device memory
+    if (c->walls) {
+        if (c->wall_kind != AZP_WALL_LJ93 && c->wall_kind != AZP_WALL_COLLOID) return fail(AZP_ERR_INVALID, m);
+        if (!c->wall_params || !c->wall_r_cut || !c->wall_r_extrap) return fail(AZP_ERR_INVALID, m);
+        WallField wf;
+        st = make_wall_field(c->walls, &wf);
+        if (st) return fail(st, m);
+        std::vector<double> tab((size_t)WALL_TAB * c->ntypes, 0.0);
+        for (uint32_t t = 0; t < c->ntypes; ++t) {
+            for (int k = 0; k < 4; ++k) tab[WALL_TAB * t + k] = c->wall_params[4 * t + k];
+            const double rc = c->wall_r_cut[t], rx = c->wall_r_extrap[t];
+            if (!(rc >= 0.0) || !(rx >= 0.0)) return fail(AZP_ERR_INVALID, m);
+            tab[WALL_TAB * t + 4] = rc * rc;
+            tab[WALL_TAB * t + 5] = rx;
+            tab[WALL_TAB * t + 6] = std::max(rc, rx);
+        }
+        ALLOC(m->d_walls, 1);
+        ALLOC(m->d_wall_tab, tab.size());
+        CTRY(cudaMemcpy(m->d_walls, &wf, sizeof(wf), cudaMemcpyHostToDevice));
+        CTRY(cudaMemcpy(m->d_wall_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+        m->wall_kind = c->wall_kind;
+        // the FP32 screen's positions are good to a few L 2^-24 (hi word, float scale)
+        const double Lmax = std::max(m->box.L[0], std::max(m->box.L[1], m->box.L[2]));
+        m->wall_tol = (float)(4e-6 * Lmax + 1e-5);
     }
     CTRY(cudaStreamCreateWithFlags(&m->graph_stream, cudaStreamNonBlocking));
 #undef ALLOC

@@ -4,6 +4,7 @@
 #include "common.cuh"
 #include "fixed64.cuh"
 #include "integrate.cuh"
+#include "walls.cuh"
 
 namespace azp
 {
@@ -86,6 +87,12 @@ struct MDArgs {
     int bar_geom;
     const void* bar_tab;
     const unsigned long long* bar_hdr;
+    // wall potential added to the net force (wall_kind -1: none); wall_tab per
+    // type: record (4), r_cut^2, r_extrap, r_cut, - ; walls in device memory
+    int wall_kind;
+    const WallField* walls;
+    const double* wall_tab;
+    float wall_tol;             // FP32 screening margin (FP32-force step)
 };
 
 constexpr int MD_INTEG_LANGEVIN = 0;

@@ -207,6 +207,64 @@ AZP_D void barrier_fx(const MDArgs& a, const uint4& fi, unsigned long long ts, f
         spherical_barrier_fx(fi, r, a.sfix, f, e);
 }
 
+// ---------------------------------------------------------------- walls
+// wall_tab row of a type: record (4 doubles), r_cut^2, r_extrap, r_cut, -
+constexpr int WALL_TAB = 8;
+
+// FP64 force and energy of every wall on a particle at x (type t), added to
+// F[0..2] and F[3]. Out of line: its registers and stack do not count against
+// the step's neighbour loop.
+static __device__ __noinline__ void engine_walls(int kind, const WallField* __restrict__ wf, const double* __restrict__ tab,
+                                          double x0, double x1, double x2, uint32_t t, double* F)
+{
+    const double* row = tab + (size_t)t * WALL_TAB;
+    const double p[4] = {row[0], row[1], row[2], row[3]};
+    const double x[3] = {x0, x1, x2};
+    double f[3] = {0.0, 0.0, 0.0}, u = 0.0;
+    if (kind == AZP_WALL_LJ93)
+        walls_force<WallLJ93>(*wf, p, row[4], row[5], x, f, u);
+    else
+        walls_force<WallColloid>(*wf, p, row[4], row[5], x, f, u);
+    F[0] += f[0];
+    F[1] += f[1];
+    F[2] += f[2];
+    F[3] += u;
+}
+
+// FP32 screen of the FP32-force step: could any wall act on a particle at
+// (x, y, z) (positions good to about L 2^-24, covered by tol)? A wall acts within
+// r_cut on its active side, and anywhere on its inactive side with r_extrap > 0.
+AZP_D bool walls_near_f(const WallField* __restrict__ wf, const double* __restrict__ tab, uint32_t t, float x,
+                        float y, float z, float tol)
+{
+    const double* row = tab + (size_t)t * WALL_TAB;
+    const float reach = (float)row[6] + tol;
+    const bool extrap = row[5] > 0.0;
+    for (int k = 0; k < wf->ns; ++k) {
+        const WallSphereD& w = wf->s[k];
+        const float dx = x - (float)w.o[0], dy = y - (float)w.o[1], dz = z - (float)w.o[2];
+        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float d = w.inside ? (float)w.r - r : r - (float)w.r;
+        if (d < reach && (extrap || d > -tol)) return true;
+    }
+    for (int k = 0; k < wf->nc; ++k) {
+        const WallCylinderD& w = wf->c[k];
+        const float dx = x - (float)w.o[0], dy = y - (float)w.o[1], dz = z - (float)w.o[2];
+        const float al = dx * (float)w.ax[0] + dy * (float)w.ax[1] + dz * (float)w.ax[2];
+        const float px = dx - al * (float)w.ax[0], py = dy - al * (float)w.ax[1], pz = dz - al * (float)w.ax[2];
+        const float r = sqrtf(px * px + py * py + pz * pz);
+        const float d = w.inside ? (float)w.r - r : r - (float)w.r;
+        if (d < reach && (extrap || d > -tol)) return true;
+    }
+    for (int k = 0; k < wf->np; ++k) {
+        const WallPlaneD& w = wf->p[k];
+        const float d = (x - (float)w.o[0]) * (float)w.n[0] + (y - (float)w.o[1]) * (float)w.n[1] +
+                        (z - (float)w.o[2]) * (float)w.n[2];
+        if (d < reach && (extrap || d > -tol)) return true;
+    }
+    return false;
+}
+
 // |fixed - fixed at the last build|^2 > threshold, in FP32 on exact integer differences
 AZP_D bool displaced(const uint4& f, const uint4& fb, const float* sfix, float thresh2)
 {
@@ -313,9 +371,31 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
             Fy += fb[1];
             Fz += fb[2];
         }
+        double fw[4] = {0.0, 0.0, 0.0, 0.0};
+        double4_32a pw;
+        if (a.wall_kind >= 0) {
+            // the wall potential's force joins the net force (HOOMD adds the
+            // external wall compute into net_force)
+            pw = a.pos[i];
+            engine_walls(a.wall_kind, a.walls, a.wall_tab, pw.x, pw.y, pw.z, type_of(pw.w), fw);
+            Fx += fw[0];
+            Fy += fw[1];
+            Fz += fw[2];
+            Ub += fw[3];
+        }
         if (a.out) {
             a.out_force[i] = make_double4_32a(Fx, Fy, Fz, acc.U() + Ub);
-            for (int c = 0; c < 6; ++c) a.out_virial[(size_t)c * a.N + i] = (double)acc.w[c];
+            double wv[6] = {(double)acc.w[0], (double)acc.w[1], (double)acc.w[2],
+                            (double)acc.w[3], (double)acc.w[4], (double)acc.w[5]};
+            if (a.wall_kind >= 0) {
+                wv[0] += fw[0] * pw.x;
+                wv[1] += fw[0] * pw.y;
+                wv[2] += fw[0] * pw.z;
+                wv[3] += fw[1] * pw.y;
+                wv[4] += fw[1] * pw.z;
+                wv[5] += fw[2] * pw.z;
+            }
+            for (int c = 0; c < 6; ++c) a.out_virial[(size_t)c * a.N + i] = wv[c];
         }
         if constexpr (INTEG != MD_FORCES_ONLY) {
             const unsigned long long ts = *a.d_timestep;
@@ -544,6 +624,22 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
     const uint32_t sub = gid & (tpp - 1u);
     const bool active = i < a.N;
     constexpr bool vir = OUT;
+    // walls first, while nothing else is live: an FP32 screen on the high words,
+    // then the FP64 evaluation on the full 64-bit position for the particles some
+    // wall can reach; the result waits in this thread's shared-memory slot
+    __shared__ float4 s_wall[MD_BLOCK];
+    if (a.wall_kind >= 0 && active && sub == 0) {
+        const uint4 hw = __ldg(a.fix + i);
+        double fw[4] = {0.0, 0.0, 0.0, 0.0};
+        if (walls_near_f(a.walls, a.wall_tab, hw.w, (float)(int32_t)hw.x * a.sfix[0],
+                         (float)(int32_t)hw.y * a.sfix[1], (float)(int32_t)hw.z * a.sfix[2], a.wall_tol)) {
+            const uint4 lw = __ldg(a.flo + i);
+            engine_walls(a.wall_kind, a.walls, a.wall_tab, fx_to_double(fx_join(hw.x, lw.x), a.l64[0]),
+                         fx_to_double(fx_join(hw.y, lw.y), a.l64[1]), fx_to_double(fx_join(hw.z, lw.z), a.l64[2]),
+                         hw.w, fw);
+        }
+        s_wall[threadIdx.x] = make_float4((float)fw[0], (float)fw[1], (float)fw[2], (float)fw[3]);
+    }
     AccFx acc;
     uint4 fi = make_uint4(0u, 0u, 0u, 0u);
     if (active) {
@@ -591,16 +687,33 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
         if (a.bar_geom >= 0)
             // the barrier's force joins the net force (src/HarmonicBarrier.h:149-180)
             barrier_fx(a, fi, *a.d_timestep + (INTEG == MD_INTEG_LANGEVIN ? 1ull : 0ull), fb, ub);
+        // the walls' force, evaluated before the neighbour loop
+        const float4 fw = a.wall_kind >= 0 ? s_wall[threadIdx.x] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if constexpr (OUT) {
-            a.out_force[i] = make_double4_32a(acc.Fx() + fb[0], acc.Fy() + fb[1], acc.Fz() + fb[2], acc.U() + ub);
-            for (int c = 0; c < 6; ++c) a.out_virial[(size_t)c * a.N + i] = (double)acc.w[c];
+            a.out_force[i] = make_double4_32a(acc.Fx() + fb[0] + fw.x, acc.Fy() + fb[1] + fw.y,
+                                              acc.Fz() + fb[2] + fw.z, acc.U() + ub + fw.w);
+            double wv[6];
+            for (int c = 0; c < 6; ++c) wv[c] = (double)acc.w[c];
+            if (a.wall_kind >= 0) {
+                // the wall virial F_a x_b (FP32 position: 2^-24 relative)
+                const float x = (float)(int32_t)fi.x * a.sfix[0], y = (float)(int32_t)fi.y * a.sfix[1],
+                            z = (float)(int32_t)fi.z * a.sfix[2];
+                wv[0] += fw.x * x;
+                wv[1] += fw.x * y;
+                wv[2] += fw.x * z;
+                wv[3] += fw.y * y;
+                wv[4] += fw.y * z;
+                wv[5] += fw.z * z;
+            }
+            for (int c = 0; c < 6; ++c) a.out_virial[(size_t)c * a.N + i] = wv[c];
         }
         if constexpr (INTEG != MD_FORCES_ONLY) {
             const unsigned long long ts = *a.d_timestep;
             const uint32_t ti = fi.w;
             const uint32_t tg = __ldg(a.tag + i);
-            const float fx = acc.fx.s + (acc.fx.c + fb[0]), fy = acc.fy.s + (acc.fy.c + fb[1]),
-                        fz = acc.fz.s + (acc.fz.c + fb[2]);
+            const float fx = acc.fx.s + (acc.fx.c + (fb[0] + fw.x));
+            const float fy = acc.fy.s + (acc.fy.c + (fb[1] + fw.y));
+            const float fz = acc.fz.s + (acc.fz.c + (fb[2] + fw.z));
             const float gam = a.use_lambda ? a.lambdaf * (float)a.diameter[i] : s_gamma[ti];
             const float c = a.noiseless ? 0.0f : (a.use_lambda ? sqrtf(6.0f * gam * a.kTf / a.dtf) : s_noise[ti]);
             float ux, uy, uz;

@@ -1,0 +1,182 @@
+// walls.cu -- azp_wall_forces: the azplugins wall potentials (LJ93, Colloid) over
+// HOOMD's wall geometries, as the drop-in for
+// gpu_compute_potential_external_forces<EvaluatorWalls<WallEvaluator*>>
+// (src/PotentialExternalWallGPUKernel.cu.inc:26-30), and their param_type
+// builders (src/WallEvaluatorLJ93.h:31-45, src/WallEvaluatorColloid.h:31-53).
+//
+// One thread per particle; the walls travel as a kernel argument (HOOMD passes
+// its wall field by value too), so every thread reads them from the constant
+// bank. Arithmetic FP64 in both output precisions: each particle costs a few
+// dozen operations per wall against 32 bytes read and up to 80 written.
+#include <cmath>
+
+#include "common.cuh"
+#include "walls.cuh"
+
+namespace azp
+{
+namespace
+{
+constexpr int kBlock = 128;
+
+template<class EV, typename T>
+__global__ void __launch_bounds__(kBlock) k_walls(const double4_32a* __restrict__ pos,
+                                                  const double4_32a* __restrict__ params,
+                                                  const double* __restrict__ r_cut,
+                                                  const double* __restrict__ r_extrap, const WallField wf, uint32_t N,
+                                                  T* __restrict__ force, T* __restrict__ virial, uint32_t pitch)
+{
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= N) return;
+    const double4_32a pp = pos[i];
+    const uint32_t t = type_of(pp.w);
+    const double4_32a rec = params[t];
+    const double p[4] = {rec.x, rec.y, rec.z, rec.w};
+    const double rc = __ldg(r_cut + t);
+    const double x[3] = {pp.x, pp.y, pp.z};
+    double F[3] = {0.0, 0.0, 0.0}, U = 0.0;
+    walls_force<EV>(wf, p, rc * rc, __ldg(r_extrap + t), x, F, U);
+    if constexpr (sizeof(T) == 8)
+        reinterpret_cast<double4_32a*>(force)[i] = make_double4_32a(F[0], F[1], F[2], U);
+    else
+        reinterpret_cast<float4*>(force)[i] = make_float4((float)F[0], (float)F[1], (float)F[2], (float)U);
+    if (virial) {
+        const double v[6] = {F[0] * x[0], F[0] * x[1], F[0] * x[2], F[1] * x[1], F[1] * x[2], F[2] * x[2]};
+        for (int c = 0; c < 6; ++c) virial[(size_t)c * pitch + i] = (T)v[c];
+    }
+}
+
+template<class EV>
+void launch_walls(const azp_system* sys, const double* params, const double* r_cut, const double* r_extrap,
+                  const WallField& wf, const azp_forces* out, cudaStream_t s)
+{
+    const uint32_t grid = (sys->N + kBlock - 1) / kBlock;
+    const uint32_t pitch = out->virial_pitch ? out->virial_pitch : sys->N;
+    const auto* pos = reinterpret_cast<const double4_32a*>(sys->pos);
+    const auto* par = reinterpret_cast<const double4_32a*>(params);
+    if (out->precision == AZP_FP64)
+        k_walls<EV, double><<<grid, kBlock, 0, s>>>(pos, par, r_cut, r_extrap, wf, sys->N,
+                                                    static_cast<double*>(out->force),
+                                                    static_cast<double*>(out->virial), pitch);
+    else
+        k_walls<EV, float><<<grid, kBlock, 0, s>>>(pos, par, r_cut, r_extrap, wf, sys->N,
+                                                   static_cast<float*>(out->force), static_cast<float*>(out->virial),
+                                                   pitch);
+}
+
+bool unit(const double* v, double* u)
+{
+    const double n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (!(n > 0.0) || !std::isfinite(n)) return false;
+    for (int d = 0; d < 3; ++d) u[d] = v[d] / n;
+    return true;
+}
+}  // namespace
+
+int make_wall_field(const azp_walls* w, WallField* out)
+{
+    *out = WallField{};
+    if (!w) return AZP_ERR_INVALID;
+    if (w->n_spheres > (uint32_t)WALL_MAX_SPHERES || w->n_cylinders > (uint32_t)WALL_MAX_CYLINDERS ||
+        w->n_planes > (uint32_t)WALL_MAX_PLANES)
+        return record_error(AZP_ERR_INVALID, "azp_wall_forces: more walls than the wall field holds (20 spheres, "
+                                             "20 cylinders, 60 planes)");
+    if ((w->n_spheres && !w->spheres) || (w->n_cylinders && !w->cylinders) || (w->n_planes && !w->planes))
+        return AZP_ERR_INVALID;
+    out->ns = (int)w->n_spheres;
+    out->nc = (int)w->n_cylinders;
+    out->np = (int)w->n_planes;
+    for (int k = 0; k < out->ns; ++k) {
+        const azp_wall_sphere& s = w->spheres[k];
+        if (!(s.r >= 0.0)) return AZP_ERR_INVALID;
+        out->s[k].r = s.r;
+        for (int d = 0; d < 3; ++d) out->s[k].o[d] = s.origin[d];
+        out->s[k].inside = s.inside != 0;
+        out->s[k].open = s.open != 0;
+    }
+    for (int k = 0; k < out->nc; ++k) {
+        const azp_wall_cylinder& c = w->cylinders[k];
+        if (!(c.r >= 0.0) || !unit(c.axis, out->c[k].ax)) return AZP_ERR_INVALID;
+        out->c[k].r = c.r;
+        for (int d = 0; d < 3; ++d) out->c[k].o[d] = c.origin[d];
+        out->c[k].inside = c.inside != 0;
+        out->c[k].open = c.open != 0;
+    }
+    for (int k = 0; k < out->np; ++k) {
+        const azp_wall_plane& p = w->planes[k];
+        if (!unit(p.normal, out->p[k].n)) return AZP_ERR_INVALID;
+        for (int d = 0; d < 3; ++d) out->p[k].o[d] = p.origin[d];
+        out->p[k].open = p.open != 0;
+    }
+    return AZP_OK;
+}
+
+}  // namespace azp
+
+extern "C" {
+
+int azp_wall_params_from_values(int kind, const double* v, double* out)
+{
+    if (!v || !out) return AZP_ERR_INVALID;
+    for (int k = 0; k < 4; ++k) out[k] = 0.0;
+    if (kind == AZP_WALL_LJ93) {
+        // WallParametersLJ93(dict): sigma_3 = sigma^3, A
+        const double A = v[0], sigma = v[1];
+        out[0] = sigma * sigma * sigma;
+        out[1] = A;
+        return AZP_OK;
+    }
+    if (kind == AZP_WALL_COLLOID) {
+        // WallParametersColloid(dict): c_1 = A sigma^6 / 7560, c_2 = A / 6, a
+        const double A = v[0], a = v[1], sigma = v[2];
+        const double sigma_3 = sigma * sigma * sigma;
+        out[0] = A * sigma_3 * sigma_3 / 7560.0;
+        out[1] = A / 6.0;
+        out[2] = a;
+        return AZP_OK;
+    }
+    return AZP_ERR_INVALID;
+}
+
+int azp_wall_params_to_values(int kind, const double* rec, double* v)
+{
+    if (!v || !rec) return AZP_ERR_INVALID;
+    if (kind == AZP_WALL_LJ93) {
+        // asDict(): sigma = cbrt(sigma_3)
+        v[0] = rec[1];
+        v[1] = std::cbrt(rec[0]);
+        return AZP_OK;
+    }
+    if (kind == AZP_WALL_COLLOID) {
+        // asDict(): A = 6 c_2, sigma = (7560 c_1 / A)^(1/6)
+        const double A = 6.0 * rec[1];
+        v[0] = A;
+        v[1] = rec[2];
+        v[2] = std::pow(7560.0 * rec[0] / A, 1.0 / 6.0);
+        return AZP_OK;
+    }
+    return AZP_ERR_INVALID;
+}
+
+int azp_wall_forces(const azp_system* sys, int kind, const azp_walls* walls, const double* params, const double* r_cut,
+                    const double* r_extrap, const azp_forces* out, void* stream)
+{
+    using namespace azp;
+    if (!sys || !out || !out->force) return AZP_ERR_INVALID;
+    if (kind != AZP_WALL_LJ93 && kind != AZP_WALL_COLLOID) return AZP_ERR_INVALID;
+    if (out->precision != AZP_FP64 && out->precision != AZP_FP32) return AZP_ERR_INVALID;
+    WallField wf;
+    const int st = make_wall_field(walls, &wf);
+    if (st) return st;
+    if (sys->N == 0) return AZP_OK;
+    if (!sys->pos || !params || !r_cut || !r_extrap) return AZP_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    if (kind == AZP_WALL_LJ93)
+        launch_walls<WallLJ93>(sys, params, r_cut, r_extrap, wf, out, s);
+    else
+        launch_walls<WallColloid>(sys, params, r_cut, r_extrap, wf, out, s);
+    AZP_CHECK_LAUNCH("k_walls");
+    return AZP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,231 @@
+// walls.cuh -- wall potentials (src/WallEvaluatorLJ93.h, src/WallEvaluatorColloid.h)
+// over HOOMD's wall geometries (spheres, cylinders, planes), as HOOMD's
+// EvaluatorWalls applies a wall evaluator (restated from its documented
+// behaviour; it is not part of the azplugins tree).
+//
+// For each wall: dr = the particle minus the nearest point of the wall surface,
+// and whether the particle is on the wall's active side ("inside"). Standard mode
+// (r_extrap = 0): the energy-shifted evaluator at |dr| on the active side only.
+// Extrapolated mode (r_extrap > 0): the evaluator where the particle is on the
+// active side at least r_extrap from the surface, elsewhere the linear
+// continuation U(r_extrap) + F(r_extrap) (r_extrap - d) with d the signed
+// distance (negative on the inactive side) and the constant force F(r_extrap)
+// directed towards the active side. Energies are whole (no pair halving); the
+// virial is F_a x_b.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace azp
+{
+// limits of HOOMD's wall field (MAX_N_SWALLS, MAX_N_CWALLS, MAX_N_PWALLS)
+constexpr int WALL_MAX_SPHERES = AZP_WALL_MAX_SPHERES;
+constexpr int WALL_MAX_CYLINDERS = AZP_WALL_MAX_CYLINDERS;
+constexpr int WALL_MAX_PLANES = AZP_WALL_MAX_PLANES;
+
+struct WallSphereD {
+    double r, o[3];
+    int inside, open;
+};
+struct WallCylinderD {
+    double r, o[3], ax[3];  // ax: unit axis
+    int inside, open;
+};
+struct WallPlaneD {
+    double o[3], n[3];  // n: unit normal (the active side)
+    int open, pad_;
+};
+// passed by value as a kernel argument (read from the constant bank)
+struct WallField {
+    int ns, nc, np, pad_;
+    WallSphereD s[WALL_MAX_SPHERES];
+    WallCylinderD c[WALL_MAX_CYLINDERS];
+    WallPlaneD p[WALL_MAX_PLANES];
+};
+
+// ---------------------------------------------------------------- evaluators
+// src/WallEvaluatorLJ93.h:100-133: p = {sigma^3, A}; energy shifted at r_cut
+struct WallLJ93 {
+    AZP_HD static bool eval(const double* p, double rsq, double rcutsq, double& fdr, double& e)
+    {
+        const double lj1 = (2.0 / 15.0) * p[1] * p[0] * p[0] * p[0];
+        const double lj2 = p[1] * p[0];
+        if (!(rsq < rcutsq) || lj1 == 0.0) return false;
+        const double r2inv = 1.0 / rsq;
+        const double r3inv = r2inv * sqrt(r2inv);
+        const double r6inv = r3inv * r3inv;
+        fdr = r2inv * r3inv * (9.0 * lj1 * r6inv - 3.0 * lj2);
+        e = r3inv * (lj1 * r6inv - lj2);
+        const double rc2inv = 1.0 / rcutsq;
+        const double rc3inv = rc2inv * sqrt(rc2inv);
+        const double rc6inv = rc3inv * rc3inv;
+        e -= rc3inv * (lj1 * rc6inv - lj2);
+        return true;
+    }
+};
+
+// src/WallEvaluatorColloid.h:118-183: p = {c_1, c_2, a}; energy shifted at r_cut
+struct WallColloid {
+    AZP_HD static double potential(const double* p, double rsq, bool force, double& fdr)
+    {
+        const double c1 = p[0], c2 = p[1], a = p[2];
+        const double r = sqrt(rsq);
+        const double arinv = a / r;
+        const double rma = 1.0 / (r - a), rpa = 1.0 / (r + a);
+        const double r2ma2 = rma * rpa;
+        const double rma2 = rma * rma, rma6 = rma2 * rma2 * rma2;
+        const double rpa2 = rpa * rpa, rpa6 = rpa2 * rpa2 * rpa2;
+        if (force) {
+            const double arinv8 = 8.0 * arinv;
+            fdr = 6.0 * c1 * ((arinv8 - 1.0) * rma2 * rma6 + (arinv8 + 1.0) * rpa2 * rpa6);
+            fdr -= c2 * (4.0 * a * a * arinv * r2ma2 * r2ma2);
+        }
+        const double a7 = 7.0 * a;
+        double en = c1 * ((a7 - r) * rma * rma6 + (a7 + r) * rpa * rpa6);
+        en -= c2 * (2.0 * a * r * r2ma2 + log(rpa / rma));
+        return en;
+    }
+    AZP_HD static bool eval(const double* p, double rsq, double rcutsq, double& fdr, double& e)
+    {
+        if (!(rsq < rcutsq) || p[0] == 0.0 || !(p[2] > 0.0)) return false;
+        double unused = 0.0;
+        e = potential(p, rsq, true, fdr) - potential(p, rcutsq, false, unused);
+        return true;
+    }
+};
+
+// ---------------------------------------------------------------- geometry
+// dr = x - nearest surface point; nrm = unit normal towards the active side at
+// that point (used when the particle lies exactly on the surface)
+AZP_HD void wall_sphere(const WallSphereD& w, const double* x, double* dr, double* nrm, bool& inside)
+{
+    const double t[3] = {x[0] - w.o[0], x[1] - w.o[1], x[2] - w.o[2]};
+    const double rxyz = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+    if (rxyz > 0.0) {
+        inside = (w.inside ? rxyz < w.r : rxyz > w.r) || (rxyz == w.r && !w.open);
+        const double s = w.r / rxyz;
+        for (int d = 0; d < 3; ++d) {
+            dr[d] = t[d] - t[d] * s;
+            nrm[d] = w.inside ? -t[d] / rxyz : t[d] / rxyz;
+        }
+    } else {
+        // at the centre every surface point is nearest: the one along +x
+        inside = w.inside != 0;
+        dr[0] = -w.r;
+        dr[1] = dr[2] = 0.0;
+        nrm[0] = nrm[1] = nrm[2] = 0.0;
+    }
+}
+
+AZP_HD void wall_cylinder(const WallCylinderD& w, const double* x, double* dr, double* nrm, bool& inside)
+{
+    const double t[3] = {x[0] - w.o[0], x[1] - w.o[1], x[2] - w.o[2]};
+    const double along = t[0] * w.ax[0] + t[1] * w.ax[1] + t[2] * w.ax[2];
+    const double pp[3] = {t[0] - along * w.ax[0], t[1] - along * w.ax[1], t[2] - along * w.ax[2]};
+    const double rxy = sqrt(pp[0] * pp[0] + pp[1] * pp[1] + pp[2] * pp[2]);
+    if (rxy > 0.0) {
+        inside = (w.inside ? rxy < w.r : rxy > w.r) || (rxy == w.r && !w.open);
+        const double s = w.r / rxy;
+        for (int d = 0; d < 3; ++d) {
+            dr[d] = pp[d] - pp[d] * s;
+            nrm[d] = w.inside ? -pp[d] / rxy : pp[d] / rxy;
+        }
+    } else {
+        // on the axis: the surface point along the first direction normal to the axis
+        inside = w.inside != 0;
+        double u[3];
+        if (fabs(w.ax[0]) < 0.9) {
+            u[0] = 0.0;
+            u[1] = w.ax[2];
+            u[2] = -w.ax[1];
+        } else {
+            u[0] = -w.ax[2];
+            u[1] = 0.0;
+            u[2] = w.ax[0];
+        }
+        const double un = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        for (int d = 0; d < 3; ++d) {
+            dr[d] = -w.r * u[d] / un;
+            nrm[d] = 0.0;
+        }
+    }
+}
+
+AZP_HD void wall_plane(const WallPlaneD& w, const double* x, double* dr, double* nrm, bool& inside)
+{
+    const double d = (x[0] - w.o[0]) * w.n[0] + (x[1] - w.o[1]) * w.n[1] + (x[2] - w.o[2]) * w.n[2];
+    inside = d > 0.0 || (d == 0.0 && !w.open);
+    for (int k = 0; k < 3; ++k) {
+        dr[k] = d * w.n[k];
+        nrm[k] = w.n[k];
+    }
+}
+
+// one wall's force and energy added to (F, U)
+template<class EV>
+AZP_HD void wall_apply(const double* p, double rcutsq, double rextrap, const double* dr, const double* nrm,
+                       bool inside, double* F, double& U)
+{
+    const double rsq = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+    double fdr = 0.0, e = 0.0;
+    if (rextrap > 0.0) {
+        const double rextrapsq = rextrap * rextrap;
+        if (inside && rsq >= rextrapsq) {
+            if (EV::eval(p, rsq, rcutsq, fdr, e)) {
+                for (int d = 0; d < 3; ++d) F[d] += dr[d] * fdr;
+                U += e;
+            }
+            return;
+        }
+        const double r = sqrt(rsq);
+        double u[3];
+        if (rsq > 0.0) {
+            const double sgn = inside ? 1.0 : -1.0;
+            for (int d = 0; d < 3; ++d) u[d] = sgn * dr[d] / r;
+        } else {
+            for (int d = 0; d < 3; ++d) u[d] = nrm[d];
+        }
+        const double rp = inside ? rextrap - r : rextrap + r;
+        if (EV::eval(p, rextrapsq, rcutsq, fdr, e)) {
+            const double fmag = fdr * rextrap;
+            for (int d = 0; d < 3; ++d) F[d] += u[d] * fmag;
+            U += e + fmag * rp;
+        }
+        return;
+    }
+    if (!inside) return;
+    if (EV::eval(p, rsq, rcutsq, fdr, e)) {
+        for (int d = 0; d < 3; ++d) F[d] += dr[d] * fdr;
+        U += e;
+    }
+}
+
+// all walls: spheres, then cylinders, then planes
+template<class EV>
+AZP_HD void walls_force(const WallField& wf, const double* p, double rcutsq, double rextrap, const double* x,
+                        double* F, double& U)
+{
+    double dr[3], nrm[3];
+    bool inside = false;
+    for (int k = 0; k < wf.ns; ++k) {
+        wall_sphere(wf.s[k], x, dr, nrm, inside);
+        wall_apply<EV>(p, rcutsq, rextrap, dr, nrm, inside, F, U);
+    }
+    for (int k = 0; k < wf.nc; ++k) {
+        wall_cylinder(wf.c[k], x, dr, nrm, inside);
+        wall_apply<EV>(p, rcutsq, rextrap, dr, nrm, inside, F, U);
+    }
+    for (int k = 0; k < wf.np; ++k) {
+        wall_plane(wf.p[k], x, dr, nrm, inside);
+        wall_apply<EV>(p, rcutsq, rextrap, dr, nrm, inside, F, U);
+    }
+}
+
+// host: the C-ABI wall list as a WallField (axes and normals normalised, as
+// HOOMD's wall constructors do); AZP_ERR_INVALID on a bad wall or count
+int make_wall_field(const azp_walls* walls, WallField* out);
+
+}  // namespace azp

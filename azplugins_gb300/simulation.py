@@ -129,15 +129,24 @@ class State:
 
 
 class _Operations:
-    def __init__(self):
+    def __init__(self, sim=None):
         self.integrator = None
         self.computes = []
+        self._sim = sim
 
     def add(self, op):
-        """Add a force as a compute (HOOMD ``Operations.add``): it is not
-        integrated, its ``forces`` / ``energies`` / ``virials`` are read."""
+        """Add a compute, or a force as a compute (HOOMD ``Operations.add``): it
+        is not integrated; its quantities are read at the current state. On a
+        simulation that has run it attaches at once."""
         if op not in self.computes:
             self.computes.append(op)
+        if self._sim is not None and self._sim._has_run:
+            op._sim = self._sim
+
+    def remove(self, op):
+        """Detach a compute (HOOMD ``Operations.remove``)."""
+        self.computes.remove(op)
+        op._sim = None
 
 
 class Integrator:
@@ -167,12 +176,13 @@ class Simulation:
         self.seed = int(seed) & 0xFFFFFFFF
         self.precision = precision
         self.device = device
-        self.operations = _Operations()
+        self.operations = _Operations(self)
         self.state = None
         self._engine = None
         self._engine_key = None
         self._state_changed = False
         self._timestep = 0
+        self._has_run = False
 
     @property
     def timestep(self):
@@ -193,9 +203,7 @@ class Simulation:
     # ------------------------------------------------------------------ run
     def _attach(self):
         integ = self.operations.integrator
-        if integ is None:
-            raise RuntimeError("set sim.operations.integrator first")
-        for f in list(integ.forces) + list(self.operations.computes):
+        for f in list(integ.forces if integ is not None else []) + list(self.operations.computes):
             f._sim = self
         return integ
 
@@ -204,9 +212,12 @@ class Simulation:
         if self.state is None:
             raise RuntimeError("create the state first")
         integ = self._attach()
+        self._has_run = True
         steps = int(steps)
         if steps == 0:
             return
+        if integ is None:
+            raise RuntimeError("set sim.operations.integrator first")
         from . import _engine
 
         key = _engine.Engine.config_key(self, integ)

@@ -22,6 +22,10 @@
  *   flow fields         src/ConstantFlow.h:30-65, src/ParabolicFlow.h:51-98
  *   RNG stream ids      src/RNGIdentifiers.h:20-27
  *   harmonic barriers   HarmonicBarrierGPU<Evaluator>, src/HarmonicBarrierGPU.cuh:50-83
+ *   wall potentials     gpu_compute_potential_external_forces<EvaluatorWalls<...>>,
+ *                       src/PotentialExternalWallGPUKernel.cu.inc:26-30
+ *   velocity fields     VelocityFieldComputeGPU<BinOp>, src/VelocityFieldComputeGPU.cuh:35-72;
+ *                       VelocityComputeGPU, src/VelocityComputeGPU.cu:49-62
  */
 #ifndef AZPLUGINS_GB300_H_
 #define AZPLUGINS_GB300_H_
@@ -64,6 +68,7 @@ enum azp_status {
 #define AZP_EBIT_NONFINITE 0x4u
 #define AZP_EBIT_TIMEOUT 0x8u
 #define AZP_EBIT_CELL_OVERFLOW 0x10u
+#define AZP_EBIT_RANGE 0x20u          /* a value outside a fixed-point range */
 
 /* ------------------------------------------------------------------ kinds */
 enum azp_pair_kind {
@@ -262,6 +267,73 @@ enum azp_barrier_geometry { AZP_BARRIER_PLANAR = 0, AZP_BARRIER_SPHERICAL = 1 };
 AZP_API int azp_harmonic_barrier_forces(const azp_system* sys, int geometry, double location, const double* params,
                                         const azp_forces* out, void* stream);
 
+/* Wall potentials (replaces gpu_compute_potential_external_forces<
+ * EvaluatorWalls<WallEvaluator*>>, src/PotentialExternalWallGPUKernel.cu.inc:26-30,
+ * with src/WallEvaluatorLJ93.h:100-133 and src/WallEvaluatorColloid.h:118-183;
+ * walls as hoomd.wall.Sphere / Cylinder / Plane). For every wall the distance from
+ * the particle to the wall surface is the argument of the energy-shifted
+ * evaluator on the wall's active side (inside a sphere / cylinder with
+ * inside != 0, outside otherwise; the normal's side of a plane; a particle on the
+ * surface counts as active when open == 0). r_extrap > 0 continues the potential
+ * linearly (constant force towards the active side) closer than r_extrap and on
+ * the inactive side. Walls are visited spheres, cylinders, planes; cylinder axes
+ * and plane normals need not be unit (they are normalised). A particle exactly at
+ * a sphere's centre or on a cylinder's axis takes the surface point along a fixed
+ * direction (+x; the first normal of the axis).
+ * params: device [ntypes][4] records (azp_params_wall_*); r_cut, r_extrap: device
+ * [ntypes]. OVERWRITES out->force (fx, fy, fz, energy) and out->virial
+ * (F_a x_b, may be NULL). Arithmetic FP64 in both output precisions. */
+enum azp_wall_kind { AZP_WALL_LJ93 = 0, AZP_WALL_COLLOID = 1 };
+#define AZP_WALL_MAX_SPHERES 20
+#define AZP_WALL_MAX_CYLINDERS 20
+#define AZP_WALL_MAX_PLANES 60
+typedef struct { double r; double origin[3]; int32_t inside; int32_t open; } azp_wall_sphere;
+typedef struct { double r; double origin[3]; double axis[3]; int32_t inside; int32_t open; } azp_wall_cylinder;
+typedef struct { double origin[3]; double normal[3]; int32_t open; int32_t pad_; } azp_wall_plane;
+typedef struct {
+    uint32_t n_spheres, n_cylinders, n_planes, pad_;
+    const azp_wall_sphere* spheres;     /* host */
+    const azp_wall_cylinder* cylinders; /* host */
+    const azp_wall_plane* planes;       /* host */
+} azp_walls;
+/* param_type records, 4 doubles (src/WallEvaluatorLJ93.h:31-56, src/WallEvaluatorColloid.h:31-64) */
+typedef struct { double sigma_3, A, pad_[2]; } azp_params_wall_lj93;
+typedef struct { double c_1, c_2, a, pad_; } azp_params_wall_colloid;
+/* dict constructor / asDict: values LJ93 {A, sigma}, Colloid {A, a, sigma} */
+AZP_API int azp_wall_params_from_values(int kind, const double* values, double* record);
+AZP_API int azp_wall_params_to_values(int kind, const double* record, double* values);
+AZP_API int azp_wall_forces(const azp_system* sys, int kind, const azp_walls* walls, const double* params,
+                            const double* r_cut, const double* r_extrap, const azp_forces* out, void* stream);
+
+/* ------------------------------------------------------------------ velocity fields
+ * Mass-averaged velocity per bin (replaces VelocityFieldComputeGPU<BinOp> with
+ * src/VelocityFieldComputeGPU.cuh:35-72, src/CartesianBinningOperation.h and
+ * src/CylindricalBinningOperation.h; the centre-of-mass velocity of
+ * src/VelocityCompute.h is the Cartesian case with num_bins = {0, 0, 0}).
+ * num_bins[d] = 0 ignores coordinate d; bins of coordinate d span
+ * [lower[d], upper[d]) (Cartesian x, y, z; cylindrical r, theta in [0, 2 pi), z),
+ * flattened with the last coordinate fastest. Each member's position is wrapped
+ * into the box, its momentum m v turned into the bin's coordinates (cylindrical:
+ * v_r, v_theta, v_z) and summed with its mass; velocity = momentum / mass, 0 in an
+ * empty bin. Sums are exact 64-bit fixed-point integer sums of the contributions
+ * rounded to 2^-40: the result does not depend on the order of the particles or
+ * the schedule. A contribution of magnitude 2^22 or more sets AZP_EBIT_RANGE
+ * (azp_vfield_error) and is left out. The object holds its accumulators; compute
+ * is stream-ordered and allocates nothing. */
+enum azp_binning_kind { AZP_BINNING_CARTESIAN = 0, AZP_BINNING_CYLINDRICAL = 1 };
+typedef struct azp_vfield azp_vfield;
+AZP_API azp_vfield* azp_vfield_create(int kind, const uint32_t* num_bins, const double* lower, const double* upper,
+                                      int* status);
+AZP_API void azp_vfield_destroy(azp_vfield* vf);
+AZP_API uint32_t azp_vfield_num_bins(const azp_vfield* vf);
+/* group: device index list of n_group members, or NULL for all sys->N particles
+ * (reads sys->pos and sys->vel, mass in vel.w). Outputs are device arrays, each
+ * may be NULL: mass [nbins], momentum [nbins][3], velocity [nbins][3]. */
+AZP_API int azp_vfield_compute(azp_vfield* vf, const azp_system* sys, const uint32_t* group, uint32_t n_group,
+                               double* mass, double* momentum, double* velocity, void* stream);
+/* the accumulated error bits (AZP_EBIT_RANGE); synchronises the stream */
+AZP_API int azp_vfield_error(azp_vfield* vf, uint32_t* err_word, void* stream);
+
 /* Bond forces from a per-particle bond table (replaces
  * gpu_compute_bond_forces<Eval,2>): for particle i its bonds are
  * table[k * N + i] = (partner index, bond type) for k < n_bonds[i].
@@ -351,6 +423,14 @@ typedef struct {
      * reference's HarmonicBarrier in the integrator's forces, src/HarmonicBarrier.h) */
     int32_t barrier_geometry;   /* azp_barrier_geometry (read when barrier_params is set) */
     const double* barrier_params; /* host [ntypes][2] (k, offset); NULL: no barrier */
+    /* wall potential added to the net force inside the fused step (the
+     * reference's wall.LJ93 / wall.Colloid in the integrator's forces), with the
+     * semantics of azp_wall_forces */
+    int32_t wall_kind;          /* azp_wall_kind (read when walls is set) */
+    const azp_walls* walls;     /* host; NULL: no walls */
+    const double* wall_params;  /* host [ntypes][4] records */
+    const double* wall_r_cut;   /* host [ntypes] */
+    const double* wall_r_extrap; /* host [ntypes] */
 } azp_md_config;
 
 AZP_API azp_md* azp_md_create(const azp_md_config* cfg, int* status);

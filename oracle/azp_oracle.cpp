@@ -25,6 +25,9 @@
 //                       with |dx|^2 < (r_cut_ij + r_buff)^2, r_cut_ij > 0,
 //                       minus exclusions; rebuilt when a particle moved more
 //                       than r_buff/2 since the last build.
+//   * wall potentials   src/WallEvaluatorLJ93.h:100-133, src/WallEvaluatorColloid.h:118-183
+//                       (HOOMD's EvaluatorWalls restated from its documentation)
+//   * velocity field    src/VelocityFieldCompute.h:196-344, src/*BinningOperation.h
 //   * harmonic barrier  src/HarmonicBarrier.h:149-180,
 //                       src/PlanarBarrierEvaluator.h:36-56,
 //                       src/SphericalBarrierEvaluator.h:36-61
@@ -947,6 +950,312 @@ int orc_harmonic_barrier(int N, const double* pos, const int32_t* type, const do
         energy[i] = e;
     }
     return 0;
+}
+
+// ---- wall potentials (src/WallEvaluatorLJ93.h:100-133, src/WallEvaluatorColloid.h:
+// 118-183) applied through HOOMD's EvaluatorWalls (not in the tree; restated from
+// its documented behaviour): for every wall, the vector from the nearest point of
+// the wall surface to the particle and whether the particle is on the wall's
+// active side; standard mode (r_extrap = 0): the shifted pair form of the
+// distance d on the active side only; extrapolated mode (r_extrap > 0): that form
+// for d >= r_extrap on the active side, else the linear continuation
+// U(r_extrap) + F(r_extrap) (r_extrap - d_signed) with the constant force
+// F(r_extrap) pushing towards the active side. Full energy per particle; virial
+// F_a x_b. Walls are visited spheres, cylinders, planes.
+//   params[4 * type]: LJ93 {sigma^3, A, -, -}; Colloid {c_1, c_2, a, -}
+//   spheres  [ns][6]: r, origin xyz, inside, open
+//   cylinders[nc][9]: r, origin xyz, unit axis xyz, inside, open
+//   planes   [np][7]: origin xyz, unit normal xyz, open
+enum WallKind { WALL_LJ93 = 0, WALL_COLLOID = 1 };
+
+// energy-shifted evaluator at squared distance rsq; false when not evaluated
+bool wall_eval(int kind, const double* p, double rsq, double rcutsq, double& fdr, double& e)
+{
+    if (kind == WALL_LJ93) {
+        const double lj1 = (2.0 / 15.0) * p[1] * p[0] * p[0] * p[0];
+        const double lj2 = p[1] * p[0];
+        if (!(rsq < rcutsq) || lj1 == 0.0) return false;
+        const double r2inv = 1.0 / rsq;
+        const double r3inv = r2inv * std::sqrt(r2inv);
+        const double r6inv = r3inv * r3inv;
+        fdr = r2inv * r3inv * (9.0 * lj1 * r6inv - 3.0 * lj2);
+        e = r3inv * (lj1 * r6inv - lj2);
+        const double rc2inv = 1.0 / rcutsq;
+        const double rc3inv = rc2inv * std::sqrt(rc2inv);
+        const double rc6inv = rc3inv * rc3inv;
+        e -= rc3inv * (lj1 * rc6inv - lj2);
+        return true;
+    }
+    const double c1 = p[0], c2 = p[1], a = p[2];
+    if (!(rsq < rcutsq) || c1 == 0.0 || !(a > 0.0)) return false;
+    auto potential = [&](double r2, bool force, double& f) {
+        const double r = std::sqrt(r2);
+        const double arinv = a / r;
+        const double rma = 1.0 / (r - a), rpa = 1.0 / (r + a);
+        const double r2ma2 = rma * rpa;
+        const double rma2 = rma * rma, rma6 = rma2 * rma2 * rma2;
+        const double rpa2 = rpa * rpa, rpa6 = rpa2 * rpa2 * rpa2;
+        if (force) {
+            const double arinv8 = 8.0 * arinv;
+            f = 6.0 * c1 * ((arinv8 - 1.0) * rma2 * rma6 + (arinv8 + 1.0) * rpa2 * rpa6);
+            f -= c2 * (4.0 * a * a * arinv * r2ma2 * r2ma2);
+        }
+        const double a7 = 7.0 * a;
+        double en = c1 * ((a7 - r) * rma * rma6 + (a7 + r) * rpa * rpa6);
+        en -= c2 * (2.0 * a * r * r2ma2 + std::log(rpa / rma));
+        return en;
+    };
+    double dummy = 0.0;
+    e = potential(rsq, true, fdr);
+    e -= potential(rcutsq, false, dummy);
+    return true;
+}
+
+// dr = particle - nearest wall point (the reference's dr = -drv), inside flag
+void wall_sphere(const double* w, const double* x, double* dr, bool& inside)
+{
+    const double t[3] = {x[0] - w[1], x[1] - w[2], x[2] - w[3]};
+    const double rxyz = std::sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+    const double R = w[0];
+    const bool win = w[4] != 0.0, open = w[5] != 0.0;
+    if (rxyz > 0.0) {
+        inside = (win ? rxyz < R : rxyz > R) || (rxyz == R && !open);
+        const double s = R / rxyz;
+        for (int d = 0; d < 3; ++d) dr[d] = t[d] - t[d] * s;
+    } else {
+        // at the centre every surface point is nearest: the one along +x
+        inside = win;
+        dr[0] = -R;
+        dr[1] = dr[2] = 0.0;
+    }
+}
+
+void wall_cylinder(const double* w, const double* x, double* dr, bool& inside)
+{
+    const double t[3] = {x[0] - w[1], x[1] - w[2], x[2] - w[3]};
+    const double* ax = w + 4;
+    const double along = t[0] * ax[0] + t[1] * ax[1] + t[2] * ax[2];
+    const double perp[3] = {t[0] - along * ax[0], t[1] - along * ax[1], t[2] - along * ax[2]};
+    const double rxy = std::sqrt(perp[0] * perp[0] + perp[1] * perp[1] + perp[2] * perp[2]);
+    const double R = w[0];
+    const bool win = w[7] != 0.0, open = w[8] != 0.0;
+    if (rxy > 0.0) {
+        inside = (win ? rxy < R : rxy > R) || (rxy == R && !open);
+        const double s = R / rxy;
+        for (int d = 0; d < 3; ++d) dr[d] = perp[d] - perp[d] * s;
+    } else {
+        // on the axis: the surface point along the first direction normal to the axis
+        inside = win;
+        double u[3];
+        if (std::fabs(ax[0]) < 0.9) {
+            u[0] = 0.0; u[1] = ax[2]; u[2] = -ax[1];
+        } else {
+            u[0] = -ax[2]; u[1] = 0.0; u[2] = ax[0];
+        }
+        const double un = std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        for (int d = 0; d < 3; ++d) dr[d] = -R * u[d] / un;
+    }
+}
+
+void wall_plane(const double* w, const double* x, double* dr, bool& inside)
+{
+    const double* n = w + 3;
+    const double d = (x[0] - w[0]) * n[0] + (x[1] - w[1]) * n[1] + (x[2] - w[2]) * n[2];
+    const bool open = w[6] != 0.0;
+    inside = d > 0.0 || (d == 0.0 && !open);
+    for (int k = 0; k < 3; ++k) dr[k] = d * n[k];
+}
+
+// one wall's contribution; nrm = the wall normal used when the particle lies on the surface
+void wall_apply(int kind, const double* p, double rcutsq, double rextrap, const double* dr, bool inside,
+                const double* nrm, double* F, double& U)
+{
+    const double rsq = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+    if (rextrap > 0.0) {
+        const double rextrapsq = rextrap * rextrap;
+        if (inside && rsq >= rextrapsq) {
+            double fdr = 0.0, e = 0.0;
+            if (wall_eval(kind, p, rsq, rcutsq, fdr, e)) {
+                for (int d = 0; d < 3; ++d) F[d] += dr[d] * fdr;
+                U += e;
+            }
+            return;
+        }
+        // unit vector from the wall towards the active side
+        double u[3];
+        const double r = std::sqrt(rsq);
+        if (rsq > 0.0) {
+            const double sgn = inside ? 1.0 : -1.0;
+            for (int d = 0; d < 3; ++d) u[d] = sgn * dr[d] / r;
+        } else {
+            for (int d = 0; d < 3; ++d) u[d] = nrm[d];
+        }
+        const double rp = inside ? rextrap - r : rextrap + r;  // r_extrap - signed distance
+        double fdr = 0.0, e = 0.0;
+        if (wall_eval(kind, p, rextrapsq, rcutsq, fdr, e)) {
+            const double fmag = fdr * rextrap;
+            for (int d = 0; d < 3; ++d) F[d] += u[d] * fmag;
+            U += e + fmag * rp;
+        }
+        return;
+    }
+    if (!inside) return;
+    double fdr = 0.0, e = 0.0;
+    if (wall_eval(kind, p, rsq, rcutsq, fdr, e)) {
+        for (int d = 0; d < 3; ++d) F[d] += dr[d] * fdr;
+        U += e;
+    }
+}
+
+void orc_wall_forces(int N, const double* pos, const int32_t* type, int kind, const double* params,
+                     const double* rcut, const double* rextrap, int ns, const double* spheres, int nc,
+                     const double* cylinders, int np, const double* planes, double* force, double* energy,
+                     double* virial)
+{
+    for (int i = 0; i < N; ++i) {
+        const double x[3] = {pos[4 * i], pos[4 * i + 1], pos[4 * i + 2]};
+        const int t = type[i];
+        const double* p = params + 4 * t;
+        const double rcutsq = rcut[t] * rcut[t];
+        double F[3] = {0.0, 0.0, 0.0}, U = 0.0;
+        double dr[3], nrm[3];
+        bool inside = false;
+        for (int k = 0; k < ns; ++k) {
+            const double* w = spheres + 6 * k;
+            wall_sphere(w, x, dr, inside);
+            // on the surface: towards the centre for an inside wall, outwards otherwise
+            const double t0[3] = {x[0] - w[1], x[1] - w[2], x[2] - w[3]};
+            const double tn = std::sqrt(t0[0] * t0[0] + t0[1] * t0[1] + t0[2] * t0[2]);
+            for (int d = 0; d < 3; ++d) nrm[d] = tn > 0.0 ? (w[4] != 0.0 ? -t0[d] / tn : t0[d] / tn) : 0.0;
+            wall_apply(kind, p, rcutsq, rextrap[t], dr, inside, nrm, F, U);
+        }
+        for (int k = 0; k < nc; ++k) {
+            const double* w = cylinders + 9 * k;
+            wall_cylinder(w, x, dr, inside);
+            const double t0[3] = {x[0] - w[1], x[1] - w[2], x[2] - w[3]};
+            const double along = t0[0] * w[4] + t0[1] * w[5] + t0[2] * w[6];
+            const double pp[3] = {t0[0] - along * w[4], t0[1] - along * w[5], t0[2] - along * w[6]};
+            const double pn = std::sqrt(pp[0] * pp[0] + pp[1] * pp[1] + pp[2] * pp[2]);
+            for (int d = 0; d < 3; ++d) nrm[d] = pn > 0.0 ? (w[7] != 0.0 ? -pp[d] / pn : pp[d] / pn) : 0.0;
+            wall_apply(kind, p, rcutsq, rextrap[t], dr, inside, nrm, F, U);
+        }
+        for (int k = 0; k < np; ++k) {
+            const double* w = planes + 7 * k;
+            wall_plane(w, x, dr, inside);
+            wall_apply(kind, p, rcutsq, rextrap[t], dr, inside, w + 3, F, U);
+        }
+        for (int d = 0; d < 3; ++d) force[3 * i + d] = F[d];
+        energy[i] = U;
+        if (virial) {
+            double* v = virial + 6 * i;
+            v[0] = F[0] * x[0];
+            v[1] = F[0] * x[1];
+            v[2] = F[0] * x[2];
+            v[3] = F[1] * x[1];
+            v[4] = F[1] * x[2];
+            v[5] = F[2] * x[2];
+        }
+    }
+}
+
+// param_type dict constructors (src/WallEvaluatorLJ93.h:31-45, src/WallEvaluatorColloid.h:31-53)
+// LJ93 values {A, sigma} -> {sigma^3, A}; Colloid values {A, a, sigma} -> {c_1, c_2, a}
+int orc_wall_params(int kind, const double* v, double* out)
+{
+    out[0] = out[1] = out[2] = out[3] = 0.0;
+    if (kind == WALL_LJ93) {
+        const double A = v[0], sigma = v[1];
+        out[0] = sigma * sigma * sigma;
+        out[1] = A;
+        return 0;
+    }
+    if (kind == WALL_COLLOID) {
+        const double A = v[0], a = v[1], sigma = v[2];
+        const double sigma_3 = sigma * sigma * sigma;
+        out[0] = A * sigma_3 * sigma_3 / 7560.0;
+        out[1] = A / 6.0;
+        out[2] = a;
+        return 0;
+    }
+    return -1;
+}
+
+// ---- velocity field (src/VelocityFieldCompute.h:196-205 addParticleToBin and
+// :292-344 binParticles, src/BinningOperation.h:71-87 bin1D,
+// src/CartesianBinningOperation.h:27-52, src/CylindricalBinningOperation.h:27-76):
+// each member's position wrapped into the box, binned, its momentum m v (turned
+// into (v_r, v_theta, v_z) for cylindrical bins) and mass summed per bin in
+// member order; velocity = momentum / mass (0 in an empty bin). kind 0
+// Cartesian, 1 cylindrical; num_bins 0 ignores a coordinate. members: index
+// list or NULL for all N. Outputs mass[nb], momentum[3 nb], velocity[3 nb].
+static bool bin1d(double x, double lo, double hi, unsigned n, unsigned& b)
+{
+    const int k = (int)std::floor(((x - lo) / (hi - lo)) * n);
+    if (k >= 0 && k < (int)n) {
+        b = (unsigned)k;
+        return true;
+    }
+    return false;
+}
+
+void orc_velocity_field(int N, const double* pos, const double* vel, const double* L, const int32_t* members,
+                        int n_members, int kind, const uint32_t* num_bins, const double* lo, const double* hi,
+                        double* mass, double* momentum, double* velocity)
+{
+    const Box b = make_box(L);
+    unsigned nb[3];
+    bool use[3];
+    for (int d = 0; d < 3; ++d) {
+        use[d] = num_bins[d] > 0;
+        nb[d] = use[d] ? num_bins[d] : 1u;
+    }
+    const size_t total = (size_t)nb[0] * nb[1] * nb[2];
+    for (size_t k = 0; k < total; ++k) {
+        mass[k] = 0.0;
+        momentum[3 * k] = momentum[3 * k + 1] = momentum[3 * k + 2] = 0.0;
+    }
+    const int n = members ? n_members : N;
+    for (int m = 0; m < n; ++m) {
+        const int i = members ? members[m] : m;
+        double x[3] = {pos[4 * i], pos[4 * i + 1], pos[4 * i + 2]};
+        int img[3] = {0, 0, 0};
+        wrap(b, x, img);
+        const double mi = vel[4 * i + 3];
+        const double p[3] = {vel[4 * i] * mi, vel[4 * i + 1] * mi, vel[4 * i + 2] * mi};
+        unsigned bin[3] = {0, 0, 0};
+        double t[3];
+        if (kind == 0) {
+            bool ok = true;
+            for (int d = 0; d < 3 && ok; ++d)
+                if (use[d]) ok = bin1d(x[d], lo[d], hi[d], nb[d], bin[d]);
+            if (!ok) continue;
+            t[0] = p[0];
+            t[1] = p[1];
+            t[2] = p[2];
+        } else {
+            if (use[2] && !bin1d(x[2], lo[2], hi[2], nb[2], bin[2])) continue;
+            if (use[1]) {
+                double theta = std::atan2(x[1], x[0]);
+                if (theta < 0.0) theta += 2.0 * M_PI;
+                if (!bin1d(theta, lo[1], hi[1], nb[1], bin[1])) continue;
+            }
+            const double r = std::sqrt(x[0] * x[0] + x[1] * x[1]);
+            if (use[0] && !bin1d(r, lo[0], hi[0], nb[0], bin[0])) continue;
+            double c = 1.0, s = 0.0;
+            if (r > 0.0) {
+                c = x[0] / r;
+                s = x[1] / r;
+            }
+            t[0] = c * p[0] + s * p[1];
+            t[1] = -s * p[0] + c * p[1];
+            t[2] = p[2];
+        }
+        const size_t k = (size_t)bin[2] + nb[2] * ((size_t)bin[1] + nb[1] * (size_t)bin[0]);
+        mass[k] += mi;
+        for (int d = 0; d < 3; ++d) momentum[3 * k + d] += t[d];
+    }
+    for (size_t k = 0; k < total; ++k)
+        for (int d = 0; d < 3; ++d) velocity[3 * k + d] = mass[k] > 0.0 ? momentum[3 * k + d] / mass[k] : 0.0;
 }
 
 // ---- maximum squared displacement since the last list build

@@ -103,6 +103,11 @@ def lib():
     L.orc_brownian.argtypes = [c_int, _dp, _ip, _ip, _dp, _up, vp, _dp, c_int, c_double, c_int, _dp, _dp, c_double, c_double, c_u64, c_u32, c_int, c_double]
     L.orc_max_disp2.argtypes = [c_int, _dp, _dp, _dp]
     L.orc_max_disp2.restype = c_double
+    L.orc_wall_forces.argtypes = [c_int, _dp, _ip, c_int, _dp, _dp, _dp, c_int, _dp, c_int, _dp, c_int, _dp, _dp, _dp,
+                                  vp]
+    L.orc_wall_params.argtypes = [c_int, _dp, _dp]
+    L.orc_wall_params.restype = c_int
+    L.orc_velocity_field.argtypes = [c_int, _dp, _dp, _dp, vp, c_int, c_int, _up, _dp, _dp, _dp, _dp, _dp]
     L.orc_barrier_valid.argtypes = [c_int, c_double, _dp]
     L.orc_harmonic_barrier.argtypes = [c_int, _dp, _ip, _dp, c_int, c_double, _dp, _dp, _dp]
     _lib = L
@@ -260,6 +265,75 @@ def dpd_forces(pos4, vel4, types, tags, ntypes, L, start, idx, params, rcutsq, k
     return F, U, W
 
 
+WALL_KINDS = {"LJ93": 0, "Colloid": 1}
+WALL_KEYS = {"LJ93": ("A", "sigma"), "Colloid": ("A", "a", "sigma")}
+
+
+def wall_params(name, d):
+    """param_type record (4 doubles) of a wall potential from its dict."""
+    out = np.zeros(4)
+    vals = np.array([d[k] for k in WALL_KEYS[name]], dtype=np.float64)
+    assert lib().orc_wall_params(WALL_KINDS[name], vals, out) == 0
+    return out
+
+
+def wall_forces(pos4, types, name, params, rcut, rextrap, spheres=(), cylinders=(), planes=()):
+    """Wall force [N,3], energy [N], virial [N,6] (HOOMD EvaluatorWalls semantics).
+    params [ntypes, 4] records; rcut, rextrap [ntypes]; spheres rows (r, ox, oy, oz,
+    inside, open); cylinders (r, ox, oy, oz, ax, ay, az, inside, open) with a unit
+    axis; planes (ox, oy, oz, nx, ny, nz, open) with a unit normal."""
+    N = pos4.shape[0]
+    F = np.zeros((N, 3))
+    U = np.zeros(N)
+    W = np.zeros((N, 6))
+    sp = np.ascontiguousarray(np.asarray(spheres, dtype=np.float64).reshape(-1, 6))
+    cy = np.ascontiguousarray(np.asarray(cylinders, dtype=np.float64).reshape(-1, 9))
+    pl = np.ascontiguousarray(np.asarray(planes, dtype=np.float64).reshape(-1, 7))
+    lib().orc_wall_forces(
+        N,
+        np.ascontiguousarray(pos4, dtype=np.float64),
+        np.ascontiguousarray(types, dtype=np.int32),
+        WALL_KINDS[name],
+        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        np.ascontiguousarray(rcut, dtype=np.float64).reshape(-1),
+        np.ascontiguousarray(rextrap, dtype=np.float64).reshape(-1),
+        len(sp), sp.reshape(-1) if len(sp) else np.zeros(1),
+        len(cy), cy.reshape(-1) if len(cy) else np.zeros(1),
+        len(pl), pl.reshape(-1) if len(pl) else np.zeros(1),
+        F, U, _ptr(W),
+    )
+    return F, U, W
+
+
+def velocity_field(pos4, vel4, L, kind, num_bins, lower, upper, members=None):
+    """Per-bin mass, momentum and mass-averaged velocity (src/VelocityFieldCompute.h);
+    kind "cartesian" or "cylindrical"; members an index list or None for all.
+    Returns arrays shaped [total bins], [total bins, 3], [total bins, 3] in the
+    reference's ravel order (z fastest)."""
+    nb = [max(int(n), 1) for n in num_bins]
+    total = nb[0] * nb[1] * nb[2]
+    mass = np.zeros(total)
+    mom = np.zeros((total, 3))
+    vel = np.zeros((total, 3))
+    mem = None if members is None else np.ascontiguousarray(members, dtype=np.int32)
+    lib().orc_velocity_field(
+        pos4.shape[0],
+        np.ascontiguousarray(pos4, dtype=np.float64),
+        np.ascontiguousarray(vel4, dtype=np.float64),
+        np.ascontiguousarray(L, dtype=np.float64),
+        None if mem is None else mem.ctypes.data,
+        0 if mem is None else len(mem),
+        {"cartesian": 0, "cylindrical": 1}[kind],
+        np.ascontiguousarray(num_bins, dtype=np.uint32),
+        np.ascontiguousarray(lower, dtype=np.float64),
+        np.ascontiguousarray(upper, dtype=np.float64),
+        mass,
+        mom,
+        vel,
+    )
+    return mass, mom, vel
+
+
 BARRIER_GEOMETRIES = {"planar": 0, "spherical": 1}
 
 
@@ -385,7 +459,7 @@ class OracleMD:
 
     def __init__(self, system, pair=None, bond=None, method="langevin", gamma=(1.0,), flow_kind=0,
                  flow_p=(0.0, 0.0, 0.0), kT=1.0, dt=0.005, seed=0, r_buff=0.4, noiseless=False, exclude_bonds=True,
-                 max_disp=0.0, force_cap=0.0, barrier=None):
+                 max_disp=0.0, force_cap=0.0, barrier=None, walls=None):
         self.s = {k: (np.ascontiguousarray(v).copy() if isinstance(v, np.ndarray) else v) for k, v in system.items()}
         s = self.s
         self.N = s["pos4"].shape[0]
@@ -402,6 +476,8 @@ class OracleMD:
         self.force_cap = force_cap
         # dict(geometry, location: float or callable(timestep), params [ntypes, 2])
         self.barrier = barrier
+        # dict(name, params [ntypes, 4], rcut [ntypes], rextrap [ntypes], spheres, cylinders, planes)
+        self.walls = walls
         self.timestep = int(s.get("timestep", 0))
         self.ntypes = int(s.get("ntypes", int(s["types"].max()) + 1))
         self.exclusions = s["bonds"] if (exclude_bonds and s.get("bonds") is not None and len(s["bonds"])) else None
@@ -443,6 +519,13 @@ class OracleMD:
                                   self.pair["params"], rc * rc, ronsq, self.pair.get("mode", "none"), self.force_cap)
         if self.bond is not None and self.table is not None:
             bond_forces_pp(s["pos4"], s["L"], self.table, self.bond["name"], self.bond["params"], F, U, W)
+        if self.walls is not None:
+            w = self.walls
+            Fw, Uw, Ww = wall_forces(s["pos4"], s["types"], w["name"], w["params"], w["rcut"], w["rextrap"],
+                                     w.get("spheres", ()), w.get("cylinders", ()), w.get("planes", ()))
+            F = F + Fw
+            U = U + Uw
+            W = W + Ww
         if self.barrier is not None:
             loc = self.barrier["location"]
             t = self.timestep if timestep is None else timestep

@@ -1,7 +1,7 @@
 """Extract the known-answer cases of the reference's own tests into kats.json.
 
-Reads ``src/pytest/test_pair.py`` and ``src/pytest/test_bond.py`` of the
-azplugins tree AS TEXT (``ast``; the files import hoomd, which is not needed):
+Reads ``src/pytest/test_pair.py``, ``src/pytest/test_bond.py`` and
+``src/pytest/test_wall.py`` of the azplugins tree AS TEXT (``ast``; the files import hoomd, which is not needed):
 every ``PotentialTestCase(...)`` call becomes one record with its line number.
 
 Usage: python tests/golden/make_kats.py [/path/to/azplugins]
@@ -43,13 +43,16 @@ def main():
     pair = cases(os.path.join(root, "src", "pytest", "test_pair.py"),
                  ["params", "r_cut", "shift", "distance", "energy", "force"])
     bond = cases(os.path.join(root, "src", "pytest", "test_bond.py"), ["params", "distance", "energy", "force"])
+    wall = cases(os.path.join(root, "src", "pytest", "test_wall.py"), ["params", "position", "energy", "force"])
     for r in pair:
         r["source"] = f"src/pytest/test_pair.py:{r['line']}"
     for r in bond:
         r["source"] = f"src/pytest/test_bond.py:{r['line']}"
+    for r in wall:
+        r["source"] = f"src/pytest/test_wall.py:{r['line']}"
     with open(os.path.join(HERE, "kats.json"), "w") as f:
-        json.dump({"pair": pair, "bond": bond}, f, indent=1)
-    print(f"{len(pair)} pair and {len(bond)} bond cases")
+        json.dump({"pair": pair, "bond": bond, "wall": wall}, f, indent=1)
+    print(f"{len(pair)} pair, {len(bond)} bond and {len(wall)} wall cases")
 
 
 if __name__ == "__main__":

@@ -1,0 +1,213 @@
+"""Wall potentials on the GPU.
+
+* The reference's known answers (src/pytest/test_wall.py:22-111): one particle at
+  (0, 0, z) in a box of 20 above the plane z = 0, the potential in the
+  integrator's forces, energies and forces read after run(0) (4 decimals as
+  there), in both precisions.
+* The drop-in driver azp_wall_forces against the oracle with every geometry at
+  once (inside and outside spheres, tilted cylinders, planes; standard and
+  extrapolated types): FP64 1e-12 (LJ93) / 1e-11 (Colloid) norm-wise with
+  energies and virials, FP32 output within 1e-6.
+* The resident engine with the walls in the integrator's forces (fused into the
+  step kernel) against the oracle's MD loop: a Lennard-Jones fluid in a slit
+  between two LJ93 planes (Langevin) and in a Colloid-walled cylindrical pore
+  (Brownian), FP64 (positions 1e-9) and FP32 forces (1e-3 / 1e-5), plus the
+  engine's forces, energy and virial at the final state.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import azplugins_gb300 as az
+from helpers import force_error, load_golden, oracle_system, rel
+
+pytestmark = pytest.mark.gpu
+KATS = load_golden("kats.json")["wall"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("case", KATS, ids=lambda c: f"{c['potential']}@{c['line']}")
+def test_reference_kats(case, precision):
+    s = az.Snapshot(1)
+    s.particles.position = np.array([case["position"]], dtype=np.float64)
+    s.configuration.box = [20.0, 20.0, 20.0, 0.0, 0.0, 0.0]
+    sim = az.Simulation(seed=1, precision=precision)
+    sim.create_state_from_snapshot(s)
+    wall = az.wall.Plane(origin=(0, 0, 0), normal=(0, 0, 1))
+    pot = getattr(az.wall, case["potential"])(walls=[wall])
+    pot.params["A"] = case["params"]
+    m = az.methods.LangevinFlow("all", kT=0.0, flow_field=az.flow.ConstantFlow((0.0, 0.0, 0.0)), default_gamma=0.0)
+    sim.operations.integrator = az.md.Integrator(dt=0.001, methods=[m], forces=[pot])
+    sim.run(0)
+    for k, v in case["params"].items():
+        assert pot.params["A"][k] == v
+    np.testing.assert_array_almost_equal(pot.energies, [case["energy"]], decimal=4)
+    np.testing.assert_array_almost_equal(pot.forces, [[0.0, 0.0, case["force"]]], decimal=4)
+    # the engine's net force at the state carries the wall force too
+    sim.run(1)
+    f, w = sim._engine.forces()
+    np.testing.assert_array_almost_equal(f[:, 3], [case["energy"]], decimal=4)
+    np.testing.assert_array_almost_equal(f[:, :3], [[0.0, 0.0, case["force"]]], decimal=4)
+
+
+def _walls_zoo():
+    return [
+        az.wall.Sphere(radius=9.0, origin=(0.3, -0.2, 0.1), inside=True),
+        az.wall.Sphere(radius=2.5, origin=(-3.0, 2.0, 1.0), inside=False),
+        az.wall.Cylinder(radius=7.5, axis=(0.2, 0.1, 1.0), origin=(0.5, 0.0, 0.0), inside=True),
+        az.wall.Cylinder(radius=1.5, axis=(1.0, -1.0, 0.3), origin=(2.0, -2.0, -1.0), inside=False),
+        az.wall.Plane(origin=(0.0, -8.0, 0.0), normal=(0.0, 1.0, 0.0)),
+        az.wall.Plane(origin=(0.0, 8.0, 0.0), normal=(0.1, -1.0, 0.05)),
+        az.wall.Plane(origin=(0.0, 0.0, -7.0), normal=(0.0, 0.0, 1.0), open=False),
+    ]
+
+
+@pytest.mark.parametrize("name", ["LJ93", "Colloid"])
+def test_driver_matches_oracle(orc, name):
+    import torch
+
+    from azplugins_gb300 import _lib
+
+    Lib = _lib.load()
+    rng = np.random.Generator(np.random.PCG64(81))
+    N = 30011
+    L = np.array([20.0, 20.0, 20.0])
+    pos = rng.uniform(-0.5, 0.5, size=(N, 3)) * L
+    types = rng.integers(0, 3, size=N).astype(np.int32)
+    pot = getattr(az.wall, name)(walls=_walls_zoo())
+    if name == "LJ93":
+        pot.params["A"] = dict(A=1.0, sigma=1.0, r_cut=3.0)
+        pot.params["B"] = dict(A=0.5, sigma=1.2, r_cut=2.5, r_extrap=0.8)
+        pot.params["C"] = dict(A=2.0, sigma=0.8, r_cut=1.5, r_extrap=0.4)
+    else:
+        pot.params["A"] = dict(A=1.0, a=0.5, sigma=1.0, r_cut=3.0, r_extrap=0.9)
+        pot.params["B"] = dict(A=4.0, a=1.0, sigma=1.0, r_cut=3.5, r_extrap=1.4)
+        pot.params["C"] = dict(A=0.3, a=0.3, sigma=0.9, r_cut=2.0, r_extrap=0.5)
+    rec, rc, rx = pot._tables(["A", "B", "C"])
+    sp, cy, pl = pot._oracle_walls()
+    # the standard form diverges at the surface: redraw the few particles whose
+    # wall force would leave the FP32 range
+    for _ in range(10):
+        F, U, W = orc.wall_forces(np.concatenate([pos, types[:, None]], axis=1), types, name, rec, rc, rx, sp, cy,
+                                  pl)
+        bad = ~(np.abs(F).max(axis=1) < 1e8) | ~(np.abs(U) < 1e8)
+        if not bad.any():
+            break
+        pos[bad] = rng.uniform(-0.5, 0.5, size=(bad.sum(), 3)) * L
+    assert not bad.any() and (np.abs(U) > 0).sum() > 1000
+    dpos = torch.zeros((N, 4), dtype=torch.float64, device="cuda")
+    dpos[:, :3] = torch.from_numpy(pos).cuda()
+    dpos.view(torch.int64)[:, 3] = torch.from_numpy(types.astype(np.int64)).cuda()
+    s = _lib.System()
+    s.N, s.ntypes, s.pos = N, 3, dpos.data_ptr()
+    for d in range(3):
+        s.box.L[d] = L[d]
+    dev = [torch.from_numpy(np.ascontiguousarray(a).reshape(-1).copy()).cuda() for a in (rec, rc, rx)]
+    walls, keep = pot._walls_struct()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    # FP64: the Colloid form subtracts two large terms near the surface, so FMA
+    # contraction differences show at 1e-12; LJ93 stays within 1e-12
+    tol64 = 1e-12 if name == "LJ93" else 1e-11
+    for prec, dt, tol in ((_lib.FP64, torch.float64, tol64), (_lib.FP32, torch.float32, 1e-6)):
+        force = torch.full((N, 4), float("nan"), dtype=dt, device="cuda")
+        vir = torch.full((6, N), float("nan"), dtype=dt, device="cuda")
+        out = _lib.Forces()
+        out.force, out.virial, out.virial_pitch, out.precision = force.data_ptr(), vir.data_ptr(), N, prec
+        _lib.check(Lib.azp_wall_forces(ctypes.byref(s), pot.kind, ctypes.byref(walls), dev[0].data_ptr(),
+                                       dev[1].data_ptr(), dev[2].data_ptr(), ctypes.byref(out), stream),
+                   "azp_wall_forces")
+        torch.cuda.synchronize()
+        f = force.double().cpu().numpy()
+        w = vir.double().cpu().numpy().T
+        assert force_error(f, F) < tol
+        assert np.abs(f[:, 3] - U).max() <= tol * max(np.abs(U).max(), 1.0)
+        assert np.abs(w - W).max() <= tol * max(np.abs(W).max(), 1.0)
+    del keep
+
+
+def _slit_fluid(seed, n_xz=8, n_y=10, spacing=1.2):
+    """Jittered lattice filling |y| <= 5.4 of a 9.6 x 16 x 9.6 box (walls at y = +-7)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    gx = (np.arange(n_xz) + 0.5) * spacing - 0.5 * n_xz * spacing
+    gy = (np.arange(n_y) + 0.5) * spacing - 0.5 * n_y * spacing
+    X, Y, Z = np.meshgrid(gx, gy, gx, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1) + rng.uniform(-0.08, 0.08, size=(X.size, 3))
+    N = len(pts)
+    s = az.Snapshot(N)
+    s.particles.types = ["A", "B"]
+    s.particles.position = pts
+    s.particles.typeid = rng.integers(0, 2, size=N).astype(np.int32)
+    s.particles.velocity = rng.normal(size=(N, 3))
+    s.particles.velocity -= s.particles.velocity.mean(axis=0)
+    s.particles.mass = rng.uniform(0.8, 1.2, size=N)
+    s.particles.acceleration = np.zeros((N, 3))
+    s.configuration.box = [n_xz * spacing, 16.0, n_xz * spacing, 0.0, 0.0, 0.0]
+    return s
+
+
+def _run(orc, snap, precision, method, pot, steps, dt, seed):
+    sim = az.Simulation(seed=seed, precision=precision)
+    sim.create_state_from_snapshot(snap)
+    lj = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), default_r_cut=2.5)
+    lj.params[[("A", "A"), ("A", "B"), ("B", "B")]] = dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.5)
+    mcls = az.methods.LangevinFlow if method == "langevin" else az.methods.BrownianFlow
+    m = mcls("all", kT=1.0, flow_field=az.flow.ConstantFlow((0.0, 0.0, 0.0)), default_gamma=1.0)
+    sim.operations.integrator = az.md.Integrator(dt=dt, methods=[m], forces=[lj, pot])
+    sim.run(steps // 2)
+    sim.run(steps - steps // 2)
+    rec = orc.pair_params("PerturbedLennardJones", dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.5))
+    wrec, wrc, wrx = pot._tables(["A", "B"])
+    sp, cy, pl = pot._oracle_walls()
+    md = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
+                      pair=dict(name="PerturbedLennardJones", params=np.tile(rec, (2, 2, 1)),
+                                rcut=np.full((2, 2), 2.5), mode="none"),
+                      method=method, gamma=[1.0, 1.0], kT=1.0, dt=dt, seed=seed,
+                      walls=dict(name=pot._name, params=wrec, rcut=wrc, rextrap=wrx, spheres=sp, cylinders=cy,
+                                 planes=pl))
+    md.run(steps)
+    return sim, md
+
+
+def _unwrapped_err(sim, md, L):
+    out = sim.state.get_snapshot().particles
+    return float(np.abs((out.position + out.image * L) - (md.s["pos4"][:, :3] + md.s["image"] * L)).max())
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32", 1e-3)])
+def test_engine_langevin_slit(orc, precision, tol):
+    snap = _slit_fluid(91)
+    L = np.array(snap.configuration.box[:3])
+    pot = az.wall.LJ93(walls=[az.wall.Plane(origin=(0, -7.0, 0), normal=(0, 1, 0)),
+                              az.wall.Plane(origin=(0, 7.0, 0), normal=(0, -1, 0))])
+    pot.params["A"] = dict(A=2.0, sigma=1.0, r_cut=3.0)
+    pot.params["B"] = dict(A=1.0, sigma=1.2, r_cut=3.0, r_extrap=0.6)
+    sim, md = _run(orc, snap, precision, "langevin", pot, 60, 0.004, seed=91)
+    F_md, U_md, W_md = md.forces()
+    Fw, Uw, _ = orc.wall_forces(md.s["pos4"], md.s["types"], "LJ93", *pot._tables(["A", "B"]),
+                                planes=pot._oracle_walls()[2])
+    assert (Uw != 0).sum() > 50  # the walls act on the layers next to them
+    assert _unwrapped_err(sim, md, L) < tol
+    f, w = sim._engine.forces()
+    ftol = 1e-12 if precision == "fp64" else 1e-5
+    assert force_error(f, F_md) < ftol
+    th = sim.thermo()
+    assert rel(th["potential_energy"], U_md.sum()) < ftol
+    for c in range(6):
+        assert abs(th["virial"][c] - W_md[:, c].sum()) <= ftol * max(np.abs(W_md[:, c]).sum(), 1.0)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32", 1e-5)])
+def test_engine_brownian_cylindrical_pore(orc, precision, tol):
+    snap = _slit_fluid(92)
+    L = np.array(snap.configuration.box[:3])
+    # a pore of radius 4.2 along y through the slab, and a colloid-walled outer region
+    pot = az.wall.Colloid(walls=[az.wall.Cylinder(radius=4.2, axis=(0, 1, 0), inside=True)])
+    pot.params["A"] = dict(A=3.0, a=0.4, sigma=1.0, r_cut=2.5, r_extrap=0.7)
+    pot.params["B"] = dict(A=5.0, a=0.5, sigma=1.0, r_cut=3.0, r_extrap=0.9)
+    sim, md = _run(orc, snap, precision, "brownian", pot, 40, 2e-4, seed=92)
+    F_md, U_md, _ = md.forces()
+    assert _unwrapped_err(sim, md, L) < tol
+    f, _ = sim._engine.forces()
+    assert force_error(f, F_md) < (1e-12 if precision == "fp64" else 1e-5)
