@@ -231,7 +231,11 @@ def bond_forces(state, bond, precision="fp64"):
     if b.N:
         n, table, h = bond_table(N, b.group, b.typeid)
         pos = device_positions(snap)
-        sysd = make_system(snap, pos)
+        extra = {}
+        if bond.kind == _lib.BOND_KINDS["ImageHarmonic"]:
+            img = torch.from_numpy(np.ascontiguousarray(snap.particles.image, dtype=np.int32).reshape(-1)).cuda()
+            extra["image"] = img.data_ptr()
+        sysd = make_system(snap, pos, **extra)
         n_d = torch.from_numpy(n.view(np.int32)).cuda()
         t_d = torch.from_numpy(table.reshape(-1).view(np.int32)).cuda()
         params_d = torch.from_numpy(bond._table(b.types).reshape(-1)).cuda()

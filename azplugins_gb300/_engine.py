@@ -34,6 +34,9 @@ def split_forces(integ):
     if any(len(x) > 1 for x in found):
         raise NotImplementedError("the engine advances at most one pair, one bond, one barrier and one wall potential")
     pairs = found[0]
+    if found[1] and found[1][0]._name == "ImageHarmonic":
+        raise NotImplementedError("ImageHarmonic runs through the drop-in driver (azp_bond_forces); "
+                                  "the resident engine does not take it")
     if pairs and pairs[0]._name == "DPDGeneralWeight":
         raise NotImplementedError("DPDGeneralWeight runs through the drop-in driver (azp_dpd_forces); "
                                   "the resident engine does not take it")

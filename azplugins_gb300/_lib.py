@@ -32,7 +32,7 @@ STATUS = {
 
 # header enums
 PAIR_KINDS = {"PerturbedLennardJones": 0, "ExpandedYukawa": 1, "Hertz": 2, "Colloid": 3, "DPDGeneralWeight": 4}
-BOND_KINDS = {"Quartic": 0, "DoubleWell": 1}
+BOND_KINDS = {"Quartic": 0, "DoubleWell": 1, "ImageHarmonic": 2}
 MODES = {"none": 0, "shift": 1, "xplor": 2}
 FP64, FP32 = 0, 1
 FLOW_CONSTANT, FLOW_PARABOLIC = 0, 1

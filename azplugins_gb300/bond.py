@@ -2,8 +2,8 @@
 
 ``params["A-A"]`` keys follow the reference schemas (``src/bond.py:45-49`` for
 DoubleWell, ``:141-156`` for Quartic, whose ``delta`` defaults to 0 as in the
-reference); records are built by the native ports of the reference dict
-constructors.
+reference, ``:160-192`` for ImageHarmonic's ``k``, ``r0``); records are built by
+the native ports of the reference dict constructors.
 """
 
 from __future__ import annotations
@@ -90,3 +90,14 @@ class Quartic(Bond):
 
 
 __all__ = ["Bond", "DoubleWell", "Quartic"]
+
+
+class ImageHarmonic(Bond):
+    """Harmonic bond U = k/2 (r - r0)^2 on the image-unwrapped distance
+    (``src/ImagePotentialBond.h``, ``src/bond.py:160-192``): the bond vector is
+    (x_j + img_j L) - (x_i + img_i L), so a bond may span more than half the box.
+    Evaluated by the drop-in driver (``azp_bond_forces``, reading the images);
+    the resident engine (``Simulation.run``) does not take it."""
+
+    _name = "ImageHarmonic"
+    _keys = ("k", "r0")

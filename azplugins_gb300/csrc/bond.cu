@@ -5,8 +5,10 @@
 // One thread per particle walks its own bonds (each bond appears on both of its
 // particles): dx = x_i - x_j (minimum image), F_i += dx f/r, U_i += U/2,
 // W_i += dx (x) dx f/(2r) -- the convention of src/ImagePotentialBondGPU.cuh:
-// 180-244 with the minimum image instead of the image shift. A refusing evaluator
-// sets AZP_EBIT_BOND in the error word (the reference sets *d_flags = 1).
+// 180-244 with the minimum image instead of the image shift. With an image array
+// (the ImageHarmonic bond, src/ImagePotentialBond.h:136-140) the displacement is
+// the unwrapped one instead: dx = (x_i - x_j) + (img_i - img_j) L. A refusing
+// evaluator sets AZP_EBIT_BOND in the error word (the reference sets *d_flags = 1).
 #include "bond.cuh"
 #include "evaluators.cuh"
 
@@ -33,9 +35,16 @@ __global__ void __launch_bounds__(BOND_BLOCK) k_bond(BondArgs a)
         for (uint32_t k = 0; k < nb; ++k) {
             const uint2 e = a.table[(size_t)k * a.N + i];
             const double4_32a pj = a.pos[e.x];
-            const double dx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
-            const double dy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
-            const double dz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
+            double dx, dy, dz;
+            if (a.image) {
+                dx = (pi.x - pj.x) + (double)(a.image[3 * i] - a.image[3 * e.x]) * a.L[0];
+                dy = (pi.y - pj.y) + (double)(a.image[3 * i + 1] - a.image[3 * e.x + 1]) * a.L[1];
+                dz = (pi.z - pj.z) + (double)(a.image[3 * i + 2] - a.image[3 * e.x + 2]) * a.L[2];
+            } else {
+                dx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
+                dy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
+                dz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
+            }
             const double rsq = rsq_exact(dx, dy, dz);
             double fdr, en;
             if (!Eval::eval(s_p + e.y * AZP_BOND_PARAM_DOUBLES, rsq, fdr, en)) {
@@ -58,11 +67,16 @@ __global__ void __launch_bounds__(BOND_BLOCK) k_bond(BondArgs a)
         // FP32 evaluation; displacement from the fixed-point shadow when the
         // caller has one, else from the FP64 minimum image
         const uint4 fi = a.fixed ? a.fixed[i] : make_uint4(0, 0, 0, 0);
-        const double4_32a pi = a.fixed ? make_double4_32a(0, 0, 0, 0) : a.pos[i];
+        const double4_32a pi = (a.fixed && !a.image) ? make_double4_32a(0, 0, 0, 0) : a.pos[i];
         for (uint32_t k = 0; k < nb; ++k) {
             const uint2 e = a.table[(size_t)k * a.N + i];
             float dx, dy, dz;
-            if (a.fixed) {
+            if (a.image) {
+                const double4_32a pj = a.pos[e.x];
+                dx = (float)((pi.x - pj.x) + (double)(a.image[3 * i] - a.image[3 * e.x]) * a.L[0]);
+                dy = (float)((pi.y - pj.y) + (double)(a.image[3 * i + 1] - a.image[3 * e.x + 1]) * a.L[1]);
+                dz = (float)((pi.z - pj.z) + (double)(a.image[3 * i + 2] - a.image[3 * e.x + 2]) * a.L[2]);
+            } else if (a.fixed) {
                 const uint4 fj = a.fixed[e.x];
                 dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
                 dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
@@ -139,6 +153,7 @@ int launch_bond(int kind, int precision, const BondArgs& a, cudaStream_t s)
     switch (kind) {
     case AZP_BOND_QUARTIC: return launch_b<QuarticBond>(precision, a, s);
     case AZP_BOND_DOUBLE_WELL: return launch_b<DoubleWellBond>(precision, a, s);
+    case AZP_BOND_IMAGE_HARMONIC: return a.image ? launch_b<HarmonicBond>(precision, a, s) : AZP_ERR_INVALID;
     default: return AZP_ERR_INVALID;
     }
 }

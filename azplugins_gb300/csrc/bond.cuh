@@ -19,6 +19,7 @@ struct BondArgs {
     void* virial;            // accumulated: [6][pitch] or null
     uint32_t pitch;
     uint32_t* err;           // AZP_EBIT_BOND on refusal, may be null
+    const int* image;        // [N][3]: image-unwrapped displacements, else null (minimum image)
 };
 
 int launch_bond(int kind, int precision, const BondArgs& a, cudaStream_t s);

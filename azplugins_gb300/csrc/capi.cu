@@ -50,6 +50,7 @@ int n_bond_values(int kind)
     switch (kind) {
     case AZP_BOND_QUARTIC: return 8;
     case AZP_BOND_DOUBLE_WELL: return 4;
+    case AZP_BOND_IMAGE_HARMONIC: return 2;
     default: return -1;
     }
 }
@@ -159,6 +160,11 @@ int azp_bond_params_from_values(int kind, const double* v, double* rec)
         rec[2] = v[2];          // U_1
         rec[3] = v[3];          // U_tilt
         return AZP_OK;
+    case AZP_BOND_IMAGE_HARMONIC:
+        // HOOMD's harmonic bond parameters {k, r0} (src/bond.py:160-192)
+        rec[0] = v[0];
+        rec[1] = v[1];
+        return AZP_OK;
     default: return AZP_ERR_INVALID;
     }
 }
@@ -178,6 +184,10 @@ int azp_bond_params_to_values(int kind, const double* rec, double* v)
         v[1] = rec[0];
         v[2] = rec[2];
         v[3] = rec[3];
+        return AZP_OK;
+    case AZP_BOND_IMAGE_HARMONIC:
+        v[0] = rec[0];
+        v[1] = rec[1];
         return AZP_OK;
     default: return AZP_ERR_INVALID;
     }
@@ -233,6 +243,9 @@ int azp_bond_forces(const azp_system* sys, const uint32_t* n_bonds, const uint32
     a.virial = out->virial;
     a.pitch = out->virial_pitch ? out->virial_pitch : sys->N;
     a.err = err;
+    // the ImageHarmonic bond measures the image-unwrapped distance (src/ImagePotentialBond.h:136-140)
+    a.image = kind == AZP_BOND_IMAGE_HARMONIC ? sys->image : nullptr;
+    if (kind == AZP_BOND_IMAGE_HARMONIC && !sys->image) return AZP_ERR_INVALID;
     return azp::launch_bond(kind, out->precision, a, azp::as_stream(stream));
 }
 

@@ -348,4 +348,18 @@ struct DoubleWellBond {
     AZP_D static bool eval_f(const float* q, float rsq, float& fdr, float& e) { return eval(q, rsq, fdr, e); }
 };
 
+// Harmonic bond U = k/2 (r - r_0)^2 (HOOMD's EvaluatorBondHarmonic, which
+// src/ImagePotentialBond.h:144-152 applies to the image-unwrapped distance):
+// p = {k, r_0}. At r = 0 the force is set to 0 (its direction is undefined).
+struct HarmonicBond {
+    template<typename R> AZP_HD static bool eval(const R* p, R rsq, R& fdr, R& e)
+    {
+        const R k = p[0], r0 = p[1];
+        const R r = sqrt(rsq);
+        fdr = r > R(0) ? k * (r0 / r - R(1)) : R(0);
+        e = R(0.5) * k * (r0 - r) * (r0 - r);
+        return true;
+    }
+};
+
 }  // namespace azp

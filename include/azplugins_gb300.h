@@ -82,7 +82,10 @@ enum azp_pair_kind {
 enum azp_bond_kind {
     AZP_BOND_QUARTIC = 0,          /* BondEvaluatorQuartic */
     AZP_BOND_DOUBLE_WELL = 1,      /* BondEvaluatorDoubleWell */
-    AZP_BOND_NUM_KINDS = 2
+    AZP_BOND_NUM_KINDS = 2,        /* kinds of the engine */
+    AZP_BOND_IMAGE_HARMONIC = 2    /* ImagePotentialBondHarmonic (src/ImagePotentialBond.h): harmonic
+                                      U = k/2 (r - r0)^2 on the image-unwrapped distance; azp_bond_forces
+                                      only, reads sys->image */
 };
 /* HOOMD pair.Pair modes accepted by azplugins (src/pair.py:415) */
 enum azp_shift_mode { AZP_MODE_NONE = 0, AZP_MODE_SHIFT = 1, AZP_MODE_XPLOR = 2 };
@@ -123,6 +126,7 @@ typedef struct { double r_1, r_diff, U_1, U_tilt, pad_[4]; } azp_params_double_w
  *   DPDGeneralWeight:      A, gamma, s
  *   Quartic:               k, r_0, b_1, b_2, U_0, sigma, epsilon, delta
  *   DoubleWell:            r_0, r_1, U_1, U_tilt
+ *   ImageHarmonic:         k, r0
  * Replaces e.g. PairParametersPerturbedLennardJones(pybind11::dict) and asDict()
  * (src/PairEvaluatorPerturbedLennardJones.h:33-54). */
 AZP_API int azp_pair_params_from_values(int kind, const double* values, double* record);
@@ -339,6 +343,9 @@ AZP_API int azp_vfield_error(azp_vfield* vf, uint32_t* err_word, void* stream);
  * table[k * N + i] = (partner index, bond type) for k < n_bonds[i].
  * params: device table [nbondtypes] of 8-double records. ACCUMULATES into out.
  * FP32 precision evaluates in FP32 on the FP64 minimum-image displacement.
+ * AZP_BOND_IMAGE_HARMONIC (src/ImagePotentialBond.h:57-204) measures the
+ * image-unwrapped displacement (x_i - x_j) + (img_i - img_j) L instead and needs
+ * sys->image.
  * err: device uint32 error word (AZP_EBIT_BOND set when an evaluator refuses). */
 AZP_API int azp_bond_forces(const azp_system* sys, const uint32_t* n_bonds, const uint32_t* table,
                     uint32_t table_height, int kind, const double* params, uint32_t nbondtypes,

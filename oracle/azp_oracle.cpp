@@ -48,7 +48,7 @@ namespace
 {
 // ---------------------------------------------------------------- evaluators
 enum PairKind { PAIR_PLJ = 0, PAIR_EYUK = 1, PAIR_HERTZ = 2, PAIR_COLLOID = 3, PAIR_DPD = 4 };
-enum BondKind { BOND_QUARTIC = 0, BOND_DOUBLEWELL = 1 };
+enum BondKind { BOND_QUARTIC = 0, BOND_DOUBLEWELL = 1, BOND_IMAGE_HARMONIC = 2 };
 enum ShiftMode { MODE_NONE = 0, MODE_SHIFT = 1, MODE_XPLOR = 2 };
 
 // Perturbed LJ: p = {sigma^6, 4 eps, lambda, 2^(1/3) sigma^2}
@@ -279,11 +279,23 @@ bool eval_doublewell(const double* p, double rsq, double& fdr, double& e)
     return true;
 }
 
+// harmonic bond (HOOMD's EvaluatorBondHarmonic, applied by src/ImagePotentialBond.h:
+// 144-152): p = {k, r_0}; U = k/2 (r - r_0)^2, F/r = k (r_0/r - 1) (0 at r = 0)
+bool eval_harmonic(const double* p, double rsq, double& f, double& e)
+{
+    const double k = p[0], r0 = p[1];
+    const double r = std::sqrt(rsq);
+    f = r > 0.0 ? k * (r0 / r - 1.0) : 0.0;
+    e = 0.5 * k * (r0 - r) * (r0 - r);
+    return true;
+}
+
 bool eval_bond(int kind, const double* p, double rsq, double& f, double& e)
 {
     switch (kind) {
     case BOND_QUARTIC: return eval_quartic(p, rsq, f, e);
     case BOND_DOUBLEWELL: return eval_doublewell(p, rsq, f, e);
+    case BOND_IMAGE_HARMONIC: return eval_harmonic(p, rsq, f, e);
     default: return false;
     }
 }
@@ -463,6 +475,9 @@ int orc_bond_params(int kind, const double* in, double* out)
     }
     case BOND_DOUBLEWELL:
         out[0] = in[1]; out[1] = in[1] - in[0]; out[2] = in[2]; out[3] = in[3];
+        return 0;
+    case BOND_IMAGE_HARMONIC:
+        out[0] = in[0]; out[1] = in[1];
         return 0;
     default: return -1;
     }
@@ -1256,6 +1271,46 @@ void orc_velocity_field(int N, const double* pos, const double* vel, const doubl
     }
     for (size_t k = 0; k < total; ++k)
         for (int d = 0; d < 3; ++d) velocity[3 * k + d] = mass[k] > 0.0 ? momentum[3 * k + d] / mass[k] : 0.0;
+}
+
+// ---- image-unwrapped bonds (src/ImagePotentialBond.h:57-204): for bond (a, b)
+// the vector dx = (x_b - x_a) + (img_b - img_a) L, F_b += f/r dx, F_a -= f/r dx,
+// half the energy and the virial dx (x) dx f/(2r) to each particle, bonds in list
+// order. ACCUMULATES. Returns 0, or 1 + the first refused bond.
+long orc_image_bond_forces(int N, const double* pos, const int32_t* image, const double* L, long nbonds,
+                           const int32_t* bonds, const int32_t* btype, int kind, const double* params, int pstride,
+                           double* force, double* energy, double* virial)
+{
+    (void)N;
+    long bad = 0;
+    for (long k = 0; k < nbonds; ++k) {
+        const int ia = bonds[2 * k], ib = bonds[2 * k + 1];
+        double dx[3];
+        for (int d = 0; d < 3; ++d)
+            dx[d] = (pos[4 * ib + d] - pos[4 * ia + d]) + (double)(image[3 * ib + d] - image[3 * ia + d]) * L[d];
+        const double rsq = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
+        double fdr = 0.0, e = 0.0;
+        if (!eval_bond(kind, params + (size_t)btype[k] * pstride, rsq, fdr, e)) {
+            if (!bad) bad = k + 1;
+            continue;
+        }
+        e *= 0.5;
+        const double h = 0.5 * fdr;
+        const double w[6] = {dx[0] * dx[0] * h, dx[0] * dx[1] * h, dx[0] * dx[2] * h,
+                             dx[1] * dx[1] * h, dx[1] * dx[2] * h, dx[2] * dx[2] * h};
+        for (int d = 0; d < 3; ++d) {
+            force[3 * ib + d] += fdr * dx[d];
+            force[3 * ia + d] -= fdr * dx[d];
+        }
+        energy[ib] += e;
+        energy[ia] += e;
+        if (virial)
+            for (int c = 0; c < 6; ++c) {
+                virial[6 * ib + c] += w[c];
+                virial[6 * ia + c] += w[c];
+            }
+    }
+    return bad;
 }
 
 // ---- maximum squared displacement since the last list build

@@ -31,7 +31,7 @@ PAIR_KINDS = {
     "Colloid": 3,
     "DPDGeneralWeight": 4,
 }
-BOND_KINDS = {"Quartic": 0, "DoubleWell": 1}
+BOND_KINDS = {"Quartic": 0, "DoubleWell": 1, "ImageHarmonic": 2}
 
 # dict keys in the order the C parameter builders read them
 PAIR_KEYS = {
@@ -44,6 +44,7 @@ PAIR_KEYS = {
 BOND_KEYS = {
     "Quartic": ("k", "r_0", "b_1", "b_2", "U_0", "sigma", "epsilon", "delta"),
     "DoubleWell": ("r_0", "r_1", "U_1", "U_tilt"),
+    "ImageHarmonic": ("k", "r0"),
 }
 PAIR_STRIDE = 4
 BOND_STRIDE = 8
@@ -108,6 +109,8 @@ def lib():
     L.orc_wall_params.argtypes = [c_int, _dp, _dp]
     L.orc_wall_params.restype = c_int
     L.orc_velocity_field.argtypes = [c_int, _dp, _dp, _dp, vp, c_int, c_int, _up, _dp, _dp, _dp, _dp, _dp]
+    L.orc_image_bond_forces.argtypes = [c_int, _dp, _ip, _dp, c_long, _ip, _ip, c_int, _dp, c_int, _dp, _dp, vp]
+    L.orc_image_bond_forces.restype = c_long
     L.orc_barrier_valid.argtypes = [c_int, c_double, _dp]
     L.orc_harmonic_barrier.argtypes = [c_int, _dp, _ip, _dp, c_int, c_double, _dp, _dp, _dp]
     _lib = L
@@ -358,6 +361,24 @@ def harmonic_barrier(pos4, types, L, geometry, location, params):
     if st:
         raise ValueError("Barrier position is invalid")
     return F, U
+
+
+def image_bond_forces(pos4, image, L, bonds, btypes, name, params):
+    """Image-unwrapped bond forces (src/ImagePotentialBond.h:57-204): F [N,3],
+    U [N], W [N,6] from the bond list (B,2) and per-bond types."""
+    N = pos4.shape[0]
+    F = np.zeros((N, 3))
+    U = np.zeros(N)
+    W = np.zeros((N, 6))
+    bonds = np.ascontiguousarray(bonds, dtype=np.int32).reshape(-1, 2)
+    bad = lib().orc_image_bond_forces(
+        N, np.ascontiguousarray(pos4, dtype=np.float64), np.ascontiguousarray(image, dtype=np.int32).reshape(-1),
+        np.ascontiguousarray(L, dtype=np.float64), len(bonds), bonds.reshape(-1),
+        np.ascontiguousarray(btypes, dtype=np.int32), BOND_KINDS[name],
+        np.ascontiguousarray(params, dtype=np.float64).reshape(-1), BOND_STRIDE, F, U, _ptr(W))
+    if bad:
+        raise ValueError(f"bond {bad - 1} refused")
+    return F, U, W
 
 
 def bond_forces(pos4, L, bonds, btypes, name, params, F=None, U=None, W=None):

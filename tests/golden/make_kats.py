@@ -1,7 +1,8 @@
 """Extract the known-answer cases of the reference's own tests into kats.json.
 
-Reads ``src/pytest/test_pair.py``, ``src/pytest/test_bond.py`` and
-``src/pytest/test_wall.py`` of the azplugins tree AS TEXT (``ast``; the files import hoomd, which is not needed):
+Reads ``src/pytest/test_pair.py``, ``src/pytest/test_bond.py`` (also the
+``test_image_harmonic`` parameter list) and ``src/pytest/test_wall.py`` of the
+azplugins tree AS TEXT (``ast``; the files import hoomd, which is not needed):
 every ``PotentialTestCase(...)`` call becomes one record with its line number.
 
 Usage: python tests/golden/make_kats.py [/path/to/azplugins]
@@ -38,12 +39,27 @@ def cases(path, fields):
     return out
 
 
+def image_bond_cases(path):
+    """The parametrize list of test_image_harmonic: positions and images of the
+    two bonded particles (the test computes the expected values from them)."""
+    tree = ast.parse(open(path).read())
+    for node in tree.body:
+        if isinstance(node, ast.FunctionDef) and node.name == "test_image_harmonic":
+            for dec in node.decorator_list:
+                if isinstance(dec, ast.Call) and ast.unparse(dec.func).endswith("parametrize"):
+                    rows = ast.literal_eval(dec.args[1])
+                    return [{"position_1": r[0], "position_2": r[1], "image_1": r[2], "image_2": r[3],
+                             "line": node.lineno, "source": f"src/pytest/test_bond.py:{dec.lineno}"} for r in rows]
+    return []
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     pair = cases(os.path.join(root, "src", "pytest", "test_pair.py"),
                  ["params", "r_cut", "shift", "distance", "energy", "force"])
     bond = cases(os.path.join(root, "src", "pytest", "test_bond.py"), ["params", "distance", "energy", "force"])
     wall = cases(os.path.join(root, "src", "pytest", "test_wall.py"), ["params", "position", "energy", "force"])
+    image_bond = image_bond_cases(os.path.join(root, "src", "pytest", "test_bond.py"))
     for r in pair:
         r["source"] = f"src/pytest/test_pair.py:{r['line']}"
     for r in bond:
@@ -51,8 +67,8 @@ def main():
     for r in wall:
         r["source"] = f"src/pytest/test_wall.py:{r['line']}"
     with open(os.path.join(HERE, "kats.json"), "w") as f:
-        json.dump({"pair": pair, "bond": bond, "wall": wall}, f, indent=1)
-    print(f"{len(pair)} pair, {len(bond)} bond and {len(wall)} wall cases")
+        json.dump({"pair": pair, "bond": bond, "wall": wall, "image_bond": image_bond}, f, indent=1)
+    print(f"{len(pair)} pair, {len(bond)} bond, {len(wall)} wall and {len(image_bond)} image-bond cases")
 
 
 if __name__ == "__main__":
