@@ -87,10 +87,30 @@ def test_thin_box_and_overflow_regrow(orc):
     np.testing.assert_array_equal(i, io)
 
 
-# ---------------------------------------------------------------- shared-memory staged build
-# Grids with at least 9 cells per axis take the staged build (row chunks staged
-# in shared memory as relative floats, with its own FP32 band); crowded chunks
-# fall back to global gathers inside the same kernel. The same bit-exact bar.
+@pytest.mark.parametrize("cells", [(3, 3, 3), (4, 3, 5), (6, 4, 3), (3, 7, 4), (5, 5, 5), (12, 3, 4)])
+def test_small_grids_bit_exact(orc, cells):
+    """Boxes of 3-12 cells per axis: the stencil's periodic wrap at the faces,
+    and axes whose whole extent the stencil covers (every neighbour cell also
+    a periodic image of another), against the oracle's brute-force sets."""
+    import azplugins_gb300 as az
+
+    rng = np.random.Generator(np.random.PCG64(sum(cells)))
+    rc, r_buff = 2.5, 0.4
+    rl = rc + r_buff
+    L = np.array([c * rl * 1.07 for c in cells])
+    N = int(0.6 * np.prod(L))
+    snap = az.Snapshot(N)
+    snap.particles.position = rng.uniform(-0.5, 0.5, size=(N, 3)) * L
+    snap.configuration.box = [L[0], L[1], L[2], 0, 0, 0]
+    s, i = _gpu_list(snap, np.array([[rc]]), r_buff, max_neighbors=96)
+    so, io = orc.nlist(pos4_of(snap), snap.particles.typeid, 1, box_of(snap), np.array([[rl * rl]]), method="brute")
+    np.testing.assert_array_equal(s, so)
+    np.testing.assert_array_equal(i, io)
+
+
+# ---------------------------------------------------------------- melt-density systems
+# Larger grids at the bead-spring melt's density, several types, exclusions,
+# boundary pairs and crowded clumps. The same bit-exact bar.
 
 
 def _check(orc, snap, rc, r_buff, ex=None, ntypes=1):
@@ -102,13 +122,13 @@ def _check(orc, snap, rc, r_buff, ex=None, ntypes=1):
 
 
 @pytest.mark.parametrize("seed", [7, 8])
-def test_staged_melt_density_bit_exact(orc, seed):
+def test_melt_density_bit_exact(orc, seed):
     # WCA list radius at melt density: 21 cells per axis
     snap = random_fluid(30000, 0.85, seed=seed, min_dist=0.8)
     _check(orc, snap, np.array([[2 ** (1 / 6)]]), 0.4)
 
 
-def test_staged_multitype_and_exclusions(orc):
+def test_melt_multitype_and_exclusions(orc):
     snap = random_fluid(30000, 0.6, seed=9, ntypes=3, min_dist=0.6)
     rc = np.array([[1.1, 1.3, 0.0], [1.3, 1.5, 1.2], [0.0, 1.2, 1.0]])
     N = snap.particles.N
@@ -116,7 +136,7 @@ def test_staged_multitype_and_exclusions(orc):
     _check(orc, snap, rc, 0.3, ex, ntypes=3)
 
 
-def test_staged_boundary_pairs(orc):
+def test_melt_boundary_pairs(orc):
     import azplugins_gb300 as az
 
     rng = np.random.Generator(np.random.PCG64(10))
@@ -136,7 +156,7 @@ def test_staged_boundary_pairs(orc):
     _check(orc, snap, np.array([[1.1]]), 0.4)
 
 
-def test_staged_crowded_chunks_fall_back(orc):
+def test_crowded_clumps(orc):
     # a dense clump overflows the shared-memory staging of its chunks
     import azplugins_gb300 as az
 
