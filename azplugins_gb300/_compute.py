@@ -154,7 +154,7 @@ def pair_forces(state, pair, precision="fp64", tpp=4):
     return f, w
 
 
-def dpd_forces(state, pair, precision, dt, timestep, seed, tpp=4):
+def dpd_forces(state, pair, precision, dt, timestep, seed, tpp=2):
     """(force4 [N,4], virial [N,6]) of a DPDGeneralWeight potential at the state:
     conservative + dissipative + random forces, conservative energy and virial."""
     torch = _torch()

@@ -28,6 +28,8 @@ namespace
 constexpr int DPD_BLOCK = 256;
 // per type pair: rcutsq, rcinv, rc, A, gamma, s/2, sigma_R = sqrt(6 kT gamma / dt), -
 constexpr int DPD_TBL = 8;
+// in-range partners a thread queues before evaluating them (FP32 path)
+constexpr uint32_t DPD_QUEUE = 16;
 
 struct DpdArgs {
     const double4_32a* pos;
@@ -75,6 +77,26 @@ __global__ void k_vel_f(const double4_32a* __restrict__ vel, uint32_t N, float4*
     out[i] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.0f);
 }
 
+// (1 - r / r_cut)^(s/2): the exponents s/2 = 1/4, 1/2, 1 (s = 1/2, 1, 2, the
+// usual choices) as square roots, which agree with pow to an ulp or two and
+// avoid its cost (in FP64 a pow costs as much as the rest of the pair); any
+// other exponent through pow
+AZP_D double dpd_weight(double x, double h)
+{
+    if (h == 0.5) return sqrt(x);
+    if (h == 0.25) return sqrt(sqrt(x));
+    if (h == 1.0) return x;
+    return pow(x, h);
+}
+
+AZP_D float dpd_weight_f(float x, float h)
+{
+    if (h == 0.5f) return sqrtf(x);
+    if (h == 0.25f) return sqrtf(sqrtf(x));
+    if (h == 1.0f) return x;
+    return powf(x, h);
+}
+
 // alpha of a pair, FP64: the first 64-bit word of the pair's Philox block
 AZP_D double dpd_alpha(uint32_t k0, uint32_t k1, uint32_t ti, uint32_t tj)
 {
@@ -106,7 +128,7 @@ AZP_D bool dpd_pair_fp64(const DpdArgs& a, const double* c, const double4_32a& p
     const double r = 1.0 / rinv;
     const double dot = dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z);
     fc = c[3] * (rinv - c[1]);
-    const double wR = pow(fmax(1.0 - r * c[1], 0.0), c[5]) * rinv;  // never below 0 (r < r_cut)
+    const double wR = dpd_weight(fmax(1.0 - r * c[1], 0.0), c[5]) * rinv;  // never below 0 (r < r_cut)
     const double alpha = dpd_alpha(a.k0, a.k1, tgi, tgj);
     fdr = fc - c[4] * wR * wR * dot + c[6] * wR * alpha;
     e = c[3] * (c[2] - r) - 0.5 * c[3] * c[1] * (c[0] - rs);
@@ -189,12 +211,21 @@ template<> struct DpdAcc<float> {
     }
 };
 
+// FP32: at most 64 registers a thread (4 blocks an SM): the kernel is latency
+// bound and gains more from resident warps than from registers
 template<typename R, int TPP>
-__global__ void __launch_bounds__(DPD_BLOCK) k_dpd(DpdArgs a)
+__global__ void __launch_bounds__(DPD_BLOCK, std::is_same<R, float>::value ? 4 : 1) k_dpd(DpdArgs a)
 {
+    // the type-pair table in FP64 (FP64 pairs) and, for the FP32 path, as floats
+    // (converted once per block, not per pair)
     extern __shared__ __align__(16) double s_tbl[];
     const uint32_t nt2 = a.ntypes * a.ntypes;
-    for (uint32_t t = threadIdx.x; t < nt2 * DPD_TBL; t += blockDim.x) s_tbl[t] = a.table[t];
+    float* s_tf = reinterpret_cast<float*>(s_tbl + (size_t)nt2 * DPD_TBL);
+    uint32_t* s_queue = reinterpret_cast<uint32_t*>(s_tf + (size_t)nt2 * DPD_TBL);
+    for (uint32_t t = threadIdx.x; t < nt2 * DPD_TBL; t += blockDim.x) {
+        s_tbl[t] = a.table[t];
+        if constexpr (std::is_same<R, float>::value) s_tf[t] = (float)a.table[t];
+    }
     __syncthreads();
     const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i = gid / TPP;
@@ -220,6 +251,38 @@ __global__ void __launch_bounds__(DPD_BLOCK) k_dpd(DpdArgs a)
             const uint4 fi = a.fixed[i];
             const float4 vi = a.vel_f[i];
             const uint32_t ti = fi.w;
+            // Two phases per thread: the candidate scan (a gather and a distance)
+            // queues the partners inside r_cut in this thread's shared-memory
+            // slots, then the queue is evaluated (a Philox draw and the weight per
+            // pair), so the warp runs the costly part with its lanes together
+            // instead of once per lane whose candidate happens to be in range.
+            uint32_t* q = s_queue + threadIdx.x * DPD_QUEUE;
+            uint32_t nq = 0;
+            auto flush = [&]() {
+                for (uint32_t m = 0; m < nq; ++m) {
+                    const uint32_t j = q[m];
+                    const uint4 fj = a.fixed[j];
+                    const float dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
+                    const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
+                    const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
+                    const float rs = dx * dx + dy * dy + dz * dz;
+                    const float* cf = s_tf + (size_t)(ti * a.ntypes + fj.w) * DPD_TBL;
+                    const float rc2 = cf[0];
+                    const float4 vj = a.vel_f[j];
+                    const float rcinv = cf[1];
+                    const float A = cf[3];
+                    const float rinv = rsqrtf(rs);
+                    const float r = rs * rinv;
+                    const float dot = dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z);
+                    const float fc = A * (rinv - rcinv);
+                    const float wR = dpd_weight_f(fmaxf(1.0f - r * rcinv, 0.0f), cf[5]) * rinv;
+                    const float alpha = dpd_alpha_f(a.k0, a.k1, tgi, a.tag[j]);
+                    const float fdr = fc - cf[4] * wR * wR * dot + cf[6] * wR * alpha;
+                    const float e = A * (cf[2] - r) - 0.5f * A * rcinv * (rc2 - rs);
+                    acc.add(dx, dy, dz, fdr, fc, e);
+                }
+                nq = 0;
+            };
             for (uint32_t k = sub; k < n; k += TPP) {
                 const uint32_t j = a.nbrs[(size_t)k * a.N + i];
                 const uint4 fj = a.fixed[j];
@@ -227,10 +290,17 @@ __global__ void __launch_bounds__(DPD_BLOCK) k_dpd(DpdArgs a)
                 const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
                 const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
                 const float rs = dx * dx + dy * dy + dz * dz;
-                const double* c = s_tbl + (size_t)(ti * a.ntypes + fj.w) * DPD_TBL;
-                const float rc2 = (float)c[0];
+                const size_t tp = (size_t)(ti * a.ntypes + fj.w) * DPD_TBL;
+                const float* cf = s_tf + tp;
+                const float rc2 = cf[0];
                 if (rs >= rc2 * 1.000004f) continue;
-                if (rs >= rc2 * 0.998f) {
+                if (rs < rc2 * 0.998f) {
+                    q[nq++] = j;
+                    if (nq == DPD_QUEUE) flush();
+                    continue;
+                }
+                {
+                    const double* c = s_tbl + tp;
                     // Near r_cut the random weight (1 - r / r_cut)^(s/2) is steep
                     // (infinitely so at r_cut for s < 2): an FP32 or fixed-point r
                     // would cost percents of this pair's force. Such pairs (about
@@ -240,21 +310,9 @@ __global__ void __launch_bounds__(DPD_BLOCK) k_dpd(DpdArgs a)
                     if (dpd_pair_fp64(a, c, a.pos[i], a.pos[j], a.vel[i], a.vel[j], tgi, a.tag[j], ddx, ddy, ddz, dfdr,
                                       dfc, de))
                         acc.add((float)ddx, (float)ddy, (float)ddz, (float)dfdr, (float)dfc, (float)de);
-                    continue;
                 }
-                const float4 vj = a.vel_f[j];
-                const float rcinv = (float)c[1];
-                const float A = (float)c[3];
-                const float rinv = rsqrtf(rs);
-                const float r = rs * rinv;
-                const float dot = dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z);
-                const float fc = A * (rinv - rcinv);
-                const float wR = powf(fmaxf(1.0f - r * rcinv, 0.0f), (float)c[5]) * rinv;
-                const float alpha = dpd_alpha_f(a.k0, a.k1, tgi, a.tag[j]);
-                const float fdr = fc - (float)c[4] * wR * wR * dot + (float)c[6] * wR * alpha;
-                const float e = A * ((float)c[2] - r) - 0.5f * A * rcinv * (rc2 - rs);
-                acc.add(dx, dy, dz, fdr, fc, e);
             }
+            flush();
         }
     }
     if (TPP > 1) acc.reduce(TPP);
@@ -318,7 +376,8 @@ extern "C" int azp_dpd_forces(const azp_system* sys, azp_nlist* nl, const double
     a.force = out->force;
     a.virial = out->virial;
     a.pitch = out->virial_pitch ? out->virial_pitch : sys->N;
-    const size_t smem = (size_t)nt2 * DPD_TBL * sizeof(double);
+    const size_t smem = (size_t)nt2 * DPD_TBL * (sizeof(double) + sizeof(float)) +
+                        (out->precision == AZP_FP32 ? (size_t)DPD_BLOCK * DPD_QUEUE * sizeof(uint32_t) : 0);
     if (out->precision == AZP_FP32) {
         launch_to_fixed(a.pos, nl->fixed, sys->N, sys->box, s);
         k_vel_f<<<(sys->N + 255) / 256, 256, 0, s>>>(a.vel, sys->N, nl->vel_f);

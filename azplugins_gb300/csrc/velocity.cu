@@ -40,44 +40,72 @@ struct BinSpec {
     uint32_t nb[3];
     int use[3];
     double lo[3], hi[3];
+    double scale[3];  // nb / (hi - lo)
     uint32_t total;
 };
 
-// src/BinningOperation.h:71-87
-AZP_HD bool bin1d(double x, double lo, double hi, uint32_t n, uint32_t& b)
+// src/BinningOperation.h:71-87: floor((x - lo) / (hi - lo) * n), inside [0, n).
+// FP64 division is slow here (about 1/64 of the FP32 rate), so the bin comes
+// from a multiplication by n / (hi - lo); a value within 1e-9 of a bin edge,
+// where the two roundings could disagree, takes the reference's division.
+AZP_HD bool bin1d(double x, double lo, double hi, double scale, uint32_t n, uint32_t& b)
 {
-    const int k = (int)floor(((x - lo) / (hi - lo)) * n);
-    if (k >= 0 && k < (int)n) {
+    const double u = (x - lo) * scale;
+    const double fu = floor(u);
+    const double k = (u - fu < 1e-9 || fu + 1.0 - u < 1e-9) ? floor(((x - lo) / (hi - lo)) * n) : fu;
+    if (k >= 0.0 && k < (double)n) {
         b = (uint32_t)k;
         return true;
     }
     return false;
 }
 
-// src/CartesianBinningOperation.h:27-52, src/CylindricalBinningOperation.h:27-76
+// theta in [0, 2 pi) for the bin: atan2f, or the FP64 atan2 within 1e-5 of an
+// edge (atan2f is good to a few 1e-7 here)
+AZP_D bool bin_theta(const BinSpec& s, double x, double y, uint32_t& b)
+{
+    float tf = atan2f((float)y, (float)x);
+    if (tf < 0.0f) tf += 6.283185307179586f;
+    const double u = ((double)tf - s.lo[1]) * s.scale[1];
+    const double fu = floor(u);
+    const double guard = 1e-5 * s.scale[1];
+    if (u - fu < guard || fu + 1.0 - u < guard) {
+        double theta = atan2(y, x);
+        if (theta < 0.0) theta += 2.0 * M_PI;
+        return bin1d(theta, s.lo[1], s.hi[1], s.scale[1], s.nb[1], b);
+    }
+    if (fu >= 0.0 && fu < (double)s.nb[1]) {
+        b = (uint32_t)fu;
+        return true;
+    }
+    return false;
+}
+
+// src/CartesianBinningOperation.h:27-52, src/CylindricalBinningOperation.h:27-76.
+// x: the position (binned axes already wrapped), p: the momentum m v
 AZP_D bool bin_particle(const BinSpec& s, const double* x, const double* p, uint32_t& idx, double* t)
 {
     uint32_t b[3] = {0u, 0u, 0u};
     if (s.kind == AZP_BINNING_CARTESIAN) {
         for (int d = 0; d < 3; ++d)
-            if (s.use[d] && !bin1d(x[d], s.lo[d], s.hi[d], s.nb[d], b[d])) return false;
+            if (s.use[d] && !bin1d(x[d], s.lo[d], s.hi[d], s.scale[d], s.nb[d], b[d])) return false;
         t[0] = p[0];
         t[1] = p[1];
         t[2] = p[2];
     } else {
-        if (s.use[2] && !bin1d(x[2], s.lo[2], s.hi[2], s.nb[2], b[2])) return false;
-        if (s.use[1]) {
-            double theta = atan2(x[1], x[0]);
-            if (theta < 0.0) theta += 2.0 * M_PI;
-            if (!bin1d(theta, s.lo[1], s.hi[1], s.nb[1], b[1])) return false;
+        if (s.use[2] && !bin1d(x[2], s.lo[2], s.hi[2], s.scale[2], s.nb[2], b[2])) return false;
+        if (s.use[1] && !bin_theta(s, x[0], x[1], b[1])) return false;
+        // 1/r from rsqrtf and one Newton step in FP64 (relative error ~1e-14)
+        const double r2 = x[0] * x[0] + x[1] * x[1];
+        double c = 1.0, sn = 0.0, r = 0.0;
+        if (r2 > 0.0) {
+            const double g = (double)rsqrtf((float)r2);
+            const double rinv = g * (1.5 - 0.5 * r2 * g * g);
+            r = r2 * rinv;
+            c = x[0] * rinv;
+            sn = x[1] * rinv;
         }
-        const double r = sqrt(x[0] * x[0] + x[1] * x[1]);
-        if (s.use[0] && !bin1d(r, s.lo[0], s.hi[0], s.nb[0], b[0])) return false;
-        double c = 1.0, sn = 0.0;
-        if (r > 0.0) {
-            c = x[0] / r;
-            sn = x[1] / r;
-        }
+        if (s.use[0] && !bin1d(r, s.lo[0], s.hi[0], s.scale[0], s.nb[0], b[0])) return false;
         t[0] = c * p[0] + sn * p[1];
         t[1] = -sn * p[0] + c * p[1];
         t[2] = p[2];
@@ -97,7 +125,8 @@ AZP_D unsigned long long warp_sum(unsigned long long v)
 __global__ void __launch_bounds__(kBlock) k_vfield(const double4_32a* __restrict__ pos,
                                                    const double4_32a* __restrict__ vel,
                                                    const uint32_t* __restrict__ group, uint32_t n, BoxD box,
-                                                   BinSpec spec, int use_smem, unsigned long long* __restrict__ acc,
+                                                   const __grid_constant__ BinSpec spec, int use_smem,
+                                                   unsigned long long* __restrict__ acc,
                                                    uint32_t* __restrict__ err)
 {
     extern __shared__ unsigned long long s_acc[];
@@ -119,23 +148,28 @@ __global__ void __launch_bounds__(kBlock) k_vfield(const double4_32a* __restrict
             const double4_32a pp = pos[i];
             const double4_32a vv = vel[i];
             double x[3] = {pp.x, pp.y, pp.z};
-            // src/VelocityFieldCompute.h:196-198: wrap into the box first
+            // src/VelocityFieldCompute.h:196-198: wrap into the box first (the axes
+            // the bins read: the binned Cartesian ones; x, y and a binned z for
+            // cylindrical bins)
             int img = 0;
-            for (int d = 0; d < 3; ++d) wrap1(x[d], img, box.L[d], box.lo[d], box.hi[d]);
+            for (int d = 0; d < 3; ++d)
+                if (spec.use[d] || (spec.kind == AZP_BINNING_CYLINDRICAL && d < 2))
+                    wrap1(x[d], img, box.L[d], box.lo[d], box.hi[d]);
             const double mi = vv.w;
-            const double p[3] = {vv.x * mi, vv.y * mi, vv.z * mi};
+            // the mass folded into the fixed-point scale: m 2^40 is exact
+            const double ms = mi * kScale;
+            const double p[3] = {vv.x * ms, vv.y * ms, vv.z * ms};
             double t[3];
             ok = bin_particle(spec, x, p, bin, t);
             if (ok) {
-                const double vals[4] = {mi, t[0], t[1], t[2]};
+                const double vals[4] = {ms, t[0], t[1], t[2]};
                 for (int c = 0; c < 4; ++c) {
-                    const double s = vals[c] * kScale;
-                    if (!(fabs(s) < kMaxFixed)) {
+                    if (!(fabs(vals[c]) < kMaxFixed)) {
                         atomicOr(err, AZP_EBIT_RANGE);
                         ok = false;
                         break;
                     }
-                    q[c] = __double2ll_rn(s);
+                    q[c] = __double2ll_rn(vals[c]);
                 }
             }
         }
@@ -214,6 +248,7 @@ azp_vfield* azp_vfield_create(int kind, const uint32_t* num_bins, const double* 
         s.lo[d] = lower[d];
         s.hi[d] = upper[d];
         if (s.use[d] && !(upper[d] > lower[d])) return fail(AZP_ERR_INVALID);
+        s.scale[d] = s.use[d] ? (double)s.nb[d] / (upper[d] - lower[d]) : 0.0;
         total *= s.nb[d];
     }
     if (total > (1ull << 26)) return fail(record_error(AZP_ERR_TOO_LARGE, "azp_vfield_create: more than 2^26 bins"));

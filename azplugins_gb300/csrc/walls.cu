@@ -5,9 +5,11 @@
 // builders (src/WallEvaluatorLJ93.h:31-45, src/WallEvaluatorColloid.h:31-53).
 //
 // One thread per particle; the walls travel as a kernel argument (HOOMD passes
-// its wall field by value too), so every thread reads them from the constant
-// bank. Arithmetic FP64 in both output precisions: each particle costs a few
-// dozen operations per wall against 32 bytes read and up to 80 written.
+// its wall field by value too), declared __grid_constant__ so that every thread
+// reads them from the constant bank (without it the device code's references
+// into the 5.4 KB field make a per-thread copy in local memory). FP64 output: FP64 arithmetic throughout. FP32 output: FP32 arithmetic
+// except the differences that cancel near a surface (walls.cuh), because FP64
+// runs at about 1/64 of the FP32 rate and the FP64 form is bound by it.
 #include <cmath>
 
 #include "common.cuh"
@@ -23,7 +25,8 @@ template<class EV, typename T>
 __global__ void __launch_bounds__(kBlock) k_walls(const double4_32a* __restrict__ pos,
                                                   const double4_32a* __restrict__ params,
                                                   const double* __restrict__ r_cut,
-                                                  const double* __restrict__ r_extrap, const WallField wf, uint32_t N,
+                                                  const double* __restrict__ r_extrap,
+                                                  const __grid_constant__ WallField wf, uint32_t N,
                                                   T* __restrict__ force, T* __restrict__ virial, uint32_t pitch)
 {
     const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
@@ -46,7 +49,39 @@ __global__ void __launch_bounds__(kBlock) k_walls(const double4_32a* __restrict_
     }
 }
 
-template<class EV>
+// FP32 output: FP32 arithmetic with the FP64 parts that cancellation needs
+// (walls.cuh), per-type float records made once per block in shared memory
+template<class EV, class EVF>
+__global__ void __launch_bounds__(kBlock) k_walls_f(const double4_32a* __restrict__ pos,
+                                                    const double4_32a* __restrict__ params,
+                                                    const double* __restrict__ r_cut,
+                                                    const double* __restrict__ r_extrap, uint32_t ntypes,
+                                                    const __grid_constant__ WallField wf, uint32_t N,
+                                                    float* __restrict__ force,
+                                                    float* __restrict__ virial, uint32_t pitch)
+{
+    extern __shared__ float s_q[];
+    for (uint32_t t = threadIdx.x; t < ntypes; t += kBlock) {
+        const double4_32a rec = params[t];
+        const double p[4] = {rec.x, rec.y, rec.z, rec.w};
+        wall_record_f<EV>(p, r_cut[t], r_extrap[t], s_q + (size_t)t * WALL_F);
+    }
+    __syncthreads();
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= N) return;
+    const double4_32a pp = pos[i];
+    const double x[3] = {pp.x, pp.y, pp.z};
+    float F[3] = {0.0f, 0.0f, 0.0f}, U = 0.0f;
+    walls_force_f<EVF>(wf, s_q + (size_t)type_of(pp.w) * WALL_F, x, F, U);
+    reinterpret_cast<float4*>(force)[i] = make_float4(F[0], F[1], F[2], U);
+    if (virial) {
+        const float xf = (float)x[0], yf = (float)x[1], zf = (float)x[2];
+        const float v[6] = {F[0] * xf, F[0] * yf, F[0] * zf, F[1] * yf, F[1] * zf, F[2] * zf};
+        for (int c = 0; c < 6; ++c) virial[(size_t)c * pitch + i] = v[c];
+    }
+}
+
+template<class EV, class EVF>
 void launch_walls(const azp_system* sys, const double* params, const double* r_cut, const double* r_extrap,
                   const WallField& wf, const azp_forces* out, cudaStream_t s)
 {
@@ -59,9 +94,9 @@ void launch_walls(const azp_system* sys, const double* params, const double* r_c
                                                     static_cast<double*>(out->force),
                                                     static_cast<double*>(out->virial), pitch);
     else
-        k_walls<EV, float><<<grid, kBlock, 0, s>>>(pos, par, r_cut, r_extrap, wf, sys->N,
-                                                   static_cast<float*>(out->force), static_cast<float*>(out->virial),
-                                                   pitch);
+        k_walls_f<EV, EVF><<<grid, kBlock, sizeof(float) * WALL_F * sys->ntypes, s>>>(
+            pos, par, r_cut, r_extrap, sys->ntypes, wf, sys->N, static_cast<float*>(out->force),
+            static_cast<float*>(out->virial), pitch);
 }
 
 bool unit(const double* v, double* u)
@@ -171,10 +206,11 @@ int azp_wall_forces(const azp_system* sys, int kind, const azp_walls* walls, con
     if (sys->N == 0) return AZP_OK;
     if (!sys->pos || !params || !r_cut || !r_extrap) return AZP_ERR_INVALID;
     cudaStream_t s = as_stream(stream);
+    if (sys->ntypes == 0 || sys->ntypes > 4096) return AZP_ERR_INVALID;
     if (kind == AZP_WALL_LJ93)
-        launch_walls<WallLJ93>(sys, params, r_cut, r_extrap, wf, out, s);
+        launch_walls<WallLJ93, WallLJ93F>(sys, params, r_cut, r_extrap, wf, out, s);
     else
-        launch_walls<WallColloid>(sys, params, r_cut, r_extrap, wf, out, s);
+        launch_walls<WallColloid, WallColloidF>(sys, params, r_cut, r_extrap, wf, out, s);
     AZP_CHECK_LAUNCH("k_walls");
     return AZP_OK;
 }

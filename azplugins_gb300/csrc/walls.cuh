@@ -106,10 +106,12 @@ AZP_HD void wall_sphere(const WallSphereD& w, const double* x, double* dr, doubl
     const double rxyz = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
     if (rxyz > 0.0) {
         inside = (w.inside ? rxyz < w.r : rxyz > w.r) || (rxyz == w.r && !w.open);
-        const double s = w.r / rxyz;
+        // one reciprocal instead of four divisions (FP64 division is slow here)
+        const double rinv = 1.0 / rxyz;
+        const double s = w.r * rinv;
         for (int d = 0; d < 3; ++d) {
             dr[d] = t[d] - t[d] * s;
-            nrm[d] = w.inside ? -t[d] / rxyz : t[d] / rxyz;
+            nrm[d] = w.inside ? -t[d] * rinv : t[d] * rinv;
         }
     } else {
         // at the centre every surface point is nearest: the one along +x
@@ -128,10 +130,11 @@ AZP_HD void wall_cylinder(const WallCylinderD& w, const double* x, double* dr, d
     const double rxy = sqrt(pp[0] * pp[0] + pp[1] * pp[1] + pp[2] * pp[2]);
     if (rxy > 0.0) {
         inside = (w.inside ? rxy < w.r : rxy > w.r) || (rxy == w.r && !w.open);
-        const double s = w.r / rxy;
+        const double rinv = 1.0 / rxy;
+        const double s = w.r * rinv;
         for (int d = 0; d < 3; ++d) {
             dr[d] = pp[d] - pp[d] * s;
-            nrm[d] = w.inside ? -pp[d] / rxy : pp[d] / rxy;
+            nrm[d] = w.inside ? -pp[d] * rinv : pp[d] * rinv;
         }
     } else {
         // on the axis: the surface point along the first direction normal to the axis
@@ -183,8 +186,8 @@ AZP_HD void wall_apply(const double* p, double rcutsq, double rextrap, const dou
         const double r = sqrt(rsq);
         double u[3];
         if (rsq > 0.0) {
-            const double sgn = inside ? 1.0 : -1.0;
-            for (int d = 0; d < 3; ++d) u[d] = sgn * dr[d] / r;
+            const double sr = (inside ? 1.0 : -1.0) / r;
+            for (int d = 0; d < 3; ++d) u[d] = sr * dr[d];
         } else {
             for (int d = 0; d < 3; ++d) u[d] = nrm[d];
         }
@@ -221,6 +224,186 @@ AZP_HD void walls_force(const WallField& wf, const double* p, double rcutsq, dou
     for (int k = 0; k < wf.np; ++k) {
         wall_plane(wf.p[k], x, dr, nrm, inside);
         wall_apply<EV>(p, rcutsq, rextrap, dr, nrm, inside, F, U);
+    }
+}
+
+// ---------------------------------------------------------------- FP32 path
+// Per-type float record of the FP32 driver, made once per block from the FP64
+// evaluator: q[0..2] the evaluator's constants (LJ93: lj1 = 2/15 A sigma^9,
+// lj2 = A sigma^3; Colloid: c_1, c_2, a), q[3] the energy at r_cut (the shift),
+// q[4] r_cut^2, q[5] the force magnitude F(r_extrap) = (F/r)(r_extrap) r_extrap,
+// q[6] U(r_extrap) (shifted), q[7] r_extrap.
+constexpr int WALL_F = 8;
+
+template<class EV> AZP_D void wall_record_f(const double* p, double rc, double rx, float* q);
+
+template<> AZP_D void wall_record_f<WallLJ93>(const double* p, double rc, double rx, float* q)
+{
+    const double lj1 = (2.0 / 15.0) * p[1] * p[0] * p[0] * p[0], lj2 = p[1] * p[0];
+    const double rc2 = rc * rc;
+    const double rc2inv = 1.0 / rc2, rc3inv = rc2inv * sqrt(rc2inv), rc6inv = rc3inv * rc3inv;
+    q[0] = (float)lj1;
+    q[1] = (float)lj2;
+    q[2] = 0.0f;
+    q[3] = (float)(rc3inv * (lj1 * rc6inv - lj2));
+    q[4] = (float)rc2;
+    double fdr = 0.0, e = 0.0;
+    const bool ok = rx > 0.0 && WallLJ93::eval(p, rx * rx, rc2, fdr, e);
+    q[5] = ok ? (float)(fdr * rx) : 0.0f;
+    q[6] = ok ? (float)e : 0.0f;
+    q[7] = (float)rx;
+}
+
+template<> AZP_D void wall_record_f<WallColloid>(const double* p, double rc, double rx, float* q)
+{
+    const double rc2 = rc * rc;
+    double unused = 0.0;
+    q[0] = (float)p[0];
+    q[1] = (float)p[1];
+    q[2] = (float)p[2];
+    q[3] = (p[0] != 0.0 && p[2] > 0.0) ? (float)WallColloid::potential(p, rc2, false, unused) : 0.0f;
+    q[4] = (float)rc2;
+    double fdr = 0.0, e = 0.0;
+    const bool ok = rx > 0.0 && WallColloid::eval(p, rx * rx, rc2, fdr, e);
+    q[5] = ok ? (float)(fdr * rx) : 0.0f;
+    q[6] = ok ? (float)e : 0.0f;
+    q[7] = (float)rx;
+}
+
+// FP32 evaluators on the float record (the same forms as the FP64 ones)
+struct WallLJ93F {
+    AZP_D static bool eval(const float* q, float rsq, float& fdr, float& e)
+    {
+        if (!(rsq < q[4]) || q[0] == 0.0f) return false;
+        const float r2inv = 1.0f / rsq;
+        const float r3inv = r2inv * sqrtf(r2inv);
+        const float r6inv = r3inv * r3inv;
+        fdr = r2inv * r3inv * (9.0f * q[0] * r6inv - 3.0f * q[1]);
+        e = r3inv * (q[0] * r6inv - q[1]) - q[3];
+        return true;
+    }
+};
+
+struct WallColloidF {
+    AZP_D static bool eval(const float* q, float rsq, float& fdr, float& e)
+    {
+        const float c1 = q[0], c2 = q[1], a = q[2];
+        if (!(rsq < q[4]) || c1 == 0.0f || !(a > 0.0f)) return false;
+        const float r = sqrtf(rsq);
+        const float arinv = a / r;
+        const float rma = 1.0f / (r - a), rpa = 1.0f / (r + a);
+        const float r2ma2 = rma * rpa;
+        const float rma2 = rma * rma, rma6 = rma2 * rma2 * rma2;
+        const float rpa2 = rpa * rpa, rpa6 = rpa2 * rpa2 * rpa2;
+        const float arinv8 = 8.0f * arinv;
+        fdr = 6.0f * c1 * ((arinv8 - 1.0f) * rma2 * rma6 + (arinv8 + 1.0f) * rpa2 * rpa6) -
+              c2 * (4.0f * a * a * arinv * r2ma2 * r2ma2);
+        const float a7 = 7.0f * a;
+        e = c1 * ((a7 - r) * rma * rma6 + (a7 + r) * rpa * rpa6) - c2 * (2.0f * a * r * r2ma2 + logf(rpa / rma)) - q[3];
+        return true;
+    }
+};
+
+// one wall in FP32 from its distance d >= 0, the unit vector u from the nearest
+// surface point to the particle (dr = d u), the active-side flag and the surface
+// normal towards the active side (used at d = 0)
+template<class EVF>
+AZP_D void wall_apply_f(const float* q, float d, const float* u, bool inside, const float* nrm, float* F, float& U)
+{
+    const float rx = q[7];
+    float fdr = 0.0f, e = 0.0f;
+    if (rx > 0.0f) {
+        if (inside && d >= rx) {
+            if (EVF::eval(q, d * d, fdr, e)) {
+                for (int k = 0; k < 3; ++k) F[k] += u[k] * (d * fdr);
+                U += e;
+            }
+            return;
+        }
+        // linear continuation: constant force towards the active side
+        const float sgn = inside ? 1.0f : -1.0f;
+        const float* dir = d > 0.0f ? u : nrm;
+        const float s = d > 0.0f ? sgn : 1.0f;
+        for (int k = 0; k < 3; ++k) F[k] += s * dir[k] * q[5];
+        U += q[6] + q[5] * (rx - sgn * d);
+        return;
+    }
+    if (!inside) return;
+    if (EVF::eval(q, d * d, fdr, e)) {
+        for (int k = 0; k < 3; ++k) F[k] += u[k] * (d * fdr);
+        U += e;
+    }
+}
+
+// a curved wall (sphere: axis = nullptr; cylinder: unit axis) in FP32 with the
+// FP64 parts that cancellation needs: x - origin, r^2 and R^2 - r^2, so that the
+// distance R - r = (R^2 - r^2) / (R + r) keeps FP32 relative accuracy near the
+// surface without an FP64 square root
+template<class EVF>
+AZP_D void curved_wall_f(double R, const double* o, const double* ax, int w_inside, int w_open, const double* x,
+                         const float* q, float* F, float& U)
+{
+    double t[3] = {x[0] - o[0], x[1] - o[1], x[2] - o[2]};
+    if (ax) {
+        const double al = t[0] * ax[0] + t[1] * ax[1] + t[2] * ax[2];
+        for (int k = 0; k < 3; ++k) t[k] -= al * ax[k];
+    }
+    const double r2 = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+    float u[3], nrm[3], d;
+    bool inside;
+    if (r2 > 0.0) {
+        const float rf = sqrtf((float)r2);
+        const float din = (float)(R * R - r2) / ((float)R + rf);  // R - r, > 0 inside the surface
+        const float rinv = 1.0f / rf;
+        const float th[3] = {(float)t[0] * rinv, (float)t[1] * rinv, (float)t[2] * rinv};
+        inside = (w_inside ? din > 0.0f : din < 0.0f) || (din == 0.0f && !w_open);
+        d = fabsf(din);
+        const float sd = din > 0.0f ? -1.0f : 1.0f;  // from the surface point to the particle
+        for (int k = 0; k < 3; ++k) {
+            u[k] = sd * th[k];
+            nrm[k] = w_inside ? -th[k] : th[k];
+        }
+    } else {
+        // at the centre (on the axis): the surface point along a fixed direction, as in the FP64 path
+        double dir[3] = {1.0, 0.0, 0.0};
+        if (ax) {
+            if (fabs(ax[0]) < 0.9) {
+                dir[0] = 0.0;
+                dir[1] = ax[2];
+                dir[2] = -ax[1];
+            } else {
+                dir[0] = -ax[2];
+                dir[1] = 0.0;
+                dir[2] = ax[0];
+            }
+            const double un = sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+            for (int k = 0; k < 3; ++k) dir[k] /= un;
+        }
+        inside = w_inside != 0;
+        d = (float)R;
+        for (int k = 0; k < 3; ++k) {
+            u[k] = -(float)dir[k];
+            nrm[k] = 0.0f;
+        }
+    }
+    wall_apply_f<EVF>(q, d, u, inside, nrm, F, U);
+}
+
+template<class EVF>
+AZP_D void walls_force_f(const WallField& wf, const float* q, const double* x, float* F, float& U)
+{
+    for (int k = 0; k < wf.ns; ++k)
+        curved_wall_f<EVF>(wf.s[k].r, wf.s[k].o, nullptr, wf.s[k].inside, wf.s[k].open, x, q, F, U);
+    for (int k = 0; k < wf.nc; ++k)
+        curved_wall_f<EVF>(wf.c[k].r, wf.c[k].o, wf.c[k].ax, wf.c[k].inside, wf.c[k].open, x, q, F, U);
+    for (int k = 0; k < wf.np; ++k) {
+        const WallPlaneD& w = wf.p[k];
+        const float ds = (float)((x[0] - w.o[0]) * w.n[0] + (x[1] - w.o[1]) * w.n[1] + (x[2] - w.o[2]) * w.n[2]);
+        const bool inside = ds > 0.0f || (ds == 0.0f && !w.open);
+        const float nrm[3] = {(float)w.n[0], (float)w.n[1], (float)w.n[2]};
+        const float sg = ds < 0.0f ? -1.0f : 1.0f;
+        const float u[3] = {sg * nrm[0], sg * nrm[1], sg * nrm[2]};
+        wall_apply_f<EVF>(q, fabsf(ds), u, inside, nrm, F, U);
     }
 }
 

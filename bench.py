@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
-    ap.add_argument("--suite", default="melt", choices=["melt", "batched", "adjoint", "precision", "lj"],
+    ap.add_argument("--suite", default="melt", choices=["melt", "batched", "adjoint", "precision", "lj", "drivers"],
                     help="melt: the headline line; the others measure the remaining workloads")
     return ap.parse_args()
 

@@ -21,6 +21,10 @@ Each suite prints one JSON line:
   BrownianFlow, ConstantFlow U = 0.1 x, dt = 0.001, drag gamma = 10 diameter) --
   FP32-compensated against FP64 forces, energy and virial every 500 steps along the
   FP32-force Brownian trajectory.
+* ``drivers``: the drop-in drivers of the rows beside the headline path
+  (DPDGeneralWeight, HarmonicBarrier, LJ93 walls, velocity fields, ImageHarmonic)
+  on about 10^6 particles: time per call, algorithmic bytes, fraction of the
+  measured HBM bandwidth, and the oracle's host time on a sample.
 """
 
 from __future__ import annotations
@@ -325,8 +329,238 @@ def suite_precision(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- drop-in drivers of the widened rows
+def _sys_struct(N, ntypes, L, **ptrs):
+    from azplugins_gb300 import _lib
+
+    s = _lib.System()
+    s.N, s.ntypes = N, ntypes
+    for k, v in ptrs.items():
+        setattr(s, k, v)
+    for d in range(3):
+        s.box.L[d] = L[d]
+    return s
+
+
+def _forces_out(N, precision, torch):
+    from azplugins_gb300 import _lib
+
+    dt = torch.float32 if precision == "fp32" else torch.float64
+    force = torch.zeros((N, 4), dtype=dt, device="cuda")
+    vir = torch.zeros((6, N), dtype=dt, device="cuda")
+    out = _lib.Forces()
+    out.force, out.virial, out.virial_pitch = force.data_ptr(), vir.data_ptr(), N
+    out.precision = _lib.FP32 if precision == "fp32" else _lib.FP64
+    return force, vir, out
+
+
+def suite_drivers(args):
+    """Each drop-in driver of the rows beyond the headline path (DPDGeneralWeight,
+    HarmonicBarrier, walls, velocity field, ImageHarmonic) on about 10^6 particles:
+    CUDA-event time per call (inputs resident in HBM, 20 calls after 3 warm-up
+    calls; every call's inputs exceed the L2), algorithmic bytes per call (what the
+    caller's arrays and the outputs hold: the caller's FP64 position and velocity
+    records, list indices, outputs in the output precision; neighbour gathers are
+    cache traffic and not counted, as for the pair force) and the fraction of the
+    measured HBM copy bandwidth; beside each, the oracle's time on a sample of the
+    same inputs on the host cores (one thread), scaled to the full size."""
+    import torch
+
+    import azplugins_gb300 as az
+    from azplugins_gb300 import _compute, _lib
+    from bench import measured_peak
+    from oracle import oracle as orc
+
+    L_ = _lib.load()
+    peak, peak_kind = measured_peak()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rng = np.random.Generator(np.random.PCG64(17))
+    reps = max(1, min(20, args.steps))  # --steps 1: one timed call per driver (profiling runs)
+    rows = {}
+
+    def record(name, ms, nbytes, cpu_s, sample, **extra):
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        rows[name] = {"ms_per_call": ms, "bytes_per_call": nbytes, "achieved_gbs": gbs, "frac": gbs / peak,
+                      "cpu_oracle_ms_per_call_scaled": None if cpu_s is None else cpu_s * 1e3,
+                      "cpu_sample": sample, **extra}
+
+    def cpu_time(fn, frac):
+        t0 = time.perf_counter()
+        fn()
+        return (time.perf_counter() - t0) / frac
+
+    # -- a 2-type fluid of 2^20 particles at the melt's density, positions in FP64
+    N = 1 << 20
+    L = np.full(3, (N / 0.85) ** (1.0 / 3.0))
+    pos = (rng.uniform(-0.5, 0.5, size=(N, 3)) * L)
+    types = rng.integers(0, 2, size=N).astype(np.int32)
+    vel = rng.normal(size=(N, 3))
+    mass = rng.uniform(0.8, 1.2, size=N)
+    dpos = torch.zeros((N, 4), dtype=torch.float64, device="cuda")
+    dpos[:, :3] = torch.from_numpy(pos).cuda()
+    dpos.view(torch.int64)[:, 3] = torch.from_numpy(types.astype(np.int64)).cuda()
+    dvel = torch.zeros((N, 4), dtype=torch.float64, device="cuda")
+    dvel[:, :3] = torch.from_numpy(vel).cuda()
+    dvel[:, 3] = torch.from_numpy(mass).cuda()
+    sysd = _sys_struct(N, 2, L, pos=dpos.data_ptr(), vel=dvel.data_ptr())
+    pos4 = np.concatenate([pos, types[:, None].astype(float)], axis=1)
+    sample = N // 16
+    # HarmonicBarrier, planar at 0.3 L: read 32 B, write force and virial
+    bpar = torch.tensor([[50.0, 0.1], [200.0, -0.1]], dtype=torch.float64, device="cuda")
+    for prec in ("fp64", "fp32"):
+        force, vir, out = _forces_out(N, prec, torch)
+
+        def call():
+            _lib.check(L_.azp_harmonic_barrier_forces(ctypes.byref(sysd), 0, 0.3 * L[1], bpar.data_ptr(),
+                                                      ctypes.byref(out), stream), "barrier")
+
+        for _ in range(3):
+            call()
+        ms = _cuda_ms(call, reps)
+        wb = 8 if prec == "fp64" else 4
+        cpu = cpu_time(lambda: orc.harmonic_barrier(pos4[:sample], types[:sample], L, "planar", 0.3 * L[1],
+                                                    np.array([[50.0, 0.1], [200.0, -0.1]])), sample / N)
+        record(f"harmonic_barrier_{prec}", ms, N * (32 + 4 * wb + 6 * wb), cpu, f"{sample} particles")
+    # walls: LJ93 slit (two planes) and a cylinder, 2 types
+    pot = az.wall.LJ93(walls=[az.wall.Plane(origin=(0, -0.45 * L[1], 0), normal=(0, 1, 0)),
+                              az.wall.Plane(origin=(0, 0.45 * L[1], 0), normal=(0, -1, 0)),
+                              az.wall.Cylinder(radius=0.4 * L[0], axis=(0, 0, 1), inside=True)])
+    pot.params["A"] = dict(A=1.0, sigma=1.0, r_cut=3.0)
+    pot.params["B"] = dict(A=2.0, sigma=1.2, r_cut=3.0, r_extrap=0.5)
+    rec, rc, rx = pot._tables(["A", "B"])
+    walls, keep = pot._walls_struct()
+    wdev = [torch.from_numpy(np.ascontiguousarray(a).reshape(-1).copy()).cuda() for a in (rec, rc, rx)]
+    sp, cy, pl = pot._oracle_walls()
+    for prec in ("fp64", "fp32"):
+        force, vir, out = _forces_out(N, prec, torch)
+
+        def call():
+            _lib.check(L_.azp_wall_forces(ctypes.byref(sysd), pot.kind, ctypes.byref(walls), wdev[0].data_ptr(),
+                                          wdev[1].data_ptr(), wdev[2].data_ptr(), ctypes.byref(out), stream),
+                       "walls")
+
+        for _ in range(3):
+            call()
+        ms = _cuda_ms(call, reps)
+        wb = 8 if prec == "fp64" else 4
+        cpu = cpu_time(lambda: orc.wall_forces(pos4[:sample], types[:sample], "LJ93", rec, rc, rx, sp, cy, pl),
+                       sample / N)
+        record(f"walls_lj93_{prec}", ms, N * (32 + 4 * wb + 6 * wb), cpu, f"{sample} particles", walls="2 planes + 1 cylinder")
+    del keep
+    # velocity fields: 100 slabs along y; cylindrical 20 x 16 x 10 bins; both read pos and vel (64 B)
+    vel4 = np.concatenate([vel, mass[:, None]], axis=1)
+    for kind, nb, lo, hi in (("cartesian", (0, 100, 0), (0, -L[1] / 2, 0), (0, L[1] / 2, 0)),
+                             ("cylindrical", (20, 16, 10), (0, 0, -L[2] / 2), (L[0] / 2, 2 * np.pi, L[2] / 2))):
+        nb_ = np.ascontiguousarray(nb, dtype=np.uint32)
+        lo_, hi_ = np.ascontiguousarray(lo, dtype=np.float64), np.ascontiguousarray(hi, dtype=np.float64)
+        st = ctypes.c_int(0)
+        vf = L_.azp_vfield_create(_lib.BINNING_KINDS[kind], nb_.ctypes.data, lo_.ctypes.data, hi_.ctypes.data,
+                                  ctypes.byref(st))
+        _lib.check(st.value, "azp_vfield_create")
+        total = int(L_.azp_vfield_num_bins(vf))
+        vout = torch.zeros((total, 7), dtype=torch.float64, device="cuda")
+
+        def call():
+            _lib.check(L_.azp_vfield_compute(vf, ctypes.byref(sysd), None, 0, vout.data_ptr(), None, None, stream),
+                       "vfield")
+
+        for _ in range(3):
+            call()
+        ms = _cuda_ms(call, reps)
+        cpu = cpu_time(lambda: orc.velocity_field(pos4[:sample], vel4[:sample], L, kind, nb, lo, hi), sample / N)
+        L_.azp_vfield_destroy(vf)
+        record(f"velocity_field_{kind}", ms, N * 64, cpu, f"{sample} particles", bins=total)
+    # ImageHarmonic on 10,486 chains x 100 beads (random walks, 1 in 25 bonds longer than half the box)
+    n_chains, length = 10486, 100
+    Nc = n_chains * length
+    Lc = np.full(3, (Nc / 0.85) ** (1.0 / 3.0))
+    steps = rng.normal(size=(n_chains, length, 3))
+    steps *= 0.97 / np.linalg.norm(steps, axis=2, keepdims=True)
+    un = np.cumsum(steps, axis=1).reshape(Nc, 3) + np.repeat(rng.uniform(-0.5, 0.5, size=(n_chains, 3)) * Lc, length, 0)
+    img = np.floor((un + 0.5 * Lc) / Lc).astype(np.int32)
+    cpos = un - img * Lc
+    bonds = (np.arange(Nc).reshape(n_chains, length)[:, :-1].reshape(-1, 1) + np.array([0, 1])).astype(np.int64)
+    n, table, h = _compute.bond_table(Nc, bonds, np.zeros(len(bonds), dtype=np.int32))
+    cd = torch.zeros((Nc, 4), dtype=torch.float64, device="cuda")
+    cd[:, :3] = torch.from_numpy(cpos).cuda()
+    dimg = torch.from_numpy(img.reshape(-1)).cuda()
+    csys = _sys_struct(Nc, 1, Lc, pos=cd.data_ptr(), image=dimg.data_ptr())
+    n_d = torch.from_numpy(n.view(np.int32)).cuda()
+    t_d = torch.from_numpy(table.reshape(-1).view(np.int32)).cuda()
+    bp = np.zeros(8)
+    bp[:2] = [30.0, 1.0]
+    bp_d = torch.from_numpy(bp).cuda()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nbm = float(n.mean())
+    for prec in ("fp64", "fp32"):
+        force, vir, out = _forces_out(Nc, prec, torch)
+
+        def call():
+            _lib.check(L_.azp_bond_forces(ctypes.byref(csys), n_d.data_ptr(), t_d.data_ptr(), h, 2, bp_d.data_ptr(), 1,
+                                          ctypes.byref(out), err.data_ptr(), stream), "image bond")
+
+        for _ in range(3):
+            call()
+        ms = _cuda_ms(call, reps)
+        wb = 8 if prec == "fp64" else 4
+        cs = Nc // 16
+        cb = bonds[(bonds < cs).all(axis=1)]
+        cpu = cpu_time(lambda: orc.image_bond_forces(np.concatenate([cpos[:cs], np.zeros((cs, 1))], axis=1), img[:cs],
+                                                     Lc, cb, np.zeros(len(cb), dtype=np.int32), "ImageHarmonic",
+                                                     bp[None]), cs / Nc)
+        # own position and image, bond count and table; force and virial accumulated (read + write)
+        record(f"image_harmonic_{prec}", ms, int(Nc * (32 + 12 + 4 + 8 * nbm + 2 * 4 * wb + 2 * 6 * wb)), cpu,
+               f"{cs} particles", bonds_per_particle=nbm)
+    # DPDGeneralWeight at density 3, r_cut 1, buffer 0.3, 2 types, thermostat on
+    Nd = 1 << 20
+    Ld = np.full(3, (Nd / 3.0) ** (1.0 / 3.0))
+    snap = az.Snapshot(Nd)
+    snap.particles.types = ["A", "B"]
+    snap.particles.position = rng.uniform(-0.5, 0.5, size=(Nd, 3)) * Ld
+    snap.particles.typeid = rng.integers(0, 2, size=Nd).astype(np.int32)
+    snap.particles.velocity = rng.normal(size=(Nd, 3))
+    snap.particles.mass = np.ones(Nd)
+    snap.configuration.box = [*Ld, 0, 0, 0]
+    dpd = az.pair.DPDGeneralWeight(nlist=az.nlist.Cell(buffer=0.3), kT=1.0, default_r_cut=1.0)
+    dpd.params[("A", "A")] = dict(A=25.0, gamma=4.5, s=0.5)
+    dpd.params[("A", "B")] = dict(A=30.0, gamma=4.5, s=1.0)
+    dpd.params[("B", "B")] = dict(A=25.0, gamma=4.5, s=2.0)
+    drec, drc, _ = dpd._tables(["A", "B"])
+    ppos = _compute.device_positions(snap)
+    pvel = torch.zeros((Nd, 4), dtype=torch.float64, device="cuda")
+    pvel[:, :3] = torch.from_numpy(snap.particles.velocity).cuda()
+    pvel[:, 3] = 1.0
+    tags = torch.arange(Nd, dtype=torch.int32, device="cuda")
+    dsys = _compute.make_system(snap, ppos, vel=pvel.data_ptr(), tag=tags.data_ptr())
+    nl = _compute.NeighborList(Nd, 2, drc, 0.3, tpp=4)
+    nl.build(dsys)
+    counts, _ = nl.to_csr()
+    nbar = float(np.diff(counts).mean())
+    dparams = torch.from_numpy(drec.reshape(-1).copy()).cuda()
+    drc_d = torch.from_numpy(drc.reshape(-1).copy()).cuda()
+    for prec, tpp in (("fp64", 4), ("fp32", 1), ("fp32", 2), ("fp32", 4)):
+        force, vir, out = _forces_out(Nd, prec, torch)
+        _lib.check(L_.azp_nlist_set_tpp(nl.handle, tpp), "azp_nlist_set_tpp")
+
+        def call():
+            _lib.check(L_.azp_dpd_forces(ctypes.byref(dsys), nl.handle, dparams.data_ptr(), drc_d.data_ptr(), 1.0, 0.01,
+                                         77, 5, ctypes.byref(out), stream), "dpd")
+
+        for _ in range(3):
+            call()
+        ms = _cuda_ms(call, reps)
+        wb = 8 if prec == "fp64" else 4
+        record(f"dpd_{prec}_tpp{tpp}", ms, int(Nd * (32 + 32 + 4 + 4 + 4 * nbar + 4 * wb + 6 * wb)), None, None,
+               mean_neighbours=nbar, density=3.0, pairs_per_s=float(np.diff(counts).sum()) / (ms * 1e-3))
+    nl.close()
+    line = {"suite": "drivers", "n_particles": N, "peak_gbs": peak, "peak_kind": peak_kind, "reps": reps,
+            "drivers": rows}
+    print(json.dumps(line), flush=True)
+
+
 def run(args):
     import torch
 
     torch.cuda.set_device(0)
-    {"lj": suite_lj, "batched": suite_batched, "adjoint": suite_adjoint, "precision": suite_precision}[args.suite](args)
+    {"lj": suite_lj, "batched": suite_batched, "adjoint": suite_adjoint, "precision": suite_precision,
+     "drivers": suite_drivers}[args.suite](args)

@@ -266,7 +266,8 @@ AZP_API int azp_dpd_forces(const azp_system* sys, azp_nlist* nl, const double* p
  * A location that fails the evaluator's valid(box) -- planar: -Ly/2 <= H < Ly/2;
  * spherical: R >= 0 and 2R <= each edge -- returns AZP_ERR_INVALID with
  * "Barrier position is invalid" in azp_last_error, before any device work.
- * Arithmetic FP64 in both output precisions. */
+ * FP64 output: FP64 arithmetic. FP32 output: FP32 arithmetic after the FP64
+ * wrap and the cancelling difference (y - c, or r^2 - c^2). */
 enum azp_barrier_geometry { AZP_BARRIER_PLANAR = 0, AZP_BARRIER_SPHERICAL = 1 };
 AZP_API int azp_harmonic_barrier_forces(const azp_system* sys, int geometry, double location, const double* params,
                                         const azp_forces* out, void* stream);
@@ -286,7 +287,9 @@ AZP_API int azp_harmonic_barrier_forces(const azp_system* sys, int geometry, dou
  * direction (+x; the first normal of the axis).
  * params: device [ntypes][4] records (azp_params_wall_*); r_cut, r_extrap: device
  * [ntypes]. OVERWRITES out->force (fx, fy, fz, energy) and out->virial
- * (F_a x_b, may be NULL). Arithmetic FP64 in both output precisions. */
+ * (F_a x_b, may be NULL). FP64 output: FP64 arithmetic. FP32 output: FP32
+ * arithmetic except x - origin and R^2 - r^2 (FP64), so distances keep FP32
+ * relative accuracy near a surface. */
 enum azp_wall_kind { AZP_WALL_LJ93 = 0, AZP_WALL_COLLOID = 1 };
 #define AZP_WALL_MAX_SPHERES 20
 #define AZP_WALL_MAX_CYLINDERS 20

@@ -6,7 +6,7 @@
   there; the FP64 values also equal the oracle's bit for bit).
 * The drop-in driver azp_harmonic_barrier_forces against the oracle on a
   three-type system with particles drifted outside the box: FP64 bit-identical,
-  FP32 output the FP64 value rounded once; the virial written as zeros.
+  FP32 (FP32 arithmetic) within 1e-6 norm-wise; the virial written as zeros.
 * The resident engine with the barrier in the integrator's forces (fused into
   the step kernel) against the oracle's HOOMD-order MD loop, Langevin with a
   ramped planar barrier and Brownian with a spherical one: unwrapped positions
@@ -149,8 +149,9 @@ def test_driver_matches_oracle(orc, geometry, location):
             np.testing.assert_array_equal(f[:, :3], F)
             np.testing.assert_array_equal(f[:, 3], U)
         else:
-            np.testing.assert_array_equal(f[:, :3], F.astype(np.float32))
-            np.testing.assert_array_equal(f[:, 3], U.astype(np.float32))
+            # FP32 arithmetic after the FP64 wrap and cancelling difference
+            assert force_error(f, F) < 1e-6
+            assert np.abs(f[:, 3] - U).max() <= 1e-6 * np.abs(U).max()
 
 
 def _barrier_run(orc, precision, method, geometry, location, oracle_location, steps, seed, k=(5.0, 10.0)):

@@ -7,7 +7,7 @@
 * The drop-in driver azp_wall_forces against the oracle with every geometry at
   once (inside and outside spheres, tilted cylinders, planes; standard and
   extrapolated types): FP64 1e-12 (LJ93) / 1e-11 (Colloid) norm-wise with
-  energies and virials, FP32 output within 1e-6.
+  energies and virials, FP32 (FP32 arithmetic) within 1e-5.
 * The resident engine with the walls in the integrator's forces (fused into the
   step kernel) against the oracle's MD loop: a Lennard-Jones fluid in a slit
   between two LJ93 planes (Langevin) and in a Colloid-walled cylindrical pore
@@ -108,9 +108,10 @@ def test_driver_matches_oracle(orc, name):
     walls, keep = pot._walls_struct()
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     # FP64: the Colloid form subtracts two large terms near the surface, so FMA
-    # contraction differences show at 1e-12; LJ93 stays within 1e-12
+    # contraction differences show at 1e-12; LJ93 stays within 1e-12. FP32: FP32
+    # arithmetic on FP64 distances (the pair driver's FP32 bound)
     tol64 = 1e-12 if name == "LJ93" else 1e-11
-    for prec, dt, tol in ((_lib.FP64, torch.float64, tol64), (_lib.FP32, torch.float32, 1e-6)):
+    for prec, dt, tol in ((_lib.FP64, torch.float64, tol64), (_lib.FP32, torch.float32, 1e-5)):
         force = torch.full((N, 4), float("nan"), dtype=dt, device="cuda")
         vir = torch.full((6, N), float("nan"), dtype=dt, device="cuda")
         out = _lib.Forces()
