@@ -37,9 +37,6 @@ def split_forces(integ):
     if found[1] and found[1][0]._name == "ImageHarmonic":
         raise NotImplementedError("ImageHarmonic runs through the drop-in driver (azp_bond_forces); "
                                   "the resident engine does not take it")
-    if pairs and pairs[0]._name == "DPDGeneralWeight":
-        raise NotImplementedError("DPDGeneralWeight runs through the drop-in driver (azp_dpd_forces); "
-                                  "the resident engine does not take it")
     return tuple(x[0] if x else None for x in found)
 
 
@@ -58,7 +55,7 @@ class Engine:
         if pair is not None:
             parts += [type(pair).__name__, pair.mode, sorted(pair.params.items()), sorted(pair.r_cut.items()),
                       pair.r_cut.default, sorted(pair.r_on.items()), pair.r_on.default, pair.nlist.buffer,
-                      pair.nlist.exclusions]
+                      pair.nlist.exclusions, getattr(pair, "kT", None)]
         if bond is not None:
             parts += [type(bond).__name__, sorted((k, sorted(v.items())) for k, v in bond.params.items())]
         if barrier is not None:
@@ -101,6 +98,10 @@ class Engine:
             c.r_on = arr(ro.reshape(-1))
             c.r_buff = pair.nlist.buffer
             c.exclude_bonds = int(pair.nlist.exclude_bonds)
+            if pair._name == "DPDGeneralWeight":
+                if isinstance(m, BrownianFlow):
+                    raise NotImplementedError("DPDGeneralWeight needs velocities: use ConstantVolume or LangevinFlow")
+                c.dpd_kT = float(pair.kT)
         else:
             c.pair_kind = -1
             c.r_buff = 0.4

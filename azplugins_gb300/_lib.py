@@ -145,6 +145,7 @@ class MDConfig(ctypes.Structure):
         ("wall_params", ctypes.c_void_p),
         ("wall_r_cut", ctypes.c_void_p),
         ("wall_r_extrap", ctypes.c_void_p),
+        ("dpd_kT", ctypes.c_double),
     ]
 
 

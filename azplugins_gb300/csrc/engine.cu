@@ -30,6 +30,7 @@ int launch_md_step(int pair_kind, int bond_kind, int precision, int integ, const
     case AZP_PAIR_EXPANDED_YUKAWA: return launch_md_eyuk(bond_kind, precision, integ, a, s);
     case AZP_PAIR_HERTZ: return launch_md_hertz(bond_kind, precision, integ, a, s);
     case AZP_PAIR_COLLOID: return launch_md_colloid(bond_kind, precision, integ, a, s);
+    case AZP_PAIR_DPD_GENERAL_WEIGHT: return launch_md_dpd(bond_kind, precision, integ, a, s);
     default: return AZP_ERR_INVALID;
     }
 }
@@ -228,6 +229,19 @@ __global__ void k_md_step1_fx(uint4* __restrict__ fix, uint4* __restrict__ lo, c
         if (bad) atomicOr(&flags[1], AZP_EBIT_NONFINITE);
     }
     if (__any_sync(0xffffffffu, want) && (threadIdx.x & 31) == 0) atomicOr(&flags[0], 1u);
+}
+
+// DPD: the velocities at a step's start, read for the neighbours while their
+// owners update them in the step (FP64: (v, mass); FP32-force: the leading
+// floats (v, 1/m))
+__global__ void k_dpd_vel_snapshot(const double4_32a* __restrict__ vel, uint32_t N, int fx, void* __restrict__ out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    if (fx)
+        reinterpret_cast<float4*>(out)[i] = reinterpret_cast<const VelFF*>(vel)[i].h;
+    else
+        reinterpret_cast<double4_32a*>(out)[i] = vel[i];
 }
 
 // FP32-force mode: FP64 state (k_load_state's layout) -> fixed words, float-float
@@ -530,6 +544,9 @@ struct azp_md {
     WallField* d_walls = nullptr;
     double* d_wall_tab = nullptr;
     float wall_tol = 0.0f;
+    // DPD: kT of the thermostat and the step's velocity snapshot
+    double dpd_kT = 0.0;
+    double* d_dvel = nullptr;
     // control
     uint32_t* flags = nullptr;  // [0] rebuild request [1] error bits [2] builds [3] max count [4] ticket
     unsigned long long* d_ts = nullptr;
@@ -596,7 +613,7 @@ void free_all(azp_md* m)
                     m->d_bond_params, m->d_pair_table, m->d_gamma, m->d_noise, m->flags, m->d_ts, m->out_force, m->out_virial,
                     m->partials, m->thermo, m->tmp4, m->tmpd, m->snap_pos, m->snap_vel, m->snap_acc,
                     m->snap_img, m->snap_diam, m->st_pos, m->st_vel, m->st_acc, m->st_img, m->st_diam,
-                    m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab};
+                    m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab, m->d_dvel};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -689,6 +706,7 @@ MDArgs base_args(azp_md* m)
     a.walls = m->d_walls;
     a.wall_tab = m->d_wall_tab;
     a.wall_tol = m->wall_tol;
+    a.dvel = m->d_dvel;
     a.flowf.kind = m->flow.kind;
     if (m->flow.kind == AZP_FLOW_PARABOLIC) {
         a.flowf.a = (float)m->flow.a;
@@ -759,6 +777,18 @@ int enqueue_rebuild(azp_md* m, cudaStream_t s, const uint32_t* gate)
     return AZP_OK;
 }
 
+// the step kernel, preceded for DPD by the velocity snapshot it reads
+int md_launch(azp_md* m, int integ, const MDArgs& a, cudaStream_t s)
+{
+    if (m->pair_kind == AZP_PAIR_DPD_GENERAL_WEIGHT) {
+        k_dpd_vel_snapshot<<<blocks_for(m->N, 256), 256, 0, s>>>(m->vel, m->N, m->precision == AZP_FP32 ? 1 : 0,
+                                                                 m->d_dvel);
+        AZP_CHECK_LAUNCH("k_dpd_vel_snapshot");
+        m->launches += 1;
+    }
+    return launch_md_step(m->pair_kind, m->bond_kind, m->precision, integ, a, s);
+}
+
 int enqueue_step(azp_md* m, int integ, int next, int out, cudaStream_t s, int set_cond,
                  cudaGraphConditionalHandle h)
 {
@@ -767,7 +797,7 @@ int enqueue_step(azp_md* m, int integ, int next, int out, cudaStream_t s, int se
     a.out = out;
     a.set_cond = set_cond;
     a.next_cond = h;
-    const int st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, integ, a, s);
+    const int st = md_launch(m, integ, a, s);
     m->launches += 1;
     return st;
 }
@@ -850,16 +880,25 @@ int build_pair_graph(azp_md* m, int cur0, int integ, cudaGraphExec_t* out)
             st = record_cuda_error(e2, "capture step");
             break;
         }
-        // find the node just added: the one that depends on cnode
-        size_t nd = 0;
-        AZP_CUDA_TRY(cudaGraphNodeGetDependentNodes(cnode, nullptr, nullptr, &nd));
-        std::vector<cudaGraphNode_t> deps(nd);
-        AZP_CUDA_TRY(cudaGraphNodeGetDependentNodes(cnode, deps.data(), nullptr, &nd));
-        if (nd != 1) {
+        // the captured nodes form one chain after cnode (DPD: snapshot -> step);
+        // the next conditional depends on its last node
+        cudaGraphNode_t tail = cnode;
+        for (int hop = 0; hop < 8; ++hop) {
+            size_t nd = 0;
+            AZP_CUDA_TRY(cudaGraphNodeGetDependentNodes(tail, nullptr, nullptr, &nd));
+            if (nd == 0) break;
+            if (nd != 1) {
+                st = AZP_ERR_CUDA;
+                break;
+            }
+            AZP_CUDA_TRY(cudaGraphNodeGetDependentNodes(tail, &tail, nullptr, &nd));
+        }
+        if (st) break;
+        if (tail == cnode) {
             st = AZP_ERR_CUDA;
             break;
         }
-        prev = deps[0];
+        prev = tail;
         m->cur ^= 1;
     }
     m->cur = saved_cur;
@@ -956,7 +995,16 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     if (c->precision != AZP_FP64 && c->precision != AZP_FP32) return fail(AZP_ERR_INVALID, nullptr);
     if (c->method != AZP_METHOD_LANGEVIN_FLOW && c->method != AZP_METHOD_BROWNIAN_FLOW)
         return fail(AZP_ERR_INVALID, nullptr);
-    if (c->pair_kind >= AZP_PAIR_NUM_KINDS || c->bond_kind >= AZP_BOND_NUM_KINDS) return fail(AZP_ERR_INVALID, nullptr);
+    if ((c->pair_kind >= AZP_PAIR_NUM_KINDS && c->pair_kind != AZP_PAIR_DPD_GENERAL_WEIGHT) ||
+        c->bond_kind >= AZP_BOND_NUM_KINDS)
+        return fail(AZP_ERR_INVALID, nullptr);
+    // the DPD thermostat acts on velocities: Langevin-type methods only (the
+    // noiseless, drag-free Langevin step is HOOMD's ConstantVolume)
+    if (c->pair_kind == AZP_PAIR_DPD_GENERAL_WEIGHT &&
+        (c->method != AZP_METHOD_LANGEVIN_FLOW || !(c->dpd_kT >= 0.0) || c->shift_mode != AZP_MODE_NONE))
+        return fail(record_error(AZP_ERR_UNSUPPORTED, "azp_md_create: DPD needs a Langevin-type method, kT >= 0 "
+                                                      "and mode none"),
+                    nullptr);
     if (!(c->dt > 0.0)) return fail(AZP_ERR_INVALID, nullptr);
     if (!c->use_lambda && !c->gamma) return fail(AZP_ERR_INVALID, nullptr);
     azp_md* m = new (std::nothrow) azp_md();
@@ -1052,6 +1100,7 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     ALLOC(m->thermo, 8);
     ALLOC(m->d_gamma, c->ntypes);
     ALLOC(m->d_noise, c->ntypes);
+    if (c->pair_kind == AZP_PAIR_DPD_GENERAL_WEIGHT) ALLOC(m->d_dvel, (size_t)4 * N);
     CTRY(cudaMemset(m->flags, 0, sizeof(uint32_t) * 8));
     CTRY(cudaMemcpy(m->d_gamma, m->gamma.data(), sizeof(double) * c->ntypes, cudaMemcpyHostToDevice));
     {
@@ -1065,10 +1114,31 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     }
     // pair table + list thresholds + cell grid
     if (m->pair_kind >= 0) {
-        std::vector<double> table((size_t)nt2 * PAIR_TBL);
-        st = build_pair_table(m->pair_kind, m->pair_params.data(), m->r_cut.data(), m->r_on.data(), m->shift_mode,
-                              c->ntypes, table.data());
-        if (st) return fail(st, m);
+        std::vector<double> table((size_t)nt2 * PAIR_TBL, 0.0);
+        if (m->pair_kind == AZP_PAIR_DPD_GENERAL_WEIGHT) {
+            // DpdEngine record: 1/r_cut, r_cut, A, gamma, s/2, sqrt(6 kT gamma / dt);
+            // cut record: r_cut^2 (src/DPDPairEvaluatorGeneralWeight.h:165-255)
+            m->dpd_kT = c->dpd_kT;
+            for (uint32_t t = 0; t < nt2; ++t) {
+                double* rec = &table[(size_t)t * PAIR_TBL];
+                const double* p = &m->pair_params[(size_t)t * AZP_PAIR_PARAM_DOUBLES];
+                const double rc = m->r_cut[t];
+                if (rc > 0.0) {
+                    const double rcinv = 1.0 / std::sqrt(rc * rc);
+                    rec[0] = rcinv;
+                    rec[1] = 1.0 / rcinv;
+                    rec[2] = p[0];
+                    rec[3] = p[1];
+                    rec[4] = 0.5 * p[2];
+                    rec[5] = std::sqrt(6.0 * c->dpd_kT * p[1] / c->dt);
+                    rec[PAIR_REC] = rc * rc;
+                }
+            }
+        } else {
+            st = build_pair_table(m->pair_kind, m->pair_params.data(), m->r_cut.data(), m->r_on.data(), m->shift_mode,
+                                  c->ntypes, table.data());
+            if (st) return fail(st, m);
+        }
         ALLOC(m->d_pair_table, table.size());
         CTRY(cudaMemcpy(m->d_pair_table, table.data(), sizeof(double) * table.size(), cudaMemcpyHostToDevice));
         m->pair_table_host = table;
@@ -1261,7 +1331,7 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         // HOOMD starts a run from a = F / m when no acceleration is known
         MDArgs a = base_args(m);
         a.out = 1;
-        st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
+        st = md_launch(m, MD_FORCES_ONLY, a, s);
         if (st) return st;
         k_accel_from_force<<<blocks_for(N, 256), 256, 0, s>>>(m->out_force, m->vel, m->mass, m->accel, N);
         AZP_CHECK_LAUNCH("k_accel_from_force");
@@ -1402,7 +1472,7 @@ int azp_md_forces(azp_md* m, double* force, double* virial, int on_device, void*
     if (st) return st;
     MDArgs a = base_args(m);
     a.out = 1;
-    st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
+    st = md_launch(m, MD_FORCES_ONLY, a, s);
     if (st) return st;
     m->forces_valid = true;
     k_to_tag_order4<<<blocks_for(N, 256), 256, 0, s>>>(m->out_force, m->tag, N, m->tmp4);
@@ -1429,7 +1499,7 @@ int azp_md_thermo(azp_md* m, double* out, void* stream)
         if (st) return st;
         MDArgs a = base_args(m);
         a.out = 1;
-        st = launch_md_step(m->pair_kind, m->bond_kind, m->precision, MD_FORCES_ONLY, a, s);
+        st = md_launch(m, MD_FORCES_ONLY, a, s);
         if (st) return st;
         m->forces_valid = true;
     }

@@ -11,6 +11,7 @@
 
 #include "barrier.cuh"
 #include "engine.cuh"
+#include "philox.cuh"
 #include "evaluators.cuh"
 #include "pair.cuh"
 
@@ -51,6 +52,23 @@ template<> struct Acc<double> {
         u += 0.5 * e;
         if (vir) {
             const double h = 0.5 * fdr;
+            w[0] += h * dx * dx;
+            w[1] += h * dx * dy;
+            w[2] += h * dx * dz;
+            w[3] += h * dy * dy;
+            w[4] += h * dy * dz;
+            w[5] += h * dz * dz;
+        }
+    }
+    // force from fdr, virial from fvir (DPD: the conservative part only)
+    AZP_D void add_split(double dx, double dy, double dz, double fdr, double fvir, double e, bool vir)
+    {
+        fx += dx * fdr;
+        fy += dy * fdr;
+        fz += dz * fdr;
+        u += 0.5 * e;
+        if (vir) {
+            const double h = 0.5 * fvir;
             w[0] += h * dx * dx;
             w[1] += h * dx * dy;
             w[2] += h * dx * dz;
@@ -136,6 +154,23 @@ struct AccFx {
         if (out) {
             bu += 0.5f * e;
             const float h = 0.5f * fdr;
+            w[0] += h * dx * dx;
+            w[1] += h * dx * dy;
+            w[2] += h * dx * dz;
+            w[3] += h * dy * dy;
+            w[4] += h * dy * dz;
+            w[5] += h * dz * dz;
+        }
+    }
+    // force from fdr, virial from fvir (DPD: the conservative part only)
+    AZP_D void add_split(float dx, float dy, float dz, float fdr, float fvir, float e, bool out)
+    {
+        bx += dx * fdr;
+        by += dy * fdr;
+        bz += dz * fdr;
+        if (out) {
+            bu += 0.5f * e;
+            const float h = 0.5f * fvir;
             w[0] += h * dx * dx;
             w[1] += h * dx * dy;
             w[2] += h * dx * dz;
@@ -274,6 +309,60 @@ AZP_D bool displaced(const uint4& f, const uint4& fb, const float* sfix, float t
     return dx * dx + dy * dy + dz * dz > thresh2;
 }
 
+// ---------------------------------------------------------------- DPD in the step
+// The timestep whose forces a step evaluates (the DPD draw's timestep): a
+// Langevin step at t evaluates t + 1 (HOOMD computes the net force of t + 1
+// between the halves), a forces-only launch its own timestep.
+template<int INTEG> AZP_D unsigned long long force_timestep(const MDArgs& a)
+{
+    return *a.d_timestep + (INTEG == MD_INTEG_LANGEVIN ? 1ull : 0ull);
+}
+
+// alpha in (-1, 1) of the pair (tags ti, tj): the first 64-bit word of the
+// pair's Philox block, stream (AZP_RNG_DPD_GENERAL_WEIGHT, timestep, seed),
+// counter {0, min tag, max tag, 0}, as azp_dpd_forces draws it
+AZP_D void dpd_key(const MDArgs& a, unsigned long long ts, uint32_t& k0, uint32_t& k1)
+{
+    stream_key(AZP_RNG_DPD_GENERAL_WEIGHT, ts, a.seed, k0, k1);
+}
+
+AZP_D double dpd_weight_engine(double x, double h)
+{
+    if (h == 0.5) return sqrt(x);
+    if (h == 0.25) return sqrt(sqrt(x));
+    if (h == 1.0) return x;
+    return pow(x, h);
+}
+
+AZP_D float dpd_weight_engine_f(float x, float h)
+{
+    if (h == 0.5f) return sqrtf(x);
+    if (h == 0.25f) return sqrtf(sqrtf(x));
+    if (h == 1.0f) return x;
+    return powf(x, h);
+}
+
+// one pair in FP64: dx = x_i - x_j, dv = v_i - v_j; rec as in DpdEngine.
+// Returns false outside r_cut (rsq >= rcutsq).
+AZP_D bool dpd_term_fp64(const double* rec, double rcutsq, double dx, double dy, double dz, double dvx, double dvy,
+                         double dvz, uint32_t k0, uint32_t k1, uint32_t tgi, uint32_t tgj, double& fdr, double& fc,
+                         double& e)
+{
+    const double rs = rsq_exact(dx, dy, dz);
+    if (!(rs < rcutsq)) return false;
+    const double rcinv = rec[0], rc = rec[1], A = rec[2], gamma = rec[3];
+    const double rinv = 1.0 / sqrt(rs);
+    const double r = 1.0 / rinv;
+    const double dot = dx * dvx + dy * dvy + dz * dvz;
+    fc = A * (rinv - rcinv);
+    const double wR = dpd_weight_engine(fmax(1.0 - r * rcinv, 0.0), rec[4]) * rinv;
+    const Philox4 ph = philox4x32_10(0u, min(tgi, tgj), max(tgi, tgj), 0u, k0, k1);
+    const double alpha = -1.0 + 2.0 * open01(ph.v[0], ph.v[1]);
+    fdr = fc - gamma * wR * wR * dot + rec[5] * wR * alpha;
+    e = A * (rc - r) - 0.5 * A * rcinv * (rcutsq - rs);
+    return true;
+}
+
 // FP64 step: FP64 positions, forces and integration, the oracle's rounding for
 // every decision.
 template<class PE, class BE, typename R, int INTEG>
@@ -316,6 +405,13 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
             {
                 const double4_32a pi = a.pos[i];
                 const uint32_t ti = type_of(pi.w);
+                uint32_t k0 = 0, k1 = 0, tgi = 0;
+                double4_32a vi{};
+                if constexpr (std::is_same<PE, DpdEngine>::value) {
+                    dpd_key(a, force_timestep<INTEG>(a), k0, k1);
+                    tgi = a.tag[i];
+                    vi = reinterpret_cast<const double4_32a*>(a.dvel)[i];
+                }
                 for (uint32_t k = sub; k < n; k += tpp) {
                     const uint32_t j = a.nbrs[(size_t)k * a.N + i];
                     const double4_32a pj = a.pos[j];
@@ -326,6 +422,14 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
                     const uint32_t tp = ti * a.ntypes + type_of(pj.w);
                     const R* rec = s_rec + (size_t)tp * PAIR_TBL;
                     const R* cut = rec + PAIR_REC;
+                    if constexpr (std::is_same<PE, DpdEngine>::value) {
+                        const double4_32a vj = reinterpret_cast<const double4_32a*>(a.dvel)[j];
+                        double fdr, fc, e;
+                        if (dpd_term_fp64(rec, cut[0], dx, dy, dz, vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, k0, k1, tgi,
+                                          a.tag[j], fdr, fc, e))
+                            acc.add_split(dx, dy, dz, fdr, fc, e, vir);
+                        continue;
+                    }
                     if (!(rsq < cut[0]) || !PE::enabled(rec)) continue;
                     R fdr, e;
                     PE::eval(rec, rsq, fdr, e);
@@ -538,6 +642,51 @@ AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint3
     acc.add(dx, dy, dz, fdr, e, vir);
 }
 
+// DPD pair in the FP32-force step: FP32 on the exact fixed-point displacement,
+// FP64 from the full 64-bit positions within 0.2 % of r_cut^2 (the weight
+// (1 - r / r_cut)^(s/2) is steep there, and the cutoff decision is the oracle's);
+// velocities from the step's snapshot (float4: v, 1/m)
+AZP_D void pair_term_dpd_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j,
+                            const float* s_rec, const double* s_rc2, AccFx& acc, bool vir, const float4& vi,
+                            uint32_t tgi, uint32_t k0, uint32_t k1)
+{
+    const float dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
+    const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
+    const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
+    const float rs = dx * dx + dy * dy + dz * dz;
+    const uint32_t tp = fi.w * a.ntypes + fj.w;
+    const float* rec = s_rec + (size_t)tp * PAIR_TBL;
+    const float rc2 = rec[PAIR_REC];
+    if (!(rc2 > 0.0f) || rs >= rc2 * 1.000004f) return;
+    const float4 vj = reinterpret_cast<const float4*>(a.dvel)[j];
+    const uint32_t tgj = a.tag[j];
+    if (rs >= rc2 * 0.998f) {
+        const uint4 li = a.flo[i], lj = a.flo[j];
+        const double ddx = min_image1(fx_to_double(fx_join(fi.x, li.x), a.l64[0]) - fx_to_double(fx_join(fj.x, lj.x), a.l64[0]),
+                                      a.L[0], a.Linv[0]);
+        const double ddy = min_image1(fx_to_double(fx_join(fi.y, li.y), a.l64[1]) - fx_to_double(fx_join(fj.y, lj.y), a.l64[1]),
+                                      a.L[1], a.Linv[1]);
+        const double ddz = min_image1(fx_to_double(fx_join(fi.z, li.z), a.l64[2]) - fx_to_double(fx_join(fj.z, lj.z), a.l64[2]),
+                                      a.L[2], a.Linv[2]);
+        double fdr, fc, e;
+        if (dpd_term_fp64(a.pair_table + (size_t)tp * PAIR_TBL, s_rc2[tp], ddx, ddy, ddz, (double)(vi.x - vj.x),
+                          (double)(vi.y - vj.y), (double)(vi.z - vj.z), k0, k1, tgi, tgj, fdr, fc, e))
+            acc.add_split((float)ddx, (float)ddy, (float)ddz, (float)fdr, (float)fc, (float)e, vir);
+        return;
+    }
+    const float rcinv = rec[0], A = rec[2];
+    const float rinv = rsqrtf(rs);
+    const float r = rs * rinv;
+    const float dot = dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z);
+    const float fc = A * (rinv - rcinv);
+    const float wR = dpd_weight_engine_f(fmaxf(1.0f - r * rcinv, 0.0f), rec[4]) * rinv;
+    const Philox4 ph = philox4x32_10(0u, min(tgi, tgj), max(tgi, tgj), 0u, k0, k1);
+    const float alpha = -1.0f + 2.0f * open01f(ph.v[0]);
+    const float fdr = fc - rec[3] * wR * wR * dot + rec[5] * wR * alpha;
+    const float e = A * (rec[1] - r) - 0.5f * A * rcinv * (rc2 - rs);
+    acc.add_split(dx, dy, dz, fdr, fc, e, vir);
+}
+
 template<class BE>
 AZP_D void bond_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t btype, const float* s_bond,
                         AccFx& acc, bool vir)
@@ -648,19 +797,31 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
         if constexpr (!std::is_same<PE, NoPair>::value) {
             const uint32_t n = min(__ldg(a.counts + i), a.max_nn);
             const uint32_t* col = a.nbrs + i;
-            for (uint32_t k0 = sub; k0 < n; k0 += FX_BATCH * tpp) {
+            uint32_t k0 = 0, k1 = 0, tgi = 0;
+            float4 vi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if constexpr (std::is_same<PE, DpdEngine>::value) {
+                dpd_key(a, force_timestep<INTEG>(a), k0, k1);
+                tgi = __ldg(a.tag + i);
+                vi = reinterpret_cast<const float4*>(a.dvel)[i];
+            }
+            for (uint32_t kb = sub; kb < n; kb += FX_BATCH * tpp) {
                 uint32_t jj[FX_BATCH];
                 uint4 fj[FX_BATCH];
 #pragma unroll
                 for (int u = 0; u < FX_BATCH; ++u) {
-                    const uint32_t k = k0 + u * tpp;
+                    const uint32_t k = kb + u * tpp;
                     jj[u] = k < n ? __ldg(col + (size_t)k * a.N) : i;
                 }
 #pragma unroll
                 for (int u = 0; u < FX_BATCH; ++u) fj[u] = __ldg(a.fix + jj[u]);
 #pragma unroll
                 for (int u = 0; u < FX_BATCH; ++u)
-                    if (k0 + u * tpp < n) pair_term_fx<PE>(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir);
+                    if (kb + u * tpp < n) {
+                        if constexpr (std::is_same<PE, DpdEngine>::value)
+                            pair_term_dpd_fx(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir, vi, tgi, k0, k1);
+                        else
+                            pair_term_fx<PE>(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir);
+                    }
                 acc.commit(vir);
             }
         }
@@ -847,5 +1008,6 @@ int launch_md_plj(int bond_kind, int precision, int integ, const MDArgs& a, cuda
 int launch_md_eyuk(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s);
 int launch_md_hertz(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s);
 int launch_md_colloid(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s);
+int launch_md_dpd(int bond_kind, int precision, int integ, const MDArgs& a, cudaStream_t s);
 
 }  // namespace azp

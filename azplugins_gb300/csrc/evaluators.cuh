@@ -348,6 +348,22 @@ struct DoubleWellBond {
     AZP_D static bool eval_f(const float* q, float rsq, float& fdr, float& e) { return eval(q, rsq, fdr, e); }
 };
 
+// DPD with a general weight function inside the resident engine
+// (src/DPDPairEvaluatorGeneralWeight.h:165-255). The fused step evaluates it
+// in its own pair term (velocities and a per-pair Philox draw), not through
+// eval(); the kernel record, built by the engine on the host, holds
+// rec = {1/r_cut, r_cut, A, gamma, s/2, sigma_R = sqrt(6 kT gamma / dt), -, -}
+// and the cut record's r_cut^2.
+struct DpdEngine {
+    static constexpr int SHIFT_SLOT = 7;
+    template<typename R> AZP_HD static bool enabled(const R* rec) { return rec[1] > R(0); }
+    template<typename R> AZP_HD static void eval(const R*, R, R& fdr, R& e)
+    {
+        fdr = R(0);
+        e = R(0);
+    }
+};
+
 // Harmonic bond U = k/2 (r - r_0)^2 (HOOMD's EvaluatorBondHarmonic, which
 // src/ImagePotentialBond.h:144-152 applies to the image-unwrapped distance):
 // p = {k, r_0}. At r = 0 the force is set to 0 (its direction is undefined).

@@ -65,4 +65,16 @@ class BrownianFlow(_FlowMethod):
         self.force_cap = float(force_cap)
 
 
-__all__ = ["LangevinFlow", "BrownianFlow"]
+class ConstantVolume(LangevinFlow):
+    """Constant-volume, constant-energy integration (HOOMD ``md.methods.ConstantVolume``
+    without a thermostat): velocity Verlet, i.e. the Langevin step above with no
+    drag and no noise. A DPDGeneralWeight pair force thermostats it, as in
+    ``src/pytest/test_pair_dpd.py``."""
+
+    def __init__(self, filter):
+        from .flow import ConstantFlow
+
+        super().__init__(filter, kT=0.0, flow_field=ConstantFlow((0.0, 0.0, 0.0)), default_gamma=0.0, noiseless=True)
+
+
+__all__ = ["LangevinFlow", "BrownianFlow", "ConstantVolume"]

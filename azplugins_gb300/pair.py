@@ -114,7 +114,10 @@ class DPDGeneralWeight(Pair):
     The forces depend on the velocities, the timestep and the Simulation's seed:
     ``forces`` / ``energies`` / ``virials`` are evaluated by the drop-in driver
     (``azp_dpd_forces``) at the current state, timestep and integrator ``dt``.
-    The resident engine (``Simulation.run``) does not take this potential."""
+    ``Simulation.run`` advances it inside the resident engine's fused step with a
+    Langevin-type method (``methods.ConstantVolume`` for the plain DPD
+    thermostat): the forces of timestep t + 1 from the half-step velocities, the
+    same per-pair draws as the driver."""
 
     _name = "DPDGeneralWeight"
     _keys = ("A", "gamma", "s")

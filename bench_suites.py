@@ -24,7 +24,8 @@ Each suite prints one JSON line:
 * ``drivers``: the drop-in drivers of the rows beside the headline path
   (DPDGeneralWeight, HarmonicBarrier, LJ93 walls, velocity fields, ImageHarmonic)
   on about 10^6 particles: time per call, algorithmic bytes, fraction of the
-  measured HBM bandwidth, and the oracle's host time on a sample.
+  measured HBM bandwidth, and the oracle's host time on a sample; and the DPD
+  fluid advanced by the resident engine (ConstantVolume + DPDGeneralWeight).
 """
 
 from __future__ import annotations
@@ -534,8 +535,16 @@ def suite_drivers(args):
     dsys = _compute.make_system(snap, ppos, vel=pvel.data_ptr(), tag=tags.data_ptr())
     nl = _compute.NeighborList(Nd, 2, drc, 0.3, tpp=4)
     nl.build(dsys)
-    counts, _ = nl.to_csr()
+    counts, didx = nl.to_csr()
     nbar = float(np.diff(counts).mean())
+    # the oracle (OpenMP, all host cores) on the first 1/16 of the rows
+    Sd = Nd // 16
+    dcores = orc.set_threads(os.cpu_count() or 1)
+    dvel4 = np.concatenate([snap.particles.velocity, np.ones((Nd, 1))], axis=1)
+    dpos4 = np.concatenate([snap.particles.position, snap.particles.typeid[:, None].astype(float)], axis=1)
+    dcpu = cpu_time(lambda: orc.dpd_forces(dpos4, dvel4, snap.particles.typeid,
+                                           np.arange(Nd, dtype=np.uint32), 2, Ld, np.minimum(counts, counts[Sd]),
+                                           didx[:counts[Sd]], drec, drc * drc, 1.0, 0.01, 5, 77), Sd / Nd)
     dparams = torch.from_numpy(drec.reshape(-1).copy()).cuda()
     drc_d = torch.from_numpy(drc.reshape(-1).copy()).cuda()
     for prec, tpp in (("fp64", 4), ("fp32", 1), ("fp32", 2), ("fp32", 4)):
@@ -550,9 +559,38 @@ def suite_drivers(args):
             call()
         ms = _cuda_ms(call, reps)
         wb = 8 if prec == "fp64" else 4
-        record(f"dpd_{prec}_tpp{tpp}", ms, int(Nd * (32 + 32 + 4 + 4 + 4 * nbar + 4 * wb + 6 * wb)), None, None,
-               mean_neighbours=nbar, density=3.0, pairs_per_s=float(np.diff(counts).sum()) / (ms * 1e-3))
+        record(f"dpd_{prec}_tpp{tpp}", ms, int(Nd * (32 + 32 + 4 + 4 + 4 * nbar + 4 * wb + 6 * wb)), dcpu,
+               f"{Sd} particles' rows", cpu_cores=dcores, mean_neighbours=nbar, density=3.0,
+               pairs_per_s=float(np.diff(counts).sum()) / (ms * 1e-3))
     nl.close()
+    # the same fluid advanced by the resident engine: ConstantVolume + DPDGeneralWeight,
+    # one fused launch per step (forces of t + 1 at the half-step velocities, both
+    # velocity-Verlet halves) after a velocity snapshot; wall clock around run(K)
+    # with the device synchronised on both sides (one host check per run call).
+    # Bytes per particle and step: FP32 forces read and write the fixed-point words
+    # (2 x 16 B), the float-float velocity (2 x 32 B) and the snapshot (16 B written,
+    # 16 B read); FP64 the position (2 x 32 B), fixed words (16 B), velocity (2 x 32 B)
+    # and snapshot (2 x 32 B); both the list row (4 B count, 4 B per neighbour)
+    steps = 10 * reps
+    for prec in ("fp32", "fp64"):
+        pot = az.pair.DPDGeneralWeight(nlist=az.nlist.Cell(buffer=0.3), kT=1.0, default_r_cut=1.0)
+        pot.params[("A", "A")] = dict(A=25.0, gamma=4.5, s=0.5)
+        pot.params[("A", "B")] = dict(A=30.0, gamma=4.5, s=1.0)
+        pot.params[("B", "B")] = dict(A=25.0, gamma=4.5, s=2.0)
+        sim = az.Simulation(seed=5, precision=prec)
+        sim.create_state_from_snapshot(snap)
+        sim.operations.integrator = az.md.Integrator(dt=0.01, methods=[az.methods.ConstantVolume("all")],
+                                                     forces=[pot])
+        sim.run(20)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.run(steps)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / steps
+        per = (2 * 16 + 2 * 32 + 2 * 16) if prec == "fp32" else (2 * 32 + 16 + 2 * 32 + 2 * 32)
+        record(f"dpd_engine_step_{prec}", ms, int(Nd * (per + 4 + 4 * nbar)), None, None, steps=steps,
+               timesteps_per_s=1e3 / ms, pairs_per_s=float(np.diff(counts).sum()) / (ms * 1e-3), density=3.0)
+        sim.close()
     line = {"suite": "drivers", "n_particles": N, "peak_gbs": peak, "peak_kind": peak_kind, "reps": reps,
             "drivers": rows}
     print(json.dumps(line), flush=True)

@@ -76,8 +76,8 @@ enum azp_pair_kind {
     AZP_PAIR_EXPANDED_YUKAWA = 1,  /* PairEvaluatorExpandedYukawa */
     AZP_PAIR_HERTZ = 2,            /* PairEvaluatorHertz */
     AZP_PAIR_COLLOID = 3,          /* PairEvaluatorColloid */
-    AZP_PAIR_NUM_KINDS = 4,        /* kinds of azp_pair_forces and the engine */
-    AZP_PAIR_DPD_GENERAL_WEIGHT = 4 /* DPDPairEvaluatorGeneralWeight: azp_dpd_forces only */
+    AZP_PAIR_NUM_KINDS = 4,        /* kinds of azp_pair_forces */
+    AZP_PAIR_DPD_GENERAL_WEIGHT = 4 /* DPDPairEvaluatorGeneralWeight: azp_dpd_forces and the engine */
 };
 enum azp_bond_kind {
     AZP_BOND_QUARTIC = 0,          /* BondEvaluatorQuartic */
@@ -441,6 +441,10 @@ typedef struct {
     const double* wall_params;  /* host [ntypes][4] records */
     const double* wall_r_cut;   /* host [ntypes] */
     const double* wall_r_extrap; /* host [ntypes] */
+    /* pair_kind AZP_PAIR_DPD_GENERAL_WEIGHT: the thermostat temperature (the
+     * dissipative and random terms, sqrt(6 kT gamma / dt)); needs the Langevin
+     * method (with default gamma 0 and noiseless: HOOMD's ConstantVolume) */
+    double dpd_kT;
 } azp_md_config;
 
 AZP_API azp_md* azp_md_create(const azp_md_config* cfg, int* status);

@@ -531,7 +531,15 @@ class OracleMD:
         F = np.zeros((N, 3))
         U = np.zeros(N)
         W = np.zeros((N, 6))
-        if self.pair is not None:
+        if self.pair is not None and self.pair["name"] == "DPDGeneralWeight":
+            # velocity-dependent: the current (half-step) velocities, the draw of
+            # the timestep the positions belong to
+            self._check_build()
+            rc = np.asarray(self.pair["rcut"], dtype=np.float64)
+            t = self.timestep if timestep is None else timestep
+            F, U, W = dpd_forces(s["pos4"], s["vel4"], s["types"], s["tags"], self.ntypes, s["L"], *self.nlist_csr,
+                                 self.pair["params"], rc * rc, self.pair["kT"], self.dt, t, self.seed)
+        elif self.pair is not None:
             self._check_build()
             rc = np.asarray(self.pair["rcut"], dtype=np.float64)
             ron = self.pair.get("ron")

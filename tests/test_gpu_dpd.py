@@ -168,3 +168,81 @@ def test_dpd_thermostat_holds_temperature():
             temps.append(float((vv * vv).sum()) / (3 * N - 3))
     nl.close()
     assert np.mean(temps) == pytest.approx(kT, rel=0.1)
+
+
+# ---------------------------------------------------------------- DPD inside the resident engine
+def _engine_dpd_run(orc, precision, steps=20, seed=77):
+    snap = _dpd_system(N=3000, seed=54)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    pot = _dpd_pot(kT=1.5)
+    sim = az.Simulation(seed=seed, precision=precision)
+    sim.create_state_from_snapshot(snap)
+    sim.operations.integrator = az.md.Integrator(dt=0.01, methods=[az.methods.ConstantVolume("all")], forces=[pot])
+    sim.run(steps // 2)
+    sim.run(steps - steps // 2)
+    from helpers import oracle_system
+
+    rec, rc, _ = pot._tables(list(snap.particles.types))
+    md = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
+                      pair=dict(name="DPDGeneralWeight", params=rec, rcut=rc, kT=1.5), method="langevin",
+                      gamma=[0.0, 0.0], kT=0.0, dt=0.01, seed=seed, r_buff=0.3, noiseless=True)
+    md.run(steps)
+    return sim, md, box_of(snap)
+
+
+@pytest.mark.parametrize("precision,ptol,vtol", [("fp64", 1e-9, 1e-8), ("fp32", 2e-4, 2e-3)])
+def test_engine_dpd_matches_oracle(orc, precision, ptol, vtol):
+    """ConstantVolume + DPDGeneralWeight advanced by the fused engine step against
+    the oracle's HOOMD-order loop (forces of t + 1 at the half-step velocities,
+    the same per-pair draws): positions, velocities, and the forces and energy
+    the engine reports at the end."""
+    sim, md, L = _engine_dpd_run(orc, precision)
+    snap = sim.state.get_snapshot()
+    out = snap.particles
+    d = out.position - md.s["pos4"][:, :3]
+    d -= L * np.rint(d / L)
+    assert np.abs(d).max() < ptol
+    assert np.abs(out.velocity - md.s["vel4"][:, :3]).max() < vtol
+    # forces and energy at the engine's own end state (same timestep, same draws):
+    # the weight (1 - r/r_cut)^(s/2) has an unbounded slope at r_cut, so two
+    # trajectories that differ by rounding are not compared force by force
+    from helpers import oracle_system
+
+    system = oracle_system(snap)
+    system["timestep"] = sim.timestep
+    rec, rc, _ = _dpd_pot(kT=1.5)._tables(list(snap.particles.types))
+    at_end = orc.OracleMD(system, pair=dict(name="DPDGeneralWeight", params=rec, rcut=rc, kT=1.5), method="langevin",
+                          gamma=[0.0, 0.0], kT=0.0, dt=0.01, seed=77, r_buff=0.3, noiseless=True)
+    f, _ = sim._engine.forces()
+    F, U, _ = at_end.forces()
+    assert force_error(f, F) < (1e-12 if precision == "fp64" else 1e-5)
+    assert rel(sim.thermo()["potential_energy"], U.sum()) < (1e-12 if precision == "fp64" else 1e-5)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_engine_dpd_thermostat_holds_temperature(precision):
+    """src/pytest/test_pair_dpd.py through Simulation.run: 1000 particles on a
+    10^3 lattice of spacing 0.6 at kT = 1.5, DPD (A = 0, gamma = 4.5, s = 0.5,
+    r_cut 1) with ConstantVolume, dt = 0.01: the kinetic temperature settles at kT."""
+    n, a, kT = 10, 0.6, 1.5
+    g = (np.arange(n) - 0.5 * (n - 1)) * a
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    N = n ** 3
+    snap = az.Snapshot(N)
+    snap.particles.position = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    snap.configuration.box = [n * a] * 3 + [0.0, 0.0, 0.0]
+    rng = np.random.Generator(np.random.PCG64(55))
+    v = rng.normal(0.0, np.sqrt(kT), size=(N, 3))
+    snap.particles.velocity = v - v.mean(axis=0)
+    pot = az.pair.DPDGeneralWeight(nlist=az.nlist.Cell(buffer=0.4), kT=kT, default_r_cut=1.0)
+    pot.params[("A", "A")] = dict(A=0.0, gamma=4.5, s=0.5)
+    sim = az.Simulation(seed=9, precision=precision)
+    sim.create_state_from_snapshot(snap)
+    sim.operations.integrator = az.md.Integrator(dt=0.01, methods=[az.methods.ConstantVolume("all")], forces=[pot])
+    sim.run(10)
+    temps = []
+    for _ in range(10):
+        sim.run(10)
+        vv = sim.state.get_snapshot().particles.velocity
+        temps.append(float((vv * vv).sum()) / (3 * N - 3))
+    assert np.mean(temps) == pytest.approx(kT, rel=0.1)
