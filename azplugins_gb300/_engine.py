@@ -33,10 +33,6 @@ def split_forces(integ):
         raise NotImplementedError(f"unsupported force objects: {other}")
     if any(len(x) > 1 for x in found):
         raise NotImplementedError("the engine advances at most one pair, one bond, one barrier and one wall potential")
-    pairs = found[0]
-    if found[1] and found[1][0]._name == "ImageHarmonic":
-        raise NotImplementedError("ImageHarmonic runs through the drop-in driver (azp_bond_forces); "
-                                  "the resident engine does not take it")
     return tuple(x[0] if x else None for x in found)
 
 

@@ -96,8 +96,9 @@ class ImageHarmonic(Bond):
     """Harmonic bond U = k/2 (r - r0)^2 on the image-unwrapped distance
     (``src/ImagePotentialBond.h``, ``src/bond.py:160-192``): the bond vector is
     (x_j + img_j L) - (x_i + img_i L), so a bond may span more than half the box.
-    Evaluated by the drop-in driver (``azp_bond_forces``, reading the images);
-    the resident engine (``Simulation.run``) does not take it."""
+    Evaluated by the drop-in driver (``azp_bond_forces``, reading the images) and
+    inside the resident engine's step (``Simulation.run``), which measures each
+    bond from the image counts of the step's start."""
 
     _name = "ImageHarmonic"
     _keys = ("k", "r0")

@@ -231,17 +231,23 @@ __global__ void k_md_step1_fx(uint4* __restrict__ fix, uint4* __restrict__ lo, c
     if (__any_sync(0xffffffffu, want) && (threadIdx.x & 31) == 0) atomicOr(&flags[0], 1u);
 }
 
-// DPD: the velocities at a step's start, read for the neighbours while their
-// owners update them in the step (FP64: (v, mass); FP32-force: the leading
-// floats (v, 1/m))
-__global__ void k_dpd_vel_snapshot(const double4_32a* __restrict__ vel, uint32_t N, int fx, void* __restrict__ out)
+// What a step reads of its neighbours while their owners update it in the same
+// step, copied right before the step: DPD the velocities (FP64: (v, mass);
+// FP32-force: the leading floats (v, 1/m)), ImageHarmonic bonds the image counts.
+// Either output may be null.
+__global__ void k_step_snapshot(const double4_32a* __restrict__ vel, const int* __restrict__ image, uint32_t N,
+                                int fx, void* __restrict__ vel_out, int* __restrict__ img_out)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
-    if (fx)
-        reinterpret_cast<float4*>(out)[i] = reinterpret_cast<const VelFF*>(vel)[i].h;
-    else
-        reinterpret_cast<double4_32a*>(out)[i] = vel[i];
+    if (vel_out) {
+        if (fx)
+            reinterpret_cast<float4*>(vel_out)[i] = reinterpret_cast<const VelFF*>(vel)[i].h;
+        else
+            reinterpret_cast<double4_32a*>(vel_out)[i] = vel[i];
+    }
+    if (img_out)
+        for (int d = 0; d < 3; ++d) img_out[3 * (size_t)i + d] = image[3 * (size_t)i + d];
 }
 
 // FP32-force mode: FP64 state (k_load_state's layout) -> fixed words, float-float
@@ -547,6 +553,7 @@ struct azp_md {
     // DPD: kT of the thermostat and the step's velocity snapshot
     double dpd_kT = 0.0;
     double* d_dvel = nullptr;
+    int* d_img0 = nullptr;
     // control
     uint32_t* flags = nullptr;  // [0] rebuild request [1] error bits [2] builds [3] max count [4] ticket
     unsigned long long* d_ts = nullptr;
@@ -613,7 +620,7 @@ void free_all(azp_md* m)
                     m->d_bond_params, m->d_pair_table, m->d_gamma, m->d_noise, m->flags, m->d_ts, m->out_force, m->out_virial,
                     m->partials, m->thermo, m->tmp4, m->tmpd, m->snap_pos, m->snap_vel, m->snap_acc,
                     m->snap_img, m->snap_diam, m->st_pos, m->st_vel, m->st_acc, m->st_img, m->st_diam,
-                    m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab, m->d_dvel};
+                    m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab, m->d_dvel, m->d_img0};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -697,6 +704,8 @@ MDArgs base_args(azp_md* m)
     if (m->bond_kind == AZP_BOND_QUARTIC && !m->bond_params.empty()) QuarticBond::prepare_f(m->bond_params.data(), a.bond0);
     if (m->bond_kind == AZP_BOND_DOUBLE_WELL && !m->bond_params.empty())
         DoubleWellBond::prepare_f(m->bond_params.data(), a.bond0);
+    if (m->bond_kind == AZP_BOND_IMAGE_HARMONIC && !m->bond_params.empty())
+        HarmonicBond::prepare_f(m->bond_params.data(), a.bond0);
     a.gamma0 = m->gamma.empty() ? 0.0f : (float)m->gamma[0];
     a.noise0 = m->noise_host.empty() ? 0.0f : (float)m->noise_host[0];
     a.bar_geom = m->bar_geom;
@@ -707,6 +716,7 @@ MDArgs base_args(azp_md* m)
     a.wall_tab = m->d_wall_tab;
     a.wall_tol = m->wall_tol;
     a.dvel = m->d_dvel;
+    a.img0 = m->d_img0;
     a.flowf.kind = m->flow.kind;
     if (m->flow.kind == AZP_FLOW_PARABOLIC) {
         a.flowf.a = (float)m->flow.a;
@@ -777,13 +787,13 @@ int enqueue_rebuild(azp_md* m, cudaStream_t s, const uint32_t* gate)
     return AZP_OK;
 }
 
-// the step kernel, preceded for DPD by the velocity snapshot it reads
+// the step kernel, preceded for DPD and ImageHarmonic bonds by the snapshot it reads
 int md_launch(azp_md* m, int integ, const MDArgs& a, cudaStream_t s)
 {
-    if (m->pair_kind == AZP_PAIR_DPD_GENERAL_WEIGHT) {
-        k_dpd_vel_snapshot<<<blocks_for(m->N, 256), 256, 0, s>>>(m->vel, m->N, m->precision == AZP_FP32 ? 1 : 0,
-                                                                 m->d_dvel);
-        AZP_CHECK_LAUNCH("k_dpd_vel_snapshot");
+    if (m->d_dvel || m->d_img0) {
+        k_step_snapshot<<<blocks_for(m->N, 256), 256, 0, s>>>(m->vel, m->image, m->N, m->precision == AZP_FP32 ? 1 : 0,
+                                                              m->d_dvel, m->d_img0);
+        AZP_CHECK_LAUNCH("k_step_snapshot");
         m->launches += 1;
     }
     return launch_md_step(m->pair_kind, m->bond_kind, m->precision, integ, a, s);
@@ -996,7 +1006,7 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     if (c->method != AZP_METHOD_LANGEVIN_FLOW && c->method != AZP_METHOD_BROWNIAN_FLOW)
         return fail(AZP_ERR_INVALID, nullptr);
     if ((c->pair_kind >= AZP_PAIR_NUM_KINDS && c->pair_kind != AZP_PAIR_DPD_GENERAL_WEIGHT) ||
-        c->bond_kind >= AZP_BOND_NUM_KINDS)
+        (c->bond_kind >= AZP_BOND_NUM_KINDS && c->bond_kind != AZP_BOND_IMAGE_HARMONIC))
         return fail(AZP_ERR_INVALID, nullptr);
     // the DPD thermostat acts on velocities: Langevin-type methods only (the
     // noiseless, drag-free Langevin step is HOOMD's ConstantVolume)
@@ -1101,6 +1111,7 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     ALLOC(m->d_gamma, c->ntypes);
     ALLOC(m->d_noise, c->ntypes);
     if (c->pair_kind == AZP_PAIR_DPD_GENERAL_WEIGHT) ALLOC(m->d_dvel, (size_t)4 * N);
+    if (m->bond_kind == AZP_BOND_IMAGE_HARMONIC) ALLOC(m->d_img0, (size_t)3 * N);
     CTRY(cudaMemset(m->flags, 0, sizeof(uint32_t) * 8));
     CTRY(cudaMemcpy(m->d_gamma, m->gamma.data(), sizeof(double) * c->ntypes, cudaMemcpyHostToDevice));
     {

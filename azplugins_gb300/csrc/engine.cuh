@@ -97,6 +97,9 @@ struct MDArgs {
     // step, so that neighbours are read while their owners update them):
     // double4 (v, mass) in FP64 steps, float4 (v, 1/m) in FP32-force steps
     const void* dvel;
+    // ImageHarmonic bonds: the image counts of the step's start ([N][3], a
+    // snapshot for the same reason: the step updates image[] in place)
+    const int* img0;
 };
 
 constexpr int MD_INTEG_LANGEVIN = 0;

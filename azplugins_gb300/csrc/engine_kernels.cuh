@@ -448,9 +448,19 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
                 const uint2 e2 = a.bt[(size_t)k * a.N + i];
                 const double4_32a pi = a.pos[i];
                 const double4_32a pj = a.pos[e2.x];
-                const double dx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
-                const double dy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
-                const double dz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
+                double dx, dy, dz;
+                if constexpr (bond_uses_image<BE>::value) {
+                    // (x_i - x_j) + (img_i - img_j) L (src/ImagePotentialBond.h:144-152)
+                    const int* gi = a.img0 + 3 * (size_t)i;
+                    const int* gj = a.img0 + 3 * (size_t)e2.x;
+                    dx = __dadd_rn(pi.x - pj.x, __dmul_rn((double)(gi[0] - gj[0]), a.L[0]));
+                    dy = __dadd_rn(pi.y - pj.y, __dmul_rn((double)(gi[1] - gj[1]), a.L[1]));
+                    dz = __dadd_rn(pi.z - pj.z, __dmul_rn((double)(gi[2] - gj[2]), a.L[2]));
+                } else {
+                    dx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
+                    dy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
+                    dz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
+                }
                 const double rsq = rsq_exact(dx, dy, dz);
                 double fdr, en;
                 if (!BE::eval(s_bond + e2.y * AZP_BOND_PARAM_DOUBLES, rsq, fdr, en)) {
@@ -703,6 +713,43 @@ AZP_D void bond_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint3
     acc.add(dx, dy, dz, fdr, en, vir);
 }
 
+// image-unwrapped displacement of one axis from the 64-bit fixed positions
+// (hi, lo words) and the image difference: the wrapping 64-bit difference is
+// the minimum image; w = +-1 where the exact difference overflowed it; the
+// result is (minimum image) + (img_i - img_j + w) L, in FP32
+AZP_D float unwrapped_fx(uint32_t hi_i, uint32_t lo_i, uint32_t hi_j, uint32_t lo_j, int dimg, float sfix)
+{
+    const long long qi = fx_join(hi_i, lo_i), qj = fx_join(hi_j, lo_j);
+    const long long dq = (long long)((unsigned long long)qi - (unsigned long long)qj);
+    const int w = (qi >= 0 && qj < 0 && dq < 0) ? 1 : ((qi < 0 && qj >= 0 && dq >= 0) ? -1 : 0);
+    const float dmin =
+        ((float)(int)(dq >> 32) + (float)(unsigned)((unsigned long long)dq & 0xffffffffull) * 2.3283064365386963e-10f) *
+        sfix;
+    // sfix = L 2^-32 rounded to float, so sfix 2^32 is L rounded to float
+    return dmin + (float)(dimg + w) * (sfix * 4294967296.0f);
+}
+
+// one ImageHarmonic bond of particle i (fixed words fi / li, images g[3] of the
+// step's start) with partner j in the FP32-force step
+template<class BE>
+AZP_D void bond_term_fx_image(const MDArgs& a, const uint4& fi, const uint4& li, const int* g, uint32_t j,
+                              uint32_t btype, const float* s_bond, AccFx& acc, bool vir)
+{
+    const uint4 fj = __ldg(a.fix + j);
+    const uint4 lj = __ldg(a.flo + j);
+    const int* gj = a.img0 + 3 * (size_t)j;
+    const float dx = unwrapped_fx(fi.x, li.x, fj.x, lj.x, g[0] - __ldg(gj), a.sfix[0]);
+    const float dy = unwrapped_fx(fi.y, li.y, fj.y, lj.y, g[1] - __ldg(gj + 1), a.sfix[1]);
+    const float dz = unwrapped_fx(fi.z, li.z, fj.z, lj.z, g[2] - __ldg(gj + 2), a.sfix[2]);
+    const float rsq = dx * dx + dy * dy + dz * dz;
+    float fdr, en;
+    if (!BE::eval_f(s_bond + btype * BOND_F, rsq, fdr, en)) {
+        atomicOr(&a.flags[1], AZP_EBIT_BOND);
+        return;
+    }
+    acc.add(dx, dy, dz, fdr, en, vir);
+}
+
 // the last block to finish advances the timestep and arms the next rebuild
 AZP_D void finish_step(const MDArgs& a, bool want_rebuild)
 {
@@ -826,7 +873,17 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
             }
         }
         // ---------------------------------------------------------------- bonds
-        if constexpr (!std::is_same<BE, NoBond>::value) {
+        if constexpr (bond_uses_image<BE>::value) {
+            const uint32_t nb = __ldg(a.bt_n + i);
+            const uint4 li = __ldg(a.flo + i);
+            const int g[3] = {__ldg(a.img0 + 3 * (size_t)i), __ldg(a.img0 + 3 * (size_t)i + 1),
+                              __ldg(a.img0 + 3 * (size_t)i + 2)};
+            for (uint32_t k = sub; k < nb; k += tpp) {
+                const uint2 e = __ldg(a.bt + (size_t)k * a.N + i);
+                bond_term_fx_image<BE>(a, fi, li, g, e.x, e.y, s_bond, acc, vir);
+                acc.commit(vir);
+            }
+        } else if constexpr (!std::is_same<BE, NoBond>::value) {
             const uint32_t nb = __ldg(a.bt_n + i);
             for (uint32_t k0 = sub; k0 < nb; k0 += 2u * tpp) {
                 const uint32_t k1 = k0 + tpp;
@@ -991,6 +1048,7 @@ int launch_md_pe(int bond_kind, int precision, int integ, const MDArgs& a, cudaS
         case -1: return launch_md_integ<PE, NoBond, float>(integ, a, s);
         case AZP_BOND_QUARTIC: return launch_md_integ<PE, QuarticBond, float>(integ, a, s);
         case AZP_BOND_DOUBLE_WELL: return launch_md_integ<PE, DoubleWellBond, float>(integ, a, s);
+        case AZP_BOND_IMAGE_HARMONIC: return launch_md_integ<PE, HarmonicBond, float>(integ, a, s);
         default: return AZP_ERR_INVALID;
         }
     }
@@ -998,6 +1056,7 @@ int launch_md_pe(int bond_kind, int precision, int integ, const MDArgs& a, cudaS
     case -1: return launch_md_integ<PE, NoBond, double>(integ, a, s);
     case AZP_BOND_QUARTIC: return launch_md_integ<PE, QuarticBond, double>(integ, a, s);
     case AZP_BOND_DOUBLE_WELL: return launch_md_integ<PE, DoubleWellBond, double>(integ, a, s);
+    case AZP_BOND_IMAGE_HARMONIC: return launch_md_integ<PE, HarmonicBond, double>(integ, a, s);
     default: return AZP_ERR_INVALID;
     }
 }

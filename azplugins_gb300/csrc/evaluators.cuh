@@ -376,6 +376,30 @@ struct HarmonicBond {
         e = R(0.5) * k * (r0 - r) * (r0 - r);
         return true;
     }
+    // FP32 record of the fused step: q = k, r_0
+    AZP_HD static void prepare_f(const double* p, float* q)
+    {
+        for (int c = 0; c < BOND_F; ++c) q[c] = 0.0f;
+        q[0] = (float)p[0];
+        q[1] = (float)p[1];
+    }
+    AZP_D static bool eval_f(const float* q, float rsq, float& fdr, float& e)
+    {
+        const float k = q[0], r0 = q[1];
+        const float r = sqrtf(rsq);
+        fdr = r > 0.0f ? k * (r0 / r - 1.0f) : 0.0f;
+        e = 0.5f * k * (r0 - r) * (r0 - r);
+        return true;
+    }
+};
+
+// bond evaluators measured between image-unwrapped positions (x + img L)
+// instead of the minimum image: the ImageHarmonic bond
+template<class BE> struct bond_uses_image {
+    static constexpr bool value = false;
+};
+template<> struct bond_uses_image<HarmonicBond> {
+    static constexpr bool value = true;
 };
 
 }  // namespace azp

@@ -82,10 +82,10 @@ enum azp_pair_kind {
 enum azp_bond_kind {
     AZP_BOND_QUARTIC = 0,          /* BondEvaluatorQuartic */
     AZP_BOND_DOUBLE_WELL = 1,      /* BondEvaluatorDoubleWell */
-    AZP_BOND_NUM_KINDS = 2,        /* kinds of the engine */
+    AZP_BOND_NUM_KINDS = 2,        /* kinds with the minimum-image displacement */
     AZP_BOND_IMAGE_HARMONIC = 2    /* ImagePotentialBondHarmonic (src/ImagePotentialBond.h): harmonic
                                       U = k/2 (r - r0)^2 on the image-unwrapped distance; azp_bond_forces
-                                      only, reads sys->image */
+                                      (reads sys->image) and the engine (azp_md_config.bond_kind) */
 };
 /* HOOMD pair.Pair modes accepted by azplugins (src/pair.py:415) */
 enum azp_shift_mode { AZP_MODE_NONE = 0, AZP_MODE_SHIFT = 1, AZP_MODE_XPLOR = 2 };

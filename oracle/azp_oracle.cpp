@@ -1313,6 +1313,45 @@ long orc_image_bond_forces(int N, const double* pos, const int32_t* image, const
     return bad;
 }
 
+// ---- the same per particle (each bond on both ends, the MD loop's table):
+// dx = (x_i - x_j) + (img_i - img_j) L, F_i += dx f/r, U_i += U/2, W_i += dx dx f/2r
+// (src/ImagePotentialBond.h:144-190 seen from each end)
+long orc_image_bond_forces_pp(int N, const double* pos, const int32_t* image, const double* L,
+                              const int32_t* bt_start, const int32_t* bt_partner, const int32_t* bt_type, int kind,
+                              const double* params, int pstride, double* force, double* energy, double* virial)
+{
+    long fail = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(max : fail)
+#endif
+    for (int i = 0; i < N; ++i) {
+        for (int k = bt_start[i]; k < bt_start[i + 1]; ++k) {
+            const int j = bt_partner[k];
+            double v[3];
+            for (int d = 0; d < 3; ++d)
+                v[d] = (pos[4 * i + d] - pos[4 * j + d]) + (double)(image[3 * i + d] - image[3 * j + d]) * L[d];
+            const double rs = rsq_of(v);
+            double fdr = 0.0, e = 0.0;
+            if (!eval_bond(kind, params + (size_t)bt_type[k] * pstride, rs, fdr, e)) {
+                fail = std::max<long>(fail, 1 + i);
+                continue;
+            }
+            for (int d = 0; d < 3; ++d) force[3 * i + d] += fdr * v[d];
+            energy[i] += 0.5 * e;
+            if (virial) {
+                const double h = 0.5 * fdr;
+                virial[6 * i + 0] += h * v[0] * v[0];
+                virial[6 * i + 1] += h * v[0] * v[1];
+                virial[6 * i + 2] += h * v[0] * v[2];
+                virial[6 * i + 3] += h * v[1] * v[1];
+                virial[6 * i + 4] += h * v[1] * v[2];
+                virial[6 * i + 5] += h * v[2] * v[2];
+            }
+        }
+    }
+    return fail;
+}
+
 // ---- maximum squared displacement since the last list build
 double orc_max_disp2(int N, const double* pos, const double* pos_build, const double* L)
 {

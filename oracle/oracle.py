@@ -111,6 +111,8 @@ def lib():
     L.orc_velocity_field.argtypes = [c_int, _dp, _dp, _dp, vp, c_int, c_int, _up, _dp, _dp, _dp, _dp, _dp]
     L.orc_image_bond_forces.argtypes = [c_int, _dp, _ip, _dp, c_long, _ip, _ip, c_int, _dp, c_int, _dp, _dp, vp]
     L.orc_image_bond_forces.restype = c_long
+    L.orc_image_bond_forces_pp.argtypes = [c_int, _dp, _ip, _dp, _ip, _ip, _ip, c_int, _dp, c_int, _dp, _dp, vp]
+    L.orc_image_bond_forces_pp.restype = c_long
     L.orc_barrier_valid.argtypes = [c_int, c_double, _dp]
     L.orc_harmonic_barrier.argtypes = [c_int, _dp, _ip, _dp, c_int, c_double, _dp, _dp, _dp]
     _lib = L
@@ -441,6 +443,29 @@ def bond_forces_pp(pos4, L, table, name, params, F, U, W=None):
         raise RuntimeError(f"bond.{name}: bond out of bounds (particle {rc - 1})")
 
 
+def image_bond_forces_pp(pos4, image, L, table, name, params, F, U, W=None):
+    """Image-unwrapped bond forces from the per-particle table, accumulated into
+    F/U/W: the MD loop's form of ``image_bond_forces``."""
+    start, partner, btype = table
+    rc = lib().orc_image_bond_forces_pp(
+        pos4.shape[0],
+        pos4,
+        np.ascontiguousarray(image, dtype=np.int32).reshape(-1),
+        np.ascontiguousarray(L, dtype=np.float64),
+        start,
+        partner,
+        btype,
+        BOND_KINDS[name],
+        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        BOND_STRIDE,
+        F,
+        U,
+        _ptr(W),
+    )
+    if rc:
+        raise RuntimeError(f"bond.{name}: bond refused (particle {rc - 1})")
+
+
 # ------------------------------------------------------------------ integrators
 FLOW_CONSTANT, FLOW_PARABOLIC = 0, 1
 
@@ -547,7 +572,12 @@ class OracleMD:
             F, U, W = pair_forces(s["pos4"], s["types"], self.ntypes, s["L"], *self.nlist_csr, self.pair["name"],
                                   self.pair["params"], rc * rc, ronsq, self.pair.get("mode", "none"), self.force_cap)
         if self.bond is not None and self.table is not None:
-            bond_forces_pp(s["pos4"], s["L"], self.table, self.bond["name"], self.bond["params"], F, U, W)
+            if self.bond["name"] == "ImageHarmonic":
+                # the bond measured between the unwrapped positions (x + img L)
+                image_bond_forces_pp(s["pos4"], s["image"], s["L"], self.table, self.bond["name"],
+                                     self.bond["params"], F, U, W)
+            else:
+                bond_forces_pp(s["pos4"], s["L"], self.table, self.bond["name"], self.bond["params"], F, U, W)
         if self.walls is not None:
             w = self.walls
             Fw, Uw, Ww = wall_forces(s["pos4"], s["types"], w["name"], w["params"], w["rcut"], w["rextrap"],

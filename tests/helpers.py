@@ -108,3 +108,24 @@ def pair_tables(orc, name, params_by_pair, types, rcut_by_pair, ron_by_pair=None
             if ron_by_pair is not None:
                 ro[a, b] = ron_by_pair[key]
     return rec, rc, ro
+
+
+def image_chains(seed=111, n_chains=300, length=12, L=(6.0, 7.0, 5.0)):
+    """Random bead chains drawn in unwrapped space (bond lengths 0.9-1.4, every
+    fourth bond 3.5x longer, so that many bonds span more than half the box),
+    wrapped into the box with image counts, two bond types.
+
+    Returns (pos [N,3], img [N,3] int32, unwrapped [N,3], bonds [B,2], btypes [B], L [3])."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    L = np.asarray(L, dtype=np.float64)
+    N = n_chains * length
+    steps = rng.normal(size=(n_chains, length, 3))
+    steps *= rng.uniform(0.9, 1.4, size=(n_chains, length, 1)) / np.linalg.norm(steps, axis=2, keepdims=True)
+    steps[:, ::4] *= 3.5
+    un = np.cumsum(steps, axis=1).reshape(N, 3) + rng.uniform(-20, 20, size=(n_chains, 1, 3)).repeat(length, 1).reshape(
+        N, 3)
+    img = np.floor((un + 0.5 * L) / L).astype(np.int32)
+    pos = un - img * L
+    bonds = np.array([[c * length + k, c * length + k + 1] for c in range(n_chains) for k in range(length - 1)])
+    btypes = rng.integers(0, 2, size=len(bonds)).astype(np.int32)
+    return pos, img, un, bonds, btypes, L

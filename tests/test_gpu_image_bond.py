@@ -3,13 +3,17 @@ the reference test's cases through the Python front end
 (src/pytest/test_bond.py:240-309, 4 decimals as there) in both precisions, and
 random chains whose bonds span more than half the box against the oracle's
 image-unwrapped bond loop (FP64 1e-12, FP32 1e-5 norm-wise, energies and
-virials)."""
+virials), and the same chains advanced by the resident engine (Langevin with
+noise, with and without a Hertz pair force that excludes bonded pairs) against
+the oracle's MD loop: unwrapped positions and velocities after 30 steps
+(FP64 1e-9 / 1e-8, FP32 2e-4 / 2e-3) and forces at the engine's end state
+(FP64 1e-12, FP32 1e-5)."""
 
 import numpy as np
 import pytest
 
 import azplugins_gb300 as az
-from helpers import force_error, load_golden
+from helpers import force_error, image_chains, load_golden, oracle_system
 
 pytestmark = pytest.mark.gpu
 CASES = load_golden("kats.json")["image_bond"]
@@ -86,3 +90,67 @@ def test_chains_match_oracle(orc, precision, tol):
     assert force_error(f, F) < tol
     assert np.abs(f[:, 3] - U).max() <= tol * np.abs(U).max()
     assert np.abs(w - W).max() <= tol * np.abs(W).max()
+
+
+def _engine_chains(orc, precision, with_pair, steps=30):
+    pos, img, un, bonds, btypes, L = image_chains(n_chains=200, L=(9.0, 10.0, 8.0))
+    N = len(pos)
+    rng = np.random.Generator(np.random.PCG64(7))
+    s = az.Snapshot(N)
+    s.configuration.box = [*L, 0, 0, 0]
+    s.particles.position = pos
+    s.particles.image = img
+    s.particles.velocity = rng.normal(0.0, 1.0, size=(N, 3))
+    s.particles.acceleration = np.zeros((N, 3))
+    s.resize_bonds(len(bonds))
+    s.bonds.group = bonds
+    s.bonds.typeid = btypes
+    s.bonds.types = ["A-A", "A-B"]
+    ih = az.bond.ImageHarmonic()
+    ih.params["A-A"] = dict(k=30.0, r0=1.0)
+    ih.params["A-B"] = dict(k=5.0, r0=1.5)
+    forces = [ih]
+    pair = None
+    if with_pair:
+        # a soft repulsion between non-bonded beads (bonded pairs excluded, as
+        # HOOMD's nlist exclusions=("bond",)): Hertz stays finite at r = 0, so
+        # the randomly placed chains start without a blow-up
+        pair = az.pair.Hertz(nlist=az.nlist.Cell(buffer=0.4, exclusions=("bond",)), default_r_cut=0.8)
+        pair.params[("A", "A")] = dict(epsilon=5.0)
+        forces.append(pair)
+    m = az.methods.LangevinFlow("all", kT=1.0, flow_field=az.flow.ConstantFlow((0.0, 0.0, 0.0)), default_gamma=1.0)
+    sim = az.Simulation(seed=21, precision=precision)
+    sim.create_state_from_snapshot(s)
+    sim.operations.integrator = az.md.Integrator(dt=0.002, methods=[m], forces=forces)
+    sim.run(steps // 2)
+    sim.run(steps - steps // 2)
+    rec = np.zeros((2, 8))
+    rec[0, :2] = [30.0, 1.0]
+    rec[1, :2] = [5.0, 1.5]
+    kw = dict(bond=dict(name="ImageHarmonic", params=rec), method="langevin", gamma=[1.0], kT=1.0, dt=0.002, seed=21)
+    if pair is not None:
+        prec, prc, _ = pair._tables(["A"])
+        kw["pair"] = dict(name="Hertz", params=prec, rcut=prc, mode="none")
+        kw["r_buff"] = 0.4
+    md = orc.OracleMD(oracle_system(s, s.particles.acceleration), **kw)
+    md.run(steps)
+    return sim, md, L, kw, img
+
+
+@pytest.mark.parametrize("with_pair", [False, True], ids=["bonds", "bonds+hertz"])
+@pytest.mark.parametrize("precision,ptol,vtol,ftol", [("fp64", 1e-9, 1e-8, 1e-12), ("fp32", 2e-4, 2e-3, 1e-5)])
+def test_engine_chains_match_oracle(orc, precision, ptol, vtol, ftol, with_pair):
+    sim, md, L, kw, img0 = _engine_chains(orc, precision, with_pair)
+    snap = sim.state.get_snapshot()
+    out = snap.particles
+    ue = out.position + out.image * L
+    uo = md.s["pos4"][:, :3] + md.s["image"] * L
+    assert np.abs(ue - uo).max() < ptol
+    assert np.abs(out.velocity - md.s["vel4"][:, :3]).max() < vtol
+    assert np.abs(out.image - img0).sum() > 10  # particles crossed the faces during the run
+    # forces at the engine's own end state (its positions and images)
+    at_end = orc.OracleMD(oracle_system(snap), **kw)
+    f, _ = sim._engine.forces()
+    F, U, _ = at_end.forces()
+    assert force_error(f, F) < ftol
+    assert np.abs(f[:, 3].sum() - U.sum()) <= ftol * np.abs(U).sum()
