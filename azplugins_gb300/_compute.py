@@ -102,6 +102,17 @@ class NeighborList:
             idx[start[i]:start[i + 1]] = np.sort(nbrs[: counts[i], i])
         return start, idx
 
+    def counts(self):
+        """Per-particle list lengths (host uint32 [N])."""
+        max_nn, nb = ctypes.c_uint32(), ctypes.c_uint32()
+        _lib.check(self._L.azp_nlist_view(self._nl, None, None, ctypes.byref(max_nn), ctypes.byref(nb)),
+                   "azp_nlist_view")
+        counts = np.zeros(max(self.N, 1), dtype=np.uint32)
+        nbrs = np.zeros((max(max_nn.value, 1), max(self.N, 1)), dtype=np.uint32)
+        _lib.check(self._L.azp_nlist_download(self._nl, counts.ctypes.data, nbrs.ctypes.data, _stream()),
+                   "azp_nlist_download")
+        return counts[: self.N]
+
     def close(self):
         if getattr(self, "_nl", None):
             self._L.azp_nlist_destroy(self._nl)

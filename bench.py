@@ -367,7 +367,7 @@ def run_ours(args):
 
     log(f"timed region done: {ms:.1f} ms")
     state_after = sim.state.get_snapshot()
-    n_nbr, n_bond = neighbour_stats(state_after)
+    n_nbr, n_bond, n_cut = neighbour_stats(state_after)
     log("neighbour statistics done")
     accuracy = force_accuracy(az, eng, state_after, args.precision)
     log("force accuracy done")
@@ -401,7 +401,8 @@ def run_ours(args):
                                  "max_displacement": RELAX_MAX_DISP}},
             "gpu_launches": int(launches),
             "nlist_builds_per_step": builds / args.steps,
-            "pair_interactions_per_s": None,
+            "pair_interactions_per_s": N * n_cut / (t_max / args.steps * 1e-3),
+            "mean_neighbours_in_cut": n_cut,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": (TRAFFIC_BYTES_PER_PARTICLE_FP32 * N if args.precision == "fp32" else None),
                          "traffic_source": "ncu capture at N=700,000 scaled by N (profiles/k_md_step_fx_melt700k.md)",
@@ -444,9 +445,14 @@ def neighbour_stats(s):
     sysd = _compute.make_system(s, pos)
     nl = _compute.NeighborList(N, 1, np.array([[RCUT]]), R_BUFF, ex)
     nl.build(sysd)
-    st, _ = nl.to_csr()
+    n_list = float(nl.counts().astype(np.float64).sum()) / N
     nl.close()
-    return float(st[-1]) / N, 2.0 * s.bonds.N / N
+    # the same list without the buffer: the full-list count inside r_cut (pair interactions)
+    nl = _compute.NeighborList(N, 1, np.array([[RCUT]]), 0.0, ex)
+    nl.build(sysd)
+    n_cut = float(nl.counts().astype(np.float64).sum()) / N
+    nl.close()
+    return n_list, 2.0 * s.bonds.N / N, n_cut
 
 
 def force_accuracy(az, eng, snap, precision):

@@ -318,6 +318,23 @@ def suite_precision(args):
         sim.run(every)
         t_run += time.perf_counter() - t0
         done += every
+    sim.close()
+    # trajectory deviation: the same start, seed and random draws advanced 100
+    # steps with FP32 forces and with FP64 forces; RMS and largest difference of
+    # the unwrapped positions
+    Lbox = np.array(snap.configuration.box[:3])
+    traj = {}
+    for prec in ("fp32", "fp64"):
+        t = az.Simulation(seed=11, precision=prec)
+        t.create_state_from_snapshot(snap)
+        tm = az.methods.BrownianFlow("all", kT=1.0, flow_field=az.flow.ConstantFlow((0.1, 0.0, 0.0)), alpha=10.0)
+        t.operations.integrator = az.md.Integrator(dt=0.001, methods=[tm], forces=[colloid()])
+        t.run(100)
+        p = t.state.get_snapshot().particles
+        traj[prec] = p.position + p.image * Lbox
+        t.close()
+    dev = traj["fp32"] - traj["fp64"]
+    dev2 = (dev * dev).sum(axis=1)
     finite = all(np.isfinite([r["force_error"], r["energy_rel_error"], r["virial_rel_error"]]).all() for r in rows)
     line = {"suite": "precision", "workload": f"colloid mixture N={N}, 4% colloids (d=5), phi=0.3, BrownianFlow "
                                               f"U=0.1x dt=0.001 gamma=10 diameter, {total} steps (FP32-force trajectory)",
@@ -326,6 +343,9 @@ def suite_precision(args):
             "max_energy_rel_error": max(r["energy_rel_error"] for r in rows),
             "max_virial_rel_error": max(r["virial_rel_error"] for r in rows),
             "reference": "FP64 drivers (equal to the FP64 oracle to 1e-12, tests/test_gpu_pair.py)",
+            "trajectory_100_steps": {"rms_position_deviation": float(np.sqrt(dev2.mean())),
+                                     "max_position_deviation": float(np.sqrt(dev2.max())),
+                                     "compared": "FP32-force vs FP64-force engine, same start, seed and draws"},
             "fp32_brownian_timesteps_per_s": total / t_run if t_run else None}
     print(json.dumps(line), flush=True)
 
