@@ -5,7 +5,7 @@
 // Stream layout (the same in the oracle): the reference keys its integrator
 // streams as RandomGenerator(RNGIdentifier, seed, tag, timestep)
 // (src/TwoStepLangevinFlow.h:216-219, src/TwoStepBrownianFlow.h:161-164) with
-// ids from src/RNGIdentifiers.h:20-27; this build packs them as
+// ids from src/RNGIdentifiers.h:20-27; azplugins_gb300 packs them as
 //   key = { id << 24 | (seed & 0xffff) << 8 | (timestep >> 32) & 0xff,
 //           timestep & 0xffffffff }
 //   ctr = { call index, tag, 0, 0 }

@@ -1,7 +1,8 @@
 // azp_oracle.cpp -- CPU restatement of the azplugins short-range
 // force-and-integrate path, in FP64. TEST INFRASTRUCTURE ONLY: the tests, the
-// smoke check and the bench's CPU-baseline leg load it as the checker; the
-// product (azplugins_gb300) never links, imports or calls it.
+// smoke check and the bench's CPU-baseline leg load it to check and time the
+// GPU results against; the product (azplugins_gb300) never links, imports or
+// calls it.
 //
 // What is restated, and from where (paths relative to the azplugins tree):
 //   * pair evaluators   src/PairEvaluatorPerturbedLennardJones.h:117-155,
@@ -330,7 +331,7 @@ void philox(const uint32_t in[4], const uint32_t key_in[2], uint32_t out[4])
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-// Stream layout of this build (mirrors HOOMD's Seed(id, timestep, seed) +
+// Stream layout used here and on the GPU (mirrors HOOMD's Seed(id, timestep, seed) +
 // Counter(tag) structure; HOOMD's exact packing is not available to pin):
 //   key = { id<<24 | (seed & 0xffff)<<8 | (timestep>>32 & 0xff), timestep & 0xffffffff }
 //   ctr = { call index, tag, 0, 0 }

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (``azp_oracle.cpp``).
 
 TEST INFRASTRUCTURE ONLY. The tests, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` use it as the checker; the product package
+CPU-baseline leg of ``bench.py`` use it to check and time the GPU results; the product package
 ``azplugins_gb300`` never imports it.
 
 The oracle restates, in FP64, the azplugins short-range force-and-integrate
