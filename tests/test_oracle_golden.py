@@ -199,3 +199,32 @@ def test_dpd_thermostat_oracle_pair_draw_is_shared(orc):
     F2, _, _ = orc.dpd_forces(pos4, vel4, np.zeros(N, dtype=np.int32), np.arange(N, dtype=np.uint32), 1, Lv, st, idx,
                               rec, np.array([[1.0]]), 1.5, 0.01, 12, 4)
     assert not np.allclose(F, F2)
+
+
+def test_dpd_md_loop_conserves_momentum_and_thermostats(orc):
+    """The oracle's MD loop with DPDGeneralWeight and the drag-free, noiseless
+    Langevin step (HOOMD's ConstantVolume): every DPD force is pairwise
+    antisymmetric, so the total momentum stays at its start value; the random and
+    dissipative terms drive the kinetic temperature of a cold start towards kT
+    (src/pytest/test_pair_dpd.py's check, here on the oracle)."""
+    rng = np.random.Generator(np.random.PCG64(12))
+    n, a, kT = 8, 0.6, 1.5
+    g = (np.arange(n) - 0.5 * (n - 1)) * a
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    N = n ** 3
+    L = np.full(3, n * a)
+    pos = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1) + rng.uniform(-0.05, 0.05, size=(N, 3))
+    v = rng.normal(0.0, 0.1, size=(N, 3))
+    system = dict(pos4=np.concatenate([pos, np.zeros((N, 1))], axis=1),
+                  vel4=np.concatenate([v, np.ones((N, 1))], axis=1), accel=np.zeros((N, 3)),
+                  image=np.zeros((N, 3), dtype=np.int32), types=np.zeros(N, dtype=np.int32),
+                  tags=np.arange(N, dtype=np.uint32), L=L, ntypes=1)
+    rec = orc.pair_params("DPDGeneralWeight", dict(A=0.0, gamma=4.5, s=0.5)).reshape(1, 1, 4)
+    md = orc.OracleMD(system, pair=dict(name="DPDGeneralWeight", params=rec, rcut=np.array([[1.0]]), kT=kT),
+                      method="langevin", gamma=[0.0], kT=0.0, dt=0.01, seed=9, r_buff=0.4, noiseless=True)
+    p0 = md.s["vel4"][:, :3].sum(axis=0)
+    md.run(150)
+    vv = md.s["vel4"][:, :3]
+    assert np.abs(vv.sum(axis=0) - p0).max() < 1e-10
+    T = float((vv * vv).sum()) / (3 * N - 3)
+    assert T == pytest.approx(kT, rel=0.15)
