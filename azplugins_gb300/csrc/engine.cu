@@ -1448,7 +1448,9 @@ int azp_md_run(azp_md* m, uint64_t steps, void* stream)
             }
         while (mid >= 2) {
             AZP_CUDA_TRY(cudaGraphLaunch(m->gexec[m->cur], s));
-            m->launches += 3;  // arm + two step kernels (+ rebuild bodies when armed)
+            // arm + two step kernels (+ their snapshot kernels for DPD / ImageHarmonic);
+            // the rebuild bodies run only when armed and are not counted
+            m->launches += 3 + ((m->d_dvel || m->d_img0) ? 2 : 0);
             mid -= 2;
         }
     }
