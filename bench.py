@@ -216,6 +216,14 @@ def algorithmic_bytes(n_nbr_mean, n_bond_mean, precision="fp32"):
     return 16 + 4 + 4 * n_nbr_mean + 4 + 8 * n_bond_mean + 32 + 32 + 4 + 16 + 32 + 32 + 16
 
 
+def step_bytes(n_particles, n_nbr_mean, n_bond_mean, builds_per_step, precision="fp32"):
+    """Algorithmic bytes of one whole timestep: the fused step launch plus the
+    list build amortised over the steps between builds, N (16 + 4 n) per build
+    (the fixed-point record read once and the list written)."""
+    return n_particles * (algorithmic_bytes(n_nbr_mean, n_bond_mean, precision)
+                          + builds_per_step * (16 + 4 * n_nbr_mean))
+
+
 # DRAM traffic of one FP32-force fused step per particle, from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on the melt at
 # N = 700,000, whose step traffic and resident set exceed L2
@@ -417,6 +425,8 @@ def run_ours(args):
                                  "max_displacement": RELAX_MAX_DISP}},
             "gpu_launches": int(launches),
             "nlist_builds_per_step": builds / args.steps,
+            "step_gbs": step_bytes(N, n_nbr, n_bond, builds / args.steps, args.precision)
+            / (t_max / args.steps * 1e-3) / 1e9,
             "pair_interactions_per_s": N * n_cut / (t_max / args.steps * 1e-3),
             "mean_neighbours_in_cut": n_cut,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
