@@ -39,6 +39,18 @@ FLOW_CONSTANT, FLOW_PARABOLIC = 0, 1
 METHOD_LANGEVIN, METHOD_BROWNIAN = 0, 1
 BARRIER_GEOMETRIES = {"planar": 0, "spherical": 1}
 WALL_KINDS = {"LJ93": 0, "Colloid": 1}
+# record classes of azp_record_size / azp_params_from_single
+RECORD_PAIR, RECORD_BOND, RECORD_WALL = 0, 1, 2
+
+
+def record_doubles(record_class: int, kind: int) -> int:
+    """Doubles per param_type record of (class, kind) in the layout every table
+    argument of the C ABI takes: the reference's sizeof in a double-precision
+    HOOMD build, divided by 8."""
+    n = load().azp_record_size(record_class, kind, 0)
+    if n <= 0:
+        raise ValueError(f"unknown record class {record_class} / kind {kind}")
+    return n // 8
 EBIT_NLIST_OVERFLOW, EBIT_BOND, EBIT_NONFINITE, EBIT_TIMEOUT = 0x1, 0x2, 0x4, 0x8
 EBIT_RANGE = 0x20
 BINNING_KINDS = {"cartesian": 0, "cylindrical": 1}
@@ -189,6 +201,8 @@ _SIGNATURES = [
     ("azp_bond_params_to_values", _i, [_i, _vp, _vp]),
     ("azp_pair_num_values", _i, [_i]),
     ("azp_bond_num_values", _i, [_i]),
+    ("azp_record_size", _i, [_i, _i, _i]),
+    ("azp_params_from_single", _i, [_i, _i, _vp, _u32, _vp]),
     ("azp_nlist_create", _vp, [_u32, _u32, _u32, ctypes.POINTER(_i)]),
     ("azp_nlist_destroy", None, [_vp]),
     ("azp_nlist_set_cutoffs", _i, [_vp, _vp, _d]),

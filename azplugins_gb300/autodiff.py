@@ -160,7 +160,7 @@ class Context:
 def _pair_tables(ctx, values):
     torch = _torch()
     L = _lib.load()
-    rec = np.zeros(4)
+    rec = np.zeros(_lib.record_doubles(_lib.RECORD_PAIR, ctx.pair.kind))
     vals = np.ascontiguousarray([float(v) for v in values], dtype=np.float64)
     _lib.check(L.azp_pair_params_from_values(ctx.pair.kind, vals.ctypes.data, rec.ctypes.data), "params")
     nt = len(ctx.types)
@@ -235,7 +235,7 @@ def _make_bond_fn():
             L = _lib.load()
             pos4 = ctx.pos4(x)
             sysd = ctx.system(pos4)
-            rec = np.zeros(8)
+            rec = np.zeros(_lib.record_doubles(_lib.RECORD_BOND, ctx.bond.kind))
             vals = np.ascontiguousarray([float(v) for v in values], dtype=np.float64)
             _lib.check(L.azp_bond_params_from_values(ctx.bond.kind, vals.ctypes.data, rec.ctypes.data), "params")
             params = torch.from_numpy(np.tile(rec, len(ctx.bond_types))).cuda()

@@ -46,7 +46,7 @@ class ReplicaBatch:
         self.off = np.concatenate([[0], np.cumsum(self.N)]).astype(np.int64)
         box = np.array([s.configuration.box[:3] for s in snapshots], dtype=np.float64)
         pot = pair_cls(nlist=None, mode=mode)
-        recs = np.zeros((self.S, 4))
+        recs = np.zeros((self.S, _lib.record_doubles(_lib.RECORD_PAIR, pot.kind)))
         for r, d in enumerate(params):
             vals = np.ascontiguousarray([float(d[k]) for k in pot._keys], dtype=np.float64)
             _lib.check(L.azp_pair_params_from_values(pot.kind, vals.ctypes.data, recs[r].ctypes.data), "params")

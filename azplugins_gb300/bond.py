@@ -32,13 +32,14 @@ class Bond:
 
     def _table(self, bond_types):
         L = _lib.load()
-        rec = np.zeros((len(bond_types), 8))
+        d_rec = _lib.record_doubles(_lib.RECORD_BOND, self.kind)
+        rec = np.zeros((len(bond_types), d_rec))
         for t, name in enumerate(bond_types):
             if name not in self.params:
                 raise KeyError(f"{type(self).__name__}.params[{name!r}] is not set")
             d = self.params[name]
             vals = np.ascontiguousarray([d[k] for k in self._keys], dtype=np.float64)
-            out = np.zeros(8)
+            out = np.zeros(d_rec)
             _lib.check(L.azp_bond_params_from_values(self.kind, vals.ctypes.data, out.ctypes.data), "params")
             rec[t] = out
         return rec

@@ -35,7 +35,7 @@ __global__ void k_pair_adj_table(const double* __restrict__ params, const double
     if (t >= ntypes * ntypes) return;
     D5 p[AZP_PAIR_PARAM_DOUBLES];
     for (int m = 0; m < AZP_PAIR_PARAM_DOUBLES; ++m) {
-        p[m] = D5(params[(size_t)t * AZP_PAIR_PARAM_DOUBLES + m]);
+        p[m] = D5(m < Eval::REC_DOUBLES ? params[(size_t)t * Eval::REC_DOUBLES + m] : 0.0);
         p[m].d[1 + m] = 1.0;
     }
     D5* rec = out + (size_t)t * PAIR_TBL;
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) k_bond_adjoint(BondAdjArgs a)
         const double dz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
         D9 p[8];
         for (int m = 0; m < 8; ++m) {
-            p[m] = D9(a.params[(size_t)e2.y * AZP_BOND_PARAM_DOUBLES + m]);
+            p[m] = D9(m < Eval::REC_DOUBLES ? a.params[(size_t)e2.y * Eval::REC_DOUBLES + m] : 0.0);
             p[m].d[1 + m] = 1.0;
         }
         D9 x(rsq_exact(dx, dy, dz));

@@ -98,25 +98,17 @@ __global__ void k_b_scatter(const uint32_t* __restrict__ cell_of, const uint32_t
     members[cell_start[cell_of[i]] + slot[i]] = i;
 }
 
-__global__ void k_b_cell_sort(const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ members, uint32_t ncell,
-                              const uint32_t* __restrict__ gate)
+// each cell's members sorted by index (deterministic order), one warp per cell
+__global__ void __launch_bounds__(kSortWarps * 32) k_b_cell_sort(const uint32_t* __restrict__ cell_start,
+                                                                 uint32_t* __restrict__ members, uint32_t ncell,
+                                                                 const uint32_t* __restrict__ gate)
 {
     if (gated_off(gate)) return;
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ uint32_t s_rows[kSortWarps][kMaxSortedCell];
+    const uint32_t w = threadIdx.x >> 5;
+    const uint32_t c = blockIdx.x * kSortWarps + w;
     if (c >= ncell) return;
-    const uint32_t b = cell_start[c], e = cell_start[c + 1];
-    // a cell this crowded only occurs in a broken configuration: keep the
-    // arrival order rather than spend O(n^2) on it
-    if (e - b > kMaxSortedCell) return;
-    for (uint32_t a = b + 1; a < e; ++a) {
-        const uint32_t v = members[a];
-        uint32_t k = a;
-        while (k > b && members[k - 1] > v) {
-            members[k] = members[k - 1];
-            --k;
-        }
-        members[k] = v;
-    }
+    warp_sort_cell(members, cell_start[c], cell_start[c + 1], s_rows[w]);
 }
 
 struct BPerm {
@@ -648,7 +640,8 @@ int b_rebuild(azp_batch* b, cudaStream_t s, const uint32_t* gate)
     int st = exclusive_scan(b->cell_count, b->cell_start, b->ncell, b->scan_tmp, s, gate);
     if (st) return st;
     k_b_scatter<<<nblk(N), 256, 0, s>>>(b->cell_of, b->slot, b->cell_start, b->members, N, gate);
-    k_b_cell_sort<<<nblk(b->ncell), 256, 0, s>>>(b->cell_start, b->members, b->ncell, gate);
+    k_b_cell_sort<<<(b->ncell + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(b->cell_start, b->members,
+                                                                                      b->ncell, gate);
     BPerm p;
     p.members = b->members;
     p.pos = b->pos[b->cur];
@@ -854,7 +847,8 @@ azp_batch* azp_batch_create(const azp_batch_config* c, int* status)
         const double zero = 0.0;
         int st = AZP_OK;
         double rec[PAIR_TBL];
-        st = build_pair_table(c->pair_kind, c->pair_params + (size_t)4 * r, &rc, &zero, c->shift_mode, 1, rec);
+        st = build_pair_table(c->pair_kind, c->pair_params + (size_t)pair_record_doubles(c->pair_kind) * r, &rc, &zero,
+                              c->shift_mode, 1, rec);
         if (st) return fail(st, b);
         for (int k = 0; k < PAIR_TBL; ++k) si.rec[k] = rec[k];
         // the evaluator subtracts the shift itself in the single-system kernel; here fold it

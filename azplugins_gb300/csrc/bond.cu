@@ -21,8 +21,11 @@ template<class Eval, typename R>
 __global__ void __launch_bounds__(BOND_BLOCK) k_bond(BondArgs a)
 {
     __shared__ R s_p[MAX_BOND_TYPES * AZP_BOND_PARAM_DOUBLES];
-    for (uint32_t t = threadIdx.x; t < a.nbondtypes * AZP_BOND_PARAM_DOUBLES; t += blockDim.x)
-        s_p[t] = (R)a.params[t];
+    // the caller's records (Eval::REC_DOUBLES each) zero-padded to 8 values
+    for (uint32_t t = threadIdx.x; t < a.nbondtypes * AZP_BOND_PARAM_DOUBLES; t += blockDim.x) {
+        const uint32_t b = t / AZP_BOND_PARAM_DOUBLES, m = t % AZP_BOND_PARAM_DOUBLES;
+        s_p[t] = m < (uint32_t)Eval::REC_DOUBLES ? (R)a.params[(size_t)b * Eval::REC_DOUBLES + m] : R(0);
+    }
     __syncthreads();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.N) return;

@@ -14,7 +14,7 @@ struct BondArgs {
     float sfix[3];
     const uint32_t* n_bonds; // [N]
     const uint2* table;      // [height][N] (partner index, bond type)
-    const double* params;    // [nbondtypes][8] reference param records
+    const double* params;    // [nbondtypes] reference param records (Eval::REC_DOUBLES each)
     void* force;             // accumulated: double4_32a / float4 [N]
     void* virial;            // accumulated: [6][pitch] or null
     uint32_t pitch;

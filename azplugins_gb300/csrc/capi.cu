@@ -92,13 +92,77 @@ const char* azp_last_error(void) { return azp::g_last_error.c_str(); }
 int azp_pair_num_values(int kind) { return n_pair_values(kind); }
 int azp_bond_num_values(int kind) { return n_bond_values(kind); }
 
+// Scalars declared by each param_type (src/PairEvaluatorPerturbedLennardJones.h:57-60,
+// src/PairEvaluatorExpandedYukawa.h:45-47, src/PairEvaluatorHertz.h:41,
+// src/PairEvaluatorColloid.h:48-51, src/DPDPairEvaluatorGeneralWeight.h:54-56,
+// src/BondEvaluatorQuartic.h:69-76, src/BondEvaluatorDoubleWell.h:52-55, HOOMD's
+// harmonic bond {k, r_0}, src/WallEvaluatorLJ93.h:50-51, src/WallEvaluatorColloid.h:58-60)
+// and the record alignment of the single-precision build (the aligned(...)
+// branch for HOOMD_LONGREAL_SIZE == 32); 0 for an unknown kind
+static int record_fields(int cls, int kind, int* align_single)
+{
+    *align_single = 16;
+    if (cls == AZP_RECORD_PAIR) {
+        switch (kind) {
+        case AZP_PAIR_PERTURBED_LJ: return 4;
+        case AZP_PAIR_EXPANDED_YUKAWA: return 3;
+        case AZP_PAIR_HERTZ: *align_single = 4; return 1;
+        case AZP_PAIR_COLLOID: return 4;
+        case AZP_PAIR_DPD_GENERAL_WEIGHT: return 3;
+        default: return 0;
+        }
+    }
+    if (cls == AZP_RECORD_BOND) {
+        switch (kind) {
+        case AZP_BOND_QUARTIC: return 8;
+        case AZP_BOND_DOUBLE_WELL: return 4;
+        case AZP_BOND_IMAGE_HARMONIC: *align_single = 8; return 2;
+        default: return 0;
+        }
+    }
+    if (cls == AZP_RECORD_WALL) {
+        *align_single = 8;
+        if (kind == AZP_WALL_LJ93) return 2;
+        if (kind == AZP_WALL_COLLOID) return 3;
+    }
+    return 0;
+}
+
+int azp_record_size(int cls, int kind, int single)
+{
+    int align = 0;
+    const int n = record_fields(cls, kind, &align);
+    if (n == 0) return AZP_ERR_INVALID;
+    if (single) return ((n * 4 + align - 1) / align) * align;
+    const int d = cls == AZP_RECORD_PAIR ? azp::pair_record_doubles(kind)
+                                         : (cls == AZP_RECORD_BOND ? azp::bond_record_doubles(kind)
+                                                                   : azp::wall_record_doubles(kind));
+    return 8 * d;
+}
+
+int azp_params_from_single(int cls, int kind, const void* src, uint32_t n, double* dst)
+{
+    int align = 0;
+    const int fields = record_fields(cls, kind, &align);
+    if (fields == 0 || (n && (!src || !dst))) return AZP_ERR_INVALID;
+    const int sb = azp_record_size(cls, kind, 1), dd = azp_record_size(cls, kind, 0) / 8;
+    const unsigned char* in = static_cast<const unsigned char*>(src);
+    for (uint32_t r = 0; r < n; ++r) {
+        float f[8];
+        std::memcpy(f, in + (size_t)r * sb, sizeof(float) * fields);
+        for (int k = 0; k < dd; ++k) dst[(size_t)r * dd + k] = k < fields ? (double)f[k] : 0.0;
+    }
+    return AZP_OK;
+}
+
 // PairParameters*(pybind11::dict) -- src/PairEvaluatorPerturbedLennardJones.h:33-45,
 // src/PairEvaluatorExpandedYukawa.h:28-33, src/PairEvaluatorHertz.h:28-31,
 // src/PairEvaluatorColloid.h:28-35
 int azp_pair_params_from_values(int kind, const double* v, double* rec)
 {
     if (!v || !rec) return AZP_ERR_INVALID;
-    for (int k = 0; k < AZP_PAIR_PARAM_DOUBLES; ++k) rec[k] = 0.0;
+    if (n_pair_values(kind) <= 0) return AZP_ERR_INVALID;
+    for (int k = 0; k < azp::pair_record_doubles(kind); ++k) rec[k] = 0.0;
     switch (kind) {
     case AZP_PAIR_PERTURBED_LJ: {
         const double sigma = v[1], s2 = sigma * sigma, s4 = s2 * s2;
@@ -140,7 +204,8 @@ int azp_pair_params_to_values(int kind, const double* rec, double* v)
 int azp_bond_params_from_values(int kind, const double* v, double* rec)
 {
     if (!v || !rec) return AZP_ERR_INVALID;
-    for (int k = 0; k < AZP_BOND_PARAM_DOUBLES; ++k) rec[k] = 0.0;
+    if (n_bond_values(kind) <= 0) return AZP_ERR_INVALID;
+    for (int k = 0; k < azp::bond_record_doubles(kind); ++k) rec[k] = 0.0;
     switch (kind) {
     case AZP_BOND_QUARTIC: {
         const double sigma = v[5], s2 = sigma * sigma, s4 = s2 * s2;

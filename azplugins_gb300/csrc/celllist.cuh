@@ -8,6 +8,43 @@ namespace azp
 {
 // cells holding more particles than this are not sorted by index
 constexpr uint32_t kMaxSortedCell = 512;
+// warps per block of the cell-sort kernels (one warp per cell)
+constexpr int kSortWarps = 8;
+
+// Sort the members of one cell, members[b, e), by particle index: the order in
+// which atomics placed them is not deterministic, the sorted order is. One warp
+// per cell: the members are staged in the warp's shared-memory row s_row
+// (kMaxSortedCell entries), and the rank of each member is the number of members
+// with a smaller index (indices are distinct), counted by a broadcast read of the
+// row per compare; each lane ranks up to four members per pass over the row, so
+// a cell of n members costs n * ceil(n / 128) shared-memory reads per lane. A
+// cell above kMaxSortedCell keeps its arrival order (only a broken configuration
+// crowds a cell that much). Warp-uniform control flow; no block barrier.
+__device__ __forceinline__ void warp_sort_cell(uint32_t* __restrict__ members, uint32_t b, uint32_t e,
+                                               uint32_t* __restrict__ s_row)
+{
+    const uint32_t n = e - b;
+    if (n < 2 || n > kMaxSortedCell) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t k = lane; k < n; k += 32u) s_row[k] = members[b + k];
+    __syncwarp();
+    for (uint32_t base = 0; base < n; base += 128u) {
+        uint32_t v[4], r[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t k = base + (uint32_t)u * 32u + lane;
+            v[u] = k < n ? s_row[k] : 0xffffffffu;
+        }
+        for (uint32_t q = 0; q < n; ++q) {
+            const uint32_t x = s_row[q];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) r[u] += x < v[u] ? 1u : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (base + (uint32_t)u * 32u + lane < n) members[b + r[u]] = v[u];
+    }
+}
 
 // Cells of width >= r_list_max along each axis; an axis with fewer than 3 cells
 // is scanned as a single cell (no duplicate images).

@@ -37,6 +37,16 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 // not re-binned: the run ends with the error instead). NULL: always run.
 AZP_D bool gated_off(const uint32_t* gate) { return gate && (gate[0] == 0u || gate[1] != 0u); }
 
+// ---------------------------------------------------------------- param_type strides
+// doubles of one param_type record in the reference's double-precision layout
+// (sizeof / 8): every table argument of the C ABI is an array at this stride
+AZP_HD int pair_record_doubles(int kind) { return kind == AZP_PAIR_HERTZ ? 1 : 4; }
+AZP_HD int bond_record_doubles(int kind)
+{
+    return kind == AZP_BOND_QUARTIC ? 8 : (kind == AZP_BOND_DOUBLE_WELL ? 4 : 2);
+}
+AZP_HD int wall_record_doubles(int kind) { return kind == AZP_WALL_LJ93 ? 2 : 4; }
+
 // ---------------------------------------------------------------- type bits
 // The type lives in the low 32 bits of pos.w's bit pattern (HOOMD __int_as_scalar).
 AZP_HD uint32_t type_of(double w)

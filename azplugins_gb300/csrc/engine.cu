@@ -1041,7 +1041,8 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     const uint32_t nt2 = c->ntypes * c->ntypes;
     if (m->pair_kind >= 0) {
         if (!c->pair_params || !c->r_cut) return fail(AZP_ERR_INVALID, m);
-        m->pair_params.assign(c->pair_params, c->pair_params + (size_t)nt2 * AZP_PAIR_PARAM_DOUBLES);
+        // the caller's table, in the reference layout (pair_record_doubles per record)
+        m->pair_params.assign(c->pair_params, c->pair_params + (size_t)nt2 * pair_record_doubles(m->pair_kind));
         m->r_cut.assign(c->r_cut, c->r_cut + nt2);
         if (c->r_on) m->r_on.assign(c->r_on, c->r_on + nt2);
         else m->r_on.assign(nt2, 0.0);
@@ -1132,7 +1133,7 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
             m->dpd_kT = c->dpd_kT;
             for (uint32_t t = 0; t < nt2; ++t) {
                 double* rec = &table[(size_t)t * PAIR_TBL];
-                const double* p = &m->pair_params[(size_t)t * AZP_PAIR_PARAM_DOUBLES];
+                const double* p = &m->pair_params[(size_t)t * pair_record_doubles(AZP_PAIR_DPD_GENERAL_WEIGHT)];
                 const double rc = m->r_cut[t];
                 if (rc > 0.0) {
                     const double rcinv = 1.0 / std::sqrt(rc * rc);
@@ -1172,7 +1173,12 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
             c->nbondtypes > MD_MAX_BOND_TYPES)
             return fail(AZP_ERR_INVALID, m);
         m->nbt = c->nbondtypes;
-        m->bond_params.assign(c->bond_params, c->bond_params + (size_t)c->nbondtypes * AZP_BOND_PARAM_DOUBLES);
+        // the caller's records (bond_record_doubles each) zero-padded to 8 values
+        m->bond_params.assign((size_t)c->nbondtypes * AZP_BOND_PARAM_DOUBLES, 0.0);
+        for (uint32_t t = 0; t < c->nbondtypes; ++t)
+            for (int k = 0; k < bond_record_doubles(m->bond_kind); ++k)
+                m->bond_params[(size_t)t * AZP_BOND_PARAM_DOUBLES + k] =
+                    c->bond_params[(size_t)t * bond_record_doubles(m->bond_kind) + k];
         std::vector<uint32_t> n(N, 0);
         for (uint32_t b = 0; b < c->nbonds; ++b) {
             const uint32_t x = c->bonds[2 * b], y = c->bonds[2 * b + 1];
@@ -1230,7 +1236,8 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         if (st) return fail(st, m);
         std::vector<double> tab((size_t)WALL_TAB * c->ntypes, 0.0);
         for (uint32_t t = 0; t < c->ntypes; ++t) {
-            for (int k = 0; k < 4; ++k) tab[WALL_TAB * t + k] = c->wall_params[4 * t + k];
+            const int wd = wall_record_doubles(c->wall_kind);
+            for (int k = 0; k < wd; ++k) tab[WALL_TAB * t + k] = c->wall_params[(size_t)wd * t + k];
             const double rc = c->wall_r_cut[t], rx = c->wall_r_extrap[t];
             if (!(rc >= 0.0) || !(rx >= 0.0)) return fail(AZP_ERR_INVALID, m);
             tab[WALL_TAB * t + 4] = rc * rc;

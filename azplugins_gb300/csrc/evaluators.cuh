@@ -43,6 +43,7 @@ AZP_HD float rcp(float x)
 struct PerturbedLJ {
     // rec: lj1, lj2, lambda, rwcasq, wca_shift, 12 lj1, 6 lj2, (shift)
     static constexpr int SHIFT_SLOT = 7;
+    static constexpr int REC_DOUBLES = 4;  // param_type: sigma_6, epsilon_x_4, attraction_scale_factor, rwcasq
     template<typename R> AZP_HD static void prepare(const R* p, R* rec)
     {
         const R s6 = p[0], e4 = p[1], lam = p[2];
@@ -76,6 +77,7 @@ struct PerturbedLJ {
 struct ExpandedYukawa {
     // rec: epsilon, kappa, delta, (shift)
     static constexpr int SHIFT_SLOT = 3;
+    static constexpr int REC_DOUBLES = 4;  // param_type: epsilon, kappa, delta (aligned(32))
     template<typename R> AZP_HD static void prepare(const R* p, R* rec)
     {
         rec[0] = p[0];
@@ -98,6 +100,7 @@ struct ExpandedYukawa {
 struct Hertz {
     // rec: epsilon, r_cut, (shift, never set: the reference has no shift branch)
     static constexpr int SHIFT_SLOT = 7;
+    static constexpr int REC_DOUBLES = 1;  // param_type: epsilon (aligned(8))
     template<typename R> AZP_HD static void prepare(const R* p, R* rec)
     {
         rec[0] = p[0];
@@ -118,6 +121,7 @@ struct Hertz {
 struct Colloid {
     // rec: A, a_1, a_2, sigma^3, sigma^6, form (0 SS, 1 CS, 2 CC), max(a_1,a_2), (shift)
     static constexpr int SHIFT_SLOT = 7;
+    static constexpr int REC_DOUBLES = 4;  // param_type: A, a_1, a_2, sigma_3
     template<typename R> AZP_HD static void prepare(const R* p, R* rec)
     {
         rec[0] = p[0];
@@ -192,7 +196,7 @@ struct Colloid {
 };
 
 // Host: fill the kernel record and cut record of one type pair.
-// p: the reference param_type (4 doubles); mode: azp_shift_mode.
+// p: the reference param_type zero-padded to 4 doubles; mode: azp_shift_mode.
 template<class Eval, typename R>
 AZP_HD void prepare_pair_t(const R* p, double rcut, double ron, int mode, R* rec, R* cut)
 {
@@ -220,6 +224,17 @@ AZP_HD void prepare_pair(const double* p, double rcut, double ron, int mode, dou
     prepare_pair_t<Eval, double>(p, rcut, ron, mode, rec, cut);
 }
 
+// one record of a caller's table (Eval::REC_DOUBLES doubles at p) zero-padded to 4
+template<class Eval> AZP_HD void load_pair_record(const double* p, double* q)
+{
+    for (int k = 0; k < 4; ++k) q[k] = k < Eval::REC_DOUBLES ? p[k] : 0.0;
+}
+// the same for a bond record, padded to AZP_BOND_PARAM_DOUBLES
+template<class Eval> AZP_HD void load_bond_record(const double* p, double* q)
+{
+    for (int k = 0; k < AZP_BOND_PARAM_DOUBLES; ++k) q[k] = k < Eval::REC_DOUBLES ? p[k] : 0.0;
+}
+
 // XPLOR smoothing of (fdr, e) for ronsq <= rsq < rcutsq (HOOMD pair.Pair mode
 // "xplor"): S = (rc2 - r2)^2 (rc2 + 2 r2 - 3 ro2) / (rc2 - ro2)^3.
 template<typename R> AZP_HD void xplor(const R* cut, R rsq, R& fdr, R& e)
@@ -234,7 +249,8 @@ template<typename R> AZP_HD void xplor(const R* cut, R rsq, R& fdr, R& e)
 }
 
 // ================================================================ bond potentials
-// rec = the reference param_type (8 doubles). eval returns false when the
+// rec = the reference param_type, zero-padded to 8 doubles (load_bond_record).
+// eval returns false when the
 // evaluator refuses (the reference's "invalid parameters" returns).
 // The FP32-force engine step uses FP32 records of BOND_F floats per bond type
 // instead, with the per-type constants of eval precomputed (prepare_f), so its
@@ -242,6 +258,7 @@ template<typename R> AZP_HD void xplor(const R* cut, R rsq, R& fdr, R& e)
 constexpr int BOND_F = 12;
 
 struct QuarticBond {
+    static constexpr int REC_DOUBLES = 8;  // param_type: k, r_0, b_1, b_2, U_0, sigma_6, epsilon_x_4, delta
     template<typename R> AZP_HD static bool eval(const R* p, R rsq, R& fdr, R& e)
     {
         const R k = p[0], r0 = p[1], b1 = p[2], b2 = p[3], U0 = p[4];
@@ -328,6 +345,7 @@ struct QuarticBond {
 };
 
 struct DoubleWellBond {
+    static constexpr int REC_DOUBLES = 4;  // param_type: r_1, r_diff, U_1, U_tilt
     template<typename R> AZP_HD static bool eval(const R* p, R rsq, R& fdr, R& e)
     {
         const R r1 = p[0], rd = p[1], U1 = p[2], Ut = p[3];
@@ -368,6 +386,7 @@ struct DpdEngine {
 // src/ImagePotentialBond.h:144-152 applies to the image-unwrapped distance):
 // p = {k, r_0}. At r = 0 the force is set to 0 (its direction is undefined).
 struct HarmonicBond {
+    static constexpr int REC_DOUBLES = 2;  // HOOMD harmonic bond param_type: k, r_0
     template<typename R> AZP_HD static bool eval(const R* p, R rsq, R& fdr, R& e)
     {
         const R k = p[0], r0 = p[1];

@@ -128,26 +128,17 @@ __global__ void k_cell_scatter(const uint32_t* __restrict__ cell_of, const uint3
     members[cell_start[cell_of[i]] + slot[i]] = i;
 }
 
-// insertion sort of each cell's members by index: deterministic order
-__global__ void k_cell_sort(const uint32_t* __restrict__ cell_start, uint32_t* __restrict__ members, uint32_t ncell,
-                            const uint32_t* __restrict__ gate)
+// each cell's members sorted by index (deterministic order), one warp per cell
+__global__ void __launch_bounds__(kSortWarps * 32) k_cell_sort(const uint32_t* __restrict__ cell_start,
+                                                               uint32_t* __restrict__ members, uint32_t ncell,
+                                                               const uint32_t* __restrict__ gate)
 {
     if (gated_off(gate)) return;
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ uint32_t s_rows[kSortWarps][kMaxSortedCell];
+    const uint32_t w = threadIdx.x >> 5;
+    const uint32_t c = blockIdx.x * kSortWarps + w;
     if (c >= ncell) return;
-    const uint32_t b = cell_start[c], e = cell_start[c + 1];
-    // a cell this crowded only occurs in a broken configuration: keep the
-    // arrival order rather than spend O(n^2) on it
-    if (e - b > kMaxSortedCell) return;
-    for (uint32_t a = b + 1; a < e; ++a) {
-        const uint32_t v = members[a];
-        uint32_t k = a;
-        while (k > b && members[k - 1] > v) {
-            members[k] = members[k - 1];
-            --k;
-        }
-        members[k] = v;
-    }
+    warp_sort_cell(members, cell_start[c], cell_start[c + 1], s_rows[w]);
 }
 
 struct BoxArgs {
@@ -352,7 +343,7 @@ void launch_cell_scatter(const uint32_t* cell_of, const uint32_t* slot, const ui
 {
     if (N == 0) return;
     k_cell_scatter<<<(N + 255) / 256, 256, 0, s>>>(cell_of, slot, cell_start, members, N, gate);
-    k_cell_sort<<<(ncell + 255) / 256, 256, 0, s>>>(cell_start, members, ncell, gate);
+    k_cell_sort<<<(ncell + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(cell_start, members, ncell, gate);
 }
 
 __global__ void k_to_fixed2(const double4_32a* __restrict__ pos, uint4* __restrict__ fa, uint4* __restrict__ fb,

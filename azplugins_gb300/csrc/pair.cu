@@ -200,8 +200,9 @@ void fill_table(const double* params, const double* r_cut, const double* r_on, i
 {
     for (uint32_t t = 0; t < ntypes * ntypes; ++t) {
         double* rec = out + (size_t)t * PAIR_TBL;
-        prepare_pair<Eval>(params + (size_t)t * AZP_PAIR_PARAM_DOUBLES, r_cut[t], r_on ? r_on[t] : 0.0, mode, rec,
-                           rec + PAIR_REC);
+        double p[4];
+        load_pair_record<Eval>(params + (size_t)t * Eval::REC_DOUBLES, p);
+        prepare_pair<Eval>(p, r_cut[t], r_on ? r_on[t] : 0.0, mode, rec, rec + PAIR_REC);
     }
 }
 
@@ -212,8 +213,9 @@ __global__ void k_pair_table(const double* __restrict__ params, const double* __
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntypes * ntypes) return;
     double* rec = out + (size_t)t * PAIR_TBL;
-    prepare_pair<Eval>(params + (size_t)t * AZP_PAIR_PARAM_DOUBLES, r_cut[t], r_on ? r_on[t] : 0.0, mode, rec,
-                       rec + PAIR_REC);
+    double p[4];
+    load_pair_record<Eval>(params + (size_t)t * Eval::REC_DOUBLES, p);
+    prepare_pair<Eval>(p, r_cut[t], r_on ? r_on[t] : 0.0, mode, rec, rec + PAIR_REC);
 }
 
 int launch_pair_table(int kind, const double* params, const double* r_cut, const double* r_on, int mode,

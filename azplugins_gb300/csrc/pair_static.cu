@@ -15,7 +15,6 @@
 // column-major neighbors[k * N + i]), the parameter tables and the outputs, as
 // for azp_pair_forces. The kernels are the ones azp_pair_forces launches, with
 // the same threads per particle, so the results are identical.
-#include <mutex>
 #include <string>
 
 #include "celllist.cuh"
@@ -30,10 +29,6 @@ constexpr int kStaticTpp = 4;
 constexpr size_t kTableBytes = (size_t)MAX_PAIR_TYPES * MAX_PAIR_TYPES * PAIR_TBL * sizeof(double);
 constexpr size_t kFixedOffset = (kTableBytes + 255) & ~(size_t)255;
 constexpr size_t kScratchBytes = kFixedOffset + (size_t)AZP_STATIC_MAX_N * sizeof(uint4);
-constexpr int kMaxDevices = 64;
-
-std::mutex g_scratch_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
 
 bool box_valid(const azp_box& b)
 {
@@ -47,22 +42,17 @@ bool box_valid(const azp_box& b)
 // Shared by every call in the process on a given device.
 static __device__ __align__(256) unsigned char g_pair_scratch[kScratchBytes];
 
-// Device address of g_pair_scratch on the current device. Looked up once per
-// device (the first call on that device), with that device current; the host
-// symbol g_pair_scratch itself is not a device address and is never passed on.
+// Device address of g_pair_scratch on the current device, looked up on every
+// call with the caller's device current. The host symbol g_pair_scratch itself is
+// not a device address and is never passed on. The lookup enqueues no work; no
+// address is kept between calls, so a context torn down and created again
+// (cudaDeviceReset) gets the array's new address on its next call.
 static int scratch_address(unsigned char** out)
 {
-    int dev = 0;
-    AZP_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return record_error(AZP_ERR_INVALID, "azp_pair_forces_static: device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        AZP_CUDA_TRY(cudaGetSymbolAddress(&p, g_pair_scratch));
-        if (!p) return record_error(AZP_ERR_CUDA, "azp_pair_forces_static: cudaGetSymbolAddress returned NULL");
-        g_scratch_addr[dev] = p;
-    }
-    *out = static_cast<unsigned char*>(g_scratch_addr[dev]);
+    void* p = nullptr;
+    AZP_CUDA_TRY(cudaGetSymbolAddress(&p, g_pair_scratch));
+    if (!p) return record_error(AZP_ERR_CUDA, "azp_pair_forces_static: cudaGetSymbolAddress returned NULL");
+    *out = static_cast<unsigned char*>(p);
     return AZP_OK;
 }
 

@@ -21,9 +21,15 @@ namespace
 {
 constexpr int kBlock = 128;
 
+// one wall record of a caller's table (stride doubles each) zero-padded to 4
+AZP_D void load_wall_record(const double* __restrict__ params, uint32_t t, int stride, double* p)
+{
+    for (int k = 0; k < 4; ++k) p[k] = k < stride ? __ldg(params + (size_t)t * stride + k) : 0.0;
+}
+
 template<class EV, typename T>
 __global__ void __launch_bounds__(kBlock) k_walls(const double4_32a* __restrict__ pos,
-                                                  const double4_32a* __restrict__ params,
+                                                  const double* __restrict__ params, int stride,
                                                   const double* __restrict__ r_cut,
                                                   const double* __restrict__ r_extrap,
                                                   const __grid_constant__ WallField wf, uint32_t N,
@@ -33,8 +39,8 @@ __global__ void __launch_bounds__(kBlock) k_walls(const double4_32a* __restrict_
     if (i >= N) return;
     const double4_32a pp = pos[i];
     const uint32_t t = type_of(pp.w);
-    const double4_32a rec = params[t];
-    const double p[4] = {rec.x, rec.y, rec.z, rec.w};
+    double p[4];
+    load_wall_record(params, t, stride, p);
     const double rc = __ldg(r_cut + t);
     const double x[3] = {pp.x, pp.y, pp.z};
     double F[3] = {0.0, 0.0, 0.0}, U = 0.0;
@@ -53,7 +59,7 @@ __global__ void __launch_bounds__(kBlock) k_walls(const double4_32a* __restrict_
 // (walls.cuh), per-type float records made once per block in shared memory
 template<class EV, class EVF>
 __global__ void __launch_bounds__(kBlock) k_walls_f(const double4_32a* __restrict__ pos,
-                                                    const double4_32a* __restrict__ params,
+                                                    const double* __restrict__ params, int stride,
                                                     const double* __restrict__ r_cut,
                                                     const double* __restrict__ r_extrap, uint32_t ntypes,
                                                     const __grid_constant__ WallField wf, uint32_t N,
@@ -62,8 +68,8 @@ __global__ void __launch_bounds__(kBlock) k_walls_f(const double4_32a* __restric
 {
     extern __shared__ float s_q[];
     for (uint32_t t = threadIdx.x; t < ntypes; t += kBlock) {
-        const double4_32a rec = params[t];
-        const double p[4] = {rec.x, rec.y, rec.z, rec.w};
+        double p[4];
+        load_wall_record(params, t, stride, p);
         wall_record_f<EV>(p, r_cut[t], r_extrap[t], s_q + (size_t)t * WALL_F);
     }
     __syncthreads();
@@ -82,20 +88,19 @@ __global__ void __launch_bounds__(kBlock) k_walls_f(const double4_32a* __restric
 }
 
 template<class EV, class EVF>
-void launch_walls(const azp_system* sys, const double* params, const double* r_cut, const double* r_extrap,
-                  const WallField& wf, const azp_forces* out, cudaStream_t s)
+void launch_walls(const azp_system* sys, const double* params, int stride, const double* r_cut,
+                  const double* r_extrap, const WallField& wf, const azp_forces* out, cudaStream_t s)
 {
     const uint32_t grid = (sys->N + kBlock - 1) / kBlock;
     const uint32_t pitch = out->virial_pitch ? out->virial_pitch : sys->N;
     const auto* pos = reinterpret_cast<const double4_32a*>(sys->pos);
-    const auto* par = reinterpret_cast<const double4_32a*>(params);
     if (out->precision == AZP_FP64)
-        k_walls<EV, double><<<grid, kBlock, 0, s>>>(pos, par, r_cut, r_extrap, wf, sys->N,
+        k_walls<EV, double><<<grid, kBlock, 0, s>>>(pos, params, stride, r_cut, r_extrap, wf, sys->N,
                                                     static_cast<double*>(out->force),
                                                     static_cast<double*>(out->virial), pitch);
     else
         k_walls_f<EV, EVF><<<grid, kBlock, sizeof(float) * WALL_F * sys->ntypes, s>>>(
-            pos, par, r_cut, r_extrap, sys->ntypes, wf, sys->N, static_cast<float*>(out->force),
+            pos, params, stride, r_cut, r_extrap, sys->ntypes, wf, sys->N, static_cast<float*>(out->force),
             static_cast<float*>(out->virial), pitch);
 }
 
@@ -153,7 +158,8 @@ extern "C" {
 int azp_wall_params_from_values(int kind, const double* v, double* out)
 {
     if (!v || !out) return AZP_ERR_INVALID;
-    for (int k = 0; k < 4; ++k) out[k] = 0.0;
+    if (kind != AZP_WALL_LJ93 && kind != AZP_WALL_COLLOID) return AZP_ERR_INVALID;
+    for (int k = 0; k < azp::wall_record_doubles(kind); ++k) out[k] = 0.0;
     if (kind == AZP_WALL_LJ93) {
         // WallParametersLJ93(dict): sigma_3 = sigma^3, A
         const double A = v[0], sigma = v[1];
@@ -208,9 +214,10 @@ int azp_wall_forces(const azp_system* sys, int kind, const azp_walls* walls, con
     cudaStream_t s = as_stream(stream);
     if (sys->ntypes == 0 || sys->ntypes > 4096) return AZP_ERR_INVALID;
     if (kind == AZP_WALL_LJ93)
-        launch_walls<WallLJ93, WallLJ93F>(sys, params, r_cut, r_extrap, wf, out, s);
+        launch_walls<WallLJ93, WallLJ93F>(sys, params, wall_record_doubles(kind), r_cut, r_extrap, wf, out, s);
     else
-        launch_walls<WallColloid, WallColloidF>(sys, params, r_cut, r_extrap, wf, out, s);
+        launch_walls<WallColloid, WallColloidF>(sys, params, wall_record_doubles(kind), r_cut, r_extrap, wf, out,
+                                                s);
     AZP_CHECK_LAUNCH("k_walls");
     return AZP_OK;
 }

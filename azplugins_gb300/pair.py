@@ -44,10 +44,12 @@ class Pair:
         return _lib.PAIR_KINDS[self._name]
 
     def _tables(self, types):
-        """Host tables for ``types``: records [nt*nt*4], r_cut [nt*nt], r_on [nt*nt]."""
+        """Host tables for ``types``: records [nt, nt, d] (d doubles per record, the
+        reference's param_type size), r_cut [nt, nt], r_on [nt, nt]."""
         L = _lib.load()
         nt = len(types)
-        rec = np.zeros((nt, nt, 4))
+        d_rec = _lib.record_doubles(_lib.RECORD_PAIR, self.kind)
+        rec = np.zeros((nt, nt, d_rec))
         rc = np.zeros((nt, nt))
         ro = np.zeros((nt, nt))
         for a in range(nt):
@@ -57,7 +59,7 @@ class Pair:
                     raise KeyError(f"{type(self).__name__}.params{key} is not set")
                 d = self.params[key]
                 vals = np.ascontiguousarray([d[k] for k in self._keys], dtype=np.float64)
-                out = np.zeros(4)
+                out = np.zeros(d_rec)
                 _lib.check(L.azp_pair_params_from_values(self.kind, vals.ctypes.data, out.ctypes.data), "params")
                 rec[a, b] = out
                 rc[a, b] = self.r_cut[key] if key in self.r_cut else 0.0

@@ -131,10 +131,12 @@ class WallPotential:
         return _lib.WALL_KINDS[self._name]
 
     def _tables(self, types):
-        """Host tables for ``types``: records [nt, 4], r_cut [nt], r_extrap [nt]."""
+        """Host tables for ``types``: records [nt, d] (the reference's param_type
+        size in doubles), r_cut [nt], r_extrap [nt]."""
         L = _lib.load()
         nt = len(types)
-        rec = np.zeros((nt, 4))
+        d_rec = _lib.record_doubles(_lib.RECORD_WALL, self.kind)
+        rec = np.zeros((nt, d_rec))
         rc = np.zeros(nt)
         rx = np.zeros(nt)
         for a, name in enumerate(types):
@@ -142,7 +144,7 @@ class WallPotential:
                 raise KeyError(f"{type(self).__name__}.params[{name!r}] is not set")
             d = self.params[name]
             vals = np.ascontiguousarray([d[k] for k in self._keys], dtype=np.float64)
-            out = np.zeros(4)
+            out = np.zeros(d_rec)
             _lib.check(L.azp_wall_params_from_values(self.kind, vals.ctypes.data, out.ctypes.data), "wall params")
             rec[a] = out
             rc[a] = d["r_cut"]
@@ -169,12 +171,6 @@ class WallPotential:
         w.n_spheres, w.n_cylinders, w.n_planes = len(sp), len(cy), len(pl)
         w.spheres, w.cylinders, w.planes = (ctypes.cast(k, ctypes.c_void_p) for k in keep)
         return w, keep
-
-    def _oracle_walls(self):
-        """Rows of the walls in the oracle's layout (test helper)."""
-        return (np.array([w._row() for w in self.walls if isinstance(w, Sphere)]).reshape(-1, 6),
-                np.array([w._row() for w in self.walls if isinstance(w, Cylinder)]).reshape(-1, 9),
-                np.array([w._row() for w in self.walls if isinstance(w, Plane)]).reshape(-1, 7))
 
     def record_to_dict(self, rec):
         """asDict() of a param_type record (the reference round trip)."""

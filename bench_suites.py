@@ -451,7 +451,9 @@ def suite_drivers(args):
     rec, rc, rx = pot._tables(["A", "B"])
     walls, keep = pot._walls_struct()
     wdev = [torch.from_numpy(np.ascontiguousarray(a).reshape(-1).copy()).cuda() for a in (rec, rc, rx)]
-    sp, cy, pl = pot._oracle_walls()
+    from tests.helpers import oracle_walls
+
+    sp, cy, pl = oracle_walls(pot)
     for prec in ("fp64", "fp32"):
         force, vir, out = _forces_out(N, prec, torch)
 

@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define AZP_ABI_VERSION 1
+#define AZP_ABI_VERSION 2
 
 /* every entry point is exported; everything else in the library is hidden */
 #if defined(__GNUC__)
@@ -102,22 +102,45 @@ enum azp_method { AZP_METHOD_LANGEVIN_FLOW = 0, AZP_METHOD_BROWNIAN_FLOW = 1 };
 #define AZP_RNG_LANGEVIN_FLOW 202u
 
 /* ------------------------------------------------------------------ parameter structs
- * Field names and order of the reference param_type structs. Every pair record
- * is padded to 4 doubles (32 bytes, the reference's aligned(32)), every bond
- * record to 8 doubles; tables are indexed [type_i * ntypes + type_j] (pairs,
- * symmetric) or [bond_type] (bonds). */
+ * Field names, order and size of the reference param_type structs in HOOMD's
+ * default double-precision build (HOOMD_LONGREAL_SIZE 64): sizeof is 32 bytes
+ * (aligned(32)) for PerturbedLJ, ExpandedYukawa, Colloid, DPDGeneralWeight and
+ * DoubleWell, 8 for Hertz (aligned(8)), 64 for Quartic, 16 for the ImageHarmonic
+ * (HOOMD harmonic bond) record, 16 for the LJ93 wall and 32 for the Colloid wall
+ * (src/PairEvaluatorPerturbedLennardJones.h:57-66, src/PairEvaluatorHertz.h:41-47,
+ * src/BondEvaluatorDoubleWell.h:52-61, src/WallEvaluatorLJ93.h:50-58, ...).
+ * Every table an entry point takes is an array of these records at that stride
+ * (azp_record_size), indexed [type_i * ntypes + type_j] (pairs, symmetric),
+ * [bond_type] (bonds) or [type] (walls): HOOMD's GPUArray<param_type> passes
+ * straight through. A single-precision HOOMD build (Scalar = float) converts its
+ * table with azp_params_from_single first. */
 typedef struct { double sigma_6, epsilon_x_4, attraction_scale_factor, rwcasq; } azp_params_perturbed_lj;
 typedef struct { double epsilon, kappa, delta, pad_; } azp_params_expanded_yukawa;
-typedef struct { double epsilon, pad_[3]; } azp_params_hertz;
+typedef struct { double epsilon; } azp_params_hertz;
 typedef struct { double A, a_1, a_2, sigma_3; } azp_params_colloid;
 typedef struct { double A, gamma, s, pad_; } azp_params_dpd_general_weight;
 typedef struct { double k, r_0, b_1, b_2, U_0, sigma_6, epsilon_x_4, delta; } azp_params_quartic;
-typedef struct { double r_1, r_diff, U_1, U_tilt, pad_[4]; } azp_params_double_well;
+typedef struct { double r_1, r_diff, U_1, U_tilt; } azp_params_double_well;
+typedef struct { double k, r_0; } azp_params_harmonic;
 
+/* largest record, in doubles, of any pair / bond kind (buffer sizes) */
 #define AZP_PAIR_PARAM_DOUBLES 4
 #define AZP_BOND_PARAM_DOUBLES 8
 
+/* record classes of azp_record_size / azp_params_from_single */
+enum azp_record_class { AZP_RECORD_PAIR = 0, AZP_RECORD_BOND = 1, AZP_RECORD_WALL = 2 };
+/* Bytes of one param_type record of (record class, kind): single == 0 gives the
+ * double-precision layout every table argument uses, single != 0 the layout of a
+ * HOOMD build with Scalar = float (aligned(16) / aligned(8) / aligned(4)
+ * variants). Negative (AZP_ERR_INVALID) for an unknown class or kind. */
+AZP_API int azp_record_size(int record_class, int kind, int single);
+/* Widen n records of a single-precision HOOMD build (host memory, the layout
+ * azp_record_size(cls, kind, 1) gives) into the double-precision layout the entry
+ * points take (host memory, azp_record_size(cls, kind, 0) bytes each). */
+AZP_API int azp_params_from_single(int record_class, int kind, const void* src, uint32_t n, double* dst);
+
 /* Dict constructor / asDict of each param_type, host-only, no device work.
+ * record: one record of azp_record_size(class, kind, 0) bytes.
  * values[] holds the Python parameter dict in this key order:
  *   PerturbedLennardJones: epsilon, sigma, attraction_scale_factor
  *   ExpandedYukawa:        epsilon, kappa, delta
@@ -208,7 +231,7 @@ AZP_API int azp_nlist_download(const azp_nlist* nl, uint32_t* counts, uint32_t* 
 
 /* ------------------------------------------------------------------ force drivers
  * Pair forces over the list (replaces gpu_compute_pair_forces<Eval>).
- * params: device table [ntypes*ntypes] of 4-double param_type records;
+ * params: device table [ntypes*ntypes] of param_type records;
  * r_cut / r_on: device tables [ntypes*ntypes] (r_on may be NULL).
  * Overwrites out->force (and virial). Uses nl as its workspace (type-pair table,
  * FP32 fixed-point shadow): stream-ordered, no allocation, no synchronisation. */
@@ -229,9 +252,14 @@ AZP_API int azp_nlist_set_tpp(azp_nlist* nl, int tpp);
  * Its scratch (type-pair table, FP32 position shadow) is one static device array
  * of this library, about 4.1 MB, held on every GPU that loads the library until
  * the process exits. Limits: N <= AZP_STATIC_MAX_N (else AZP_ERR_TOO_LARGE with a
- * message in azp_last_error) and ntypes <= 16.
- * The first call on a device looks the array's address up for that device (with
- * that device current); make that first call before any stream capture.
+ * message in azp_last_error) and ntypes <= 16 (else AZP_ERR_INVALID).
+ * Preconditions, as for any caller-built list: every neighbors[k * N + i] with
+ * k < min(counts[i], max_neighbors) is a particle index < N, and every type in
+ * pos.w is < ntypes; the kernels read without range checks.
+ * Every call looks the array's address up for the current device (with that
+ * device current); the first call on a device may load the library's device code
+ * there, so make that first call before any stream capture. Nothing is cached
+ * between calls, so a device reset in between is harmless.
  * Calls share the array: two calls whose kernels overlap on the GPU (different
  * streams, or different host threads, on one device) race on it. Every call
  * rewrites what it reads, so nothing carries over from the previous call. */
@@ -285,7 +313,7 @@ AZP_API int azp_harmonic_barrier_forces(const azp_system* sys, int geometry, dou
  * and plane normals need not be unit (they are normalised). A particle exactly at
  * a sphere's centre or on a cylinder's axis takes the surface point along a fixed
  * direction (+x; the first normal of the axis).
- * params: device [ntypes][4] records (azp_params_wall_*); r_cut, r_extrap: device
+ * params: device [ntypes] records (azp_params_wall_*); r_cut, r_extrap: device
  * [ntypes]. OVERWRITES out->force (fx, fy, fz, energy) and out->virial
  * (F_a x_b, may be NULL). FP64 output: FP64 arithmetic. FP32 output: FP32
  * arithmetic except x - origin and R^2 - r^2 (FP64), so distances keep FP32
@@ -303,8 +331,8 @@ typedef struct {
     const azp_wall_cylinder* cylinders; /* host */
     const azp_wall_plane* planes;       /* host */
 } azp_walls;
-/* param_type records, 4 doubles (src/WallEvaluatorLJ93.h:31-56, src/WallEvaluatorColloid.h:31-64) */
-typedef struct { double sigma_3, A, pad_[2]; } azp_params_wall_lj93;
+/* param_type records (src/WallEvaluatorLJ93.h:31-58: 16 bytes, src/WallEvaluatorColloid.h:31-67: 32 bytes) */
+typedef struct { double sigma_3, A; } azp_params_wall_lj93;
 typedef struct { double c_1, c_2, a, pad_; } azp_params_wall_colloid;
 /* dict constructor / asDict: values LJ93 {A, sigma}, Colloid {A, a, sigma} */
 AZP_API int azp_wall_params_from_values(int kind, const double* values, double* record);
@@ -344,7 +372,7 @@ AZP_API int azp_vfield_error(azp_vfield* vf, uint32_t* err_word, void* stream);
 /* Bond forces from a per-particle bond table (replaces
  * gpu_compute_bond_forces<Eval,2>): for particle i its bonds are
  * table[k * N + i] = (partner index, bond type) for k < n_bonds[i].
- * params: device table [nbondtypes] of 8-double records. ACCUMULATES into out.
+ * params: device table [nbondtypes] of param_type records. ACCUMULATES into out.
  * FP32 precision evaluates in FP32 on the FP64 minimum-image displacement.
  * AZP_BOND_IMAGE_HARMONIC (src/ImagePotentialBond.h:57-204) measures the
  * image-unwrapped displacement (x_i - x_j) + (img_i - img_j) L instead and needs
@@ -405,14 +433,14 @@ typedef struct {
     /* pair */
     int32_t pair_kind;          /* -1: no pair force */
     int32_t shift_mode;
-    const double* pair_params;  /* host [ntypes*ntypes][4] param_type records */
+    const double* pair_params;  /* host [ntypes*ntypes] param_type records */
     const double* r_cut;        /* host [ntypes*ntypes] */
     const double* r_on;         /* host [ntypes*ntypes] or NULL */
     double r_buff;
     /* bonds */
     int32_t bond_kind;          /* -1: no bond force */
     uint32_t nbondtypes;
-    const double* bond_params;  /* host [nbondtypes][8] */
+    const double* bond_params;  /* host [nbondtypes] param_type records */
     uint32_t nbonds;
     const uint32_t* bonds;      /* host [nbonds][2] tags */
     const uint32_t* bond_types; /* host [nbonds] */
@@ -438,7 +466,7 @@ typedef struct {
      * semantics of azp_wall_forces */
     int32_t wall_kind;          /* azp_wall_kind (read when walls is set) */
     const azp_walls* walls;     /* host; NULL: no walls */
-    const double* wall_params;  /* host [ntypes][4] records */
+    const double* wall_params;  /* host [ntypes] param_type records */
     const double* wall_r_cut;   /* host [ntypes] */
     const double* wall_r_extrap; /* host [ntypes] */
     /* pair_kind AZP_PAIR_DPD_GENERAL_WEIGHT: the thermostat temperature (the
@@ -507,7 +535,7 @@ typedef struct {
     int32_t precision;
     int32_t pair_kind;
     int32_t shift_mode;
-    const double* pair_params;  /* host [nsys][4] param_type records */
+    const double* pair_params;  /* host [nsys] param_type records */
     const double* r_cut;        /* host [nsys] */
     double r_buff;
     double dt, kT, gamma;

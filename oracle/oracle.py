@@ -129,6 +129,20 @@ def _ptr(a):
 
 
 # ------------------------------------------------------------------ evaluators
+def _records(params, width):
+    """A parameter table as the oracle's flat array: the last axis padded with
+    zeros to ``width`` values per record (4 for pair and wall records, 8 for
+    bonds), so tables at the reference's param_type strides and the oracle's
+    own padded ones are both accepted."""
+    a = np.asarray(params, dtype=np.float64)
+    if a.ndim == 0:
+        a = a.reshape(1)
+    if a.shape[-1] < width:
+        pad = np.zeros(a.shape[:-1] + (width - a.shape[-1],))
+        a = np.concatenate([a, pad], axis=-1)
+    return np.ascontiguousarray(a).reshape(-1)
+
+
 def pair_params(name: str, d: dict) -> np.ndarray:
     """The reference param_type fields built from a parameter dict (padded to 4)."""
     vals = np.array([float(d[k]) for k in PAIR_KEYS[name]], dtype=np.float64)
@@ -226,7 +240,7 @@ def pair_forces(pos4, types, ntypes, L, start, idx, name, params, rcutsq, ronsq=
         np.ascontiguousarray(start, dtype=np.int32),
         np.ascontiguousarray(idx, dtype=np.int32),
         PAIR_KINDS[name],
-        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        _records(params, 4),
         PAIR_STRIDE,
         np.ascontiguousarray(rcutsq, dtype=np.float64).reshape(-1),
         _ptr(ron),
@@ -257,7 +271,7 @@ def dpd_forces(pos4, vel4, types, tags, ntypes, L, start, idx, params, rcutsq, k
         np.ascontiguousarray(L, dtype=np.float64),
         np.ascontiguousarray(start, dtype=np.int32),
         np.ascontiguousarray(idx, dtype=np.int32),
-        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        _records(params, 4),
         np.ascontiguousarray(rcutsq, dtype=np.float64).reshape(-1),
         float(kT),
         float(dt),
@@ -299,7 +313,7 @@ def wall_forces(pos4, types, name, params, rcut, rextrap, spheres=(), cylinders=
         np.ascontiguousarray(pos4, dtype=np.float64),
         np.ascontiguousarray(types, dtype=np.int32),
         WALL_KINDS[name],
-        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        _records(params, 4),
         np.ascontiguousarray(rcut, dtype=np.float64).reshape(-1),
         np.ascontiguousarray(rextrap, dtype=np.float64).reshape(-1),
         len(sp), sp.reshape(-1) if len(sp) else np.zeros(1),
@@ -377,7 +391,7 @@ def image_bond_forces(pos4, image, L, bonds, btypes, name, params):
         N, np.ascontiguousarray(pos4, dtype=np.float64), np.ascontiguousarray(image, dtype=np.int32).reshape(-1),
         np.ascontiguousarray(L, dtype=np.float64), len(bonds), bonds.reshape(-1),
         np.ascontiguousarray(btypes, dtype=np.int32), BOND_KINDS[name],
-        np.ascontiguousarray(params, dtype=np.float64).reshape(-1), BOND_STRIDE, F, U, _ptr(W))
+        _records(params, 8), BOND_STRIDE, F, U, _ptr(W))
     if bad:
         raise ValueError(f"bond {bad - 1} refused")
     return F, U, W
@@ -398,7 +412,7 @@ def bond_forces(pos4, L, bonds, btypes, name, params, F=None, U=None, W=None):
         bonds,
         np.ascontiguousarray(btypes, dtype=np.int32),
         BOND_KINDS[name],
-        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        _records(params, 8),
         BOND_STRIDE,
         F,
         U,
@@ -433,7 +447,7 @@ def bond_forces_pp(pos4, L, table, name, params, F, U, W=None):
         partner,
         btype,
         BOND_KINDS[name],
-        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        _records(params, 8),
         BOND_STRIDE,
         F,
         U,
@@ -456,7 +470,7 @@ def image_bond_forces_pp(pos4, image, L, table, name, params, F, U, W=None):
         partner,
         btype,
         BOND_KINDS[name],
-        np.ascontiguousarray(params, dtype=np.float64).reshape(-1),
+        _records(params, 8),
         BOND_STRIDE,
         F,
         U,

@@ -2,15 +2,21 @@
 // reference's header-only evaluator and flow-field functors on the host for the
 // oracle pin (oracle/_ref). Test infrastructure; never linked into the product.
 //
-// Scalar is double (HOOMD_LONGREAL_SIZE == 64). __host__/__device__ expand to
-// nothing because ConstantFlow.h / ParabolicFlow.h emit them in host builds.
+// Scalar is double (HOOMD_LONGREAL_SIZE == 64); with AZP_REF_SINGLE defined it is
+// float (HOOMD_LONGREAL_SIZE == 32, HOOMD's single-precision build), used only to
+// take sizeof of the param_type records (oracle/ref_sizes.cpp). __host__/__device__
+// expand to nothing because ConstantFlow.h / ParabolicFlow.h emit them in host builds.
 #ifndef AZP_REF_SHIM_HOOMDMATH_H_
 #define AZP_REF_SHIM_HOOMDMATH_H_
 
 #include <cmath>
 #include <cstdint>
 
+#ifdef AZP_REF_SINGLE
+#define HOOMD_LONGREAL_SIZE 32
+#else
 #define HOOMD_LONGREAL_SIZE 64
+#endif
 #ifndef __host__
 #define __host__
 #endif
@@ -20,16 +26,20 @@
 
 namespace hoomd
     {
+#ifdef AZP_REF_SINGLE
+typedef float Scalar;
+#else
 typedef double Scalar;
+#endif
 struct Scalar3
     {
-    double x, y, z;
+    Scalar x, y, z;
     };
 struct Scalar4
     {
-    double x, y, z, w;
+    Scalar x, y, z, w;
     };
-inline Scalar3 make_scalar3(double x, double y, double z)
+inline Scalar3 make_scalar3(Scalar x, Scalar y, Scalar z)
     {
     return Scalar3 {x, y, z};
     }
@@ -48,6 +58,22 @@ inline double exp(double x)
     return std::exp(x);
     }
 inline double pow(double x, double y)
+    {
+    return std::pow(x, y);
+    }
+inline float sqrt(float x)
+    {
+    return std::sqrt(x);
+    }
+inline float rsqrt(float x)
+    {
+    return 1.0f / std::sqrt(x);
+    }
+inline float exp(float x)
+    {
+    return std::exp(x);
+    }
+inline float pow(float x, float y)
     {
     return std::pow(x, y);
     }

@@ -82,7 +82,9 @@ def _walk(stmts, env, case, stage):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AZP_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_barrier_kats.py <azplugins source tree> (or set AZP_REFERENCE_ROOT)")
     path = os.path.join(root, "src", "pytest", "test_external.py")
     tree = ast.parse(open(path).read())
     out = {"source": "src/pytest/test_external.py"}

@@ -54,7 +54,9 @@ def image_bond_cases(path):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AZP_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_kats.py <azplugins source tree> (or set AZP_REFERENCE_ROOT)")
     pair = cases(os.path.join(root, "src", "pytest", "test_pair.py"),
                  ["params", "r_cut", "shift", "distance", "energy", "force"])
     bond = cases(os.path.join(root, "src", "pytest", "test_bond.py"), ["params", "distance", "energy", "force"])

@@ -6,13 +6,18 @@ distances, the reference's (evaluated, force/r, energy), its param_type fields
 and asDict round trip, and the flow-field values. The fixture travels to
 machines without the reference tree; tests compare the oracle and the GPU to it.
 
-Usage: python tests/golden/make_ref_vectors.py
+Also records sizeof(param_type) of every evaluator in the reference's double- and
+single-precision layouts (``oracle/_ref/ref_sizes_*``), which pins the C ABI's
+record strides.
+
+Usage: python tests/golden/make_ref_vectors.py (after oracle/build_ref.sh)
 """
 
 from __future__ import annotations
 
 import json
 import os
+import subprocess
 import sys
 
 import numpy as np
@@ -91,9 +96,16 @@ def main():
         out = azp_ref.parabolic_flow(mv, sep, r)
         flow.append(dict(kind="parabolic", mean_velocity=mv, separation=sep, r=r, u=list(out[:3]),
                          get_mean_velocity=out[3], get_separation=out[4]))
+    # sizeof(param_type) of every evaluator, double- and single-precision HOOMD
+    # builds, printed by oracle/ref_sizes.cpp compiled from the reference headers
+    sizes = {}
+    for tag in ("double", "single"):
+        exe = os.path.join(REPO, "oracle", "_ref", f"ref_sizes_{tag}")
+        sizes[tag] = json.loads(subprocess.run([exe], check=True, capture_output=True, text=True).stdout)
     with open(os.path.join(HERE, "ref_vectors.json"), "w") as f:
-        json.dump({"generator": "tests/golden/make_ref_vectors.py", "pair": pair, "bond": bond, "flow": flow}, f)
-    print(f"{len(pair)} pair, {len(bond)} bond, {len(flow)} flow vectors")
+        json.dump({"generator": "tests/golden/make_ref_vectors.py", "pair": pair, "bond": bond, "flow": flow,
+                   "record_bytes": sizes}, f)
+    print(f"{len(pair)} pair, {len(bond)} bond, {len(flow)} flow vectors; record sizes {sizes}")
 
 
 if __name__ == "__main__":

@@ -129,3 +129,13 @@ def image_chains(seed=111, n_chains=300, length=12, L=(6.0, 7.0, 5.0)):
     bonds = np.array([[c * length + k, c * length + k + 1] for c in range(n_chains) for k in range(length - 1)])
     btypes = rng.integers(0, 2, size=len(bonds)).astype(np.int32)
     return pos, img, un, bonds, btypes, L
+
+
+def oracle_walls(pot):
+    """Rows of a wall potential's walls in the oracle's layout: spheres [n, 6],
+    cylinders [n, 9], planes [n, 7]."""
+    from azplugins_gb300.wall import Cylinder, Plane, Sphere
+
+    return (np.array([w._row() for w in pot.walls if isinstance(w, Sphere)]).reshape(-1, 6),
+            np.array([w._row() for w in pot.walls if isinstance(w, Cylinder)]).reshape(-1, 9),
+            np.array([w._row() for w in pot.walls if isinstance(w, Plane)]).reshape(-1, 7))

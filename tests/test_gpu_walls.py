@@ -21,7 +21,7 @@ import numpy as np
 import pytest
 
 import azplugins_gb300 as az
-from helpers import force_error, load_golden, oracle_system, rel
+from helpers import force_error, load_golden, oracle_system, oracle_walls, rel
 
 pytestmark = pytest.mark.gpu
 KATS = load_golden("kats.json")["wall"]
@@ -86,7 +86,7 @@ def test_driver_matches_oracle(orc, name):
         pot.params["B"] = dict(A=4.0, a=1.0, sigma=1.0, r_cut=3.5, r_extrap=1.4)
         pot.params["C"] = dict(A=0.3, a=0.3, sigma=0.9, r_cut=2.0, r_extrap=0.5)
     rec, rc, rx = pot._tables(["A", "B", "C"])
-    sp, cy, pl = pot._oracle_walls()
+    sp, cy, pl = oracle_walls(pot)
     # the standard form diverges at the surface: redraw the few particles whose
     # wall force would leave the FP32 range
     for _ in range(10):
@@ -160,7 +160,7 @@ def _run(orc, snap, precision, method, pot, steps, dt, seed):
     sim.run(steps - steps // 2)
     rec = orc.pair_params("PerturbedLennardJones", dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.5))
     wrec, wrc, wrx = pot._tables(["A", "B"])
-    sp, cy, pl = pot._oracle_walls()
+    sp, cy, pl = oracle_walls(pot)
     md = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
                       pair=dict(name="PerturbedLennardJones", params=np.tile(rec, (2, 2, 1)),
                                 rcut=np.full((2, 2), 2.5), mode="none"),
@@ -187,7 +187,7 @@ def test_engine_langevin_slit(orc, precision, tol):
     sim, md = _run(orc, snap, precision, "langevin", pot, 60, 0.004, seed=91)
     F_md, U_md, W_md = md.forces()
     Fw, Uw, _ = orc.wall_forces(md.s["pos4"], md.s["types"], "LJ93", *pot._tables(["A", "B"]),
-                                planes=pot._oracle_walls()[2])
+                                planes=oracle_walls(pot)[2])
     assert (Uw != 0).sum() > 50  # the walls act on the layers next to them
     assert _unwrapped_err(sim, md, L) < tol
     f, w = sim._engine.forces()

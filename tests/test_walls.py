@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import azplugins_gb300 as az
-from helpers import load_golden
+from helpers import load_golden, oracle_walls
 
 KATS = load_golden("kats.json")["wall"]
 PLANE_Z = [[0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 1.0]]  # hoomd.wall.Plane(origin=(0, 0, 0), normal=(0, 0, 1))
@@ -101,9 +101,10 @@ def test_front_end():
     rec, rc, rx = lj._tables(["A", "B"])
     np.testing.assert_array_equal(rc, [3.0, 2.0])
     np.testing.assert_array_equal(rx, [0.0, 0.4])
-    np.testing.assert_allclose(rec[1], [0.125, 2.0, 0.0, 0.0])
+    # LJ93 records are 16 bytes (sigma_3, A), as the reference param_type
+    np.testing.assert_allclose(rec[1], [0.125, 2.0])
     assert lj.record_to_dict(rec[1]) == pytest.approx(dict(A=2.0, sigma=0.5))
-    s, c, p = lj._oracle_walls()
+    s, c, p = oracle_walls(lj)
     np.testing.assert_allclose(p[0], [0, 0, 0, 0, 0, 1, 1])
     assert s.shape == (1, 6) and c.shape == (1, 9)
     with pytest.raises(KeyError):

@@ -97,6 +97,11 @@ def _both(inp, precision):
 
 def _compare(f_ref, w_ref, f_st, w_st, tol):
     assert np.isfinite(f_st).all() and np.isfinite(w_st).all()
+    # the same kernels with the same threads per particle on the same inputs:
+    # bit-identical results (a stale byte of the shared array would show here)
+    assert np.array_equal(f_st, f_ref)
+    assert np.array_equal(w_st, w_ref)
+    # and, as a diagnostic, within the tolerance the other GPU tests use
     assert force_error(f_st, f_ref) <= tol
     assert rel(f_st[:, 3].sum(), f_ref[:, 3].sum()) <= tol
     for c in range(6):
@@ -144,3 +149,24 @@ def test_static_entry_rejects_too_many_particles():
                                   ctypes.byref(out), None)
     assert st == -11
     assert b"262144" in L.azp_last_error()
+
+
+def test_static_entry_rejects_too_many_types():
+    """ntypes above the static table's 16 is refused before any device work."""
+    from azplugins_gb300 import _lib
+
+    L = _lib.load()
+    s = _lib.System()
+    s.N = 100
+    s.ntypes = 17
+    s.pos = 1  # never dereferenced: the type check comes first
+    for d in range(3):
+        s.box.L[d] = 100.0
+    out = _lib.Forces()
+    out.force = 1
+    out.precision = _lib.FP64
+    one = np.zeros(17 * 17 * 4)
+    st = L.azp_pair_forces_static(ctypes.byref(s), None, None, 0, 0, one.ctypes.data, one.ctypes.data, None, 0,
+                                  ctypes.byref(out), None)
+    assert st == -1
+
