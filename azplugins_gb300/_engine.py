@@ -45,7 +45,7 @@ class Engine:
         if len(integ.methods) != 1 or not isinstance(integ.methods[0], (LangevinFlow, BrownianFlow)):
             raise NotImplementedError("exactly one LangevinFlow or BrownianFlow method is required")
         m = integ.methods[0]
-        parts = [sim.precision, sim.seed, integ.dt, type(m).__name__, m.kT, m.noiseless, m.alpha,
+        parts = [sim.precision, sim.seed, integ.dt, type(m).__name__, m.kT, repr(m.filter), m.noiseless, m.alpha,
                  getattr(m, "max_displacement", 0.0), getattr(m, "force_cap", 0.0), repr(m.flow_field), sorted(m.gamma.items()),
                  m.gamma.default]
         if pair is not None:
@@ -114,7 +114,10 @@ class Engine:
             c.bond_kind = -1
         c.method = _lib.METHOD_BROWNIAN if isinstance(m, BrownianFlow) else _lib.METHOD_LANGEVIN
         c.dt = integ.dt
-        c.kT = m.kT
+        # a varying temperature is tabulated run by run (azp_md_set_temperatures)
+        self._kT = m.kT
+        c.kT = m.kT_constant if m.kT_constant is not None else float(m.kT(0))
+        c.group_types = m._group_types(types)
         c.seed = sim.seed
         c.noiseless = int(m.noiseless)
         c.gamma = arr(m._gamma_table(types))
@@ -205,19 +208,35 @@ class Engine:
         _lib.check(self._L.azp_md_set_barrier_locations(self._md, int(t0), len(vals), vals.ctypes.data, _stream()),
                    "azp_md_set_barrier_locations")
 
+    def _set_temperature(self, t0, steps):
+        """Tabulate a varying kT for the timesteps a run of ``steps`` from ``t0``
+        integrates (step two and the Brownian move of timestep t use kT(t))."""
+        kT = self._kT
+        if hasattr(kT, "values"):
+            vals = np.asarray(kT.values(t0, steps + 1), dtype=np.float64)
+        else:
+            vals = np.array([float(kT(t)) for t in range(t0, t0 + steps + 1)], dtype=np.float64)
+        vals = np.ascontiguousarray(vals)
+        _lib.check(self._L.azp_md_set_temperatures(self._md, int(t0), len(vals), vals.ctypes.data, _stream()),
+                   "azp_md_set_temperatures")
+
     def _chunks(self, steps):
-        """Runs of at most BARRIER_ROWS - 1 steps when a moving barrier is tabulated."""
+        """Runs of at most BARRIER_ROWS - 1 steps when a moving barrier or a varying
+        temperature is tabulated."""
         steps = int(steps)
-        if self._barrier is None:
-            yield steps
-            return
-        if isinstance(self._barrier.location, Constant):
-            self._set_barrier(self.timestep, steps)
+        moving = self._barrier is not None and not isinstance(self._barrier.location, Constant)
+        varying = not isinstance(self._kT, Constant)
+        if not moving and not varying:
+            if self._barrier is not None:
+                self._set_barrier(self.timestep, steps)
             yield steps
             return
         while steps > 0:
             n = min(steps, BARRIER_ROWS - 1)
-            self._set_barrier(self.timestep, n)
+            if self._barrier is not None:
+                self._set_barrier(self.timestep, n if moving else 0)
+            if varying:
+                self._set_temperature(self.timestep, n)
             yield n
             steps -= n
 

@@ -158,6 +158,7 @@ class MDConfig(ctypes.Structure):
         ("wall_r_cut", ctypes.c_void_p),
         ("wall_r_extrap", ctypes.c_void_p),
         ("dpd_kT", ctypes.c_double),
+        ("group_types", ctypes.c_uint32),
     ]
 
 
@@ -237,6 +238,7 @@ _SIGNATURES = [
     ("azp_md_set_state", _i, [_vp, _vp, _vp, _vp, _vp, _vp, _u64, _i, _vp]),
     ("azp_md_get_state", _i, [_vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64), _i, _vp]),
     ("azp_md_set_barrier_locations", _i, [_vp, _u64, _u32, _vp, _vp]),
+    ("azp_md_set_temperatures", _i, [_vp, _u64, _u32, _vp, _vp]),
     ("azp_md_run", _i, [_vp, _u64, _vp]),
     ("azp_md_run_checked", _i, [_vp, _u64, _vp]),
     ("azp_md_forces", _i, [_vp, _vp, _vp, _i, _vp]),

@@ -150,11 +150,15 @@ __global__ void k_arm(const uint32_t* __restrict__ flags, cudaGraphConditionalHa
 __global__ void k_md_step1(double4_32a* __restrict__ pos, uint4* __restrict__ fix, const uint4* __restrict__ fix_build,
                            double4_32a* __restrict__ vel, const double* __restrict__ accel, int* __restrict__ image,
                            uint32_t N, double dt, double L0, double L1, double L2, double Li0, double Li1, double Li2,
-                           float s0, float s1, float s2, float thresh2, uint32_t* __restrict__ flags)
+                           float s0, float s1, float s2, float thresh2, uint32_t* __restrict__ flags,
+                           uint32_t group_types)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool want = false;
-    if (i < N) {
+    // a particle outside the method's group does not move
+    const bool mover = i < N && (group_types == 0xffffffffu ||
+                                 (type_of(pos[i].w) < 32u && ((group_types >> type_of(pos[i].w)) & 1u)));
+    if (mover) {
         double4_32a p = pos[i];
         double4_32a v = vel[i];
         const double ax = accel[3 * i], ay = accel[3 * i + 1], az = accel[3 * i + 2];
@@ -196,11 +200,14 @@ __global__ void k_md_step1(double4_32a* __restrict__ pos, uint4* __restrict__ fi
 __global__ void k_md_step1_fx(uint4* __restrict__ fix, uint4* __restrict__ lo, const uint4* __restrict__ fix_build,
                               VelFF* __restrict__ vel, const double* __restrict__ accel, int* __restrict__ image,
                               uint32_t N, float dt, float3 s64h, float3 s64l, float3 sfix, float thresh2,
-                              uint32_t* __restrict__ flags)
+                              uint32_t* __restrict__ flags, uint32_t group_types)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool want = false;
-    if (i < N) {
+    // a particle outside the method's group does not move
+    const bool mover = i < N && (group_types == 0xffffffffu ||
+                                 (fix[i].w < 32u && ((group_types >> fix[i].w) & 1u)));
+    if (mover) {
         uint4 f = fix[i];
         uint4 l = lo[i];
         VelFF v = vel[i];
@@ -550,6 +557,13 @@ struct azp_md {
     WallField* d_walls = nullptr;
     double* d_wall_tab = nullptr;
     float wall_tol = 0.0f;
+    // integration group by type (0xffffffff: every particle)
+    uint32_t group_types = 0xffffffffu;
+    // temperature table of a varying kT (allocated on the first
+    // azp_md_set_temperatures; null while kT is the constant of the config)
+    unsigned long long* d_kT_hdr = nullptr;
+    double* d_kT_tab = nullptr;
+    double* d_noise_tab = nullptr;
     // DPD: kT of the thermostat and the step's velocity snapshot
     double dpd_kT = 0.0;
     double* d_dvel = nullptr;
@@ -620,7 +634,8 @@ void free_all(azp_md* m)
                     m->d_bond_params, m->d_pair_table, m->d_gamma, m->d_noise, m->flags, m->d_ts, m->out_force, m->out_virial,
                     m->partials, m->thermo, m->tmp4, m->tmpd, m->snap_pos, m->snap_vel, m->snap_acc,
                     m->snap_img, m->snap_diam, m->st_pos, m->st_vel, m->st_acc, m->st_img, m->st_diam,
-                    m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab, m->d_dvel, m->d_img0};
+                    m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab, m->d_dvel, m->d_img0,
+                    m->d_kT_hdr, m->d_kT_tab, m->d_noise_tab};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -717,6 +732,10 @@ MDArgs base_args(azp_md* m)
     a.wall_tol = m->wall_tol;
     a.dvel = m->d_dvel;
     a.img0 = m->d_img0;
+    a.group_types = m->group_types;
+    a.kT_hdr = m->d_kT_hdr;
+    a.kT_tab = m->d_kT_tab;
+    a.noise_tab = m->d_noise_tab;
     a.flowf.kind = m->flow.kind;
     if (m->flow.kind == AZP_FLOW_PARABOLIC) {
         a.flowf.a = (float)m->flow.a;
@@ -820,7 +839,7 @@ int enqueue_step1(azp_md* m, cudaStream_t s)
         k_md_step1_fx<<<blocks_for(m->N, 256), 256, 0, s>>>(
             m->fix[m->cur], m->lo[m->cur], m->fix_build, a.velf, m->accel, m->image, m->N, a.dtf,
             make_float3(a.s64h[0], a.s64h[1], a.s64h[2]), make_float3(a.s64l[0], a.s64l[1], a.s64l[2]),
-            make_float3(a.sfix[0], a.sfix[1], a.sfix[2]), a.disp_thresh2, m->flags);
+            make_float3(a.sfix[0], a.sfix[1], a.sfix[2]), a.disp_thresh2, m->flags, a.group_types);
         AZP_CHECK_LAUNCH("k_md_step1_fx");
         m->launches += 1;
         return AZP_OK;
@@ -829,7 +848,8 @@ int enqueue_step1(azp_md* m, cudaStream_t s)
         m->pos[m->cur], m->fix[m->cur], m->fix_build, m->vel, m->accel, m->image, m->N, m->dt, m->box.L[0],
         m->box.L[1], m->box.L[2], 1.0 / m->box.L[0], 1.0 / m->box.L[1], 1.0 / m->box.L[2],
         (float)(m->box.L[0] * 2.3283064365386963e-10), (float)(m->box.L[1] * 2.3283064365386963e-10),
-        (float)(m->box.L[2] * 2.3283064365386963e-10), (float)(half * half * (1.0 - 1e-5)), m->flags);
+        (float)(m->box.L[2] * 2.3283064365386963e-10), (float)(half * half * (1.0 - 1e-5)), m->flags,
+        m->group_types);
     AZP_CHECK_LAUNCH("k_md_step1");
     m->launches += 1;
     return AZP_OK;
@@ -1031,6 +1051,10 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     m->r_buff = c->r_buff;
     m->dt = c->dt;
     m->kT = c->kT;
+    if (c->group_types != 0u) {
+        if (c->ntypes > 32u) return fail(AZP_ERR_INVALID, m);
+        m->group_types = c->group_types;
+    }
     m->seed = c->seed;
     m->noiseless = c->noiseless;
     m->use_lambda = c->use_lambda;
@@ -1427,6 +1451,41 @@ int azp_md_set_barrier_locations(azp_md* m, uint64_t t_first, uint32_t n, const 
     AZP_CUDA_TRY(cudaStreamSynchronize(s));
     m->bar_set = true;
     m->forces_valid = false;
+    return AZP_OK;
+}
+
+int azp_md_set_temperatures(azp_md* m, uint64_t t_first, uint32_t n, const double* kT, void* stream)
+{
+    if (!m || n == 0 || !kT) return AZP_ERR_INVALID;
+    if (n > AZP_MD_KT_ROWS) {
+        const std::string msg = "azp_md_set_temperatures: " + std::to_string(n) + " rows exceed the table of " +
+                                std::to_string(AZP_MD_KT_ROWS) + " (set the temperatures run by run)";
+        return record_error(AZP_ERR_TOO_LARGE, msg.c_str());
+    }
+    for (uint32_t r = 0; r < n; ++r)
+        if (!(kT[r] >= 0.0) || !std::isfinite(kT[r])) return record_error(AZP_ERR_INVALID, "kT must be finite and >= 0");
+    const uint32_t nt = m->ntypes;
+    if (!m->d_kT_hdr) {
+        // first table: allocate it, and drop the captured graphs, whose step
+        // arguments were taken without one
+        int st = dalloc(&m->d_kT_hdr, 2);
+        if (!st) st = dalloc(&m->d_kT_tab, AZP_MD_KT_ROWS);
+        if (!st) st = dalloc(&m->d_noise_tab, (size_t)AZP_MD_KT_ROWS * nt);
+        if (st) return st;
+        free_graphs(m);
+    }
+    // noise amplitude per (row, type) with the operations of the reference's
+    // step two, sqrt(6 gamma kT / dt) (src/TwoStepLangevinFlow.h:213-215)
+    std::vector<double> noise((size_t)n * nt, 0.0);
+    if (!m->noiseless)
+        for (uint32_t r = 0; r < n; ++r)
+            for (uint32_t t = 0; t < nt; ++t) noise[(size_t)r * nt + t] = std::sqrt(6.0 * m->gamma[t] * kT[r] / m->dt);
+    const unsigned long long hdr[2] = {(unsigned long long)t_first, (unsigned long long)n};
+    cudaStream_t s = as_stream(stream);
+    AZP_CUDA_TRY(cudaMemcpyAsync(m->d_kT_tab, kT, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    AZP_CUDA_TRY(cudaMemcpyAsync(m->d_noise_tab, noise.data(), sizeof(double) * noise.size(), cudaMemcpyHostToDevice, s));
+    AZP_CUDA_TRY(cudaMemcpyAsync(m->d_kT_hdr, hdr, sizeof(hdr), cudaMemcpyHostToDevice, s));
+    AZP_CUDA_TRY(cudaStreamSynchronize(s));
     return AZP_OK;
 }
 

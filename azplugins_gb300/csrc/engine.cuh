@@ -100,7 +100,27 @@ struct MDArgs {
     // ImageHarmonic bonds: the image counts of the step's start ([N][3], a
     // snapshot for the same reason: the step updates image[] in place)
     const int* img0;
+    // integration group by type (bit t: type t moves); 0xffffffff: every particle
+    uint32_t group_types;
+    // temperature table (kT_hdr null: the constant kT and noise above): row r
+    // holds timestep kT_hdr[0] + r, clamped to the kT_hdr[1] rows
+    const unsigned long long* kT_hdr;
+    const double* kT_tab;       // [rows] kT
+    const double* noise_tab;    // [rows][ntypes] sqrt(6 gamma kT / dt), 0 when noiseless
 };
+
+// does the method move particles of type t?
+AZP_D bool in_group(const MDArgs& a, uint32_t t)
+{
+    return a.group_types == 0xffffffffu || (t < 32u && ((a.group_types >> t) & 1u));
+}
+
+// row of timestep ts in the temperature table
+AZP_D size_t kT_row(const MDArgs& a, unsigned long long ts)
+{
+    const unsigned long long t0 = a.kT_hdr[0], rows = a.kT_hdr[1];
+    return (size_t)(ts <= t0 ? 0ull : min(ts - t0, rows - 1ull));
+}
 
 constexpr int MD_INTEG_LANGEVIN = 0;
 constexpr int MD_INTEG_BROWNIAN = 1;

@@ -522,7 +522,15 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
                 // amplitude sqrt(6 gamma kT / dt) comes from a host table built with
                 // the same double operations, so the draws stay bit-exact
                 const double gam = a.use_lambda ? a.lambda * a.diameter[i] : s_gamma[ti];
-                const double c = a.noiseless ? 0.0 : (a.use_lambda ? sqrt(6.0 * gam * a.kT / a.dt) : s_noise[ti]);
+                // the method's temperature at this timestep (a table when it varies)
+                double kTv = a.kT, nz = a.use_lambda ? 0.0 : s_noise[ti];
+                if (a.kT_hdr) {
+                    const size_t r = kT_row(a, ts);
+                    kTv = a.kT_tab[r];
+                    nz = a.noise_tab[r * a.ntypes + ti];
+                }
+                const double c = a.noiseless ? 0.0 : (a.use_lambda ? sqrt(6.0 * gam * kTv / a.dt) : nz);
+                const bool mover = in_group(a, ti);
                 double ux, uy, uz;
                 flow_at(a.flow, p.y, ux, uy, uz);
                 double r0, r1, r2;
@@ -534,19 +542,23 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
                     const double ay = (Fy + (r1 - gam * (v.y - uy))) * minv;
                     const double az = (Fz + (r2 - gam * (v.z - uz))) * minv;
                     const double h = 0.5 * a.dt;
-                    v.x += h * ax;
-                    v.y += h * ay;
-                    v.z += h * az;
-                    if (a.next) {
-                        // step one of the next timestep with the acceleration just computed
-                        p.x += (v.x + h * ax) * a.dt;
-                        p.y += (v.y + h * ay) * a.dt;
-                        p.z += (v.z + h * az) * a.dt;
+                    if (mover) {
                         v.x += h * ax;
                         v.y += h * ay;
                         v.z += h * az;
+                    }
+                    if (a.next) {
+                        // step one of the next timestep with the acceleration just computed
+                        if (mover) {
+                            p.x += (v.x + h * ax) * a.dt;
+                            p.y += (v.y + h * ay) * a.dt;
+                            p.z += (v.z + h * az) * a.dt;
+                            v.x += h * ax;
+                            v.y += h * ay;
+                            v.z += h * az;
+                        }
                         moved = true;
-                    } else {
+                    } else if (mover) {
                         a.accel[3 * i] = ax;
                         a.accel[3 * i + 1] = ay;
                         a.accel[3 * i + 2] = az;
@@ -562,9 +574,11 @@ __global__ void __launch_bounds__(MD_BLOCK) k_md_step(MDArgs a)
                         dy = fmin(fmax(dy, -a.max_disp), a.max_disp);
                         dz = fmin(fmax(dz, -a.max_disp), a.max_disp);
                     }
-                    p.x += dx;
-                    p.y += dy;
-                    p.z += dz;
+                    if (mover) {
+                        p.x += dx;
+                        p.y += dy;
+                        p.z += dz;
+                    }
                     moved = true;
                 }
                 if (moved) {
@@ -630,6 +644,14 @@ AZP_D bool inside_exact(const MDArgs& a, uint32_t i, uint32_t j, double rc2)
     return rsq_exact(vx, vy, vz) < rc2;
 }
 
+// exact minimum-image displacement of one axis from the 64-bit fixed positions
+// (the wrapping 64-bit difference), in FP64 (one rounding)
+AZP_D double fx_disp(uint32_t hi_i, uint32_t lo_i, uint32_t hi_j, uint32_t lo_j, double l64)
+{
+    const long long d = (long long)((unsigned long long)fx_join(hi_i, lo_i) - (unsigned long long)fx_join(hi_j, lo_j));
+    return (double)d * l64;
+}
+
 template<class PE>
 AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j,
                         const float* s_rec, const double* s_rc2, AccFx& acc, bool vir)
@@ -645,11 +667,71 @@ AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint3
     if (rsq >= rc2 * 1.000004f || !PE::enabled(rec)) return;
     if (rsq >= rc2 * 0.999996f && !inside_exact(a, i, j, s_rc2[tp])) return;
     float fdr, e;
-    PE::eval(rec, rsq, fdr, e);
+    if constexpr (has_gap_form<PE>::value) {
+        if (PE::gap_form(rec)) {
+            // the cancelling contact difference (colloid point-sphere and
+            // sphere-sphere forms) in FP64 from the exact 64-bit displacement
+            const uint4 li = __ldg(a.flo + i), lj = __ldg(a.flo + j);
+            const double vx = fx_disp(fi.x, li.x, fj.x, lj.x, a.l64[0]);
+            const double vy = fx_disp(fi.y, li.y, fj.y, lj.y, a.l64[1]);
+            const double vz = fx_disp(fi.z, li.z, fj.z, lj.z, a.l64[2]);
+            const double rsq_d = vx * vx + vy * vy + vz * vz;
+            const double dq = PE::contact2(a.pair_table + (size_t)tp * PAIR_TBL) - rsq_d;
+            PE::eval_gap(rec, (float)rsq_d, (float)dq, fdr, e);
+        } else {
+            PE::eval(rec, rsq, fdr, e);
+        }
+    } else {
+        PE::eval(rec, rsq, fdr, e);
+    }
     e -= rec[PE::SHIFT_SLOT];
     xplor(cut, rsq, fdr, e);
     if (a.fcapf > 0.0f && fdr * fdr * rsq > a.fcapf * a.fcapf) fdr = copysignf(a.fcapf * rsqrtf(rsq), fdr);
     acc.add(dx, dy, dz, fdr, e, vir);
+}
+
+// pair_term_fx for a candidate that may be a padding slot (ok false) or lie
+// outside r_cut: the evaluator runs on every lane (at r_cut where the pair does
+// not count) and the pair's terms are masked, so a batch has no per-lane exits;
+// only the rare candidate in the band around r_cut takes the exact FP64 branch
+template<class PE>
+AZP_D void pair_term_fx_masked(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j, bool ok,
+                               const float* s_rec, const double* s_rc2, AccFx& acc, bool vir)
+{
+    const float dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
+    const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
+    const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
+    const float rsq = dx * dx + dy * dy + dz * dz;
+    const uint32_t tp = fi.w * a.ntypes + fj.w;
+    const float* rec = s_rec + (size_t)tp * PAIR_TBL;
+    const float* cut = rec + PAIR_REC;
+    const float rc2 = cut[0];
+    const bool on = ok && PE::enabled(rec);
+    bool in = on && rsq < rc2 * 0.999996f;
+    if (on && !in && rsq < rc2 * 1.000004f) in = inside_exact(a, i, j, s_rc2[tp]);
+    const float rs = in ? rsq : rc2;
+    float fdr, e;
+    if constexpr (has_gap_form<PE>::value) {
+        if (in && PE::gap_form(rec)) {
+            // the cancelling contact difference (colloid point-sphere and
+            // sphere-sphere forms) in FP64 from the exact 64-bit displacement
+            const uint4 li = __ldg(a.flo + i), lj = __ldg(a.flo + j);
+            const double vx = fx_disp(fi.x, li.x, fj.x, lj.x, a.l64[0]);
+            const double vy = fx_disp(fi.y, li.y, fj.y, lj.y, a.l64[1]);
+            const double vz = fx_disp(fi.z, li.z, fj.z, lj.z, a.l64[2]);
+            const double rsq_d = vx * vx + vy * vy + vz * vz;
+            const double dq = PE::contact2(a.pair_table + (size_t)tp * PAIR_TBL) - rsq_d;
+            PE::eval_gap(rec, (float)rsq_d, (float)dq, fdr, e);
+        } else {
+            PE::eval(rec, rs, fdr, e);
+        }
+    } else {
+        PE::eval(rec, rs, fdr, e);
+    }
+    e -= rec[PE::SHIFT_SLOT];
+    xplor(cut, rs, fdr, e);
+    if (a.fcapf > 0.0f && fdr * fdr * rs > a.fcapf * a.fcapf) fdr = copysignf(a.fcapf * rsqrtf(rs), fdr);
+    acc.add(dx, dy, dz, in ? fdr : 0.0f, in ? e : 0.0f, vir);
 }
 
 // DPD pair in the FP32-force step: FP32 on the exact fixed-point displacement,
@@ -779,6 +861,58 @@ constexpr int FX_BATCH = AZP_FX_BATCH;
 #define AZP_FX_MIN_BLOCKS 4
 #endif
 
+// prefetch of the DRAM rows a warp's particles read (0 off, 1 into L1, 2 into L2)
+#ifndef AZP_FX_PREFETCH
+#define AZP_FX_PREFETCH 1
+#endif
+// neighbour batches walked to the warp's longest row with masked lanes instead of
+// per-lane loop exits and early returns
+#ifndef AZP_FX_UNIFORM
+#define AZP_FX_UNIFORM 1
+#endif
+
+AZP_D void prefetch_line(const void* p)
+{
+#if AZP_FX_PREFETCH == 1
+    asm volatile("prefetch.L1 [%0];" ::"l"(p));
+#elif AZP_FX_PREFETCH == 2
+    asm volatile("prefetch.L2 [%0];" ::"l"(p));
+#else
+    (void)p;
+#endif
+}
+
+// Prefetch, by one instruction per lane, the lines of the warp's particles
+// [i0, i_last] that the step reads from DRAM (velocities, low position words,
+// build shadow, tags, bond counts, the first two bond-table columns) and the
+// first nmax columns of their list rows, so that those latencies overlap at
+// the start instead of chaining behind the neighbour loop. Addresses stay
+// inside the arrays: every one is clamped to the warp's last particle.
+AZP_D void prefetch_warp_rows(const MDArgs& a, uint32_t i0, uint32_t i_last, uint32_t nmax, bool bonds)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    if (lane < nmax) {
+        prefetch_line(a.nbrs + (size_t)lane * a.N + i0);
+        prefetch_line(a.nbrs + (size_t)lane * a.N + i_last);
+    }
+    const void* p = nullptr;
+    if (lane < 8u) {
+        p = a.velf + min(i0 + lane * 4u, i_last);
+    } else if (lane < 12u) {
+        p = a.flo + min(i0 + (lane - 8u) * 8u, i_last);
+    } else if (lane < 16u) {
+        p = a.fix_build + min(i0 + (lane - 12u) * 8u, i_last);
+    } else if (lane < 18u) {
+        p = a.tag + (lane == 16u ? i0 : i_last);
+    } else if (bonds && lane < 20u) {
+        p = a.bt_n + (lane == 18u ? i0 : i_last);
+    } else if (bonds && lane < 26u) {
+        const uint32_t c = (lane - 20u) / 3u, part = (lane - 20u) % 3u;
+        p = a.bt + (size_t)c * a.N + min(i0 + part * 16u, i_last);
+    }
+    if (p) prefetch_line(p);
+}
+
 // ONE: single-type system, records from the kernel arguments (no shared-memory
 // tables, no block barrier before the work)
 template<class PE, class BE, int INTEG, bool OUT, bool ONE>
@@ -838,11 +972,26 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
     }
     AccFx acc;
     uint4 fi = make_uint4(0u, 0u, 0u, 0u);
+    uint32_t n = 0u;
+    if constexpr (!std::is_same<PE, NoPair>::value) n = active ? min(__ldg(a.counts + i), a.max_nn) : 0u;
+#if AZP_FX_PREFETCH || AZP_FX_UNIFORM
+    // the warp's longest list row
+    const uint32_t nmax = __reduce_max_sync(0xffffffffu, n);
+#endif
+#if AZP_FX_PREFETCH
+    {
+        const uint32_t i0 = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) >> a.tpp_shift;
+        if (i0 < a.N) {
+            const uint32_t i_last = min(i0 + (32u >> a.tpp_shift) - 1u, a.N - 1u);
+            prefetch_warp_rows(a, i0, i_last, std::is_same<PE, NoPair>::value ? 0u : nmax,
+                               !std::is_same<BE, NoBond>::value);
+        }
+    }
+#endif
     if (active) {
         fi = __ldg(a.fix + i);
         // ---------------------------------------------------------------- pair
         if constexpr (!std::is_same<PE, NoPair>::value) {
-            const uint32_t n = min(__ldg(a.counts + i), a.max_nn);
             const uint32_t* col = a.nbrs + i;
             uint32_t k0 = 0, k1 = 0, tgi = 0;
             float4 vi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -851,7 +1000,14 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
                 tgi = __ldg(a.tag + i);
                 vi = reinterpret_cast<const float4*>(a.dvel)[i];
             }
-            for (uint32_t kb = sub; kb < n; kb += FX_BATCH * tpp) {
+#if AZP_FX_UNIFORM
+            // every lane walks to the warp's longest row; slots past a lane's own
+            // row are masked (no per-lane loop exit)
+            const uint32_t kend = std::is_same<PE, DpdEngine>::value ? n : nmax;
+#else
+            const uint32_t kend = n;
+#endif
+            for (uint32_t kb = sub; kb < kend; kb += FX_BATCH * tpp) {
                 uint32_t jj[FX_BATCH];
                 uint4 fj[FX_BATCH];
 #pragma unroll
@@ -862,13 +1018,18 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
 #pragma unroll
                 for (int u = 0; u < FX_BATCH; ++u) fj[u] = __ldg(a.fix + jj[u]);
 #pragma unroll
-                for (int u = 0; u < FX_BATCH; ++u)
-                    if (kb + u * tpp < n) {
-                        if constexpr (std::is_same<PE, DpdEngine>::value)
+                for (int u = 0; u < FX_BATCH; ++u) {
+                    if constexpr (std::is_same<PE, DpdEngine>::value) {
+                        if (kb + u * tpp < n)
                             pair_term_dpd_fx(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir, vi, tgi, k0, k1);
-                        else
-                            pair_term_fx<PE>(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir);
+                    } else {
+#if AZP_FX_UNIFORM
+                        pair_term_fx_masked<PE>(a, fi, fj[u], i, jj[u], kb + u * tpp < n, s_rec, s_rc2, acc, vir);
+#else
+                        if (kb + u * tpp < n) pair_term_fx<PE>(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir);
+#endif
                     }
+                }
                 acc.commit(vir);
             }
         }
@@ -933,7 +1094,15 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
             const float fy = acc.fy.s + (acc.fy.c + (fb[1] + fw.y));
             const float fz = acc.fz.s + (acc.fz.c + (fb[2] + fw.z));
             const float gam = a.use_lambda ? a.lambdaf * (float)a.diameter[i] : s_gamma[ti];
-            const float c = a.noiseless ? 0.0f : (a.use_lambda ? sqrtf(6.0f * gam * a.kTf / a.dtf) : s_noise[ti]);
+            // the method's temperature at this timestep (a table when it varies)
+            float kTv = a.kTf, nz = a.use_lambda ? 0.0f : s_noise[ti];
+            if (a.kT_hdr) {
+                const size_t r = kT_row(a, ts);
+                kTv = (float)a.kT_tab[r];
+                nz = (float)a.noise_tab[r * a.ntypes + ti];
+            }
+            const float c = a.noiseless ? 0.0f : (a.use_lambda ? sqrtf(6.0f * gam * kTv / a.dtf) : nz);
+            const bool mover = in_group(a, ti);
             float ux, uy, uz;
             flow_at_ff(a.flowf, (float)(int32_t)fi.y * a.sfix[1], ux, uy, uz);
             const float dt = a.dtf;
@@ -942,7 +1111,7 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
             if constexpr (INTEG == MD_INTEG_LANGEVIN) {
                 uniform3f(AZP_RNG_LANGEVIN_FLOW, ts, a.seed, tg, -c, 2.0f * c, r0, r1, r2);
                 VelFF v = a.velf[i];
-                const float minv = v.h.w;
+                const float minv = mover ? v.h.w : 0.0f;  // a particle outside the group keeps its velocity
                 const float ax = (fx + (r0 - gam * (v.h.x - ux))) * minv;
                 const float ay = (fy + (r1 - gam * (v.h.y - uy))) * minv;
                 const float az = (fz + (r2 - gam * (v.h.z - uz))) * minv;
@@ -950,9 +1119,10 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
                     // v(t + dt/2) = v(t - dt/2) + dt a: the half kick of step two and of
                     // step one; then x += v(t + dt/2) dt
                     const float kx = dt * ax, ky = dt * ay, kz = dt * az;
-                    ddx = (v.h.x + kx) * dt;
-                    ddy = (v.h.y + ky) * dt;
-                    ddz = (v.h.z + kz) * dt;
+                    const float mdt = mover ? dt : 0.0f;
+                    ddx = (v.h.x + kx) * mdt;
+                    ddy = (v.h.y + ky) * mdt;
+                    ddz = (v.h.z + kz) * mdt;
                     ff_add(v.h.x, v.l.x, kx);
                     ff_add(v.h.y, v.l.y, ky);
                     ff_add(v.h.z, v.l.z, kz);
@@ -970,9 +1140,10 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
             } else {
                 uniform3f(AZP_RNG_BROWNIAN_FLOW, ts, a.seed, tg, -c, 2.0f * c, r0, r1, r2);
                 const float gi = 1.0f / gam;
-                ddx = (ux + (fx + r0) * gi) * dt;
-                ddy = (uy + (fy + r1) * gi) * dt;
-                ddz = (uz + (fz + r2) * gi) * dt;
+                const float mdt = mover ? dt : 0.0f;
+                ddx = (ux + (fx + r0) * gi) * mdt;
+                ddy = (uy + (fy + r1) * gi) * mdt;
+                ddz = (uz + (fz + r2) * gi) * mdt;
                 if (a.max_dispf > 0.0f) {
                     const float m = a.max_dispf;
                     ddx = fminf(fmaxf(ddx, -m), m);

@@ -143,9 +143,53 @@ struct Colloid {
         return g * xi;
     }
 
-    template<typename R> AZP_HD static void eval(const R* rec, R rsq, R& fdr, R& e)
+    // point -- sphere of radius a, with d = a^2 - rsq supplied
+    template<typename R> AZP_HD static void cs_form(const R* rec, R rsq, R d, R& fdr, R& e)
     {
         const R A = rec[0], s3 = rec[3], s6 = rec[4];
+        const R a = rec[6];
+        const R a2 = a * a;
+        const R d3 = d * d * d;
+        const R d6 = d3 * d3;
+        const R r4 = rsq * rsq;
+        const R pre = s3 * A * a * a2 / d3;
+        const R poly = R(2) * (a2 + rsq) * (a2 * (R(5) * a2 + R(22) * rsq) + R(5) * r4);
+        fdr = R(4.0 / 15.0) * pre * (poly * s6 / d6 - R(5)) / d;
+        const R poly_e = a2 * (a2 * (a2 / R(3) + R(3) * rsq) + R(4.2) * r4) + rsq * r4;
+        e = R(2.0 / 9.0) * pre * (R(1) - poly_e * s6 / d6);
+    }
+
+    // sphere -- sphere (Everaers & Ejtehadi, PRE 67, 041710), with r = sqrt(rsq)
+    // and the surface gap sm = (a_1 + a_2) - r supplied
+    template<typename R> AZP_HD static void cc_form(const R* rec, R r, R sm, R& fdr, R& e)
+    {
+        const R A = rec[0], s6 = rec[4];
+        const R ai = rec[1], aj = rec[2];
+        const R prod = ai * aj, sum = ai + aj, dif = ai - aj;
+        const R sp = sum + r, dp = dif + r, dm = dif - r;
+        const R q7 = rcp(sp * sm);
+        const R q8 = rcp(dp * dm);
+        R g0 = inv7(sp), g1 = inv7(sm), g2 = inv7(dp), g3 = inv7(dm);
+        const R h0 = ((sp + R(5) * sum) * sp + R(30) * prod) * g0;
+        const R h1 = ((sm + R(5) * sum) * sm + R(30) * prod) * g1;
+        const R h2 = ((dp + R(5) * dif) * dp - R(30) * prod) * g2;
+        const R h3 = ((dm + R(5) * dif) * dm - R(30) * prod) * g3;
+        const R pre = A * s6 / r / R(37800);
+        R u = pre * (h0 - h1 - h2 + h3);
+        g0 *= R(42) * prod / sp + R(6) * sum + sp;
+        g1 *= R(42) * prod / sm + R(6) * sum + sm;
+        g2 *= R(-42) * prod / dp + R(6) * dif + dp;
+        g3 *= R(-42) * prod / dm + R(6) * dif + dm;
+        const R dur = u / r + R(5) * pre * (g0 + g1 - g2 - g3);
+        const R dua = -A / R(3) * r * ((R(2) * prod * q7 + R(1)) * q7 + (R(2) * prod * q8 - R(1)) * q8);
+        fdr = (dur + dua) / r;
+        u += A / R(6) * (R(2) * prod * (q7 + q8) - log(q8 / q7));
+        e = u;
+    }
+
+    template<typename R> AZP_HD static void eval(const R* rec, R rsq, R& fdr, R& e)
+    {
+        const R A = rec[0], s6 = rec[4];
         const int form = (int)rec[5];
         if (form == 0) {
             // integrated over no sphere: LJ with prefactor A/36
@@ -155,44 +199,44 @@ struct Colloid {
             fdr = R(6) * c * r2inv * r6inv * (R(2) * s6 * r6inv - R(1));
             e = c * r6inv * (s6 * r6inv - R(1));
         } else if (form == 1) {
-            // point -- sphere of radius a
             const R a = rec[6];
-            const R a2 = a * a;
-            const R d = a2 - rsq;
-            const R d3 = d * d * d;
-            const R d6 = d3 * d3;
-            const R r4 = rsq * rsq;
-            const R pre = s3 * A * a * a2 / d3;
-            const R poly = R(2) * (a2 + rsq) * (a2 * (R(5) * a2 + R(22) * rsq) + R(5) * r4);
-            fdr = R(4.0 / 15.0) * pre * (poly * s6 / d6 - R(5)) / d;
-            const R poly_e = a2 * (a2 * (a2 / R(3) + R(3) * rsq) + R(4.2) * r4) + rsq * r4;
-            e = R(2.0 / 9.0) * pre * (R(1) - poly_e * s6 / d6);
+            cs_form(rec, rsq, a * a - rsq, fdr, e);
         } else {
-            // sphere -- sphere (Everaers & Ejtehadi, PRE 67, 041710)
-            const R ai = rec[1], aj = rec[2];
             const R r = sqrt(rsq);
-            const R prod = ai * aj, sum = ai + aj, dif = ai - aj;
-            const R sp = sum + r, sm = sum - r, dp = dif + r, dm = dif - r;
-            const R q7 = rcp(sp * sm);
-            const R q8 = rcp(dp * dm);
-            R g0 = inv7(sp), g1 = inv7(sm), g2 = inv7(dp), g3 = inv7(dm);
-            const R h0 = ((sp + R(5) * sum) * sp + R(30) * prod) * g0;
-            const R h1 = ((sm + R(5) * sum) * sm + R(30) * prod) * g1;
-            const R h2 = ((dp + R(5) * dif) * dp - R(30) * prod) * g2;
-            const R h3 = ((dm + R(5) * dif) * dm - R(30) * prod) * g3;
-            const R pre = A * s6 / r / R(37800);
-            R u = pre * (h0 - h1 - h2 + h3);
-            g0 *= R(42) * prod / sp + R(6) * sum + sp;
-            g1 *= R(42) * prod / sm + R(6) * sum + sm;
-            g2 *= R(-42) * prod / dp + R(6) * dif + dp;
-            g3 *= R(-42) * prod / dm + R(6) * dif + dm;
-            const R dur = u / r + R(5) * pre * (g0 + g1 - g2 - g3);
-            const R dua = -A / R(3) * r * ((R(2) * prod * q7 + R(1)) * q7 + (R(2) * prod * q8 - R(1)) * q8);
-            fdr = (dur + dua) / r;
-            u += A / R(6) * (R(2) * prod * (q7 + q8) - log(q8 / q7));
-            e = u;
+            cc_form(rec, r, (rec[1] + rec[2]) - r, fdr, e);
         }
     }
+
+    // Forms whose arguments cancel near contact: point-sphere (a^2 - r^2) and
+    // sphere-sphere ((a_1 + a_2) - r). Their forces fall off like the ninth or
+    // higher power of that difference, so in FP32 a difference formed from a
+    // rounded r^2 loses the force budget a fraction of sigma from contact.
+    template<typename R> AZP_HD static bool gap_form(const R* rec) { return rec[5] != R(0); }
+    // squared contact distance of the form, from the FP64 record: a^2 or (a_1 + a_2)^2
+    AZP_HD static double contact2(const double* rec_d)
+    {
+        const double c = rec_d[5] == 1.0 ? rec_d[6] : rec_d[1] + rec_d[2];
+        return c * c;
+    }
+    // FP32 evaluation of a gap form with rsq and dq = contact^2 - rsq formed by
+    // the caller in FP64 from an exact displacement, each rounded once to FP32:
+    // the point-sphere d is dq, the sphere-sphere gap is dq / (a_1 + a_2 + r).
+    AZP_D static void eval_gap(const float* rec, float rsq, float dq, float& fdr, float& e)
+    {
+        if (rec[5] == 1.0f) {
+            cs_form(rec, rsq, dq, fdr, e);
+        } else {
+            const float r = sqrtf(rsq);
+            cc_form(rec, r, dq / ((rec[1] + rec[2]) + r), fdr, e);
+        }
+    }
+};
+
+template<class E> struct has_gap_form {
+    static constexpr bool value = false;
+};
+template<> struct has_gap_form<Colloid> {
+    static constexpr bool value = true;
 };
 
 // Host: fill the kernel record and cut record of one type pair.

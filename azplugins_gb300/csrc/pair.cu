@@ -183,7 +183,25 @@ __global__ void __launch_bounds__(PAIR_BLOCK) k_pair(PairArgs a)
                     if (!(rsq_exact(vx, vy, vz) < s_rc2[tp])) continue;
                 }
                 R fdr, e;
-                Eval::eval(rec, (R)rsq, fdr, e);
+                if constexpr (has_gap_form<Eval>::value) {
+                    if (Eval::gap_form(rec)) {
+                        // the cancelling contact difference from the FP64
+                        // positions, rounded once (colloid point-sphere and
+                        // sphere-sphere forms)
+                        const double4_32a pi = a.pos[i];
+                        const double4_32a pj = a.pos[j];
+                        const double vx = min_image1(pi.x - pj.x, a.L[0], a.Linv[0]);
+                        const double vy = min_image1(pi.y - pj.y, a.L[1], a.Linv[1]);
+                        const double vz = min_image1(pi.z - pj.z, a.L[2], a.Linv[2]);
+                        const double rsq_d = vx * vx + vy * vy + vz * vz;
+                        const double dq = Eval::contact2(a.table + (size_t)tp * PAIR_TBL) - rsq_d;
+                        Eval::eval_gap(rec, (float)rsq_d, (float)dq, fdr, e);
+                    } else {
+                        Eval::eval(rec, (R)rsq, fdr, e);
+                    }
+                } else {
+                    Eval::eval(rec, (R)rsq, fdr, e);
+                }
                 e -= rec[Eval::SHIFT_SLOT];
                 xplor(cut, (R)rsq, fdr, e);
                 acc.add((R)dx, (R)dy, (R)dz, fdr, e);

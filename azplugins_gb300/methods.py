@@ -7,26 +7,35 @@ field, seed, use_lambda / lambda, noiseless) whose Python front end was removed
 (``CHANGELOG.rst:300-303`` records the v0 ``flow.langevin`` / ``flow.brownian``).
 These classes give that integrator a HOOMD-v4-style front end:
 
+* ``filter``: the particles the method integrates, ``"all"`` / ``filter.All()``
+  or ``filter.Type(types)`` (the reference's ParticleGroup, src/TwoStepLangevinFlow.h:35;
+  particles outside it feel and exert forces but do not move);
 * ``gamma[type]`` per-type drag (``default_gamma``), or ``alpha`` for
   gamma = alpha * diameter (the reference's use_lambda / lambda);
-* ``kT`` is a constant (a HOOMD Variant is not supported);
+* ``kT`` is a float or a variant of the timestep (the reference's
+  ``std::shared_ptr<Variant> T``, evaluated at the timestep of step two,
+  src/TwoStepLangevinFlow.h:194-219);
 * the RNG seed is the Simulation's seed.
 """
 
 from __future__ import annotations
 
+from . import filter as _filter
 from .flow import FlowField
 from .typeparam import TypeParameterDict
+from .variant import Constant, as_variant
 
 
 class _FlowMethod:
     def __init__(self, filter, kT, flow_field, default_gamma=1.0, alpha=None, noiseless=False):
-        if filter not in (None, "all"):
-            raise ValueError("only the whole system (filter='all') is supported")
+        if filter in (None, "all"):
+            filter = _filter.All()
+        if not isinstance(filter, (_filter.All, _filter.Type)):
+            raise ValueError("the method's group is filter.All() or filter.Type(types)")
         if not isinstance(flow_field, FlowField):
             raise TypeError("flow_field must be an azplugins_gb300.flow.FlowField")
-        self.filter = "all"
-        self.kT = float(kT)
+        self.filter = filter
+        self.kT = as_variant(kT)
         self.flow_field = flow_field
         self.noiseless = bool(noiseless)
         self.alpha = None if alpha is None else float(alpha)
@@ -35,6 +44,23 @@ class _FlowMethod:
 
     def _gamma_table(self, types):
         return [self.gamma[t] for t in types]
+
+    def _group_types(self, types):
+        """Bit mask of the integrated types (0: every particle)."""
+        if isinstance(self.filter, _filter.All):
+            return 0
+        if len(types) > 32:
+            raise ValueError("filter.Type groups need at most 32 particle types")
+        mask = 0
+        for k, t in enumerate(types):
+            if t in self.filter.types:
+                mask |= 1 << k
+        return mask
+
+    @property
+    def kT_constant(self):
+        """The temperature when it does not vary, else None."""
+        return self.kT.value if isinstance(self.kT, Constant) else None
 
 
 class LangevinFlow(_FlowMethod):

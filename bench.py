@@ -52,7 +52,7 @@ RELAX_STEPS, RELAX_DT, RELAX_MAX_DISP = 200, 0.002, 0.02
 RELAX_CAPS = (20.0, 50.0, 200.0, 1000.0)
 RELAX_FMAX = 2000.0
 # reference arm (the oracle on the host cores): warm-up cap and time box of the timed steps
-REF_MAX_WARMUP, REF_TIME_BOX_S = 3, 60.0
+REF_MAX_WARMUP, REF_TIME_BOX_S = 10, 60.0
 
 
 def parse():
@@ -96,55 +96,87 @@ def forces_and_method(az, flow, precision_unused=None):
     return wca, qb
 
 
-def max_force(az, snap):
-    """Largest |F_i| of the melt's forces (FP64 drop-in drivers) at a snapshot."""
-    from azplugins_gb300 import _compute
+def _melt_oracle(orc, snap, method, dt, seed, **kw):
+    """The melt's forces (WCA pair, Quartic bonds, bonded pairs excluded) on the
+    oracle, as an OracleMD loop on a copy of ``snap``."""
+    from tests.helpers import oracle_system
 
-    sim = az.Simulation(precision="fp64")
-    sim.create_state_from_snapshot(snap)
-    wca, qb = forces_and_method(az, None)
-    f1, _ = _compute.pair_forces(sim.state, wca, "fp64")
-    f2, _ = _compute.bond_forces(sim.state, qb, "fp64")
-    f = f1[:, :3] + f2[:, :3]
-    return float(np.sqrt((f * f).sum(axis=1)).max())
+    rec = orc.pair_params("PerturbedLennardJones", dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.0))
+    brec = orc.bond_params("Quartic", QUARTIC)
+    return orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
+                        pair=dict(name="PerturbedLennardJones", params=rec.reshape(1, 1, 4), rcut=np.array([[RCUT]])),
+                        bond=dict(name="Quartic", params=brec.reshape(1, 8)), method=method, gamma=[GAMMA], kT=KT,
+                        dt=dt, seed=seed, r_buff=R_BUFF, **kw)
 
 
-def relaxed_melt(az, n_chains, seed):
-    """Random-walk melt with overlaps removed by capped Brownian steps (FP64)."""
+def state_hash(snap):
+    """First 16 hex digits of the SHA-256 of the positions, images and velocities."""
+    import hashlib
+
+    p = snap.particles
+    h = hashlib.sha256()
+    for a in (p.position, p.image, p.velocity):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()[:16]
+
+
+def relaxed_melt(n_chains, seed):
+    """Random-walk melt with overlaps removed by capped Brownian steps, on the
+    host with the FP64 oracle (deterministic for any thread count), so that both
+    arms of the benchmark start from the same state: four stages of 50 steps with
+    the per-pair force capped at 20, 50, 200, 1000 and displacements at 0.02, then
+    up to four uncapped 50-step stages while the largest force exceeds
+    RELAX_FMAX. Velocities Maxwell-Boltzmann at kT (zero momentum), accelerations
+    zero. Returns (snapshot, relaxation summary)."""
+    from oracle import oracle as orc
+
     snap = make_melt(n_chains, seed)
-    wca, qb = forces_and_method(az, None)
-    stages = [(cap, RELAX_STEPS // len(RELAX_CAPS)) for cap in RELAX_CAPS]
-    extra = 0
-    k = 0
-    while k < len(stages):
-        cap, n = stages[k]
-        sim = az.Simulation(seed=seed + k, precision="fp64")
-        sim.create_state_from_snapshot(snap)
-        relax = az.methods.BrownianFlow("all", kT=KT, flow_field=az.flow.ConstantFlow((0.0, 0.0, 0.0)),
-                                        max_displacement=RELAX_MAX_DISP, force_cap=cap)
-        sim.operations.integrator = az.md.Integrator(dt=RELAX_DT, methods=[relax], forces=[wca, qb])
-        sim.run(n)
-        snap = sim.state.get_snapshot()
-        sim.close()
-        k += 1
-        if k == len(stages) and extra < 4 and max_force(az, snap) > RELAX_FMAX:
-            stages.append((0.0, 50))
-            extra += 1
-    out = snap
-    fmax = max_force(az, out)
-    p = out.particles
+    p = snap.particles
+    p.acceleration = np.zeros((p.N, 3))
+    threads = orc.set_threads(os.cpu_count() or 1)
+    try:
+        stages = [(cap, RELAX_STEPS // len(RELAX_CAPS)) for cap in RELAX_CAPS]
+        k, extra, fmax = 0, 0, None
+        while k < len(stages):
+            cap, n = stages[k]
+            md = _melt_oracle(orc, snap, "brownian", RELAX_DT, seed + k, max_disp=RELAX_MAX_DISP, force_cap=cap)
+            md.run(n)
+            p.position = md.s["pos4"][:, :3].copy()
+            p.image = md.s["image"].copy()
+            k += 1
+            if k == len(stages):
+                F, _, _ = _melt_oracle(orc, snap, "brownian", RELAX_DT, seed).forces()
+                fmax = float(np.sqrt((F * F).sum(axis=1)).max())
+                if extra < 4 and fmax > RELAX_FMAX:
+                    stages.append((0.0, 50))
+                    extra += 1
+    finally:
+        orc.set_threads(threads)
     rng = np.random.Generator(np.random.PCG64(seed + 1))
     v = rng.normal(0.0, np.sqrt(KT), size=(p.N, 3))
     p.velocity = v - v.mean(axis=0)
-    p.acceleration = np.zeros((p.N, 3))
     # broken bonds (stretched past r_0 by the relaxation), reported
-    g = np.asarray(out.bonds.group)
-    L = np.array(out.configuration.box[:3])
+    g = np.asarray(snap.bonds.group)
+    L = np.array(snap.configuration.box[:3])
     d = p.position[g[:, 0]] - p.position[g[:, 1]]
     d -= L * np.rint(d / L)
     broken = int((np.sqrt((d * d).sum(axis=1)) >= QUARTIC["r_0"]).sum())
-    log(f"relaxation: {RELAX_STEPS + 50 * extra} steps, max |F| {fmax:.1f}, {broken} stretched bonds")
-    return out, broken
+    info = {"steps": RELAX_STEPS + 50 * extra, "dt": RELAX_DT, "pair_force_caps": list(RELAX_CAPS),
+            "uncapped_stages": extra, "max_displacement": RELAX_MAX_DISP, "max_force_after": fmax,
+            "broken_bonds": broken, "engine": "oracle (host, FP64)", "state_sha256_16": state_hash(snap)}
+    log(f"relaxation: {info['steps']} steps, max |F| {fmax:.1f}, {broken} stretched bonds, "
+        f"state {info['state_sha256_16']}")
+    return snap, info
+
+
+def melt_config(N, n_chains, relax, precision):
+    """The ``config`` dict both arms print for the melt workload."""
+    return {"workload": f"bead-spring melt N={N} PLJ(WCA)+Quartic LangevinFlow(Parabolic)", "N": N,
+            "chains": n_chains, "chain_length": CHAIN_LEN, "density": DENSITY, "dt": DT, "r_buff": R_BUFF,
+            "relax": relax, "l2": "working set > L2 (no flush needed)",
+            "forces": precision,
+            "integration": ("64-bit fixed-point positions, float-pair velocities, FP32 kicks"
+                            if precision == "fp32" else "f64")}
 
 
 class ClockSampler:
@@ -240,38 +272,44 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(snap, gpu_builds_per_step, seconds=15.0):
+def cpu_baseline(snap, seconds=15.0):
     """The oracle port (OpenMP, all host cores) on a bounded sample of the same
-    workload: full N, a few steps after one untimed step; the list-build cost is
-    timed separately and amortised at the GPU run's rebuild rate."""
+    workload: the state after the GPU's timed run, full N, one untimed step, then
+    full-N steps for about ``seconds`` with the list rebuilt whenever a particle
+    moved more than r_buff / 2 (the rebuilds inside the sample are counted); then
+    two steps on one thread."""
     from oracle import oracle as orc
-    from tests.helpers import oracle_system  # noqa: E402
 
     cores = orc.set_threads(os.cpu_count() or 1)
-    rec = orc.pair_params("PerturbedLennardJones", dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.0))
-    brec = orc.bond_params("Quartic", QUARTIC)
     L = np.array(snap.configuration.box[:3])
-    md = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
-                      pair=dict(name="PerturbedLennardJones", params=rec.reshape(1, 1, 4), rcut=np.array([[RCUT]])),
-                      bond=dict(name="Quartic", params=brec.reshape(1, 8)), gamma=[GAMMA], kT=KT, dt=DT, seed=7,
-                      flow_kind=1, flow_p=(2.0 / 3.0, L[1], 0.0), r_buff=R_BUFF)
-    t0 = time.perf_counter()
+    md = _melt_oracle(orc, snap, "langevin", DT, 7, flow_kind=1, flow_p=(2.0 / 3.0, L[1], 0.0))
     md.step()  # includes the first list build
-    first = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    md.nlist_csr = orc.nlist(md.s["pos4"], md.s["types"], 1, L, np.array([[(RCUT + R_BUFF) ** 2]]), md.exclusions)
-    build = time.perf_counter() - t0
-    md.pos_build = md.s["pos4"].copy()
+    builds0 = md.builds
     steps, t0 = 0, time.perf_counter()
     while time.perf_counter() - t0 < seconds or steps < 2:
         md.step()
         steps += 1
     per_step = (time.perf_counter() - t0) / steps
-    per_step_amortised = per_step + build * gpu_builds_per_step
-    return {"value": 1.0 / per_step_amortised, "unit": "timesteps/s", "cores": cores, "kind": "port",
-            "sample": f"N={snap.particles.N} full system, {steps} timed steps after one untimed step "
-                      f"({first:.2f} s incl. list build); list build {build:.3f} s amortised at "
-                      f"{gpu_builds_per_step:.4f} builds/step; oracle/azp_oracle.cpp, OpenMP {cores} threads"}
+    builds = md.builds - builds0
+    one = cpu_single_thread(orc, md)
+    return {"value": 1.0 / per_step, "unit": "timesteps/s", "cores": cores, "kind": "port",
+            "sample": f"N={snap.particles.N} full system from the state after the timed run, {steps} FP64 steps "
+                      f"after one untimed step, {builds} list builds inside them; oracle/azp_oracle.cpp, "
+                      f"OpenMP {cores} threads",
+            "single_thread": {"value": 1.0 / one, "unit": "timesteps/s", "cores": 1,
+                              "sample": "2 full-N steps on one thread after the sample"}}
+
+
+def cpu_single_thread(orc, md, steps=2):
+    """Seconds per full-N oracle step on one thread (HOOMD's CPU model: serial per
+    MPI rank), over ``steps`` steps of the loop as it stands."""
+    threads = orc.set_threads(1)
+    try:
+        t0 = time.perf_counter()
+        md.run(steps)
+        return (time.perf_counter() - t0) / steps
+    finally:
+        orc.set_threads(threads)
 
 
 def run_reference(args):
@@ -281,34 +319,17 @@ def run_reference(args):
         return
     import azplugins_gb300 as az  # noqa: F401  (snapshot types only, no GPU work)
     from oracle import oracle as orc
-    from tests.helpers import oracle_system
 
-    snap = make_melt(args.chains, seed=1)
+    snap, relax = relaxed_melt(args.chains, seed=1)
     cores = orc.set_threads(os.cpu_count() or 1)
     L = np.array(snap.configuration.box[:3])
-    rec = orc.pair_params("PerturbedLennardJones", dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.0))
-    brec = orc.bond_params("Quartic", QUARTIC)
-    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
-    # the oracle relaxes its own copy on the host: the same capped Brownian stages
-    for k, cap in enumerate(RELAX_CAPS):
-        relax = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
-                             pair=dict(name="PerturbedLennardJones", params=rec.reshape(1, 1, 4),
-                                       rcut=np.array([[RCUT]])),
-                             bond=dict(name="Quartic", params=brec.reshape(1, 8)), method="brownian", gamma=[GAMMA],
-                             kT=KT, dt=RELAX_DT, seed=1 + k, r_buff=R_BUFF, max_disp=RELAX_MAX_DISP, force_cap=cap)
-        relax.run(RELAX_STEPS // len(RELAX_CAPS))
-        snap.particles.position = relax.s["pos4"][:, :3].copy()
-        snap.particles.image = relax.s["image"].copy()
-    md = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
-                      pair=dict(name="PerturbedLennardJones", params=rec.reshape(1, 1, 4), rcut=np.array([[RCUT]])),
-                      bond=dict(name="Quartic", params=brec.reshape(1, 8)), gamma=[GAMMA], kT=KT, dt=DT, seed=7,
-                      flow_kind=1, flow_p=(2.0 / 3.0, L[1], 0.0), r_buff=R_BUFF)
+    md = _melt_oracle(orc, snap, "langevin", DT, 7, flow_kind=1, flow_p=(2.0 / 3.0, L[1], 0.0))
     # bounded sample: a full-N oracle step takes about 0.1 s on 16 cores, so the
     # warm-up is capped at REF_MAX_WARMUP steps and the timed steps stop after
     # REF_TIME_BOX_S seconds (the rate of full-N steps is what is reported)
     warm = min(args.warmup, REF_MAX_WARMUP)
-    for _ in range(warm):
-        md.step()
+    md.run(warm)
+    builds0 = md.builds
     t0 = time.perf_counter()
     done = 0
     while done < args.steps:
@@ -317,17 +338,22 @@ def run_reference(args):
         if time.perf_counter() - t0 > REF_TIME_BOX_S:
             break
     t = time.perf_counter() - t0
+    builds = md.builds - builds0
     v = done / t
+    one = cpu_single_thread(orc, md)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "timesteps/s", "n_gpus": args.gpus,
         "steps": done, "warmup": warm, "ms_per_step": 1e3 * t / done, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random-walk melt)",
-        "config": {"workload": f"bead-spring melt N={snap.particles.N} PLJ(WCA)+Quartic LangevinFlow(Parabolic)",
-                   "N": snap.particles.N, "chains": args.chains, "chain_length": CHAIN_LEN},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random-walk melt, "
+                                                                        "capped-Brownian relaxed)",
+        "config": melt_config(snap.particles.N, args.chains, relax, args.precision),
+        "nlist_builds_in_timed_steps": builds,
         "cpu_baseline": {"value": v, "unit": "timesteps/s", "cores": cores, "kind": "port",
-                         "sample": f"{done} full-N steps timed ({args.steps} requested, time box "
-                                   f"{REF_TIME_BOX_S:.0f} s) after {warm} warm-up steps, melt relaxed by the "
-                                   "200 capped Brownian steps on the host"},
+                         "sample": f"{done} full-N FP64 steps timed ({args.steps} requested, time box "
+                                   f"{REF_TIME_BOX_S:.0f} s) after {warm} warm-up steps, {builds} list builds "
+                                   "inside them; oracle/azp_oracle.cpp OpenMP",
+                         "single_thread": {"value": 1.0 / one, "unit": "timesteps/s", "cores": 1,
+                                           "sample": "2 full-N steps on one thread after the timed steps"}},
         "e2e": {"value": v, "unit": "timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -350,8 +376,7 @@ def run_ours(args):
     dev = torch.cuda.current_device()
     _lib.load()
     log("relaxing the melt")
-    snap, broken = relaxed_melt(az, args.chains, seed=1 + rank)
-    log(f"relaxed: {broken} stretched bonds")
+    snap, relax = relaxed_melt(args.chains, seed=1 + rank)
     N = snap.particles.N
     L = snap.configuration.box[:3]
     flow = az.flow.ParabolicFlow(mean_velocity=2.0 / 3.0, separation=L[1])
@@ -393,7 +418,7 @@ def run_ours(args):
     state_after = sim.state.get_snapshot()
     n_nbr, n_bond, n_cut = neighbour_stats(state_after)
     log("neighbour statistics done")
-    accuracy = force_accuracy(az, eng, state_after, args.precision)
+    accuracy = force_accuracy(eng, state_after, args.precision)
     log("force accuracy done")
     # end to end through the public C ABI with pinned host buffers
     torch.cuda.nvtx.range_push("e2e")
@@ -416,14 +441,10 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
             "data": "synthetic (seeded random-walk melt, capped-Brownian relaxed)",
-            "config": {"workload": f"bead-spring melt N={N} PLJ(WCA)+Quartic LangevinFlow(Parabolic)",
-                       "N": N, "chains": args.chains, "chain_length": CHAIN_LEN, "density": DENSITY,
-                       "forces": args.precision, "integration": "f64", "dt": DT, "r_buff": R_BUFF,
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "working set > L2 (no flush needed)", "broken_bonds_after_relax": broken,
-                       "relax": {"steps": RELAX_STEPS, "dt": RELAX_DT, "pair_force_caps": RELAX_CAPS,
-                                 "max_displacement": RELAX_MAX_DISP}},
+            "config": dict(melt_config(N, args.chains, relax, args.precision),
+                           parallelism="replicas" if world > 1 else "single GPU"),
             "gpu_launches": int(launches),
+            "nlist_builds_in_timed_steps": builds,
             "nlist_builds_per_step": builds / args.steps,
             "step_gbs": step_bytes(N, n_nbr, n_bond, builds / args.steps, args.precision)
             / (t_max / args.steps * 1e-3) / 1e9,
@@ -442,7 +463,7 @@ def run_ours(args):
         }
         if not args.no_cpu_baseline:
             log("cpu baseline")
-            line["cpu_baseline"] = cpu_baseline(state_after, builds / args.steps)
+            line["cpu_baseline"] = cpu_baseline(state_after)
         print(json.dumps(line), flush=True)
     sim.close()
     if world > 1:
@@ -481,25 +502,24 @@ def neighbour_stats(s):
     return n_list, 2.0 * s.bonds.N / N, n_cut
 
 
-def force_accuracy(az, eng, snap, precision):
+def force_accuracy(eng, snap, precision):
     """The engine's forces (pair + bond, its own precision and list) at the state
-    after the timed run against the FP64 drop-in drivers at the same positions
-    (tests/test_gpu_pair.py holds those to 1e-12 of the FP64 oracle):
-    max_i |dF_i| / max(|F_i|, F_rms) and the relative error of the total energy."""
-    from azplugins_gb300 import _compute
+    after the timed run against the FP64 oracle at the same positions (all host
+    cores): max_i |dF_i| / max(|F_i|, F_rms) over all particles and the relative
+    error of the total energy."""
+    from oracle import oracle as orc
     from tests.helpers import force_error
 
     f_eng, _ = eng.forces()
-    ref = az.Simulation(precision="fp64")
-    ref.create_state_from_snapshot(snap)
-    wca, qb = forces_and_method(az, None)
-    fp, _ = _compute.pair_forces(ref.state, wca, "fp64")
-    fb, _ = _compute.bond_forces(ref.state, qb, "fp64")
-    f64 = fp + fb
-    return {"forces": precision, "reference": "FP64 drivers at the same state",
-            "force_error": force_error(f_eng, f64),
-            "energy_rel_error": abs(f_eng[:, 3].sum() - f64[:, 3].sum()) / abs(f64[:, 3].sum()),
-            "norm": "max_i |dF_i| / max(|F_i|, F_rms)"}
+    threads = orc.set_threads(os.cpu_count() or 1)
+    try:
+        F, U, _ = _melt_oracle(orc, snap, "langevin", DT, 7).forces()
+    finally:
+        orc.set_threads(threads)
+    return {"forces": precision, "reference": "FP64 oracle (oracle/azp_oracle.cpp) at the same state",
+            "force_error": force_error(f_eng, F),
+            "energy_rel_error": abs(f_eng[:, 3].sum() - U.sum()) / abs(U.sum()),
+            "norm": "max_i |dF_i| / max(|F_i|, F_rms), all particles"}
 
 
 def time_step_kernel(eng, reps):
@@ -555,9 +575,30 @@ def e2e_measure(eng, s, steps):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     h2d = N * (32 + 32 + 24 + 12)
+    # where an end-to-end step goes: each call timed alone, synchronised
+    parts = {"set_state": 0.0, "run": 0.0, "get_state": 0.0, "thermo": 0.0}
+    reps = max(2, min(steps, 10))
+    for t in range(reps):
+        for name, fn in (("set_state", lambda: L.azp_md_set_state(eng._md, pos.data_ptr(), vel.data_ptr(),
+                                                                  acc.data_ptr(), img.data_ptr(), None,
+                                                                  1000 + t, 0, stream)),
+                         ("run", lambda: L.azp_md_run(eng._md, 1, stream)),
+                         ("get_state", lambda: L.azp_md_get_state(eng._md, pos.data_ptr(), vel.data_ptr(),
+                                                                  acc.data_ptr(), img.data_ptr(), ctypes.byref(ts),
+                                                                  0, stream)),
+                         ("thermo", lambda: L.azp_md_thermo(eng._md, thermo.ctypes.data, stream))):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            _lib.check(fn(), name)
+            torch.cuda.synchronize()
+            parts[name] += (time.perf_counter() - t1) / reps
+    breakdown = {f"{k}_ms": 1e3 * v for k, v in parts.items()}
+    breakdown["set_state_h2d_gbs"] = h2d / parts["set_state"] / 1e9
+    breakdown["get_state_d2h_gbs"] = h2d / parts["get_state"] / 1e9
     return {"value": steps / dt, "unit": "timesteps/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": h2d + 72, "api": "azp_md_set_state / azp_md_run(1) / azp_md_get_state / azp_md_thermo",
-            "steps": steps}
+            "steps": steps, "breakdown": breakdown,
+            "note": "set_state copies the host state (pinned) and re-sorts / rebuilds the list; rates include that"}
 
 
 def main():

@@ -473,6 +473,11 @@ typedef struct {
      * dissipative and random terms, sqrt(6 kT gamma / dt)); needs the Langevin
      * method (with default gamma 0 and noiseless: HOOMD's ConstantVolume) */
     double dpd_kT;
+    /* particles the method integrates, by type: bit t set means particles of type
+     * t move (HOOMD's filter.Type group of the method, src/TwoStepLangevinFlow.h:35);
+     * the others feel and exert forces but keep their positions and velocities.
+     * 0 means every particle (filter.All). Types above 31 need 0. */
+    uint32_t group_types;
 } azp_md_config;
 
 AZP_API azp_md* azp_md_create(const azp_md_config* cfg, int* status);
@@ -489,6 +494,15 @@ AZP_API void azp_md_destroy(azp_md* md);
 #define AZP_MD_BARRIER_ROWS 65536u
 AZP_API int azp_md_set_barrier_locations(azp_md* md, uint64_t t_first, uint32_t n, const double* location,
                                          void* stream);
+/* Temperature of the method as a per-timestep table (HOOMD's Variant kT of
+ * TwoStepLangevinFlow / TwoStepBrownianFlow, evaluated at the timestep of step
+ * two or of the Brownian move, src/TwoStepLangevinFlow.h:194-219): kT[r] belongs
+ * to timestep t_first + r, r < n <= AZP_MD_KT_ROWS; timesteps outside the rows
+ * take the nearest row. Replaces azp_md_config.kT until the engine is destroyed;
+ * the noise amplitudes sqrt(6 gamma kT / dt) are formed on the host with the
+ * reference's operations. Synchronises the stream. */
+#define AZP_MD_KT_ROWS 65536u
+AZP_API int azp_md_set_temperatures(azp_md* md, uint64_t t_first, uint32_t n, const double* kT, void* stream);
 /* Load state in TAG order from host (on_device == 0) or device pointers:
  * pos [N][4] (w = type as an integer-valued double), vel [N][4] (w = mass),
  * accel [N][3], image [N][3], diameter [N] or NULL. */

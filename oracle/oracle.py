@@ -519,7 +519,7 @@ class OracleMD:
 
     def __init__(self, system, pair=None, bond=None, method="langevin", gamma=(1.0,), flow_kind=0,
                  flow_p=(0.0, 0.0, 0.0), kT=1.0, dt=0.005, seed=0, r_buff=0.4, noiseless=False, exclude_bonds=True,
-                 max_disp=0.0, force_cap=0.0, barrier=None, walls=None):
+                 max_disp=0.0, force_cap=0.0, barrier=None, walls=None, group_types=None):
         self.s = {k: (np.ascontiguousarray(v).copy() if isinstance(v, np.ndarray) else v) for k, v in system.items()}
         s = self.s
         self.N = s["pos4"].shape[0]
@@ -529,7 +529,13 @@ class OracleMD:
         self.gamma = np.asarray(gamma, dtype=np.float64)
         self.flow_kind = flow_kind
         self.flow_p = np.asarray(flow_p, dtype=np.float64)
+        # kT: a float or a function of the timestep (the reference evaluates its
+        # Variant at the timestep of step two, src/TwoStepLangevinFlow.h:194-219)
         self.kT, self.dt, self.seed = kT, dt, seed
+        # the method's group as the integrated type ids (None: every particle);
+        # the reference's kernels visit the group's members only
+        # (src/TwoStepLangevinFlowGPU.cuh:25-55), so the others keep their state
+        self.group_types = None if group_types is None else np.asarray(group_types, dtype=np.int32)
         self.r_buff = r_buff
         self.noiseless = noiseless
         self.max_disp = max_disp
@@ -608,18 +614,30 @@ class OracleMD:
             U = U + Ub
         return F, U, W
 
+    def _kT_at(self, t):
+        return float(self.kT(t)) if callable(self.kT) else self.kT
+
     def step(self):
         s = self.s
         t = self.timestep
+        keep = None
+        if self.group_types is not None:
+            out = ~np.isin(s["types"], self.group_types)
+            keep = (out, s["pos4"][out].copy(), s["image"][out].copy(), s["vel4"][out].copy(), s["accel"][out].copy())
         if self.method == "langevin":
             langevin_step1(s["pos4"], s["image"], s["vel4"], s["accel"], s["L"], self.dt)
+            if keep is not None:
+                s["pos4"][keep[0]], s["image"][keep[0]], s["vel4"][keep[0]] = keep[1], keep[2], keep[3]
             F, U, W = self.forces(t + 1)
             langevin_step2(s["pos4"], s["types"], s["vel4"], s["accel"], F, s["tags"], self.gamma, self.flow_kind,
-                           self.flow_p, self.kT, self.dt, t, self.seed, self.noiseless)
+                           self.flow_p, self._kT_at(t), self.dt, t, self.seed, self.noiseless)
         else:
             F, U, W = self.forces(t)
             brownian(s["pos4"], s["image"], s["types"], F, s["tags"], self.gamma, self.flow_kind, self.flow_p,
-                     s["L"], self.kT, self.dt, t, self.seed, self.noiseless, max_disp=self.max_disp)
+                     s["L"], self._kT_at(t), self.dt, t, self.seed, self.noiseless, max_disp=self.max_disp)
+        if keep is not None:
+            out = keep[0]
+            s["pos4"][out], s["image"][out], s["vel4"][out], s["accel"][out] = keep[1], keep[2], keep[3], keep[4]
         self.timestep = t + 1
         self.last = (F, U, W)
 

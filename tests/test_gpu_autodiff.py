@@ -261,15 +261,17 @@ def test_rollout_gradient_matches_dense_autograd():
     import azplugins_gb300 as az
     from azplugins_gb300 import autodiff, workloads
 
+    # N = 512, K = 100 Langevin steps with checkpoints every 10 (the gradient
+    # workload's dense check)
     snap = workloads.lj_fluid(n_side=8, density=0.8, seed=48)
     pot = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), mode="shift")
     ctx = _ctx(snap, pot, 2.5)
     L = torch.tensor(snap.configuration.box[:3], dtype=torch.float64, device="cuda")
     x0 = torch.tensor(snap.particles.position, dtype=torch.float64, device="cuda")
     v0 = torch.tensor(snap.particles.velocity, dtype=torch.float64, device="cuda")
-    K, dt, seed = 10, 0.005, 9
+    K, dt, seed = 100, 0.005, 9
     vals = torch.tensor([1.0, 1.0, 0.5], dtype=torch.float64, device="cuda", requires_grad=True)
-    x, v, F, U = autodiff.langevin_rollout(x0, v0, vals, ctx, K, dt, seed=seed, checkpoint_every=5)
+    x, v, F, U = autodiff.langevin_rollout(x0, v0, vals, ctx, K, dt, seed=seed, checkpoint_every=10)
     loss = (F ** 2).sum(dim=1).mean() + (U.sum() / x.shape[0]) ** 2
     (gv,) = torch.autograd.grad(loss, (vals,))
     # dense
@@ -311,3 +313,50 @@ def test_rollout_gradient_matches_dense_autograd():
     loss_d = (FF ** 2).sum(dim=1).mean() + (UU.sum() / xx.shape[0]) ** 2
     (gd,) = torch.autograd.grad(loss_d, (p,))
     assert bool(((gv - gd).abs() <= 1e-6 * gd.abs() + 1e-10).all()), (gv, gd)
+
+
+def test_rollout_gradient_at_workload_size():
+    """The gradient workload at its own size: PerturbedLJ fluid, N = 65,536 at
+    density 0.8, (epsilon, sigma, lambda) = (1, 1, 0.5), loss on forces and energy
+    against targets at (1.1, 0.98, 0.4), K = 100 Langevin steps (dt = 0.005,
+    fixed seed) with checkpoints every 10, against FP64 central differences
+    (h = 1e-6). Forces smoothed to zero at r_cut (xplor, r_on = 2.5, r_cut = 3)
+    so that no pair crossing r_cut makes the loss jump. epsilon and lambda meet
+    1e-6. sigma moves the kink of the WCA split at r^2 = 2^(1/3) sigma^2
+    (PairEvaluatorPerturbedLennardJones.h:131-145: the force's derivative jumps
+    there), so over 100 steps pairs straddle the kink inside [sigma - h, sigma + h]
+    and the central difference itself carries an error; sigma is held to 1e-4
+    here and to 1e-6 against the exact dense gradient of the same dynamics
+    (test_rollout_gradient_matches_dense_autograd)."""
+    torch = _torch()
+    import azplugins_gb300 as az
+    from azplugins_gb300 import autodiff
+
+    snap = _fluid(65536, 0.8, seed=5)
+    pot = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), mode="xplor")
+    ctx = autodiff.Context(pot, snap.particles.types, snap.particles.typeid, snap.configuration.box, 3.0, r_on=2.5)
+    x0 = torch.tensor(snap.particles.position, dtype=torch.float64, device="cuda")
+    v0 = torch.tensor(snap.particles.velocity, dtype=torch.float64, device="cuda")
+    vals = torch.tensor([1.0, 1.0, 0.5], dtype=torch.float64, device="cuda", requires_grad=True)
+    with torch.no_grad():
+        Ft, Ut = autodiff.pair_forces(x0, torch.tensor([1.1, 0.98, 0.4], dtype=torch.float64, device="cuda"), ctx)
+        Ut = Ut.sum()
+
+    def roll(v):
+        x, vel, F, U = autodiff.langevin_rollout(x0, v0, v, ctx, 100, 0.005, seed=9, checkpoint_every=10)
+        return ((F - Ft) ** 2).sum(dim=1).mean() + (U.sum() - Ut) ** 2
+
+    (g,) = torch.autograd.grad(roll(vals), (vals,))
+    h = 1e-6
+    err = []
+    for k in range(3):
+        with torch.no_grad():
+            vp, vm = vals.detach().clone(), vals.detach().clone()
+            vp[k] += h
+            vm[k] -= h
+            fd = (roll(vp) - roll(vm)) / (2 * h)
+        err.append(abs(float(g[k]) - float(fd)) / abs(float(fd)))
+    print("rollout FD relative errors (eps, sigma, lambda):", err)
+    assert err[0] <= 1e-6 and err[2] <= 1e-6, err
+    assert err[1] <= 1e-4, err
+

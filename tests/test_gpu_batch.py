@@ -1,6 +1,6 @@
 """Batched replicas (one fused launch per step for all replicas) against the
-same replicas run one by one through the single-system engine, and the
-autotuner keeping the state intact."""
+oracle's MD loop run replica by replica, against the same replicas run one by one
+through the single-system engine, and the autotuner keeping the state intact."""
 
 import numpy as np
 import pytest
@@ -71,3 +71,36 @@ def test_autotune_restores_state():
         assert np.array_equal(np.sort(x, axis=0), np.sort(y, axis=0))
     b.run(10)
     b.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32", 1e-4)])
+def test_batch_replicas_match_oracle(orc, precision, tol):
+    """Every replica of the batch against the oracle's HOOMD-order Langevin loop
+    (ExpandedYukawa, its own box, parameters and seed; 40 steps at dt = 0.002):
+    positions to 1e-9 (FP64 forces) or 1e-4 (FP32 forces), velocities to 10x
+    that, the same list builds decided the same way."""
+    from azplugins_gb300.batch import ReplicaBatch
+    from helpers import oracle_system
+
+    snaps, params, _ = _replicas(6, seed=53)
+    seeds = [200 + r for r in range(len(snaps))]
+    b = ReplicaBatch(snaps, az.pair.ExpandedYukawa, [dict(epsilon=p["epsilon"], kappa=p["kappa"], delta=p["delta"])
+                                                     for p in params],
+                     [p["r_cut"] for p in params], seeds, dt=0.002, precision=precision)
+    b.run(40)
+    arrays = b.get_arrays()
+    for r, (s, p) in enumerate(zip(snaps, params)):
+        rec = orc.pair_params("ExpandedYukawa", dict(epsilon=p["epsilon"], kappa=p["kappa"], delta=p["delta"]))
+        acc = s.particles.acceleration if s.particles.acceleration is not None else np.zeros((s.particles.N, 3))
+        md = orc.OracleMD(oracle_system(s, acc),
+                          pair=dict(name="ExpandedYukawa", params=rec.reshape(1, 1, 4), rcut=np.array([[p["r_cut"]]])),
+                          gamma=[1.0], kT=1.0, dt=0.002, seed=seeds[r])
+        md.run(40)
+        pos, vel, _, img = b.replica(r, arrays)
+        L = np.array(s.configuration.box[:3])
+        assert _pos_err(pos, md.s["pos4"][:, :3], L) < tol, r
+        assert np.abs(vel - md.s["vel4"][:, :3]).max() < 10 * tol, r
+        if precision == "fp64":
+            assert np.array_equal(img, md.s["image"]), r
+    b.close()
+
