@@ -253,6 +253,7 @@ _SIGNATURES = [
     ("azp_batch_run", _i, [_vp, _u64, _vp]),
     ("azp_batch_error", _i, [_vp, ctypes.POINTER(_u32), ctypes.POINTER(_u32), _vp]),
     ("azp_batch_set_tpp", _i, [_vp, _i]),
+    ("azp_batch_set_block", _i, [_vp, _i]),
     ("azp_batch_last_launches", _u64, [_vp]),
 ]
 

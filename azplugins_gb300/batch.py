@@ -72,6 +72,7 @@ class ReplicaBatch:
         self.timestep = timestep
         self.set_state(snapshots)
         self.tpp = 1
+        self.block = 256
 
     def set_state(self, snapshots):
         tot = int(self.off[-1])
@@ -125,28 +126,40 @@ class ReplicaBatch:
         _lib.check(self._L.azp_batch_set_tpp(self._b, int(tpp)), "azp_batch_set_tpp")
         self.tpp = int(tpp)
 
-    def autotune(self, candidates=(1, 2, 4, 8), steps=20, repeats=2):
-        """Pick the threads-per-particle of the fused step by timing (CUDA events).
+    def set_block(self, block):
+        _lib.check(self._L.azp_batch_set_block(self._b, int(block)), "azp_batch_set_block")
+        self.block = int(block)
 
-        The state is restored afterwards; returns {tpp: ms per step}."""
+    def autotune(self, candidates=(1, 2, 4, 8), steps=20, repeats=2, blocks=(256,)):
+        """Pick the threads-per-particle and the block size of the fused step by
+        timing every pair (CUDA events on the launching stream).
+
+        The state is restored afterwards; returns {tpp: ms per step} when one
+        block size is tried, else {(tpp, block): ms per step}."""
         import torch
 
         saved = self.get_arrays()
         t0 = self.timestep
         res = {}
-        for tpp in candidates:
-            self.set_tpp(tpp)
-            self.run(2, check=False)  # graph capture + warm-up
-            best = float("inf")
-            for _ in range(repeats):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                self.run(steps, check=False)
-                e1.record()
-                torch.cuda.synchronize()
-                best = min(best, e0.elapsed_time(e1) / steps)
-            res[tpp] = best
-        self.set_tpp(min(res, key=res.get))
+        for block in blocks:
+            self.set_block(block)
+            for tpp in candidates:
+                self.set_tpp(tpp)
+                self.run(2, check=False)  # graph capture + warm-up
+                best = float("inf")
+                for _ in range(repeats):
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    self.run(steps, check=False)
+                    e1.record()
+                    torch.cuda.synchronize()
+                    best = min(best, e0.elapsed_time(e1) / steps)
+                res[(tpp, block)] = best
+        tpp, block = min(res, key=res.get)
+        self.set_block(block)
+        self.set_tpp(tpp)
+        if len(blocks) == 1:
+            res = {k[0]: v for k, v in res.items()}
         self.timestep = t0
         pos, vel, acc, img = saved
         _lib.check(self._L.azp_batch_set_state(self._b, pos.ctypes.data, vel.ctypes.data, acc.ctypes.data,

@@ -45,7 +45,8 @@ struct SysInfo {
     double rec[PAIR_TBL];     // pair kernel record + cut record (one type)
 };
 
-constexpr int BATCH_BLOCK = 256;
+constexpr int BATCH_BLOCK = 256;      // default threads per block of the fused step
+constexpr int BATCH_BLOCK_MAX = 512;  // largest block azp_batch_set_block accepts
 
 AZP_D void comp_shfl_add(Comp& c, int m)
 {
@@ -98,17 +99,15 @@ __global__ void k_b_scatter(const uint32_t* __restrict__ cell_of, const uint32_t
     members[cell_start[cell_of[i]] + slot[i]] = i;
 }
 
-// each cell's members sorted by index (deterministic order), one warp per cell
+// each cell's members sorted by index (deterministic order): one warp per 32
+// consecutive cells, a lane per cell for small cells, the whole warp for crowded ones
 __global__ void __launch_bounds__(kSortWarps * 32) k_b_cell_sort(const uint32_t* __restrict__ cell_start,
                                                                  uint32_t* __restrict__ members, uint32_t ncell,
                                                                  const uint32_t* __restrict__ gate)
 {
     if (gated_off(gate)) return;
     __shared__ uint32_t s_rows[kSortWarps][kMaxSortedCell];
-    const uint32_t w = threadIdx.x >> 5;
-    const uint32_t c = blockIdx.x * kSortWarps + w;
-    if (c >= ncell) return;
-    warp_sort_cell(members, cell_start[c], cell_start[c + 1], s_rows[w]);
+    sort_cells_warp(cell_start, members, ncell, s_rows[threadIdx.x >> 5]);
 }
 
 struct BPerm {
@@ -267,12 +266,13 @@ struct BStep {
     float disp_thresh2;
     int next;
     int tpp;
+    int block;  // threads per block of the launch
     cudaGraphConditionalHandle next_cond;
     int set_cond;
 };
 
 template<class PE, typename R>
-__global__ void __launch_bounds__(BATCH_BLOCK) k_b_step(BStep a)
+__global__ void __launch_bounds__(BATCH_BLOCK_MAX) k_b_step(BStep a)
 {
     const int tpp = a.tpp;
     const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -536,12 +536,12 @@ __global__ void k_b_store(const double4_32a* __restrict__ pos, const double4_32a
 template<class PE>
 int launch_b_step(int precision, const BStep& a, cudaStream_t s)
 {
-    const uint32_t blocks = (uint32_t)(((size_t)a.N * a.tpp + BATCH_BLOCK - 1) / BATCH_BLOCK);
+    const uint32_t blocks = (uint32_t)(((size_t)a.N * a.tpp + a.block - 1) / a.block);
     if (blocks == 0) return AZP_OK;
     if (precision == AZP_FP32)
-        k_b_step<PE, float><<<blocks, BATCH_BLOCK, 0, s>>>(a);
+        k_b_step<PE, float><<<blocks, a.block, 0, s>>>(a);
     else
-        k_b_step<PE, double><<<blocks, BATCH_BLOCK, 0, s>>>(a);
+        k_b_step<PE, double><<<blocks, a.block, 0, s>>>(a);
     AZP_CHECK_LAUNCH("k_b_step");
     return AZP_OK;
 }
@@ -564,7 +564,7 @@ using namespace azp;
 struct azp_batch {
     uint32_t S = 0, N = 0;
     std::vector<uint32_t> n_of, off;
-    int precision = AZP_FP64, kind = 0, tpp = 1;
+    int precision = AZP_FP64, kind = 0, tpp = 1, block = BATCH_BLOCK;
     double dt = 0.005, kT = 1.0, gamma = 1.0, r_buff = 0.4;
     int noiseless = 0;
     FlowD flow{};
@@ -640,8 +640,8 @@ int b_rebuild(azp_batch* b, cudaStream_t s, const uint32_t* gate)
     int st = exclusive_scan(b->cell_count, b->cell_start, b->ncell, b->scan_tmp, s, gate);
     if (st) return st;
     k_b_scatter<<<nblk(N), 256, 0, s>>>(b->cell_of, b->slot, b->cell_start, b->members, N, gate);
-    k_b_cell_sort<<<(b->ncell + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(b->cell_start, b->members,
-                                                                                      b->ncell, gate);
+    k_b_cell_sort<<<(b->ncell + 32 * kSortWarps - 1) / (32 * kSortWarps), kSortWarps * 32, 0, s>>>(
+        b->cell_start, b->members, b->ncell, gate);
     BPerm p;
     p.members = b->members;
     p.pos = b->pos[b->cur];
@@ -700,6 +700,7 @@ BStep b_args(azp_batch* b)
     const double half = 0.5 * b->r_buff;
     a.disp_thresh2 = (float)(half * half * (1.0 - 1e-5));
     a.tpp = b->tpp;
+    a.block = b->block;
     return a;
 }
 
@@ -1047,6 +1048,14 @@ int azp_batch_error(azp_batch* b, uint32_t* err_word, uint32_t* n_builds, void* 
     if (f[3] > b->max_nn) e |= AZP_EBIT_NLIST_OVERFLOW;
     *err_word = e;
     if (n_builds) *n_builds = f[2];
+    return AZP_OK;
+}
+
+int azp_batch_set_block(azp_batch* b, int block)
+{
+    if (!b || !(block == 64 || block == 128 || block == 256 || block == 512)) return AZP_ERR_INVALID;
+    if (b->block != block) b_free_graphs(b);
+    b->block = block;
     return AZP_OK;
 }
 

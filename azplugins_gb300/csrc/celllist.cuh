@@ -8,8 +8,25 @@ namespace azp
 {
 // cells holding more particles than this are not sorted by index
 constexpr uint32_t kMaxSortedCell = 512;
-// warps per block of the cell-sort kernels (one warp per cell)
+// warps per block of the cell-sort kernels (each warp: 32 consecutive cells)
 constexpr int kSortWarps = 8;
+// cells up to this size are sorted by one lane, larger ones by the whole warp
+constexpr uint32_t kSerialCell = 12;
+
+// Insertion sort of a small cell's members by one thread (a handful of entries:
+// the dense-melt case of about three particles per cell)
+__device__ __forceinline__ void thread_sort_cell(uint32_t* __restrict__ members, uint32_t b, uint32_t e)
+{
+    for (uint32_t a = b + 1; a < e; ++a) {
+        const uint32_t v = members[a];
+        uint32_t k = a;
+        while (k > b && members[k - 1] > v) {
+            members[k] = members[k - 1];
+            --k;
+        }
+        members[k] = v;
+    }
+}
 
 // Sort the members of one cell, members[b, e), by particle index: the order in
 // which atomics placed them is not deterministic, the sorted order is. One warp
@@ -107,5 +124,31 @@ void launch_to_fixed2(const double4_32a* pos, uint4* a, uint4* b, uint32_t N, co
 // host: thresholds for r_cut[ntypes^2], r_buff and the box
 void make_list_cuts(const double* r_cut, uint32_t ntypes, double r_buff, const azp_box& box, ListCut* out,
                     double* rlist_max, double* rlist_min = nullptr);
+
+// The cells of one warp, 32 consecutive cells from (global warp index) * 32: a
+// lane sorts its own cell when it holds at most kSerialCell members, then the
+// warp sorts the larger ones together, one after another (warp_sort_cell).
+__device__ __forceinline__ void sort_cells_warp(const uint32_t* __restrict__ cell_start,
+                                                uint32_t* __restrict__ members, uint32_t ncell,
+                                                uint32_t* __restrict__ s_row)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t c = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32u + lane;
+    uint32_t b = 0u, e = 0u;
+    if (c < ncell) {
+        b = cell_start[c];
+        e = cell_start[c + 1];
+    }
+    const uint32_t n = e - b;
+    if (n >= 2u && n <= kSerialCell) thread_sort_cell(members, b, e);
+    uint32_t big = __ballot_sync(0xffffffffu, n > kSerialCell && n <= kMaxSortedCell);
+    while (big) {
+        const int l = __ffs(big) - 1;
+        big &= big - 1u;
+        const uint32_t bb = __shfl_sync(0xffffffffu, b, l), ee = __shfl_sync(0xffffffffu, e, l);
+        warp_sort_cell(members, bb, ee, s_row);
+        __syncwarp();
+    }
+}
 
 }  // namespace azp

@@ -128,17 +128,15 @@ __global__ void k_cell_scatter(const uint32_t* __restrict__ cell_of, const uint3
     members[cell_start[cell_of[i]] + slot[i]] = i;
 }
 
-// each cell's members sorted by index (deterministic order), one warp per cell
+// each cell's members sorted by index (deterministic order): one warp per 32
+// consecutive cells, a lane per cell for small cells, the whole warp for crowded ones
 __global__ void __launch_bounds__(kSortWarps * 32) k_cell_sort(const uint32_t* __restrict__ cell_start,
                                                                uint32_t* __restrict__ members, uint32_t ncell,
                                                                const uint32_t* __restrict__ gate)
 {
     if (gated_off(gate)) return;
     __shared__ uint32_t s_rows[kSortWarps][kMaxSortedCell];
-    const uint32_t w = threadIdx.x >> 5;
-    const uint32_t c = blockIdx.x * kSortWarps + w;
-    if (c >= ncell) return;
-    warp_sort_cell(members, cell_start[c], cell_start[c + 1], s_rows[w]);
+    sort_cells_warp(cell_start, members, ncell, s_rows[threadIdx.x >> 5]);
 }
 
 struct BoxArgs {
@@ -343,7 +341,8 @@ void launch_cell_scatter(const uint32_t* cell_of, const uint32_t* slot, const ui
 {
     if (N == 0) return;
     k_cell_scatter<<<(N + 255) / 256, 256, 0, s>>>(cell_of, slot, cell_start, members, N, gate);
-    k_cell_sort<<<(ncell + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(cell_start, members, ncell, gate);
+    k_cell_sort<<<(ncell + 32 * kSortWarps - 1) / (32 * kSortWarps), kSortWarps * 32, 0, s>>>(cell_start, members,
+                                                                                              ncell, gate);
 }
 
 __global__ void k_to_fixed2(const double4_32a* __restrict__ pos, uint4* __restrict__ fa, uint4* __restrict__ fb,

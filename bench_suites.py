@@ -115,7 +115,7 @@ def suite_batched(args):
     yk = [dict(epsilon=p["epsilon"], kappa=p["kappa"], delta=p["delta"]) for p in params]
     rc = [p["r_cut"] for p in params]
     b = ReplicaBatch(snaps, az.pair.ExpandedYukawa, yk, rc, seeds, dt=0.002, precision="fp32")
-    tune = b.autotune(candidates=(1, 2, 4, 8), steps=20)
+    tune = b.autotune(candidates=(1, 2, 4, 8), steps=20, blocks=(128, 256, 512))
     b.run(50)  # warm-up
     steps = args.steps if args.steps != 2000 else 500
     ms = _cuda_ms(lambda: b.run(steps, check=False))
@@ -153,8 +153,10 @@ def suite_batched(args):
             "total_particles": int(sum(s.particles.N for s in snaps)), "redraws_for_min_image": redraws,
             "batched_replica_steps_per_s": batched, "separate_replica_steps_per_s": separate,
             "speedup": batched / separate, "autotune_ms_per_step": {str(k): v for k, v in tune.items()},
-            "tpp": int(min(tune, key=tune.get)), "batched_launches_in_timed_region": launches,
-            "steps_batched": steps, "steps_separate": sep_steps, "forces": "fp32", "integration": "f64"}
+            "tpp": int(min(tune, key=tune.get)[0]), "block": int(min(tune, key=tune.get)[1]),
+            "batched_launches_in_timed_region": launches,
+            "steps_batched": steps, "steps_separate": sep_steps, "forces": "fp32",
+            "integration": "f64 positions and velocities"}
     print(json.dumps(line), flush=True)
 
 

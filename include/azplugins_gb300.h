@@ -568,8 +568,11 @@ AZP_API int azp_batch_get_state(azp_batch* b, double* pos, double* vel, double* 
                                 void* stream);
 AZP_API int azp_batch_run(azp_batch* b, uint64_t steps, void* stream);
 AZP_API int azp_batch_error(azp_batch* b, uint32_t* err_word, uint32_t* n_builds, void* stream);
-/* threads per particle of the fused step (the autotuner's knob) */
+/* threads per particle of the fused step (the autotuner's first knob) */
 AZP_API int azp_batch_set_tpp(azp_batch* b, int tpp);
+/* threads per block of the fused step: 64, 128, 256 (default) or 512 (the
+ * autotuner's second knob) */
+AZP_API int azp_batch_set_block(azp_batch* b, int block);
 AZP_API uint64_t azp_batch_last_launches(const azp_batch* b);
 
 #ifdef __cplusplus

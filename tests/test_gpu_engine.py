@@ -441,3 +441,52 @@ def test_pinned_and_pageable_state_transfers_agree():
         outs.append(get(False))
     for x, y in zip(*outs):
         assert torch.equal(x, y)
+
+
+def _binary_fluid(seed):
+    snap = random_fluid(1200, 0.7, seed=seed, ntypes=2)
+    snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+    return snap
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32", 1e-4)])
+@pytest.mark.parametrize("method", ["langevin", "brownian"])
+def test_type_group_and_variant_kT(orc, precision, tol, method):
+    """A method on filter.Type(["A"]) (the reference's ParticleGroup: B particles
+    feel and exert forces but keep their positions and velocities) with kT a
+    ramp of the timestep (the reference's Variant T, evaluated at the timestep of
+    step two), against the oracle's loop with the same group and temperatures."""
+    from azplugins_gb300 import variant
+
+    snap = _binary_fluid(61)
+    ramp = variant.Ramp(0.5, 2.0, 10, 40)
+    sim = az.Simulation(seed=13, precision=precision)
+    sim.create_state_from_snapshot(snap)
+    lj = az.pair.PerturbedLennardJones(nlist=az.nlist.Cell(buffer=0.4), default_r_cut=2.5)
+    for k in [("A", "A"), ("A", "B"), ("B", "B")]:
+        lj.params[k] = dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.5)
+    cls = az.methods.LangevinFlow if method == "langevin" else az.methods.BrownianFlow
+    m = cls(az.filter.Type(["A"]), kT=ramp, flow_field=az.flow.ConstantFlow((0.1, 0.0, 0.0)), default_gamma=1.0)
+    dt = 0.005 if method == "langevin" else 0.0005
+    sim.operations.integrator = az.md.Integrator(dt=dt, methods=[m], forces=[lj])
+    sim.run(30)
+    sim.run(30)
+    out = sim.state.get_snapshot().particles
+    rec = orc.pair_params("PerturbedLennardJones", dict(epsilon=1.0, sigma=1.0, attraction_scale_factor=0.5))
+    md = orc.OracleMD(oracle_system(snap, snap.particles.acceleration),
+                      pair=dict(name="PerturbedLennardJones", params=np.tile(rec, (2, 2, 1)),
+                                rcut=np.full((2, 2), 2.5)),
+                      method=method, gamma=[1.0, 1.0], kT=ramp, dt=dt, seed=13, flow_kind=0, flow_p=(0.1, 0.0, 0.0),
+                      group_types=[0])
+    md.run(60)
+    L = box_of(snap)
+    b = snap.particles.typeid == 1
+    # B particles did not move (FP32-force mode keeps positions as 64-bit fixed
+    # point and velocities as float pairs: equal to the input within that storage)
+    still = 0.0 if precision == "fp64" else 1e-12
+    assert np.abs(out.position[b] - snap.particles.position[b]).max() <= still
+    if method == "langevin":
+        assert np.abs(out.velocity[b] - snap.particles.velocity[b]).max() <= (0.0 if precision == "fp64" else 1e-11)
+    assert _pos_err(out.position, md.s["pos4"][:, :3], L) < tol
+    if method == "langevin":
+        assert np.abs(out.velocity - md.s["vel4"][:, :3]).max() < 10 * tol
