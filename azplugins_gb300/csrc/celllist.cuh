@@ -82,6 +82,45 @@ struct ListCut {
     float pad;
 };
 
+// Shared-memory neighbour tiles of the single-type FP32-force step. Particles
+// are stored in cell order, so the list candidates of a block of TILE_P
+// consecutive particles lie, stencil row by stencil row, in a few contiguous
+// particle-index ranges; the step stages those ranges of 16-byte position
+// records in shared memory and the list addresses them there. Per block one
+// record of TILE_REC words: [0] number of ranges (0: the block is not tiled),
+// [1] total records, then per range k: begin [2 + 3k], end [3 + 3k], tile offset
+// [4 + 3k]. A list entry below 2^31 is a tile offset; TILE_GLOBAL | j is the
+// particle index j (candidates outside the ranges: the wrapped cell at an x
+// face, or a block whose ranges exceed TILE_CAP records).
+constexpr uint32_t TILE_P = 256;
+constexpr uint32_t TILE_REC = 32;
+constexpr uint32_t TILE_MAX_RANGES = 9;
+constexpr uint32_t TILE_CAP = 3072;  // 48 KB of 16-byte records
+constexpr uint32_t TILE_GLOBAL = 0x80000000u;
+
+// list entry of particle j for the block record t
+__device__ __forceinline__ uint32_t tile_encode(const uint32_t* t, uint32_t j)
+{
+    const uint32_t nr = t[0];
+    for (uint32_t k = 0; k < nr; ++k) {
+        const uint32_t b = t[2 + 3 * k], e = t[3 + 3 * k];
+        if (j >= b && j < e) return t[4 + 3 * k] + (j - b);
+    }
+    return TILE_GLOBAL | j;
+}
+
+// particle index of a list entry for the block record t
+__device__ __forceinline__ uint32_t tile_decode(const uint32_t* __restrict__ t, uint32_t e)
+{
+    if (e & TILE_GLOBAL) return e & ~TILE_GLOBAL;
+    const uint32_t nr = __ldg(t);
+    for (uint32_t k = 0; k < nr; ++k) {
+        const uint32_t off = __ldg(t + 4 + 3 * k), b = __ldg(t + 2 + 3 * k), e2 = __ldg(t + 3 + 3 * k);
+        if (e >= off && e < off + (e2 - b)) return b + (e - off);
+    }
+    return 0u;  // not reached for entries the list build wrote
+}
+
 // Launch helpers (all stream-ordered, no allocation, no synchronisation).
 // fixed[N] <- 16-byte fixed-point shadow of pos (x, y, z fractions of L, type)
 void launch_to_fixed(const double4_32a* pos, uint4* fixed, uint32_t N, const azp_box& box, cudaStream_t s);
@@ -107,7 +146,14 @@ void launch_nlist_build(const double4_32a* pos, const uint4* fixed, uint32_t N, 
                         const ListCut* cuts, uint32_t ntypes, const uint32_t* ex_n, const uint32_t* ex_keys,
                         uint32_t ex_width, const uint32_t* keys, uint32_t* counts, uint32_t* nbrs,
                         uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s,
-                        const uint4* lo, double rlist_min);
+                        const uint4* lo, double rlist_min, const uint32_t* tile = nullptr);
+// tile != NULL: particles in cell order (members NULL), entries encoded for the
+// block records of launch_tile_table.
+
+// block records of the shared-memory tiles (particles in cell order, cell_of of
+// the last binning): tab[(N + TILE_P - 1) / TILE_P][TILE_REC]
+void launch_tile_table(const uint32_t* cell_of, const uint32_t* cell_start, const CellGrid& g, uint32_t N,
+                       uint32_t* tab, const uint32_t* gate, cudaStream_t s);
 // lo != NULL: positions are the 64-bit fixed words (fixed = high, lo = low) of the
 // FP32-force engine, and the exact FP64 test runs on their FP64 conversion.
 // rlist_min: the smallest listed r_cut + r_buff (sets the FP32 band of the

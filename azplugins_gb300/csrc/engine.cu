@@ -559,6 +559,8 @@ struct azp_md {
     float wall_tol = 0.0f;
     // integration group by type (0xffffffff: every particle)
     uint32_t group_types = 0xffffffffu;
+    // shared-memory neighbour tiles of the single-type FP32-force step (null: off)
+    uint32_t* tile_tab = nullptr;
     // temperature table of a varying kT (allocated on the first
     // azp_md_set_temperatures; null while kT is the constant of the config)
     unsigned long long* d_kT_hdr = nullptr;
@@ -635,7 +637,7 @@ void free_all(azp_md* m)
                     m->partials, m->thermo, m->tmp4, m->tmpd, m->snap_pos, m->snap_vel, m->snap_acc,
                     m->snap_img, m->snap_diam, m->st_pos, m->st_vel, m->st_acc, m->st_img, m->st_diam,
                     m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab, m->d_dvel, m->d_img0,
-                    m->d_kT_hdr, m->d_kT_tab, m->d_noise_tab};
+                    m->d_kT_hdr, m->d_kT_tab, m->d_noise_tab, m->tile_tab};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -736,6 +738,7 @@ MDArgs base_args(azp_md* m)
     a.kT_hdr = m->d_kT_hdr;
     a.kT_tab = m->d_kT_tab;
     a.noise_tab = m->d_noise_tab;
+    a.tile = m->tile_tab;
     a.flowf.kind = m->flow.kind;
     if (m->flow.kind == AZP_FLOW_PARABOLIC) {
         a.flowf.a = (float)m->flow.a;
@@ -796,10 +799,11 @@ int enqueue_rebuild(azp_md* m, cudaStream_t s, const uint32_t* gate)
         k_bond_table<<<nb, 256, 0, s>>>(m->tag, m->rtag, m->bt_n_tag, m->bt_partner_tag, m->bt_type_tag, N, m->bt_n,
                                         m->bt, m->ex_n, m->ex_idx, m->exclude_bonds, gate);
     if (!fx) launch_to_fixed2(m->pos[m->cur], m->fix[m->cur], m->fix_build, N, m->box, s, gate);
+    if (m->tile_tab) launch_tile_table(m->cell_of, m->cell_start, m->grid, N, m->tile_tab, gate, s);
     if (m->pair_kind >= 0)
         launch_nlist_build(fx ? nullptr : m->pos[m->cur], m->fix[m->cur], N, m->box, m->grid, m->cell_start, nullptr,
                            m->cell_of, m->cuts, m->ntypes, m->ex_n, m->ex_idx, m->bt_width, nullptr, m->counts, m->nbrs,
-                           m->max_nn, m->flags + 3, gate, s, fx ? m->lo[m->cur] : nullptr, m->rlist_min);
+                           m->max_nn, m->flags + 3, gate, s, fx ? m->lo[m->cur] : nullptr, m->rlist_min, m->tile_tab);
     k_finish_rebuild<<<1, 1, 0, s>>>(m->flags, gate);
     AZP_CHECK_LAUNCH("enqueue_rebuild");
     m->launches += 11 + (m->bond_kind >= 0) + (m->pair_kind >= 0) - (fx ? 1 : 0);
@@ -1186,6 +1190,13 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         CTRY(cudaMemcpy(m->cuts, cuts.data(), sizeof(ListCut) * nt2, cudaMemcpyHostToDevice));
         m->max_nn = 32;
         ALLOC(m->nbrs, (size_t)N * m->max_nn);
+        // the single-type FP32-force step reads its neighbours from shared-memory
+        // tiles (AZP_TILES=0 keeps plain gathers, for comparison)
+        const char* env_tiles = std::getenv("AZP_TILES");
+        const bool one = c->ntypes == 1 && (c->bond_kind < 0 || c->nbondtypes <= 1) && !c->use_lambda;
+        if (c->precision == AZP_FP32 && one && m->tpp == 1 && m->pair_kind != AZP_PAIR_DPD_GENERAL_WEIGHT &&
+            m->bond_kind != AZP_BOND_IMAGE_HARMONIC && !(env_tiles && env_tiles[0] == '0'))
+            ALLOC(m->tile_tab, (size_t)((N + TILE_P - 1) / TILE_P) * TILE_REC);
     }
     m->grid = make_grid(m->box, m->rlist_max > 0.0 ? m->rlist_max : std::max(m->box.L[0], 1.0));
     ALLOC(m->cell_count, m->grid.ncell);

@@ -107,6 +107,9 @@ struct MDArgs {
     const unsigned long long* kT_hdr;
     const double* kT_tab;       // [rows] kT
     const double* noise_tab;    // [rows][ntypes] sqrt(6 gamma kT / dt), 0 when noiseless
+    // shared-memory neighbour tiles (celllist.cuh): block records, or null when
+    // the list holds plain particle indices
+    const uint32_t* tile;
 };
 
 // does the method move particles of type t?

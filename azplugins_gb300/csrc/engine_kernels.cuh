@@ -10,6 +10,7 @@
 #pragma once
 
 #include "barrier.cuh"
+#include "celllist.cuh"
 #include "engine.cuh"
 #include "philox.cuh"
 #include "evaluators.cuh"
@@ -19,6 +20,11 @@ namespace azp
 {
 static_assert(MD_PAIR_TBL == PAIR_TBL && MD_BOND_F == BOND_F, "record sizes of MDArgs");
 constexpr int MD_BLOCK = 256;
+// threads per block of the FP32-force step
+#ifndef AZP_FX_BLOCK
+#define AZP_FX_BLOCK 256
+#endif
+constexpr int FX_BLOCK = AZP_FX_BLOCK;
 constexpr uint32_t MD_MAX_BOND_TYPES = 32;
 
 struct NoPair {
@@ -694,10 +700,16 @@ AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint3
 // outside r_cut: the evaluator runs on every lane (at r_cut where the pair does
 // not count) and the pair's terms are masked, so a batch has no per-lane exits;
 // only the rare candidate in the band around r_cut takes the exact FP64 branch
-template<class PE>
-AZP_D void pair_term_fx_masked(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j, bool ok,
-                               const float* s_rec, const double* s_rc2, AccFx& acc, bool vir)
+template<class PE, bool TILE = false>
+AZP_D void pair_term_fx_masked(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t ent, bool ok,
+                               const float* s_rec, const double* s_rc2, AccFx& acc, bool vir,
+                               const uint32_t* trec = nullptr)
 {
+    // the particle index of the entry, needed only on the rare exact paths
+    const auto jof = [&]() -> uint32_t {
+        if constexpr (TILE) return tile_decode(trec, ent);
+        return ent;
+    };
     const float dx = (float)(int32_t)(fi.x - fj.x) * a.sfix[0];
     const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
     const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
@@ -708,14 +720,14 @@ AZP_D void pair_term_fx_masked(const MDArgs& a, const uint4& fi, const uint4& fj
     const float rc2 = cut[0];
     const bool on = ok && PE::enabled(rec);
     bool in = on && rsq < rc2 * 0.999996f;
-    if (on && !in && rsq < rc2 * 1.000004f) in = inside_exact(a, i, j, s_rc2[tp]);
+    if (on && !in && rsq < rc2 * 1.000004f) in = inside_exact(a, i, jof(), s_rc2[tp]);
     const float rs = in ? rsq : rc2;
     float fdr, e;
     if constexpr (has_gap_form<PE>::value) {
         if (in && PE::gap_form(rec)) {
             // the cancelling contact difference (colloid point-sphere and
             // sphere-sphere forms) in FP64 from the exact 64-bit displacement
-            const uint4 li = __ldg(a.flo + i), lj = __ldg(a.flo + j);
+            const uint4 li = __ldg(a.flo + i), lj = __ldg(a.flo + jof());
             const double vx = fx_disp(fi.x, li.x, fj.x, lj.x, a.l64[0]);
             const double vy = fx_disp(fi.y, li.y, fj.y, lj.y, a.l64[1]);
             const double vz = fx_disp(fi.z, li.z, fj.z, lj.z, a.l64[2]);
@@ -915,8 +927,11 @@ AZP_D void prefetch_warp_rows(const MDArgs& a, uint32_t i0, uint32_t i_last, uin
 
 // ONE: single-type system, records from the kernel arguments (no shared-memory
 // tables, no block barrier before the work)
-template<class PE, class BE, int INTEG, bool OUT, bool ONE>
-__global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDArgs a)
+// TILE (single-type systems, TILE_P particles per block, one thread each): the
+// block's neighbour ranges are staged in shared memory first and the list
+// entries address them there (celllist.cuh, TILE_GLOBAL entries are gathered)
+template<class PE, class BE, int INTEG, bool OUT, bool ONE, bool TILE = false>
+__global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t nt2 = a.ntypes * a.ntypes;
@@ -925,12 +940,25 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
     float* s_bond = s_rec + nt2 * PAIR_TBL;
     float* s_gamma = s_bond + a.nbondtypes * BOND_F;
     float* s_noise = s_gamma + a.ntypes;
+    const uint4* s_tile = reinterpret_cast<const uint4*>(smem_raw);
+    const uint32_t* trec = nullptr;
     if constexpr (ONE) {
         s_rc2 = &a.rc2_0;
         s_rec = a.rec0;
         s_bond = a.bond0;
         s_gamma = &a.gamma0;
         s_noise = &a.noise0;
+        if constexpr (TILE) {
+            // stage the block's neighbour ranges: coalesced 16-byte copies
+            trec = a.tile + (size_t)blockIdx.x * TILE_REC;
+            const uint32_t nr = __ldg(trec);
+            uint4* st = reinterpret_cast<uint4*>(smem_raw);
+            for (uint32_t k = 0; k < nr; ++k) {
+                const uint32_t b = __ldg(trec + 2 + 3 * k), e = __ldg(trec + 3 + 3 * k), off = __ldg(trec + 4 + 3 * k);
+                for (uint32_t q = threadIdx.x; q < e - b; q += blockDim.x) st[off + q] = __ldg(a.fix + b + q);
+            }
+            __syncthreads();
+        }
     } else {
         if (!std::is_same<PE, NoPair>::value)
             for (uint32_t t = threadIdx.x; t < nt2 * PAIR_TBL; t += blockDim.x) {
@@ -957,7 +985,7 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
     // walls first, while nothing else is live: an FP32 screen on the high words,
     // then the FP64 evaluation on the full 64-bit position for the particles some
     // wall can reach; the result waits in this thread's shared-memory slot
-    __shared__ float4 s_wall[MD_BLOCK];
+    __shared__ float4 s_wall[FX_BLOCK];
     if (a.wall_kind >= 0 && active && sub == 0) {
         const uint4 hw = __ldg(a.fix + i);
         double fw[4] = {0.0, 0.0, 0.0, 0.0};
@@ -1013,10 +1041,16 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
 #pragma unroll
                 for (int u = 0; u < FX_BATCH; ++u) {
                     const uint32_t k = kb + u * tpp;
-                    jj[u] = k < n ? __ldg(col + (size_t)k * a.N) : i;
+                    jj[u] = k < n ? __ldg(col + (size_t)k * a.N) : (TILE ? (TILE_GLOBAL | i) : i);
                 }
+                if constexpr (TILE) {
 #pragma unroll
-                for (int u = 0; u < FX_BATCH; ++u) fj[u] = __ldg(a.fix + jj[u]);
+                    for (int u = 0; u < FX_BATCH; ++u)
+                        fj[u] = (jj[u] & TILE_GLOBAL) ? __ldg(a.fix + (jj[u] & ~TILE_GLOBAL)) : s_tile[jj[u]];
+                } else {
+#pragma unroll
+                    for (int u = 0; u < FX_BATCH; ++u) fj[u] = __ldg(a.fix + jj[u]);
+                }
 #pragma unroll
                 for (int u = 0; u < FX_BATCH; ++u) {
                     if constexpr (std::is_same<PE, DpdEngine>::value) {
@@ -1024,7 +1058,8 @@ __global__ void __launch_bounds__(MD_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
                             pair_term_dpd_fx(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir, vi, tgi, k0, k1);
                     } else {
 #if AZP_FX_UNIFORM
-                        pair_term_fx_masked<PE>(a, fi, fj[u], i, jj[u], kb + u * tpp < n, s_rec, s_rc2, acc, vir);
+                        pair_term_fx_masked<PE, TILE>(a, fi, fj[u], i, jj[u], kb + u * tpp < n, s_rec, s_rc2, acc,
+                                                      vir, trec);
 #else
                         if (kb + u * tpp < n) pair_term_fx<PE>(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir);
 #endif
@@ -1177,17 +1212,33 @@ template<class PE, class BE, typename R, int INTEG>
 int launch_md_t(const MDArgs& a, cudaStream_t s)
 {
     const size_t threads = (size_t)a.N * a.tpp;
-    const uint32_t blocks = (uint32_t)((threads + MD_BLOCK - 1) / MD_BLOCK);
+    const int bs = std::is_same<R, float>::value ? FX_BLOCK : MD_BLOCK;
+    const uint32_t blocks = (uint32_t)((threads + bs - 1) / bs);
     if (blocks == 0) return AZP_OK;
     const size_t nt2 = (size_t)a.ntypes * a.ntypes;
     if constexpr (std::is_same<R, float>::value) {
         const size_t smem = nt2 * sizeof(double) + nt2 * PAIR_TBL * sizeof(float) +
                             (size_t)a.nbondtypes * BOND_F * sizeof(float) + 2 * a.ntypes * sizeof(float);
+        constexpr bool can_tile = !std::is_same<PE, NoPair>::value && !std::is_same<PE, DpdEngine>::value &&
+                                  !bond_uses_image<BE>::value;
         auto k = a.out ? (a.one_type ? k_md_step_fx<PE, BE, INTEG, true, true> : k_md_step_fx<PE, BE, INTEG, true, false>)
                        : (a.one_type ? k_md_step_fx<PE, BE, INTEG, false, true>
                                      : k_md_step_fx<PE, BE, INTEG, false, false>);
-        if (smem > 48 * 1024) AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<blocks, MD_BLOCK, smem, s>>>(a);
+        size_t smem_k = smem;
+        if (a.tile && (FX_BLOCK != (int)TILE_P || a.tpp != 1 || !a.one_type || !can_tile))
+            return record_error(AZP_ERR_UNSUPPORTED, "k_md_step_fx: tiles need one type, 256-thread blocks, tpp 1");
+        if constexpr (can_tile) {
+            if (a.tile) {
+                k = a.out ? k_md_step_fx<PE, BE, INTEG, true, true, true> : k_md_step_fx<PE, BE, INTEG, false, true, true>;
+                smem_k = (size_t)TILE_CAP * sizeof(uint4);
+            }
+        }
+        if (smem_k > 32 * 1024)
+            AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
+#ifdef AZP_FX_CARVEOUT
+        AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, AZP_FX_CARVEOUT));
+#endif
+        k<<<blocks, FX_BLOCK, smem_k, s>>>(a);
         AZP_CHECK_LAUNCH("k_md_step_fx");
     } else {
         const size_t smem = nt2 * sizeof(double) + 2 * a.ntypes * sizeof(double) + nt2 * PAIR_TBL * sizeof(R) +

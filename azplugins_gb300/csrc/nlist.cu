@@ -186,6 +186,7 @@ __global__ void k_cell_assign_fx(const uint4* __restrict__ fixed, uint32_t N, Ce
 
 constexpr uint32_t MAX_LIST_TYPES = 16;  // ntypes^2 <= 256 thresholds in shared memory
 constexpr int NLIST_BLOCK = 128;
+static_assert(TILE_P % NLIST_BLOCK == 0, "a list-build block lies inside one tile block");
 constexpr uint32_t NL_EX_REG = 4;  // exclusion keys of a particle held in registers
 
 // The oracle's exact FP64 decision for a candidate inside the ambiguous band
@@ -227,12 +228,17 @@ __global__ void __launch_bounds__(NLIST_BLOCK)
                           const uint32_t* __restrict__ ex_n, const uint32_t* __restrict__ ex_keys,
                           const uint32_t* __restrict__ keys, uint32_t* __restrict__ counts,
                           uint32_t* __restrict__ nbrs, uint32_t max_nn, uint32_t* __restrict__ flags,
-                          const uint32_t* __restrict__ gate, const uint4* __restrict__ lo)
+                          const uint32_t* __restrict__ gate, const uint4* __restrict__ lo,
+                          const uint32_t* __restrict__ tile)
 {
     if (gated_off(gate)) return;
     __shared__ ListCut s_cut[MAX_LIST_TYPES * MAX_LIST_TYPES];
+    // the tile record of this block's particles (NLIST_BLOCK divides TILE_P)
+    __shared__ uint32_t s_trec[TILE_REC];
     const uint32_t nt2 = ntypes * ntypes;
     for (uint32_t t = threadIdx.x; t < nt2; t += blockDim.x) s_cut[t] = cuts[t];
+    if (tile && threadIdx.x < TILE_REC)
+        s_trec[threadIdx.x] = tile[(size_t)(blockIdx.x * blockDim.x / TILE_P) * TILE_REC + threadIdx.x];
     __syncthreads();
 
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -314,12 +320,102 @@ __global__ void __launch_bounds__(NLIST_BLOCK)
             if (nex > NL_EX_REG) drop |= nl_excluded_tail(i, kj, nex, N, ex_keys);
         }
         if (!drop) {
-            if (m != k) nbrs[(size_t)m * N + i] = j;
+            if (tile) nbrs[(size_t)m * N + i] = tile_encode(s_trec, j);
+            else if (m != k) nbrs[(size_t)m * N + i] = j;
             ++m;
         }
     }
     counts[i] = n > max_nn ? n : m;
     if (n > max_nn) atomicMax(&flags[0], n);
+}
+
+// Block records of the shared-memory tiles: for every stencil row of the block's
+// TILE_P particles, the range of particle indices that row's x-ranges cover
+// (cx - 1 .. cx + 1 clipped to the row; the wrapped cell at an x face stays
+// outside and is addressed globally), merged into disjoint ranges in increasing
+// order with their offsets in the tile. A block whose ranges exceed TILE_CAP
+// records (a row wrapping through a y or z face makes its range span most of the
+// box) gets 0 ranges: its entries are all global.
+__global__ void __launch_bounds__(TILE_P) k_tile_table(const uint32_t* __restrict__ cell_of,
+                                                       const uint32_t* __restrict__ cell_start, CellGrid g, uint32_t N,
+                                                       uint32_t* __restrict__ tab, const uint32_t* __restrict__ gate)
+{
+    if (gated_off(gate)) return;
+    __shared__ uint32_t s_lo[TILE_MAX_RANGES], s_hi[TILE_MAX_RANGES];
+    if (threadIdx.x < TILE_MAX_RANGES) {
+        s_lo[threadIdx.x] = 0xffffffffu;
+        s_hi[threadIdx.x] = 0u;
+    }
+    __syncthreads();
+    const uint32_t i = blockIdx.x * TILE_P + threadIdx.x;
+    if (i < N) {
+        const uint32_t cc = __ldg(cell_of + i);
+        const int dx = g.dim[0], dy = g.dim[1], dz = g.dim[2];
+        const int cx = (int)(cc % (uint32_t)dx);
+        const int cy = (int)((cc / (uint32_t)dx) % (uint32_t)dy);
+        const int cz = (int)(cc / ((uint32_t)dx * (uint32_t)dy));
+        const int x0 = max(cx - g.reach[0], 0), x1 = min(cx + g.reach[0], dx - 1);
+        uint32_t r = 0;
+        for (int oz = -g.reach[2]; oz <= g.reach[2]; ++oz) {
+            int nz = cz + oz;
+            nz += (nz < 0) ? dz : 0;
+            nz -= (nz >= dz) ? dz : 0;
+            for (int oy = -g.reach[1]; oy <= g.reach[1]; ++oy, ++r) {
+                int ny = cy + oy;
+                ny += (ny < 0) ? dy : 0;
+                ny -= (ny >= dy) ? dy : 0;
+                const uint32_t rb = ((uint32_t)nz * dy + ny) * dx;
+                const uint32_t sb = __ldg(cell_start + rb + x0), se = __ldg(cell_start + rb + x1 + 1);
+                if (se > sb) {
+                    atomicMin(&s_lo[r], sb);
+                    atomicMax(&s_hi[r], se);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    uint32_t lo[TILE_MAX_RANGES], hi[TILE_MAX_RANGES], n = 0;
+    for (uint32_t r = 0; r < TILE_MAX_RANGES; ++r)
+        if (s_hi[r] > s_lo[r]) {
+            // insertion by begin
+            uint32_t k = n++;
+            while (k > 0 && lo[k - 1] > s_lo[r]) {
+                lo[k] = lo[k - 1];
+                hi[k] = hi[k - 1];
+                --k;
+            }
+            lo[k] = s_lo[r];
+            hi[k] = s_hi[r];
+        }
+    // merge overlapping or touching ranges
+    uint32_t m = 0;
+    for (uint32_t k = 0; k < n; ++k) {
+        if (m > 0 && lo[k] <= hi[m - 1]) {
+            hi[m - 1] = max(hi[m - 1], hi[k]);
+        } else {
+            lo[m] = lo[k];
+            hi[m] = hi[k];
+            ++m;
+        }
+    }
+    uint32_t* t = tab + (size_t)blockIdx.x * TILE_REC;
+    uint32_t total = 0;
+    for (uint32_t k = 0; k < m; ++k) {
+        t[2 + 3 * k] = lo[k];
+        t[3 + 3 * k] = hi[k];
+        t[4 + 3 * k] = total;
+        total += hi[k] - lo[k];
+    }
+    t[0] = total <= TILE_CAP ? m : 0u;
+    t[1] = total;
+}
+
+void launch_tile_table(const uint32_t* cell_of, const uint32_t* cell_start, const CellGrid& g, uint32_t N,
+                       uint32_t* tab, const uint32_t* gate, cudaStream_t s)
+{
+    if (N == 0) return;
+    k_tile_table<<<(N + TILE_P - 1) / TILE_P, TILE_P, 0, s>>>(cell_of, cell_start, g, N, tab, gate);
 }
 
 // ---------------------------------------------------------------- launch helpers
@@ -373,7 +469,7 @@ void launch_nlist_build(const double4_32a* pos, const uint4* fixed, uint32_t N, 
                         const ListCut* cuts, uint32_t ntypes, const uint32_t* ex_n, const uint32_t* ex_keys,
                         uint32_t ex_width, const uint32_t* keys, uint32_t* counts, uint32_t* nbrs,
                         uint32_t max_nn, uint32_t* flags, const uint32_t* gate, cudaStream_t s, const uint4* lo,
-                        double rlist_min)
+                        double rlist_min, const uint32_t* tile)
 {
     (void)ex_width;
     (void)rlist_min;
@@ -382,7 +478,7 @@ void launch_nlist_build(const double4_32a* pos, const uint4* fixed, uint32_t N, 
     const uint32_t blocks = (N + NLIST_BLOCK - 1) / NLIST_BLOCK;
 #define AZP_NL_ARGS                                                                                              \
     pos, fixed, N, bx, g, cell_start, members, cell_of, cuts, ntypes, ex_n, ex_keys, keys, counts, nbrs, max_nn, \
-        flags, gate, lo
+        flags, gate, lo, members ? nullptr : tile
     if (ntypes == 1) {
         if (members) k_nlist_build_threads<true, false><<<blocks, NLIST_BLOCK, 0, s>>>(AZP_NL_ARGS);
         else k_nlist_build_threads<true, true><<<blocks, NLIST_BLOCK, 0, s>>>(AZP_NL_ARGS);
