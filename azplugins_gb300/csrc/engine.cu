@@ -1190,12 +1190,13 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         CTRY(cudaMemcpy(m->cuts, cuts.data(), sizeof(ListCut) * nt2, cudaMemcpyHostToDevice));
         m->max_nn = 32;
         ALLOC(m->nbrs, (size_t)N * m->max_nn);
-        // the single-type FP32-force step reads its neighbours from shared-memory
-        // tiles (AZP_TILES=0 keeps plain gathers, for comparison)
+        // AZP_TILES=1: the single-type FP32-force step reads its neighbours from
+        // shared-memory tiles instead of gathering them (bit-identical results;
+        // measured slower on the bead-spring melt, so off by default)
         const char* env_tiles = std::getenv("AZP_TILES");
         const bool one = c->ntypes == 1 && (c->bond_kind < 0 || c->nbondtypes <= 1) && !c->use_lambda;
         if (c->precision == AZP_FP32 && one && m->tpp == 1 && m->pair_kind != AZP_PAIR_DPD_GENERAL_WEIGHT &&
-            m->bond_kind != AZP_BOND_IMAGE_HARMONIC && !(env_tiles && env_tiles[0] == '0'))
+            m->bond_kind != AZP_BOND_IMAGE_HARMONIC && env_tiles && env_tiles[0] == '1')
             ALLOC(m->tile_tab, (size_t)((N + TILE_P - 1) / TILE_P) * TILE_REC);
     }
     m->grid = make_grid(m->box, m->rlist_max > 0.0 ? m->rlist_max : std::max(m->box.L[0], 1.0));

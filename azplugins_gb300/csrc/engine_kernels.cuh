@@ -1235,9 +1235,6 @@ int launch_md_t(const MDArgs& a, cudaStream_t s)
         }
         if (smem_k > 32 * 1024)
             AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
-#ifdef AZP_FX_CARVEOUT
-        AZP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, AZP_FX_CARVEOUT));
-#endif
         k<<<blocks, FX_BLOCK, smem_k, s>>>(a);
         AZP_CHECK_LAUNCH("k_md_step_fx");
     } else {
