@@ -294,19 +294,18 @@ __global__ void k_store_state_fx(const uint4* __restrict__ fix, const uint4* __r
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
     const uint32_t i = rtag[t];
+    // 16-byte stores: the outputs may be the caller's pinned buffers, written over the host link
     if (pos_out) {
         const uint4 h = fix[i], l = lo[i];
-        pos_out[4 * t] = fx_to_double(fx_join(h.x, l.x), l0);
-        pos_out[4 * t + 1] = fx_to_double(fx_join(h.y, l.y), l1);
-        pos_out[4 * t + 2] = fx_to_double(fx_join(h.z, l.z), l2);
-        pos_out[4 * t + 3] = (double)h.w;
+        reinterpret_cast<double2*>(pos_out)[2 * t] =
+            make_double2(fx_to_double(fx_join(h.x, l.x), l0), fx_to_double(fx_join(h.y, l.y), l1));
+        reinterpret_cast<double2*>(pos_out)[2 * t + 1] = make_double2(fx_to_double(fx_join(h.z, l.z), l2), (double)h.w);
     }
     if (vel_out) {
         const VelFF v = vel[i];
-        vel_out[4 * t] = (double)v.h.x + (double)v.l.x;
-        vel_out[4 * t + 1] = (double)v.h.y + (double)v.l.y;
-        vel_out[4 * t + 2] = (double)v.h.z + (double)v.l.z;
-        vel_out[4 * t + 3] = mass[i];
+        reinterpret_cast<double2*>(vel_out)[2 * t] =
+            make_double2((double)v.h.x + (double)v.l.x, (double)v.h.y + (double)v.l.y);
+        reinterpret_cast<double2*>(vel_out)[2 * t + 1] = make_double2((double)v.h.z + (double)v.l.z, mass[i]);
     }
     for (int d = 0; d < 3; ++d) {
         if (accel_out) accel_out[3 * t + d] = accel[3 * i + d];
@@ -431,9 +430,13 @@ __global__ void k_load_state_ordered(const double* __restrict__ pos_in, const do
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
     const uint32_t i = rtag[t];
-    pos[i] = make_double4_32a(pos_in[4 * t], pos_in[4 * t + 1], pos_in[4 * t + 2],
-                              type_as_double((uint32_t)pos_in[4 * t + 3]));
-    vel[i] = make_double4_32a(vel_in[4 * t], vel_in[4 * t + 1], vel_in[4 * t + 2], vel_in[4 * t + 3]);
+    // 16-byte loads: the inputs may be the caller's pinned buffers, read over the host link
+    const double2 p01 = reinterpret_cast<const double2*>(pos_in)[2 * t];
+    const double2 p23 = reinterpret_cast<const double2*>(pos_in)[2 * t + 1];
+    const double2 v01 = reinterpret_cast<const double2*>(vel_in)[2 * t];
+    const double2 v23 = reinterpret_cast<const double2*>(vel_in)[2 * t + 1];
+    pos[i] = make_double4_32a(p01.x, p01.y, p23.x, type_as_double((uint32_t)p23.y));
+    vel[i] = make_double4_32a(v01.x, v01.y, v23.x, v23.y);
     for (int d = 0; d < 3; ++d) {
         accel[3 * i + d] = accel_in ? accel_in[3 * t + d] : 0.0;
         image[3 * i + d] = image_in ? image_in[3 * t + d] : 0;
@@ -956,6 +959,30 @@ int check_errors(azp_md* m, cudaStream_t s)
     return AZP_OK;
 }
 
+// The device address of a host buffer the GPU can read and write in place:
+// pinned memory mapped into the unified address space (cudaHostAlloc,
+// cudaHostRegister, torch's pin_memory). On GB300 such a buffer is reached over
+// NVLink-C2C, so the state kernels move it without a staging copy. Null for
+// pageable memory (staged instead) or when AZP_ZERO_COPY=0.
+void* mapped_view(const void* h)
+{
+    if (!h) return nullptr;
+    static const bool off = [] {
+        const char* e = std::getenv("AZP_ZERO_COPY");
+        return e && e[0] == '0';
+    }();
+    if (off) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (at.type == cudaMemoryTypeHost && at.devicePointer) ? at.devicePointer : nullptr;
+}
+
+// the state kernels move positions and velocities as 16-byte pairs
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0u; }
+
 // staging buffers of the host transfers (first use only)
 int ensure_staging(azp_md* m)
 {
@@ -1316,8 +1343,11 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
     if (!on_device) {
         int st0 = ensure_staging(m);
         if (st0) return st0;
+        // pinned buffers are read in place by the load kernels; pageable ones staged
         auto up = [&](const void* h, void* d, size_t bytes) -> const void* {
             if (!h) return nullptr;
+            if (aligned16(h))
+                if (void* v = mapped_view(h)) return v;
             cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s);
             return d;
         };
@@ -1327,6 +1357,14 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         di = (const int*)up(image, m->st_img, sizeof(int) * 3 * N);
         dd = (const double*)up(diameter, m->st_diam, sizeof(double) * N);
         AZP_CHECK_LAUNCH("azp_md_set_state (host to device)");
+    } else if (!aligned16(pos) || !aligned16(vel)) {
+        // device inputs not on a 16-byte boundary: aligned copies first
+        int st0 = ensure_staging(m);
+        if (st0) return st0;
+        AZP_CUDA_TRY(cudaMemcpyAsync(m->st_pos, pos, sizeof(double) * 4 * N, cudaMemcpyDeviceToDevice, s));
+        AZP_CUDA_TRY(cudaMemcpyAsync(m->st_vel, vel, sizeof(double) * 4 * N, cudaMemcpyDeviceToDevice, s));
+        dp = m->st_pos;
+        dv = m->st_vel;
     }
     m->cur = 0;
     m->forces_valid = false;
@@ -1408,9 +1446,22 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
         *timestep = ts;
     }
     if (N == 0) return AZP_OK;
-    if (on_device) {
+    if (on_device && aligned16(pos) && aligned16(vel)) {
         enqueue_store_state(m, pos, vel, accel, image, s);
         AZP_CHECK_LAUNCH("k_store_state");
+        return AZP_OK;
+    }
+    const cudaMemcpyKind back = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    // pinned outputs are written in place by the store kernel; pageable ones staged
+    void* vp = on_device || !aligned16(pos) ? nullptr : mapped_view(pos);
+    void* vv = on_device || !aligned16(vel) ? nullptr : mapped_view(vel);
+    void* va = on_device ? nullptr : mapped_view(accel);
+    void* vi = on_device ? nullptr : mapped_view(image);
+    if ((!pos || vp) && (!vel || vv) && (!accel || va) && (!image || vi)) {
+        enqueue_store_state(m, static_cast<double*>(vp), static_cast<double*>(vv), static_cast<double*>(va),
+                            static_cast<int*>(vi), s);
+        AZP_CHECK_LAUNCH("k_store_state");
+        AZP_CUDA_TRY(cudaStreamSynchronize(s));
         return AZP_OK;
     }
     int st0 = ensure_staging(m);
@@ -1421,11 +1472,11 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
     int* di = image ? m->st_img : nullptr;
     enqueue_store_state(m, dp, dv, da, di, s);
     AZP_CHECK_LAUNCH("k_store_state");
-    if (pos) AZP_CUDA_TRY(cudaMemcpyAsync(pos, dp, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, s));
-    if (vel) AZP_CUDA_TRY(cudaMemcpyAsync(vel, dv, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, s));
-    if (accel) AZP_CUDA_TRY(cudaMemcpyAsync(accel, da, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
-    if (image) AZP_CUDA_TRY(cudaMemcpyAsync(image, di, sizeof(int) * 3 * N, cudaMemcpyDeviceToHost, s));
-    AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    if (pos) AZP_CUDA_TRY(cudaMemcpyAsync(pos, dp, sizeof(double) * 4 * N, back, s));
+    if (vel) AZP_CUDA_TRY(cudaMemcpyAsync(vel, dv, sizeof(double) * 4 * N, back, s));
+    if (accel) AZP_CUDA_TRY(cudaMemcpyAsync(accel, da, sizeof(double) * 3 * N, back, s));
+    if (image) AZP_CUDA_TRY(cudaMemcpyAsync(image, di, sizeof(int) * 3 * N, back, s));
+    if (!on_device) AZP_CUDA_TRY(cudaStreamSynchronize(s));
     return AZP_OK;
 }
 

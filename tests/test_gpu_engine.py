@@ -540,3 +540,59 @@ def test_shared_memory_tiles_match_plain_gathers(bonds):
     assert np.array_equal(a[0].position, b[0].position)
     assert np.array_equal(a[0].velocity, b[0].velocity)
     assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+
+
+def test_state_transfers_from_unaligned_device_buffers():
+    """Device state buffers that start 8 bytes past a 16-byte boundary (the state
+    kernels move positions and velocities as 16-byte pairs) go through aligned
+    copies and give the same state as aligned buffers."""
+    import ctypes
+
+    import torch
+
+    from azplugins_gb300 import _lib, workloads
+
+    for precision in ("fp64", "fp32"):
+        snap = workloads.lj_fluid(n_side=8, density=0.8, seed=43)
+        snap.particles.acceleration = np.zeros((snap.particles.N, 3))
+        sim, lj = _lj_setup(snap, precision=precision)
+        sim.run(10)
+        eng = sim._engine
+        N = snap.particles.N
+        L = eng._L
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+        def buffers(shift):
+            raw = [torch.zeros(N * 4 + 2, dtype=torch.float64, device="cuda") for _ in range(2)]
+            pos, vel = (r[shift:shift + 4 * N] for r in raw)
+            acc = torch.zeros(N * 3, dtype=torch.float64, device="cuda")
+            img = torch.zeros(N * 3, dtype=torch.int32, device="cuda")
+            return raw, pos, vel, acc, img
+
+        got = []
+        for shift in (0, 1):
+            raw, pos, vel, acc, img = buffers(shift)
+            assert (pos.data_ptr() % 16 == 0) == (shift == 0)
+            _lib.check(L.azp_md_get_state(eng._md, pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), img.data_ptr(), None,
+                                          1, stream), "azp_md_get_state")
+            torch.cuda.synchronize()
+            got.append([t.clone() for t in (pos, vel, acc, img)])
+        for x, y in zip(*got):
+            assert torch.equal(x, y)
+        # set from the unaligned copy, run, read back: equal to the aligned round trip
+        outs = []
+        for shift in (0, 1):
+            raw, pos, vel, acc, img = buffers(shift)
+            for t, v in zip((pos, vel, acc, img), got[0]):
+                t.copy_(v)
+            _lib.check(L.azp_md_set_state(eng._md, pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), img.data_ptr(),
+                                          None, 10, 1, stream), "azp_md_set_state")
+            _lib.check(L.azp_md_run(eng._md, 5, stream), "azp_md_run")
+            o = [torch.zeros_like(t) for t in got[0]]
+            _lib.check(L.azp_md_get_state(eng._md, o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(), o[3].data_ptr(),
+                                          None, 1, stream), "azp_md_get_state")
+            torch.cuda.synchronize()
+            outs.append(o)
+        for x, y in zip(*outs):
+            assert torch.equal(x, y)
+        sim.close()
