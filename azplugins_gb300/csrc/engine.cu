@@ -360,13 +360,24 @@ __global__ void k_thermo_partials(const double4_32a* __restrict__ f, const doubl
         for (int c = 0; c < 8; ++c) part[(size_t)blockIdx.x * 8 + c] = s[0][c];
 }
 
-__global__ void k_thermo_final(const double* __restrict__ part, uint32_t nb, double* __restrict__ out)
+// one block of THERMO_BLOCK threads: thread t sums the partials of blocks t,
+// t + THERMO_BLOCK, ... in order, then a fixed tree adds the threads' sums (the
+// same order every call)
+__global__ void __launch_bounds__(THERMO_BLOCK) k_thermo_final(const double* __restrict__ part, uint32_t nb,
+                                                              double* __restrict__ out)
 {
-    const int c = threadIdx.x;
-    if (c >= 8) return;
-    double acc = 0.0;
-    for (uint32_t b = 0; b < nb; ++b) acc += part[(size_t)b * 8 + c];
-    out[c] = acc;
+    __shared__ double s[THERMO_BLOCK][8];
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t b = threadIdx.x; b < nb; b += THERMO_BLOCK)
+        for (int c = 0; c < 8; ++c) acc[c] += part[(size_t)b * 8 + c];
+    for (int c = 0; c < 8; ++c) s[threadIdx.x][c] = acc[c];
+    __syncthreads();
+    for (int st = THERMO_BLOCK / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st)
+            for (int c = 0; c < 8; ++c) s[threadIdx.x][c] += s[threadIdx.x + st][c];
+        __syncthreads();
+    }
+    if (threadIdx.x < 8) out[threadIdx.x] = s[0][threadIdx.x];
 }
 
 // index order -> tag order
@@ -1647,7 +1658,7 @@ int azp_md_thermo(azp_md* m, double* out, void* stream)
     }
     const uint32_t nb = blocks_for(N, THERMO_BLOCK);
     k_thermo_partials<<<nb, THERMO_BLOCK, 0, s>>>(m->out_force, m->out_virial, m->vel, m->mass, N, m->partials);
-    k_thermo_final<<<1, 32, 0, s>>>(m->partials, nb, m->thermo);
+    k_thermo_final<<<1, THERMO_BLOCK, 0, s>>>(m->partials, nb, m->thermo);
     AZP_CHECK_LAUNCH("azp_md_thermo");
     double h[8];
     uint32_t f[8];
@@ -1656,7 +1667,11 @@ int azp_md_thermo(azp_md* m, double* out, void* stream)
     AZP_CUDA_TRY(cudaStreamSynchronize(s));
     for (int c = 0; c < 8; ++c) out[c] = h[c];
     out[8] = (double)f[2];
-    return check_errors(m, s);
+    // the error word came back with the sums (check_errors without a second read)
+    if (f[3] > m->max_nn) return AZP_ERR_NLIST_OVERFLOW;
+    if (f[1] & AZP_EBIT_BOND) return AZP_ERR_BOND;
+    if (f[1] & AZP_EBIT_NONFINITE) return AZP_ERR_NONFINITE;
+    return AZP_OK;
 }
 
 int azp_md_error(azp_md* m, uint32_t* err_word, void* stream)
