@@ -282,35 +282,80 @@ __global__ void k_state_to_fx(const double4_32a* __restrict__ pos, double4_32a* 
     *reinterpret_cast<VelFF*>(vel + i) = f;
 }
 
-// FP32-force mode: device state -> tag order output (the k_store_state layout)
-__global__ void k_store_state_fx(const uint4* __restrict__ fix, const uint4* __restrict__ lo,
-                                 const VelFF* __restrict__ vel, const double* __restrict__ mass,
-                                 const double* __restrict__ accel, const int* __restrict__ image,
-                                 const uint32_t* __restrict__ rtag, uint32_t N, double l0, double l1, double l2,
-                                 double* __restrict__ pos_out, double* __restrict__ vel_out,
-                                 double* __restrict__ accel_out, int* __restrict__ image_out)
+// Rows of three per particle (accelerations, image counts) of one full block of
+// STATE_BLOCK tags move between the caller's buffer and shared memory as 16-byte
+// vectors, so that over the host link they travel in whole lines; a partial last
+// block, or a buffer off a 16-byte boundary, moves them one element at a time.
+constexpr int STATE_BLOCK = 256;
+
+template <class T>
+__device__ __forceinline__ void rows3_copy(T* __restrict__ dst, const T* __restrict__ src)
 {
+    static_assert(3 * STATE_BLOCK * sizeof(T) % 16 == 0, "whole vectors per block");
+    constexpr int NV = 3 * STATE_BLOCK * (int)sizeof(T) / 16;
+    for (int k = threadIdx.x; k < NV; k += STATE_BLOCK)
+        reinterpret_cast<uint4*>(dst)[k] = reinterpret_cast<const uint4*>(src)[k];
+}
+
+// Writes particle i's rows of three (tag t, thread `lane` of the block) to the
+// block's shared rows or straight to the outputs; the block then writes its shared
+// rows out whole. `vec` is uniform over the block.
+__device__ __forceinline__ void store_rows3(const double* __restrict__ accel, const int* __restrict__ image,
+                                            uint32_t i, uint32_t t, bool live, bool vec, double* s_acc, int* s_img,
+                                            double* __restrict__ accel_out, int* __restrict__ image_out,
+                                            uint32_t t0)
+{
+    if (live)
+        for (int d = 0; d < 3; ++d) {
+            if (accel_out) {
+                const double a = accel[3 * (size_t)i + d];
+                if (vec) s_acc[3 * threadIdx.x + d] = a;
+                else accel_out[3 * (size_t)t + d] = a;
+            }
+            if (image_out) {
+                const int g = image[3 * (size_t)i + d];
+                if (vec) s_img[3 * threadIdx.x + d] = g;
+                else image_out[3 * (size_t)t + d] = g;
+            }
+        }
+    if (vec) {
+        __syncthreads();
+        if (accel_out) rows3_copy(accel_out + 3 * (size_t)t0, s_acc);
+        if (image_out) rows3_copy(image_out + 3 * (size_t)t0, s_img);
+    }
+}
+
+// FP32-force mode: device state -> tag order output (the k_store_state layout)
+__global__ void __launch_bounds__(STATE_BLOCK)
+    k_store_state_fx(const uint4* __restrict__ fix, const uint4* __restrict__ lo, const VelFF* __restrict__ vel,
+                     const double* __restrict__ mass, const double* __restrict__ accel, const int* __restrict__ image,
+                     const uint32_t* __restrict__ rtag, uint32_t N, double l0, double l1, double l2,
+                     double* __restrict__ pos_out, double* __restrict__ vel_out, double* __restrict__ accel_out,
+                     int* __restrict__ image_out, int rows_aligned)
+{
+    __shared__ __align__(16) double s_acc[3 * STATE_BLOCK];
+    __shared__ __align__(16) int s_img[3 * STATE_BLOCK];
     // one thread per tag: the outputs are written in order
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= N) return;
-    const uint32_t i = rtag[t];
+    const uint32_t t0 = blockIdx.x * STATE_BLOCK;
+    const uint32_t t = t0 + threadIdx.x;
+    const bool live = t < N;
+    const uint32_t i = live ? rtag[t] : 0u;
     // 16-byte stores: the outputs may be the caller's pinned buffers, written over the host link
-    if (pos_out) {
+    if (live && pos_out) {
         const uint4 h = fix[i], l = lo[i];
-        reinterpret_cast<double2*>(pos_out)[2 * t] =
+        reinterpret_cast<double2*>(pos_out)[2 * (size_t)t] =
             make_double2(fx_to_double(fx_join(h.x, l.x), l0), fx_to_double(fx_join(h.y, l.y), l1));
-        reinterpret_cast<double2*>(pos_out)[2 * t + 1] = make_double2(fx_to_double(fx_join(h.z, l.z), l2), (double)h.w);
+        reinterpret_cast<double2*>(pos_out)[2 * (size_t)t + 1] =
+            make_double2(fx_to_double(fx_join(h.z, l.z), l2), (double)h.w);
     }
-    if (vel_out) {
+    if (live && vel_out) {
         const VelFF v = vel[i];
-        reinterpret_cast<double2*>(vel_out)[2 * t] =
+        reinterpret_cast<double2*>(vel_out)[2 * (size_t)t] =
             make_double2((double)v.h.x + (double)v.l.x, (double)v.h.y + (double)v.l.y);
-        reinterpret_cast<double2*>(vel_out)[2 * t + 1] = make_double2((double)v.h.z + (double)v.l.z, mass[i]);
+        reinterpret_cast<double2*>(vel_out)[2 * (size_t)t + 1] = make_double2((double)v.h.z + (double)v.l.z, mass[i]);
     }
-    for (int d = 0; d < 3; ++d) {
-        if (accel_out) accel_out[3 * t + d] = accel[3 * i + d];
-        if (image_out) image_out[3 * t + d] = image[3 * i + d];
-    }
+    store_rows3(accel, image, i, t, live, rows_aligned && t0 + STATE_BLOCK <= N, s_acc, s_img, accel_out,
+                image_out, t0);
 }
 
 // accelerations a = F / m (HOOMD sets them this way before the first step)
@@ -408,21 +453,51 @@ __global__ void k_to_tag_order_i3(const int* __restrict__ src, const uint32_t* _
     dst[3 * t + 2] = src[3 * i + 2];
 }
 
-// tag-order input (pos w = integer-valued type) -> device state, identity order
-__global__ void k_load_state(const double* __restrict__ pos_in, const double* __restrict__ vel_in,
-                             const double* __restrict__ accel_in, const int* __restrict__ image_in,
-                             const double* __restrict__ diam_in, uint32_t N, double4_32a* __restrict__ pos,
-                             double4_32a* __restrict__ vel, double* __restrict__ accel, int* __restrict__ image,
-                             double* __restrict__ diam, uint32_t* __restrict__ tag, uint32_t* __restrict__ rtag)
+// Reads the rows of three of the block's tags (see store_rows3) into shared
+// memory when `vec`; returns particle t's row values either way.
+__device__ __forceinline__ void load_rows3(const double* __restrict__ accel_in, const int* __restrict__ image_in,
+                                           uint32_t t, bool live, bool vec, double* s_acc, int* s_img, uint32_t t0,
+                                           double a[3], int g[3])
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    pos[i] = make_double4_32a(pos_in[4 * i], pos_in[4 * i + 1], pos_in[4 * i + 2],
-                              type_as_double((uint32_t)pos_in[4 * i + 3]));
-    vel[i] = make_double4_32a(vel_in[4 * i], vel_in[4 * i + 1], vel_in[4 * i + 2], vel_in[4 * i + 3]);
+    if (vec) {
+        if (accel_in) rows3_copy(s_acc, accel_in + 3 * (size_t)t0);
+        if (image_in) rows3_copy(s_img, image_in + 3 * (size_t)t0);
+        __syncthreads();
+    }
+    if (!live) return;
     for (int d = 0; d < 3; ++d) {
-        accel[3 * i + d] = accel_in ? accel_in[3 * i + d] : 0.0;
-        image[3 * i + d] = image_in ? image_in[3 * i + d] : 0;
+        a[d] = !accel_in ? 0.0 : vec ? s_acc[3 * threadIdx.x + d] : accel_in[3 * (size_t)t + d];
+        g[d] = !image_in ? 0 : vec ? s_img[3 * threadIdx.x + d] : image_in[3 * (size_t)t + d];
+    }
+}
+
+// tag-order input (pos w = integer-valued type) -> device state, identity order
+__global__ void __launch_bounds__(STATE_BLOCK)
+    k_load_state(const double* __restrict__ pos_in, const double* __restrict__ vel_in,
+                 const double* __restrict__ accel_in, const int* __restrict__ image_in,
+                 const double* __restrict__ diam_in, uint32_t N, double4_32a* __restrict__ pos,
+                 double4_32a* __restrict__ vel, double* __restrict__ accel, int* __restrict__ image,
+                 double* __restrict__ diam, uint32_t* __restrict__ tag, uint32_t* __restrict__ rtag, int rows_aligned)
+{
+    __shared__ __align__(16) double s_acc[3 * STATE_BLOCK];
+    __shared__ __align__(16) int s_img[3 * STATE_BLOCK];
+    const uint32_t t0 = blockIdx.x * STATE_BLOCK;
+    const uint32_t i = t0 + threadIdx.x;
+    const bool live = i < N;
+    double a[3];
+    int g[3];
+    load_rows3(accel_in, image_in, i, live, rows_aligned && t0 + STATE_BLOCK <= N, s_acc, s_img, t0, a, g);
+    if (!live) return;
+    // 16-byte loads: the inputs may be the caller's pinned buffers, read over the host link
+    const double2 p01 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)i];
+    const double2 p23 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)i + 1];
+    const double2 v01 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)i];
+    const double2 v23 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)i + 1];
+    pos[i] = make_double4_32a(p01.x, p01.y, p23.x, type_as_double((uint32_t)p23.y));
+    vel[i] = make_double4_32a(v01.x, v01.y, v23.x, v23.y);
+    for (int d = 0; d < 3; ++d) {
+        accel[3 * (size_t)i + d] = a[d];
+        image[3 * (size_t)i + d] = g[d];
     }
     if (diam) diam[i] = diam_in ? diam_in[i] : 1.0;
     tag[i] = i;
@@ -431,26 +506,34 @@ __global__ void k_load_state(const double* __restrict__ pos_in, const double* __
 
 // tag-order input -> device state in the engine's current index order (particle
 // i takes the input row of its tag); tag / rtag are kept
-__global__ void k_load_state_ordered(const double* __restrict__ pos_in, const double* __restrict__ vel_in,
-                                     const double* __restrict__ accel_in, const int* __restrict__ image_in,
-                                     const double* __restrict__ diam_in, const uint32_t* __restrict__ rtag,
-                                     uint32_t N, double4_32a* __restrict__ pos, double4_32a* __restrict__ vel,
-                                     double* __restrict__ accel, int* __restrict__ image, double* __restrict__ diam)
+__global__ void __launch_bounds__(STATE_BLOCK)
+    k_load_state_ordered(const double* __restrict__ pos_in, const double* __restrict__ vel_in,
+                         const double* __restrict__ accel_in, const int* __restrict__ image_in,
+                         const double* __restrict__ diam_in, const uint32_t* __restrict__ rtag, uint32_t N,
+                         double4_32a* __restrict__ pos, double4_32a* __restrict__ vel, double* __restrict__ accel,
+                         int* __restrict__ image, double* __restrict__ diam, int rows_aligned)
 {
+    __shared__ __align__(16) double s_acc[3 * STATE_BLOCK];
+    __shared__ __align__(16) int s_img[3 * STATE_BLOCK];
     // one thread per tag: the inputs are read in order
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= N) return;
+    const uint32_t t0 = blockIdx.x * STATE_BLOCK;
+    const uint32_t t = t0 + threadIdx.x;
+    const bool live = t < N;
+    double a[3];
+    int g[3];
+    load_rows3(accel_in, image_in, t, live, rows_aligned && t0 + STATE_BLOCK <= N, s_acc, s_img, t0, a, g);
+    if (!live) return;
     const uint32_t i = rtag[t];
     // 16-byte loads: the inputs may be the caller's pinned buffers, read over the host link
-    const double2 p01 = reinterpret_cast<const double2*>(pos_in)[2 * t];
-    const double2 p23 = reinterpret_cast<const double2*>(pos_in)[2 * t + 1];
-    const double2 v01 = reinterpret_cast<const double2*>(vel_in)[2 * t];
-    const double2 v23 = reinterpret_cast<const double2*>(vel_in)[2 * t + 1];
+    const double2 p01 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)t];
+    const double2 p23 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)t + 1];
+    const double2 v01 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)t];
+    const double2 v23 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)t + 1];
     pos[i] = make_double4_32a(p01.x, p01.y, p23.x, type_as_double((uint32_t)p23.y));
     vel[i] = make_double4_32a(v01.x, v01.y, v23.x, v23.y);
     for (int d = 0; d < 3; ++d) {
-        accel[3 * i + d] = accel_in ? accel_in[3 * t + d] : 0.0;
-        image[3 * i + d] = image_in ? image_in[3 * t + d] : 0;
+        accel[3 * (size_t)i + d] = a[d];
+        image[3 * (size_t)i + d] = g[d];
     }
     if (diam) diam[i] = diam_in ? diam_in[t] : 1.0;
 }
@@ -473,33 +556,31 @@ __global__ void k_request_if_displaced(const uint4* __restrict__ fix, const uint
 }
 
 // device state -> tag order output (pos w = type as an integer-valued double)
-__global__ void k_store_state(const double4_32a* __restrict__ pos, const double4_32a* __restrict__ vel,
-                              const double* __restrict__ accel, const int* __restrict__ image,
-                              const uint32_t* __restrict__ rtag, uint32_t N, double* __restrict__ pos_out,
-                              double* __restrict__ vel_out, double* __restrict__ accel_out, int* __restrict__ image_out)
+__global__ void __launch_bounds__(STATE_BLOCK)
+    k_store_state(const double4_32a* __restrict__ pos, const double4_32a* __restrict__ vel,
+                  const double* __restrict__ accel, const int* __restrict__ image, const uint32_t* __restrict__ rtag,
+                  uint32_t N, double* __restrict__ pos_out, double* __restrict__ vel_out,
+                  double* __restrict__ accel_out, int* __restrict__ image_out, int rows_aligned)
 {
-    // one thread per tag: the outputs are written in order
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= N) return;
-    const uint32_t i = rtag[t];
-    const double4_32a p = pos[i];
-    if (pos_out) {
-        pos_out[4 * t] = p.x;
-        pos_out[4 * t + 1] = p.y;
-        pos_out[4 * t + 2] = p.z;
-        pos_out[4 * t + 3] = (double)type_of(p.w);
+    __shared__ __align__(16) double s_acc[3 * STATE_BLOCK];
+    __shared__ __align__(16) int s_img[3 * STATE_BLOCK];
+    // one thread per tag: the outputs are written in order, 16 bytes at a time
+    const uint32_t t0 = blockIdx.x * STATE_BLOCK;
+    const uint32_t t = t0 + threadIdx.x;
+    const bool live = t < N;
+    const uint32_t i = live ? rtag[t] : 0u;
+    if (live && pos_out) {
+        const double4_32a p = pos[i];
+        reinterpret_cast<double2*>(pos_out)[2 * (size_t)t] = make_double2(p.x, p.y);
+        reinterpret_cast<double2*>(pos_out)[2 * (size_t)t + 1] = make_double2(p.z, (double)type_of(p.w));
     }
-    if (vel_out) {
+    if (live && vel_out) {
         const double4_32a v = vel[i];
-        vel_out[4 * t] = v.x;
-        vel_out[4 * t + 1] = v.y;
-        vel_out[4 * t + 2] = v.z;
-        vel_out[4 * t + 3] = v.w;
+        reinterpret_cast<double2*>(vel_out)[2 * (size_t)t] = make_double2(v.x, v.y);
+        reinterpret_cast<double2*>(vel_out)[2 * (size_t)t + 1] = make_double2(v.z, v.w);
     }
-    for (int d = 0; d < 3; ++d) {
-        if (accel_out) accel_out[3 * t + d] = accel[3 * i + d];
-        if (image_out) image_out[3 * t + d] = image[3 * i + d];
-    }
+    store_rows3(accel, image, i, t, live, rows_aligned && t0 + STATE_BLOCK <= N, s_acc, s_img, accel_out,
+                image_out, t0);
 }
 
 }  // namespace azp
@@ -993,6 +1074,8 @@ void* mapped_view(const void* h)
 
 // the state kernels move positions and velocities as 16-byte pairs
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0u; }
+// rows of three per particle (accelerations, image counts) move as 16-byte vectors
+int rows_aligned(const void* accel, const void* image) { return aligned16(accel) && aligned16(image); }
 
 // staging buffers of the host transfers (first use only)
 int ensure_staging(azp_md* m)
@@ -1012,13 +1095,13 @@ void enqueue_store_state(azp_md* m, double* pos, double* vel, double* accel, int
 {
     const uint32_t N = m->N;
     if (m->precision == AZP_FP32)
-        k_store_state_fx<<<blocks_for(N, 256), 256, 0, s>>>(
+        k_store_state_fx<<<blocks_for(N, STATE_BLOCK), STATE_BLOCK, 0, s>>>(
             m->fix[m->cur], m->lo[m->cur], reinterpret_cast<const VelFF*>(m->vel), m->mass, m->accel, m->image, m->rtag,
             N, m->box.L[0] * 5.421010862427522e-20, m->box.L[1] * 5.421010862427522e-20,
-            m->box.L[2] * 5.421010862427522e-20, pos, vel, accel, image);
+            m->box.L[2] * 5.421010862427522e-20, pos, vel, accel, image, rows_aligned(accel, image));
     else
-        k_store_state<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[m->cur], m->vel, m->accel, m->image, m->rtag, N, pos,
-                                                          vel, accel, image);
+        k_store_state<<<blocks_for(N, STATE_BLOCK), STATE_BLOCK, 0, s>>>(
+            m->pos[m->cur], m->vel, m->accel, m->image, m->rtag, N, pos, vel, accel, image, rows_aligned(accel, image));
 }
 
 
@@ -1061,7 +1144,8 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         }
         return nullptr;
     };
-    if (!c || c->ntypes == 0 || c->ntypes > MAX_PAIR_TYPES) return fail(AZP_ERR_INVALID, nullptr);
+    // particle indices below 2^31: neighbour-list entries carry marks in bit 31
+    if (!c || c->ntypes == 0 || c->ntypes > MAX_PAIR_TYPES || c->N >= 0x80000000u) return fail(AZP_ERR_INVALID, nullptr);
     for (int d = 0; d < 3; ++d)
         if (!(c->box.L[d] > 0.0)) return fail(AZP_ERR_INVALID, nullptr);
     if (c->precision != AZP_FP64 && c->precision != AZP_FP32) return fail(AZP_ERR_INVALID, nullptr);
@@ -1391,8 +1475,8 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         // its position at the last build (a state read back from this engine and
         // set again moves nothing). A denser new state that overflows the list
         // takes the full path below.
-        k_load_state_ordered<<<blocks_for(N, 256), 256, 0, s>>>(dp, dv, da, di, dd, m->rtag, N, m->pos[0], m->vel,
-                                                                 m->accel, m->image, m->diam);
+        k_load_state_ordered<<<blocks_for(N, STATE_BLOCK), STATE_BLOCK, 0, s>>>(
+            dp, dv, da, di, dd, m->rtag, N, m->pos[0], m->vel, m->accel, m->image, m->diam, rows_aligned(da, di));
         AZP_CHECK_LAUNCH("k_load_state_ordered");
         if (m->precision == AZP_FP32) {
             k_state_to_fx<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[0], m->vel, m->fix[0], m->lo[0], m->mass, N,
@@ -1414,8 +1498,8 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         if (!placed) AZP_CUDA_TRY(cudaMemsetAsync(m->flags, 0, sizeof(uint32_t) * 8, s));
     }
     if (!placed) {
-        k_load_state<<<blocks_for(N, 256), 256, 0, s>>>(dp, dv, da, di, dd, N, m->pos[0], m->vel, m->accel, m->image,
-                                                         m->diam, m->tag, m->rtag);
+        k_load_state<<<blocks_for(N, STATE_BLOCK), STATE_BLOCK, 0, s>>>(
+            dp, dv, da, di, dd, N, m->pos[0], m->vel, m->accel, m->image, m->diam, m->tag, m->rtag, rows_aligned(da, di));
         AZP_CHECK_LAUNCH("k_load_state");
         if (m->precision == AZP_FP32) {
             k_state_to_fx<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[0], m->vel, m->fix[0], m->lo[0], m->mass, N,
@@ -1463,18 +1547,10 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
         return AZP_OK;
     }
     const cudaMemcpyKind back = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    // pinned outputs are written in place by the store kernel; pageable ones staged
-    void* vp = on_device || !aligned16(pos) ? nullptr : mapped_view(pos);
-    void* vv = on_device || !aligned16(vel) ? nullptr : mapped_view(vel);
-    void* va = on_device ? nullptr : mapped_view(accel);
-    void* vi = on_device ? nullptr : mapped_view(image);
-    if ((!pos || vp) && (!vel || vv) && (!accel || va) && (!image || vi)) {
-        enqueue_store_state(m, static_cast<double*>(vp), static_cast<double*>(vv), static_cast<double*>(va),
-                            static_cast<int*>(vi), s);
-        AZP_CHECK_LAUNCH("k_store_state");
-        AZP_CUDA_TRY(cudaStreamSynchronize(s));
-        return AZP_OK;
-    }
+    // Host outputs are staged on the device and copied by the copy engines: the
+    // store kernel writing pinned memory in place over the host link measured
+    // 103 GB/s at N = 1M against 165 GB/s for the staged copies (reads, in
+    // set_state, go the other way: in place is the faster there).
     int st0 = ensure_staging(m);
     if (st0) return st0;
     double* dp = pos ? m->st_pos : nullptr;

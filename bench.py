@@ -234,6 +234,21 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+CLOCK_ROLL_S = 0.6
+
+
+def _roll(eng, seconds):
+    """Untimed steps of the workload for about `seconds` (clock sampling under load)."""
+    import torch
+
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        eng.run_async(20)
+        torch.cuda.synchronize()
+        n += 20
+    return n
+
+
 def algorithmic_bytes(n_nbr_mean, n_bond_mean, precision="fp32"):
     """Bytes per particle of one fused step launch.
 
@@ -388,29 +403,32 @@ def run_ours(args):
     sim.run(args.warmup)
     log("warm-up done")
     eng = sim._engine
-    builds0 = sim.thermo()["nlist_builds"]
     stream = torch.cuda.current_stream()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
     with ClockSampler(dev) as clk:
+        # nvidia-smi polls every 200 ms, longer than a short timed region: the
+        # sampler also runs over CLOCK_ROLL_S of the same steps on each side of it
+        roll = roll_before = _roll(eng, CLOCK_ROLL_S)
+        builds0 = sim.thermo()["nlist_builds"]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
         torch.cuda.nvtx.range_push("timed")
         start.record(stream)
         eng.run_async(args.steps)
         end.record(stream)
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
-    if world > 1:
-        torch.distributed.barrier()
-    ms = start.elapsed_time(end)
-    launches = eng.last_launches
-    err = eng.error_word()
-    if err:
-        raise RuntimeError(f"timed region raised device error word 0x{err:x}: measurement invalid")
-    th = sim.thermo()
-    builds = th["nlist_builds"] - builds0
-    sim._timestep += args.steps
+        if world > 1:
+            torch.distributed.barrier()
+        ms = start.elapsed_time(end)
+        launches = eng.last_launches
+        err = eng.error_word()
+        if err:
+            raise RuntimeError(f"timed region raised device error word 0x{err:x}: measurement invalid")
+        builds = sim.thermo()["nlist_builds"] - builds0
+        roll += _roll(eng, CLOCK_ROLL_S)
+    sim._timestep += args.steps + roll
     sim.state._host_valid = False
     t_max, value = reduce_over_ranks(ms, args.steps, world, "cuda")
 
@@ -457,7 +475,9 @@ def run_ours(args):
                          "kernel_ms": kernel_ms, "bytes_per_launch": bytes_per_launch,
                          "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "mean_neighbours": n_nbr,
                          "mean_bonds": n_bond},
-            "clocks": clk.summary(),
+            "clocks": dict(clk.summary(), window=f"nvidia-smi every 200 ms over the timed region and {CLOCK_ROLL_S} s "
+                           "of the same steps on each side of it"),
+            "untimed_steps_before_timed_region": {"warmup": args.warmup, "clock_window": roll_before},
             "accuracy": accuracy,
             "e2e": e2e,
         }

@@ -211,7 +211,8 @@ AZP_API const char* azp_last_error(void);
  * i for j), pairs with r_cut == 0 never listed, exclusions removed. Membership is
  * decided in FP64 with the oracle's exact rounding (|dx|^2 < r_list^2), so the
  * sets are bit-exact. Layout: column-major neighbours[k * N + i], counts[i].
- * Replaces HOOMD's NeighborListGPUBinned behind hoomd.md.nlist.Cell(buffer=...). */
+ * Replaces HOOMD's NeighborListGPUBinned behind hoomd.md.nlist.Cell(buffer=...).
+ * N < 2^31 (AZP_ERR_INVALID otherwise; the same bound holds for azp_md_create). */
 typedef struct azp_nlist azp_nlist;
 AZP_API azp_nlist* azp_nlist_create(uint32_t N, uint32_t ntypes, uint32_t max_neighbors, int* status);
 AZP_API void azp_nlist_destroy(azp_nlist* nl);

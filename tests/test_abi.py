@@ -70,6 +70,10 @@ def test_invalid_arguments_are_rejected(lib):
     # ntypes == 0 is refused before any device work
     assert not lib.azp_nlist_create(10, 0, 8, ctypes.byref(st))
     assert st.value == -1
+    # particle indices must stay below 2^31 (list entries carry a mark in bit 31)
+    st.value = 0
+    assert not lib.azp_nlist_create(0x80000000, 1, 8, ctypes.byref(st))
+    assert st.value == -1
 
 
 # sizeof(param_type) of the reference's evaluators, printed by oracle/ref_sizes.cpp
