@@ -238,6 +238,26 @@ __global__ void k_md_step1_fx(uint4* __restrict__ fix, uint4* __restrict__ lo, c
     if (__any_sync(0xffffffffu, want) && (threadIdx.x & 31) == 0) atomicOr(&flags[0], 1u);
 }
 
+// FP32-force mode: the walls' force and energy of each particle at the step's
+// positions, for the step kernel to add: an FP32 screen on the high words, then
+// the FP64 evaluation on the full 64-bit position for the particles some wall
+// can reach (the others get zero)
+__global__ void k_walls_fx(MDArgs a)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    const uint4 hw = __ldg(a.fix + i);
+    double fw[4] = {0.0, 0.0, 0.0, 0.0};
+    if (walls_near_f(a.walls, a.wall_tab, hw.w, (float)(int32_t)hw.x * a.sfix[0], (float)(int32_t)hw.y * a.sfix[1],
+                     (float)(int32_t)hw.z * a.sfix[2], a.wall_tol)) {
+        const uint4 lw = __ldg(a.flo + i);
+        engine_walls(a.wall_kind, a.walls, a.wall_tab, fx_to_double(fx_join(hw.x, lw.x), a.l64[0]),
+                     fx_to_double(fx_join(hw.y, lw.y), a.l64[1]), fx_to_double(fx_join(hw.z, lw.z), a.l64[2]), hw.w,
+                     fw);
+    }
+    const_cast<float4*>(a.wall_f)[i] = make_float4((float)fw[0], (float)fw[1], (float)fw[2], (float)fw[3]);
+}
+
 // What a step reads of its neighbours while their owners update it in the same
 // step, copied right before the step: DPD the velocities (FP64: (v, mass);
 // FP32-force: the leading floats (v, 1/m)), ImageHarmonic bonds the image counts.
@@ -651,6 +671,7 @@ struct azp_md {
     int wall_kind = -1;
     WallField* d_walls = nullptr;
     double* d_wall_tab = nullptr;
+    float4* d_wall_f = nullptr;  // FP32-force mode: per-particle wall force and energy
     float wall_tol = 0.0f;
     // integration group by type (0xffffffff: every particle)
     uint32_t group_types = 0xffffffffu;
@@ -732,7 +753,7 @@ void free_all(azp_md* m)
                     m->partials, m->thermo, m->tmp4, m->tmpd, m->snap_pos, m->snap_vel, m->snap_acc,
                     m->snap_img, m->snap_diam, m->st_pos, m->st_vel, m->st_acc, m->st_img, m->st_diam,
                     m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab, m->d_dvel, m->d_img0,
-                    m->d_kT_hdr, m->d_kT_tab, m->d_noise_tab, m->tile_tab};
+                    m->d_kT_hdr, m->d_kT_tab, m->d_noise_tab, m->tile_tab, m->d_wall_f};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -826,6 +847,7 @@ MDArgs base_args(azp_md* m)
     a.wall_kind = m->wall_kind;
     a.walls = m->d_walls;
     a.wall_tab = m->d_wall_tab;
+    a.wall_f = m->d_wall_f;
     a.wall_tol = m->wall_tol;
     a.dvel = m->d_dvel;
     a.img0 = m->d_img0;
@@ -908,6 +930,11 @@ int enqueue_rebuild(azp_md* m, cudaStream_t s, const uint32_t* gate)
 // the step kernel, preceded for DPD and ImageHarmonic bonds by the snapshot it reads
 int md_launch(azp_md* m, int integ, const MDArgs& a, cudaStream_t s)
 {
+    if (m->d_wall_f) {
+        k_walls_fx<<<blocks_for(m->N, 256), 256, 0, s>>>(a);
+        AZP_CHECK_LAUNCH("k_walls_fx");
+        m->launches += 1;
+    }
     if (m->d_dvel || m->d_img0) {
         k_step_snapshot<<<blocks_for(m->N, 256), 256, 0, s>>>(m->vel, m->image, m->N, m->precision == AZP_FP32 ? 1 : 0,
                                                               m->d_dvel, m->d_img0);
@@ -1407,6 +1434,7 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         CTRY(cudaMemcpy(m->d_walls, &wf, sizeof(wf), cudaMemcpyHostToDevice));
         CTRY(cudaMemcpy(m->d_wall_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
         m->wall_kind = c->wall_kind;
+        if (m->precision == AZP_FP32) ALLOC(m->d_wall_f, N);
         // the FP32 screen's positions are good to a few L 2^-24 (hi word, float scale)
         const double Lmax = std::max(m->box.L[0], std::max(m->box.L[1], m->box.L[2]));
         m->wall_tol = (float)(4e-6 * Lmax + 1e-5);
@@ -1666,7 +1694,7 @@ int azp_md_run(azp_md* m, uint64_t steps, void* stream)
             AZP_CUDA_TRY(cudaGraphLaunch(m->gexec[m->cur], s));
             // arm + two step kernels (+ their snapshot kernels for DPD / ImageHarmonic);
             // the rebuild bodies run only when armed and are not counted
-            m->launches += 3 + ((m->d_dvel || m->d_img0) ? 2 : 0);
+            m->launches += 3 + ((m->d_dvel || m->d_img0) ? 2 : 0) + (m->d_wall_f ? 2 : 0);
             mid -= 2;
         }
     }

@@ -93,6 +93,10 @@ struct MDArgs {
     const WallField* walls;
     const double* wall_tab;
     float wall_tol;             // FP32 screening margin (FP32-force step)
+    // FP32-force step: each particle's wall force and energy, written by
+    // k_walls_fx right before the step (an out-of-line wall call inside the step
+    // would cost it a stack frame and spills even with the walls off)
+    const float4* wall_f;
     // DPD: the velocities of the step's start (a snapshot taken right before the
     // step, so that neighbours are read while their owners update them):
     // double4 (v, mass) in FP64 steps, float4 (v, 1/m) in FP32-force steps

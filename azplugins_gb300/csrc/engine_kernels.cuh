@@ -658,7 +658,9 @@ AZP_D double fx_disp(uint32_t hi_i, uint32_t lo_i, uint32_t hi_j, uint32_t lo_j,
     return (double)d * l64;
 }
 
-template<class PE>
+// ONE: a single-type system; the type pair is 0 at compile time, so the record
+// lookups resolve to the caller's registers
+template<class PE, bool ONE = false>
 AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j,
                         const float* s_rec, const double* s_rc2, AccFx& acc, bool vir)
 {
@@ -666,7 +668,7 @@ AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint3
     const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
     const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
     const float rsq = dx * dx + dy * dy + dz * dz;
-    const uint32_t tp = fi.w * a.ntypes + fj.w;
+    const uint32_t tp = ONE ? 0u : fi.w * a.ntypes + fj.w;
     const float* rec = s_rec + (size_t)tp * PAIR_TBL;
     const float* cut = rec + PAIR_REC;
     const float rc2 = cut[0];
@@ -700,7 +702,7 @@ AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint3
 // outside r_cut: the evaluator runs on every lane (at r_cut where the pair does
 // not count) and the pair's terms are masked, so a batch has no per-lane exits;
 // only the rare candidate in the band around r_cut takes the exact FP64 branch
-template<class PE, bool TILE = false>
+template<class PE, bool TILE = false, bool ONE = false>
 AZP_D void pair_term_fx_masked(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t ent, bool ok,
                                const float* s_rec, const double* s_rc2, AccFx& acc, bool vir,
                                const uint32_t* trec = nullptr)
@@ -714,7 +716,7 @@ AZP_D void pair_term_fx_masked(const MDArgs& a, const uint4& fi, const uint4& fj
     const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
     const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
     const float rsq = dx * dx + dy * dy + dz * dz;
-    const uint32_t tp = fi.w * a.ntypes + fj.w;
+    const uint32_t tp = ONE ? 0u : fi.w * a.ntypes + fj.w;
     const float* rec = s_rec + (size_t)tp * PAIR_TBL;
     const float* cut = rec + PAIR_REC;
     const float rc2 = cut[0];
@@ -750,6 +752,7 @@ AZP_D void pair_term_fx_masked(const MDArgs& a, const uint4& fi, const uint4& fj
 // FP64 from the full 64-bit positions within 0.2 % of r_cut^2 (the weight
 // (1 - r / r_cut)^(s/2) is steep there, and the cutoff decision is the oracle's);
 // velocities from the step's snapshot (float4: v, 1/m)
+template<bool ONE = false>
 AZP_D void pair_term_dpd_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j,
                             const float* s_rec, const double* s_rc2, AccFx& acc, bool vir, const float4& vi,
                             uint32_t tgi, uint32_t k0, uint32_t k1)
@@ -758,7 +761,7 @@ AZP_D void pair_term_dpd_fx(const MDArgs& a, const uint4& fi, const uint4& fj, u
     const float dy = (float)(int32_t)(fi.y - fj.y) * a.sfix[1];
     const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
     const float rs = dx * dx + dy * dy + dz * dz;
-    const uint32_t tp = fi.w * a.ntypes + fj.w;
+    const uint32_t tp = ONE ? 0u : fi.w * a.ntypes + fj.w;
     const float* rec = s_rec + (size_t)tp * PAIR_TBL;
     const float rc2 = rec[PAIR_REC];
     if (!(rc2 > 0.0f) || rs >= rc2 * 1.000004f) return;
@@ -791,7 +794,7 @@ AZP_D void pair_term_dpd_fx(const MDArgs& a, const uint4& fi, const uint4& fj, u
     acc.add_split(dx, dy, dz, fdr, fc, e, vir);
 }
 
-template<class BE>
+template<class BE, bool ONE = false>
 AZP_D void bond_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t btype, const float* s_bond,
                         AccFx& acc, bool vir)
 {
@@ -800,7 +803,7 @@ AZP_D void bond_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint3
     const float dz = (float)(int32_t)(fi.z - fj.z) * a.sfix[2];
     const float rsq = dx * dx + dy * dy + dz * dz;
     float fdr, en;
-    if (!BE::eval_f(s_bond + btype * BOND_F, rsq, fdr, en)) {
+    if (!BE::eval_f(s_bond + (ONE ? 0u : btype) * BOND_F, rsq, fdr, en)) {
         atomicOr(&a.flags[1], AZP_EBIT_BOND);
         return;
     }
@@ -825,7 +828,7 @@ AZP_D float unwrapped_fx(uint32_t hi_i, uint32_t lo_i, uint32_t hi_j, uint32_t l
 
 // one ImageHarmonic bond of particle i (fixed words fi / li, images g[3] of the
 // step's start) with partner j in the FP32-force step
-template<class BE>
+template<class BE, bool ONE = false>
 AZP_D void bond_term_fx_image(const MDArgs& a, const uint4& fi, const uint4& li, const int* g, uint32_t j,
                               uint32_t btype, const float* s_bond, AccFx& acc, bool vir)
 {
@@ -837,7 +840,7 @@ AZP_D void bond_term_fx_image(const MDArgs& a, const uint4& fi, const uint4& li,
     const float dz = unwrapped_fx(fi.z, li.z, fj.z, lj.z, g[2] - __ldg(gj + 2), a.sfix[2]);
     const float rsq = dx * dx + dy * dy + dz * dz;
     float fdr, en;
-    if (!BE::eval_f(s_bond + btype * BOND_F, rsq, fdr, en)) {
+    if (!BE::eval_f(s_bond + (ONE ? 0u : btype) * BOND_F, rsq, fdr, en)) {
         atomicOr(&a.flags[1], AZP_EBIT_BOND);
         return;
     }
@@ -942,12 +945,24 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
     float* s_noise = s_gamma + a.ntypes;
     const uint4* s_tile = reinterpret_cast<const uint4*>(smem_raw);
     const uint32_t* trec = nullptr;
+    // single-type systems: the records copied from the kernel arguments into
+    // registers (every lookup below has a compile-time index; no address of the
+    // kernel argument is taken, so it is not copied to local memory)
+    float one_rec[ONE ? PAIR_TBL : 1], one_bond[ONE ? BOND_F : 1], one_gamma = 0.0f, one_noise = 0.0f;
+    double one_rc2 = 0.0;
     if constexpr (ONE) {
-        s_rc2 = &a.rc2_0;
-        s_rec = a.rec0;
-        s_bond = a.bond0;
-        s_gamma = &a.gamma0;
-        s_noise = &a.noise0;
+#pragma unroll
+        for (int k = 0; k < PAIR_TBL; ++k) one_rec[k] = a.rec0[k];
+#pragma unroll
+        for (int k = 0; k < BOND_F; ++k) one_bond[k] = a.bond0[k];
+        one_rc2 = a.rc2_0;
+        one_gamma = a.gamma0;
+        one_noise = a.noise0;
+        s_rc2 = &one_rc2;
+        s_rec = one_rec;
+        s_bond = one_bond;
+        s_gamma = &one_gamma;
+        s_noise = &one_noise;
         if constexpr (TILE) {
             // stage the block's neighbour ranges: coalesced 16-byte copies
             trec = a.tile + (size_t)blockIdx.x * TILE_REC;
@@ -982,22 +997,6 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
     const uint32_t sub = gid & (tpp - 1u);
     const bool active = i < a.N;
     constexpr bool vir = OUT;
-    // walls first, while nothing else is live: an FP32 screen on the high words,
-    // then the FP64 evaluation on the full 64-bit position for the particles some
-    // wall can reach; the result waits in this thread's shared-memory slot
-    __shared__ float4 s_wall[FX_BLOCK];
-    if (a.wall_kind >= 0 && active && sub == 0) {
-        const uint4 hw = __ldg(a.fix + i);
-        double fw[4] = {0.0, 0.0, 0.0, 0.0};
-        if (walls_near_f(a.walls, a.wall_tab, hw.w, (float)(int32_t)hw.x * a.sfix[0],
-                         (float)(int32_t)hw.y * a.sfix[1], (float)(int32_t)hw.z * a.sfix[2], a.wall_tol)) {
-            const uint4 lw = __ldg(a.flo + i);
-            engine_walls(a.wall_kind, a.walls, a.wall_tab, fx_to_double(fx_join(hw.x, lw.x), a.l64[0]),
-                         fx_to_double(fx_join(hw.y, lw.y), a.l64[1]), fx_to_double(fx_join(hw.z, lw.z), a.l64[2]),
-                         hw.w, fw);
-        }
-        s_wall[threadIdx.x] = make_float4((float)fw[0], (float)fw[1], (float)fw[2], (float)fw[3]);
-    }
     AccFx acc;
     uint4 fi = make_uint4(0u, 0u, 0u, 0u);
     uint32_t n = 0u;
@@ -1055,13 +1054,13 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
                 for (int u = 0; u < FX_BATCH; ++u) {
                     if constexpr (std::is_same<PE, DpdEngine>::value) {
                         if (kb + u * tpp < n)
-                            pair_term_dpd_fx(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir, vi, tgi, k0, k1);
+                            pair_term_dpd_fx<ONE>(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir, vi, tgi, k0, k1);
                     } else {
 #if AZP_FX_UNIFORM
-                        pair_term_fx_masked<PE, TILE>(a, fi, fj[u], i, jj[u], kb + u * tpp < n, s_rec, s_rc2, acc,
-                                                      vir, trec);
+                        pair_term_fx_masked<PE, TILE, ONE>(a, fi, fj[u], i, jj[u], kb + u * tpp < n, s_rec, s_rc2,
+                                                           acc, vir, trec);
 #else
-                        if (kb + u * tpp < n) pair_term_fx<PE>(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir);
+                        if (kb + u * tpp < n) pair_term_fx<PE, ONE>(a, fi, fj[u], i, jj[u], s_rec, s_rc2, acc, vir);
 #endif
                     }
                 }
@@ -1076,7 +1075,7 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
                               __ldg(a.img0 + 3 * (size_t)i + 2)};
             for (uint32_t k = sub; k < nb; k += tpp) {
                 const uint2 e = __ldg(a.bt + (size_t)k * a.N + i);
-                bond_term_fx_image<BE>(a, fi, li, g, e.x, e.y, s_bond, acc, vir);
+                bond_term_fx_image<BE, ONE>(a, fi, li, g, e.x, e.y, s_bond, acc, vir);
                 acc.commit(vir);
             }
         } else if constexpr (!std::is_same<BE, NoBond>::value) {
@@ -1087,8 +1086,8 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
                 const uint2 e1 = k1 < nb ? __ldg(a.bt + (size_t)k1 * a.N + i) : make_uint2(i, 0u);
                 const uint4 f0 = __ldg(a.fix + e0.x);
                 const uint4 f1 = __ldg(a.fix + e1.x);
-                bond_term_fx<BE>(a, fi, f0, e0.y, s_bond, acc, vir);
-                if (k1 < nb) bond_term_fx<BE>(a, fi, f1, e1.y, s_bond, acc, vir);
+                bond_term_fx<BE, ONE>(a, fi, f0, e0.y, s_bond, acc, vir);
+                if (k1 < nb) bond_term_fx<BE, ONE>(a, fi, f1, e1.y, s_bond, acc, vir);
                 acc.commit(vir);
             }
         }
@@ -1101,8 +1100,8 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
         if (a.bar_geom >= 0)
             // the barrier's force joins the net force (src/HarmonicBarrier.h:149-180)
             barrier_fx(a, fi, *a.d_timestep + (INTEG == MD_INTEG_LANGEVIN ? 1ull : 0ull), fb, ub);
-        // the walls' force, evaluated before the neighbour loop
-        const float4 fw = a.wall_kind >= 0 ? s_wall[threadIdx.x] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        // the walls' force and energy (k_walls_fx, launched right before the step)
+        const float4 fw = a.wall_kind >= 0 ? a.wall_f[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if constexpr (OUT) {
             a.out_force[i] = make_double4_32a(acc.Fx() + fb[0] + fw.x, acc.Fy() + fb[1] + fw.y,
                                               acc.Fz() + fb[2] + fw.z, acc.U() + ub + fw.w);
@@ -1128,9 +1127,10 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
             const float fx = acc.fx.s + (acc.fx.c + (fb[0] + fw.x));
             const float fy = acc.fy.s + (acc.fy.c + (fb[1] + fw.y));
             const float fz = acc.fz.s + (acc.fz.c + (fb[2] + fw.z));
-            const float gam = a.use_lambda ? a.lambdaf * (float)a.diameter[i] : s_gamma[ti];
+            const uint32_t tix = ONE ? 0u : ti;
+            const float gam = a.use_lambda ? a.lambdaf * (float)a.diameter[i] : s_gamma[tix];
             // the method's temperature at this timestep (a table when it varies)
-            float kTv = a.kTf, nz = a.use_lambda ? 0.0f : s_noise[ti];
+            float kTv = a.kTf, nz = a.use_lambda ? 0.0f : s_noise[tix];
             if (a.kT_hdr) {
                 const size_t r = kT_row(a, ts);
                 kTv = (float)a.kT_tab[r];
