@@ -558,6 +558,63 @@ __global__ void __launch_bounds__(STATE_BLOCK)
     if (diam) diam[i] = diam_in ? diam_in[t] : 1.0;
 }
 
+// FP32-force mode, the three passes of an order-keeping load in one: tag-order
+// input -> fixed words, float-float velocities and masses of particle i = rtag[t]
+// (k_load_state_ordered + k_state_to_fx), and the rebuild request when i lies
+// more than r_buff / 2 from its position at the last build (k_request_if_displaced)
+__global__ void __launch_bounds__(STATE_BLOCK)
+    k_load_state_ordered_fx(const double* __restrict__ pos_in, const double* __restrict__ vel_in,
+                            const double* __restrict__ accel_in, const int* __restrict__ image_in,
+                            const double* __restrict__ diam_in, const uint32_t* __restrict__ rtag, uint32_t N,
+                            double Li0, double Li1, double Li2, uint4* __restrict__ fix, uint4* __restrict__ lo,
+                            VelFF* __restrict__ velf, double* __restrict__ mass, double* __restrict__ accel,
+                            int* __restrict__ image, double* __restrict__ diam, const uint4* __restrict__ fix_build,
+                            float s0, float s1, float s2, float thresh2, uint32_t* __restrict__ flags, int rows_aligned)
+{
+    __shared__ __align__(16) double s_acc[3 * STATE_BLOCK];
+    __shared__ __align__(16) int s_img[3 * STATE_BLOCK];
+    const uint32_t t0 = blockIdx.x * STATE_BLOCK;
+    const uint32_t t = t0 + threadIdx.x;
+    const bool live = t < N;
+    double a3[3];
+    int g3[3];
+    load_rows3(accel_in, image_in, t, live, rows_aligned && t0 + STATE_BLOCK <= N, s_acc, s_img, t0, a3, g3);
+    bool want = false;
+    if (live) {
+        const uint32_t i = rtag[t];
+        // 16-byte loads: the inputs may be the caller's pinned buffers, read over the host link
+        const double2 p01 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)t];
+        const double2 p23 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)t + 1];
+        const double2 v01 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)t];
+        const double2 v23 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)t + 1];
+        uint4 h, l;
+        fx_split(fx_from_double(p01.x, Li0), h.x, l.x);
+        fx_split(fx_from_double(p01.y, Li1), h.y, l.y);
+        fx_split(fx_from_double(p23.x, Li2), h.z, l.z);
+        h.w = type_of(type_as_double((uint32_t)p23.y));
+        l.w = 0u;
+        fix[i] = h;
+        lo[i] = l;
+        VelFF f;
+        f.h = make_float4((float)v01.x, (float)v01.y, (float)v23.x, (float)(1.0 / v23.y));
+        f.l = make_float4((float)(v01.x - (double)f.h.x), (float)(v01.y - (double)f.h.y),
+                          (float)(v23.x - (double)f.h.z), 0.0f);
+        velf[i] = f;
+        mass[i] = v23.y;
+        for (int d = 0; d < 3; ++d) {
+            accel[3 * (size_t)i + d] = a3[d];
+            image[3 * (size_t)i + d] = g3[d];
+        }
+        if (diam) diam[i] = diam_in ? diam_in[t] : 1.0;
+        const uint4 fb = fix_build[i];
+        const float dx = (float)(int32_t)(h.x - fb.x) * s0;
+        const float dy = (float)(int32_t)(h.y - fb.y) * s1;
+        const float dz = (float)(int32_t)(h.z - fb.z) * s2;
+        want = dx * dx + dy * dy + dz * dz > thresh2;
+    }
+    if (__any_sync(0xffffffffu, want) && (threadIdx.x & 31) == 0) atomicOr(&flags[0], 1u);
+}
+
 // rebuild request when a particle of the loaded state lies more than r_buff / 2
 // from its position at the last list build (the step kernels' criterion)
 __global__ void k_request_if_displaced(const uint4* __restrict__ fix, const uint4* __restrict__ fix_build, uint32_t N,
@@ -718,6 +775,7 @@ struct azp_md {
     // graphs
     bool use_graphs = true;
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // pair of mid steps starting at cur = 0 / 1
+    cudaGraphExec_t gexec_rb[2] = {nullptr, nullptr};  // conditional rebuild alone, at cur = 0 / 1
     uint32_t graph_steps = 0;
     cudaStream_t graph_stream = nullptr;
 };
@@ -735,6 +793,11 @@ template<typename T> int dalloc(T** p, size_t n)
 void free_graphs(azp_md* m)
 {
     for (auto& g : m->gexec)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    for (auto& g : m->gexec_rb)
         if (g) {
             cudaGraphExecDestroy(g);
             g = nullptr;
@@ -1065,6 +1128,69 @@ int build_pair_graph(azp_md* m, int cur0, int integ, cudaGraphExec_t* out)
     }
     cudaGraphDestroy(g);
     return st;
+}
+
+// The rebuild alone as a graph: the arm node and the conditional rebuild body,
+// with the buffers of parity cur0
+int build_rebuild_graph(azp_md* m, int cur0, cudaGraphExec_t* out)
+{
+    cudaGraph_t g = nullptr;
+    AZP_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    int st = AZP_OK;
+    const int saved_cur = m->cur;
+    m->cur = cur0;
+    cudaStream_t s = m->graph_stream;
+    cudaGraphNode_t arm = nullptr;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        k_arm<<<1, 1, 0, s>>>(m->flags, h);
+        cudaGraph_t gg = nullptr;
+        e = cudaStreamEndCapture(s, &gg);
+    }
+    if (e == cudaSuccess) {
+        size_t n = 1;
+        e = cudaGraphGetNodes(g, &arm, &n);
+    }
+    if (e == cudaSuccess) {
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cnode;
+        e = cudaGraphAddNode(&cnode, g, &arm, nullptr, 1, &cp);
+        if (e == cudaSuccess)
+            e = cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            st = enqueue_rebuild(m, s, nullptr);
+            cudaGraph_t bb = nullptr;
+            e = cudaStreamEndCapture(s, &bb);
+        }
+    }
+    if (e == cudaSuccess && st == AZP_OK) e = cudaGraphInstantiate(out, g, 0);
+    if (e != cudaSuccess && st == AZP_OK) st = record_cuda_error(e, "rebuild graph");
+    m->cur = saved_cur;
+    cudaGraphDestroy(g);
+    return st;
+}
+
+// The list rebuild if a step or a loaded state requested it: with graphs, one
+// replay of the rebuild graph (its arm kernel decides; a rebuild that is not
+// needed costs that one kernel); without, the rebuild kernels gated by the flag.
+int rebuild_if_requested(azp_md* m, cudaStream_t s)
+{
+    if (!m->use_graphs) return enqueue_rebuild(m, s, m->flags);
+    cudaGraphExec_t& ge = m->gexec_rb[m->cur];
+    if (!ge) {
+        const int st = build_rebuild_graph(m, m->cur, &ge);
+        if (st) return st;
+    }
+    AZP_CUDA_TRY(cudaGraphLaunch(ge, s));
+    m->launches += 1;
+    return AZP_OK;
 }
 
 int check_errors(azp_md* m, cudaStream_t s)
@@ -1503,21 +1629,23 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         // its position at the last build (a state read back from this engine and
         // set again moves nothing). A denser new state that overflows the list
         // takes the full path below.
-        k_load_state_ordered<<<blocks_for(N, STATE_BLOCK), STATE_BLOCK, 0, s>>>(
-            dp, dv, da, di, dd, m->rtag, N, m->pos[0], m->vel, m->accel, m->image, m->diam, rows_aligned(da, di));
-        AZP_CHECK_LAUNCH("k_load_state_ordered");
-        if (m->precision == AZP_FP32) {
-            k_state_to_fx<<<blocks_for(N, 256), 256, 0, s>>>(m->pos[0], m->vel, m->fix[0], m->lo[0], m->mass, N,
-                                                              1.0 / m->box.L[0], 1.0 / m->box.L[1], 1.0 / m->box.L[2]);
-            AZP_CHECK_LAUNCH("k_state_to_fx");
-        } else {
-            launch_to_fixed(m->pos[0], m->fix[0], N, m->box, s);
-        }
         const MDArgs a = base_args(m);
-        k_request_if_displaced<<<blocks_for(N, 256), 256, 0, s>>>(m->fix[0], m->fix_build, N, a.sfix[0], a.sfix[1],
-                                                                   a.sfix[2], a.disp_thresh2, m->flags);
-        AZP_CHECK_LAUNCH("k_request_if_displaced");
-        st = enqueue_rebuild(m, s, m->flags);
+        if (m->precision == AZP_FP32) {
+            k_load_state_ordered_fx<<<blocks_for(N, STATE_BLOCK), STATE_BLOCK, 0, s>>>(
+                dp, dv, da, di, dd, m->rtag, N, 1.0 / m->box.L[0], 1.0 / m->box.L[1], 1.0 / m->box.L[2], m->fix[0],
+                m->lo[0], reinterpret_cast<VelFF*>(m->vel), m->mass, m->accel, m->image, m->diam, m->fix_build,
+                a.sfix[0], a.sfix[1], a.sfix[2], a.disp_thresh2, m->flags, rows_aligned(da, di));
+            AZP_CHECK_LAUNCH("k_load_state_ordered_fx");
+        } else {
+            k_load_state_ordered<<<blocks_for(N, STATE_BLOCK), STATE_BLOCK, 0, s>>>(
+                dp, dv, da, di, dd, m->rtag, N, m->pos[0], m->vel, m->accel, m->image, m->diam, rows_aligned(da, di));
+            AZP_CHECK_LAUNCH("k_load_state_ordered");
+            launch_to_fixed(m->pos[0], m->fix[0], N, m->box, s);
+            k_request_if_displaced<<<blocks_for(N, 256), 256, 0, s>>>(m->fix[0], m->fix_build, N, a.sfix[0],
+                                                                       a.sfix[1], a.sfix[2], a.disp_thresh2, m->flags);
+            AZP_CHECK_LAUNCH("k_request_if_displaced");
+        }
+        st = rebuild_if_requested(m, s);
         if (st) return st;
         uint32_t f3 = 0;
         AZP_CUDA_TRY(cudaMemcpyAsync(&f3, m->flags + 3, sizeof(f3), cudaMemcpyDeviceToHost, s));
@@ -1699,7 +1827,7 @@ int azp_md_run(azp_md* m, uint64_t steps, void* stream)
         }
     }
     while (mid > 0) {
-        st = enqueue_rebuild(m, s, m->flags);
+        st = rebuild_if_requested(m, s);
         if (st) return st;
         st = enqueue_step(m, integ, 1, 0, s, 0, 0);
         if (st) return st;
@@ -1707,7 +1835,7 @@ int azp_md_run(azp_md* m, uint64_t steps, void* stream)
         --mid;
     }
     if (integ == MD_INTEG_LANGEVIN) {
-        st = enqueue_rebuild(m, s, m->flags);
+        st = rebuild_if_requested(m, s);
         if (st) return st;
         st = enqueue_step(m, integ, 0, 1, s, 0, 0);
         if (st) return st;
@@ -1725,7 +1853,7 @@ int azp_md_forces(azp_md* m, double* force, double* virial, int on_device, void*
     cudaStream_t s = as_stream(stream);
     const uint32_t N = m->N;
     if (N == 0) return AZP_OK;
-    int st = enqueue_rebuild(m, s, m->flags);
+    int st = rebuild_if_requested(m, s);
     if (st) return st;
     MDArgs a = base_args(m);
     a.out = 1;
@@ -1752,7 +1880,7 @@ int azp_md_thermo(azp_md* m, double* out, void* stream)
     if (!m->forces_valid) {
         if (m->bar_geom >= 0 && !m->bar_set)
             return record_error(AZP_ERR_INVALID, "azp_md_thermo: the barrier locations are not set");
-        int st = enqueue_rebuild(m, s, m->flags);
+        int st = rebuild_if_requested(m, s);
         if (st) return st;
         MDArgs a = base_args(m);
         a.out = 1;

@@ -871,10 +871,26 @@ AZP_D void finish_step(const MDArgs& a, bool want_rebuild)
 #define AZP_FX_BATCH 4
 #endif
 constexpr int FX_BATCH = AZP_FX_BATCH;
-// resident blocks per SM the FP32-force step is compiled for (register cap)
-#ifndef AZP_FX_MIN_BLOCKS
-#define AZP_FX_MIN_BLOCKS 4
+// Resident blocks per SM the FP32-force step is compiled for (the register cap):
+// 5 (48 registers) for the plain single-type step of the light evaluators, whose
+// few spilled bytes cost less than the extra resident warps gain (measured on the
+// melt at N = 1M: 0.0946 -> 0.0897 ms); 4 (64 registers) for the rest, which
+// would spill hundreds of bytes at 48 (Colloid, DPD, energy-writing launches).
+// AZP_FX_MIN_BLOCKS overrides both.
+template<class PE> struct fx_light : std::false_type {};
+template<> struct fx_light<PerturbedLJ> : std::true_type {};
+template<> struct fx_light<ExpandedYukawa> : std::true_type {};
+template<> struct fx_light<Hertz> : std::true_type {};
+template<> struct fx_light<NoPair> : std::true_type {};
+template<class PE, bool OUT, bool ONE>
+constexpr int fx_min_blocks()
+{
+#ifdef AZP_FX_MIN_BLOCKS
+    return AZP_FX_MIN_BLOCKS;
+#else
+    return (ONE && !OUT && fx_light<PE>::value && FX_BLOCK == 256) ? 5 : 4;
 #endif
+}
 
 // prefetch of the DRAM rows a warp's particles read (0 off, 1 into L1, 2 into L2)
 #ifndef AZP_FX_PREFETCH
@@ -885,6 +901,29 @@ constexpr int FX_BATCH = AZP_FX_BATCH;
 #ifndef AZP_FX_UNIFORM
 #define AZP_FX_UNIFORM 1
 #endif
+
+// the per-particle rows of step two / step one (velocity record, low position
+// words, build shadow, tag) copied into shared memory by cp.async at the start of
+// the step, so that their DRAM latency passes while the neighbour loop runs (1),
+// or loaded where they are used (0)
+#ifndef AZP_FX_STAGE
+#define AZP_FX_STAGE 1
+#endif
+
+// per-thread asynchronous global -> shared copies (completed by cp_async_wait_all
+// in the issuing thread, which alone reads what it copied)
+AZP_D void cp_async16(void* smem, const void* g)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(g)
+                 : "memory");
+}
+AZP_D void cp_async4(void* smem, const void* g)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(g)
+                 : "memory");
+}
+AZP_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+AZP_D void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 AZP_D void prefetch_line(const void* p)
 {
@@ -903,7 +942,7 @@ AZP_D void prefetch_line(const void* p)
 // first nmax columns of their list rows, so that those latencies overlap at
 // the start instead of chaining behind the neighbour loop. Addresses stay
 // inside the arrays: every one is clamped to the warp's last particle.
-AZP_D void prefetch_warp_rows(const MDArgs& a, uint32_t i0, uint32_t i_last, uint32_t nmax, bool bonds)
+AZP_D void prefetch_warp_rows(const MDArgs& a, uint32_t i0, uint32_t i_last, uint32_t nmax, bool bonds, bool rows)
 {
     const uint32_t lane = threadIdx.x & 31u;
     if (lane < nmax) {
@@ -911,7 +950,9 @@ AZP_D void prefetch_warp_rows(const MDArgs& a, uint32_t i0, uint32_t i_last, uin
         prefetch_line(a.nbrs + (size_t)lane * a.N + i_last);
     }
     const void* p = nullptr;
-    if (lane < 8u) {
+    if (!rows && lane < 18u) {
+        // the integration rows are staged in shared memory instead
+    } else if (lane < 8u) {
         p = a.velf + min(i0 + lane * 4u, i_last);
     } else if (lane < 12u) {
         p = a.flo + min(i0 + (lane - 8u) * 8u, i_last);
@@ -934,7 +975,7 @@ AZP_D void prefetch_warp_rows(const MDArgs& a, uint32_t i0, uint32_t i_last, uin
 // block's neighbour ranges are staged in shared memory first and the list
 // entries address them there (celllist.cuh, TILE_GLOBAL entries are gathered)
 template<class PE, class BE, int INTEG, bool OUT, bool ONE, bool TILE = false>
-__global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDArgs a)
+__global__ void __launch_bounds__(FX_BLOCK, (fx_min_blocks<PE, OUT, ONE>())) k_md_step_fx(MDArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t nt2 = a.ntypes * a.ntypes;
@@ -997,6 +1038,28 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
     const uint32_t sub = gid & (tpp - 1u);
     const bool active = i < a.N;
     constexpr bool vir = OUT;
+#if AZP_FX_STAGE
+    constexpr bool STAGE = INTEG != MD_FORCES_ONLY;
+    constexpr bool STAGE_V = INTEG == MD_INTEG_LANGEVIN;
+#else
+    constexpr bool STAGE = false, STAGE_V = false;
+#endif
+    __shared__ __align__(32) VelFF st_vel[STAGE_V ? FX_BLOCK : 1];
+    __shared__ __align__(16) uint4 st_lo[STAGE ? FX_BLOCK : 1];
+    __shared__ __align__(16) uint4 st_fb[STAGE ? FX_BLOCK : 1];
+    __shared__ uint32_t st_tag[STAGE ? FX_BLOCK : 1];
+    if constexpr (STAGE) {
+        if (active && sub == 0) {
+            if constexpr (STAGE_V) {
+                cp_async16(&st_vel[threadIdx.x].h, &a.velf[i].h);
+                cp_async16(&st_vel[threadIdx.x].l, &a.velf[i].l);
+            }
+            cp_async16(&st_lo[threadIdx.x], a.flo + i);
+            cp_async16(&st_fb[threadIdx.x], a.fix_build + i);
+            cp_async4(&st_tag[threadIdx.x], a.tag + i);
+            cp_async_commit();
+        }
+    }
     AccFx acc;
     uint4 fi = make_uint4(0u, 0u, 0u, 0u);
     uint32_t n = 0u;
@@ -1011,7 +1074,7 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
         if (i0 < a.N) {
             const uint32_t i_last = min(i0 + (32u >> a.tpp_shift) - 1u, a.N - 1u);
             prefetch_warp_rows(a, i0, i_last, std::is_same<PE, NoPair>::value ? 0u : nmax,
-                               !std::is_same<BE, NoBond>::value);
+                               !std::is_same<BE, NoBond>::value, !AZP_FX_STAGE || INTEG == MD_FORCES_ONLY);
         }
     }
 #endif
@@ -1121,9 +1184,10 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
             for (int c = 0; c < 6; ++c) a.out_virial[(size_t)c * a.N + i] = wv[c];
         }
         if constexpr (INTEG != MD_FORCES_ONLY) {
+            if constexpr (STAGE) cp_async_wait_all();
             const unsigned long long ts = *a.d_timestep;
             const uint32_t ti = fi.w;
-            const uint32_t tg = __ldg(a.tag + i);
+            const uint32_t tg = STAGE ? st_tag[threadIdx.x] : __ldg(a.tag + i);
             const float fx = acc.fx.s + (acc.fx.c + (fb[0] + fw.x));
             const float fy = acc.fy.s + (acc.fy.c + (fb[1] + fw.y));
             const float fz = acc.fz.s + (acc.fz.c + (fb[2] + fw.z));
@@ -1145,7 +1209,7 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
             bool moved = false;
             if constexpr (INTEG == MD_INTEG_LANGEVIN) {
                 uniform3f(AZP_RNG_LANGEVIN_FLOW, ts, a.seed, tg, -c, 2.0f * c, r0, r1, r2);
-                VelFF v = a.velf[i];
+                VelFF v = STAGE_V ? st_vel[threadIdx.x] : a.velf[i];
                 const float minv = mover ? v.h.w : 0.0f;  // a particle outside the group keeps its velocity
                 const float ax = (fx + (r0 - gam * (v.h.x - ux))) * minv;
                 const float ay = (fy + (r1 - gam * (v.h.y - uy))) * minv;
@@ -1188,7 +1252,7 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
                 moved = true;
             }
             if (moved) {
-                uint4 lo = a.flo[i];
+                uint4 lo = STAGE ? st_lo[threadIdx.x] : a.flo[i];
                 bool bad = false;
                 const int wx = fx_advance(fi.x, lo.x, ddx, a.s64h[0], a.s64l[0], bad);
                 const int wy = fx_advance(fi.y, lo.y, ddy, a.s64h[1], a.s64l[1], bad);
@@ -1200,7 +1264,7 @@ __global__ void __launch_bounds__(FX_BLOCK, AZP_FX_MIN_BLOCKS) k_md_step_fx(MDAr
                 }
                 a.fix_next[i] = fi;
                 a.flo_next[i] = lo;
-                want_rebuild = displaced(fi, a.fix_build[i], a.sfix, a.disp_thresh2);
+                want_rebuild = displaced(fi, STAGE ? st_fb[threadIdx.x] : a.fix_build[i], a.sfix, a.disp_thresh2);
                 if (bad) atomicOr(&a.flags[1], AZP_EBIT_NONFINITE);
             }
         }

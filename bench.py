@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
-    ap.add_argument("--suite", default="melt", choices=["melt", "batched", "adjoint", "precision", "lj", "drivers"],
+    ap.add_argument("--suite", default="melt", choices=["melt", "batched", "adjoint", "precision", "lj", "drivers", "nlist"],
                     help="melt: the headline line; the others measure the remaining workloads")
     return ap.parse_args()
 

@@ -21,6 +21,11 @@ Each suite prints one JSON line:
   BrownianFlow, ConstantFlow U = 0.1 x, dt = 0.001, drag gamma = 10 diameter) --
   FP32-compensated against FP64 forces, energy and virial every 500 steps along the
   FP32-force Brownian trajectory.
+* ``nlist``: the neighbour-list drop-in driver (``azp_nlist_build``: cell binning,
+  scan, scatter, per-cell sort and the list kernel) on the relaxed headline melt
+  (N = 1,048,600, WCA r_cut 2^(1/6), buffer 0.4, bonded pairs excluded), positions
+  resident; in the melt's chain order and in cell order (the order the resident
+  engine keeps its particles in).
 * ``drivers``: the drop-in drivers of the rows beside the headline path
   (DPDGeneralWeight, HarmonicBarrier, LJ93 walls, velocity fields, ImageHarmonic)
   on about 10^6 particles: time per call, algorithmic bytes, fraction of the
@@ -620,9 +625,55 @@ def suite_drivers(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- list build
+def suite_nlist(args):
+    import torch
+
+    import bench
+    from azplugins_gb300 import _compute
+
+    snap, _ = bench.relaxed_melt(args.chains, seed=1)
+    N = snap.particles.N
+    L = np.array(snap.configuration.box[:3])
+    r_list = bench.RCUT + bench.R_BUFF
+    # cell order: particles sorted by the index of a cell of width >= r_list
+    dims = np.floor(L / r_list).astype(np.int64)
+    cell = np.floor((snap.particles.position + L / 2) / L * dims).astype(np.int64) % dims
+    order = np.argsort((cell[:, 2] * dims[1] + cell[:, 1]) * dims[0] + cell[:, 0], kind="stable")
+    rank = np.empty(N, dtype=np.int64)
+    rank[order] = np.arange(N)
+    out = {"suite": "nlist", "workload": "bead-spring melt N=1048600 after relaxation, WCA r_cut 2^(1/6), "
+           "buffer 0.4, bonded pairs excluded", "N": N}
+    for name, perm in (("chain_order", None), ("cell_order", order)):
+        pos = snap.particles.position if perm is None else snap.particles.position[perm]
+        group = snap.bonds.group if perm is None else rank[snap.bonds.group]
+        ex = _compute.exclusions_csr(N, group)
+        sub = type(snap)(N)
+        sub.configuration.box = list(snap.configuration.box)
+        sub.particles.position = pos
+        sub.particles.typeid = np.zeros(N, dtype=np.int32)
+        posd = _compute.device_positions(sub)
+        sysd = _compute.make_system(sub, posd)
+        nl = _compute.NeighborList(N, 1, np.array([[bench.RCUT]]), bench.R_BUFF, ex)
+        nl.build(sysd)  # sizes the list
+        for _ in range(3):
+            nl.build(sysd)
+        ms = _cuda_ms(lambda: nl.build(sysd), reps=20)
+        torch.cuda.nvtx.range_push(f"nlist_build_{name}")
+        nl.build(sysd)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        counts = nl.counts()
+        out[name] = {"ms_per_build": ms, "mean_listed": float(counts.mean()), "max_listed": int(counts.max())}
+        nl.close()
+    out["note"] = ("one azp_nlist_build = cell binning + scan + scatter + per-cell sort + list kernel; CUDA events "
+                   "over 20 builds after 4")
+    print(json.dumps(out), flush=True)
+
+
 def run(args):
     import torch
 
     torch.cuda.set_device(0)
     {"lj": suite_lj, "batched": suite_batched, "adjoint": suite_adjoint, "precision": suite_precision,
-     "drivers": suite_drivers}[args.suite](args)
+     "drivers": suite_drivers, "nlist": suite_nlist}[args.suite](args)

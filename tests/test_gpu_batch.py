@@ -133,5 +133,5 @@ def test_autotune_over_block_sizes():
         out.append(r.get_arrays())
         r.close()
     for other in out[1:]:
-        assert np.abs(other[0][:, :3] - out[0][:, :3]).max() < 1e-9
+        assert np.abs(other[0][:, :3] - out[0][0][:, :3]).max() < 1e-9
         assert np.abs(other[1][:, :3] - out[0][1][:, :3]).max() < 1e-8
