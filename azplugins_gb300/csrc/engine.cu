@@ -845,6 +845,13 @@ MDArgs base_args(azp_md* m)
         a.sfix[d] = (float)(m->box.L[d] * 2.3283064365386963e-10);
         a.fscale[d] = a.Linv[d] * 4294967296.0;
     }
+    a.cubic = (m->box.L[0] == m->box.L[1] && m->box.L[1] == m->box.L[2]) ? 1 : 0;
+    {
+        const double q = m->box.L[0] * 2.3283064365386963e-10;
+        const double q2 = q * q;
+        a.s2h = (float)q2;
+        a.s2l = (float)(q2 - (double)a.s2h);
+    }
     a.counts = m->counts;
     a.nbrs = m->nbrs;
     a.max_nn = m->max_nn;
