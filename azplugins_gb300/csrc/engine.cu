@@ -715,6 +715,7 @@ struct azp_md {
     uint32_t* ex_idx = nullptr;
     double* d_bond_params = nullptr;
     double* d_pair_table = nullptr;
+    long long* d_contact_q = nullptr;  // colloid gap forms in a cubic box
     double* d_gamma = nullptr;
     double* d_noise = nullptr;
     // harmonic barrier (bar_geom -1: none): per-type (k, offset), the device table
@@ -816,7 +817,7 @@ void free_all(azp_md* m)
                     m->partials, m->thermo, m->tmp4, m->tmpd, m->snap_pos, m->snap_vel, m->snap_acc,
                     m->snap_img, m->snap_diam, m->st_pos, m->st_vel, m->st_acc, m->st_img, m->st_diam,
                     m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab, m->d_dvel, m->d_img0,
-                    m->d_kT_hdr, m->d_kT_tab, m->d_noise_tab, m->tile_tab, m->d_wall_f};
+                    m->d_kT_hdr, m->d_kT_tab, m->d_noise_tab, m->tile_tab, m->d_wall_f, m->d_contact_q};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -856,6 +857,7 @@ MDArgs base_args(azp_md* m)
     a.nbrs = m->nbrs;
     a.max_nn = m->max_nn;
     a.pair_table = m->d_pair_table;
+    a.contact_q = m->d_contact_q;
     a.bt_n = m->bt_n;
     a.bt = m->bt;
     a.bond_params = m->d_bond_params;
@@ -1463,6 +1465,24 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         }
         ALLOC(m->d_pair_table, table.size());
         CTRY(cudaMemcpy(m->d_pair_table, table.data(), sizeof(double) * table.size(), cudaMemcpyHostToDevice));
+        if (c->pair_kind == AZP_PAIR_COLLOID && c->box.L[0] == c->box.L[1] && c->box.L[1] == c->box.L[2]) {
+            // contact distances squared in the units of the integer r^2 of the
+            // FP32-force step: (2^32 / L)^2
+            const double u = 4294967296.0 / c->box.L[0];
+            std::vector<long long> cq(nt2, 0);
+            bool fits = true;  // contacts inside the half box: below 2^62 in these units
+            for (size_t t = 0; t < nt2; ++t) {
+                const double* rec = table.data() + t * PAIR_TBL;
+                if (!Colloid::gap_form(rec)) continue;
+                const double c2 = Colloid::contact2(rec);
+                if (!(c2 < 0.25 * c->box.L[0] * c->box.L[0])) fits = false;
+                else cq[t] = std::llround(c2 * u * u);
+            }
+            if (fits) {
+                ALLOC(m->d_contact_q, nt2);
+                CTRY(cudaMemcpy(m->d_contact_q, cq.data(), sizeof(long long) * nt2, cudaMemcpyHostToDevice));
+            }
+        }
         m->pair_table_host = table;
         std::vector<ListCut> cuts(nt2);
         make_list_cuts(m->r_cut.data(), c->ntypes, m->r_buff, m->box, cuts.data(), &m->rlist_max, &m->rlist_min);

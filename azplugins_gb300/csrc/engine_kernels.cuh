@@ -676,11 +676,60 @@ AZP_D float fx_rsq(const MDArgs& a, const uint4& fi, const uint4& fj, float dx, 
         const long long ix = (int32_t)(fi.x - fj.x), iy = (int32_t)(fi.y - fj.y), iz = (int32_t)(fi.z - fj.z);
         const unsigned long long q = (unsigned long long)(ix * ix) + (unsigned long long)(iy * iy) +
                                      (unsigned long long)(iz * iz);
+#if AZP_FX_IRSQ == 2
+        // the 64-bit sum to FP32 through its two 32-bit halves (the high half,
+        // below 2^23, converts exactly; one rounding in the low half, one in the FMA)
+        const float qf = fmaf((float)(uint32_t)(q >> 32), 4294967296.0f, (float)(uint32_t)q);
+#else
         const float qf = __ull2float_rn(q);
+#endif
         return fmaf(qf, a.s2h, qf * a.s2l);
     }
 #endif
     return dx * dx + dy * dy + dz * dz;
+}
+
+// r^2 and the contact difference dq = c^2 - r^2 of a colloid point-sphere or
+// sphere-sphere pair, each rounded once to FP32, for PE::eval_gap.
+// AZP_COLLOID_GAP 1: in FP64 from the exact 64-bit displacement. 2 (cubic boxes):
+// from the 64-bit displacement rounded to 2^-32 L, whose integer sum of squares q
+// (below 2^62 for a pair inside the half box) is exact, with c^2 held in the
+// same units as the 64-bit integer contact_q (c^2 2^64 / L^2): dq = contact_q - q
+// is an exact integer difference, so the cancellation costs nothing and no FP64
+// instruction runs.
+#ifndef AZP_COLLOID_GAP
+#define AZP_COLLOID_GAP 1
+#endif
+#ifndef AZP_COLLOID_NEAR
+#define AZP_COLLOID_NEAR 0
+#endif
+template<class PE>
+AZP_D void gap_args(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j, uint32_t tp,
+                    float& rsq, float& dq)
+{
+    const uint4 li = __ldg(a.flo + i), lj = __ldg(a.flo + j);
+#if AZP_COLLOID_GAP == 2
+    if (a.contact_q) {
+        const auto axis = [](uint32_t hi_i, uint32_t lo_i, uint32_t hi_j, uint32_t lo_j) -> long long {
+            const unsigned long long d = (unsigned long long)fx_join(hi_i, lo_i) - (unsigned long long)fx_join(hi_j, lo_j);
+            return (long long)(d + 0x80000000ull) >> 32;  // rounded to 2^-32 L
+        };
+        const long long ix = axis(fi.x, li.x, fj.x, lj.x), iy = axis(fi.y, li.y, fj.y, lj.y),
+                        iz = axis(fi.z, li.z, fj.z, lj.z);
+        const long long q = ix * ix + iy * iy + iz * iz;
+        const long long dqi = __ldg(a.contact_q + tp) - q;
+        const float qf = __ll2float_rn(q), df = __ll2float_rn(dqi);
+        rsq = fmaf(qf, a.s2h, qf * a.s2l);
+        dq = fmaf(df, a.s2h, df * a.s2l);
+        return;
+    }
+#endif
+    const double vx = fx_disp(fi.x, li.x, fj.x, lj.x, a.l64[0]);
+    const double vy = fx_disp(fi.y, li.y, fj.y, lj.y, a.l64[1]);
+    const double vz = fx_disp(fi.z, li.z, fj.z, lj.z, a.l64[2]);
+    const double rsq_d = vx * vx + vy * vy + vz * vz;
+    rsq = (float)rsq_d;
+    dq = (float)(PE::contact2(a.pair_table + (size_t)tp * PAIR_TBL) - rsq_d);
 }
 
 // ONE: a single-type system; the type pair is 0 at compile time, so the record
@@ -701,16 +750,12 @@ AZP_D void pair_term_fx(const MDArgs& a, const uint4& fi, const uint4& fj, uint3
     if (rsq >= rc2 * 0.999996f && !inside_exact(a, i, j, s_rc2[tp])) return;
     float fdr, e;
     if constexpr (has_gap_form<PE>::value) {
-        if (PE::gap_form(rec)) {
+        if (AZP_COLLOID_GAP && PE::gap_form(rec)) {
             // the cancelling contact difference (colloid point-sphere and
-            // sphere-sphere forms) in FP64 from the exact 64-bit displacement
-            const uint4 li = __ldg(a.flo + i), lj = __ldg(a.flo + j);
-            const double vx = fx_disp(fi.x, li.x, fj.x, lj.x, a.l64[0]);
-            const double vy = fx_disp(fi.y, li.y, fj.y, lj.y, a.l64[1]);
-            const double vz = fx_disp(fi.z, li.z, fj.z, lj.z, a.l64[2]);
-            const double rsq_d = vx * vx + vy * vy + vz * vz;
-            const double dq = PE::contact2(a.pair_table + (size_t)tp * PAIR_TBL) - rsq_d;
-            PE::eval_gap(rec, (float)rsq_d, (float)dq, fdr, e);
+            // sphere-sphere forms) formed exactly
+            float rg, dq;
+            gap_args<PE>(a, fi, fj, i, j, tp, rg, dq);
+            PE::eval_gap(rec, rg, dq, fdr, e);
         } else {
             PE::eval(rec, rsq, fdr, e);
         }
@@ -750,20 +795,24 @@ AZP_D void pair_term_fx_masked(const MDArgs& a, const uint4& fi, const uint4& fj
     if (on && !in && rsq < rc2 * 1.000004f) in = inside_exact(a, i, jof(), s_rc2[tp]);
     const float rs = in ? rsq : rc2;
     float fdr, e;
-    if constexpr (has_gap_form<PE>::value) {
-        if (in && PE::gap_form(rec)) {
-            // the cancelling contact difference (colloid point-sphere and
-            // sphere-sphere forms) in FP64 from the exact 64-bit displacement
-            const uint4 li = __ldg(a.flo + i), lj = __ldg(a.flo + jof());
-            const double vx = fx_disp(fi.x, li.x, fj.x, lj.x, a.l64[0]);
-            const double vy = fx_disp(fi.y, li.y, fj.y, lj.y, a.l64[1]);
-            const double vz = fx_disp(fi.z, li.z, fj.z, lj.z, a.l64[2]);
-            const double rsq_d = vx * vx + vy * vy + vz * vz;
-            const double dq = PE::contact2(a.pair_table + (size_t)tp * PAIR_TBL) - rsq_d;
-            PE::eval_gap(rec, (float)rsq_d, (float)dq, fdr, e);
-        } else {
-            PE::eval(rec, rs, fdr, e);
+    if constexpr (has_gap_form<PE>::value && AZP_COLLOID_GAP != 0) {
+        // the cancelling contact difference of the colloid point-sphere and
+        // sphere-sphere forms formed exactly for a pair inside r_cut (a masked
+        // slot takes any finite gap); every lane then runs one evaluation of its
+        // own form, so a warp never runs a gap form twice
+        float rg = rs, dq = 0.0f;
+        if (PE::gap_form(rec)) {
+            const float c2 = PE::contact2_f(rec);
+            dq = c2 - rs;
+#if AZP_COLLOID_NEAR
+            // only near contact (r^2 < 2 c^2) does the FP32 difference cancel
+            // enough to matter; farther out it stays within a few 1e-7 of c^2
+            if (in && rs < 2.0f * c2) gap_args<PE>(a, fi, fj, i, jof(), tp, rg, dq);
+#else
+            if (in) gap_args<PE>(a, fi, fj, i, jof(), tp, rg, dq);
+#endif
         }
+        PE::eval_any(rec, rg, dq, fdr, e);
     } else {
         PE::eval(rec, rs, fdr, e);
     }
@@ -916,6 +965,12 @@ constexpr int fx_min_blocks()
     return (ONE && !OUT && fx_light<PE>::value && FX_BLOCK == 256) ? 5 : 4;
 #endif
 }
+
+// neighbour list entries of the next batch loaded while the current batch is
+// evaluated (1), or at the top of each batch (0)
+#ifndef AZP_FX_PIPE
+#define AZP_FX_PIPE 0
+#endif
 
 // prefetch of the DRAM rows a warp's particles read (0 off, 1 into L1, 2 into L2)
 #ifndef AZP_FX_PREFETCH
@@ -1122,14 +1177,29 @@ __global__ void __launch_bounds__(FX_BLOCK, (fx_min_blocks<PE, OUT, ONE>())) k_m
 #else
             const uint32_t kend = n;
 #endif
+#if AZP_FX_PIPE
+            // the list entries of the first batch; each later batch's entries are
+            // loaded while the current batch is evaluated
+            uint32_t jn[FX_BATCH];
+#pragma unroll
+            for (int u = 0; u < FX_BATCH; ++u) {
+                const uint32_t k = sub + u * tpp;
+                jn[u] = k < n ? __ldg(col + (size_t)k * a.N) : (TILE ? (TILE_GLOBAL | i) : i);
+            }
+#endif
             for (uint32_t kb = sub; kb < kend; kb += FX_BATCH * tpp) {
                 uint32_t jj[FX_BATCH];
                 uint4 fj[FX_BATCH];
+#if AZP_FX_PIPE
+#pragma unroll
+                for (int u = 0; u < FX_BATCH; ++u) jj[u] = jn[u];
+#else
 #pragma unroll
                 for (int u = 0; u < FX_BATCH; ++u) {
                     const uint32_t k = kb + u * tpp;
                     jj[u] = k < n ? __ldg(col + (size_t)k * a.N) : (TILE ? (TILE_GLOBAL | i) : i);
                 }
+#endif
                 if constexpr (TILE) {
 #pragma unroll
                     for (int u = 0; u < FX_BATCH; ++u)
@@ -1138,6 +1208,13 @@ __global__ void __launch_bounds__(FX_BLOCK, (fx_min_blocks<PE, OUT, ONE>())) k_m
 #pragma unroll
                     for (int u = 0; u < FX_BATCH; ++u) fj[u] = __ldg(a.fix + jj[u]);
                 }
+#if AZP_FX_PIPE
+#pragma unroll
+                for (int u = 0; u < FX_BATCH; ++u) {
+                    const uint32_t k = kb + (FX_BATCH + u) * tpp;
+                    jn[u] = k < n ? __ldg(col + (size_t)k * a.N) : (TILE ? (TILE_GLOBAL | i) : i);
+                }
+#endif
 #pragma unroll
                 for (int u = 0; u < FX_BATCH; ++u) {
                     if constexpr (std::is_same<PE, DpdEngine>::value) {

@@ -219,8 +219,8 @@ struct Colloid {
         return c * c;
     }
     // FP32 evaluation of a gap form with rsq and dq = contact^2 - rsq formed by
-    // the caller in FP64 from an exact displacement, each rounded once to FP32:
-    // the point-sphere d is dq, the sphere-sphere gap is dq / (a_1 + a_2 + r).
+    // the caller from an exact displacement, each rounded once to FP32: the
+    // point-sphere d is dq, the sphere-sphere gap is dq / (a_1 + a_2 + r).
     AZP_D static void eval_gap(const float* rec, float rsq, float dq, float& fdr, float& e)
     {
         if (rec[5] == 1.0f) {
@@ -229,6 +229,19 @@ struct Colloid {
             const float r = sqrtf(rsq);
             cc_form(rec, r, dq / ((rec[1] + rec[2]) + r), fdr, e);
         }
+    }
+    // squared contact distance of the form from the FP32 record
+    AZP_D static float contact2_f(const float* rec)
+    {
+        const float c = rec[5] == 1.0f ? rec[6] : rec[1] + rec[2];
+        return c * c;
+    }
+    // one evaluation per pair whatever its form: the LJ form (solvent pairs) on
+    // rsq, the gap forms on (rsq, dq) as eval_gap
+    AZP_D static void eval_any(const float* rec, float rsq, float dq, float& fdr, float& e)
+    {
+        if (rec[5] == 0.0f) eval(rec, rsq, fdr, e);
+        else eval_gap(rec, rsq, dq, fdr, e);
     }
 };
 
