@@ -110,6 +110,16 @@ __global__ void __launch_bounds__(kSortWarps * 32) k_b_cell_sort(const uint32_t*
     sort_cells_warp(cell_start, members, ncell, s_rows[threadIdx.x >> 5]);
 }
 
+__global__ void __launch_bounds__(kSortWarps * 32) k_b_cell_sort_crowded(const uint32_t* __restrict__ cell_start,
+                                                                         uint32_t* __restrict__ members,
+                                                                         uint32_t ncell,
+                                                                         const uint32_t* __restrict__ gate)
+{
+    if (gated_off(gate)) return;
+    __shared__ uint32_t s_rows[kSortWarps][kMaxSortedCell];
+    sort_cell_per_warp(cell_start, members, ncell, s_rows[threadIdx.x >> 5]);
+}
+
 struct BPerm {
     const uint32_t* members;
     double4_32a *pos, *t_pos, *vel, *t_vel;
@@ -271,6 +281,12 @@ struct BStep {
     int set_cond;
 };
 
+// neighbours gathered per batch in the FP32-force pair loop
+#ifndef AZP_B_BATCH
+#define AZP_B_BATCH 4
+#endif
+constexpr int B_BATCH = AZP_B_BATCH;
+
 template<class PE, typename R>
 __global__ void __launch_bounds__(BATCH_BLOCK_MAX) k_b_step(BStep a)
 {
@@ -307,27 +323,42 @@ __global__ void __launch_bounds__(BATCH_BLOCK_MAX) k_b_step(BStep a)
         } else {
             const uint4 fi = a.fix[i];
             const float rc2 = (float)si->rcutsq;
-            for (uint32_t k = sub; k < n; k += tpp) {
-                const uint32_t j = a.nbrs[(size_t)k * a.N + i];
-                const uint4 fj = a.fix[j];
-                const float dx = (float)(int32_t)(fi.x - fj.x) * si->sfix[0];
-                const float dy = (float)(int32_t)(fi.y - fj.y) * si->sfix[1];
-                const float dz = (float)(int32_t)(fi.z - fj.z) * si->sfix[2];
-                const float rsq = dx * dx + dy * dy + dz * dz;
-                if (rsq >= rc2 * 1.000004f) continue;
-                if (rsq >= rc2 * 0.999996f) {
-                    const double4_32a pi = a.pos[i];
-                    const double4_32a pj = a.pos[j];
-                    const double vx = min_image1(pi.x - pj.x, si->L[0], si->Linv[0]);
-                    const double vy = min_image1(pi.y - pj.y, si->L[1], si->Linv[1]);
-                    const double vz = min_image1(pi.z - pj.z, si->L[2], si->Linv[2]);
-                    if (!(rsq_exact(vx, vy, vz) < si->rcutsq)) continue;
+            // neighbours in batches of B_BATCH: the list entries of a batch first,
+            // then their fixed-point words, so that B_BATCH gathers are in flight;
+            // the pairs are then added in list order as one at a time would
+            const uint32_t* col = a.nbrs + i;
+            for (uint32_t kb = sub; kb < n; kb += B_BATCH * tpp) {
+                uint32_t jj[B_BATCH];
+                uint4 fj[B_BATCH];
+#pragma unroll
+                for (int u = 0; u < B_BATCH; ++u) {
+                    const uint32_t k = kb + u * tpp;
+                    jj[u] = k < n ? __ldg(col + (size_t)k * a.N) : i;
                 }
-                float fdr, e;
-                PE::eval(rec, rsq, fdr, e);
-                cx.add(dx * fdr);
-                cy.add(dy * fdr);
-                cz.add(dz * fdr);
+#pragma unroll
+                for (int u = 0; u < B_BATCH; ++u) fj[u] = __ldg(a.fix + jj[u]);
+#pragma unroll
+                for (int u = 0; u < B_BATCH; ++u) {
+                    if (kb + u * tpp >= n) break;
+                    const float dx = (float)(int32_t)(fi.x - fj[u].x) * si->sfix[0];
+                    const float dy = (float)(int32_t)(fi.y - fj[u].y) * si->sfix[1];
+                    const float dz = (float)(int32_t)(fi.z - fj[u].z) * si->sfix[2];
+                    const float rsq = dx * dx + dy * dy + dz * dz;
+                    if (rsq >= rc2 * 1.000004f) continue;
+                    if (rsq >= rc2 * 0.999996f) {
+                        const double4_32a pi = a.pos[i];
+                        const double4_32a pj = a.pos[jj[u]];
+                        const double vx = min_image1(pi.x - pj.x, si->L[0], si->Linv[0]);
+                        const double vy = min_image1(pi.y - pj.y, si->L[1], si->Linv[1]);
+                        const double vz = min_image1(pi.z - pj.z, si->L[2], si->Linv[2]);
+                        if (!(rsq_exact(vx, vy, vz) < si->rcutsq)) continue;
+                    }
+                    float fdr, e;
+                    PE::eval(rec, rsq, fdr, e);
+                    cx.add(dx * fdr);
+                    cy.add(dy * fdr);
+                    cz.add(dz * fdr);
+                }
             }
         }
     }
@@ -640,8 +671,12 @@ int b_rebuild(azp_batch* b, cudaStream_t s, const uint32_t* gate)
     int st = exclusive_scan(b->cell_count, b->cell_start, b->ncell, b->scan_tmp, s, gate);
     if (st) return st;
     k_b_scatter<<<nblk(N), 256, 0, s>>>(b->cell_of, b->slot, b->cell_start, b->members, N, gate);
-    k_b_cell_sort<<<(b->ncell + 32 * kSortWarps - 1) / (32 * kSortWarps), kSortWarps * 32, 0, s>>>(
-        b->cell_start, b->members, b->ncell, gate);
+    if (crowded_grid(N, b->ncell))
+        k_b_cell_sort_crowded<<<(b->ncell + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(
+            b->cell_start, b->members, b->ncell, gate);
+    else
+        k_b_cell_sort<<<(b->ncell + 32 * kSortWarps - 1) / (32 * kSortWarps), kSortWarps * 32, 0, s>>>(
+            b->cell_start, b->members, b->ncell, gate);
     BPerm p;
     p.members = b->members;
     p.pos = b->pos[b->cur];

@@ -67,13 +67,16 @@ __device__ __forceinline__ void warp_sort_cell(uint32_t* __restrict__ members, u
 // is scanned as a single cell (no duplicate images).
 struct CellGrid {
     int dim[3];
-    int reach[3];    // 1 when the axis has >= 3 cells, else 0
+    int reach[3];    // stencil cells each way (the subdivision), 0 for an axis too short for it
     double lo[3];    // -L/2
     double scale[3]; // dim / L
     uint32_t ncell;
 };
 
-CellGrid make_grid(const azp_box& box, double rlist_max);
+// sub: cells of width >= r_list_max / sub and a stencil of sub cells each way
+CellGrid make_grid(const azp_box& box, double rlist_max, int sub = 1);
+// the subdivision the engine and the list object use (AZP_NL_SUB, default 1)
+int grid_subdivision();
 
 // Per type pair thresholds of the list decision (host-built, ntypes^2 entries).
 struct ListCut {
@@ -196,5 +199,25 @@ __device__ __forceinline__ void sort_cells_warp(const uint32_t* __restrict__ cel
         __syncwarp();
     }
 }
+
+// Crowded grids (more than kSerialCell particles per cell on average): one warp
+// per cell, so that the cells are sorted side by side instead of 32 after one
+// another in each warp.
+__device__ __forceinline__ void sort_cell_per_warp(const uint32_t* __restrict__ cell_start,
+                                                   uint32_t* __restrict__ members, uint32_t ncell,
+                                                   uint32_t* __restrict__ s_row)
+{
+    const uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= ncell) return;  // warp-uniform
+    const uint32_t b = cell_start[c], e = cell_start[c + 1];
+    if (e - b <= kSerialCell) {
+        if ((threadIdx.x & 31u) == 0u && e - b >= 2u) thread_sort_cell(members, b, e);
+        return;
+    }
+    warp_sort_cell(members, b, e, s_row);
+}
+
+// whether a grid of ncell cells holding N particles is sorted a warp per cell
+inline bool crowded_grid(uint32_t N, uint32_t ncell) { return ncell > 0 && N > kSerialCell * ncell; }
 
 }  // namespace azp

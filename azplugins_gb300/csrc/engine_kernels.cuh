@@ -691,17 +691,18 @@ AZP_D float fx_rsq(const MDArgs& a, const uint4& fi, const uint4& fj, float dx, 
 
 // r^2 and the contact difference dq = c^2 - r^2 of a colloid point-sphere or
 // sphere-sphere pair, each rounded once to FP32, for PE::eval_gap.
-// AZP_COLLOID_GAP 1: in FP64 from the exact 64-bit displacement. 2 (cubic boxes):
-// from the 64-bit displacement rounded to 2^-32 L, whose integer sum of squares q
-// (below 2^62 for a pair inside the half box) is exact, with c^2 held in the
-// same units as the 64-bit integer contact_q (c^2 2^64 / L^2): dq = contact_q - q
-// is an exact integer difference, so the cancellation costs nothing and no FP64
-// instruction runs.
+// AZP_COLLOID_GAP 2 (default; cubic boxes): from the 64-bit displacement rounded
+// to 2^-32 L, whose integer sum of squares q (below 2^62 for a pair inside the
+// half box) is exact, with c^2 held in the same units as the 64-bit integer
+// contact_q (c^2 2^64 / L^2): dq = contact_q - q is an exact integer difference,
+// so the cancellation costs nothing and no FP64 instruction runs. Other boxes, and
+// AZP_COLLOID_GAP 1: in FP64 from the exact 64-bit displacement. Measured on the
+// colloid mixture (N = 262,144, 5000 Brownian steps): FP64 841 timesteps/s, force
+// error 6.7e-6; integer 968, 7.2e-6; the FP32 forms on the FP32 r^2 (0) 1,399 but
+// 1.1e-5, over the 1e-5 budget; the exact difference only for r^2 < 2 c^2 1,015,
+// 8.2e-6.
 #ifndef AZP_COLLOID_GAP
-#define AZP_COLLOID_GAP 1
-#endif
-#ifndef AZP_COLLOID_NEAR
-#define AZP_COLLOID_NEAR 0
+#define AZP_COLLOID_GAP 2
 #endif
 template<class PE>
 AZP_D void gap_args(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j, uint32_t tp,
@@ -802,15 +803,8 @@ AZP_D void pair_term_fx_masked(const MDArgs& a, const uint4& fi, const uint4& fj
         // own form, so a warp never runs a gap form twice
         float rg = rs, dq = 0.0f;
         if (PE::gap_form(rec)) {
-            const float c2 = PE::contact2_f(rec);
-            dq = c2 - rs;
-#if AZP_COLLOID_NEAR
-            // only near contact (r^2 < 2 c^2) does the FP32 difference cancel
-            // enough to matter; farther out it stays within a few 1e-7 of c^2
-            if (in && rs < 2.0f * c2) gap_args<PE>(a, fi, fj, i, jof(), tp, rg, dq);
-#else
+            dq = PE::contact2_f(rec) - rs;
             if (in) gap_args<PE>(a, fi, fj, i, jof(), tp, rg, dq);
-#endif
         }
         PE::eval_any(rec, rg, dq, fdr, e);
     } else {

@@ -10,6 +10,7 @@
 // larger than its worst-case error, so the sets are bit-exact.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -22,25 +23,42 @@
 namespace azp
 {
 // ---------------------------------------------------------------- host helpers
-CellGrid make_grid(const azp_box& box, double rlist_max)
+CellGrid make_grid(const azp_box& box, double rlist_max, int sub)
 {
     CellGrid g;
     g.ncell = 1;
-    // cell width >= r_list; widened if the grid would exceed 2^24 cells
-    double w = rlist_max;
+    // cell width >= r_list / sub, the stencil reaching sub cells each way;
+    // widened if the grid would exceed 2^24 cells
+    if (sub < 1) sub = 1;
+    double w = rlist_max / sub;
     if (w > 0.0) {
         while ((box.L[0] / w) * (box.L[1] / w) * (box.L[2] / w) > 16777216.0) w *= 1.25;
     }
     for (int d = 0; d < 3; ++d) {
         int n = w > 0.0 ? (int)std::floor(box.L[d] / w) : 1;
-        if (n < 3) n = 1;
+        int reach = sub;
+        if (n < 2 * reach + 1) {
+            // too few cells for distinct images along this axis: one cell
+            n = 1;
+            reach = 0;
+        }
         g.dim[d] = n;
-        g.reach[d] = n >= 3 ? 1 : 0;
+        g.reach[d] = reach;
         g.lo[d] = -0.5 * box.L[d];
         g.scale[d] = (double)n / box.L[d];
         g.ncell *= (uint32_t)n;
     }
     return g;
+}
+
+int grid_subdivision()
+{
+    static const int sub = [] {
+        const char* e = std::getenv("AZP_NL_SUB");
+        const int v = e ? std::atoi(e) : 1;
+        return v >= 1 && v <= 4 ? v : 1;
+    }();
+    return sub;
 }
 
 void make_list_cuts(const double* r_cut, uint32_t ntypes, double r_buff, const azp_box& box, ListCut* out,
@@ -137,6 +155,16 @@ __global__ void __launch_bounds__(kSortWarps * 32) k_cell_sort(const uint32_t* _
     if (gated_off(gate)) return;
     __shared__ uint32_t s_rows[kSortWarps][kMaxSortedCell];
     sort_cells_warp(cell_start, members, ncell, s_rows[threadIdx.x >> 5]);
+}
+
+// crowded grids: a warp per cell
+__global__ void __launch_bounds__(kSortWarps * 32) k_cell_sort_crowded(const uint32_t* __restrict__ cell_start,
+                                                                       uint32_t* __restrict__ members, uint32_t ncell,
+                                                                       const uint32_t* __restrict__ gate)
+{
+    if (gated_off(gate)) return;
+    __shared__ uint32_t s_rows[kSortWarps][kMaxSortedCell];
+    sort_cell_per_warp(cell_start, members, ncell, s_rows[threadIdx.x >> 5]);
 }
 
 struct BoxArgs {
@@ -258,13 +286,17 @@ __global__ void __launch_bounds__(NLIST_BLOCK)
     const int cx = (int)(cc % (uint32_t)dx);
     const int cy = (int)((cc / (uint32_t)dx) % (uint32_t)dy);
     const int cz = (int)(cc / ((uint32_t)dx * (uint32_t)dy));
-    int x0 = cx - g.reach[0], x1 = cx + g.reach[0], xw = -1;
+    // the x-cells cx - reach .. cx + reach: one contiguous range inside the row,
+    // and the wrapped part at an x face, contiguous too ([wb, we]; empty: wb > we)
+    int x0 = cx - g.reach[0], x1 = cx + g.reach[0], wb = 1, we = 0;
     if (x0 < 0) {
-        xw = dx - 1;
+        wb = dx + x0;
+        we = dx - 1;
         x0 = 0;
     }
     if (x1 >= dx) {
-        xw = 0;
+        wb = 0;
+        we = x1 - dx;
         x1 = dx - 1;
     }
     uint32_t ex[NL_EX_REG];
@@ -286,9 +318,9 @@ __global__ void __launch_bounds__(NLIST_BLOCK)
                     sb = __ldg(cell_start + rb + x0);
                     se = __ldg(cell_start + rb + x1 + 1);
                 } else {
-                    if (xw < 0) break;
-                    sb = __ldg(cell_start + rb + xw);
-                    se = __ldg(cell_start + rb + xw + 1);
+                    if (wb > we) break;
+                    sb = __ldg(cell_start + rb + wb);
+                    se = __ldg(cell_start + rb + we + 1);
                 }
 #pragma unroll 4
                 for (uint32_t sl = sb; sl < se; ++sl) {
@@ -452,8 +484,12 @@ void launch_cell_scatter(const uint32_t* cell_of, const uint32_t* slot, const ui
 {
     if (N == 0) return;
     k_cell_scatter<<<(N + 255) / 256, 256, 0, s>>>(cell_of, slot, cell_start, members, N, gate);
-    k_cell_sort<<<(ncell + 32 * kSortWarps - 1) / (32 * kSortWarps), kSortWarps * 32, 0, s>>>(cell_start, members,
-                                                                                              ncell, gate);
+    if (crowded_grid(N, ncell))
+        k_cell_sort_crowded<<<(ncell + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(cell_start, members,
+                                                                                            ncell, gate);
+    else
+        k_cell_sort<<<(ncell + 32 * kSortWarps - 1) / (32 * kSortWarps), kSortWarps * 32, 0, s>>>(cell_start, members,
+                                                                                                  ncell, gate);
 }
 
 __global__ void k_to_fixed2(const double4_32a* __restrict__ pos, uint4* __restrict__ fa, uint4* __restrict__ fb,
@@ -654,7 +690,7 @@ int azp_nlist_build(azp_nlist* nl, const azp_system* sys, void* stream)
     azp::make_list_cuts(nl->r_cut.data(), nl->ntypes, nl->r_buff, sys->box, cuts.data(), &rmax, &rmin);
     for (int d = 0; d < 3; ++d)
         if (rmax > 0.0 && sys->box.L[d] < 2.0 * rmax) return AZP_ERR_BOX_TOO_SMALL;
-    const azp::CellGrid g = azp::make_grid(sys->box, rmax);
+    const azp::CellGrid g = azp::make_grid(sys->box, rmax, azp::grid_subdivision());
     int st = ensure_cells(nl, g.ncell);
     if (st) return st;
     AZP_CUDA_TRY(cudaMemcpyAsync(nl->cuts, cuts.data(), sizeof(azp::ListCut) * cuts.size(), cudaMemcpyHostToDevice, s));
