@@ -75,8 +75,9 @@ struct CellGrid {
 
 // sub: cells of width >= r_list_max / sub and a stencil of sub cells each way
 CellGrid make_grid(const azp_box& box, double rlist_max, int sub = 1);
-// the subdivision the engine and the list object use (AZP_NL_SUB, default 1)
-int grid_subdivision();
+// the subdivision the engine and the list object use: AZP_NL_SUB when set, else
+// the ratio of the largest to the smallest list radius, 1 to 3
+int grid_subdivision(double rlist_max, double rlist_min);
 
 // Per type pair thresholds of the list decision (host-built, ntypes^2 entries).
 struct ListCut {

@@ -1498,10 +1498,12 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         const char* env_tiles = std::getenv("AZP_TILES");
         const bool one = c->ntypes == 1 && (c->bond_kind < 0 || c->nbondtypes <= 1) && !c->use_lambda;
         if (c->precision == AZP_FP32 && one && m->tpp == 1 && m->pair_kind != AZP_PAIR_DPD_GENERAL_WEIGHT &&
-            m->bond_kind != AZP_BOND_IMAGE_HARMONIC && env_tiles && env_tiles[0] == '1' && grid_subdivision() == 1)
+            m->bond_kind != AZP_BOND_IMAGE_HARMONIC && env_tiles && env_tiles[0] == '1' &&
+            grid_subdivision(m->rlist_max, m->rlist_min) == 1)
             ALLOC(m->tile_tab, (size_t)((N + TILE_P - 1) / TILE_P) * TILE_REC);
     }
-    m->grid = make_grid(m->box, m->rlist_max > 0.0 ? m->rlist_max : std::max(m->box.L[0], 1.0), grid_subdivision());
+    m->grid = make_grid(m->box, m->rlist_max > 0.0 ? m->rlist_max : std::max(m->box.L[0], 1.0),
+                        grid_subdivision(m->rlist_max, m->rlist_min));
     ALLOC(m->cell_count, m->grid.ncell);
     ALLOC(m->cell_start, (size_t)m->grid.ncell + 1);
     ALLOC(m->scan_tmp, scan_tmp_words(m->grid.ncell));
