@@ -428,7 +428,10 @@ __global__ void k_thermo_partials(const double4_32a* __restrict__ f, const doubl
 // one block of THERMO_BLOCK threads: thread t sums the partials of blocks t,
 // t + THERMO_BLOCK, ... in order, then a fixed tree adds the threads' sums (the
 // same order every call)
+// out[0..7]: the sums; out[8..11]: the engine's eight flag words, so that one
+// read returns both
 __global__ void __launch_bounds__(THERMO_BLOCK) k_thermo_final(const double* __restrict__ part, uint32_t nb,
+                                                              const uint32_t* __restrict__ flags,
                                                               double* __restrict__ out)
 {
     __shared__ double s[THERMO_BLOCK][8];
@@ -443,6 +446,7 @@ __global__ void __launch_bounds__(THERMO_BLOCK) k_thermo_final(const double* __r
         __syncthreads();
     }
     if (threadIdx.x < 8) out[threadIdx.x] = s[0][threadIdx.x];
+    else if (threadIdx.x < 16) reinterpret_cast<uint32_t*>(out + 8)[threadIdx.x - 8] = flags[threadIdx.x - 8];
 }
 
 // index order -> tag order
@@ -715,6 +719,7 @@ struct azp_md {
     uint32_t* ex_idx = nullptr;
     double* d_bond_params = nullptr;
     double* d_pair_table = nullptr;
+    double* h_thermo = nullptr;  // pinned readback of the thermo sums and flags
     long long* d_contact_q = nullptr;  // colloid gap forms in a cubic box
     double* d_gamma = nullptr;
     double* d_noise = nullptr;
@@ -819,6 +824,8 @@ void free_all(azp_md* m)
                     m->d_bar_tab, m->d_bar_hdr, m->d_walls, m->d_wall_tab, m->d_dvel, m->d_img0,
                     m->d_kT_hdr, m->d_kT_tab, m->d_noise_tab, m->tile_tab, m->d_wall_f, m->d_contact_q};
     for (void* p : ptrs) cudaFree(p);
+    if (m->h_thermo) cudaFreeHost(m->h_thermo);
+    m->h_thermo = nullptr;
 }
 
 uint32_t blocks_for(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
@@ -1420,7 +1427,8 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     ALLOC(m->tmp4, N);
     ALLOC(m->tmpd, (size_t)6 * N);
     ALLOC(m->partials, (size_t)8 * (blocks_for(N, THERMO_BLOCK) + 1));
-    ALLOC(m->thermo, 8);
+    ALLOC(m->thermo, 12);
+    CTRY(cudaMallocHost(&m->h_thermo, sizeof(double) * 12));
     ALLOC(m->d_gamma, c->ntypes);
     ALLOC(m->d_noise, c->ntypes);
     if (c->pair_kind == AZP_PAIR_DPD_GENERAL_WEIGHT) ALLOC(m->d_dvel, (size_t)4 * N);
@@ -1919,13 +1927,13 @@ int azp_md_thermo(azp_md* m, double* out, void* stream)
     }
     const uint32_t nb = blocks_for(N, THERMO_BLOCK);
     k_thermo_partials<<<nb, THERMO_BLOCK, 0, s>>>(m->out_force, m->out_virial, m->vel, m->mass, N, m->partials);
-    k_thermo_final<<<1, THERMO_BLOCK, 0, s>>>(m->partials, nb, m->thermo);
+    k_thermo_final<<<1, THERMO_BLOCK, 0, s>>>(m->partials, nb, m->flags, m->thermo);
     AZP_CHECK_LAUNCH("azp_md_thermo");
-    double h[8];
-    uint32_t f[8];
-    AZP_CUDA_TRY(cudaMemcpyAsync(h, m->thermo, sizeof(h), cudaMemcpyDeviceToHost, s));
-    AZP_CUDA_TRY(cudaMemcpyAsync(f, m->flags, sizeof(f), cudaMemcpyDeviceToHost, s));
+    double* h = m->h_thermo;
+    AZP_CUDA_TRY(cudaMemcpyAsync(h, m->thermo, sizeof(double) * 12, cudaMemcpyDeviceToHost, s));
     AZP_CUDA_TRY(cudaStreamSynchronize(s));
+    uint32_t f[8];
+    std::memcpy(f, h + 8, sizeof(f));
     for (int c = 0; c < 8; ++c) out[c] = h[c];
     out[8] = (double)f[2];
     // the error word came back with the sums (check_errors without a second read)

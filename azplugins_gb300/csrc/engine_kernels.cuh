@@ -658,16 +658,18 @@ AZP_D double fx_disp(uint32_t hi_i, uint32_t lo_i, uint32_t hi_j, uint32_t lo_j,
     return (double)d * l64;
 }
 
-// r^2 of the displacement between two fixed-point positions (high words): the
-// sum of squares of the FP32 components (default), or, with AZP_FX_IRSQ=1 and a
-// cubic box, the exact integer sum of squares of the int32 differences (each
-// below 2^62, the sum below 2^64) rounded once to FP32 and scaled by
-// (L / 2^32)^2 held as a float pair. The integer form's r^2 is about three times
-// closer (1.2e-7 against 3.4e-7 relative), which r^-14 and the bond polynomial
-// amplify: on the relaxed melt at N = 1M the force error drops from 8-9e-6 to
-// 6e-6, but the step kernel takes 12 % longer (0.090 -> 0.101 ms), so it is off.
+// r^2 of the displacement between two fixed-point positions (high words): in a
+// cubic box (AZP_FX_IRSQ=1, the default) the exact integer sum of squares of the
+// int32 differences (each below 2^62, the sum below 2^64) rounded once to FP32
+// and scaled by (L / 2^32)^2 held as a float pair; otherwise the sum of squares of
+// the FP32 components. The integer form's r^2 is about three times closer (1.2e-7
+// against 3.4e-7 relative), which r^-14 and the bond polynomial amplify: on the
+// melt at N = 1M the force error against the FP64 oracle was 8.2e-6 to 1.07e-5
+// over the end states of the bench runs with the FP32 components (over the 1e-5
+// budget once) and 5.8-6.1e-6 with the integer form, for a step kernel about
+// 9 % longer (0.090 -> 0.098 ms).
 #ifndef AZP_FX_IRSQ
-#define AZP_FX_IRSQ 0
+#define AZP_FX_IRSQ 1
 #endif
 AZP_D float fx_rsq(const MDArgs& a, const uint4& fi, const uint4& fj, float dx, float dy, float dz)
 {
@@ -940,10 +942,11 @@ AZP_D void finish_step(const MDArgs& a, bool want_rebuild)
 #endif
 constexpr int FX_BATCH = AZP_FX_BATCH;
 // Resident blocks per SM the FP32-force step is compiled for (the register cap):
-// 5 (48 registers) for the plain single-type step of the light evaluators, whose
-// few spilled bytes cost less than the extra resident warps gain (measured on the
-// melt at N = 1M: 0.0946 -> 0.0897 ms); 4 (64 registers) for the rest, which
-// would spill hundreds of bytes at 48 (Colloid, DPD, energy-writing launches).
+// with the FP32-component r^2, 5 (48 registers) for the plain single-type step of
+// the light evaluators, whose few spilled bytes cost less than the extra resident
+// warps gain (measured on the melt at N = 1M: 0.0946 -> 0.0897 ms); 4 (64
+// registers) for the rest, which would spill hundreds of bytes at 48 (Colloid,
+// DPD, energy-writing launches), and for every step with the integer r^2.
 // AZP_FX_MIN_BLOCKS overrides both.
 template<class PE> struct fx_light : std::false_type {};
 template<> struct fx_light<PerturbedLJ> : std::true_type {};
@@ -956,7 +959,8 @@ constexpr int fx_min_blocks()
 #ifdef AZP_FX_MIN_BLOCKS
     return AZP_FX_MIN_BLOCKS;
 #else
-    return (ONE && !OUT && fx_light<PE>::value && FX_BLOCK == 256) ? 5 : 4;
+    // with the integer r^2 (more registers live) 4 blocks measured faster
+    return (ONE && !OUT && fx_light<PE>::value && FX_BLOCK == 256 && !AZP_FX_IRSQ) ? 5 : 4;
 #endif
 }
 
