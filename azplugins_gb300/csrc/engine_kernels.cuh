@@ -678,13 +678,9 @@ AZP_D float fx_rsq(const MDArgs& a, const uint4& fi, const uint4& fj, float dx, 
         const long long ix = (int32_t)(fi.x - fj.x), iy = (int32_t)(fi.y - fj.y), iz = (int32_t)(fi.z - fj.z);
         const unsigned long long q = (unsigned long long)(ix * ix) + (unsigned long long)(iy * iy) +
                                      (unsigned long long)(iz * iz);
-#if AZP_FX_IRSQ == 2
-        // the 64-bit sum to FP32 through its two 32-bit halves (the high half,
-        // below 2^23, converts exactly; one rounding in the low half, one in the FMA)
-        const float qf = fmaf((float)(uint32_t)(q >> 32), 4294967296.0f, (float)(uint32_t)q);
-#else
+        // (the conversion runs on the FP64 pipe, 32 % busy; a shifted 32-bit
+        // conversion on other pipes measured slower, 0.102 against 0.098 ms)
         const float qf = __ull2float_rn(q);
-#endif
         return fmaf(qf, a.s2h, qf * a.s2l);
     }
 #endif

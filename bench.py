@@ -275,7 +275,7 @@ def step_bytes(n_particles, n_nbr_mean, n_bond_mean, builds_per_step, precision=
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernel on the melt at
 # N = 700,000, whose step traffic and resident set exceed L2
 # (profiles/k_md_step_fx_melt700k.md); scaled to a launch by N
-TRAFFIC_BYTES_PER_PARTICLE_FP32 = 185.6
+TRAFFIC_BYTES_PER_PARTICLE_FP32 = 183.0
 
 
 def measured_peak():
