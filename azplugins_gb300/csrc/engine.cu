@@ -1473,16 +1473,17 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         }
         ALLOC(m->d_pair_table, table.size());
         CTRY(cudaMemcpy(m->d_pair_table, table.data(), sizeof(double) * table.size(), cudaMemcpyHostToDevice));
-        if (c->pair_kind == AZP_PAIR_COLLOID && c->box.L[0] == c->box.L[1] && c->box.L[1] == c->box.L[2]) {
-            // contact distances squared in the units of the integer r^2 of the
-            // FP32-force step: (2^32 / L)^2
+        const bool dpd = c->pair_kind == AZP_PAIR_DPD_GENERAL_WEIGHT;
+        if ((c->pair_kind == AZP_PAIR_COLLOID || dpd) && c->box.L[0] == c->box.L[1] && c->box.L[1] == c->box.L[2]) {
+            // squared distances in the units of the integer r^2 of the FP32-force
+            // step, (2^32 / L)^2: the colloid contact distances, the DPD cutoffs
             const double u = 4294967296.0 / c->box.L[0];
             std::vector<long long> cq(nt2, 0);
-            bool fits = true;  // contacts inside the half box: below 2^62 in these units
+            bool fits = true;  // inside the half box: below 2^62 in these units
             for (size_t t = 0; t < nt2; ++t) {
                 const double* rec = table.data() + t * PAIR_TBL;
-                if (!Colloid::gap_form(rec)) continue;
-                const double c2 = Colloid::contact2(rec);
+                if (!dpd && !Colloid::gap_form(rec)) continue;
+                const double c2 = dpd ? m->r_cut[t] * m->r_cut[t] : Colloid::contact2(rec);
                 if (!(c2 < 0.25 * c->box.L[0] * c->box.L[0])) fits = false;
                 else cq[t] = std::llround(c2 * u * u);
             }

@@ -70,7 +70,8 @@ struct MDArgs {
     float s64h[3], s64l[3];     // 2^32 / L as a float pair
     int cubic;                  // Lx == Ly == Lz: r^2 from the exact integer displacement (fx_rsq)
     float s2h, s2l;             // (L / 2^32)^2 as a float pair (cubic boxes)
-    // colloid gap forms, cubic boxes: c^2 2^64 / L^2 per type pair (0: no gap form)
+    // cubic boxes, per type pair in the units of the integer r^2, c^2 2^64 / L^2:
+    // the colloid gap forms' contact distance (0: no gap form), the DPD cutoff
     const long long* contact_q;
     double l64[3];              // L * 2^-64 (exact cutoff decisions near r_cut)
     float dtf, kTf, lambdaf, fcapf, max_dispf;

@@ -702,6 +702,19 @@ AZP_D float fx_rsq(const MDArgs& a, const uint4& fi, const uint4& fj, float dx, 
 #ifndef AZP_COLLOID_GAP
 #define AZP_COLLOID_GAP 2
 #endif
+// the integer r^2, in units of (L / 2^32)^2, of the 64-bit fixed-point
+// displacement rounded to 2^-32 L per axis; exact, and below 2^62 for a pair
+// inside the half box
+AZP_D long long fx_rsq_rounded(const uint4& fi, const uint4& li, const uint4& fj, const uint4& lj)
+{
+    const auto axis = [](uint32_t hi_i, uint32_t lo_i, uint32_t hi_j, uint32_t lo_j) -> long long {
+        const unsigned long long d = (unsigned long long)fx_join(hi_i, lo_i) - (unsigned long long)fx_join(hi_j, lo_j);
+        return (long long)(d + 0x80000000ull) >> 32;
+    };
+    const long long ix = axis(fi.x, li.x, fj.x, lj.x), iy = axis(fi.y, li.y, fj.y, lj.y),
+                    iz = axis(fi.z, li.z, fj.z, lj.z);
+    return ix * ix + iy * iy + iz * iz;
+}
 template<class PE>
 AZP_D void gap_args(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t i, uint32_t j, uint32_t tp,
                     float& rsq, float& dq)
@@ -709,13 +722,7 @@ AZP_D void gap_args(const MDArgs& a, const uint4& fi, const uint4& fj, uint32_t 
     const uint4 li = __ldg(a.flo + i), lj = __ldg(a.flo + j);
 #if AZP_COLLOID_GAP == 2
     if (a.contact_q) {
-        const auto axis = [](uint32_t hi_i, uint32_t lo_i, uint32_t hi_j, uint32_t lo_j) -> long long {
-            const unsigned long long d = (unsigned long long)fx_join(hi_i, lo_i) - (unsigned long long)fx_join(hi_j, lo_j);
-            return (long long)(d + 0x80000000ull) >> 32;  // rounded to 2^-32 L
-        };
-        const long long ix = axis(fi.x, li.x, fj.x, lj.x), iy = axis(fi.y, li.y, fj.y, lj.y),
-                        iz = axis(fi.z, li.z, fj.z, lj.z);
-        const long long q = ix * ix + iy * iy + iz * iz;
+        const long long q = fx_rsq_rounded(fi, li, fj, lj);
         const long long dqi = __ldg(a.contact_q + tp) - q;
         const float qf = __ll2float_rn(q), df = __ll2float_rn(dqi);
         rsq = fmaf(qf, a.s2h, qf * a.s2l);
@@ -833,6 +840,27 @@ AZP_D void pair_term_dpd_fx(const MDArgs& a, const uint4& fi, const uint4& fj, u
     if (!(rc2 > 0.0f) || rs >= rc2 * 1.000004f) return;
     const float4 vj = reinterpret_cast<const float4*>(a.dvel)[j];
     const uint32_t tgj = a.tag[j];
+    if (rs >= rc2 * 0.998f && a.contact_q) {
+        // within 0.2 % of r_cut^2 in a cubic box: the cutoff decided and 1 - r / r_cut
+        // formed from the exact integer difference r_cut^2 - r^2, the rest in FP32
+        const long long q = fx_rsq_rounded(fi, a.flo[i], fj, a.flo[j]);
+        const long long dqi = __ldg(a.contact_q + tp) - q;
+        if (dqi <= 0) return;
+        const float qf = __ll2float_rn(q), df = __ll2float_rn(dqi);
+        const float r2 = fmaf(qf, a.s2h, qf * a.s2l), dq = fmaf(df, a.s2h, df * a.s2l);
+        const float rcinv = rec[0], rc = rec[1], A = rec[2];
+        const float rinv = rsqrtf(r2);
+        const float x = dq * rcinv / (rc + r2 * rinv);  // 1 - r / r_cut = (r_cut^2 - r^2) / (r_cut (r_cut + r))
+        const float dot = dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z);
+        const float fc = A * x * rinv;
+        const float wR = dpd_weight_engine_f(x, rec[4]) * rinv;
+        const Philox4 ph = philox4x32_10(0u, min(tgi, tgj), max(tgi, tgj), 0u, k0, k1);
+        const float alpha = -1.0f + 2.0f * open01f(ph.v[0]);
+        const float fdr = fc - rec[3] * wR * wR * dot + rec[5] * wR * alpha;
+        const float e = A * rc * x - 0.5f * A * rcinv * dq;
+        acc.add_split(dx, dy, dz, fdr, fc, e, vir);
+        return;
+    }
     if (rs >= rc2 * 0.998f) {
         const uint4 li = a.flo[i], lj = a.flo[j];
         const double ddx = min_image1(fx_to_double(fx_join(fi.x, li.x), a.l64[0]) - fx_to_double(fx_join(fj.x, lj.x), a.l64[0]),
