@@ -40,6 +40,7 @@ struct DpdArgs {
     uint32_t N, ntypes;
     double L[3], Linv[3];
     float sfix[3];
+    float s2h, s2l;       // (L / 2^32)^2 as a float pair (cubic boxes)
     const uint32_t* counts;
     const uint32_t* nbrs;
     uint32_t max_nn;
@@ -50,8 +51,10 @@ struct DpdArgs {
     uint32_t pitch;
 };
 
+// o[7]: r_cut^2 in the units of the integer r^2 of the fixed-point words,
+// (2^32 / L)^2 (u2 > 0: a cubic box), as the bits of a 64-bit integer; 0 without
 __global__ void k_dpd_table(const double* __restrict__ params, const double* __restrict__ r_cut, uint32_t nt2,
-                            double kT, double dt, double* __restrict__ out)
+                            double kT, double dt, double u2, double* __restrict__ out)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nt2) return;
@@ -66,7 +69,7 @@ __global__ void k_dpd_table(const double* __restrict__ params, const double* __r
     o[4] = gamma;
     o[5] = 0.5 * s;
     o[6] = sqrt(6.0 * kT * gamma / dt);
-    o[7] = 0.0;
+    o[7] = __longlong_as_double(u2 > 0.0 && r_cut[t] > 0.0 ? __double2ll_rn(rc2 * u2) : 0ll);
 }
 
 __global__ void k_vel_f(const double4_32a* __restrict__ vel, uint32_t N, float4* __restrict__ out)
@@ -302,10 +305,35 @@ __global__ void __launch_bounds__(DPD_BLOCK, std::is_same<R, float>::value ? 4 :
                 {
                     const double* c = s_tbl + tp;
                     // Near r_cut the random weight (1 - r / r_cut)^(s/2) is steep
-                    // (infinitely so at r_cut for s < 2): an FP32 or fixed-point r
-                    // would cost percents of this pair's force. Such pairs (about
-                    // 0.3 % of them) are evaluated in FP64 from the FP64 state, which
-                    // also decides the cutoff exactly as the oracle does.
+                    // (infinitely so at r_cut for s < 2): 1 - r / r_cut formed from a
+                    // rounded FP32 r would cost percents of this pair's force. In a
+                    // cubic box it comes from the exact integer difference
+                    // r_cut^2 - r^2 of the fixed-point words, which also decides the
+                    // cutoff; the rest of the pair in FP32.
+                    const long long rcq = __double_as_longlong(c[7]);
+                    if (rcq > 0) {
+                        const long long ix = (int32_t)(fi.x - fj.x), iy = (int32_t)(fi.y - fj.y),
+                                        iz = (int32_t)(fi.z - fj.z);
+                        const long long qq = ix * ix + iy * iy + iz * iz;
+                        const long long dqi = rcq - qq;
+                        if (dqi > 0) {
+                            const float qf = __ll2float_rn(qq), df = __ll2float_rn(dqi);
+                            const float r2 = fmaf(qf, a.s2h, qf * a.s2l), dq = fmaf(df, a.s2h, df * a.s2l);
+                            const float rinv = rsqrtf(r2);
+                            const float x = dq * cf[1] / (cf[2] + r2 * rinv);  // 1 - r / r_cut
+                            const float4 vj = a.vel_f[j];
+                            const float dot = dx * (vi.x - vj.x) + dy * (vi.y - vj.y) + dz * (vi.z - vj.z);
+                            const float fc = cf[3] * x * rinv;
+                            const float wR = dpd_weight_f(x, cf[5]) * rinv;
+                            const float alpha = dpd_alpha_f(a.k0, a.k1, tgi, a.tag[j]);
+                            const float fdr = fc - cf[4] * wR * wR * dot + cf[6] * wR * alpha;
+                            const float e = cf[3] * cf[2] * x - 0.5f * cf[3] * cf[1] * dq;
+                            acc.add(dx, dy, dz, fdr, fc, e);
+                        }
+                        continue;
+                    }
+                    // other boxes: such pairs (about 0.3 % of them) in FP64 from the
+                    // FP64 state, which also decides the cutoff as the oracle does
                     double ddx, ddy, ddz, dfdr, dfc, de;
                     if (dpd_pair_fp64(a, c, a.pos[i], a.pos[j], a.vel[i], a.vel[j], tgi, a.tag[j], ddx, ddy, ddz, dfdr,
                                       dfc, de))
@@ -354,7 +382,9 @@ extern "C" int azp_dpd_forces(const azp_system* sys, azp_nlist* nl, const double
     if (!sys->pos || !sys->vel || !sys->tag) return AZP_ERR_INVALID;
     cudaStream_t s = as_stream(stream);
     const uint32_t nt2 = sys->ntypes * sys->ntypes;
-    k_dpd_table<<<(nt2 + 63) / 64, 64, 0, s>>>(params, r_cut, nt2, kT, dt, nl->dpd_table);
+    const bool cubic = sys->box.L[0] == sys->box.L[1] && sys->box.L[1] == sys->box.L[2];
+    const double u = 4294967296.0 / sys->box.L[0];
+    k_dpd_table<<<(nt2 + 63) / 64, 64, 0, s>>>(params, r_cut, nt2, kT, dt, cubic ? u * u : 0.0, nl->dpd_table);
     DpdArgs a;
     a.pos = reinterpret_cast<const double4_32a*>(sys->pos);
     a.vel = reinterpret_cast<const double4_32a*>(sys->vel);
@@ -367,6 +397,11 @@ extern "C" int azp_dpd_forces(const azp_system* sys, azp_nlist* nl, const double
         a.L[d] = sys->box.L[d];
         a.Linv[d] = 1.0 / sys->box.L[d];
         a.sfix[d] = (float)(sys->box.L[d] * 2.3283064365386963e-10);
+    }
+    {
+        const double q = sys->box.L[0] * 2.3283064365386963e-10, q2 = q * q;
+        a.s2h = (float)q2;
+        a.s2l = (float)(q2 - (double)a.s2h);
     }
     a.counts = nl->counts;
     a.nbrs = nl->nbrs;

@@ -71,6 +71,20 @@ def test_multitype_and_exclusions(orc):
     np.testing.assert_array_equal(i, io)
 
 
+@pytest.mark.parametrize("seed", [6, 7])
+def test_disparate_cutoffs_subdivided_grid(orc, seed):
+    """List radii 1.2 and 4.6 (ratio above 3): the grid is cut to cells of a third
+    of the largest radius with a stencil of three cells each way; the sets stay
+    those of the brute-force oracle."""
+    snap = random_fluid(6000, 0.5, seed=seed, ntypes=2, min_dist=0.6)
+    rc = np.array([[0.8, 3.0], [3.0, 4.2]])
+    s, i = _gpu_list(snap, rc, 0.4, max_neighbors=256)
+    rl = (rc + 0.4) ** 2
+    so, io = orc.nlist(pos4_of(snap), snap.particles.typeid, 2, box_of(snap), rl, method="brute")
+    np.testing.assert_array_equal(s, so)
+    np.testing.assert_array_equal(i, io)
+
+
 def test_thin_box_and_overflow_regrow(orc):
     import azplugins_gb300 as az
 
