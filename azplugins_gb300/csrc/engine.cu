@@ -1599,9 +1599,15 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
         CTRY(cudaMemcpy(m->d_wall_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
         m->wall_kind = c->wall_kind;
         if (m->precision == AZP_FP32) ALLOC(m->d_wall_f, N);
-        // the FP32 screen's positions are good to a few L 2^-24 (hi word, float scale)
+        // the FP32 screen's positions are good to a few L 2^-24 (hi word, float
+        // scale); the float distances to the walls to 64 units of 2^-24 of
+        // |x|_1 (at most |L|_1 / 2) + the walls' extent + the reach
+        double reach_max = 0.0;
+        for (uint32_t t = 0; t < c->ntypes; ++t) reach_max = std::max(reach_max, tab[WALL_TAB * t + 6]);
         const double Lmax = std::max(m->box.L[0], std::max(m->box.L[1], m->box.L[2]));
-        m->wall_tol = (float)(4e-6 * Lmax + 1e-5);
+        const double L1 = m->box.L[0] + m->box.L[1] + m->box.L[2];
+        m->wall_tol = (float)std::max(4e-6 * Lmax + 1e-5,
+                                      0x1p-18 * (0.5 * L1 + (double)wall_field_extent(wf) + reach_max) + 1e-5);
     }
     CTRY(cudaStreamCreateWithFlags(&m->graph_stream, cudaStreamNonBlocking));
 #undef ALLOC

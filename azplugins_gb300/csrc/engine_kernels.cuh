@@ -279,31 +279,7 @@ AZP_D bool walls_near_f(const WallField* __restrict__ wf, const double* __restri
                         float y, float z, float tol)
 {
     const double* row = tab + (size_t)t * WALL_TAB;
-    const float reach = (float)row[6] + tol;
-    const bool extrap = row[5] > 0.0;
-    for (int k = 0; k < wf->ns; ++k) {
-        const WallSphereD& w = wf->s[k];
-        const float dx = x - (float)w.o[0], dy = y - (float)w.o[1], dz = z - (float)w.o[2];
-        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-        const float d = w.inside ? (float)w.r - r : r - (float)w.r;
-        if (d < reach && (extrap || d > -tol)) return true;
-    }
-    for (int k = 0; k < wf->nc; ++k) {
-        const WallCylinderD& w = wf->c[k];
-        const float dx = x - (float)w.o[0], dy = y - (float)w.o[1], dz = z - (float)w.o[2];
-        const float al = dx * (float)w.ax[0] + dy * (float)w.ax[1] + dz * (float)w.ax[2];
-        const float px = dx - al * (float)w.ax[0], py = dy - al * (float)w.ax[1], pz = dz - al * (float)w.ax[2];
-        const float r = sqrtf(px * px + py * py + pz * pz);
-        const float d = w.inside ? (float)w.r - r : r - (float)w.r;
-        if (d < reach && (extrap || d > -tol)) return true;
-    }
-    for (int k = 0; k < wf->np; ++k) {
-        const WallPlaneD& w = wf->p[k];
-        const float d = (x - (float)w.o[0]) * (float)w.n[0] + (y - (float)w.o[1]) * (float)w.n[1] +
-                        (z - (float)w.o[2]) * (float)w.n[2];
-        if (d < reach && (extrap || d > -tol)) return true;
-    }
-    return false;
+    return walls_near(*wf, (float)row[6] + tol, row[5] > 0.0, x, y, z, tol);
 }
 
 // |fixed - fixed at the last build|^2 > threshold, in FP32 on exact integer differences

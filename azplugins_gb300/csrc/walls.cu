@@ -27,81 +27,167 @@ AZP_D void load_wall_record(const double* __restrict__ params, uint32_t t, int s
     for (int k = 0; k < 4; ++k) p[k] = k < stride ? __ldg(params + (size_t)t * stride + k) : 0.0;
 }
 
+// A block's chunk (reps x kBlock particles from base) in two passes: every
+// thread screens its particles in FP32 (walls_near) and writes the outputs of
+// the far ones at once (force, energy and virial of a particle no wall reaches:
+// the same zeros, signs included, as the full evaluation gives), listing the near
+// ones in shared memory; then the block's threads share out the list for the
+// full evaluation. A warp's lanes so all work on particles some wall may reach,
+// in whatever order the caller keeps its particles.
+template<class Screen, class Eval>
+AZP_D void screened_chunk(uint32_t N, uint32_t reps, uint32_t* s_list, Screen screen, Eval eval)
+{
+    __shared__ uint32_t s_n;
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u, chunk = reps * kBlock;
+    const uint32_t base = blockIdx.x * chunk;
+    for (uint32_t k = threadIdx.x; k < chunk; k += kBlock) {
+        const uint32_t i = base + k;
+        const bool nr = i < N && screen(i);
+        const unsigned m = __ballot_sync(0xffffffffu, nr);
+        uint32_t at = 0;
+        if (lane == 0 && m) at = atomicAdd(&s_n, (uint32_t)__popc(m));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (nr) s_list[at + __popc(m & ((1u << lane) - 1u))] = i;
+    }
+    __syncthreads();
+    const uint32_t n = s_n;
+    for (uint32_t k = threadIdx.x; k < n; k += kBlock) eval(s_list[k]);
+}
+
+// the screen's reach of a type: max(|r_cut|, r_extrap) (a NaN of either drops
+// out, as it does from the evaluation)
+AZP_D float type_reach(const double* r_cut, const double* r_extrap, uint32_t t)
+{
+    return (float)fmax(fabs(__ldg(r_cut + t)), __ldg(r_extrap + t));
+}
+
 template<class EV, typename T>
 __global__ void __launch_bounds__(kBlock) k_walls(const double4_32a* __restrict__ pos,
                                                   const double* __restrict__ params, int stride,
                                                   const double* __restrict__ r_cut,
                                                   const double* __restrict__ r_extrap,
-                                                  const __grid_constant__ WallField wf, uint32_t N,
-                                                  T* __restrict__ force, T* __restrict__ virial, uint32_t pitch)
+                                                  const __grid_constant__ WallField wf, float mag, uint32_t N,
+                                                  uint32_t reps, T* __restrict__ force, T* __restrict__ virial,
+                                                  uint32_t pitch)
 {
-    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
-    if (i >= N) return;
-    const double4_32a pp = pos[i];
-    const uint32_t t = type_of(pp.w);
-    double p[4];
-    load_wall_record(params, t, stride, p);
-    const double rc = __ldg(r_cut + t);
-    const double x[3] = {pp.x, pp.y, pp.z};
-    double F[3] = {0.0, 0.0, 0.0}, U = 0.0;
-    walls_force<EV>(wf, p, rc * rc, __ldg(r_extrap + t), x, F, U);
-    if constexpr (sizeof(T) == 8)
-        reinterpret_cast<double4_32a*>(force)[i] = make_double4_32a(F[0], F[1], F[2], U);
-    else
-        reinterpret_cast<float4*>(force)[i] = make_float4((float)F[0], (float)F[1], (float)F[2], (float)U);
-    if (virial) {
-        const double v[6] = {F[0] * x[0], F[0] * x[1], F[0] * x[2], F[1] * x[1], F[1] * x[2], F[2] * x[2]};
-        for (int c = 0; c < 6; ++c) virial[(size_t)c * pitch + i] = (T)v[c];
-    }
+    extern __shared__ uint32_t s_list[];
+    auto write = [&](uint32_t i, const double* F, double U, const double* x) {
+        if constexpr (sizeof(T) == 8)
+            reinterpret_cast<double4_32a*>(force)[i] = make_double4_32a(F[0], F[1], F[2], U);
+        else
+            reinterpret_cast<float4*>(force)[i] = make_float4((float)F[0], (float)F[1], (float)F[2], (float)U);
+        if (virial) {
+            const double v[6] = {F[0] * x[0], F[0] * x[1], F[0] * x[2], F[1] * x[1], F[1] * x[2], F[2] * x[2]};
+            for (int c = 0; c < 6; ++c) virial[(size_t)c * pitch + i] = (T)v[c];
+        }
+    };
+    auto screen = [&](uint32_t i) {
+        const double4_32a pp = pos[i];
+        const uint32_t t = type_of(pp.w);
+        const double x[3] = {pp.x, pp.y, pp.z};
+        const float reach = type_reach(r_cut, r_extrap, t);
+        const float tol = walls_screen_tol(x, mag + reach);
+        if (walls_near(wf, reach + tol, __ldg(r_extrap + t) > 0.0, (float)x[0], (float)x[1], (float)x[2], tol))
+            return true;
+        const double F[3] = {0.0, 0.0, 0.0};
+        write(i, F, 0.0, x);
+        return false;
+    };
+    auto eval = [&](uint32_t i) {
+        const double4_32a pp = pos[i];
+        const uint32_t t = type_of(pp.w);
+        double p[4];
+        load_wall_record(params, t, stride, p);
+        const double rc = __ldg(r_cut + t);
+        const double x[3] = {pp.x, pp.y, pp.z};
+        double F[3] = {0.0, 0.0, 0.0}, U = 0.0;
+        walls_force<EV>(wf, p, rc * rc, __ldg(r_extrap + t), x, F, U);
+        write(i, F, U, x);
+    };
+    screened_chunk(N, reps, s_list, screen, eval);
 }
 
 // FP32 output: FP32 arithmetic with the FP64 parts that cancellation needs
-// (walls.cuh), per-type float records made once per block in shared memory
+// (walls.cuh), per-type float records and reaches made once per block in shared
+// memory
 template<class EV, class EVF>
 __global__ void __launch_bounds__(kBlock) k_walls_f(const double4_32a* __restrict__ pos,
                                                     const double* __restrict__ params, int stride,
                                                     const double* __restrict__ r_cut,
                                                     const double* __restrict__ r_extrap, uint32_t ntypes,
-                                                    const __grid_constant__ WallField wf, uint32_t N,
-                                                    float* __restrict__ force,
+                                                    const __grid_constant__ WallField wf, float mag, uint32_t N,
+                                                    uint32_t reps, float* __restrict__ force,
                                                     float* __restrict__ virial, uint32_t pitch)
 {
     extern __shared__ float s_q[];
+    float* s_reach = s_q + (size_t)ntypes * WALL_F;
+    uint32_t* s_list = reinterpret_cast<uint32_t*>(s_reach + ntypes);
     for (uint32_t t = threadIdx.x; t < ntypes; t += kBlock) {
         double p[4];
         load_wall_record(params, t, stride, p);
         wall_record_f<EV>(p, r_cut[t], r_extrap[t], s_q + (size_t)t * WALL_F);
+        s_reach[t] = type_reach(r_cut, r_extrap, t);
     }
     __syncthreads();
-    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
-    if (i >= N) return;
-    const double4_32a pp = pos[i];
-    const double x[3] = {pp.x, pp.y, pp.z};
-    float F[3] = {0.0f, 0.0f, 0.0f}, U = 0.0f;
-    walls_force_f<EVF>(wf, s_q + (size_t)type_of(pp.w) * WALL_F, x, F, U);
-    reinterpret_cast<float4*>(force)[i] = make_float4(F[0], F[1], F[2], U);
-    if (virial) {
-        const float xf = (float)x[0], yf = (float)x[1], zf = (float)x[2];
-        const float v[6] = {F[0] * xf, F[0] * yf, F[0] * zf, F[1] * yf, F[1] * zf, F[2] * zf};
-        for (int c = 0; c < 6; ++c) virial[(size_t)c * pitch + i] = v[c];
-    }
+    auto write = [&](uint32_t i, const float* F, float U, const double* x) {
+        reinterpret_cast<float4*>(force)[i] = make_float4(F[0], F[1], F[2], U);
+        if (virial) {
+            const float xf = (float)x[0], yf = (float)x[1], zf = (float)x[2];
+            const float v[6] = {F[0] * xf, F[0] * yf, F[0] * zf, F[1] * yf, F[1] * zf, F[2] * zf};
+            for (int c = 0; c < 6; ++c) virial[(size_t)c * pitch + i] = v[c];
+        }
+    };
+    auto screen = [&](uint32_t i) {
+        const double4_32a pp = pos[i];
+        const uint32_t t = type_of(pp.w);
+        const double x[3] = {pp.x, pp.y, pp.z};
+        const float reach = s_reach[t];
+        const float tol = walls_screen_tol(x, mag + reach);
+        if (walls_near(wf, reach + tol, s_q[(size_t)t * WALL_F + 7] > 0.0f, (float)x[0], (float)x[1], (float)x[2],
+                       tol))
+            return true;
+        const float F[3] = {0.0f, 0.0f, 0.0f};
+        write(i, F, 0.0f, x);
+        return false;
+    };
+    auto eval = [&](uint32_t i) {
+        const double4_32a pp = pos[i];
+        const double x[3] = {pp.x, pp.y, pp.z};
+        float F[3] = {0.0f, 0.0f, 0.0f}, U = 0.0f;
+        walls_force_f<EVF>(wf, s_q + (size_t)type_of(pp.w) * WALL_F, x, F, U);
+        write(i, F, U, x);
+    };
+    screened_chunk(N, reps, s_list, screen, eval);
 }
 
 template<class EV, class EVF>
 void launch_walls(const azp_system* sys, const double* params, int stride, const double* r_cut,
                   const double* r_extrap, const WallField& wf, const azp_forces* out, cudaStream_t s)
 {
-    const uint32_t grid = (sys->N + kBlock - 1) / kBlock;
+    // chunks of reps x kBlock particles: about eight blocks per SM, at least one
+    // warp's worth of particles per thread-block pass
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t per_block = (uint64_t)sys->N / ((uint64_t)8 * (uint64_t)sms * kBlock);
+    const uint32_t reps = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(per_block, 1), 16);
+    const uint32_t chunk = reps * kBlock;
+    const uint32_t grid = (uint32_t)(((uint64_t)sys->N + chunk - 1) / chunk);
     const uint32_t pitch = out->virial_pitch ? out->virial_pitch : sys->N;
     const auto* pos = reinterpret_cast<const double4_32a*>(sys->pos);
+    const float mag = wall_field_extent(wf);
+    const size_t smem_f = sizeof(float) * (WALL_F + 1) * sys->ntypes + sizeof(uint32_t) * chunk;
+    if (out->precision == AZP_FP32 && smem_f > 48 * 1024)
+        cudaFuncSetAttribute(k_walls_f<EV, EVF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
     if (out->precision == AZP_FP64)
-        k_walls<EV, double><<<grid, kBlock, 0, s>>>(pos, params, stride, r_cut, r_extrap, wf, sys->N,
-                                                    static_cast<double*>(out->force),
-                                                    static_cast<double*>(out->virial), pitch);
+        k_walls<EV, double><<<grid, kBlock, sizeof(uint32_t) * chunk, s>>>(
+            pos, params, stride, r_cut, r_extrap, wf, mag, sys->N, reps, static_cast<double*>(out->force),
+            static_cast<double*>(out->virial), pitch);
     else
-        k_walls_f<EV, EVF><<<grid, kBlock, sizeof(float) * WALL_F * sys->ntypes, s>>>(
-            pos, params, stride, r_cut, r_extrap, sys->ntypes, wf, sys->N, static_cast<float*>(out->force),
-            static_cast<float*>(out->virial), pitch);
+        k_walls_f<EV, EVF><<<grid, kBlock, smem_f, s>>>(pos, params, stride, r_cut, r_extrap, sys->ntypes, wf, mag, sys->N, reps,
+                                  static_cast<float*>(out->force), static_cast<float*>(out->virial), pitch);
 }
 
 bool unit(const double* v, double* u)
@@ -112,6 +198,17 @@ bool unit(const double* v, double* u)
     return true;
 }
 }  // namespace
+
+float wall_field_extent(const WallField& wf)
+{
+    double m = 0.0;
+    auto l1 = [](const double* o) { return std::fabs(o[0]) + std::fabs(o[1]) + std::fabs(o[2]); };
+    for (int k = 0; k < wf.ns; ++k) m = std::max(m, l1(wf.s[k].o) + std::fabs(wf.s[k].r));
+    for (int k = 0; k < wf.nc; ++k) m = std::max(m, l1(wf.c[k].o) + std::fabs(wf.c[k].r));
+    for (int k = 0; k < wf.np; ++k) m = std::max(m, l1(wf.p[k].o));
+    // a field beyond float range screens nothing out (the tolerance goes infinite)
+    return m < 1.0e37 ? (float)m : INFINITY;
+}
 
 int make_wall_field(const azp_walls* w, WallField* out)
 {

@@ -227,6 +227,55 @@ AZP_HD void walls_force(const WallField& wf, const double* p, double rcutsq, dou
     }
 }
 
+// ---------------------------------------------------------------- FP32 screen
+// True when some wall may act on a particle at (x, y, z): its float distance d
+// to a wall, positive on the active side, lies below reach (= max(r_cut,
+// r_extrap) + tol) and, without extrapolation, above -tol. tol bounds the float
+// error of d, so a false answer is exact: walls_force would add nothing (the
+// reach test covers both branches of wall_apply, the sign test its inside flag).
+#ifdef __CUDACC__
+__device__ __forceinline__ bool walls_near(const WallField& wf, float reach, bool extrap, float x, float y, float z,
+                                           float tol)
+{
+    for (int k = 0; k < wf.ns; ++k) {
+        const WallSphereD& w = wf.s[k];
+        const float dx = x - (float)w.o[0], dy = y - (float)w.o[1], dz = z - (float)w.o[2];
+        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float d = w.inside ? (float)w.r - r : r - (float)w.r;
+        if (d < reach && (extrap || d > -tol)) return true;
+    }
+    for (int k = 0; k < wf.nc; ++k) {
+        const WallCylinderD& w = wf.c[k];
+        const float dx = x - (float)w.o[0], dy = y - (float)w.o[1], dz = z - (float)w.o[2];
+        const float al = dx * (float)w.ax[0] + dy * (float)w.ax[1] + dz * (float)w.ax[2];
+        const float px = dx - al * (float)w.ax[0], py = dy - al * (float)w.ax[1], pz = dz - al * (float)w.ax[2];
+        const float r = sqrtf(px * px + py * py + pz * pz);
+        const float d = w.inside ? (float)w.r - r : r - (float)w.r;
+        if (d < reach && (extrap || d > -tol)) return true;
+    }
+    for (int k = 0; k < wf.np; ++k) {
+        const WallPlaneD& w = wf.p[k];
+        const float d = (x - (float)w.o[0]) * (float)w.n[0] + (y - (float)w.o[1]) * (float)w.n[1] +
+                        (z - (float)w.o[2]) * (float)w.n[2];
+        if (d < reach && (extrap || d > -tol)) return true;
+    }
+    return false;
+}
+
+// The screen's tolerance for a caller's FP64 position x: the float rounding of
+// x, of the wall origins, radii, axes and normals, and of the few operations
+// between them stays below 64 units of 2^-24 of |x|_1 + mag, where mag is the
+// largest |origin|_1 + radius over the walls plus the type's reach (a bound
+// with room to spare: the cylinder's projection, the longest chain, needs about
+// 40 such units). A position whose float magnitude is not finite gets an
+// infinite tolerance, so that the screen passes it on to the FP64 evaluation.
+__device__ __forceinline__ float walls_screen_tol(const double* x, float mag)
+{
+    const float m = fabsf((float)x[0]) + fabsf((float)x[1]) + fabsf((float)x[2]);
+    return m < 1.0e37f ? 0x1p-18f * (m + mag) + 1.0e-30f : INFINITY;
+}
+#endif
+
 // ---------------------------------------------------------------- FP32 path
 // Per-type float record of the FP32 driver, made once per block from the FP64
 // evaluator: q[0..2] the evaluator's constants (LJ93: lj1 = 2/15 A sigma^9,
@@ -410,5 +459,9 @@ AZP_D void walls_force_f(const WallField& wf, const float* q, const double* x, f
 // host: the C-ABI wall list as a WallField (axes and normals normalised, as
 // HOOMD's wall constructors do); AZP_ERR_INVALID on a bad wall or count
 int make_wall_field(const azp_walls* walls, WallField* out);
+
+// host: the largest |origin|_1 + |radius| over the field's walls (the wall part
+// of the FP32 screen's tolerance)
+float wall_field_extent(const WallField& wf);
 
 }  // namespace azp

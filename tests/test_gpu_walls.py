@@ -66,11 +66,6 @@ def _walls_zoo():
 
 @pytest.mark.parametrize("name", ["LJ93", "Colloid"])
 def test_driver_matches_oracle(orc, name):
-    import torch
-
-    from azplugins_gb300 import _lib
-
-    Lib = _lib.load()
     rng = np.random.Generator(np.random.PCG64(81))
     N = 30011
     L = np.array([20.0, 20.0, 20.0])
@@ -97,35 +92,129 @@ def test_driver_matches_oracle(orc, name):
             break
         pos[bad] = rng.uniform(-0.5, 0.5, size=(bad.sum(), 3)) * L
     assert not bad.any() and (np.abs(U) > 0).sum() > 1000
-    dpos = torch.zeros((N, 4), dtype=torch.float64, device="cuda")
-    dpos[:, :3] = torch.from_numpy(pos).cuda()
-    dpos.view(torch.int64)[:, 3] = torch.from_numpy(types.astype(np.int64)).cuda()
-    s = _lib.System()
-    s.N, s.ntypes, s.pos = N, 3, dpos.data_ptr()
-    for d in range(3):
-        s.box.L[d] = L[d]
-    dev = [torch.from_numpy(np.ascontiguousarray(a).reshape(-1).copy()).cuda() for a in (rec, rc, rx)]
-    walls, keep = pot._walls_struct()
-    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     # FP64: the Colloid form subtracts two large terms near the surface, so FMA
     # contraction differences show at 1e-12; LJ93 stays within 1e-12. FP32: FP32
     # arithmetic on FP64 distances (the pair driver's FP32 bound)
     tol64 = 1e-12 if name == "LJ93" else 1e-11
-    for prec, dt, tol in ((_lib.FP64, torch.float64, tol64), (_lib.FP32, torch.float32, 1e-5)):
-        force = torch.full((N, 4), float("nan"), dtype=dt, device="cuda")
-        vir = torch.full((6, N), float("nan"), dtype=dt, device="cuda")
-        out = _lib.Forces()
-        out.force, out.virial, out.virial_pitch, out.precision = force.data_ptr(), vir.data_ptr(), N, prec
-        _lib.check(Lib.azp_wall_forces(ctypes.byref(s), pot.kind, ctypes.byref(walls), dev[0].data_ptr(),
-                                       dev[1].data_ptr(), dev[2].data_ptr(), ctypes.byref(out), stream),
-                   "azp_wall_forces")
-        torch.cuda.synchronize()
-        f = force.double().cpu().numpy()
-        w = vir.double().cpu().numpy().T
+    for prec, tol in (("fp64", tol64), ("fp32", 1e-5)):
+        f, w = _driver_forces(pot, (rec, rc, rx), pos, types, L, prec)
         assert force_error(f, F) < tol
         assert np.abs(f[:, 3] - U).max() <= tol * max(np.abs(U).max(), 1.0)
         assert np.abs(w - W).max() <= tol * max(np.abs(W).max(), 1.0)
+
+
+def _driver_forces(pot, tables, pos, types, L, prec):
+    """azp_wall_forces on the GPU: forces + energies [N, 4] and virials [N, 6]
+    (outputs filled with NaN beforehand, so that a particle left unwritten shows)."""
+    import torch
+
+    from azplugins_gb300 import _lib
+
+    Lib = _lib.load()
+    N = len(pos)
+    ntypes = len(tables[1])
+    dpos = torch.zeros((N, 4), dtype=torch.float64, device="cuda")
+    dpos[:, :3] = torch.from_numpy(np.ascontiguousarray(pos)).cuda()
+    dpos.view(torch.int64)[:, 3] = torch.from_numpy(types.astype(np.int64)).cuda()
+    s = _lib.System()
+    s.N, s.ntypes, s.pos = N, ntypes, dpos.data_ptr()
+    for d in range(3):
+        s.box.L[d] = L[d]
+    dev = [torch.from_numpy(np.ascontiguousarray(a).reshape(-1).copy()).cuda() for a in tables]
+    walls, keep = pot._walls_struct()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    dt = torch.float64 if prec == "fp64" else torch.float32
+    force = torch.full((N, 4), float("nan"), dtype=dt, device="cuda")
+    vir = torch.full((6, N), float("nan"), dtype=dt, device="cuda")
+    out = _lib.Forces()
+    out.force, out.virial, out.virial_pitch = force.data_ptr(), vir.data_ptr(), N
+    out.precision = _lib.FP64 if prec == "fp64" else _lib.FP32
+    _lib.check(Lib.azp_wall_forces(ctypes.byref(s), pot.kind, ctypes.byref(walls), dev[0].data_ptr(),
+                                   dev[1].data_ptr(), dev[2].data_ptr(), ctypes.byref(out), stream),
+               "azp_wall_forces")
+    torch.cuda.synchronize()
     del keep
+    return force.double().cpu().numpy(), vir.double().cpu().numpy().T
+
+
+def _at_distance(rng, wall, d, L):
+    """Points at signed distance d (positive on the active side) from a wall,
+    at the wall's surface point nearest a random point of the box."""
+    q = rng.uniform(-0.5, 0.5, size=(len(d), 3)) * L
+    if isinstance(wall, az.wall.Plane):
+        o = np.asarray(wall.origin, float)
+        n = np.asarray(wall.normal, float)
+        n = n / np.linalg.norm(n)
+        return q - ((q - o) @ n)[:, None] * n + d[:, None] * n
+    o = np.asarray(wall.origin, float)
+    t = q - o
+    if isinstance(wall, az.wall.Cylinder):
+        a = np.asarray(wall.axis, float)
+        a = a / np.linalg.norm(a)
+        along = (t @ a)[:, None] * a
+        t = t - along
+    else:
+        along = 0.0
+    u = t / np.linalg.norm(t, axis=1)[:, None]
+    rad = wall.radius - d if wall.inside else wall.radius + d
+    return o + along + rad[:, None] * u
+
+
+def test_driver_screen_near_cutoffs(orc):
+    """The driver screens particles in FP32 and evaluates in full only those some
+    wall may reach: particles within 1e-9 relative of every cutoff and every
+    extrapolation distance of walls whose origins lie far outside the box (the
+    screen's tolerance grows with them), on both sides of each surface. Every
+    particle the oracle gives a force or energy gets one, the others exact zeros;
+    FP64 within 5e-11 of the oracle (surfaces of radius 300 and 490 leave the
+    distance to the wall, a difference of two numbers near the radius, with a
+    rounding of radius x 2^-53 that differs between the GPU's contracted FMAs and
+    the oracle's separate roundings, and the steep LJ93 form near the surface
+    multiplies it: 5.5e-12 measured), FP32 within 1e-5."""
+    rng = np.random.Generator(np.random.PCG64(29))
+    L = np.array([40.0, 40.0, 40.0])
+    walls = [
+        az.wall.Sphere(radius=490.0, origin=(500.0, 0.0, 0.0), inside=False),
+        az.wall.Sphere(radius=12.0, origin=(0.0, 0.0, 0.0), inside=True),
+        az.wall.Cylinder(radius=300.0, axis=(0.0, 0.1, 1.0), origin=(0.0, 310.0, 0.0), inside=True),
+        az.wall.Plane(origin=(1.0e4, -1.0e4, -12.0), normal=(0.0, 0.0, 1.0)),
+        az.wall.Plane(origin=(3.0, 14.0, 0.0), normal=(0.2, -1.0, 0.1)),
+    ]
+    pot = az.wall.LJ93(walls=walls)
+    pot.params["A"] = dict(A=1.0, sigma=1.0, r_cut=3.0)
+    pot.params["B"] = dict(A=0.5, sigma=1.2, r_cut=2.5, r_extrap=0.8)
+    rec, rc, rx = pot._tables(["A", "B"])
+    per = 2400
+    pos, types = [], []
+    for w in walls:
+        for t, (cut, ext) in enumerate(((3.0, 0.0), (2.5, 0.8))):
+            marks = [cut, ext] if ext > 0 else [cut]
+            base = rng.choice(marks, size=per)
+            rel_off = rng.choice([-1e-9, 1e-9, -1e-7, 1e-7, -1e-4, 1e-4, -1e-2, 1e-2], size=per)
+            d = base * (1.0 + rel_off)
+            if ext > 0:  # extrapolated types: the inactive side as well
+                d[: per // 4] = -rng.uniform(0.0, 6.0, size=per // 4)
+            pos.append(_at_distance(rng, w, d, L))
+            types.append(np.full(per, t, np.int32))
+    pos.append(rng.uniform(-0.5, 0.5, size=(4000, 3)) * L)
+    types.append(rng.integers(0, 2, size=4000).astype(np.int32))
+    pos, types = np.concatenate(pos), np.concatenate(types)
+    keep = np.all(np.abs(pos) < 0.5 * L, axis=1)
+    pos, types = pos[keep], types[keep]
+    sp, cy, pl = oracle_walls(pot)
+    F, U, W = orc.wall_forces(np.concatenate([pos, types[:, None]], axis=1), types, "LJ93", rec, rc, rx, sp, cy, pl)
+    ok = (np.abs(F).max(axis=1) < 1e8) & (np.abs(U) < 1e8)
+    pos, types, F, U, W = pos[ok], types[ok], F[ok], U[ok], W[ok]
+    acted = (F != 0.0).any(axis=1) | (U != 0.0)
+    assert acted.sum() > 5000 and (~acted).sum() > 2000
+    for prec, tol in (("fp64", 5e-11), ("fp32", 1e-5)):
+        f, w = _driver_forces(pot, (rec, rc, rx), pos, types, L, prec)
+        assert force_error(f, F) < tol
+        assert np.abs(f[:, 3] - U).max() <= tol * max(np.abs(U).max(), 1.0)
+        assert np.abs(w - W).max() <= tol * max(np.abs(W).max(), 1.0)
+        if prec == "fp64":
+            np.testing.assert_array_equal((f[:, :3] != 0.0).any(axis=1) | (f[:, 3] != 0.0), acted)
+        assert np.all(f[~acted] == 0.0) and np.all(w[~acted] == 0.0)
 
 
 def _slit_fluid(seed, n_xz=8, n_y=10, spacing=1.2):
