@@ -308,13 +308,44 @@ __global__ void k_state_to_fx(const double4_32a* __restrict__ pos, double4_32a* 
 // block, or a buffer off a 16-byte boundary, moves them one element at a time.
 constexpr int STATE_BLOCK = 256;
 
+template <int W, class T>
+__device__ __forceinline__ void rows_copy(T* __restrict__ dst, const T* __restrict__ src)
+{
+    static_assert(W * STATE_BLOCK * sizeof(T) % 16 == 0, "whole vectors per block");
+    constexpr int NV = W * STATE_BLOCK * (int)sizeof(T) / 16;
+    for (int k = threadIdx.x; k < NV; k += STATE_BLOCK)
+        reinterpret_cast<uint4*>(dst)[k] = reinterpret_cast<const uint4*>(src)[k];
+}
 template <class T>
 __device__ __forceinline__ void rows3_copy(T* __restrict__ dst, const T* __restrict__ src)
 {
-    static_assert(3 * STATE_BLOCK * sizeof(T) % 16 == 0, "whole vectors per block");
-    constexpr int NV = 3 * STATE_BLOCK * (int)sizeof(T) / 16;
-    for (int k = threadIdx.x; k < NV; k += STATE_BLOCK)
-        reinterpret_cast<uint4*>(dst)[k] = reinterpret_cast<const uint4*>(src)[k];
+    rows_copy<3>(dst, src);
+}
+
+// Rows of four doubles (positions, velocities) of tag t. A full block goes
+// through shared memory (`full`, uniform over the block), so that it reads or
+// writes the caller's buffer as one contiguous run of 16-byte vectors, a warp
+// covering whole 128-byte lines per access: over the host link that moves a
+// pinned buffer in place at the link's rate (two 16-byte accesses per lane at a
+// 32-byte stride cover half of each line apiece, and wrote at about half of it).
+__device__ __forceinline__ void put_row4(double* __restrict__ out, double* s, uint32_t t, bool full, double a,
+                                         double b, double c, double d)
+{
+    if (full) {
+        reinterpret_cast<double2*>(s)[2 * threadIdx.x] = make_double2(a, b);
+        reinterpret_cast<double2*>(s)[2 * threadIdx.x + 1] = make_double2(c, d);
+    } else {
+        reinterpret_cast<double2*>(out)[2 * (size_t)t] = make_double2(a, b);
+        reinterpret_cast<double2*>(out)[2 * (size_t)t + 1] = make_double2(c, d);
+    }
+}
+__device__ __forceinline__ void get_row4(const double* __restrict__ in, const double* s, uint32_t t, bool full,
+                                         double2& ab, double2& cd)
+{
+    const double2* src = full ? reinterpret_cast<const double2*>(s) + 2 * threadIdx.x
+                              : reinterpret_cast<const double2*>(in) + 2 * (size_t)t;
+    ab = src[0];
+    cd = src[1];
 }
 
 // Writes particle i's rows of three (tag t, thread `lane` of the block) to the
@@ -355,27 +386,29 @@ __global__ void __launch_bounds__(STATE_BLOCK)
 {
     __shared__ __align__(16) double s_acc[3 * STATE_BLOCK];
     __shared__ __align__(16) int s_img[3 * STATE_BLOCK];
-    // one thread per tag: the outputs are written in order
+    __shared__ __align__(16) double s_pos[4 * STATE_BLOCK], s_vel[4 * STATE_BLOCK];
+    // one thread per tag: the outputs are written in order (they may be the
+    // caller's pinned buffers, written over the host link)
     const uint32_t t0 = blockIdx.x * STATE_BLOCK;
     const uint32_t t = t0 + threadIdx.x;
-    const bool live = t < N;
+    const bool live = t < N, full = t0 + STATE_BLOCK <= N, rows_vec = rows_aligned && full;
     const uint32_t i = live ? rtag[t] : 0u;
-    // 16-byte stores: the outputs may be the caller's pinned buffers, written over the host link
     if (live && pos_out) {
         const uint4 h = fix[i], l = lo[i];
-        reinterpret_cast<double2*>(pos_out)[2 * (size_t)t] =
-            make_double2(fx_to_double(fx_join(h.x, l.x), l0), fx_to_double(fx_join(h.y, l.y), l1));
-        reinterpret_cast<double2*>(pos_out)[2 * (size_t)t + 1] =
-            make_double2(fx_to_double(fx_join(h.z, l.z), l2), (double)h.w);
+        put_row4(pos_out, s_pos, t, full, fx_to_double(fx_join(h.x, l.x), l0), fx_to_double(fx_join(h.y, l.y), l1),
+                 fx_to_double(fx_join(h.z, l.z), l2), (double)h.w);
     }
     if (live && vel_out) {
         const VelFF v = vel[i];
-        reinterpret_cast<double2*>(vel_out)[2 * (size_t)t] =
-            make_double2((double)v.h.x + (double)v.l.x, (double)v.h.y + (double)v.l.y);
-        reinterpret_cast<double2*>(vel_out)[2 * (size_t)t + 1] = make_double2((double)v.h.z + (double)v.l.z, mass[i]);
+        put_row4(vel_out, s_vel, t, full, (double)v.h.x + (double)v.l.x, (double)v.h.y + (double)v.l.y,
+                 (double)v.h.z + (double)v.l.z, mass[i]);
     }
-    store_rows3(accel, image, i, t, live, rows_aligned && t0 + STATE_BLOCK <= N, s_acc, s_img, accel_out,
-                image_out, t0);
+    store_rows3(accel, image, i, t, live, rows_vec, s_acc, s_img, accel_out, image_out, t0);
+    if (full) {
+        if (!rows_vec) __syncthreads();
+        if (pos_out) rows_copy<4>(pos_out + 4 * (size_t)t0, s_pos);
+        if (vel_out) rows_copy<4>(vel_out + 4 * (size_t)t0, s_vel);
+    }
 }
 
 // accelerations a = F / m (HOOMD sets them this way before the first step)
@@ -477,6 +510,17 @@ __global__ void k_to_tag_order_i3(const int* __restrict__ src, const uint32_t* _
     dst[3 * t + 2] = src[3 * i + 2];
 }
 
+// Reads the position and velocity rows of a full block into shared memory (see
+// put_row4), followed by a barrier unless load_rows3 (rows_vec) gives one.
+__device__ __forceinline__ void load_rows4(const double* __restrict__ pos_in, const double* __restrict__ vel_in,
+                                           bool full, bool rows_vec, double* s_pos, double* s_vel, uint32_t t0)
+{
+    if (!full) return;
+    rows_copy<4>(s_pos, pos_in + 4 * (size_t)t0);
+    rows_copy<4>(s_vel, vel_in + 4 * (size_t)t0);
+    if (!rows_vec) __syncthreads();
+}
+
 // Reads the rows of three of the block's tags (see store_rows3) into shared
 // memory when `vec`; returns particle t's row values either way.
 __device__ __forceinline__ void load_rows3(const double* __restrict__ accel_in, const int* __restrict__ image_in,
@@ -505,18 +549,19 @@ __global__ void __launch_bounds__(STATE_BLOCK)
 {
     __shared__ __align__(16) double s_acc[3 * STATE_BLOCK];
     __shared__ __align__(16) int s_img[3 * STATE_BLOCK];
+    __shared__ __align__(16) double s_pos[4 * STATE_BLOCK], s_vel[4 * STATE_BLOCK];
     const uint32_t t0 = blockIdx.x * STATE_BLOCK;
     const uint32_t i = t0 + threadIdx.x;
-    const bool live = i < N;
+    const bool live = i < N, full = t0 + STATE_BLOCK <= N;
     double a[3];
     int g[3];
-    load_rows3(accel_in, image_in, i, live, rows_aligned && t0 + STATE_BLOCK <= N, s_acc, s_img, t0, a, g);
+    // the inputs may be the caller's pinned buffers, read over the host link
+    load_rows4(pos_in, vel_in, full, rows_aligned && full, s_pos, s_vel, t0);
+    load_rows3(accel_in, image_in, i, live, rows_aligned && full, s_acc, s_img, t0, a, g);
     if (!live) return;
-    // 16-byte loads: the inputs may be the caller's pinned buffers, read over the host link
-    const double2 p01 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)i];
-    const double2 p23 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)i + 1];
-    const double2 v01 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)i];
-    const double2 v23 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)i + 1];
+    double2 p01, p23, v01, v23;
+    get_row4(pos_in, s_pos, i, full, p01, p23);
+    get_row4(vel_in, s_vel, i, full, v01, v23);
     pos[i] = make_double4_32a(p01.x, p01.y, p23.x, type_as_double((uint32_t)p23.y));
     vel[i] = make_double4_32a(v01.x, v01.y, v23.x, v23.y);
     for (int d = 0; d < 3; ++d) {
@@ -540,19 +585,20 @@ __global__ void __launch_bounds__(STATE_BLOCK)
     __shared__ __align__(16) double s_acc[3 * STATE_BLOCK];
     __shared__ __align__(16) int s_img[3 * STATE_BLOCK];
     // one thread per tag: the inputs are read in order
+    __shared__ __align__(16) double s_pos[4 * STATE_BLOCK], s_vel[4 * STATE_BLOCK];
     const uint32_t t0 = blockIdx.x * STATE_BLOCK;
     const uint32_t t = t0 + threadIdx.x;
-    const bool live = t < N;
+    const bool live = t < N, full = t0 + STATE_BLOCK <= N;
     double a[3];
     int g[3];
-    load_rows3(accel_in, image_in, t, live, rows_aligned && t0 + STATE_BLOCK <= N, s_acc, s_img, t0, a, g);
+    // the inputs may be the caller's pinned buffers, read over the host link
+    load_rows4(pos_in, vel_in, full, rows_aligned && full, s_pos, s_vel, t0);
+    load_rows3(accel_in, image_in, t, live, rows_aligned && full, s_acc, s_img, t0, a, g);
     if (!live) return;
     const uint32_t i = rtag[t];
-    // 16-byte loads: the inputs may be the caller's pinned buffers, read over the host link
-    const double2 p01 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)t];
-    const double2 p23 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)t + 1];
-    const double2 v01 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)t];
-    const double2 v23 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)t + 1];
+    double2 p01, p23, v01, v23;
+    get_row4(pos_in, s_pos, t, full, p01, p23);
+    get_row4(vel_in, s_vel, t, full, v01, v23);
     pos[i] = make_double4_32a(p01.x, p01.y, p23.x, type_as_double((uint32_t)p23.y));
     vel[i] = make_double4_32a(v01.x, v01.y, v23.x, v23.y);
     for (int d = 0; d < 3; ++d) {
@@ -577,20 +623,21 @@ __global__ void __launch_bounds__(STATE_BLOCK)
 {
     __shared__ __align__(16) double s_acc[3 * STATE_BLOCK];
     __shared__ __align__(16) int s_img[3 * STATE_BLOCK];
+    __shared__ __align__(16) double s_pos[4 * STATE_BLOCK], s_vel[4 * STATE_BLOCK];
     const uint32_t t0 = blockIdx.x * STATE_BLOCK;
     const uint32_t t = t0 + threadIdx.x;
-    const bool live = t < N;
+    const bool live = t < N, full = t0 + STATE_BLOCK <= N;
     double a3[3];
     int g3[3];
-    load_rows3(accel_in, image_in, t, live, rows_aligned && t0 + STATE_BLOCK <= N, s_acc, s_img, t0, a3, g3);
+    // the inputs may be the caller's pinned buffers, read over the host link
+    load_rows4(pos_in, vel_in, full, rows_aligned && full, s_pos, s_vel, t0);
+    load_rows3(accel_in, image_in, t, live, rows_aligned && full, s_acc, s_img, t0, a3, g3);
     bool want = false;
     if (live) {
         const uint32_t i = rtag[t];
-        // 16-byte loads: the inputs may be the caller's pinned buffers, read over the host link
-        const double2 p01 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)t];
-        const double2 p23 = reinterpret_cast<const double2*>(pos_in)[2 * (size_t)t + 1];
-        const double2 v01 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)t];
-        const double2 v23 = reinterpret_cast<const double2*>(vel_in)[2 * (size_t)t + 1];
+        double2 p01, p23, v01, v23;
+        get_row4(pos_in, s_pos, t, full, p01, p23);
+        get_row4(vel_in, s_vel, t, full, v01, v23);
         uint4 h, l;
         fx_split(fx_from_double(p01.x, Li0), h.x, l.x);
         fx_split(fx_from_double(p01.y, Li1), h.y, l.y);
@@ -645,23 +692,26 @@ __global__ void __launch_bounds__(STATE_BLOCK)
 {
     __shared__ __align__(16) double s_acc[3 * STATE_BLOCK];
     __shared__ __align__(16) int s_img[3 * STATE_BLOCK];
+    __shared__ __align__(16) double s_pos[4 * STATE_BLOCK], s_vel[4 * STATE_BLOCK];
     // one thread per tag: the outputs are written in order, 16 bytes at a time
     const uint32_t t0 = blockIdx.x * STATE_BLOCK;
     const uint32_t t = t0 + threadIdx.x;
-    const bool live = t < N;
+    const bool live = t < N, full = t0 + STATE_BLOCK <= N, rows_vec = rows_aligned && full;
     const uint32_t i = live ? rtag[t] : 0u;
     if (live && pos_out) {
         const double4_32a p = pos[i];
-        reinterpret_cast<double2*>(pos_out)[2 * (size_t)t] = make_double2(p.x, p.y);
-        reinterpret_cast<double2*>(pos_out)[2 * (size_t)t + 1] = make_double2(p.z, (double)type_of(p.w));
+        put_row4(pos_out, s_pos, t, full, p.x, p.y, p.z, (double)type_of(p.w));
     }
     if (live && vel_out) {
         const double4_32a v = vel[i];
-        reinterpret_cast<double2*>(vel_out)[2 * (size_t)t] = make_double2(v.x, v.y);
-        reinterpret_cast<double2*>(vel_out)[2 * (size_t)t + 1] = make_double2(v.z, v.w);
+        put_row4(vel_out, s_vel, t, full, v.x, v.y, v.z, v.w);
     }
-    store_rows3(accel, image, i, t, live, rows_aligned && t0 + STATE_BLOCK <= N, s_acc, s_img, accel_out,
-                image_out, t0);
+    store_rows3(accel, image, i, t, live, rows_vec, s_acc, s_img, accel_out, image_out, t0);
+    if (full) {
+        if (!rows_vec) __syncthreads();
+        if (pos_out) rows_copy<4>(pos_out + 4 * (size_t)t0, s_pos);
+        if (vel_out) rows_copy<4>(vel_out + 4 * (size_t)t0, s_vel);
+    }
 }
 
 }  // namespace azp
@@ -1746,11 +1796,26 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
         AZP_CHECK_LAUNCH("k_store_state");
         return AZP_OK;
     }
+    if (!on_device) {
+        // Pinned outputs mapped into the device's address space are written in
+        // place by the store kernel, whole 128-byte lines per warp access; the
+        // others are staged on the device and copied by the copy engines.
+        auto view = [](void* h, bool vec) -> void* {
+            void* v = h ? mapped_view(h) : nullptr;
+            return v && (!vec || aligned16(v)) ? v : nullptr;
+        };
+        double* hp = (double*)view(pos, true);
+        double* hv = (double*)view(vel, true);
+        double* ha = (double*)view(accel, false);
+        int* hi = (int*)view(image, false);
+        if ((!pos || hp) && (!vel || hv) && (!accel || ha) && (!image || hi)) {
+            enqueue_store_state(m, hp, hv, ha, hi, s);
+            AZP_CHECK_LAUNCH("k_store_state");
+            AZP_CUDA_TRY(cudaStreamSynchronize(s));
+            return AZP_OK;
+        }
+    }
     const cudaMemcpyKind back = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    // Host outputs are staged on the device and copied by the copy engines: the
-    // store kernel writing pinned memory in place over the host link measured
-    // 103 GB/s at N = 1M against 165 GB/s for the staged copies (reads, in
-    // set_state, go the other way: in place is the faster there).
     int st0 = ensure_staging(m);
     if (st0) return st0;
     double* dp = pos ? m->st_pos : nullptr;

@@ -401,8 +401,11 @@ def test_state_set_denser_overflows_to_full_path(orc):
     assert force_error(f, F) < 1e-12
 
 
-def test_pinned_and_pageable_state_transfers_agree():
-    # page-locked and pageable host arrays give the same state transfers
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_pinned_and_pageable_state_transfers_agree(precision):
+    # page-locked host arrays (read and written in place by the state kernels,
+    # full blocks through shared memory, the last block of 232 particles row by
+    # row) and pageable ones (staged) give the same state transfers
     import ctypes
 
     import torch
@@ -411,7 +414,7 @@ def test_pinned_and_pageable_state_transfers_agree():
 
     snap = workloads.lj_fluid(n_side=10, density=0.8, seed=41)
     snap.particles.acceleration = np.zeros((snap.particles.N, 3))
-    sim, lj = _lj_setup(snap, precision="fp32")
+    sim, lj = _lj_setup(snap, precision=precision)
     sim.run(25)
     eng = sim._engine
     N = snap.particles.N
