@@ -1259,15 +1259,21 @@ int rebuild_if_requested(azp_md* m, cudaStream_t s)
     return AZP_OK;
 }
 
+// the status the engine's eight flag words carry
+int errors_from_flags(const azp_md* m, const uint32_t* f)
+{
+    if (f[3] > m->max_nn) return AZP_ERR_NLIST_OVERFLOW;
+    if (f[1] & AZP_EBIT_BOND) return AZP_ERR_BOND;
+    if (f[1] & AZP_EBIT_NONFINITE) return AZP_ERR_NONFINITE;
+    return AZP_OK;
+}
+
 int check_errors(azp_md* m, cudaStream_t s)
 {
     uint32_t f[8];
     AZP_CUDA_TRY(cudaMemcpyAsync(f, m->flags, sizeof(f), cudaMemcpyDeviceToHost, s));
     AZP_CUDA_TRY(cudaStreamSynchronize(s));
-    if (f[3] > m->max_nn) return AZP_ERR_NLIST_OVERFLOW;
-    if (f[1] & AZP_EBIT_BOND) return AZP_ERR_BOND;
-    if (f[1] & AZP_EBIT_NONFINITE) return AZP_ERR_NONFINITE;
-    return AZP_OK;
+    return errors_from_flags(m, f);
 }
 
 // The device address of a host buffer the GPU can read and write in place:
@@ -1717,6 +1723,7 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
     AZP_CUDA_TRY(cudaMemsetAsync(m->flags, 0, sizeof(uint32_t) * 8, s));
     int st = AZP_OK;
     bool placed = false;
+    uint32_t flags_seen[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (m->have_state) {
         // Keep the current particle order and list: load the new state in index
         // order and rebuild only if some particle lies more than r_buff / 2 from
@@ -1741,10 +1748,9 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         }
         st = rebuild_if_requested(m, s);
         if (st) return st;
-        uint32_t f3 = 0;
-        AZP_CUDA_TRY(cudaMemcpyAsync(&f3, m->flags + 3, sizeof(f3), cudaMemcpyDeviceToHost, s));
+        AZP_CUDA_TRY(cudaMemcpyAsync(flags_seen, m->flags, sizeof(flags_seen), cudaMemcpyDeviceToHost, s));
         AZP_CUDA_TRY(cudaStreamSynchronize(s));
-        placed = f3 <= m->max_nn;
+        placed = flags_seen[3] <= m->max_nn;
         if (!placed) AZP_CUDA_TRY(cudaMemsetAsync(m->flags, 0, sizeof(uint32_t) * 8, s));
     }
     if (!placed) {
@@ -1764,7 +1770,8 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         }
         if (st) return st;
     }
-    if (!accel && m->method == AZP_METHOD_LANGEVIN_FLOW) {
+    const bool forces = !accel && m->method == AZP_METHOD_LANGEVIN_FLOW;
+    if (forces) {
         // HOOMD starts a run from a = F / m when no acceleration is known
         MDArgs a = base_args(m);
         a.out = 1;
@@ -1775,6 +1782,8 @@ int azp_md_set_state(azp_md* m, const double* pos, const double* vel, const doub
         m->forces_valid = true;
     }
     m->have_state = true;
+    // an order-keeping load that enqueued nothing after its flag read has its status
+    if (placed && !forces) return errors_from_flags(m, flags_seen);
     return check_errors(m, s);
 }
 
@@ -1784,17 +1793,20 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
     if (!m || !m->have_state) return AZP_ERR_INVALID;
     cudaStream_t s = as_stream(stream);
     const uint32_t N = m->N;
-    if (timestep) {
+    // the timestep is read after the state is enqueued, so that one wait covers both
+    auto read_timestep = [&]() -> int {
+        if (!timestep) return AZP_OK;
         unsigned long long ts = 0;
         AZP_CUDA_TRY(cudaMemcpyAsync(&ts, m->d_ts, sizeof(ts), cudaMemcpyDeviceToHost, s));
         AZP_CUDA_TRY(cudaStreamSynchronize(s));
         *timestep = ts;
-    }
-    if (N == 0) return AZP_OK;
+        return AZP_OK;
+    };
+    if (N == 0) return read_timestep();
     if (on_device && aligned16(pos) && aligned16(vel)) {
         enqueue_store_state(m, pos, vel, accel, image, s);
         AZP_CHECK_LAUNCH("k_store_state");
-        return AZP_OK;
+        return read_timestep();
     }
     if (!on_device) {
         // Pinned outputs mapped into the device's address space are written in
@@ -1811,6 +1823,8 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
         if ((!pos || hp) && (!vel || hv) && (!accel || ha) && (!image || hi)) {
             enqueue_store_state(m, hp, hv, ha, hi, s);
             AZP_CHECK_LAUNCH("k_store_state");
+            const int st = read_timestep();
+            if (st) return st;
             AZP_CUDA_TRY(cudaStreamSynchronize(s));
             return AZP_OK;
         }
@@ -1828,6 +1842,8 @@ int azp_md_get_state(azp_md* m, double* pos, double* vel, double* accel, int32_t
     if (vel) AZP_CUDA_TRY(cudaMemcpyAsync(vel, dv, sizeof(double) * 4 * N, back, s));
     if (accel) AZP_CUDA_TRY(cudaMemcpyAsync(accel, da, sizeof(double) * 3 * N, back, s));
     if (image) AZP_CUDA_TRY(cudaMemcpyAsync(image, di, sizeof(int) * 3 * N, back, s));
+    const int st = read_timestep();
+    if (st) return st;
     if (!on_device) AZP_CUDA_TRY(cudaStreamSynchronize(s));
     return AZP_OK;
 }
