@@ -749,11 +749,16 @@ struct azp_md {
     int exclude_bonds = 1, use_lambda = 0, noiseless = 0, tpp = 1;
     // The particles are re-sorted into cell order at every sort_every-th list
     // build (and at every unconditional one); the builds between keep the order
-    // and scan through the cell member table. Measured on the bead-spring melt
-    // (N = 1,048,600, 2,000 steps, one GB300): every build 6,063 timesteps/s,
-    // every 4th 6,241, every 8th 6,107, every 16th 6,094 (the order drifts and
-    // the member-table scan slows).
-    uint32_t sort_every = 4;
+    // and scan through the cell member table. 0 (the default): every 4th build
+    // on a grid of few particles per cell, every build on a crowded one. Measured
+    // on one GB300: the bead-spring melt (N = 1,048,600, ~3 particles per cell,
+    // 2,000 steps) 6,063 timesteps/s re-sorting at every build, 6,241 at every
+    // 4th, 6,107 at every 8th, 6,094 at every 16th (the order drifts and the
+    // member-table scan slows); crowded grids lose instead (the LJ fluid, ~33 per
+    // cell: 12,591 -> 11,714 at every 4th; the colloid mixture, ~119 per cell:
+    // 1,114 -> 1,081), where a candidate's extra indirection costs more than
+    // the re-sort saves.
+    uint32_t sort_every = 0;
     // [sort, 0, keep, 0]: gates of the two kinds of build; [4]: order-keeping
     // builds since the last re-sort (kept across loaded states, unlike flags)
     uint32_t* sort_gate = nullptr;
@@ -1049,8 +1054,9 @@ int enqueue_rebuild(azp_md* m, cudaStream_t s, const uint32_t* gate, bool force_
     if (st) return st;
     launch_cell_scatter(m->cell_of, m->slot, m->cell_start, m->members, N, m->grid.ncell, s, gate);
     // shared-memory tiles need the cell order at every build
-    const int force = force_sort || m->sort_every <= 1 || m->tile_tab != nullptr;
-    k_sort_decide<<<1, 1, 0, s>>>(gate, m->sort_every, force, m->sort_gate);
+    const uint32_t every = m->sort_every ? m->sort_every : (crowded_grid(N, m->grid.ncell) ? 1u : 4u);
+    const int force = force_sort || every <= 1 || m->tile_tab != nullptr;
+    k_sort_decide<<<1, 1, 0, s>>>(gate, every, force, m->sort_gate);
     const uint32_t* g_sort = m->sort_gate;
     const uint32_t* g_keep = m->sort_gate + 2;
     PermArgs p;
@@ -1488,8 +1494,7 @@ azp_md* azp_md_create(const azp_md_config* c, int* status)
     const char* env_graph = std::getenv("AZP_GRAPHS");
     m->use_graphs = !(env_graph && env_graph[0] == '0');
     const char* env_sort = std::getenv("AZP_SORT_EVERY");
-    const int sort_every = env_sort ? std::atoi(env_sort) : (int)m->sort_every;
-    m->sort_every = (uint32_t)std::max(1, std::min(sort_every, 1 << 20));
+    if (env_sort) m->sort_every = (uint32_t)std::max(1, std::min(std::atoi(env_sort), 1 << 20));
 
     const uint32_t N = c->N;
     int st = AZP_OK;
