@@ -750,14 +750,15 @@ struct azp_md {
     // The particles are re-sorted into cell order at every sort_every-th list
     // build (and at every unconditional one); the builds between keep the order
     // and scan through the cell member table. 0 (the default): every 4th build
-    // on a grid of few particles per cell and a 27-cell stencil, every build
-    // otherwise. Measured on one GB300: the bead-spring melt (N = 1,048,600, ~3
-    // particles per cell, 2,000 steps) 6,063 timesteps/s re-sorting at every
-    // build, 6,241 at every 4th, 6,107 at every 8th, 6,094 at every 16th (the
-    // order drifts and the member-table scan slows); the others lose instead (the
-    // LJ fluid, ~33 particles per cell: 12,591 -> 11,714 at every 4th; the colloid
-    // mixture, ~4 per cell of a subdivided grid with a 343-cell stencil: 1,114 ->
-    // 1,081), where drifted lanes scan more divergent rows than the re-sort costs.
+    // on a grid of at most 4 particles per cell and a 27-cell stencil, every
+    // build otherwise. Measured on one GB300: the bead-spring melt (N =
+    // 1,048,600, ~3 particles per cell, 2,000 steps) 6,063 timesteps/s
+    // re-sorting at every build, 6,241 at every 4th, 6,107 at every 8th, 6,094 at
+    // every 16th (the order drifts and the member-table scan slows); the others
+    // lose instead, where drifted lanes scan more divergent rows than the re-sort
+    // costs: the LJ fluid (~33 particles per cell) 12,591 -> 11,714 at every 4th,
+    // the DPD fluid (~6.6) 0.612 -> 0.641 ms per step, the colloid mixture (~4
+    // per cell of a subdivided grid with a 343-cell stencil) 1,114 -> 1,081.
     uint32_t sort_every = 0;
     // [sort, 0, keep, 0]: gates of the two kinds of build; [4]: order-keeping
     // builds since the last re-sort (kept across loaded states, unlike flags)
@@ -1054,7 +1055,7 @@ int enqueue_rebuild(azp_md* m, cudaStream_t s, const uint32_t* gate, bool force_
     if (st) return st;
     launch_cell_scatter(m->cell_of, m->slot, m->cell_start, m->members, N, m->grid.ncell, s, gate);
     // shared-memory tiles need the cell order at every build
-    const bool sparse = !crowded_grid(N, m->grid.ncell) && m->grid.reach[0] <= 1 && m->grid.reach[1] <= 1 &&
+    const bool sparse = (uint64_t)N <= 4ull * m->grid.ncell && m->grid.reach[0] <= 1 && m->grid.reach[1] <= 1 &&
                         m->grid.reach[2] <= 1;
     const uint32_t every = m->sort_every ? m->sort_every : (sparse ? 4u : 1u);
     const int force = force_sort || every <= 1 || m->tile_tab != nullptr;
