@@ -618,7 +618,7 @@ def e2e_measure(eng, s, steps):
     return {"value": steps / dt, "unit": "timesteps/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": h2d + 72, "api": "azp_md_set_state / azp_md_run(1) / azp_md_get_state / azp_md_thermo",
             "steps": steps, "breakdown": breakdown,
-            "note": "set_state copies the host state (pinned) and re-sorts / rebuilds the list; rates include that"}
+            "note": "set_state reads the pinned host state in place and rebuilds the list only when a particle lies more than r_buff / 2 from its position at the last build; get_state writes the pinned outputs in place; rates include that"}
 
 
 def main():
