@@ -301,3 +301,37 @@ def test_engine_brownian_cylindrical_pore(orc, precision, tol):
     assert _unwrapped_err(sim, md, L) < tol
     f, _ = sim._engine.forces()
     assert force_error(f, F_md) < (1e-12 if precision == "fp64" else 1e-5)
+
+
+def test_driver_many_types(orc):
+    """1,500 particle types: the FP32-output kernel's per-type float records and
+    reaches (9 floats a type, 54 KB with the block's near list) take more than
+    the default 48 KB of dynamic shared memory, so the launch raises the limit
+    first; both precisions against the oracle, every type with its own
+    parameters, cutoff and extrapolation."""
+    rng = np.random.Generator(np.random.PCG64(31))
+    nt = 1500
+    N = 20000
+    L = np.array([20.0, 20.0, 20.0])
+    pot = az.wall.LJ93(walls=_walls_zoo())
+    names = [f"T{k}" for k in range(nt)]
+    for k, name in enumerate(names):
+        pot.params[name] = dict(A=float(rng.uniform(0.5, 2.0)), sigma=float(rng.uniform(0.8, 1.2)),
+                                r_cut=float(rng.uniform(1.5, 3.5)), r_extrap=float(0.5 if k % 3 else 0.0))
+    rec, rc, rx = pot._tables(names)
+    sp, cy, pl = oracle_walls(pot)
+    pos = rng.uniform(-0.5, 0.5, size=(N, 3)) * L
+    types = rng.integers(0, nt, size=N).astype(np.int32)
+    for _ in range(10):
+        F, U, W = orc.wall_forces(np.concatenate([pos, types[:, None]], axis=1), types, "LJ93", rec, rc, rx, sp, cy,
+                                  pl)
+        bad = ~(np.abs(F).max(axis=1) < 1e8) | ~(np.abs(U) < 1e8)
+        if not bad.any():
+            break
+        pos[bad] = rng.uniform(-0.5, 0.5, size=(bad.sum(), 3)) * L
+    assert not bad.any() and (np.abs(U) > 0).sum() > 1000
+    for prec, tol in (("fp64", 1e-12), ("fp32", 1e-5)):
+        f, w = _driver_forces(pot, (rec, rc, rx), pos, types, L, prec)
+        assert force_error(f, F) < tol
+        assert np.abs(f[:, 3] - U).max() <= tol * max(np.abs(U).max(), 1.0)
+        assert np.abs(w - W).max() <= tol * max(np.abs(W).max(), 1.0)
